@@ -1,0 +1,212 @@
+"""The benchmark models of this project, built with :mod:`openmc_gb300.model`.
+
+* ``point_cube``     20 cm vacuum cube, two concentric z-cylinders (r=1, 3 cm)
+                     of one 4-nuclide mixture (A = 1, 12, 16, 56), 1 MeV
+                     isotropic point source, flux on a 10x10x10 mesh x 50
+                     log-energy bins.
+* ``lattice17``      17x17 pin lattice (pitch 1.26 cm, pin r=0.41, clad
+                     r=0.475, 200 cm tall), reflective radial and vacuum axial
+                     boundaries, 3 materials from 12 nuclides, Maxwellian
+                     (1.3 MeV) source uniform in the pins, flux on a
+                     17x17x50 mesh x 100 log-energy bins.
+* ``shield``         200x50x50 cm stack of alternating 10 cm light/heavy
+                     layers, 1 MeV monodirectional plane source at x=0,
+                     flux on a 200x10x10 mesh.
+
+Every builder writes the nuclide library it needs (seeded, deterministic) and
+returns ``(model, directory)``; ``model.export_to_model_xml`` then produces the
+``model.xml`` the C library reads.
+"""
+from __future__ import annotations
+
+from pathlib import Path
+
+import numpy as np
+
+from . import data
+from . import model as om
+
+# 24 guide tubes + 1 instrument tube of a 17x17 PWR assembly (row, col).
+GUIDE_TUBES = [(2, 5), (2, 8), (2, 11), (3, 3), (3, 13), (5, 2), (5, 5),
+               (5, 8), (5, 11), (5, 14), (8, 2), (8, 5), (8, 8), (8, 11),
+               (8, 14), (11, 2), (11, 5), (11, 8), (11, 11), (11, 14),
+               (13, 3), (13, 13), (14, 5), (14, 8), (14, 11)]
+
+
+def _library(directory, specs, n_points, seed):
+    nucs = []
+    for k, (name, A) in enumerate(specs):
+        nucs.append(data.make_nuclide(name, A, n_points, seed * 1000 + k))
+    xml = data.write_library(nucs, directory)
+    return nucs, xml
+
+
+def log_energy_bins(n, e_min=data.E_MIN, e_max=data.E_MAX):
+    return np.exp(np.linspace(np.log(e_min), np.log(e_max), n + 1))
+
+
+def point_cube(directory, particles=100_000, batches=10, n_points=2000,
+               seed=1, event_based=True, mesh_dim=(10, 10, 10), n_ebins=50):
+    om.reset_auto_ids()
+    directory = Path(directory)
+    rng = np.random.default_rng(seed)
+    specs = [("H1", 1), ("C12", 12), ("O16", 16), ("Fe56", 56)]
+    _, xs_xml = _library(directory, specs, n_points, seed)
+    frac = rng.uniform(0.2, 1.0, 4)
+    frac[0] *= 3.0
+    mat = om.Material(name="mixture")
+    for (name, _), f in zip(specs, frac / frac.sum()):
+        mat.add_nuclide(name, float(f))
+    mat.set_density("atom/b-cm", 0.08)
+    mats = om.Materials([mat], cross_sections=xs_xml.name)
+
+    planes = [om.XPlane(-10.0, boundary_type="vacuum"), om.XPlane(10.0, boundary_type="vacuum"),
+              om.YPlane(-10.0, boundary_type="vacuum"), om.YPlane(10.0, boundary_type="vacuum"),
+              om.ZPlane(-10.0, boundary_type="vacuum"), om.ZPlane(10.0, boundary_type="vacuum")]
+    box = +planes[0] & -planes[1] & +planes[2] & -planes[3] & +planes[4] & -planes[5]
+    c1, c2 = om.ZCylinder(r=1.0), om.ZCylinder(r=3.0)
+    cells = [om.Cell(fill=mat, region=-c1 & +planes[4] & -planes[5]),
+             om.Cell(fill=mat, region=+c1 & -c2 & +planes[4] & -planes[5]),
+             om.Cell(fill=mat, region=+c2 & box)]
+    geom = om.Geometry(om.Universe(cells=cells))
+
+    settings = om.Settings(particles=particles, batches=batches,
+                           event_based=event_based, seed=1)
+    settings.source = [om.IndependentSource(space=om.Point((0.0, 0.0, 0.0)),
+                                            angle=om.Isotropic(),
+                                            energy=om.Discrete([1.0e6], [1.0]))]
+    mesh = om.RegularMesh()
+    mesh.dimension = list(mesh_dim)
+    mesh.lower_left = [-10.0, -10.0, -10.0]
+    mesh.upper_right = [10.0, 10.0, 10.0]
+    t = om.Tally(name="mesh flux")
+    t.filters = [om.MeshFilter(mesh), om.EnergyFilter(log_energy_bins(n_ebins))]
+    t.scores = ["flux"]
+    return om.Model(geom, mats, settings, om.Tallies([t])), directory
+
+
+def _pin_universe(fuel, clad, mod, r_pin=0.41, r_clad=0.475, guide=False):
+    s1, s2 = om.ZCylinder(r=r_pin), om.ZCylinder(r=r_clad)
+    inner = mod if guide else fuel
+    return om.Universe(cells=[om.Cell(fill=inner, region=-s1),
+                              om.Cell(fill=clad, region=+s1 & -s2),
+                              om.Cell(fill=mod, region=+s2)])
+
+
+def _lattice_materials(directory, n_points, seed):
+    specs = [("Hv235", 235), ("Hv238", 238), ("Ox16", 16), ("Hv240", 240),
+             ("Cl56", 56), ("Cl58", 58), ("Cl90", 90), ("Cl91", 91),
+             ("Lt1", 1), ("Lt2", 2), ("Lt16", 16), ("Lt10", 10)]
+    _, xs_xml = _library(directory, specs, n_points, seed)
+    rng = np.random.default_rng(seed + 17)
+
+    def mixture(name, names, weights, density):
+        m = om.Material(name=name)
+        w = np.asarray(weights) * rng.uniform(0.9, 1.1, len(weights))
+        for n, f in zip(names, w / w.sum()):
+            m.add_nuclide(n, float(f))
+        m.set_density("atom/b-cm", density)
+        return m
+
+    fuel = mixture("heavy absorber", ["Hv235", "Hv238", "Ox16", "Hv240"],
+                   [0.03, 0.30, 0.66, 0.01], 0.069)
+    clad = mixture("clad", ["Cl56", "Cl58", "Cl90", "Cl91"],
+                   [0.6, 0.2, 0.15, 0.05], 0.043)
+    mod = mixture("light scatterer", ["Lt1", "Lt2", "Lt16", "Lt10"],
+                  [0.66, 0.001, 0.33, 0.009], 0.1)
+    return fuel, clad, mod, xs_xml
+
+
+def lattice17(directory, particles=10_000_000, batches=20, n_points=11303,
+              seed=3, event_based=True, mesh_dim=(17, 17, 50), n_ebins=100,
+              height=200.0):
+    om.reset_auto_ids()
+    directory = Path(directory)
+    fuel, clad, mod, xs_xml = _lattice_materials(directory, n_points, seed)
+    mats = om.Materials([fuel, clad, mod], cross_sections=xs_xml.name)
+    pin = _pin_universe(fuel, clad, mod)
+    gt = _pin_universe(fuel, clad, mod, r_pin=0.56, r_clad=0.60, guide=True)
+    pitch, n = 1.26, 17
+    half = pitch * n / 2.0
+    lat = om.RectLattice()
+    lat.pitch = [pitch, pitch]
+    lat.lower_left = [-half, -half]
+    rows = [[pin] * n for _ in range(n)]
+    for (i, j) in GUIDE_TUBES:
+        rows[i][j] = gt
+    lat.universes = rows
+    xs = [om.XPlane(-half, boundary_type="reflective"), om.XPlane(half, boundary_type="reflective"),
+          om.YPlane(-half, boundary_type="reflective"), om.YPlane(half, boundary_type="reflective"),
+          om.ZPlane(-height / 2, boundary_type="vacuum"), om.ZPlane(height / 2, boundary_type="vacuum")]
+    region = +xs[0] & -xs[1] & +xs[2] & -xs[3] & +xs[4] & -xs[5]
+    root = om.Universe(cells=[om.Cell(fill=lat, region=region)])
+    geom = om.Geometry(root)
+    settings = om.Settings(particles=particles, batches=batches,
+                           event_based=event_based, seed=1)
+    settings.source = [om.IndependentSource(
+        space=om.Box((-half, -half, -height / 2), (half, half, height / 2)),
+        angle=om.Isotropic(), energy=om.Maxwell(1.3e6),
+        constraints={"domains": [fuel]})]
+    mesh = om.RegularMesh()
+    mesh.dimension = list(mesh_dim)
+    mesh.lower_left = [-half, -half, -height / 2]
+    mesh.upper_right = [half, half, height / 2]
+    t = om.Tally(name="lattice flux")
+    t.filters = [om.MeshFilter(mesh), om.EnergyFilter(log_energy_bins(n_ebins))]
+    return om.Model(geom, mats, settings, om.Tallies([t])), directory
+
+
+def shield_materials(directory, n_points, seed):
+    specs = [("Lt1", 1), ("Lt16", 16), ("Lt10", 10), ("Lt2", 2),
+             ("Cl56", 56), ("Cl58", 58), ("Cl54", 54), ("Cl52", 52)]
+    _, xs_xml = _library(directory, specs, n_points, seed)
+    light = om.Material(name="light scatterer")
+    for n, f in zip(["Lt1", "Lt16", "Lt10", "Lt2"], [0.66, 0.32, 0.019, 0.001]):
+        light.add_nuclide(n, f)
+    light.set_density("atom/b-cm", 0.1)
+    heavy = om.Material(name="heavy absorber")
+    for n, f in zip(["Cl56", "Cl58", "Cl54", "Cl52"], [0.72, 0.18, 0.06, 0.04]):
+        heavy.add_nuclide(n, f)
+    heavy.set_density("atom/b-cm", 0.085)
+    return light, heavy, xs_xml
+
+
+def shield(directory, particles=1_000_000, batches=10, n_points=11303, seed=4,
+           event_based=True, length=200.0, width=50.0, layer=10.0,
+           mesh_dim=(200, 10, 10), weight_windows=None, back_face=10.0):
+    om.reset_auto_ids()
+    directory = Path(directory)
+    light, heavy, xs_xml = shield_materials(directory, n_points, seed)
+    mats = om.Materials([light, heavy], cross_sections=xs_xml.name)
+    n_layers = int(round(length / layer))
+    xp = [om.XPlane(k * layer) for k in range(n_layers + 1)]
+    xp[0].boundary_type = "vacuum"
+    xp[-1].boundary_type = "vacuum"
+    hw = width / 2.0
+    side = (+om.YPlane(-hw, boundary_type="vacuum") & -om.YPlane(hw, boundary_type="vacuum")
+            & +om.ZPlane(-hw, boundary_type="vacuum") & -om.ZPlane(hw, boundary_type="vacuum"))
+    cells = [om.Cell(fill=(light if k % 2 == 0 else heavy), region=+xp[k] & -xp[k + 1] & side)
+             for k in range(n_layers)]
+    geom = om.Geometry(om.Universe(cells=cells))
+    settings = om.Settings(particles=particles, batches=batches,
+                           event_based=event_based, seed=1)
+    settings.source = [om.IndependentSource(
+        space=om.Box((1.0e-6, -hw, -hw), (1.0e-6, hw, hw)),
+        angle=om.Monodirectional((1.0, 0.0, 0.0)),
+        energy=om.Discrete([1.0e6], [1.0]))]
+    mesh = om.RegularMesh()
+    mesh.dimension = list(mesh_dim)
+    mesh.lower_left = [0.0, -hw, -hw]
+    mesh.upper_right = [length, hw, hw]
+    t = om.Tally(name="shield flux")
+    t.filters = [om.MeshFilter(mesh)]
+    back = om.RegularMesh()
+    back.dimension = [1, 1, 1]
+    back.lower_left = [length - back_face, -hw, -hw]
+    back.upper_right = [length, hw, hw]
+    tb = om.Tally(name="back face flux")
+    tb.filters = [om.MeshFilter(back)]
+    if weight_windows is not None:
+        settings.weight_windows = [weight_windows]
+        settings.weight_windows_on = True
+    return om.Model(geom, mats, settings, om.Tallies([t, tb])), directory

@@ -1,0 +1,284 @@
+"""Seeded synthetic continuous-energy nuclear data and its on-disk format.
+
+OpenMC reads incident-neutron data from HDF5 files listed in a
+``cross_sections.xml`` library (``openmc/data/library.py:101``,
+``src/cross_sections.cpp:183-343``).  Each nuclide holds one energy grid per
+temperature, the atomic weight ratio, ``kTs`` and one group per reaction with
+its ``threshold_idx`` and ``xs`` values (``docs/source/io_formats/
+nuclear_data.rst:16-64``).  Neither libhdf5 nor h5py exists on the machines
+this package runs on, so the same content is stored in a small native binary
+container with the same fields:
+
+====================  ==========================================
+field                 meaning
+====================  ==========================================
+magic ``OMCGBNUC``    8 bytes
+version               uint32 (=1)
+name                  uint32 length + UTF-8 bytes
+A, awr, kT            3 x float64 (kT in eV, one temperature)
+n_points              uint32
+n_reactions           uint32
+energy                float64[n_points] (eV, ascending)
+per reaction          uint32 MT, uint32 threshold_idx, uint32 n,
+                      float64[n] cross section (barns)
+====================  ==========================================
+
+The generator follows the recipe of the synthetic nuclides this project is
+benchmarked on: a log-uniform grid between 1e-5 eV and 20 MeV with a seeded
++-5 % jitter of the interior points, an elastic cross section made of a
+constant plus 20 Breit-Wigner peaks, and a capture (MT 102) cross section made
+of a 1/v term plus the same peaks scaled by a seeded branching ratio.  This
+mirrors the way ``tests/unit_tests/test_temp_interp.py:12-140`` of the
+reference builds a fake nuclide (MT 2 + MT 102 on one grid).
+"""
+from __future__ import annotations
+
+import struct
+from dataclasses import dataclass, field
+from pathlib import Path
+from xml.etree import ElementTree as ET
+
+import numpy as np
+
+MAGIC = b"OMCGBNUC"
+VERSION = 1
+K_BOLTZMANN = 8.617333262e-5  # eV/K, include/openmc/constants.h:100
+E_MIN = 1.0e-5
+E_MAX = 2.0e7
+MT_ELASTIC = 2
+MT_CAPTURE = 102
+
+
+@dataclass
+class Nuclide:
+    """One synthetic nuclide at one temperature (MT 2 and MT 102 only)."""
+    name: str
+    A: float
+    awr: float
+    kT: float
+    energy: np.ndarray
+    reactions: dict = field(default_factory=dict)  # mt -> (threshold_idx, xs)
+
+    @property
+    def elastic(self) -> np.ndarray:
+        return self.reactions[MT_ELASTIC][1]
+
+    @property
+    def capture(self) -> np.ndarray:
+        return self.reactions[MT_CAPTURE][1]
+
+
+def awr_of(A: float) -> float:
+    """Atomic weight ratio of a synthetic nuclide of mass number A.
+
+    Uses the A=1 value of hydrogen (0.999167) scaled linearly, so that the
+    A=1 nuclide has awr <= 1 and is always treated with the free-gas model
+    (``src/physics.cpp:857``).
+    """
+    return 0.99916733 * A
+
+
+def log_grid(n_points: int, rng: np.random.Generator,
+             e_min: float = E_MIN, e_max: float = E_MAX,
+             jitter: float = 0.05) -> np.ndarray:
+    """Log-uniform grid with seeded +-jitter on interior points, endpoints fixed."""
+    e = np.exp(np.linspace(np.log(e_min), np.log(e_max), n_points))
+    interior = e[1:-1] * (1.0 + jitter * (2.0 * rng.random(n_points - 2) - 1.0))
+    interior = np.clip(interior, e_min * (1 + 1e-12), e_max * (1 - 1e-12))
+    e[1:-1] = np.sort(interior)
+    return e
+
+
+# Base values (barns) by class of nuclide: (potential scattering, thermal
+# capture at 0.0253 eV, peak height scale, branching range).
+_CLASSES = {
+    "light": (20.0, 0.33, 30.0, (0.01, 0.05)),
+    "moderator": (4.5, 0.003, 20.0, (0.01, 0.05)),
+    "structural": (11.0, 2.5, 400.0, (0.05, 0.5)),
+    "absorber": (10.0, 30.0, 3000.0, (0.3, 0.95)),
+}
+
+
+def nuclide_class(A: float) -> str:
+    if A <= 2:
+        return "light"
+    if A <= 20:
+        return "moderator"
+    if A <= 100:
+        return "structural"
+    return "absorber"
+
+
+def make_nuclide(name: str, A: float, n_points: int, seed: int,
+                 kind: str | None = None, n_peaks: int = 20,
+                 temperature: float = 294.0) -> Nuclide:
+    """Build one synthetic nuclide from a seed (deterministic)."""
+    rng = np.random.default_rng(seed)
+    kind = kind or nuclide_class(A)
+    pot, cap_th, height, (b_lo, b_hi) = _CLASSES[kind]
+    E = log_grid(n_points, rng)
+    # Breit-Wigner peaks in the resolved range, seeded.
+    E0 = np.exp(rng.uniform(np.log(1.0), np.log(1.0e5), n_peaks))
+    gamma = E0 * 10.0 ** rng.uniform(-3.0, -1.0, n_peaks)
+    h = height * 10.0 ** rng.uniform(-1.0, 0.0, n_peaks)
+    branch = rng.uniform(b_lo, b_hi, n_peaks)
+    half = 0.5 * gamma
+    shape = (half[None, :] ** 2) / ((E[:, None] - E0[None, :]) ** 2 + half[None, :] ** 2)
+    peaks_el = shape @ h
+    peaks_cap = shape @ (h * branch)
+    elastic = pot * (1.0 + 0.02 * rng.standard_normal()) + peaks_el
+    capture = cap_th * np.sqrt(0.0253 / E) + peaks_cap
+    nuc = Nuclide(name=name, A=float(A), awr=awr_of(A),
+                  kT=K_BOLTZMANN * temperature, energy=E)
+    nuc.reactions[MT_ELASTIC] = (0, np.ascontiguousarray(elastic, dtype=np.float64))
+    nuc.reactions[MT_CAPTURE] = (0, np.ascontiguousarray(capture, dtype=np.float64))
+    return nuc
+
+
+def write_nuclide(nuc: Nuclide, path: str | Path) -> None:
+    path = Path(path)
+    name = nuc.name.encode()
+    with open(path, "wb") as f:
+        f.write(MAGIC)
+        f.write(struct.pack("<I", VERSION))
+        f.write(struct.pack("<I", len(name)))
+        f.write(name)
+        f.write(struct.pack("<3d", nuc.A, nuc.awr, nuc.kT))
+        f.write(struct.pack("<II", len(nuc.energy), len(nuc.reactions)))
+        f.write(np.ascontiguousarray(nuc.energy, dtype="<f8").tobytes())
+        for mt in sorted(nuc.reactions):
+            thr, xs = nuc.reactions[mt]
+            f.write(struct.pack("<III", mt, thr, len(xs)))
+            f.write(np.ascontiguousarray(xs, dtype="<f8").tobytes())
+
+
+def read_nuclide(path: str | Path) -> Nuclide:
+    buf = Path(path).read_bytes()
+    if buf[:8] != MAGIC:
+        raise ValueError(f"{path}: not a nuclide file")
+    off = 8
+    (version,) = struct.unpack_from("<I", buf, off); off += 4
+    if version != VERSION:
+        raise ValueError(f"{path}: unsupported version {version}")
+    (nlen,) = struct.unpack_from("<I", buf, off); off += 4
+    name = buf[off:off + nlen].decode(); off += nlen
+    A, awr, kT = struct.unpack_from("<3d", buf, off); off += 24
+    n, nrx = struct.unpack_from("<II", buf, off); off += 8
+    energy = np.frombuffer(buf, "<f8", n, off).copy(); off += 8 * n
+    nuc = Nuclide(name=name, A=A, awr=awr, kT=kT, energy=energy)
+    for _ in range(nrx):
+        mt, thr, m = struct.unpack_from("<III", buf, off); off += 12
+        xs = np.frombuffer(buf, "<f8", m, off).copy(); off += 8 * m
+        nuc.reactions[mt] = (thr, xs)
+    return nuc
+
+
+def write_library(nuclides, directory: str | Path) -> Path:
+    """Write nuclide files plus a ``cross_sections.xml`` (OpenMC schema)."""
+    directory = Path(directory)
+    directory.mkdir(parents=True, exist_ok=True)
+    root = ET.Element("cross_sections")
+    for nuc in nuclides:
+        fname = f"{nuc.name}.nuc"
+        write_nuclide(nuc, directory / fname)
+        ET.SubElement(root, "library", materials=nuc.name, path=fname,
+                      type="neutron")
+    ET.indent(root)
+    out = directory / "cross_sections.xml"
+    ET.ElementTree(root).write(out, xml_declaration=True, encoding="utf-8")
+    return out
+
+
+def read_library(xml_path: str | Path) -> dict:
+    """Map nuclide name -> file path from a cross_sections.xml."""
+    xml_path = Path(xml_path)
+    root = ET.parse(xml_path).getroot()
+    out = {}
+    for lib in root.iter("library"):
+        if lib.get("type", "neutron") != "neutron":
+            continue
+        p = Path(lib.get("path"))
+        if not p.is_absolute():
+            p = xml_path.parent / p
+        for m in lib.get("materials").split():
+            out[m] = p
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Macroscopic cross-section lookup microbenchmark data (XSBench-shaped)
+# ---------------------------------------------------------------------------
+
+@dataclass
+class XSBenchData:
+    """Flat tables for the lookup microbenchmark.
+
+    energy:   float64 [n_nuc, G]
+    xs:       float64 [n_nuc, G, 5] channels (total, elastic, absorption,
+              aux1, aux2)
+    mat_nuc:  int32 concatenated nuclide indices per material
+    mat_off:  int32 [n_mat+1] offsets into mat_nuc
+    mat_dens: float64 atom densities aligned with mat_nuc
+    mat_prob: float64 [n_mat] material sampling probabilities
+    """
+    energy: np.ndarray
+    xs: np.ndarray
+    mat_nuc: np.ndarray
+    mat_off: np.ndarray
+    mat_dens: np.ndarray
+    mat_prob: np.ndarray
+
+
+XSBENCH_MAT_COUNTS = (321, 5, 4, 4, 27, 21, 21, 21, 21, 21, 9, 9)
+# Probabilities with which the 12 materials are drawn before seeding noise
+# (fuel-dominated, as in a light-water reactor lookup mix).
+_XSBENCH_MAT_WEIGHTS = (0.140, 0.052, 0.275, 0.134, 0.154, 0.064, 0.066,
+                        0.055, 0.008, 0.015, 0.025, 0.013)
+
+
+def make_xsbench(n_nuc: int = 68, n_points: int = 11303, seed: int = 42,
+                 mat_counts=XSBENCH_MAT_COUNTS) -> XSBenchData:
+    """68 nuclides x 11,303 points x 5 channels, 12 materials, all seeded.
+
+    Material 0 has 321 entries drawn with replacement from the 68 nuclides
+    (the standalone microbenchmark sums duplicates like distinct entries).
+    """
+    rng = np.random.default_rng(seed)
+    energy = np.empty((n_nuc, n_points))
+    xs = np.empty((n_nuc, n_points, 5))
+    for i in range(n_nuc):
+        sub = np.random.default_rng(rng.integers(1 << 62))
+        A = float(sub.integers(1, 240))
+        nuc = make_nuclide(f"X{i:03d}", A, n_points, int(sub.integers(1 << 62)))
+        energy[i] = nuc.energy
+        el, cap = nuc.elastic, nuc.capture
+        aux1 = sub.uniform(0.1, 2.0) * el
+        aux2 = sub.uniform(0.0, 1.0) * cap + sub.uniform(0.0, 1.0)
+        xs[i, :, 0] = el + cap
+        xs[i, :, 1] = el
+        xs[i, :, 2] = cap
+        xs[i, :, 3] = aux1
+        xs[i, :, 4] = aux2
+    mat_nuc, mat_off, mat_dens = [], [0], []
+    for m, cnt in enumerate(mat_counts):
+        if m == 0:
+            idx = rng.integers(0, n_nuc, cnt)
+        else:
+            idx = rng.choice(n_nuc, cnt, replace=False)
+        mat_nuc.extend(int(v) for v in idx)
+        mat_dens.extend(rng.uniform(1e-5, 5e-2, cnt))
+        mat_off.append(len(mat_nuc))
+    w = np.asarray(_XSBENCH_MAT_WEIGHTS) * rng.uniform(0.9, 1.1, len(mat_counts))
+    return XSBenchData(energy=energy, xs=xs,
+                       mat_nuc=np.asarray(mat_nuc, np.int32),
+                       mat_off=np.asarray(mat_off, np.int32),
+                       mat_dens=np.asarray(mat_dens, np.float64),
+                       mat_prob=w / w.sum())
+
+
+def xsbench_lookups(data: XSBenchData, n: int, seed: int = 7):
+    """Seeded (material, energy) pairs; energies log-uniform over the grid range."""
+    rng = np.random.default_rng(seed)
+    mats = rng.choice(len(data.mat_prob), size=n, p=data.mat_prob).astype(np.int32)
+    e = np.exp(rng.uniform(np.log(E_MIN), np.log(E_MAX), n))
+    return mats, e

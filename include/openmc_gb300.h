@@ -1,0 +1,133 @@
+/* C ABI of libopenmc_gb300.so — the GB300 event-based transport library.
+ *
+ * Every function below has the name, signature, argument meaning and return
+ * convention of the reference C API it replaces (file:line in the reference
+ * tree is given beside each); functions prefixed openmc_gb300_ are additions
+ * with no reference counterpart.  Return value 0 means success; a negative
+ * value is one of the exported OPENMC_E_* codes, with a message in
+ * openmc_err_msg.
+ */
+#ifndef OPENMC_GB300_H
+#define OPENMC_GB300_H
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- error codes and message: include/openmc/capi.h:279-292, src/error.cpp:20-30 */
+extern int OPENMC_E_UNASSIGNED;
+extern int OPENMC_E_ALLOCATE;
+extern int OPENMC_E_OUT_OF_BOUNDS;
+extern int OPENMC_E_INVALID_SIZE;
+extern int OPENMC_E_INVALID_ARGUMENT;
+extern int OPENMC_E_INVALID_TYPE;
+extern int OPENMC_E_INVALID_ID;
+extern int OPENMC_E_GEOMETRY;
+extern int OPENMC_E_DATA;
+extern int OPENMC_E_PHYSICS;
+extern int OPENMC_E_WARNING;
+extern char openmc_err_msg[256];
+
+/* ---- exported globals read through ctypes: include/openmc/settings.h:67-132,
+ *      include/openmc/simulation.h:26-38, openmc/lib/__init__.py:40-50 */
+extern bool event_based;
+extern int64_t n_particles;
+extern int32_t n_inactive;
+extern int32_t gen_per_batch;
+extern int32_t max_lost_particles;
+extern double rel_max_lost_particles;
+extern bool run_CE;
+extern int verbosity;
+extern bool weight_windows_on;
+extern bool restart_run;
+extern int current_batch;
+extern bool initialized;
+extern int n_lost_particles;
+extern int n_coord_levels;
+extern bool DAGMC_ENABLED;
+extern bool LIBMESH_ENABLED;
+extern bool UWUW_ENABLED;
+
+/* ---- lifecycle: include/openmc/capi.h:62-149, src/simulation.cpp:53-280 */
+int openmc_init(int argc, char* argv[], const void* intracomm); /* capi.h:83 */
+int openmc_run(void);                                           /* capi.h:142 */
+int openmc_simulation_init(void);                               /* capi.h:149 */
+int openmc_next_batch(int* status);                             /* capi.h:123 */
+int openmc_simulation_finalize(void);                           /* capi.h:148 */
+int openmc_finalize(void);                                      /* capi.h:62 */
+int openmc_reset(void);                                         /* capi.h:140 */
+int openmc_hard_reset(void);                                    /* capi.h:82 */
+int openmc_reset_timers(void);                                  /* capi.h:141 */
+
+/* ---- seeds: include/openmc/capi.h:77-78,144-145, src/random_lcg.cpp:126-144 */
+int64_t openmc_get_seed(void);
+void openmc_set_seed(int64_t new_seed);
+uint64_t openmc_get_stride(void);
+void openmc_set_stride(uint64_t new_stride);
+
+/* ---- tallies: include/openmc/capi.h:79,81,168-174, src/tallies/tally.cpp:1554-1575.
+ * openmc_tally_results returns a borrowed pointer to [bins][scores][3]
+ * (VALUE, SUM, SUM_SQ) that stays valid until the next library call. */
+int openmc_tally_results(int32_t index, double** ptr, size_t shape_[3]);
+int openmc_get_tally_index(int32_t id, int32_t* index);
+int openmc_tally_get_id(int32_t index, int32_t* id);
+int openmc_tally_get_n_realizations(int32_t index, int32_t* n);
+int openmc_global_tallies(double** ptr);
+size_t tallies_size(void); /* src/tallies/tally.cpp:1584 */
+
+/* ---- weight windows: include/openmc/capi.h:184-221, src/weight_windows.cpp:1020-1340 */
+size_t openmc_weight_windows_size(void);
+int openmc_get_weight_windows_index(int32_t id, int32_t* idx);
+int openmc_weight_windows_get_id(int32_t index, int32_t* id);
+int openmc_weight_windows_get_bounds(int32_t index, const double** lower_bounds,
+  const double** upper_bounds, size_t* size);
+int openmc_weight_windows_set_bounds(int32_t index, const double* lower_bounds,
+  const double* upper_bounds, size_t size);
+int openmc_weight_windows_get_energy_bounds(int32_t index, const double** e_bounds,
+  size_t* e_bounds_size);
+int openmc_weight_windows_update_magic(int32_t ww_idx, int32_t tally_idx,
+  const char* value, double threshold, double ratio);
+int openmc_weight_windows_get_survival_ratio(int32_t index, double* ratio);
+int openmc_weight_windows_get_max_split(int32_t index, int* max_split);
+int openmc_weight_windows_get_mesh(int32_t index, int32_t* mesh_idx);
+
+/* ---- GB300 additions (no reference counterpart) ----------------------- */
+/* settings globals: FP32 tables (-1 = from <gb300_xs_precision>), particle
+ * slots in HBM (0 = setting or automatic), XS-queue sort on/off */
+extern int openmc_gb300_xs_fp32;
+extern int64_t openmc_gb300_in_flight;
+extern int openmc_gb300_sort;
+
+/* last batch: [ms, iterations, events, total_weight, leakage, lost, done, secondaries] */
+int openmc_gb300_last_batch(double* out);
+/* [time_active s, time_inactive s, wall_active s, particles/s (active), in-flight slots] */
+int openmc_gb300_timing(double* out);
+/* per-event traces for particle ids 1..n_hist, cap records each (48-byte records) */
+int openmc_gb300_set_trace(int64_t n_hist, int cap);
+int openmc_gb300_get_trace(void* records, int32_t* counts);
+int openmc_gb300_set_weight_windows_on(int on);
+/* [n_nuclides, n_materials, n_cells, n_surfaces, n_tallies, log_grid_bins, batches, coord_levels] */
+int openmc_gb300_model_info(int64_t* out);
+
+/* macroscopic-XS lookup on flat 5-channel tables; counterpart of
+ * Material::calculate_neutron_xs (src/material.cpp:829-901) per lookup */
+int openmc_gb300_xs_tables_create(int n_nuc, int G, const double* energy, const double* xs,
+  int n_mat, const int32_t* mat_off, const int32_t* mat_nuc, const double* mat_dens,
+  int n_log_bins, int fp32, int64_t max_lookups, void** handle);
+int openmc_gb300_xs_tables_free(void* handle);
+int openmc_gb300_xs_lookup(void* handle, int64_t n, const int32_t* mat, const double* E,
+  double* out, int32_t* grid_hash, int sort);
+int openmc_gb300_xs_lookup_device(void* handle, int64_t n, const int32_t* d_mat,
+  const double* d_E, double* d_out, int32_t* d_grid_hash, int sort);
+int openmc_gb300_xs_last_times(void* handle, float* ms);
+int openmc_gb300_xs_stream(void* handle, void** stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OPENMC_GB300_H */

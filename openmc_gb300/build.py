@@ -1,0 +1,65 @@
+"""Build the GB300 transport library in-tree (nvcc, sm_103a).
+
+Produces ``openmc_gb300/_lib/libopenmc_gb300.so`` from the sources in
+``openmc_gb300/csrc``.  Translation units compile in parallel; device code is
+built for ``sm_103a`` only with ``-fmad=false`` so that every floating-point
+multiply and add rounds separately, as in the reference's C++ expressions.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+OUT = PKG / "_lib"
+LIB = OUT / "libopenmc_gb300.so"
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-fmad=false"]
+SOURCES = ["host_model.cpp", "capi.cpp", "transport.cu", "xsbench.cu", "mlp.cu"]
+
+
+def nvcc():
+    exe = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(exe).exists():
+        raise RuntimeError("nvcc not found")
+    return exe
+
+
+def _compile(src: Path, obj: Path, extra):
+    cmd = [nvcc(), *ARCH, *COMMON, *extra, "-c", str(src), "-o", str(obj)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return r.stderr
+
+
+def build(force: bool = False, verbose: bool = False, extra=()) -> Path:
+    srcs = [CSRC / s for s in SOURCES if (CSRC / s).exists()]
+    headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh"))
+    newest = max(p.stat().st_mtime for p in srcs + headers)
+    if LIB.exists() and not force and LIB.stat().st_mtime >= newest:
+        return LIB
+    OUT.mkdir(parents=True, exist_ok=True)
+    objs = [OUT / (s.stem + ".o") for s in srcs]
+    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+        futs = [ex.submit(_compile, s, o, list(extra)) for s, o in zip(srcs, objs)]
+        for f in futs:
+            msg = f.result()
+            if verbose and msg:
+                print(msg)
+    cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    for o in objs:
+        o.unlink(missing_ok=True)
+    return LIB
+
+
+if __name__ == "__main__":
+    import sys
+    print(build(force="--force" in sys.argv, verbose=True))

@@ -1,0 +1,736 @@
+// C API of the GB300 transport library: the subset of OpenMC's
+// include/openmc/capi.h that drives a fixed-source event-based run, with the
+// same names, argument meanings, return codes and exported globals, so that
+// openmc.lib-style ctypes bindings work unchanged.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "host_model.h"
+#include "transport.h"
+
+// ------------------------------------------------ exported error globals
+// src/error.cpp:20-30, include/openmc/capi.h:279-292
+extern "C" {
+int OPENMC_E_UNASSIGNED = -1;
+int OPENMC_E_ALLOCATE = -2;
+int OPENMC_E_OUT_OF_BOUNDS = -3;
+int OPENMC_E_INVALID_SIZE = -4;
+int OPENMC_E_INVALID_ARGUMENT = -5;
+int OPENMC_E_INVALID_TYPE = -6;
+int OPENMC_E_INVALID_ID = -7;
+int OPENMC_E_GEOMETRY = -8;
+int OPENMC_E_DATA = -9;
+int OPENMC_E_PHYSICS = -10;
+int OPENMC_E_WARNING = 1;
+char openmc_err_msg[256] = {0};
+
+// exported settings / simulation globals read through ctypes in_dll
+// (include/openmc/settings.h:67-132, include/openmc/simulation.h:26-38)
+bool event_based = false;
+int64_t n_particles = 0;
+int32_t n_inactive = 0;
+int32_t gen_per_batch = 1;
+int32_t max_lost_particles = 10;
+double rel_max_lost_particles = 1.0e-6;
+bool run_CE = true;
+int verbosity = 7;
+bool weight_windows_on = false;
+bool restart_run = false;
+bool cmfd_run = false;
+bool entropy_on = false;
+bool output_summary = false;
+bool photon_transport = false;
+bool reduce_tallies = true;
+bool trigger_on = false;
+bool need_depletion_rx = false;
+int run_mode = 1;  // fixed source
+const char* path_statepoint_c = "";
+int current_batch = 0;
+int current_gen = 0;
+bool initialized = false;
+int n_lost_particles = 0;
+double keff = 1.0;
+double keff_std = 0.0;
+int n_coord_levels = 0;
+bool DAGMC_ENABLED = false;
+bool LIBMESH_ENABLED = false;
+bool UWUW_ENABLED = false;
+// GB300 extensions (no counterpart in the reference)
+int openmc_gb300_xs_fp32 = -1;          // -1: from XML (<gb300_xs_precision>), else 0/1
+int64_t openmc_gb300_in_flight = 0;     // particle slots; 0: setting or automatic
+int openmc_gb300_sort = 1;              // sort the XS queue by (material, energy)
+}
+
+namespace {
+
+using namespace omc;
+
+struct State {
+  bool model_loaded = false;
+  HModel model;
+  GpuSim* gpu = nullptr;
+  int64_t seed = 1;
+  uint64_t stride = 152917ULL;
+  std::vector<double> global_tallies;  // [4][3] K_COL, K_ABS, K_TRACK, LEAKAGE x (VAL, SUM, SUM_SQ)
+  double time_active = 0.0;            // seconds of active-batch transport (device events)
+  double time_inactive = 0.0;
+  double time_wall_active = 0.0;
+  int n_batches_run = 0;
+  BatchStats last;
+  long long trace_hist = 0;
+  int trace_cap = 0;
+  bool ww_user_set = false;
+};
+
+State& S()
+{
+  static State s;
+  return s;
+}
+
+void set_errmsg(const std::string& m)
+{
+  std::snprintf(openmc_err_msg, sizeof(openmc_err_msg), "%s", m.c_str());
+}
+
+int fail(int code, const std::string& m)
+{
+  set_errmsg(m);
+  return code;
+}
+
+void sync_globals_from_model()
+{
+  HModel& m = S().model;
+  n_particles = m.n_particles;
+  n_inactive = m.n_inactive;
+  weight_windows_on = m.ww_on;
+  n_coord_levels = m.n_coord_levels;
+  max_lost_particles = m.max_lost_particles;
+  rel_max_lost_particles = m.rel_max_lost_particles;
+  event_based = m.event_based;
+}
+
+// WeightWindowsGenerator construction + create_tally
+// (src/weight_windows.cpp:834-962): a WeightWindows object with invalid
+// bounds and a flux tally over [mesh, energy, particle].
+void setup_generators(HModel& m)
+{
+  for (auto& g : m.ww_generators) {
+    if (g.ww >= 0) continue;
+    HWeightWindows w;
+    w.id = static_cast<int>(m.weight_windows.size()) + 1;
+    w.mesh = g.mesh;
+    w.ebounds = g.ebounds.empty() ? std::vector<double> {m.energy_min, m.energy_max} : g.ebounds;
+    size_t n = (w.ebounds.size() - 1) * static_cast<size_t>(m.meshes[g.mesh].n_bins());
+    w.lower.assign(n, -1.0);
+    w.upper.assign(n, -1.0);
+    g.ww = static_cast<int>(m.weight_windows.size());
+    m.weight_windows.push_back(std::move(w));
+    int fid = 1;
+    for (const auto& f : m.filters) fid = std::max(fid, f.id + 1);
+    int mesh_filter = -1;
+    for (size_t k = 0; k < m.filters.size(); ++k)
+      if (m.filters[k].type == FILTER_MESH && m.filters[k].mesh == g.mesh) mesh_filter = static_cast<int>(k);
+    if (mesh_filter < 0) {
+      HFilter f;
+      f.id = fid++;
+      f.type = FILTER_MESH;
+      f.mesh = g.mesh;
+      f.nbins = static_cast<int>(m.meshes[g.mesh].n_bins());
+      mesh_filter = static_cast<int>(m.filters.size());
+      m.filters.push_back(f);
+    }
+    HFilter fe;
+    fe.id = fid++;
+    fe.type = FILTER_ENERGY;
+    fe.mesh = -1;
+    fe.bins = m.weight_windows[g.ww].ebounds;
+    fe.nbins = static_cast<int>(fe.bins.size()) - 1;
+    m.filters.push_back(fe);
+    HFilter fp;
+    fp.id = fid++;
+    fp.type = FILTER_PARTICLE;
+    fp.mesh = -1;
+    fp.nbins = 1;
+    m.filters.push_back(fp);
+    HTally t;
+    int tid = 1;
+    for (const auto& tt : m.tallies) tid = std::max(tid, tt.id + 1);
+    t.id = tid;
+    t.filters = {mesh_filter, static_cast<int>(m.filters.size()) - 2, static_cast<int>(m.filters.size()) - 1};
+    t.scores = {SCORE_FLUX};
+    t.generated = true;
+    t.strides.assign(3, 1);
+    int64_t stride = 1;
+    for (int i = 2; i >= 0; --i) {
+      t.strides[i] = static_cast<int>(stride);
+      stride *= m.filters[t.filters[i]].nbins;
+    }
+    t.n_filter_bins = stride;
+    t.results.assign(static_cast<size_t>(stride) * 3, 0.0);
+    g.tally = static_cast<int>(m.tallies.size());
+    m.tallies.push_back(std::move(t));
+    if (g.on_the_fly) m.ww_on = true;
+  }
+}
+
+// WeightWindows::update_weights (MAGIC), src/weight_windows.cpp:502-755
+int update_magic(HModel& m, int ww_idx, int tally_idx, const std::string& value, double threshold, double ratio)
+{
+  if (ww_idx < 0 || ww_idx >= static_cast<int>(m.weight_windows.size()))
+    return fail(OPENMC_E_OUT_OF_BOUNDS, "Index in weight windows array is out of bounds.");
+  if (tally_idx < 0 || tally_idx >= static_cast<int>(m.tallies.size()))
+    return fail(OPENMC_E_OUT_OF_BOUNDS, "Index in tallies array is out of bounds.");
+  if (value != "mean" && value != "rel_err")
+    return fail(OPENMC_E_INVALID_ARGUMENT, "Invalid value '" + value + "' specified for weight window generation.");
+  HWeightWindows& w = m.weight_windows[ww_idx];
+  HTally& t = m.tallies[tally_idx];
+  int score_index = -1;
+  for (size_t k = 0; k < t.scores.size(); ++k)
+    if (t.scores[k] == SCORE_FLUX) score_index = static_cast<int>(k);
+  if (score_index < 0) return fail(OPENMC_E_INVALID_ARGUMENT, "A 'flux' score is required for weight window generation.");
+  int mesh_pos = -1, energy_pos = -1;
+  for (size_t i = 0; i < t.filters.size(); ++i) {
+    const HFilter& f = m.filters[t.filters[i]];
+    if (f.type == FILTER_MESH) {
+      if (f.mesh != w.mesh) return fail(OPENMC_E_INVALID_ARGUMENT, "tally mesh differs from the weight-window mesh");
+      mesh_pos = static_cast<int>(i);
+    } else if (f.type == FILTER_ENERGY) {
+      if (f.bins != w.ebounds) return fail(OPENMC_E_INVALID_ARGUMENT, "tally energy bins differ from the weight-window energy bounds");
+      energy_pos = static_cast<int>(i);
+    }
+  }
+  if (mesh_pos < 0) return fail(OPENMC_E_INVALID_ARGUMENT, "tally needs a mesh filter for weight window generation");
+  const int e_bins = static_cast<int>(w.ebounds.size()) - 1;
+  const int64_t mesh_bins = m.meshes[w.mesh].n_bins();
+  const int ns = static_cast<int>(t.scores.size());
+  const int n = t.n_realizations;
+  auto idx = [&](int e, int64_t mb) {
+    int64_t k = mb * t.strides[mesh_pos];
+    if (energy_pos >= 0) k += static_cast<int64_t>(e) * t.strides[energy_pos];
+    return (k * ns + score_index) * 3;
+  };
+  std::vector<double>& nb = w.lower;
+  std::vector<double>& rel = w.upper;
+  const HMesh& mesh = m.meshes[w.mesh];
+  double vol = 1.0;
+  for (int i = 0; i < mesh.ndim; ++i) vol *= mesh.width[i];
+  for (int e = 0; e < e_bins; e++) {
+    for (int64_t mb = 0; mb < mesh_bins; mb++) {
+      int64_t k = e * mesh_bins + mb;
+      double sum = t.results[idx(e, mb) + 1];
+      double sum_sq = t.results[idx(e, mb) + 2];
+      nb[k] = sum / n;
+      if (sum > 0.0) {
+        double mean_val = nb[k];
+        double variance = (sum_sq / n - mean_val * mean_val) / (n - 1);
+        rel[k] = std::sqrt(variance) / mean_val;
+      } else {
+        rel[k] = std::numeric_limits<double>::max();
+      }
+      if (value == "rel_err") nb[k] = 1.0 / rel[k];
+    }
+  }
+  for (int e = 0; e < e_bins; e++)
+    for (int64_t mb = 0; mb < mesh_bins; mb++) nb[e * mesh_bins + mb] /= vol;
+  for (int e = 0; e < e_bins; e++) {
+    double group_max = 0.0;
+    for (int64_t mb = 0; mb < mesh_bins; mb++)
+      if (nb[e * mesh_bins + mb] > group_max) group_max = nb[e * mesh_bins + mb];
+    if (group_max > 0.0) {
+      double norm_factor = 1.0 / (2.0 * group_max);
+      for (int64_t mb = 0; mb < mesh_bins; mb++) nb[e * mesh_bins + mb] *= norm_factor;
+    }
+  }
+  for (int e = 0; e < e_bins; e++) {
+    for (int64_t mb = 0; mb < mesh_bins; mb++) {
+      int64_t k = e * mesh_bins + mb;
+      double sum = t.results[idx(e, mb) + 1];
+      if (sum <= 0.0) nb[k] = -1.0;
+      else if (rel[k] > threshold) nb[k] = -1.0;
+      w.upper[k] = ratio * w.lower[k];
+    }
+  }
+  if (S().gpu && ww_idx == 0) gpu_set_ww_bounds(S().gpu, w.lower.data(), w.upper.data(), static_cast<long long>(w.lower.size()));
+  return 0;
+}
+
+int check_device_errors(const BatchStats& st)
+{
+  HModel& m = S().model;
+  n_lost_particles += st.n_lost;
+  if (st.error & ERR_SECONDARY_OVERFLOW)
+    return fail(OPENMC_E_ALLOCATE, "The secondary particle pool on the GPU is full; raise openmc_gb300_set_secondary_capacity.");
+  if (st.error & ERR_NO_NUCLIDE) return fail(OPENMC_E_PHYSICS, "Did not sample any nuclide during collision.");
+  if (st.error & ERR_REJECTION)
+    return fail(OPENMC_E_INVALID_ARGUMENT, "Too few source sites satisfied the constraints.");
+  if (st.error & ERR_ITERATIONS) return fail(OPENMC_E_UNASSIGNED, "Event loop exceeded its iteration limit.");
+  double n_sim = static_cast<double>(current_batch) * m.n_particles;
+  if (n_lost_particles > 0 && n_lost_particles >= m.max_lost_particles &&
+      n_lost_particles >= m.rel_max_lost_particles * n_sim)
+    return fail(OPENMC_E_GEOMETRY, "Maximum number of lost particles has been reached.");
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// src/initialize.cpp:45-138, 215-330 (arguments: [-e] [-n N] [-s N] [path])
+int openmc_init(int argc, char* argv[], const void* intracomm)
+{
+  (void)intracomm;
+  try {
+    State& s = S();
+    if (s.gpu) {
+      gpu_destroy(s.gpu);
+      s.gpu = nullptr;
+    }
+    s = State();
+    std::string path = ".";
+    bool cli_event = false;
+    int64_t cli_particles = -1;
+    for (int i = 1; i < argc; ++i) {
+      std::string a = argv[i] ? argv[i] : "";
+      if (a == "-e" || a == "--event") cli_event = true;
+      else if ((a == "-n" || a == "--particles") && i + 1 < argc) cli_particles = std::stoll(argv[++i]);
+      else if ((a == "-s" || a == "--threads") && i + 1 < argc) ++i;
+      else if (a == "-r" || a == "--restart") return fail(OPENMC_E_INVALID_ARGUMENT, "restart runs are not supported");
+      else if (a == "-p" || a == "--plot" || a == "-c" || a == "--volume" || a == "-t" || a == "--track")
+        return fail(OPENMC_E_INVALID_ARGUMENT, "run mode '" + a + "' is not supported");
+      else if (!a.empty() && a[0] != '-') path = a;
+    }
+    load_model(path, s.model);
+    finalize_model(s.model);
+    if (cli_particles > 0) s.model.n_particles = cli_particles;
+    if (cli_event) s.model.event_based = true;
+    setup_generators(s.model);
+    s.seed = s.model.seed;
+    s.stride = s.model.stride;
+    s.model_loaded = true;
+    s.global_tallies.assign(12, 0.0);
+    sync_globals_from_model();
+    current_batch = 0;
+    n_lost_particles = 0;
+    initialized = false;
+    return 0;
+  } catch (const std::exception& e) {
+    return fail(OPENMC_E_INVALID_ARGUMENT, e.what());
+  }
+}
+
+// src/simulation.cpp:75-166
+int openmc_simulation_init()
+{
+  State& s = S();
+  if (initialized) return 0;
+  if (!s.model_loaded) return fail(OPENMC_E_ALLOCATE, "OpenMC has not been initialized.");
+  try {
+    HModel& m = s.model;
+    // settings Python may have changed between init and simulation_init
+    m.n_particles = n_particles;
+    m.n_inactive = n_inactive;
+    m.event_based = event_based;
+    m.ww_on = weight_windows_on;
+    m.seed = s.seed;
+    m.stride = s.stride;
+    if (m.n_batches <= m.n_inactive) return fail(OPENMC_E_INVALID_ARGUMENT, "Number of active batches must be greater than zero.");
+    GpuOptions opt;
+    opt.in_flight = openmc_gb300_in_flight > 0 ? openmc_gb300_in_flight : m.max_particles_in_flight;
+    opt.xs_fp32 = openmc_gb300_xs_fp32 >= 0 ? openmc_gb300_xs_fp32 != 0 : m.xs_precision == 32;
+    opt.sort = openmc_gb300_sort != 0;
+    if (m.ww_on && m.weight_windows.empty()) return fail(OPENMC_E_INVALID_ARGUMENT, "weight windows are on but none are defined");
+    s.gpu = gpu_create(m, opt);
+    if (s.trace_hist > 0) gpu_set_trace(s.gpu, s.trace_hist, s.trace_cap);
+    gpu_reset_tallies(s.gpu, m);
+    std::fill(s.global_tallies.begin(), s.global_tallies.end(), 0.0);
+    current_batch = 0;
+    n_lost_particles = 0;
+    s.time_active = s.time_inactive = s.time_wall_active = 0.0;
+    s.n_batches_run = 0;
+    initialized = true;
+    return 0;
+  } catch (const std::exception& e) {
+    if (s.gpu) {
+      gpu_destroy(s.gpu);
+      s.gpu = nullptr;
+    }
+    return fail(OPENMC_E_ALLOCATE, e.what());
+  }
+}
+
+// src/simulation.cpp:232-280 (status 0 normal, 1 reached max batches)
+int openmc_next_batch(int* status)
+{
+  State& s = S();
+  if (!initialized) return fail(OPENMC_E_ALLOCATE, "Simulation has not been initialized yet.");
+  HModel& m = s.model;
+  if (status) *status = 0;
+  if (current_batch >= m.n_batches) {
+    if (status) *status = 1;
+    return 0;
+  }
+  try {
+    ++current_batch;
+    bool active = current_batch > m.n_inactive;
+    auto t0 = std::chrono::steady_clock::now();
+    BatchStats st = gpu_run_batch(s.gpu, m, current_batch, active);
+    auto t1 = std::chrono::steady_clock::now();
+    s.last = st;
+    s.n_batches_run++;
+    if (active) {
+      s.time_active += st.ms * 1e-3;
+      s.time_wall_active += std::chrono::duration<double>(t1 - t0).count();
+    } else {
+      s.time_inactive += st.ms * 1e-3;
+    }
+    if (int rc = check_device_errors(st)) return rc;
+    if (active) {
+      // global leakage tally normalised by total source weight (tally.cpp:1059-1100)
+      double val = st.leakage / st.total_weight;
+      s.global_tallies[9 + 1] += val;
+      s.global_tallies[9 + 2] += val * val;
+      // weight-window generators (src/weight_windows.cpp:967-994)
+      bool need = false;
+      for (const auto& g : m.ww_generators) need = need || g.tally >= 0;
+      if (need) {
+        gpu_fetch_tallies(s.gpu, m);
+        for (const auto& g : m.ww_generators) {
+          const HTally& t = m.tallies[g.tally];
+          if (g.max_realizations < t.n_realizations || t.n_realizations % g.update_interval != 0) continue;
+          if (int rc = update_magic(m, g.ww, g.tally, g.value, g.threshold, g.ratio)) return rc;
+        }
+      }
+    }
+    if (status && current_batch >= m.n_batches) *status = 1;
+    return 0;
+  } catch (const std::exception& e) {
+    return fail(OPENMC_E_UNASSIGNED, e.what());
+  }
+}
+
+int openmc_simulation_finalize()
+{
+  State& s = S();
+  if (!initialized) return 0;
+  try {
+    gpu_fetch_tallies(s.gpu, s.model);
+    gpu_destroy(s.gpu);
+    s.gpu = nullptr;
+    initialized = false;
+    return 0;
+  } catch (const std::exception& e) {
+    return fail(OPENMC_E_UNASSIGNED, e.what());
+  }
+}
+
+// src/simulation.cpp:53-73
+int openmc_run()
+{
+  if (int rc = openmc_simulation_init()) return rc;
+  int status = 0;
+  while (status == 0) {
+    if (int rc = openmc_next_batch(&status)) {
+      openmc_simulation_finalize();
+      return rc;
+    }
+  }
+  return openmc_simulation_finalize();
+}
+
+int openmc_finalize()
+{
+  State& s = S();
+  if (s.gpu) {
+    gpu_destroy(s.gpu);
+    s.gpu = nullptr;
+  }
+  s = State();
+  initialized = false;
+  current_batch = 0;
+  n_particles = 0;
+  n_lost_particles = 0;
+  event_based = false;
+  return 0;
+}
+
+int openmc_reset()
+{
+  State& s = S();
+  for (auto& t : s.model.tallies) {
+    t.n_realizations = 0;
+    std::fill(t.results.begin(), t.results.end(), 0.0);
+  }
+  if (s.gpu) gpu_reset_tallies(s.gpu, s.model);
+  std::fill(s.global_tallies.begin(), s.global_tallies.end(), 0.0);
+  s.time_active = s.time_inactive = s.time_wall_active = 0.0;
+  return 0;
+}
+
+int openmc_hard_reset()
+{
+  openmc_reset();
+  S().seed = 1;
+  return 0;
+}
+
+int openmc_reset_timers()
+{
+  State& s = S();
+  s.time_active = s.time_inactive = s.time_wall_active = 0.0;
+  return 0;
+}
+
+// src/random_lcg.cpp:126-144
+int64_t openmc_get_seed() { return S().seed; }
+void openmc_set_seed(int64_t new_seed) { S().seed = new_seed; }
+uint64_t openmc_get_stride() { return S().stride; }
+void openmc_set_stride(uint64_t new_stride) { S().stride = new_stride; }
+
+// src/tallies/tally.cpp:1554-1575: borrowed pointer to [bins][scores][3]
+int openmc_tally_results(int32_t index, double** ptr, size_t shape_[3])
+{
+  State& s = S();
+  if (index < 0 || index >= static_cast<int32_t>(s.model.tallies.size()))
+    return fail(OPENMC_E_OUT_OF_BOUNDS, "Index in tallies array is out of bounds.");
+  try {
+    if (s.gpu) gpu_fetch_tallies(s.gpu, s.model);
+  } catch (const std::exception& e) {
+    return fail(OPENMC_E_UNASSIGNED, e.what());
+  }
+  HTally& t = s.model.tallies[index];
+  *ptr = t.results.data();
+  shape_[0] = static_cast<size_t>(t.n_filter_bins);
+  shape_[1] = t.scores.size();
+  shape_[2] = 3;
+  return 0;
+}
+
+int openmc_get_tally_index(int32_t id, int32_t* index)
+{
+  const auto& ts = S().model.tallies;
+  for (size_t k = 0; k < ts.size(); ++k)
+    if (ts[k].id == id) {
+      *index = static_cast<int32_t>(k);
+      return 0;
+    }
+  return fail(OPENMC_E_INVALID_ID, "No tally exists with ID=" + std::to_string(id) + ".");
+}
+
+int openmc_tally_get_id(int32_t index, int32_t* id)
+{
+  const auto& ts = S().model.tallies;
+  if (index < 0 || index >= static_cast<int32_t>(ts.size()))
+    return fail(OPENMC_E_OUT_OF_BOUNDS, "Index in tallies array is out of bounds.");
+  *id = ts[index].id;
+  return 0;
+}
+
+int openmc_tally_get_n_realizations(int32_t index, int32_t* n)
+{
+  const auto& ts = S().model.tallies;
+  if (index < 0 || index >= static_cast<int32_t>(ts.size()))
+    return fail(OPENMC_E_OUT_OF_BOUNDS, "Index in tallies array is out of bounds.");
+  *n = ts[index].n_realizations;
+  return 0;
+}
+
+size_t tallies_size() { return S().model.tallies.size(); }
+
+// global tallies [4][3] (K_COLLISION, K_ABSORPTION, K_TRACKLENGTH, LEAKAGE)
+int openmc_global_tallies(double** ptr)
+{
+  *ptr = S().global_tallies.data();
+  return 0;
+}
+
+// ------------------------------------------------------ weight windows
+// src/weight_windows.cpp:1020-1340
+size_t openmc_weight_windows_size() { return S().model.weight_windows.size(); }
+
+int openmc_get_weight_windows_index(int32_t id, int32_t* idx)
+{
+  const auto& w = S().model.weight_windows;
+  for (size_t k = 0; k < w.size(); ++k)
+    if (w[k].id == id) {
+      *idx = static_cast<int32_t>(k);
+      return 0;
+    }
+  return fail(OPENMC_E_INVALID_ID, "Weight windows with ID " + std::to_string(id) + " not found.");
+}
+
+int openmc_weight_windows_get_id(int32_t index, int32_t* id)
+{
+  const auto& w = S().model.weight_windows;
+  if (index < 0 || index >= static_cast<int32_t>(w.size()))
+    return fail(OPENMC_E_OUT_OF_BOUNDS, "Index in weight windows array is out of bounds.");
+  *id = w[index].id;
+  return 0;
+}
+
+int openmc_weight_windows_get_bounds(int32_t index, const double** lower_bounds, const double** upper_bounds, size_t* size)
+{
+  auto& w = S().model.weight_windows;
+  if (index < 0 || index >= static_cast<int32_t>(w.size()))
+    return fail(OPENMC_E_OUT_OF_BOUNDS, "Index in weight windows array is out of bounds.");
+  *lower_bounds = w[index].lower.data();
+  *upper_bounds = w[index].upper.data();
+  *size = w[index].lower.size();
+  return 0;
+}
+
+int openmc_weight_windows_set_bounds(int32_t index, const double* lower_bounds, const double* upper_bounds, size_t size)
+{
+  auto& w = S().model.weight_windows;
+  if (index < 0 || index >= static_cast<int32_t>(w.size()))
+    return fail(OPENMC_E_OUT_OF_BOUNDS, "Index in weight windows array is out of bounds.");
+  if (size != w[index].lower.size())
+    return fail(OPENMC_E_INVALID_ARGUMENT, "Size of weight window bounds does not match the number of bins.");
+  std::copy(lower_bounds, lower_bounds + size, w[index].lower.begin());
+  std::copy(upper_bounds, upper_bounds + size, w[index].upper.begin());
+  try {
+    if (S().gpu && index == 0) gpu_set_ww_bounds(S().gpu, lower_bounds, upper_bounds, static_cast<long long>(size));
+  } catch (const std::exception& e) {
+    return fail(OPENMC_E_UNASSIGNED, e.what());
+  }
+  return 0;
+}
+
+int openmc_weight_windows_get_energy_bounds(int32_t index, const double** e_bounds, size_t* e_bounds_size)
+{
+  auto& w = S().model.weight_windows;
+  if (index < 0 || index >= static_cast<int32_t>(w.size()))
+    return fail(OPENMC_E_OUT_OF_BOUNDS, "Index in weight windows array is out of bounds.");
+  *e_bounds = w[index].ebounds.data();
+  *e_bounds_size = w[index].ebounds.size();
+  return 0;
+}
+
+int openmc_weight_windows_update_magic(int32_t ww_idx, int32_t tally_idx, const char* value, double threshold, double ratio)
+{
+  State& s = S();
+  try {
+    if (s.gpu) gpu_fetch_tallies(s.gpu, s.model);
+    return update_magic(s.model, ww_idx, tally_idx, value ? value : "mean", threshold, ratio);
+  } catch (const std::exception& e) {
+    return fail(OPENMC_E_UNASSIGNED, e.what());
+  }
+}
+
+int openmc_weight_windows_get_survival_ratio(int32_t index, double* ratio)
+{
+  auto& w = S().model.weight_windows;
+  if (index < 0 || index >= static_cast<int32_t>(w.size())) return fail(OPENMC_E_OUT_OF_BOUNDS, "Index in weight windows array is out of bounds.");
+  *ratio = w[index].survival_ratio;
+  return 0;
+}
+
+int openmc_weight_windows_get_max_split(int32_t index, int* max_split)
+{
+  auto& w = S().model.weight_windows;
+  if (index < 0 || index >= static_cast<int32_t>(w.size())) return fail(OPENMC_E_OUT_OF_BOUNDS, "Index in weight windows array is out of bounds.");
+  *max_split = w[index].max_split;
+  return 0;
+}
+
+int openmc_weight_windows_get_mesh(int32_t index, int32_t* mesh_idx)
+{
+  auto& w = S().model.weight_windows;
+  if (index < 0 || index >= static_cast<int32_t>(w.size())) return fail(OPENMC_E_OUT_OF_BOUNDS, "Index in weight windows array is out of bounds.");
+  *mesh_idx = w[index].mesh;
+  return 0;
+}
+
+// ------------------------------------------- GB300 extensions (no reference
+// counterpart): run statistics, precision and trace controls
+int openmc_gb300_last_batch(double* out)
+{
+  const BatchStats& b = S().last;
+  out[0] = b.ms;
+  out[1] = b.iterations;
+  out[2] = static_cast<double>(b.n_events);
+  out[3] = b.total_weight;
+  out[4] = b.leakage;
+  out[5] = b.n_lost;
+  out[6] = static_cast<double>(b.n_done);
+  out[7] = b.n_secondaries;
+  return 0;
+}
+
+int openmc_gb300_timing(double* out)
+{
+  State& s = S();
+  out[0] = s.time_active;
+  out[1] = s.time_inactive;
+  out[2] = s.time_wall_active;
+  int active = std::max(0, current_batch - s.model.n_inactive);
+  // src/output.cpp:460-490 calculation rate (active)
+  out[3] = s.time_active > 0 ? static_cast<double>(s.model.n_particles) * active / s.time_active : 0.0;
+  out[4] = s.gpu ? static_cast<double>(gpu_capacity(s.gpu)) : 0.0;
+  return 0;
+}
+
+int openmc_gb300_set_trace(int64_t n_hist, int cap)
+{
+  State& s = S();
+  s.trace_hist = n_hist;
+  s.trace_cap = cap;
+  try {
+    if (s.gpu) gpu_set_trace(s.gpu, n_hist, cap);
+  } catch (const std::exception& e) {
+    return fail(OPENMC_E_ALLOCATE, e.what());
+  }
+  return 0;
+}
+
+int openmc_gb300_get_trace(void* records, int32_t* counts)
+{
+  State& s = S();
+  if (!s.gpu || s.trace_hist <= 0) return fail(OPENMC_E_ALLOCATE, "no trace is being recorded");
+  try {
+    gpu_get_trace(s.gpu, records, counts);
+  } catch (const std::exception& e) {
+    return fail(OPENMC_E_UNASSIGNED, e.what());
+  }
+  return 0;
+}
+
+int openmc_gb300_set_weight_windows_on(int on)
+{
+  State& s = S();
+  weight_windows_on = on != 0;
+  s.model.ww_on = weight_windows_on;
+  try {
+    if (s.gpu) gpu_set_ww_on(s.gpu, weight_windows_on);
+  } catch (const std::exception& e) {
+    return fail(OPENMC_E_INVALID_ARGUMENT, e.what());
+  }
+  return 0;
+}
+
+int openmc_gb300_model_info(int64_t* out)
+{
+  const HModel& m = S().model;
+  out[0] = static_cast<int64_t>(m.nuclides.size());
+  out[1] = static_cast<int64_t>(m.materials.size());
+  out[2] = static_cast<int64_t>(m.cells.size());
+  out[3] = static_cast<int64_t>(m.surfaces.size());
+  out[4] = static_cast<int64_t>(m.tallies.size());
+  out[5] = m.n_log_bins;
+  out[6] = m.n_batches;
+  out[7] = m.n_coord_levels;
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,821 @@
+// Device-side model layout and the per-particle physics/geometry functions of
+// the event-based transport path.  Every function restates the reference
+// function cited beside it with the same floating-point operation order; the
+// library is compiled with -fmad=false so that no multiply-add is fused, and
+// the only differences to a CPU build come from the device log/sin/cos.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "transport.h"
+
+namespace omc {
+
+constexpr int MAXL = 4;  // coordinate levels held per particle
+constexpr double INFTY = 1.7976931348623157e308;  // numeric_limits<double>::max()
+constexpr double PI = 3.141592653589793238462643383279502884;
+constexpr double TINY_BIT = 1e-8;
+constexpr double FP_PRECISION = 1e-14;
+constexpr double FP_REL_PRECISION = 1e-5;
+constexpr double FP_COINCIDENT = 1e-12;
+constexpr double MASS_NEUTRON_EV = 939.56542052e6;
+constexpr int C_NONE = -1;
+constexpr int SURFACE_NONE = 0;
+constexpr uint64_t PRN_MULT = 6364136223846793005ULL;
+constexpr uint64_t PRN_ADD = 1442695040888963407ULL;
+
+
+struct DSurface {
+  double c[4];
+  int type, bc;
+};
+
+struct DCell {
+  double tr[3];
+  int universe, fill_type, fill, tok_off, tok_len, simple;
+};
+
+struct DLattice {
+  double ll[3], pitch[3];
+  int n[3];
+  int is3d, outer, univ_off;
+};
+
+struct DMesh {
+  double ll[3], width[3];
+  int shape[3];
+  int ndim;
+};
+
+struct DFilter {
+  int type, mesh, nbins, e_off;
+};
+
+struct DTally {
+  long long value_off;
+  int nfilt, nscore;
+  int filt[3], stride[3];
+  int score[4];
+};
+
+struct DModel {
+  // geometry
+  const DSurface* surf;
+  const DCell* cell;
+  const int* tok;
+  const int* univ_off;
+  const int* univ_cells;
+  const DLattice* lat;
+  const int* lat_univ;
+  int n_surf, n_cell, n_univ, n_lat, root_univ, n_coord_levels;
+  // nuclear data
+  const long long* nuc_off;  // grid offsets
+  const double* energy;
+  const double4* xs64;  // (total, absorption, elastic, 0) per grid point
+  const float4* xs32;
+  const int* grid_index;  // [n_nuc][M+1]
+  const double* awr;
+  const double* kT;
+  const int* mat_off;
+  const int* mat_nuc;
+  const double* mat_dens;
+  const float* mat_dens32;
+  int n_nuc, n_mat, M, xs_fp32;
+  double e_min, e_max, log_spacing;
+  // source
+  int sp_type, an_type, en_type, dom_type, n_en, n_dom;
+  double sp[6], uref[3];
+  double en_x[8], en_prob[8];
+  int en_alias[8];
+  const int* dom_ids;
+  const int* mat_id;
+  const int* cell_id;
+  // tallies
+  int n_tally;
+  const DTally* tally;
+  const DFilter* filt;
+  const DMesh* mesh;
+  const double* ebins;
+  double* value;
+  // weight windows
+  int ww_on, ww_mesh, ww_ne, ww_max_split;
+  const double* ww_e;
+  const double* ww_lower;
+  const double* ww_upper;
+  double ww_surv, ww_mlb, ww_cut;
+  long long max_history_splits;
+  // settings
+  double energy_cutoff;
+  int max_events;
+  long long n_particles;
+  long long master_seed;
+  unsigned long long stride;
+};
+
+// Structure-of-arrays particle bank; level-major arrays are [MAXL][cap].
+struct DBank {
+  long long cap;
+  long long* id;
+  unsigned long long* seed;
+  double *E, *wgt, *wgt_born, *wgt_ww_born, *ww_factor;
+  double *ux, *uy, *uz;
+  double *rx, *ry, *rz;
+  int *cell, *univ, *latt, *lix, *liy, *liz;
+  int *n_coord, *cell_last0, *cell_born;
+  int *surface, *material, *material_last;
+  double *macro_t, *macro_a;
+  double *bdist, *dcoll;
+  int *bsurf, *blevel, *btrans;
+  int *n_event, *n_collision, *n_split;
+  int* sec_top;
+};
+
+struct DSecondary {
+  double r[3], u[3], E, wgt;
+  int surf, prev;
+};
+
+struct TraceRec {
+  int32_t kind, cell, material, surface_or_nuclide, grid_hash, n_coord;
+  double E, dist, wgt;
+};
+
+struct DCounters {
+  int n_q, n_surf, n_coll, n_next, n_free;
+  int refill_k, refill_free_base, pad0;
+  long long refill_src, next_source, n_done;
+  int n_sec, sec_cap;
+  int error, n_lost;
+  int iter, max_iter;
+  double total_weight, leakage;
+  unsigned long long n_events;
+  long long lost_id;
+};
+
+struct DQueues {
+  int* q_in;
+  int* q_surf;
+  int* q_coll;
+  int* q_tmp;
+  int* free_list;
+  int* hist;
+  int* cursor;
+  DSecondary* sec;
+  DCounters* cnt;
+  TraceRec* trace;
+  int* trace_n;
+  long long trace_hist;
+  int trace_cap;
+  int batch;
+  int sort_keys;
+};
+
+// Defined here: this header is included by exactly one translation unit.
+__constant__ DModel dm;
+__constant__ DBank db;
+__constant__ DQueues dq;
+
+// ------------------------------------------------------------------- RNG
+// src/random_lcg.cpp:32-44
+__device__ __forceinline__ double prn(unsigned long long& s)
+{
+  s = PRN_MULT * s + PRN_ADD;
+  unsigned long long word = ((s >> ((s >> 59u) + 5u)) ^ s) * 12605985483714917081ull;
+  unsigned long long result = (word >> 43u) ^ word;
+  return __ull2double_rn(result) * 5.421010862427522170037264e-20;  // 2^-64
+}
+
+// src/random_lcg.cpp:91-120
+__host__ __device__ inline unsigned long long future_seed(unsigned long long n, unsigned long long seed)
+{
+  unsigned long long g = PRN_MULT, c = PRN_ADD, g_new = 1, c_new = 0;
+  while (n > 0) {
+    if (n & 1) {
+      g_new *= g;
+      c_new = c_new * g + c;
+    }
+    c *= (g + 1);
+    g *= g;
+    n >>= 1;
+  }
+  return g_new * seed + c_new;
+}
+
+__device__ __forceinline__ double uniform_distribution(double a, double b, unsigned long long& s)
+{
+  return a + (b - a) * prn(s);
+}
+
+// src/math_functions.cpp:763-792 (phi sampled)
+__device__ inline void rotate_angle(double& ux, double& uy, double& uz, double mu, unsigned long long& s)
+{
+  double phi_ = 2.0 * PI * prn(s);
+  double sinphi = sin(phi_);
+  double cosphi = cos(phi_);
+  double a = sqrt(fmax(0., 1. - mu * mu));
+  double b = sqrt(fmax(0., 1. - uz * uz));
+  double x = ux, y = uy, z = uz;
+  if (b > 1e-10) {
+    ux = mu * x + a * (x * z * cosphi - y * sinphi) / b;
+    uy = mu * y + a * (y * z * cosphi + x * sinphi) / b;
+    uz = mu * z - a * b * cosphi;
+  } else {
+    b = sqrt(1. - y * y);
+    ux = mu * x + a * (-x * y * sinphi + z * cosphi) / b;
+    uy = mu * y + a * b * sinphi;
+    uz = mu * z - a * (y * z * sinphi + x * cosphi) / b;
+  }
+}
+
+// src/random_dist.cpp:20-32
+__device__ inline double maxwell_spectrum(double T, unsigned long long& s)
+{
+  double r1 = prn(s);
+  double r2 = prn(s);
+  double r3 = prn(s);
+  double c = cos(PI / 2. * r3);
+  return -T * (log(r1) + log(r2) * c * c);
+}
+
+// Lower bound index on a sorted double range (include/openmc/search.h:14-20).
+// Doubles of one sign order like their bit patterns; energies and bin edges
+// here are non-negative, so the comparisons run on the integer pipe.
+__device__ __forceinline__ int lower_bound_index_pos(const double* a, int lo, int hi, double v)
+{
+  // returns lower_bound(a+lo, a+hi, v) - (a+lo) - 1, or 0 when a[lo] == v
+  if (a[lo] == v) return 0;
+  long long key = __double_as_longlong(v);
+  int first = lo, count = hi - lo;
+  while (count > 0) {
+    int step = count >> 1;
+    int it = first + step;
+    if (__double_as_longlong(__ldg(a + it)) < key) {
+      first = it + 1;
+      count -= step + 1;
+    } else {
+      count = step;
+    }
+  }
+  return first - lo - 1;
+}
+
+__device__ __forceinline__ int lower_bound_index_any(const double* a, int lo, int hi, double v)
+{
+  if (a[lo] == v) return 0;
+  int first = lo, count = hi - lo;
+  while (count > 0) {
+    int step = count >> 1;
+    int it = first + step;
+    if (__ldg(a + it) < v) {
+      first = it + 1;
+      count -= step + 1;
+    } else {
+      count = step;
+    }
+  }
+  return first - lo - 1;
+}
+
+// ------------------------------------------------------------- surfaces
+// src/surface.cpp:116-130, 207-218, 399-442, 549-570
+__device__ inline double surf_evaluate(const DSurface& s, double x, double y, double z)
+{
+  switch (s.type) {
+  case 0: return x - s.c[0];
+  case 1: return y - s.c[0];
+  case 2: return z - s.c[0];
+  case 3: { double a = y - s.c[0], b = z - s.c[1]; return a * a + b * b - s.c[2] * s.c[2]; }
+  case 4: { double a = x - s.c[0], b = z - s.c[1]; return a * a + b * b - s.c[2] * s.c[2]; }
+  case 5: { double a = x - s.c[0], b = y - s.c[1]; return a * a + b * b - s.c[2] * s.c[2]; }
+  default: {
+    double a = x - s.c[0], b = y - s.c[1], c = z - s.c[2];
+    return a * a + b * b + c * c - s.c[3] * s.c[3];
+  }
+  }
+}
+
+__device__ inline double plane_distance(double r_i, double u_i, bool coincident, double offset)
+{
+  const double f = offset - r_i;
+  if (coincident || fabs(f) < FP_COINCIDENT || u_i == 0.0) return INFTY;
+  const double d = f / u_i;
+  if (d < 0.0) return INFTY;
+  return d;
+}
+
+__device__ inline double cylinder_distance(double u1, double r2_, double u2, double r3_, double u3,
+  bool coincident, double offset1, double offset2, double radius)
+{
+  const double a = 1.0 - u1 * u1;
+  if (a == 0.0) return INFTY;
+  const double r2 = r2_ - offset1;
+  const double r3 = r3_ - offset2;
+  const double k = r2 * u2 + r3 * u3;
+  const double c = r2 * r2 + r3 * r3 - radius * radius;
+  const double quad = k * k - a * c;
+  if (quad < 0.0) {
+    return INFTY;
+  } else if (coincident || fabs(c) < FP_COINCIDENT) {
+    if (k >= 0.0) return INFTY;
+    return (-k + sqrt(quad)) / a;
+  } else if (c < 0.0) {
+    return (-k + sqrt(quad)) / a;
+  } else {
+    const double d = (-k - sqrt(quad)) / a;
+    if (d < 0.0) return INFTY;
+    return d;
+  }
+}
+
+__device__ inline double sphere_distance(const DSurface& s, double x_, double y_, double z_, double ux,
+  double uy, double uz, bool coincident)
+{
+  const double x = x_ - s.c[0];
+  const double y = y_ - s.c[1];
+  const double z = z_ - s.c[2];
+  const double k = x * ux + y * uy + z * uz;
+  const double c = x * x + y * y + z * z - s.c[3] * s.c[3];
+  const double quad = k * k - c;
+  if (quad < 0.0) {
+    return INFTY;
+  } else if (coincident || fabs(c) < FP_COINCIDENT) {
+    if (k >= 0.0) return INFTY;
+    return -k + sqrt(quad);
+  } else if (c < 0.0) {
+    return -k + sqrt(quad);
+  } else {
+    const double d = -k - sqrt(quad);
+    if (d < 0.0) return INFTY;
+    return d;
+  }
+}
+
+__device__ inline double surf_distance(const DSurface& s, double x, double y, double z, double ux,
+  double uy, double uz, bool coincident)
+{
+  switch (s.type) {
+  case 0: return plane_distance(x, ux, coincident, s.c[0]);
+  case 1: return plane_distance(y, uy, coincident, s.c[0]);
+  case 2: return plane_distance(z, uz, coincident, s.c[0]);
+  case 3: return cylinder_distance(ux, y, uy, z, uz, coincident, s.c[0], s.c[1], s.c[2]);
+  case 4: return cylinder_distance(uy, x, ux, z, uz, coincident, s.c[0], s.c[1], s.c[2]);
+  case 5: return cylinder_distance(uz, x, ux, y, uy, coincident, s.c[0], s.c[1], s.c[2]);
+  default: return sphere_distance(s, x, y, z, ux, uy, uz, coincident);
+  }
+}
+
+__device__ inline void surf_normal(const DSurface& s, double x, double y, double z, double& nx, double& ny, double& nz)
+{
+  switch (s.type) {
+  case 0: nx = 1.; ny = 0.; nz = 0.; return;
+  case 1: nx = 0.; ny = 1.; nz = 0.; return;
+  case 2: nx = 0.; ny = 0.; nz = 1.; return;
+  case 3: nx = 0.0; ny = 2.0 * (y - s.c[0]); nz = 2.0 * (z - s.c[1]); return;
+  case 4: nx = 2.0 * (x - s.c[0]); ny = 0.0; nz = 2.0 * (z - s.c[1]); return;
+  case 5: nx = 2.0 * (x - s.c[0]); ny = 2.0 * (y - s.c[1]); nz = 0.0; return;
+  default: nx = 2.0 * (x - s.c[0]); ny = 2.0 * (y - s.c[1]); nz = 2.0 * (z - s.c[2]); return;
+  }
+}
+
+__device__ inline bool surf_sense(const DSurface& s, double x, double y, double z, double ux, double uy, double uz)
+{
+  const double f = surf_evaluate(s, x, y, z);
+  if (fabs(f) < FP_COINCIDENT) {
+    double nx, ny, nz;
+    surf_normal(s, x, y, z, nx, ny, nz);
+    return ux * nx + uy * ny + uz * nz > 0.0;
+  }
+  return f > 0.0;
+}
+
+// src/cell.cpp:951-969 simple regions; postfix evaluation for complex ones
+__device__ inline bool cell_contains(const DCell& c, double x, double y, double z, double ux, double uy,
+  double uz, int on_surface)
+{
+  const int* t = dm.tok + c.tok_off;
+  if (c.simple) {
+    for (int k = 0; k < c.tok_len; ++k) {
+      int token = t[k];
+      if (token == on_surface) {
+      } else if (-token == on_surface) {
+        return false;
+      } else {
+        bool sense = surf_sense(dm.surf[abs(token) - 1], x, y, z, ux, uy, uz);
+        if (sense != (token > 0)) return false;
+      }
+    }
+    return true;
+  }
+  unsigned stack = 0;  // bit stack, depth <= 32
+  int sp = 0;
+  for (int k = 0; k < c.tok_len; ++k) {
+    int token = t[k];
+    if (token < 2147483643) {  // OP_UNION
+      bool v;
+      if (token == on_surface) v = true;
+      else if (-token == on_surface) v = false;
+      else v = (surf_sense(dm.surf[abs(token) - 1], x, y, z, ux, uy, uz) == (token > 0));
+      stack = (stack & ~(1u << sp)) | (unsigned(v) << sp);
+      ++sp;
+    } else if (token == 2147483645) {  // OP_COMPLEMENT
+      stack ^= 1u << (sp - 1);
+    } else {
+      bool b = (stack >> (sp - 1)) & 1u;
+      bool a = (stack >> (sp - 2)) & 1u;
+      bool r = (token == 2147483644) ? (a && b) : (a || b);  // INTERSECTION / UNION
+      --sp;
+      stack = (stack & ~(1u << (sp - 1))) | (unsigned(r) << (sp - 1));
+    }
+  }
+  return sp > 0 ? (stack & 1u) : true;
+}
+
+// src/cell.cpp:910-936
+__device__ inline void region_distance(const DCell& c, double x, double y, double z, double ux, double uy,
+  double uz, int on_surface, double& min_dist, int& i_surf)
+{
+  min_dist = INFTY;
+  i_surf = 2147483647;
+  const int* t = dm.tok + c.tok_off;
+  for (int k = 0; k < c.tok_len; ++k) {
+    int token = t[k];
+    if (token >= 2147483643) continue;
+    bool coincident = abs(token) == abs(on_surface);
+    double d = surf_distance(dm.surf[abs(token) - 1], x, y, z, ux, uy, uz, coincident);
+    if (d < min_dist) {
+      if (min_dist - d >= FP_PRECISION * min_dist) {
+        min_dist = d;
+        i_surf = -token;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------- lattices
+// src/lattice.cpp:252-306
+__device__ inline double lattice_distance(const DLattice& lat, double x, double y, double z, double ux,
+  double uy, double uz, int& trans)
+{
+  double x0 = copysign(0.5 * lat.pitch[0], ux);
+  double y0 = copysign(0.5 * lat.pitch[1], uy);
+  double d = INFTY;
+  trans = 13;  // encoded (tx+1) + 3(ty+1) + 9(tz+1); 13 == no translation
+  if ((fabs(x - x0) > FP_PRECISION) && ux != 0) {
+    d = (x0 - x) / ux;
+    trans = (ux > 0) ? 14 : 12;
+  }
+  if ((fabs(y - y0) > FP_PRECISION) && uy != 0) {
+    double this_d = (y0 - y) / uy;
+    if (this_d < d) {
+      d = this_d;
+      trans = (uy > 0) ? 16 : 10;
+    }
+  }
+  if (lat.is3d) {
+    double z0 = copysign(0.5 * lat.pitch[2], uz);
+    if ((fabs(z - z0) > FP_PRECISION) && uz != 0) {
+      double this_d = (z0 - z) / uz;
+      if (this_d < d) {
+        d = this_d;
+        trans = (uz > 0) ? 22 : 4;
+      }
+    }
+  }
+  return d;
+}
+
+// src/lattice.cpp:310-342
+__device__ inline void lattice_get_indices(const DLattice& lat, double x, double y, double z, double ux,
+  double uy, double uz, int* res)
+{
+  double ix_ = (x - lat.ll[0]) / lat.pitch[0];
+  long long ix_close = llround(ix_);
+  if (fabs(ix_ - ix_close) < FP_COINCIDENT) res[0] = (ux > 0) ? ix_close : ix_close - 1;
+  else res[0] = static_cast<int>(floor(ix_));
+  double iy_ = (y - lat.ll[1]) / lat.pitch[1];
+  long long iy_close = llround(iy_);
+  if (fabs(iy_ - iy_close) < FP_COINCIDENT) res[1] = (uy > 0) ? iy_close : iy_close - 1;
+  else res[1] = static_cast<int>(floor(iy_));
+  res[2] = 0;
+  if (lat.is3d) {
+    double iz_ = (z - lat.ll[2]) / lat.pitch[2];
+    long long iz_close = llround(iz_);
+    if (fabs(iz_ - iz_close) < FP_COINCIDENT) res[2] = (uz > 0) ? iz_close : iz_close - 1;
+    else res[2] = static_cast<int>(floor(iz_));
+  }
+}
+
+// src/lattice.cpp:352-361
+__device__ inline void lattice_local_position(const DLattice& lat, double& x, double& y, double& z, const int* i)
+{
+  x -= (lat.ll[0] + (i[0] + 0.5) * lat.pitch[0]);
+  y -= (lat.ll[1] + (i[1] + 0.5) * lat.pitch[1]);
+  if (lat.is3d) z -= (lat.ll[2] + (i[2] + 0.5) * lat.pitch[2]);
+}
+
+__device__ __forceinline__ bool lattice_valid(const DLattice& lat, const int* i)
+{
+  return i[0] >= 0 && i[0] < lat.n[0] && i[1] >= 0 && i[1] < lat.n[1] && i[2] >= 0 && i[2] < lat.n[2];
+}
+
+// ------------------------------------------------------- particle geometry
+// Register copy of a particle's coordinate levels.
+struct Geo {
+  double r[MAXL][3];
+  double u[3];
+  int cell[MAXL], univ[MAXL], lat[MAXL], li[MAXL][3];
+  int n_coord;
+  int surface;
+  int material, material_last;
+};
+
+__device__ inline void geo_load(Geo& g, long long s)
+{
+  const long long cap = db.cap;
+  g.n_coord = db.n_coord[s];
+  g.u[0] = db.ux[s];
+  g.u[1] = db.uy[s];
+  g.u[2] = db.uz[s];
+  for (int l = 0; l < MAXL; ++l) {
+    if (l >= g.n_coord) break;
+    long long k = l * cap + s;
+    g.r[l][0] = db.rx[k];
+    g.r[l][1] = db.ry[k];
+    g.r[l][2] = db.rz[k];
+    g.cell[l] = db.cell[k];
+    g.univ[l] = db.univ[k];
+    g.lat[l] = db.latt[k];
+    g.li[l][0] = db.lix[k];
+    g.li[l][1] = db.liy[k];
+    g.li[l][2] = db.liz[k];
+  }
+  g.surface = db.surface[s];
+  g.material = db.material[s];
+  g.material_last = db.material_last[s];
+}
+
+__device__ inline void geo_store(const Geo& g, long long s)
+{
+  const long long cap = db.cap;
+  db.n_coord[s] = g.n_coord;
+  db.ux[s] = g.u[0];
+  db.uy[s] = g.u[1];
+  db.uz[s] = g.u[2];
+  for (int l = 0; l < MAXL; ++l) {
+    if (l >= g.n_coord) break;
+    long long k = l * cap + s;
+    db.rx[k] = g.r[l][0];
+    db.ry[k] = g.r[l][1];
+    db.rz[k] = g.r[l][2];
+    db.cell[k] = g.cell[l];
+    db.univ[k] = g.univ[l];
+    db.latt[k] = g.lat[l];
+    db.lix[k] = g.li[l][0];
+    db.liy[k] = g.li[l][1];
+    db.liz[k] = g.li[l][2];
+  }
+  db.surface[s] = g.surface;
+  db.material[s] = g.material;
+  db.material_last[s] = g.material_last;
+}
+
+__device__ __forceinline__ void coord_reset(Geo& g, int l)
+{
+  g.cell[l] = C_NONE;
+  g.univ[l] = C_NONE;
+  g.lat[l] = C_NONE;
+  g.li[l][0] = g.li[l][1] = g.li[l][2] = 0;
+}
+
+// src/universe.cpp:40-59
+__device__ inline bool universe_find_cell(Geo& g)
+{
+  int lvl = g.n_coord - 1;
+  int u = g.univ[lvl];
+  int a = dm.univ_off[u], b = dm.univ_off[u + 1];
+  for (int k = a; k < b; ++k) {
+    int ic = dm.univ_cells[k];
+    const DCell& c = dm.cell[ic];
+    if (c.universe != u) continue;
+    if (cell_contains(c, g.r[lvl][0], g.r[lvl][1], g.r[lvl][2], g.u[0], g.u[1], g.u[2], g.surface)) {
+      g.cell[lvl] = ic;
+      return true;
+    }
+  }
+  return false;
+}
+
+// src/geometry.cpp:102-252 (exhaustive branch; neighbour lists are an
+// ordering optimisation with the same result for non-overlapping cells)
+__device__ inline bool find_cell_inner(Geo& g, bool& lost_outer)
+{
+  for (;; ++g.n_coord) {
+    if (!universe_find_cell(g)) return false;
+    int lvl = g.n_coord - 1;
+    const DCell& c = dm.cell[g.cell[lvl]];
+    if (c.fill_type == 0) {
+      g.material_last = g.material;
+      g.material = c.fill;
+      return true;
+    }
+    if (g.n_coord >= dm.n_coord_levels) return false;
+    int nl = lvl + 1;
+    g.r[nl][0] = g.r[lvl][0] - c.tr[0];
+    g.r[nl][1] = g.r[lvl][1] - c.tr[1];
+    g.r[nl][2] = g.r[lvl][2] - c.tr[2];
+    if (c.fill_type == 1) {
+      g.univ[nl] = c.fill;
+      g.lat[nl] = C_NONE;
+    } else {
+      const DLattice& lat = dm.lat[c.fill];
+      lattice_get_indices(lat, g.r[nl][0], g.r[nl][1], g.r[nl][2], g.u[0], g.u[1], g.u[2], g.li[nl]);
+      lattice_local_position(lat, g.r[nl][0], g.r[nl][1], g.r[nl][2], g.li[nl]);
+      g.lat[nl] = c.fill;
+      if (lattice_valid(lat, g.li[nl])) {
+        g.univ[nl] = dm.lat_univ[lat.univ_off + lat.n[0] * lat.n[1] * g.li[nl][2] + lat.n[0] * g.li[nl][1] + g.li[nl][0]];
+      } else if (lat.outer != -1) {
+        g.univ[nl] = lat.outer;
+      } else {
+        lost_outer = true;
+        return false;
+      }
+    }
+    g.cell[nl] = C_NONE;
+  }
+}
+
+// src/geometry.cpp:284-298
+__device__ inline bool exhaustive_find_cell(Geo& g, bool& lost_outer)
+{
+  if (g.univ[g.n_coord - 1] == C_NONE) {
+    g.univ[0] = dm.root_univ;
+    g.n_coord = 1;
+  }
+  return find_cell_inner(g, lost_outer);
+}
+
+// src/geometry.cpp:361-453
+__device__ inline void distance_to_boundary(const Geo& g, double& dist, int& surface, int& level,
+  int& trans, bool& neg_lat)
+{
+  double d_lat = __longlong_as_double(0x7ff0000000000000LL);  // INFINITY
+  double d_surf;
+  int level_surf_cross;
+  int level_lat_trans = 13;
+  const double INF = __longlong_as_double(0x7ff0000000000000LL);
+  dist = INF;
+  surface = SURFACE_NONE;
+  level = 0;
+  trans = 13;
+  for (int i = 0; i < g.n_coord; i++) {
+    const DCell& c = dm.cell[g.cell[i]];
+    const double* r = g.r[i];
+    region_distance(c, r[0], r[1], r[2], g.u[0], g.u[1], g.u[2], g.surface, d_surf, level_surf_cross);
+    if (g.lat[i] != C_NONE) {
+      d_lat = lattice_distance(dm.lat[g.lat[i]], r[0], r[1], r[2], g.u[0], g.u[1], g.u[2], level_lat_trans);
+      if (d_lat < 0) neg_lat = true;
+    }
+    double& d = dist;
+    if (d_surf < d_lat - FP_COINCIDENT) {
+      if (d == INF || (d - d_surf) / d >= FP_REL_PRECISION) {
+        d = d_surf;
+        if (c.simple || d == INFTY) {
+          surface = level_surf_cross;
+        } else {
+          double hx = r[0] + d_surf * g.u[0];
+          double hy = r[1] + d_surf * g.u[1];
+          double hz = r[2] + d_surf * g.u[2];
+          double nx, ny, nz;
+          surf_normal(dm.surf[abs(level_surf_cross) - 1], hx, hy, hz, nx, ny, nz);
+          surface = (g.u[0] * nx + g.u[1] * ny + g.u[2] * nz > 0) ? abs(level_surf_cross) : -abs(level_surf_cross);
+        }
+        trans = 13;
+        level = i + 1;
+      }
+    } else {
+      if (d == INF || (d - d_lat) / d >= FP_REL_PRECISION) {
+        d = d_lat;
+        surface = SURFACE_NONE;
+        trans = level_lat_trans;
+        level = i + 1;
+      }
+    }
+  }
+}
+
+// --------------------------------------------------------- cross sections
+// Per-nuclide lookup: src/nuclide.cpp:724-775 (single temperature).
+struct Micro {
+  double total, absorption;
+  int i_grid;
+  double f;
+};
+
+__device__ __forceinline__ int nuclide_grid(int nuc, int i_log, double E, double& f)
+{
+  const long long off = dm.nuc_off[nuc];
+  const int G = static_cast<int>(dm.nuc_off[nuc + 1] - off);
+  const double* e = dm.energy + off;
+  int i_grid;
+  if (E < __ldg(e)) {
+    i_grid = 0;
+  } else if (E > __ldg(e + G - 1)) {
+    i_grid = G - 2;
+  } else {
+    const int* gi = dm.grid_index + static_cast<long long>(nuc) * (dm.M + 1);
+    int i_low = __ldg(gi + i_log);
+    int i_high = __ldg(gi + i_log + 1) + 1;
+    i_grid = i_low + lower_bound_index_pos(e, i_low, i_high, E);
+  }
+  double e0 = __ldg(e + i_grid), e1 = __ldg(e + i_grid + 1);
+  if (e0 == e1) {
+    ++i_grid;
+    e0 = e1;
+    e1 = __ldg(e + i_grid + 1);
+  }
+  f = (E - e0) / (e1 - e0);
+  return i_grid;
+}
+
+__device__ __forceinline__ double4 ldg4(const double4* p)
+{
+  const double2* q = reinterpret_cast<const double2*>(p);
+  double2 a = __ldg(q);
+  double2 b = __ldg(q + 1);
+  return make_double4(a.x, a.y, b.x, b.y);
+}
+
+__device__ __forceinline__ Micro micro_xs64(int nuc, int i_log, double E)
+{
+  Micro m;
+  m.i_grid = nuclide_grid(nuc, i_log, E, m.f);
+  const double4* xs = dm.xs64 + dm.nuc_off[nuc];
+  double4 a = ldg4(xs + m.i_grid);
+  double4 b = ldg4(xs + m.i_grid + 1);
+  m.total = (1.0 - m.f) * a.x + m.f * b.x;
+  m.absorption = (1.0 - m.f) * a.y + m.f * b.y;
+  return m;
+}
+
+// FP32 tables: interpolation in FP32 from an FP64 interpolation factor
+__device__ __forceinline__ void micro_xs32(int nuc, int i_log, double E, float& t, float& a_out, int& i_grid, float& f32)
+{
+  double f;
+  i_grid = nuclide_grid(nuc, i_log, E, f);
+  f32 = static_cast<float>(f);
+  const float4* xs = dm.xs32 + dm.nuc_off[nuc];
+  float4 a = __ldg(xs + i_grid);
+  float4 b = __ldg(xs + i_grid + 1);
+  t = (1.0f - f32) * a.x + f32 * b.x;
+  a_out = (1.0f - f32) * a.y + f32 * b.y;
+}
+
+// Hash bin of E (src/material.cpp:833-834), clamped to [0, M-1]: the
+// reference reads grid_index[M+1] past the end of the table for E equal to
+// the grid maximum (and a negative bin below the minimum); the clamp keeps
+// the search window inside the table and the located grid index unchanged.
+__device__ __forceinline__ int log_union_index(double E)
+{
+  int i = static_cast<int>(log(E / dm.e_min) / dm.log_spacing);
+  return i < 0 ? 0 : (i > dm.M - 1 ? dm.M - 1 : i);
+}
+
+// src/material.cpp:829-901.  Returns the grid-index hash of the material's
+// nuclides (h = 31 h + i_grid) for per-history trace comparison.
+__device__ inline uint32_t material_xs(int mat, double E, double& tot, double& abs_)
+{
+  int i_log = log_union_index(E);
+  int a = dm.mat_off[mat], b = dm.mat_off[mat + 1];
+  uint32_t h = 0;
+  if (!dm.xs_fp32) {
+    double t = 0.0, ab = 0.0;
+    for (int k = a; k < b; ++k) {
+      int nuc = dm.mat_nuc[k];
+      Micro m = micro_xs64(nuc, i_log, E);
+      h = h * 31u + static_cast<uint32_t>(m.i_grid);
+      double dens = dm.mat_dens[k];
+      t += dens * m.total;
+      ab += dens * m.absorption;
+    }
+    tot = t;
+    abs_ = ab;
+  } else {
+    float t = 0.0f, ab = 0.0f;
+    for (int k = a; k < b; ++k) {
+      int nuc = dm.mat_nuc[k];
+      float mt, ma, f32;
+      int ig;
+      micro_xs32(nuc, i_log, E, mt, ma, ig, f32);
+      h = h * 31u + static_cast<uint32_t>(ig);
+      float dens = dm.mat_dens32[k];
+      t += dens * mt;
+      ab += dens * ma;
+    }
+    tot = t;
+    abs_ = ab;
+  }
+  return h;
+}
+
+}  // namespace omc

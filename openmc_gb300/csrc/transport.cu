@@ -1,0 +1,1606 @@
+// Event-based transport on one GB300: particle bank as structure-of-arrays in
+// HBM, compacted event queues (warp ballot + one atomic per warp), optional
+// counting sort of the cross-section queue by (material, energy octave), and
+// one CUDA graph per batch whose conditional while-node runs event iterations
+// until every history of the batch has ended.
+//
+// Kernel <-> reference mapping
+//   k_refill      process_init_events  src/event.cpp:62-71 + initialize_history
+//                 src/simulation.cpp:573-649 + sample_external_source
+//                 src/source.cpp:355-415, 627-660
+//   k_xs          process_calculate_xs_events src/event.cpp:73-105 ->
+//                 Particle::event_calculate_xs src/particle.cpp:160-230
+//   k_advance     process_advance_particle_events src/event.cpp:107-128 ->
+//                 Particle::event_advance src/particle.cpp:232-286 + track-length
+//                 tallies src/tallies/tally_scoring.cpp:2416-2541
+//   k_surface     process_surface_crossing_events src/event.cpp:130-147 ->
+//                 event_cross_surface src/particle.cpp:288-329 + revive
+//   k_collision   process_collision_events src/event.cpp:149-166 ->
+//                 event_collide src/particle.cpp:331-415 + revive
+//   k_accumulate  Tally::accumulate src/tallies/tally.cpp:821-880
+//
+// Queues replace SharedArray::thread_safe_append (include/openmc/
+// shared_array.h:71-89).  Dead slots are refilled from the batch's remaining
+// source particles every iteration instead of running fixed sub-iterations of
+// max_particles_in_flight; each history depends only on its own id-derived
+// seeds, so the per-history physics is unchanged.
+//
+// Semantics kept from the history-based loop where the event-based loop of
+// the reference differs only for particles that die inside advance (time
+// cutoff, lost particle): their secondaries are still revived.
+// Particle time is not tracked: no time cutoff or time filter is supported,
+// and time does not feed any other quantity of this path.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "device.cuh"
+#include "host_model.h"
+#include "transport.h"
+
+namespace omc {
+
+// --------------------------------------------------------------- helpers
+__device__ __forceinline__ void warp_append(int* q, int* counter, int val, bool pred)
+{
+  unsigned m = __ballot_sync(0xffffffffu, pred);
+  if (!m) return;
+  int lane = threadIdx.x & 31;
+  int leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(counter, __popc(m));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (pred) q[base + __popc(m & ((1u << lane) - 1u))] = val;
+}
+
+__device__ __forceinline__ bool traced(long long id)
+{
+  return dq.trace != nullptr && id >= 1 && id <= dq.trace_hist;
+}
+
+__device__ __forceinline__ TraceRec* trace_slot(long long id)
+{
+  int n = dq.trace_n[id - 1];
+  if (n >= dq.trace_cap) return nullptr;
+  return dq.trace + (id - 1) * dq.trace_cap + n;
+}
+
+__device__ void set_error(int flag) { atomicOr(&dq.cnt->error, flag); }
+
+__device__ void mark_lost(long long s)
+{
+  db.wgt[s] = 0.0;
+  atomicAdd(&dq.cnt->n_lost, 1);
+  atomicExch(reinterpret_cast<unsigned long long*>(&dq.cnt->lost_id), static_cast<unsigned long long>(db.id[s]));
+}
+
+// ------------------------------------------------------ mesh raytrace
+// src/mesh.cpp:1328-1369 RegularMesh helpers
+__device__ __forceinline__ int mesh_index_in_direction(const DMesh& m, double r, int i)
+{
+  return static_cast<int>(ceil((r - m.ll[i]) / m.width[i]));
+}
+
+__device__ __forceinline__ void mesh_get_indices(const DMesh& m, double x, double y, double z, int* ijk, bool& in_mesh)
+{
+  double r[3] = {x, y, z};
+  in_mesh = true;
+  for (int i = 0; i < m.ndim; ++i) {
+    ijk[i] = mesh_index_in_direction(m, r[i], i);
+    if (ijk[i] < 1 || ijk[i] > m.shape[i]) in_mesh = false;
+  }
+}
+
+__device__ __forceinline__ int mesh_bin(const DMesh& m, const int* ijk)
+{
+  switch (m.ndim) {
+  case 1: return ijk[0] - 1;
+  case 2: return (ijk[1] - 1) * m.shape[0] + ijk[0] - 1;
+  default: return ((ijk[2] - 1) * m.shape[1] + (ijk[1] - 1)) * m.shape[0] + ijk[0] - 1;
+  }
+}
+
+struct MeshDist {
+  int next_index;
+  bool max_surface;
+  double distance;
+};
+
+__device__ __forceinline__ MeshDist mesh_dist(const DMesh& m, const int* ijk, int i, const double* r0, const double* u)
+{
+  MeshDist d;
+  d.next_index = ijk[i];
+  d.max_surface = true;
+  d.distance = INFTY;
+  if (fabs(u[i]) < FP_PRECISION) return d;
+  d.max_surface = (u[i] > 0);
+  if (d.max_surface && (ijk[i] <= m.shape[i])) {
+    d.next_index++;
+    d.distance = ((m.ll[i] + ijk[i] * m.width[i]) - r0[i]) / u[i];
+  } else if (!d.max_surface && (ijk[i] >= 1)) {
+    d.next_index--;
+    d.distance = ((m.ll[i] + (ijk[i] - 1) * m.width[i]) - r0[i]) / u[i];
+  }
+  return d;
+}
+
+// src/mesh.cpp:999-1146 raytrace_mesh/bins_crossed; calls f(bin, fraction)
+template<class F>
+__device__ void mesh_bins_crossed(const DMesh& m, const double* r0, const double* r1, const double* u, F f)
+{
+  double dx = r1[0] - r0[0], dy = r1[1] - r0[1], dz = r1[2] - r0[2];
+  double total_distance = sqrt(dx * dx + dy * dy + dz * dz);
+  if (total_distance == 0.0) return;
+  const int n = m.ndim;
+  bool in_mesh;
+  double traveled = 0.0;
+  int ijk[3] = {0, 0, 0};
+  mesh_get_indices(m, r0[0] + TINY_BIT * u[0], r0[1] + TINY_BIT * u[1], r0[2] + TINY_BIT * u[2], ijk, in_mesh);
+  if (total_distance < 2 * TINY_BIT) {
+    if (in_mesh) f(mesh_bin(m, ijk), 1.0);
+    return;
+  }
+  MeshDist dist[3];
+  dist[0].distance = dist[1].distance = dist[2].distance = INFTY;
+  for (int k = 0; k < n; ++k) dist[k] = mesh_dist(m, ijk, k, r0, u);
+  for (int guard = 0; guard < 1 << 24; ++guard) {
+    if (in_mesh) {
+      int k = 0;
+      if (dist[1].distance < dist[k].distance) k = 1;
+      if (dist[2].distance < dist[k].distance) k = 2;
+      f(mesh_bin(m, ijk), (fmin(dist[k].distance, total_distance) - traveled) / total_distance);
+      traveled = dist[k].distance;
+      if (traveled >= total_distance) return;
+      ijk[k] = dist[k].next_index;
+      dist[k] = mesh_dist(m, ijk, k, r0, u);
+      in_mesh = ((ijk[k] >= 1) && (ijk[k] <= m.shape[k]));
+    } else {
+      int k_max = -1;
+      for (int k = 0; k < n; ++k) {
+        if ((ijk[k] < 1 || ijk[k] > m.shape[k]) && (dist[k].distance > traveled)) {
+          traveled = dist[k].distance;
+          k_max = k;
+        }
+      }
+      if (k_max == -1) traveled += TINY_BIT;
+      if (traveled >= total_distance) return;
+      double t = traveled + TINY_BIT;
+      mesh_get_indices(m, r0[0] + t * u[0], r0[1] + t * u[1], r0[2] + t * u[2], ijk, in_mesh);
+      for (int k = 0; k < n; ++k) dist[k] = mesh_dist(m, ijk, k, r0, u);
+    }
+  }
+}
+
+// src/tallies/tally_scoring.cpp:2416-2541 + FilterBinIter :31-139 +
+// score_general_ce_nonanalog :578-1106 (flux, total, absorption)
+__device__ void score_tracklength(const double* r0, const double* r1, const double* u, double E_last,
+  double wgt, double distance, double mt, double ma)
+{
+  double flux = wgt * distance;
+  for (int t = 0; t < dm.n_tally; ++t) {
+    const DTally& T = dm.tally[t];
+    long long base = 0;
+    int mesh_slot = -1;
+    bool empty = false;
+    for (int i = 0; i < T.nfilt; ++i) {
+      const DFilter& F = dm.filt[T.filt[i]];
+      if (F.type == 0) {
+        mesh_slot = i;
+      } else if (F.type == 1) {
+        const double* b = dm.ebins + F.e_off;
+        if (E_last >= b[0] && E_last <= b[F.nbins]) {
+          base += static_cast<long long>(lower_bound_index_pos(b, 0, F.nbins + 1, E_last)) * T.stride[i];
+        } else {
+          empty = true;
+        }
+      }
+    }
+    if (empty) continue;
+    double* val = dm.value + T.value_off;
+    const int ns = T.nscore;
+    auto add = [&](long long index, double weight) {
+      for (int s = 0; s < ns; ++s) {
+        double score;
+        int sc = T.score[s];
+        if (sc == 0) score = flux;
+        else if (sc == 1) score = mt * flux;
+        else score = ma * flux;
+        atomicAdd(val + index * ns + s, score * weight);
+      }
+    };
+    if (mesh_slot < 0) {
+      add(base, 1.0);
+    } else {
+      const DMesh& M = dm.mesh[dm.filt[T.filt[mesh_slot]].mesh];
+      const long long stride = T.stride[mesh_slot];
+      mesh_bins_crossed(M, r0, r1, u, [&](int bin, double frac) {
+        add(base + bin * stride, 1. * frac);
+      });
+    }
+  }
+}
+
+// ------------------------------------------------------- weight windows
+// src/weight_windows.cpp:375-411
+__device__ bool get_weight_window(double x, double y, double z, double E, double& lower, double& upper)
+{
+  const DMesh& m = dm.mesh[dm.ww_mesh];
+  int ijk[3] = {1, 1, 1};
+  bool in_mesh;
+  mesh_get_indices(m, x, y, z, ijk, in_mesh);
+  if (!in_mesh) return false;
+  if (E < dm.ww_e[0] || E > dm.ww_e[dm.ww_ne]) return false;
+  int eb = lower_bound_index_pos(dm.ww_e, 0, dm.ww_ne + 1, E);
+  long long nm = static_cast<long long>(m.shape[0]) * m.shape[1] * m.shape[2];
+  long long k = eb * nm + mesh_bin(m, ijk);
+  lower = dm.ww_lower[k];
+  upper = dm.ww_upper[k];
+  return lower >= 0.0;
+}
+
+__device__ void push_secondaries(long long s, int n, double wgt, const double* r, const double* u, double E, int surf)
+{
+  if (n <= 0) return;
+  int base = atomicAdd(&dq.cnt->n_sec, n);
+  if (base + n > dq.cnt->sec_cap) {
+    set_error(ERR_SECONDARY_OVERFLOW);
+    return;
+  }
+  int top = db.sec_top[s];
+  for (int l = 0; l < n; ++l) {
+    DSecondary& d = dq.sec[base + l];
+    d.r[0] = r[0]; d.r[1] = r[1]; d.r[2] = r[2];
+    d.u[0] = u[0]; d.u[1] = u[1]; d.u[2] = u[2];
+    d.E = E;
+    d.wgt = wgt;
+    d.surf = surf;
+    d.prev = top;
+    top = base + l;
+  }
+  db.sec_top[s] = top;
+}
+
+// src/weight_windows.cpp:56-146 (wgt/seed passed in registers)
+__device__ void apply_weight_windows(long long s, double& wgt, unsigned long long& seed, const double* r,
+  const double* u, double E, int surface)
+{
+  if (!dm.ww_on) return;
+  if (E <= 0 || wgt == 0.0) return;
+  double lower = -1, upper = 1;
+  bool valid = get_weight_window(r[0], r[1], r[2], E, lower, upper);
+  double wgt_ww_born = db.wgt_ww_born[s];
+  if (wgt_ww_born == -1.0) {
+    wgt_ww_born = valid ? (lower + upper) / 2 : 1.0;
+    db.wgt_ww_born[s] = wgt_ww_born;
+  }
+  if (!valid) return;
+  double survival = lower * dm.ww_surv;
+  double factor = db.wgt_born[s] / wgt_ww_born;
+  lower *= factor;
+  upper *= factor;
+  survival *= factor;
+  double weight = wgt;
+  if (wgt < dm.ww_cut) {
+    wgt = 0.0;
+    return;
+  }
+  double ww_factor = db.ww_factor[s];
+  if (ww_factor == 0.0 && dm.ww_mlb > 1.0 && wgt > lower * dm.ww_mlb) {
+    ww_factor = wgt / (lower * dm.ww_mlb);
+    db.ww_factor[s] = ww_factor;
+  }
+  if (ww_factor > 1.0) {
+    lower *= ww_factor;
+    upper *= ww_factor;
+    survival *= ww_factor;
+  }
+  if (weight > upper) {
+    int n_split_hist = db.n_split[s];
+    if (n_split_hist >= dm.max_history_splits) return;
+    double n_split = ceil(weight / upper);
+    double max_split = dm.ww_max_split;
+    n_split = fmin(n_split, max_split);
+    db.n_split[s] = static_cast<int>(n_split_hist + n_split);
+    int i_split = static_cast<int>(llround(n_split));
+    push_secondaries(s, i_split - 1, weight / n_split, r, u, E, surface);
+    wgt = weight / n_split;
+  } else if (weight <= lower) {
+    double weight_survive = fmin(weight * dm.ww_max_split, survival);
+    // src/physics_common.cpp:12-19
+    if (weight_survive * prn(seed) < wgt) wgt = weight_survive;
+    else wgt = 0.;
+  }
+}
+
+// ------------------------------------------------------- source sampling
+__device__ bool satisfies_spatial_constraints(double x, double y, double z)
+{
+  Geo g;
+  g.n_coord = 1;
+  coord_reset(g, 0);
+  g.r[0][0] = x; g.r[0][1] = y; g.r[0][2] = z;
+  g.u[0] = 0.0; g.u[1] = 0.0; g.u[2] = 1.0;
+  g.surface = SURFACE_NONE;
+  g.material = C_NONE;
+  g.material_last = C_NONE;
+  bool lost_outer = false;
+  if (!exhaustive_find_cell(g, lost_outer)) return false;
+  if (dm.dom_type < 0 || dm.n_dom == 0) return true;
+  if (dm.dom_type == 1) {
+    if (g.material == C_NONE) return false;
+    int id = dm.mat_id[g.material];
+    for (int k = 0; k < dm.n_dom; ++k) if (dm.dom_ids[k] == id) return true;
+    return false;
+  }
+  for (int i = 0; i < g.n_coord; ++i) {
+    int id = dm.dom_type == 0 ? dm.cell_id[g.cell[i]] : g.univ[i];
+    for (int k = 0; k < dm.n_dom; ++k) if (dm.dom_ids[k] == id) return true;
+  }
+  return false;
+}
+
+__device__ double sample_energy(unsigned long long& seed)
+{
+  if (dm.en_type == 1) return maxwell_spectrum(dm.en_x[0], seed);
+  int n = dm.n_en;
+  if (n <= 1) return dm.en_x[0];
+  // src/distribution.cpp:87-101 alias sampling
+  int u = static_cast<int>(prn(seed) * n);
+  if (prn(seed) < dm.en_prob[u]) return dm.en_x[u];
+  return dm.en_x[dm.en_alias[u]];
+}
+
+// src/simulation.cpp:573-649 initialize_history (fixed source) into slot s
+__device__ void initialize_history(long long s, long long index_source)
+{
+  long long id = static_cast<long long>(dq.batch - 1) * dm.n_particles + index_source;
+  unsigned long long seed = future_seed(static_cast<unsigned long long>(id) * dm.stride,
+    static_cast<unsigned long long>(dm.master_seed + 1));
+  double r[3], u[3], E;
+  // src/source.cpp:355-415
+  int tries = 0;
+  for (;;) {
+    if (dm.sp_type == 0) {
+      r[0] = dm.sp[0]; r[1] = dm.sp[1]; r[2] = dm.sp[2];
+    } else {
+      double xi0 = prn(seed);
+      double xi1 = prn(seed);
+      double xi2 = prn(seed);
+      r[0] = dm.sp[0] + xi0 * (dm.sp[3] - dm.sp[0]);
+      r[1] = dm.sp[1] + xi1 * (dm.sp[4] - dm.sp[1]);
+      r[2] = dm.sp[2] + xi2 * (dm.sp[5] - dm.sp[2]);
+    }
+    if (satisfies_spatial_constraints(r[0], r[1], r[2])) break;
+    if (++tries > 1000000) {
+      set_error(ERR_REJECTION);
+      break;
+    }
+  }
+  if (dm.an_type == 0) {
+    // src/distribution_multi.cpp:106-112
+    double phi = uniform_distribution(0., 2.0 * PI, seed);
+    double mu = uniform_distribution(-1., 1., seed);
+    u[0] = mu;
+    u[1] = sqrt(1.0 - mu * mu) * cos(phi);
+    u[2] = sqrt(1.0 - mu * mu) * sin(phi);
+  } else {
+    u[0] = dm.uref[0]; u[1] = dm.uref[1]; u[2] = dm.uref[2];
+  }
+  tries = 0;
+  for (;;) {
+    E = sample_energy(seed);
+    if (E < dm.e_max) break;
+    if (++tries > 1000000) {
+      set_error(ERR_REJECTION);
+      break;
+    }
+  }
+  // from_source (src/particle.cpp:114-158)
+  const long long cap = db.cap;
+  db.n_coord[s] = 1;
+  for (int l = 0; l < MAXL; ++l) {
+    long long k = l * cap + s;
+    db.cell[k] = C_NONE;
+    db.univ[k] = C_NONE;
+    db.latt[k] = C_NONE;
+    db.lix[k] = 0; db.liy[k] = 0; db.liz[k] = 0;
+  }
+  db.cell_last0[s] = C_NONE;
+  db.cell_born[s] = C_NONE;
+  db.surface[s] = SURFACE_NONE;
+  db.material[s] = C_NONE;
+  db.material_last[s] = C_NONE;
+  db.n_collision[s] = 0;
+  db.rx[s] = r[0]; db.ry[s] = r[1]; db.rz[s] = r[2];
+  db.ux[s] = u[0]; db.uy[s] = u[1]; db.uz[s] = u[2];
+  db.E[s] = E;
+  double wgt = 1.0;
+  db.id[s] = index_source;
+  db.n_event[s] = 0;
+  db.n_split[s] = 0;
+  db.ww_factor[s] = 0.0;
+  db.wgt_born[s] = wgt;
+  db.sec_top[s] = -1;
+  unsigned long long tseed = future_seed(static_cast<unsigned long long>(id) * dm.stride,
+    static_cast<unsigned long long>(dm.master_seed + 0));
+  db.wgt_ww_born[s] = -1.0;
+  apply_weight_windows(s, wgt, tseed, r, u, E, SURFACE_NONE);
+  db.wgt[s] = wgt;
+  db.seed[s] = tseed;
+  atomicAdd(&dq.cnt->total_weight, wgt);
+  if (traced(index_source)) dq.trace_n[index_source - 1] = 0;
+}
+
+// src/particle.cpp:417-473 event_revive_from_secondary; returns alive.
+// Dead slots without secondaries go back to the free list.
+__device__ bool revive_or_free(long long s, double wgt)
+{
+  int ne = db.n_event[s] + 1;
+  if (ne == dm.max_events) {
+    wgt = 0.0;
+    db.wgt[s] = 0.0;
+  }
+  db.n_event[s] = ne;
+  if (wgt != 0.0) return true;
+  int top = db.sec_top[s];
+  if (top < 0) {
+    int k = atomicAdd(&dq.cnt->n_free, 1);
+    dq.free_list[k] = static_cast<int>(s);
+    atomicAdd(reinterpret_cast<unsigned long long*>(&dq.cnt->n_done), 1ull);
+    return false;
+  }
+  const DSecondary& site = dq.sec[top];
+  db.sec_top[s] = site.prev;
+  const long long cap = db.cap;
+  db.n_coord[s] = 1;
+  for (int l = 0; l < MAXL; ++l) {
+    long long k = l * cap + s;
+    db.cell[k] = C_NONE;
+    db.univ[k] = C_NONE;
+    db.latt[k] = C_NONE;
+    db.lix[k] = 0; db.liy[k] = 0; db.liz[k] = 0;
+  }
+  db.cell_last0[s] = C_NONE;
+  db.cell_born[s] = C_NONE;
+  db.surface[s] = site.surf;
+  db.material[s] = C_NONE;
+  db.n_collision[s] = 0;
+  db.wgt[s] = site.wgt;
+  db.rx[s] = site.r[0]; db.ry[s] = site.r[1]; db.rz[s] = site.r[2];
+  db.ux[s] = site.u[0]; db.uy[s] = site.u[1]; db.uz[s] = site.u[2];
+  db.E[s] = site.E;
+  db.n_event[s] = 0;
+  return true;
+}
+
+// ================================================================ kernels
+__global__ void k_batch_init(int batch)
+{
+  long long cap = db.cap;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < cap;
+       i += static_cast<long long>(gridDim.x) * blockDim.x)
+    dq.free_list[i] = static_cast<int>(i);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    DCounters* c = dq.cnt;
+    c->n_q = c->n_surf = c->n_coll = c->n_next = 0;
+    c->n_free = static_cast<int>(cap);
+    c->next_source = 1;
+    c->n_done = 0;
+    c->n_sec = 0;
+    c->iter = 0;
+    c->total_weight = 0.0;
+    c->leakage = 0.0;
+    c->n_events = 0;
+    c->error = 0;
+    c->n_lost = 0;
+  }
+  (void)batch;
+}
+
+// src/particle.cpp:160-230
+__global__ void __launch_bounds__(256) k_xs()
+{
+  const int n = dq.cnt->n_q;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    long long s = dq.q_in[i];
+    long long pid = db.id[s];
+    bool tr = traced(pid);
+    int lvl0 = db.n_coord[s] - 1;
+    int low_cell = db.cell[lvl0 * db.cap + s];
+    int material = db.material[s];
+    int material_last = db.material_last[s];
+    if (low_cell == C_NONE) {
+      Geo g;
+      geo_load(g, s);
+      bool lost_outer = false;
+      if (!exhaustive_find_cell(g, lost_outer)) {
+        mark_lost(s);
+        continue;
+      }
+      if (db.cell_born[s] == C_NONE) db.cell_born[s] = g.cell[g.n_coord - 1];
+      db.cell_last0[s] = g.cell[0];
+      geo_store(g, s);
+      material = g.material;
+      material_last = g.material_last;
+      low_cell = g.cell[g.n_coord - 1];
+    }
+    uint32_t h = 0xffffffffu;
+    double E = db.E[s];
+    if (material != C_NONE) {
+      if (material != material_last || tr) {
+        double t, a;
+        h = material_xs(material, E, t, a);
+        db.macro_t[s] = t;
+        db.macro_a[s] = a;
+      }
+    } else {
+      db.macro_t[s] = 0.0;
+      db.macro_a[s] = 0.0;
+    }
+    if (tr) {
+      TraceRec* rec = trace_slot(pid);
+      if (rec) {
+        rec->cell = low_cell;
+        rec->material = material;
+        rec->grid_hash = static_cast<int32_t>(h);
+        rec->n_coord = db.n_coord[s];
+        rec->E = E;
+      }
+    }
+  }
+}
+
+// src/particle.cpp:232-286
+__global__ void __launch_bounds__(256) k_advance()
+{
+  const int n = dq.cnt->n_q;
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    int i = base + threadIdx.x;
+    bool valid = i < n;
+    long long s = valid ? dq.q_in[i] : 0;
+    bool to_surf = false, to_coll = false, to_next = false;
+    if (valid) {
+      double wgt = db.wgt[s];
+      if (wgt == 0.0) {
+        to_next = revive_or_free(s, wgt);
+      } else {
+        Geo g;
+        geo_load(g, s);
+        double bd;
+        int bs, bl, bt;
+        bool neg_lat = false;
+        distance_to_boundary(g, bd, bs, bl, bt, neg_lat);
+        if (neg_lat) mark_lost(s);
+        unsigned long long seed = db.seed[s];
+        double mt = db.macro_t[s];
+        double dcoll = (mt == 0.0) ? __longlong_as_double(0x7ff0000000000000LL) : -log(prn(seed)) / mt;
+        double distance = bd;
+        if (dcoll < distance) distance = dcoll;
+        if (INFTY < distance) distance = INFTY;
+        double r0[3] = {g.r[0][0], g.r[0][1], g.r[0][2]};
+        for (int l = 0; l < g.n_coord; ++l) {
+          g.r[l][0] = g.r[l][0] + distance * g.u[0];
+          g.r[l][1] = g.r[l][1] + distance * g.u[1];
+          g.r[l][2] = g.r[l][2] + distance * g.u[2];
+        }
+        if (dm.n_tally > 0) score_tracklength(r0, g.r[0], g.u, db.E[s], wgt, distance, mt, db.macro_a[s]);
+        wgt = db.wgt[s];
+        if (distance == INFTY) {
+          wgt = 0.0;
+          db.wgt[s] = 0.0;
+        }
+        const long long cap = db.cap;
+        for (int l = 0; l < g.n_coord; ++l) {
+          long long k = l * cap + s;
+          db.rx[k] = g.r[l][0];
+          db.ry[k] = g.r[l][1];
+          db.rz[k] = g.r[l][2];
+        }
+        db.seed[s] = seed;
+        db.bdist[s] = bd;
+        db.bsurf[s] = bs;
+        db.blevel[s] = bl;
+        db.btrans[s] = bt;
+        db.dcoll[s] = dcoll;
+        long long pid = db.id[s];
+        if (traced(pid)) {
+          TraceRec* rec = trace_slot(pid);
+          if (rec) rec->dist = distance;
+        }
+        if (wgt != 0.0) {
+          to_surf = dcoll > bd;
+          to_coll = !to_surf;
+        } else {
+          to_next = revive_or_free(s, wgt);
+        }
+      }
+    }
+    warp_append(dq.q_surf, &dq.cnt->n_surf, static_cast<int>(s), to_surf);
+    warp_append(dq.q_coll, &dq.cnt->n_coll, static_cast<int>(s), to_coll);
+    warp_append(dq.q_tmp, &dq.cnt->n_next, static_cast<int>(s), to_next);
+  }
+}
+
+// src/geometry.cpp:301-357
+__device__ void cross_lattice(Geo& g, long long s, int trans)
+{
+  int lvl = g.n_coord - 1;
+  const DLattice& lat = dm.lat[g.lat[lvl]];
+  g.li[lvl][0] += trans % 3 - 1;
+  g.li[lvl][1] += (trans / 3) % 3 - 1;
+  g.li[lvl][2] += trans / 9 - 1;
+  const int up = lvl - 1;
+  const DCell& cell = dm.cell[g.cell[up]];
+  g.r[lvl][0] = g.r[up][0] - cell.tr[0];
+  g.r[lvl][1] = g.r[up][1] - cell.tr[1];
+  g.r[lvl][2] = g.r[up][2] - cell.tr[2];
+  lattice_local_position(lat, g.r[lvl][0], g.r[lvl][1], g.r[lvl][2], g.li[lvl]);
+  bool lost_outer = false;
+  if (!lattice_valid(lat, g.li[lvl])) {
+    g.n_coord = 1;
+    if (!exhaustive_find_cell(g, lost_outer)) mark_lost(s);
+  } else {
+    g.univ[lvl] = dm.lat_univ[lat.univ_off + lat.n[0] * lat.n[1] * g.li[lvl][2] + lat.n[0] * g.li[lvl][1] + g.li[lvl][0]];
+    g.cell[lvl] = C_NONE;
+    if (!exhaustive_find_cell(g, lost_outer)) {
+      g.n_coord = 1;
+      if (!exhaustive_find_cell(g, lost_outer)) mark_lost(s);
+    }
+  }
+}
+
+// src/particle.cpp:288-329, 549-710
+__global__ void __launch_bounds__(256) k_surface()
+{
+  const int n = dq.cnt->n_surf;
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    int i = base + threadIdx.x;
+    bool valid = i < n;
+    long long s = valid ? dq.q_surf[i] : 0;
+    bool to_next = false;
+    if (valid) {
+      Geo g;
+      geo_load(g, s);
+      double wgt = db.wgt[s];
+      int bsurf = db.bsurf[s];
+      int trans = db.btrans[s];
+      db.cell_last0[s] = g.cell[0];
+      g.surface = bsurf;
+      g.n_coord = db.blevel[s];
+      bool lost_outer = false;
+      if (trans != 13) {
+        cross_lattice(g, s, trans);
+        wgt = db.wgt[s];
+      } else if (g.surface == SURFACE_NONE || abs(g.surface) > dm.n_surf) {
+        mark_lost(s);
+        wgt = 0.0;
+      } else {
+        const DSurface& surf = dm.surf[abs(g.surface) - 1];
+        if (surf.bc == 1) {
+          // src/particle.cpp:631-655
+          atomicAdd(&dq.cnt->leakage, wgt);
+          wgt = 0.0;
+          db.wgt[s] = 0.0;
+        } else if (surf.bc == 2) {
+          // src/boundary_condition.cpp:38-47 + src/particle.cpp:657-710
+          double nx, ny, nz;
+          surf_normal(surf, g.r[0][0], g.r[0][1], g.r[0][2], nx, ny, nz);
+          double ux = g.u[0], uy = g.u[1], uz = g.u[2];
+          const double projection = nx * ux + ny * uy + nz * uz;
+          const double magnitude = nx * nx + ny * ny + nz * nz;
+          const double fac = 2.0 * projection / magnitude;
+          ux = ux - nx * fac;
+          uy = uy - ny * fac;
+          uz = uz - nz * fac;
+          double norm = sqrt(ux * ux + uy * uy + uz * uz);
+          ux /= norm;
+          uy /= norm;
+          uz /= norm;
+          if (g.n_coord != 1) {
+            mark_lost(s);
+            wgt = 0.0;
+          } else {
+            g.u[0] = ux; g.u[1] = uy; g.u[2] = uz;
+            g.cell[0] = db.cell_last0[s];
+            g.surface = -g.surface;
+            g.n_coord = 1;
+            if (!find_cell_inner(g, lost_outer)) {
+              mark_lost(s);
+              wgt = 0.0;
+            }
+          }
+        } else {
+          // neighbour search at the crossing level, then from the root
+          if (!find_cell_inner(g, lost_outer)) {
+            g.n_coord = 1;
+            if (!exhaustive_find_cell(g, lost_outer)) {
+              g.surface = SURFACE_NONE;
+              g.n_coord = 1;
+              g.r[0][0] = g.r[0][0] + TINY_BIT * g.u[0];
+              g.r[0][1] = g.r[0][1] + TINY_BIT * g.u[1];
+              g.r[0][2] = g.r[0][2] + TINY_BIT * g.u[2];
+              if (!exhaustive_find_cell(g, lost_outer)) {
+                mark_lost(s);
+                wgt = 0.0;
+              }
+            }
+          }
+        }
+      }
+      geo_store(g, s);
+      long long pid = db.id[s];
+      if (traced(pid)) {
+        TraceRec* rec = trace_slot(pid);
+        if (rec) {
+          rec->kind = 1;
+          rec->surface_or_nuclide = bsurf;
+          rec->wgt = wgt;
+        }
+        dq.trace_n[pid - 1] += 1;
+      }
+      to_next = revive_or_free(s, wgt);
+    }
+    warp_append(dq.q_tmp, &dq.cnt->n_next, static_cast<int>(s), to_next);
+  }
+}
+
+// src/physics.cpp:990-1041
+__device__ void sample_cxs_target_velocity(double awr, double E, const double* u, double kT,
+  unsigned long long& seed, double* vt_out)
+{
+  double beta_vn = sqrt(awr * E / kT);
+  double alpha = 1.0 / (1.0 + sqrt(PI) * beta_vn / 2.0);
+  double beta_vt_sq = 0.0;
+  double mu = 0.0;
+  for (int it = 0;; ++it) {
+    double r1 = prn(seed);
+    double r2 = prn(seed);
+    if (prn(seed) < alpha) {
+      beta_vt_sq = -log(r1 * r2);
+    } else {
+      double c = cos(PI / 2.0 * prn(seed));
+      beta_vt_sq = -log(r1) - log(r2) * c * c;
+    }
+    double beta_vt = sqrt(beta_vt_sq);
+    mu = uniform_distribution(-1., 1., seed);
+    double accept_prob = sqrt(beta_vn * beta_vn + beta_vt_sq - 2 * beta_vn * beta_vt * mu) / (beta_vn + beta_vt);
+    if (prn(seed) < accept_prob) break;
+    if (it > 1000000) {
+      set_error(ERR_REJECTION);
+      break;
+    }
+  }
+  double vt = sqrt(beta_vt_sq * kT / awr);
+  double x = u[0], y = u[1], z = u[2];
+  rotate_angle(x, y, z, mu, seed);
+  vt_out[0] = vt * x;
+  vt_out[1] = vt * y;
+  vt_out[2] = vt * z;
+}
+
+// src/physics.cpp:754-818 elastic scattering with free-gas target
+__device__ void elastic_scatter(int nuc, double& E, double* u, unsigned long long& seed)
+{
+  double vel = sqrt(E);
+  double awr = dm.awr[nuc];
+  double kT = dm.kT[nuc];
+  double vn[3] = {vel * u[0], vel * u[1], vel * u[2]};
+  double vt[3] = {0.0, 0.0, 0.0};
+  if (!(E >= 400.0 * kT && awr > 1.0)) sample_cxs_target_velocity(awr, E, u, kT, seed, vt);
+  double vcm[3];
+  for (int k = 0; k < 3; ++k) vcm[k] = (vn[k] + awr * vt[k]) / (awr + 1.0);
+  for (int k = 0; k < 3; ++k) vn[k] = vn[k] - vcm[k];
+  vel = sqrt(vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2]);
+  double mu_cm = uniform_distribution(-1., 1., seed);
+  double ucm[3] = {vn[0] / vel, vn[1] / vel, vn[2] / vel};
+  rotate_angle(ucm[0], ucm[1], ucm[2], mu_cm, seed);
+  for (int k = 0; k < 3; ++k) vn[k] = vel * ucm[k];
+  for (int k = 0; k < 3; ++k) vn[k] = vn[k] + vcm[k];
+  E = vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2];
+  vel = sqrt(E);
+  u[0] = vn[0] / vel;
+  u[1] = vn[1] / vel;
+  u[2] = vn[2] / vel;
+}
+
+// src/particle.cpp:331-415 + src/physics.cpp:43-168, 494-518, 638-752
+__global__ void __launch_bounds__(256) k_collision()
+{
+  const int n = dq.cnt->n_coll;
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    int i = base + threadIdx.x;
+    bool valid = i < n;
+    long long s = valid ? dq.q_coll[i] : 0;
+    bool to_next = false;
+    if (valid) {
+      double E = db.E[s];
+      double wgt = db.wgt[s];
+      unsigned long long seed = db.seed[s];
+      int mat = db.material[s];
+      double mt = db.macro_t[s];
+      db.surface[s] = SURFACE_NONE;
+      db.n_collision[s] += 1;
+      // sample_nuclide: CDF over atom_density * micro total in material order
+      double cutoff = prn(seed) * mt;
+      int a = 0, b = 0;
+      if (mat >= 0 && mat < dm.n_mat) {
+        a = dm.mat_off[mat];
+        b = dm.mat_off[mat + 1];
+      }
+      int i_log = log_union_index(E);
+      int chosen = -1;
+      double m_tot = 0, m_abs = 0, m_el = 0;
+      if (!dm.xs_fp32) {
+        double prob = 0.0;
+        for (int k = a; k < b; ++k) {
+          int nuc = dm.mat_nuc[k];
+          Micro m = micro_xs64(nuc, i_log, E);
+          prob += dm.mat_dens[k] * m.total;
+          if (prob >= cutoff) {
+            chosen = nuc;
+            m_tot = m.total;
+            m_abs = m.absorption;
+            const double4* xs = dm.xs64 + dm.nuc_off[nuc];
+            m_el = (1.0 - m.f) * xs[m.i_grid].z + m.f * xs[m.i_grid + 1].z;
+            break;
+          }
+        }
+      } else {
+        float prob = 0.0f;
+        for (int k = a; k < b; ++k) {
+          int nuc = dm.mat_nuc[k];
+          float t, ab, f32;
+          int ig;
+          micro_xs32(nuc, i_log, E, t, ab, ig, f32);
+          prob += dm.mat_dens32[k] * t;
+          if (static_cast<double>(prob) >= cutoff) {
+            chosen = nuc;
+            m_tot = t;
+            m_abs = ab;
+            const float4* xs = dm.xs32 + dm.nuc_off[nuc];
+            m_el = (1.0f - f32) * xs[ig].z + f32 * xs[ig + 1].z;
+            break;
+          }
+        }
+      }
+      double u[3] = {db.ux[s], db.uy[s], db.uz[s]};
+      if (chosen < 0) {
+        set_error(ERR_NO_NUCLIDE);
+        wgt = 0.0;
+      } else {
+        // absorption (analog) src/physics.cpp:638-672
+        if (m_abs > 0.0) {
+          if (m_abs > prn(seed) * m_tot) wgt = 0.0;
+        }
+        if (wgt != 0.0) {
+          // scatter src/physics.cpp:674-752: cutoff drawn, elastic for MT2
+          double c2 = prn(seed) * (m_tot - m_abs);
+          (void)c2;
+          (void)m_el;
+          elastic_scatter(chosen, E, u, seed);
+          if (dm.ww_on) {
+            double r[3] = {db.rx[s], db.ry[s], db.rz[s]};
+            apply_weight_windows(s, wgt, seed, r, u, E, SURFACE_NONE);
+          }
+          if (E < dm.energy_cutoff) wgt = 0.0;
+        }
+      }
+      db.E[s] = E;
+      db.wgt[s] = wgt;
+      db.seed[s] = seed;
+      db.ux[s] = u[0]; db.uy[s] = u[1]; db.uz[s] = u[2];
+      db.material_last[s] = C_NONE;
+      long long pid = db.id[s];
+      if (traced(pid)) {
+        TraceRec* rec = trace_slot(pid);
+        if (rec) {
+          rec->kind = 2;
+          rec->surface_or_nuclide = chosen;
+          rec->wgt = wgt;
+        }
+        dq.trace_n[pid - 1] += 1;
+      }
+      to_next = revive_or_free(s, wgt);
+    }
+    warp_append(dq.q_tmp, &dq.cnt->n_next, static_cast<int>(s), to_next);
+  }
+}
+
+__global__ void k_refill_plan()
+{
+  DCounters* c = dq.cnt;
+  long long remaining = dm.n_particles - c->next_source + 1;
+  if (remaining < 0) remaining = 0;
+  long long k = c->n_free < remaining ? c->n_free : remaining;
+  c->refill_k = static_cast<int>(k);
+  c->refill_free_base = c->n_free - static_cast<int>(k);
+  c->refill_src = c->next_source;
+  c->n_free -= static_cast<int>(k);
+  c->next_source += k;
+  c->n_surf = 0;
+  c->n_coll = 0;
+}
+
+__global__ void __launch_bounds__(256) k_refill()
+{
+  const int k = dq.cnt->refill_k;
+  const int fb = dq.cnt->refill_free_base;
+  const long long src = dq.cnt->refill_src;
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x; base < k; base += stride) {
+    int j = base + threadIdx.x;
+    bool valid = j < k;
+    int s = valid ? dq.free_list[fb + j] : 0;
+    if (valid) initialize_history(s, src + j);
+    warp_append(dq.q_tmp, &dq.cnt->n_next, s, valid);
+  }
+}
+
+// Counting sort of the next cross-section queue by (material, energy octave)
+__device__ __forceinline__ int sort_key(int s)
+{
+  int mat = db.material[s] + 1;
+  long long bits = __double_as_longlong(db.E[s]);
+  int ex = static_cast<int>((bits >> 52) & 0x7ff) - 1023 + 32;
+  ex = ex < 0 ? 0 : (ex > 63 ? 63 : ex);
+  return mat * 64 + ex;
+}
+
+__global__ void k_sort_hist()
+{
+  const int n = dq.cnt->n_next;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    atomicAdd(&dq.hist[sort_key(dq.q_tmp[i])], 1);
+}
+
+__global__ void k_sort_scan()
+{
+  // single block: exclusive scan of hist into cursor, hist cleared
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int nk = dq.sort_keys;
+  for (int base = 0; base < nk; base += blockDim.x) {
+    int i = base + threadIdx.x;
+    int v = i < nk ? dq.hist[i] : 0;
+    // block inclusive scan via warp shuffles
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    __shared__ int wsum[32];
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    if (w == 0) {
+      int t = lane < (blockDim.x >> 5) ? wsum[lane] : 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, t, o);
+        if (lane >= o) t += y;
+      }
+      wsum[lane] = t;
+    }
+    __syncthreads();
+    int incl = x + (w > 0 ? wsum[w - 1] : 0) + carry;
+    if (i < nk) {
+      dq.cursor[i] = incl - v;
+      dq.hist[i] = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = incl;
+    __syncthreads();
+  }
+}
+
+__global__ void k_sort_scatter()
+{
+  const int n = dq.cnt->n_next;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    int s = dq.q_tmp[i];
+    int pos = atomicAdd(&dq.cursor[sort_key(s)], 1);
+    dq.q_in[pos] = s;
+  }
+}
+
+__global__ void k_copy_queue()
+{
+  const int n = dq.cnt->n_next;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    dq.q_in[i] = dq.q_tmp[i];
+}
+
+__global__ void k_finish_iter(cudaGraphConditionalHandle handle)
+{
+  DCounters* c = dq.cnt;
+  c->n_events += static_cast<unsigned long long>(c->n_q);
+  c->n_q = c->n_next;
+  c->n_next = 0;
+  c->iter += 1;
+  bool more = c->n_q > 0 || c->next_source <= dm.n_particles;
+  if (c->error != 0) more = false;
+  if (c->iter >= c->max_iter) {
+    if (more) c->error |= ERR_ITERATIONS;
+    more = false;
+  }
+  cudaGraphSetConditional(handle, more ? 1u : 0u);
+}
+
+// Tally::accumulate (src/tallies/tally.cpp:821-880)
+__global__ void k_accumulate(double* value, double* sum, double* sum_sq, long long n, double norm)
+{
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    double val = value[i] * norm;
+    value[i] = 0.0;
+    sum[i] += val;
+    sum_sq[i] += val * val;
+  }
+}
+
+// ======================================================= host-side driver
+#define CK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess) {                                                              \
+      throw std::runtime_error(std::string("CUDA error ") + cudaGetErrorString(e_) +      \
+                               " at " + __FILE__ + ":" + std::to_string(__LINE__));       \
+    }                                                                                     \
+  } while (0)
+
+template<class T>
+T* dev_upload(const std::vector<T>& v, std::vector<void*>& owned)
+{
+  if (v.empty()) return nullptr;
+  T* p = nullptr;
+  CK(cudaMalloc(&p, v.size() * sizeof(T)));
+  CK(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  owned.push_back(p);
+  return p;
+}
+
+template<class T>
+T* dev_alloc(size_t n, std::vector<void*>& owned)
+{
+  if (n == 0) n = 1;
+  T* p = nullptr;
+  CK(cudaMalloc(&p, n * sizeof(T)));
+  CK(cudaMemset(p, 0, n * sizeof(T)));
+  owned.push_back(p);
+  return p;
+}
+
+struct GpuSim {
+  std::vector<void*> owned;
+  DModel model {};
+  DBank bank {};
+  DQueues queues {};
+  DCounters* cnt = nullptr;
+  double *d_value = nullptr, *d_sum = nullptr, *d_sumsq = nullptr;
+  long long n_values = 0;
+  std::vector<long long> tally_off;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr;
+  int blocks = 1216;
+  int sort = 1;
+  bool tallies_dirty = true;
+  float last_batch_ms = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // weight windows on device (one set)
+  double *d_ww_lower = nullptr, *d_ww_upper = nullptr, *d_ww_e = nullptr;
+  long long ww_size = 0;
+
+  ~GpuSim()
+  {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (stream) cudaStreamDestroy(stream);
+    for (void* p : owned) cudaFree(p);
+  }
+};
+
+static void build_model(GpuSim& G, const HModel& m, const GpuOptions& opt)
+{
+  auto& own = G.owned;
+  DModel& d = G.model;
+  // geometry
+  std::vector<DSurface> surf(m.surfaces.size());
+  for (size_t k = 0; k < surf.size(); ++k) {
+    for (int j = 0; j < 4; ++j) surf[k].c[j] = m.surfaces[k].c[j];
+    surf[k].type = m.surfaces[k].type;
+    surf[k].bc = m.surfaces[k].bc;
+  }
+  std::vector<DCell> cells(m.cells.size());
+  std::vector<int> tok;
+  for (size_t k = 0; k < cells.size(); ++k) {
+    const HCell& c = m.cells[k];
+    for (int j = 0; j < 3; ++j) cells[k].tr[j] = c.tr[j];
+    cells[k].universe = c.universe;
+    cells[k].fill_type = c.fill_type;
+    cells[k].fill = c.fill;
+    cells[k].tok_off = static_cast<int>(tok.size());
+    cells[k].tok_len = static_cast<int>(c.expr.size());
+    cells[k].simple = c.simple ? 1 : 0;
+    tok.insert(tok.end(), c.expr.begin(), c.expr.end());
+  }
+  std::vector<int> univ_off {0}, univ_cells;
+  for (const auto& u : m.universes) {
+    univ_cells.insert(univ_cells.end(), u.begin(), u.end());
+    univ_off.push_back(static_cast<int>(univ_cells.size()));
+  }
+  std::vector<DLattice> lats(m.lattices.size());
+  std::vector<int> lat_univ;
+  for (size_t k = 0; k < lats.size(); ++k) {
+    const HLattice& l = m.lattices[k];
+    for (int j = 0; j < 3; ++j) {
+      lats[k].ll[j] = l.ll[j];
+      lats[k].pitch[j] = l.pitch[j];
+      lats[k].n[j] = l.n[j];
+    }
+    lats[k].is3d = l.is3d;
+    lats[k].outer = l.outer;
+    lats[k].univ_off = static_cast<int>(lat_univ.size());
+    lat_univ.insert(lat_univ.end(), l.univ.begin(), l.univ.end());
+  }
+  d.surf = dev_upload(surf, own);
+  d.cell = dev_upload(cells, own);
+  d.tok = dev_upload(tok, own);
+  d.univ_off = dev_upload(univ_off, own);
+  d.univ_cells = dev_upload(univ_cells, own);
+  d.lat = dev_upload(lats, own);
+  d.lat_univ = dev_upload(lat_univ, own);
+  d.n_surf = static_cast<int>(surf.size());
+  d.n_cell = static_cast<int>(cells.size());
+  d.n_univ = static_cast<int>(m.universes.size());
+  d.n_lat = static_cast<int>(lats.size());
+  d.root_univ = m.root_universe;
+  d.n_coord_levels = m.n_coord_levels;
+  if (m.n_coord_levels > MAXL) throw std::runtime_error("geometry nests deeper than the supported coordinate levels");
+
+  // nuclear data: energies FP64, rows (total, absorption, elastic, 0)
+  std::vector<long long> nuc_off {0};
+  std::vector<double> energy, awr, kT;
+  std::vector<double4> xs64;
+  std::vector<float4> xs32;
+  std::vector<int> grid_index;
+  for (const auto& n : m.nuclides) {
+    energy.insert(energy.end(), n.energy.begin(), n.energy.end());
+    for (size_t k = 0; k < n.energy.size(); ++k) {
+      xs64.push_back(make_double4(n.total[k], n.absorption[k], n.elastic[k], 0.0));
+      xs32.push_back(make_float4(static_cast<float>(n.total[k]), static_cast<float>(n.absorption[k]),
+        static_cast<float>(n.elastic[k]), 0.0f));
+    }
+    nuc_off.push_back(static_cast<long long>(energy.size()));
+    grid_index.insert(grid_index.end(), n.grid_index.begin(), n.grid_index.end());
+    awr.push_back(n.awr);
+    kT.push_back(n.kT);
+  }
+  d.xs_fp32 = opt.xs_fp32 ? 1 : 0;
+  d.nuc_off = dev_upload(nuc_off, own);
+  d.energy = dev_upload(energy, own);
+  d.xs64 = d.xs_fp32 ? nullptr : dev_upload(xs64, own);
+  d.xs32 = d.xs_fp32 ? dev_upload(xs32, own) : nullptr;
+  d.grid_index = dev_upload(grid_index, own);
+  d.awr = dev_upload(awr, own);
+  d.kT = dev_upload(kT, own);
+  std::vector<int> mat_off {0}, mat_nuc, mat_id;
+  std::vector<double> mat_dens;
+  std::vector<float> mat_dens32;
+  for (const auto& mt : m.materials) {
+    mat_nuc.insert(mat_nuc.end(), mt.nuclide.begin(), mt.nuclide.end());
+    mat_dens.insert(mat_dens.end(), mt.atom_density.begin(), mt.atom_density.end());
+    for (double v : mt.atom_density) mat_dens32.push_back(static_cast<float>(v));
+    mat_off.push_back(static_cast<int>(mat_nuc.size()));
+    mat_id.push_back(mt.id);
+  }
+  d.mat_off = dev_upload(mat_off, own);
+  d.mat_nuc = dev_upload(mat_nuc, own);
+  d.mat_dens = dev_upload(mat_dens, own);
+  d.mat_dens32 = dev_upload(mat_dens32, own);
+  d.mat_id = dev_upload(mat_id, own);
+  std::vector<int> cell_id;
+  for (const auto& c : m.cells) cell_id.push_back(c.id);
+  d.cell_id = dev_upload(cell_id, own);
+  d.n_nuc = static_cast<int>(m.nuclides.size());
+  d.n_mat = static_cast<int>(m.materials.size());
+  d.M = m.n_log_bins;
+  d.e_min = m.energy_min;
+  d.e_max = m.energy_max;
+  d.log_spacing = m.log_spacing;
+
+  // source
+  const HSource& src = m.source;
+  d.sp_type = src.sp_type;
+  d.an_type = src.an_type;
+  d.en_type = src.en_type;
+  d.dom_type = src.dom_type;
+  for (size_t k = 0; k < src.sp.size() && k < 6; ++k) d.sp[k] = src.sp[k];
+  for (int k = 0; k < 3; ++k) d.uref[k] = src.uref[k];
+  if (src.en_type == 1) {
+    d.en_x[0] = src.en[0];
+    d.n_en = 1;
+  } else {
+    size_t n = src.en.size() / 2;
+    if (n < 1 || n > 8) throw std::runtime_error("discrete source energies: 1 to 8 values are supported");
+    d.n_en = static_cast<int>(n);
+    // alias table, src/distribution.cpp:23-80 (Vose)
+    std::vector<double> prob(src.en.begin() + n, src.en.end());
+    double integral = 0.0;
+    for (double p : prob) integral += p;
+    for (double& p : prob) p /= integral;
+    std::vector<size_t> large, small;
+    std::vector<int> alias(n, 0);
+    for (size_t i = 0; i < n; i++) {
+      prob[i] *= n;
+      if (prob[i] > 1.0) large.push_back(i);
+      else small.push_back(i);
+    }
+    while (!large.empty() && !small.empty()) {
+      int j = static_cast<int>(small.back());
+      int k = static_cast<int>(large.back());
+      small.pop_back();
+      prob[k] += prob[j] - 1.0;
+      alias[j] = k;
+      if (prob[k] < 1.0) {
+        small.push_back(k);
+        large.pop_back();
+      }
+    }
+    for (size_t i = 0; i < n; ++i) {
+      d.en_x[i] = src.en[i];
+      d.en_prob[i] = prob[i];
+      d.en_alias[i] = alias[i];
+    }
+  }
+  d.n_dom = static_cast<int>(src.dom_ids.size());
+  d.dom_ids = dev_upload(src.dom_ids, own);
+
+  // meshes, filters, tallies
+  std::vector<DMesh> meshes(m.meshes.size());
+  for (size_t k = 0; k < meshes.size(); ++k) {
+    for (int j = 0; j < 3; ++j) {
+      meshes[k].ll[j] = m.meshes[k].ll[j];
+      meshes[k].width[j] = m.meshes[k].width[j];
+      meshes[k].shape[j] = m.meshes[k].shape[j];
+    }
+    meshes[k].ndim = m.meshes[k].ndim;
+  }
+  std::vector<DFilter> filts(m.filters.size());
+  std::vector<double> ebins;
+  for (size_t k = 0; k < filts.size(); ++k) {
+    filts[k].type = m.filters[k].type;
+    filts[k].mesh = m.filters[k].mesh;
+    filts[k].nbins = m.filters[k].nbins;
+    filts[k].e_off = static_cast<int>(ebins.size());
+    ebins.insert(ebins.end(), m.filters[k].bins.begin(), m.filters[k].bins.end());
+  }
+  std::vector<DTally> tallies(m.tallies.size());
+  long long off = 0;
+  G.tally_off.clear();
+  for (size_t k = 0; k < tallies.size(); ++k) {
+    const HTally& t = m.tallies[k];
+    tallies[k].value_off = off;
+    tallies[k].nfilt = static_cast<int>(t.filters.size());
+    tallies[k].nscore = static_cast<int>(t.scores.size());
+    if (tallies[k].nscore > 4) throw std::runtime_error("at most four scores per tally are supported");
+    for (int j = 0; j < tallies[k].nfilt; ++j) {
+      tallies[k].filt[j] = t.filters[j];
+      tallies[k].stride[j] = t.strides[j];
+    }
+    for (int j = 0; j < tallies[k].nscore; ++j) tallies[k].score[j] = t.scores[j];
+    G.tally_off.push_back(off);
+    off += t.n_filter_bins * static_cast<long long>(t.scores.size());
+  }
+  G.tally_off.push_back(off);
+  G.n_values = off;
+  d.mesh = dev_upload(meshes, own);
+  d.filt = dev_upload(filts, own);
+  d.ebins = dev_upload(ebins, own);
+  d.tally = dev_upload(tallies, own);
+  d.n_tally = static_cast<int>(tallies.size());
+  G.d_value = dev_alloc<double>(off, own);
+  G.d_sum = dev_alloc<double>(off, own);
+  G.d_sumsq = dev_alloc<double>(off, own);
+  d.value = G.d_value;
+
+  // weight windows (first set)
+  d.ww_on = 0;
+  if (!m.weight_windows.empty()) {
+    const HWeightWindows& w = m.weight_windows[0];
+    d.ww_mesh = w.mesh;
+    d.ww_ne = static_cast<int>(w.ebounds.size()) - 1;
+    G.d_ww_e = dev_upload(w.ebounds, own);
+    G.d_ww_lower = dev_upload(w.lower, own);
+    G.d_ww_upper = dev_upload(w.upper, own);
+    G.ww_size = static_cast<long long>(w.lower.size());
+    d.ww_e = G.d_ww_e;
+    d.ww_lower = G.d_ww_lower;
+    d.ww_upper = G.d_ww_upper;
+    d.ww_surv = w.survival_ratio;
+    d.ww_mlb = w.max_lb_ratio;
+    d.ww_cut = w.weight_cutoff;
+    d.ww_max_split = w.max_split;
+    d.ww_on = m.ww_on ? 1 : 0;
+  }
+  d.max_history_splits = m.max_history_splits;
+  d.energy_cutoff = m.energy_cutoff;
+  d.max_events = m.max_particle_events;
+  d.n_particles = m.n_particles;
+  d.master_seed = m.seed;
+  d.stride = m.stride;
+}
+
+static void build_bank(GpuSim& G, long long cap, long long sec_cap)
+{
+  auto& own = G.owned;
+  DBank& b = G.bank;
+  b.cap = cap;
+  b.id = dev_alloc<long long>(cap, own);
+  b.seed = dev_alloc<unsigned long long>(cap, own);
+  b.E = dev_alloc<double>(cap, own);
+  b.wgt = dev_alloc<double>(cap, own);
+  b.wgt_born = dev_alloc<double>(cap, own);
+  b.wgt_ww_born = dev_alloc<double>(cap, own);
+  b.ww_factor = dev_alloc<double>(cap, own);
+  b.ux = dev_alloc<double>(cap, own);
+  b.uy = dev_alloc<double>(cap, own);
+  b.uz = dev_alloc<double>(cap, own);
+  b.rx = dev_alloc<double>(cap * MAXL, own);
+  b.ry = dev_alloc<double>(cap * MAXL, own);
+  b.rz = dev_alloc<double>(cap * MAXL, own);
+  b.cell = dev_alloc<int>(cap * MAXL, own);
+  b.univ = dev_alloc<int>(cap * MAXL, own);
+  b.latt = dev_alloc<int>(cap * MAXL, own);
+  b.lix = dev_alloc<int>(cap * MAXL, own);
+  b.liy = dev_alloc<int>(cap * MAXL, own);
+  b.liz = dev_alloc<int>(cap * MAXL, own);
+  b.n_coord = dev_alloc<int>(cap, own);
+  b.cell_last0 = dev_alloc<int>(cap, own);
+  b.cell_born = dev_alloc<int>(cap, own);
+  b.surface = dev_alloc<int>(cap, own);
+  b.material = dev_alloc<int>(cap, own);
+  b.material_last = dev_alloc<int>(cap, own);
+  b.macro_t = dev_alloc<double>(cap, own);
+  b.macro_a = dev_alloc<double>(cap, own);
+  b.bdist = dev_alloc<double>(cap, own);
+  b.dcoll = dev_alloc<double>(cap, own);
+  b.bsurf = dev_alloc<int>(cap, own);
+  b.blevel = dev_alloc<int>(cap, own);
+  b.btrans = dev_alloc<int>(cap, own);
+  b.n_event = dev_alloc<int>(cap, own);
+  b.n_collision = dev_alloc<int>(cap, own);
+  b.n_split = dev_alloc<int>(cap, own);
+  b.sec_top = dev_alloc<int>(cap, own);
+  DQueues& q = G.queues;
+  q.q_in = dev_alloc<int>(cap, own);
+  q.q_surf = dev_alloc<int>(cap, own);
+  q.q_coll = dev_alloc<int>(cap, own);
+  q.q_tmp = dev_alloc<int>(cap, own);
+  q.free_list = dev_alloc<int>(cap, own);
+  q.sort_keys = (G.model.n_mat + 1) * 64;
+  q.hist = dev_alloc<int>(q.sort_keys, own);
+  q.cursor = dev_alloc<int>(q.sort_keys, own);
+  q.sec = dev_alloc<DSecondary>(sec_cap, own);
+  G.cnt = dev_alloc<DCounters>(1, own);
+  q.cnt = G.cnt;
+  q.trace = nullptr;
+  q.trace_n = nullptr;
+  q.trace_hist = 0;
+  q.trace_cap = 0;
+  q.batch = 1;
+  DCounters c {};
+  c.sec_cap = static_cast<int>(sec_cap);
+  c.max_iter = 1 << 20;
+  CK(cudaMemcpy(G.cnt, &c, sizeof(c), cudaMemcpyHostToDevice));
+}
+
+static void upload_constants(GpuSim& G)
+{
+  CK(cudaMemcpyToSymbol(dm, &G.model, sizeof(DModel)));
+  CK(cudaMemcpyToSymbol(db, &G.bank, sizeof(DBank)));
+  CK(cudaMemcpyToSymbol(dq, &G.queues, sizeof(DQueues)));
+}
+
+static void build_graph(GpuSim& G)
+{
+  if (G.exec) {
+    cudaGraphExecDestroy(G.exec);
+    G.exec = nullptr;
+  }
+  if (G.graph) {
+    cudaGraphDestroy(G.graph);
+    G.graph = nullptr;
+  }
+  cudaGraph_t graph;
+  CK(cudaGraphCreate(&graph, 0));
+  cudaGraphConditionalHandle handle;
+  CK(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
+  const int nb = G.blocks, nt = 256;
+  // prologue
+  CK(cudaStreamBeginCaptureToGraph(G.stream, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  k_batch_init<<<nb, nt, 0, G.stream>>>(0);
+  CK(cudaStreamEndCapture(G.stream, &graph));
+  size_t n_nodes = 0;
+  CK(cudaGraphGetNodes(graph, nullptr, &n_nodes));
+  std::vector<cudaGraphNode_t> nodes(n_nodes);
+  CK(cudaGraphGetNodes(graph, nodes.data(), &n_nodes));
+  // conditional while node
+  cudaGraphNodeParams cp {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = handle;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t cond;
+  CK(cudaGraphAddNode(&cond, graph, nodes.data(), nullptr, n_nodes, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  CK(cudaStreamBeginCaptureToGraph(G.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  k_xs<<<nb, nt, 0, G.stream>>>();
+  k_advance<<<nb, nt, 0, G.stream>>>();
+  k_surface<<<nb, nt, 0, G.stream>>>();
+  k_collision<<<nb, nt, 0, G.stream>>>();
+  k_refill_plan<<<1, 1, 0, G.stream>>>();
+  k_refill<<<nb, nt, 0, G.stream>>>();
+  if (G.sort) {
+    k_sort_hist<<<nb, nt, 0, G.stream>>>();
+    k_sort_scan<<<1, 1024, 0, G.stream>>>();
+    k_sort_scatter<<<nb, nt, 0, G.stream>>>();
+  } else {
+    k_copy_queue<<<nb, nt, 0, G.stream>>>();
+  }
+  k_finish_iter<<<1, 1, 0, G.stream>>>(handle);
+  CK(cudaStreamEndCapture(G.stream, &body));
+  CK(cudaGraphInstantiate(&G.exec, graph, 0));
+  G.graph = graph;
+}
+
+GpuSim* gpu_create(const HModel& m, const GpuOptions& opt)
+{
+  auto* G = new GpuSim();
+  try {
+    CK(cudaSetDevice(0));
+    CK(cudaStreamCreateWithFlags(&G->stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&G->ev0));
+    CK(cudaEventCreate(&G->ev1));
+    G->sort = opt.sort ? 1 : 0;
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
+    G->blocks = sms * 8;
+    build_model(*G, m, opt);
+    long long cap = opt.in_flight > 0 ? opt.in_flight : 1 << 21;
+    if (cap > m.n_particles) cap = m.n_particles;
+    if (cap < 1) cap = 1;
+    long long sec_cap = opt.secondary_cap;
+    if (sec_cap <= 0) sec_cap = m.ww_on || !m.weight_windows.empty() ? cap * 16 : 1024;
+    if (sec_cap > (1LL << 31) - 1) sec_cap = (1LL << 31) - 1;
+    build_bank(*G, cap, sec_cap);
+    upload_constants(*G);
+    build_graph(*G);
+    CK(cudaStreamSynchronize(G->stream));
+  } catch (...) {
+    delete G;
+    throw;
+  }
+  return G;
+}
+
+void gpu_destroy(GpuSim* G) { delete G; }
+
+void gpu_set_trace(GpuSim* G, long long n_hist, int cap)
+{
+  if (n_hist <= 0) {
+    G->queues.trace = nullptr;
+    G->queues.trace_n = nullptr;
+    G->queues.trace_hist = 0;
+  } else {
+    G->queues.trace = dev_alloc<TraceRec>(static_cast<size_t>(n_hist) * cap, G->owned);
+    G->queues.trace_n = dev_alloc<int>(n_hist, G->owned);
+    G->queues.trace_hist = n_hist;
+    G->queues.trace_cap = cap;
+  }
+  CK(cudaMemcpyToSymbol(dq, &G->queues, sizeof(DQueues)));
+}
+
+void gpu_get_trace(GpuSim* G, void* rec, int* counts)
+{
+  long long n = G->queues.trace_hist;
+  if (n <= 0) return;
+  CK(cudaMemcpy(rec, G->queues.trace, sizeof(TraceRec) * n * G->queues.trace_cap, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(counts, G->queues.trace_n, sizeof(int) * n, cudaMemcpyDeviceToHost));
+}
+
+BatchStats gpu_run_batch(GpuSim* G, HModel& m, int batch, bool accumulate)
+{
+  G->queues.batch = batch;
+  CK(cudaMemcpyToSymbolAsync(dq, &G->queues, sizeof(DQueues), 0, cudaMemcpyHostToDevice, G->stream));
+  CK(cudaEventRecord(G->ev0, G->stream));
+  CK(cudaGraphLaunch(G->exec, G->stream));
+  CK(cudaEventRecord(G->ev1, G->stream));
+  BatchStats st {};
+  DCounters c {};
+  CK(cudaMemcpyAsync(&c, G->cnt, sizeof(c), cudaMemcpyDeviceToHost, G->stream));
+  CK(cudaStreamSynchronize(G->stream));
+  CK(cudaEventElapsedTime(&st.ms, G->ev0, G->ev1));
+  st.error = c.error;
+  st.n_lost = c.n_lost;
+  st.lost_id = c.lost_id;
+  st.n_done = c.n_done;
+  st.iterations = c.iter;
+  st.total_weight = c.total_weight;
+  st.leakage = c.leakage;
+  st.n_events = c.n_events;
+  st.n_secondaries = c.n_sec;
+  if (accumulate) {
+    double norm = m.source.strength / (static_cast<double>(m.n_particles) * 1);
+    if (G->n_values > 0) {
+      k_accumulate<<<G->blocks, 256, 0, G->stream>>>(G->d_value, G->d_sum, G->d_sumsq, G->n_values, norm);
+      CK(cudaGetLastError());
+    }
+    for (auto& t : m.tallies) t.n_realizations += 1;
+    G->tallies_dirty = true;
+  }
+  CK(cudaStreamSynchronize(G->stream));
+  return st;
+}
+
+void gpu_fetch_tallies(GpuSim* G, HModel& m)
+{
+  if (!G->tallies_dirty) return;
+  std::vector<double> sum(G->n_values), sq(G->n_values), val(G->n_values);
+  if (G->n_values > 0) {
+    CK(cudaMemcpy(sum.data(), G->d_sum, sizeof(double) * G->n_values, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(sq.data(), G->d_sumsq, sizeof(double) * G->n_values, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(val.data(), G->d_value, sizeof(double) * G->n_values, cudaMemcpyDeviceToHost));
+  }
+  for (size_t t = 0; t < m.tallies.size(); ++t) {
+    long long o = G->tally_off[t];
+    long long n = G->tally_off[t + 1] - o;
+    auto& r = m.tallies[t].results;
+    for (long long k = 0; k < n; ++k) {
+      r[3 * k] = val[o + k];
+      r[3 * k + 1] = sum[o + k];
+      r[3 * k + 2] = sq[o + k];
+    }
+  }
+  G->tallies_dirty = false;
+}
+
+void gpu_reset_tallies(GpuSim* G, HModel& m)
+{
+  if (G->n_values > 0) {
+    CK(cudaMemset(G->d_value, 0, sizeof(double) * G->n_values));
+    CK(cudaMemset(G->d_sum, 0, sizeof(double) * G->n_values));
+    CK(cudaMemset(G->d_sumsq, 0, sizeof(double) * G->n_values));
+  }
+  for (auto& t : m.tallies) {
+    t.n_realizations = 0;
+    std::fill(t.results.begin(), t.results.end(), 0.0);
+  }
+  G->tallies_dirty = false;
+}
+
+void gpu_set_ww_bounds(GpuSim* G, const double* lower, const double* upper, long long n)
+{
+  if (n != G->ww_size) throw std::runtime_error("weight-window bounds have the wrong size");
+  CK(cudaMemcpy(G->d_ww_lower, lower, sizeof(double) * n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(G->d_ww_upper, upper, sizeof(double) * n, cudaMemcpyHostToDevice));
+}
+
+void gpu_set_ww_on(GpuSim* G, bool on)
+{
+  if (on && !G->d_ww_lower) throw std::runtime_error("no weight windows are defined");
+  G->model.ww_on = on ? 1 : 0;
+  CK(cudaMemcpyToSymbol(dm, &G->model, sizeof(DModel)));
+}
+
+long long gpu_capacity(GpuSim* G) { return G->bank.cap; }
+
+}  // namespace omc

@@ -1,0 +1,45 @@
+// Host interface of the GPU transport layer (implemented in transport.cu).
+#pragma once
+
+#include "host_model.h"
+
+namespace omc {
+
+// device error flags (bitwise OR in the batch counters)
+constexpr int ERR_LOST = 1, ERR_SECONDARY_OVERFLOW = 2, ERR_NO_NUCLIDE = 4,
+              ERR_ITERATIONS = 8, ERR_REJECTION = 16, ERR_TRACE = 32;
+
+struct GpuSim;
+
+struct GpuOptions {
+  long long in_flight = 0;      // particle slots in HBM (0: min(n_particles, 2^21))
+  long long secondary_cap = 0;  // secondary-site pool entries (0: automatic)
+  bool xs_fp32 = false;         // FP32 cross-section tables and interpolation
+  bool sort = true;             // sort the cross-section queue by (material, energy)
+};
+
+struct BatchStats {
+  float ms = 0;
+  int error = 0;
+  int n_lost = 0;
+  long long lost_id = 0;
+  long long n_done = 0;
+  int iterations = 0;
+  double total_weight = 0;
+  double leakage = 0;
+  unsigned long long n_events = 0;
+  int n_secondaries = 0;
+};
+
+GpuSim* gpu_create(const HModel& m, const GpuOptions& opt);
+void gpu_destroy(GpuSim* g);
+BatchStats gpu_run_batch(GpuSim* g, HModel& m, int batch, bool accumulate);
+void gpu_fetch_tallies(GpuSim* g, HModel& m);
+void gpu_reset_tallies(GpuSim* g, HModel& m);
+void gpu_set_trace(GpuSim* g, long long n_hist, int cap);
+void gpu_get_trace(GpuSim* g, void* records, int* counts);
+void gpu_set_ww_bounds(GpuSim* g, const double* lower, const double* upper, long long n);
+void gpu_set_ww_on(GpuSim* g, bool on);
+long long gpu_capacity(GpuSim* g);
+
+}  // namespace omc

@@ -86,6 +86,7 @@ def log_grid(n_points: int, rng: np.random.Generator,
     interior = e[1:-1] * (1.0 + jitter * (2.0 * rng.random(n_points - 2) - 1.0))
     interior = np.clip(interior, e_min * (1 + 1e-12), e_max * (1 - 1e-12))
     e[1:-1] = np.sort(interior)
+    e[0], e[-1] = e_min, e_max
     return e
 
 
@@ -268,7 +269,8 @@ def make_xsbench(n_nuc: int = 68, n_points: int = 11303, seed: int = 42,
         mat_nuc.extend(int(v) for v in idx)
         mat_dens.extend(rng.uniform(1e-5, 5e-2, cnt))
         mat_off.append(len(mat_nuc))
-    w = np.asarray(_XSBENCH_MAT_WEIGHTS) * rng.uniform(0.9, 1.1, len(mat_counts))
+    base = np.resize(np.asarray(_XSBENCH_MAT_WEIGHTS), len(mat_counts))
+    w = base * rng.uniform(0.9, 1.1, len(mat_counts))
     return XSBenchData(energy=energy, xs=xs,
                        mat_nuc=np.asarray(mat_nuc, np.int32),
                        mat_off=np.asarray(mat_off, np.int32),

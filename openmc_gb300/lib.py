@@ -1,0 +1,459 @@
+"""ctypes bindings to ``libopenmc_gb300.so`` mirroring ``openmc.lib``.
+
+The reference's ``openmc.lib`` (``openmc/lib/core.py``, ``tally.py``,
+``weight_windows.py``, ``settings.py``, ``error.py``) loads ``libopenmc.so``
+with ``CDLL``, declares argtypes/restype per C function, maps negative return
+codes to exception classes through ``openmc_err_msg``, and exposes settings as
+``_DLLGlobal`` descriptors over exported C globals.  This module does the same
+for the GB300 library; the function names and argument meanings follow the
+reference so that code written against ``openmc.lib`` runs unchanged for the
+event-based fixed-source path.
+
+The library is required: importing this module raises if the CUDA library is
+missing or cannot be loaded (there is no CPU fallback).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import warnings
+from contextlib import contextmanager
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+_LIB = _build.LIB
+if not _LIB.exists():
+    raise ImportError(
+        f"{_LIB} is missing: build it with `python -m openmc_gb300.build` "
+        "(nvcc, sm_103a); the GB300 library has no CPU fallback")
+_dll = C.CDLL(str(_LIB))
+
+
+# ------------------------------------------------------------- exceptions
+class OpenMCError(Exception):
+    """Root exception (openmc/exceptions.py)."""
+
+
+class AllocationError(OpenMCError):
+    pass
+
+
+class OutOfBoundsError(OpenMCError):
+    pass
+
+
+class InvalidArgumentError(OpenMCError):
+    pass
+
+
+class InvalidTypeError(OpenMCError):
+    pass
+
+
+class InvalidIDError(OpenMCError):
+    pass
+
+
+class GeometryError(OpenMCError):
+    pass
+
+
+class DataError(OpenMCError):
+    pass
+
+
+class PhysicsError(OpenMCError):
+    pass
+
+
+def _error_handler(err, func, args):
+    """Raise according to the error code (openmc/lib/error.py:8-41)."""
+    def code(name):
+        return C.c_int.in_dll(_dll, name).value
+    msg = (C.c_char * 256).in_dll(_dll, "openmc_err_msg").value.decode()
+    if err == code("OPENMC_E_ALLOCATE"):
+        raise AllocationError(msg)
+    elif err == code("OPENMC_E_OUT_OF_BOUNDS"):
+        raise OutOfBoundsError(msg)
+    elif err == code("OPENMC_E_INVALID_ARGUMENT"):
+        raise InvalidArgumentError(msg)
+    elif err == code("OPENMC_E_INVALID_TYPE"):
+        raise InvalidTypeError(msg)
+    if err == code("OPENMC_E_INVALID_ID"):
+        raise InvalidIDError(msg)
+    elif err == code("OPENMC_E_GEOMETRY"):
+        raise GeometryError(msg)
+    elif err == code("OPENMC_E_DATA"):
+        raise DataError(msg)
+    elif err == code("OPENMC_E_PHYSICS"):
+        raise PhysicsError(msg)
+    elif err == code("OPENMC_E_WARNING"):
+        warnings.warn(msg)
+    elif err < 0:
+        raise OpenMCError(msg or f"Unknown error encountered (code {err}).")
+    return err
+
+
+def _fn(name, argtypes, restype=C.c_int, check=True):
+    f = getattr(_dll, name)
+    f.argtypes = argtypes
+    f.restype = restype
+    if check and restype is C.c_int:
+        f.errcheck = _error_handler
+    return f
+
+
+_p = C.POINTER
+_fn("openmc_init", [C.c_int, _p(C.c_char_p), C.c_void_p])
+_fn("openmc_run", [])
+_fn("openmc_simulation_init", [])
+_fn("openmc_simulation_finalize", [])
+_fn("openmc_next_batch", [_p(C.c_int)])
+_fn("openmc_finalize", [])
+_fn("openmc_reset", [])
+_fn("openmc_hard_reset", [])
+_fn("openmc_reset_timers", [])
+_fn("openmc_get_seed", [], C.c_int64)
+_fn("openmc_set_seed", [C.c_int64], None)
+_fn("openmc_get_stride", [], C.c_uint64)
+_fn("openmc_set_stride", [C.c_uint64], None)
+_fn("openmc_tally_results", [C.c_int32, _p(_p(C.c_double)), _p(C.c_size_t)])
+_fn("openmc_get_tally_index", [C.c_int32, _p(C.c_int32)])
+_fn("openmc_tally_get_id", [C.c_int32, _p(C.c_int32)])
+_fn("openmc_tally_get_n_realizations", [C.c_int32, _p(C.c_int32)])
+_fn("openmc_global_tallies", [_p(_p(C.c_double))])
+_fn("tallies_size", [], C.c_size_t)
+_fn("openmc_weight_windows_size", [], C.c_size_t)
+_fn("openmc_get_weight_windows_index", [C.c_int32, _p(C.c_int32)])
+_fn("openmc_weight_windows_get_id", [C.c_int32, _p(C.c_int32)])
+_fn("openmc_weight_windows_get_bounds", [C.c_int32, _p(_p(C.c_double)), _p(_p(C.c_double)), _p(C.c_size_t)])
+_fn("openmc_weight_windows_set_bounds", [C.c_int32, _p(C.c_double), _p(C.c_double), C.c_size_t])
+_fn("openmc_weight_windows_get_energy_bounds", [C.c_int32, _p(_p(C.c_double)), _p(C.c_size_t)])
+_fn("openmc_weight_windows_update_magic", [C.c_int32, C.c_int32, C.c_char_p, C.c_double, C.c_double])
+_fn("openmc_weight_windows_get_mesh", [C.c_int32, _p(C.c_int32)])
+_fn("openmc_gb300_last_batch", [_p(C.c_double)])
+_fn("openmc_gb300_timing", [_p(C.c_double)])
+_fn("openmc_gb300_set_trace", [C.c_int64, C.c_int])
+_fn("openmc_gb300_get_trace", [C.c_void_p, _p(C.c_int32)])
+_fn("openmc_gb300_set_weight_windows_on", [C.c_int])
+_fn("openmc_gb300_model_info", [_p(C.c_int64)])
+_fn("openmc_gb300_xs_tables_create", [C.c_int, C.c_int, _p(C.c_double), _p(C.c_double), C.c_int,
+                                      _p(C.c_int32), _p(C.c_int32), _p(C.c_double), C.c_int, C.c_int,
+                                      C.c_int64, _p(C.c_void_p)])
+_fn("openmc_gb300_xs_tables_free", [C.c_void_p])
+_fn("openmc_gb300_xs_lookup", [C.c_void_p, C.c_int64, _p(C.c_int32), _p(C.c_double), _p(C.c_double),
+                               _p(C.c_int32), C.c_int])
+_fn("openmc_gb300_xs_lookup_device", [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_int])
+_fn("openmc_gb300_xs_last_times", [C.c_void_p, _p(C.c_float)])
+_fn("openmc_gb300_xs_stream", [C.c_void_p, _p(C.c_void_p)])
+
+
+# ------------------------------------------------------------- globals
+class _DLLGlobal:
+    """Data descriptor over an exported C global (openmc/lib/core.py:724-735)."""
+
+    def __init__(self, ctype, name):
+        self.ctype, self.name = ctype, name
+
+    def __get__(self, instance, owner):
+        return self.ctype.in_dll(_dll, self.name).value
+
+    def __set__(self, instance, value):
+        self.ctype.in_dll(_dll, self.name).value = value
+
+
+class _Settings:
+    """openmc.lib.settings subset (openmc/lib/settings.py:27-44)."""
+    event_based = _DLLGlobal(C.c_bool, "event_based")
+    particles = _DLLGlobal(C.c_int64, "n_particles")
+    inactive = _DLLGlobal(C.c_int32, "n_inactive")
+    generations_per_batch = _DLLGlobal(C.c_int32, "gen_per_batch")
+    max_lost_particles = _DLLGlobal(C.c_int32, "max_lost_particles")
+    rel_max_lost_particles = _DLLGlobal(C.c_double, "rel_max_lost_particles")
+    run_CE = _DLLGlobal(C.c_bool, "run_CE")
+    verbosity = _DLLGlobal(C.c_int, "verbosity")
+    weight_windows_on = _DLLGlobal(C.c_bool, "weight_windows_on")
+    restart_run = _DLLGlobal(C.c_bool, "restart_run")
+    # GB300 extensions
+    xs_fp32 = _DLLGlobal(C.c_int, "openmc_gb300_xs_fp32")
+    particles_in_flight = _DLLGlobal(C.c_int64, "openmc_gb300_in_flight")
+    sort_queue = _DLLGlobal(C.c_int, "openmc_gb300_sort")
+
+    @property
+    def seed(self):
+        return _dll.openmc_get_seed()
+
+    @seed.setter
+    def seed(self, v):
+        _dll.openmc_set_seed(int(v))
+
+    @property
+    def stride(self):
+        return _dll.openmc_get_stride()
+
+    @stride.setter
+    def stride(self, v):
+        _dll.openmc_set_stride(int(v))
+
+
+settings = _Settings()
+
+
+def current_batch():
+    return C.c_int.in_dll(_dll, "current_batch").value
+
+
+def is_initialized():
+    return C.c_bool.in_dll(_dll, "initialized").value
+
+
+# ------------------------------------------------------------- lifecycle
+def init(args=None, intracomm=None, output=True, directory=None):
+    """Initialise from the model in ``directory`` (or the working directory)."""
+    argv = ["openmc"] + [str(a) for a in (args or [])]
+    if directory is not None:
+        argv.append(str(directory))
+    arr = (C.c_char_p * len(argv))(*[a.encode() for a in argv])
+    _dll.openmc_init(len(argv), arr, None)
+
+
+def finalize():
+    _dll.openmc_finalize()
+
+
+def run(output=True):
+    _dll.openmc_run()
+
+
+def simulation_init():
+    _dll.openmc_simulation_init()
+
+
+def simulation_finalize():
+    _dll.openmc_simulation_finalize()
+
+
+def next_batch():
+    status = C.c_int()
+    _dll.openmc_next_batch(C.byref(status))
+    return status.value
+
+
+def reset():
+    _dll.openmc_reset()
+
+
+def hard_reset():
+    _dll.openmc_hard_reset()
+
+
+@contextmanager
+def run_in_memory(**kwargs):
+    init(**kwargs)
+    try:
+        yield
+    finally:
+        finalize()
+
+
+# ------------------------------------------------------------- tallies
+def tally_index(tally_id):
+    idx = C.c_int32()
+    _dll.openmc_get_tally_index(int(tally_id), C.byref(idx))
+    return idx.value
+
+
+def tally_results(tally_id):
+    """Borrowed view of the results array [bins, scores, 3] (VALUE, SUM, SUM_SQ)."""
+    ptr = _p(C.c_double)()
+    shape = (C.c_size_t * 3)()
+    _dll.openmc_tally_results(tally_index(tally_id), C.byref(ptr), shape)
+    n = shape[0] * shape[1] * shape[2]
+    return np.ctypeslib.as_array(ptr, shape=(n,)).reshape(shape[0], shape[1], shape[2])
+
+
+def tally_ids():
+    """Ids of all tallies in library order (openmc/lib/tally.py:440-460)."""
+    out = []
+    for k in range(_dll.tallies_size()):
+        v = C.c_int32()
+        _dll.openmc_tally_get_id(k, C.byref(v))
+        out.append(v.value)
+    return out
+
+
+def tally_n_realizations(tally_id):
+    n = C.c_int32()
+    _dll.openmc_tally_get_n_realizations(tally_index(tally_id), C.byref(n))
+    return n.value
+
+
+def tally_mean_std(tally_id):
+    """Mean and standard deviation of the mean (openmc/tallies.py:528-566)."""
+    r = tally_results(tally_id)
+    n = tally_n_realizations(tally_id)
+    s, s2 = r[..., 1], r[..., 2]
+    mean = s / n
+    if n > 1:
+        std = np.sqrt(np.maximum(s2 / n - mean * mean, 0.0) / (n - 1))
+    else:
+        std = np.zeros_like(mean)
+    return mean, std
+
+
+def global_tallies():
+    ptr = _p(C.c_double)()
+    _dll.openmc_global_tallies(C.byref(ptr))
+    return np.ctypeslib.as_array(ptr, shape=(12,)).reshape(4, 3).copy()
+
+
+# --------------------------------------------------------- weight windows
+class WeightWindows:
+    """openmc.lib.WeightWindows subset (openmc/lib/weight_windows.py)."""
+
+    def __init__(self, index):
+        self._index = index
+
+    @classmethod
+    def from_id(cls, ww_id):
+        idx = C.c_int32()
+        _dll.openmc_get_weight_windows_index(int(ww_id), C.byref(idx))
+        return cls(idx.value)
+
+    @property
+    def id(self):
+        v = C.c_int32()
+        _dll.openmc_weight_windows_get_id(self._index, C.byref(v))
+        return v.value
+
+    @property
+    def bounds(self):
+        lo, up = _p(C.c_double)(), _p(C.c_double)()
+        n = C.c_size_t()
+        _dll.openmc_weight_windows_get_bounds(self._index, C.byref(lo), C.byref(up), C.byref(n))
+        return (np.ctypeslib.as_array(lo, shape=(n.value,)).copy(),
+                np.ctypeslib.as_array(up, shape=(n.value,)).copy())
+
+    @bounds.setter
+    def bounds(self, lu):
+        lower = np.ascontiguousarray(lu[0], dtype=np.float64).ravel()
+        upper = np.ascontiguousarray(lu[1], dtype=np.float64).ravel()
+        _dll.openmc_weight_windows_set_bounds(self._index, lower.ctypes.data_as(_p(C.c_double)),
+                                              upper.ctypes.data_as(_p(C.c_double)), lower.size)
+
+    @property
+    def energy_bounds(self):
+        ptr = _p(C.c_double)()
+        n = C.c_size_t()
+        _dll.openmc_weight_windows_get_energy_bounds(self._index, C.byref(ptr), C.byref(n))
+        return np.ctypeslib.as_array(ptr, shape=(n.value,)).copy()
+
+    def update_magic(self, tally_index, value="mean", threshold=1.0, ratio=5.0):
+        _dll.openmc_weight_windows_update_magic(self._index, int(tally_index), value.encode(),
+                                                float(threshold), float(ratio))
+
+
+def weight_windows_size():
+    return _dll.openmc_weight_windows_size()
+
+
+def set_weight_windows_on(on):
+    _dll.openmc_gb300_set_weight_windows_on(1 if on else 0)
+
+
+# ---------------------------------------------------- GB300 extensions
+TRACE_DTYPE = np.dtype([("kind", "<i4"), ("cell", "<i4"), ("material", "<i4"),
+                        ("surface_or_nuclide", "<i4"), ("grid_hash", "<i4"),
+                        ("n_coord", "<i4"), ("E", "<f8"), ("dist", "<f8"),
+                        ("wgt", "<f8")])
+
+
+def set_trace(n_hist, cap=256):
+    """Record per-event traces for particle ids 1..n_hist of each batch."""
+    _dll.openmc_gb300_set_trace(int(n_hist), int(cap))
+    set_trace._shape = (int(n_hist), int(cap))
+
+
+def get_trace():
+    n, cap = set_trace._shape
+    rec = np.zeros((n, cap), dtype=TRACE_DTYPE)
+    cnt = np.zeros(n, dtype=np.int32)
+    _dll.openmc_gb300_get_trace(rec.ctypes.data_as(C.c_void_p), cnt.ctypes.data_as(_p(C.c_int32)))
+    return rec, cnt
+
+
+def last_batch():
+    out = (C.c_double * 8)()
+    _dll.openmc_gb300_last_batch(out)
+    keys = ("ms", "iterations", "events", "total_weight", "leakage", "lost", "done", "secondaries")
+    return dict(zip(keys, list(out)))
+
+
+def timing():
+    out = (C.c_double * 5)()
+    _dll.openmc_gb300_timing(out)
+    keys = ("time_active", "time_inactive", "time_wall_active", "calculation_rate", "in_flight")
+    return dict(zip(keys, list(out)))
+
+
+def loaded_library():
+    return str(_LIB)
+
+
+class XSTables:
+    """Device tables for the macroscopic-XS lookup microbenchmark."""
+
+    def __init__(self, data, n_log_bins=8000, fp32=False, max_lookups=0):
+        n_nuc, G = data.energy.shape
+        e = np.ascontiguousarray(data.energy, np.float64)
+        x = np.ascontiguousarray(data.xs, np.float64)
+        mo = np.ascontiguousarray(data.mat_off, np.int32)
+        mn = np.ascontiguousarray(data.mat_nuc, np.int32)
+        md = np.ascontiguousarray(data.mat_dens, np.float64)
+        h = C.c_void_p()
+        _dll.openmc_gb300_xs_tables_create(n_nuc, G, e.ctypes.data_as(_p(C.c_double)),
+                                           x.ctypes.data_as(_p(C.c_double)), len(mo) - 1,
+                                           mo.ctypes.data_as(_p(C.c_int32)), mn.ctypes.data_as(_p(C.c_int32)),
+                                           md.ctypes.data_as(_p(C.c_double)), n_log_bins, 1 if fp32 else 0,
+                                           int(max_lookups), C.byref(h))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            _dll.openmc_gb300_xs_tables_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def lookup(self, mats, energies, sort=True, grid_hash=True):
+        mats = np.ascontiguousarray(mats, np.int32)
+        e = np.ascontiguousarray(energies, np.float64)
+        out = np.empty((len(e), 5))
+        gh = np.empty(len(e), np.int32) if grid_hash else None
+        _dll.openmc_gb300_xs_lookup(self.h, len(e), mats.ctypes.data_as(_p(C.c_int32)),
+                                    e.ctypes.data_as(_p(C.c_double)), out.ctypes.data_as(_p(C.c_double)),
+                                    gh.ctypes.data_as(_p(C.c_int32)) if gh is not None else None,
+                                    1 if sort else 0)
+        return out, gh
+
+    def lookup_device(self, n, d_mat, d_E, d_out, d_hash=None, sort=True):
+        """Device pointers (ints) in, asynchronous on the library stream."""
+        _dll.openmc_gb300_xs_lookup_device(self.h, int(n), d_mat, d_E, d_out, d_hash, 1 if sort else 0)
+
+    def last_times(self):
+        ms = (C.c_float * 2)()
+        _dll.openmc_gb300_xs_last_times(self.h, ms)
+        return float(ms[0]), float(ms[1])
+
+    def stream(self):
+        s = C.c_void_p()
+        _dll.openmc_gb300_xs_stream(self.h, C.byref(s))
+        return s.value

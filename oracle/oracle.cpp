@@ -23,6 +23,9 @@
 //    search of the universe, which is what is done here;
 //  * regions with unions are evaluated in postfix form; the truth value equals
 //    the reference's infix short-circuit scan (src/cell.cpp:973-1020);
+//  * the hash bin int(log(E/E_min)/spacing) (src/material.cpp:833) is clamped
+//    to [0, M-1]; the reference indexes grid_index[M+1], one past the table,
+//    when E equals the grid maximum exactly;
 //  * an elastic-only nuclide whose cutoff lands above its elastic cross
 //    section by rounding (physics.cpp:709-724, probability ~1e-16) scatters
 //    elastically instead of entering the inelastic branch with no reactions.
@@ -974,6 +977,7 @@ void material_calculate_xs(Sim& S, Particle& p)
   p.macro_absorption = 0.0;
   const Material& mat = S.materials[p.material];
   int i_grid = std::log(p.E / S.energy_min) / S.log_spacing;
+  i_grid = std::min(std::max(i_grid, 0), S.n_log_bins - 1);
   uint32_t h = 0;
   for (size_t i = 0; i < mat.nuclide.size(); ++i) {
     int i_nuclide = mat.nuclide[i];
@@ -2240,6 +2244,7 @@ void oracle_xsb_lookup(void* xv, int64_t n, const int32_t* mat, const double* Ei
     double E = Ein[k];
     int m = mat[k];
     int i_log = std::log(E / x->e_min) / x->log_spacing;
+    i_log = std::min(std::max(i_log, 0), x->M - 1);
     double macro[5] = {0, 0, 0, 0, 0};
     uint32_t h = 0;
     for (int j = x->mat_off[m]; j < x->mat_off[m + 1]; ++j) {

@@ -167,6 +167,7 @@ struct DQueues {
   int* trace_n;
   long long trace_hist;
   int trace_cap;
+  int trace_batch;  // batch whose histories are traced
   int batch;
   int sort_keys;
 };

@@ -58,7 +58,7 @@ __device__ __forceinline__ void warp_append(int* q, int* counter, int val, bool 
 
 __device__ __forceinline__ bool traced(long long id)
 {
-  return dq.trace != nullptr && id >= 1 && id <= dq.trace_hist;
+  return dq.trace != nullptr && dq.batch == dq.trace_batch && id >= 1 && id <= dq.trace_hist;
 }
 
 __device__ __forceinline__ TraceRec* trace_slot(long long id)
@@ -1505,6 +1505,7 @@ void gpu_set_trace(GpuSim* G, long long n_hist, int cap)
     G->queues.trace_n = dev_alloc<int>(n_hist, G->owned);
     G->queues.trace_hist = n_hist;
     G->queues.trace_cap = cap;
+    G->queues.trace_batch = 1;
   }
   CK(cudaMemcpyToSymbol(dq, &G->queues, sizeof(DQueues)));
 }

@@ -101,6 +101,7 @@ int openmc_weight_windows_get_mesh(int32_t index, int32_t* mesh_idx);
 extern int openmc_gb300_xs_fp32;
 extern int64_t openmc_gb300_in_flight;
 extern int openmc_gb300_sort;
+extern int openmc_gb300_trace_batch;
 
 /* last batch: [ms, iterations, events, total_weight, leakage, lost, done, secondaries] */
 int openmc_gb300_last_batch(double* out);

@@ -69,6 +69,7 @@ bool UWUW_ENABLED = false;
 int openmc_gb300_xs_fp32 = -1;          // -1: from XML (<gb300_xs_precision>), else 0/1
 int64_t openmc_gb300_in_flight = 0;     // particle slots; 0: setting or automatic
 int openmc_gb300_sort = 1;              // sort the XS queue by (material, energy)
+int openmc_gb300_trace_batch = 1;       // batch whose histories openmc_gb300_set_trace records
 }
 
 namespace {
@@ -352,7 +353,7 @@ int openmc_simulation_init()
     opt.sort = openmc_gb300_sort != 0;
     if (m.ww_on && m.weight_windows.empty()) return fail(OPENMC_E_INVALID_ARGUMENT, "weight windows are on but none are defined");
     s.gpu = gpu_create(m, opt);
-    if (s.trace_hist > 0) gpu_set_trace(s.gpu, s.trace_hist, s.trace_cap);
+    if (s.trace_hist > 0) gpu_set_trace(s.gpu, s.trace_hist, s.trace_cap, openmc_gb300_trace_batch);
     gpu_reset_tallies(s.gpu, m);
     std::fill(s.global_tallies.begin(), s.global_tallies.end(), 0.0);
     current_batch = 0;
@@ -687,7 +688,7 @@ int openmc_gb300_set_trace(int64_t n_hist, int cap)
   s.trace_hist = n_hist;
   s.trace_cap = cap;
   try {
-    if (s.gpu) gpu_set_trace(s.gpu, n_hist, cap);
+    if (s.gpu) gpu_set_trace(s.gpu, n_hist, cap, openmc_gb300_trace_batch);
   } catch (const std::exception& e) {
     return fail(OPENMC_E_ALLOCATE, e.what());
   }

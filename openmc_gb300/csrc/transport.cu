@@ -1494,7 +1494,7 @@ GpuSim* gpu_create(const HModel& m, const GpuOptions& opt)
 
 void gpu_destroy(GpuSim* G) { delete G; }
 
-void gpu_set_trace(GpuSim* G, long long n_hist, int cap)
+void gpu_set_trace(GpuSim* G, long long n_hist, int cap, int batch)
 {
   if (n_hist <= 0) {
     G->queues.trace = nullptr;
@@ -1505,7 +1505,7 @@ void gpu_set_trace(GpuSim* G, long long n_hist, int cap)
     G->queues.trace_n = dev_alloc<int>(n_hist, G->owned);
     G->queues.trace_hist = n_hist;
     G->queues.trace_cap = cap;
-    G->queues.trace_batch = 1;
+    G->queues.trace_batch = batch;
   }
   CK(cudaMemcpyToSymbol(dq, &G->queues, sizeof(DQueues)));
 }

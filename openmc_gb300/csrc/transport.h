@@ -36,7 +36,7 @@ void gpu_destroy(GpuSim* g);
 BatchStats gpu_run_batch(GpuSim* g, HModel& m, int batch, bool accumulate);
 void gpu_fetch_tallies(GpuSim* g, HModel& m);
 void gpu_reset_tallies(GpuSim* g, HModel& m);
-void gpu_set_trace(GpuSim* g, long long n_hist, int cap);
+void gpu_set_trace(GpuSim* g, long long n_hist, int cap, int batch);
 void gpu_get_trace(GpuSim* g, void* records, int* counts);
 void gpu_set_ww_bounds(GpuSim* g, const double* lower, const double* upper, long long n);
 void gpu_set_ww_on(GpuSim* g, bool on);

@@ -182,6 +182,7 @@ class _Settings:
     xs_fp32 = _DLLGlobal(C.c_int, "openmc_gb300_xs_fp32")
     particles_in_flight = _DLLGlobal(C.c_int64, "openmc_gb300_in_flight")
     sort_queue = _DLLGlobal(C.c_int, "openmc_gb300_sort")
+    trace_batch = _DLLGlobal(C.c_int, "openmc_gb300_trace_batch")
 
     @property
     def seed(self):

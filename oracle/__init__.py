@@ -50,7 +50,7 @@ def lib():
         L.oracle_create.restype = vp
         L.oracle_create.argtypes = [C.c_char_p, C.c_size_t, C.c_char_p, C.c_int]
         L.oracle_destroy.argtypes = [vp]
-        L.oracle_set_trace.argtypes = [vp, i64, C.c_int]
+        L.oracle_set_trace.argtypes = [vp, i64, C.c_int, C.c_int]
         L.oracle_trace_data.restype = vp
         L.oracle_trace_data.argtypes = [vp]
         L.oracle_trace_counts.restype = pi32
@@ -128,8 +128,8 @@ class Oracle:
             lib().oracle_destroy(self.h)
             self.h = None
 
-    def set_trace(self, n_hist, cap=256):
-        lib().oracle_set_trace(self.h, n_hist, cap)
+    def set_trace(self, n_hist, cap=256, batch=1):
+        lib().oracle_set_trace(self.h, n_hist, cap, batch)
         self._trace = (n_hist, cap)
 
     def transport(self, batch, first=1, count=None, mode=0, threads=1, in_flight=0):

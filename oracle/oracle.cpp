@@ -1966,6 +1966,7 @@ struct Handle {
   std::vector<int32_t> trace_n;
   int64_t trace_hist = 0;
   int trace_cap = 0;
+  int trace_batch = 1;
   std::string err;
 };
 
@@ -1990,9 +1991,10 @@ void* oracle_create(const uint8_t* blob, size_t n, char* err, int errlen)
 void oracle_destroy(void* h) { delete static_cast<Handle*>(h); }
 
 // Record per-event traces for the first n_hist particle ids of the next batch.
-void oracle_set_trace(void* hv, int64_t n_hist, int cap)
+void oracle_set_trace(void* hv, int64_t n_hist, int cap, int batch)
 {
   auto* h = static_cast<Handle*>(hv);
+  h->trace_batch = batch;
   h->trace_hist = n_hist;
   h->trace_cap = cap;
   h->trace.assign(static_cast<size_t>(n_hist) * cap, TraceRec {});
@@ -2027,7 +2029,7 @@ int oracle_transport(void* hv, int batch, int64_t first, int64_t count, int mode
           p.secondary_bank.clear();
           p.trace = nullptr;
           initialize_history(S, p, batch, i);
-          if (batch == 1 && i <= h->trace_hist) {
+          if (batch == h->trace_batch && i <= h->trace_hist) {
             p.trace = &h->trace[static_cast<size_t>(i - 1) * h->trace_cap];
             p.trace_cap = h->trace_cap;
             p.trace_n = 0;

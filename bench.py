@@ -1,0 +1,299 @@
+"""Benchmark of the event-based transport path on one GB300.
+
+Workload: the full-size 17x17 pin lattice (pitch 1.26 cm, pin r=0.41 cm,
+clad r=0.475 cm, 200 cm tall, reflective radial / vacuum axial boundaries;
+3 materials from 12 synthetic nuclides of 11,303 grid points; Maxwellian
+1.3 MeV source uniform in the pins; track-length flux on a 17x17x50 mesh x
+100 log-energy bins).  One step = one batch of 10^7 histories with FP32
+cross-section tables (FP64 geometry, energies, search keys and tallies).
+Seeded synthetic nuclides stand in for evaluated data (none exists here).
+
+Metric: particles/s = histories per batch / batch time (the reference's
+"Calculation Rate (active)", src/output.cpp:460-490).  `value` is timed on
+the device (CUDA events around the batch graph), with L2 flushed between
+steps; `e2e` is the same metric through the C API (openmc_next_batch +
+openmc_tally_results copying the tally arrays to host) on the host clock.
+
+--impl reference times the reference algorithm's CPU implementation (the
+oracle's restatement of OpenMC's event-based loop, OpenMP over all host
+cores) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particles/s (event-based transport, 17x17 lattice, FP32 XS tables)"
+WORKLOAD = "17x17 pin lattice, 12 nuclides x 11303 pts, flux 17x17x50 mesh x 100 E bins"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--particles", type=int, default=10_000_000)
+    ap.add_argument("--in-flight", type=int, default=0)
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-table extra measurement")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=0, help="histories in the CPU baseline sample")
+    return ap.parse_args()
+
+
+def model_dir(particles):
+    from openmc_gb300 import configs
+    d = ROOT / "_models" / f"lattice17_{particles}"
+    xml = d / "model.xml"
+    if not xml.exists():
+        m, _ = configs.lattice17(d, particles=particles, batches=1000)
+        m.export_to_model_xml(d)
+    return d
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (clocks, throttle reasons)."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu=0):
+        self.gpu = gpu
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([v.strip() for v in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[0]))
+                mx = float(s[1])
+                for k, n in enumerate(names):
+                    if s[3 + k].lower().startswith("active"):
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def flush_l2(buf):
+    import torch
+    buf.add_(1)  # writes 512 MB (> 129 MB L2)
+    torch.cuda.synchronize()
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def algorithmic_bytes(detail, levels, fp32):
+    """Bytes each kernel must move per batch (HBM layout)."""
+    row = 16 if fp32 else 32
+    dens = 4 if fp32 else 8
+    per_nuc = 8 + 16 + 2 * row + 4 + dens
+    ev = detail["events"]
+    b = {}
+    b["xs"] = ev * 36 + detail["xs_calc"] * 16 + detail["xs_nuclide_lookups"] * per_nuc
+    b["advance"] = ev * (136 + 72 * levels) + detail["mesh_segments"] * 16
+    b["surface"] = detail["surface"] * (120 + 96 * levels)
+    b["collision"] = detail["collision"] * 128 + detail["collision_nuclide_lookups"] * (per_nuc + row)
+    return b
+
+
+def run_gb300(args):
+    import torch
+    from openmc_gb300 import lib
+    path = model_dir(args.particles)
+    n = args.particles
+    out = {}
+    lib.init(directory=path)
+    try:
+        lib.settings.xs_fp32 = 1
+        lib.settings.particles_in_flight = args.in_flight
+        lib.simulation_init()
+        tid = lib.tally_ids()[0]
+        flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float64, device="cuda")
+        for _ in range(args.warmup):
+            lib.next_batch()
+        clocks = ClockSampler()
+        dev_ms, wall, iters = [], [], []
+        d2h = 0
+        clocks.start()
+        for _ in range(args.steps):
+            flush_l2(flush)
+            t0 = time.perf_counter()
+            lib.next_batch()
+            res = lib.tally_results(tid)
+            t1 = time.perf_counter()
+            d2h = res.nbytes + 256
+            lb = lib.last_batch()
+            dev_ms.append(lb["ms"])
+            iters.append(lb["iterations"])
+            wall.append(t1 - t0)
+        clk = clocks.stop()
+        detail_timed = lib.last_batch_detail()
+        # profiled batch (kernel by kernel, CUDA events) for the roofline
+        flush_l2(flush)
+        lib.settings.profile_next = 1
+        lib.next_batch()
+        prof = lib.last_batch_detail()
+        levels = 2
+        lib.simulation_finalize()
+    finally:
+        lib.finalize()
+    total_ms = sum(dev_ms)
+    value = args.steps * n / (total_ms / 1000.0)
+    e2e = args.steps * n / sum(wall)
+    kms = prof["kernel_ms"]
+    byts = algorithmic_bytes(prof, levels, True)
+    dom = max(("xs", "advance", "surface", "collision"), key=lambda k: kms[k])
+    peak, peak_kind = peaks()
+    achieved = byts[dom] / (kms[dom] * 1e-3) / 1e9
+    launches = sum(2 + 10 * int(i) for i in iters)
+    out.update(value=value, ms_per_step=total_ms / args.steps, e2e=e2e, e2e_d2h=d2h, clocks=clk,
+               launches=launches, dominant=dom, achieved=achieved, peak=peak, peak_kind=peak_kind,
+               kernel_ms=kms, bytes=byts, detail=detail_timed, profile=prof, iterations=iters)
+    if not args.no_fp64:
+        lib.init(directory=path)
+        try:
+            lib.settings.xs_fp32 = 0
+            lib.settings.particles_in_flight = args.in_flight
+            lib.simulation_init()
+            lib.next_batch()
+            flush_l2(flush)
+            lib.next_batch()
+            out["fp64_value"] = n / (lib.last_batch()["ms"] / 1000.0)
+            lib.simulation_finalize()
+        finally:
+            lib.finalize()
+    return out
+
+
+def cpu_baseline(path, sample, threads=None):
+    import oracle
+    o = oracle.Oracle(path / "model.xml")
+    threads = threads or os.cpu_count()
+    t0 = time.perf_counter()
+    o.transport(1, 1, sample, mode=1, threads=threads, in_flight=100000)
+    dt = time.perf_counter() - t0
+    return sample / dt, threads, dt
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    import __graft_entry__
+    if rank == 0:
+        __graft_entry__.build()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        dist.barrier()
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        path = model_dir(args.particles)
+        sample = args.cpu_sample or 20000
+        vals = []
+        cores = os.cpu_count()
+        for _ in range(args.warmup):
+            cpu_baseline(path, max(sample // 10, 1000), cores)
+        t_all = 0.0
+        for _ in range(args.steps):
+            v, cores, dt = cpu_baseline(path, sample, cores)
+            vals.append(v)
+            t_all += dt
+        value = args.steps * sample / t_all
+        line = {"metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * t_all / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded nuclides, full-size model)", "impl": "reference",
+                "config": {"workload": WORKLOAD, "histories_per_step": sample, "threads": cores},
+                "cpu_baseline": {"value": value, "unit": "particles/s", "cores": cores, "kind": "port",
+                                 "sample": f"{sample} histories of batch 1 per step, event-based OpenMP loop"},
+                "e2e": {"value": value, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+    import torch
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    r = run_gb300(args)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([r["ms_per_step"]], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        r["ms_per_step"] = float(t.item())
+        r["value"] = world * args.particles / (r["ms_per_step"] / 1000.0)
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        path = model_dir(args.particles)
+        sample = args.cpu_sample or 20000
+        v, cores, dt = cpu_baseline(path, sample)
+        cpu = {"value": v, "unit": "particles/s", "cores": cores, "kind": "port",
+               "sample": f"{sample} histories of the same model, event-based loop, OpenMP ({dt:.1f} s)"}
+    line = {
+        "metric": METRIC, "value": r["value"], "unit": "particles/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32-xs/f64-geometry",
+        "data": "synthetic (seeded nuclides, full-size model)",
+        "config": {"workload": WORKLOAD, "histories_per_step": args.particles,
+                   "l2": "flushed between steps (512 MB write)", "xs_tables": "fp32",
+                   "parallelism": "replicas" if args.gpus > 1 else "single GPU"},
+        "e2e": {"value": r["e2e"], "unit": "particles/s", "h2d_bytes_per_step": 256,
+                "d2h_bytes_per_step": r["e2e_d2h"]},
+        "gpu_launches": r["launches"],
+        "clocks": r["clocks"],
+        "roofline": {"bound": "hbm", "kernel": r["dominant"], "achieved": r["achieved"], "peak": r["peak"],
+                     "unit": "GB/s", "frac": r["achieved"] / r["peak"], "peak_source": r["peak_kind"],
+                     "traffic": None},
+        "cpu_baseline": cpu,
+        "kernel_ms_profiled_batch": r["kernel_ms"],
+        "fp64_xs_particles_per_s": r.get("fp64_value"),
+        "events_per_step": r["detail"]["events"],
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

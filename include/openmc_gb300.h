@@ -102,9 +102,17 @@ extern int openmc_gb300_xs_fp32;
 extern int64_t openmc_gb300_in_flight;
 extern int openmc_gb300_sort;
 extern int openmc_gb300_trace_batch;
+/* 1: run the next batch kernel by kernel (no graph) with CUDA events around
+ * each kernel; results are identical, per-kernel times land in
+ * openmc_gb300_last_batch_detail */
+extern int openmc_gb300_profile_next;
 
 /* last batch: [ms, iterations, events, total_weight, leakage, lost, done, secondaries] */
 int openmc_gb300_last_batch(double* out);
+/* [events, xs recomputations, xs nuclide lookups, surface events, collisions,
+ *  collision nuclide lookups, mesh segments, kernel ms: xs, advance, surface,
+ *  collision, refill, sort, other] */
+int openmc_gb300_last_batch_detail(double* out);
 /* [time_active s, time_inactive s, wall_active s, particles/s (active), in-flight slots] */
 int openmc_gb300_timing(double* out);
 /* per-event traces for particle ids 1..n_hist, cap records each (48-byte records) */

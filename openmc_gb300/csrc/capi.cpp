@@ -66,6 +66,7 @@ bool DAGMC_ENABLED = false;
 bool LIBMESH_ENABLED = false;
 bool UWUW_ENABLED = false;
 // GB300 extensions (no counterpart in the reference)
+int openmc_gb300_profile_next = 0;      // 1: run the next batch kernel by kernel with event timing
 int openmc_gb300_xs_fp32 = -1;          // -1: from XML (<gb300_xs_precision>), else 0/1
 int64_t openmc_gb300_in_flight = 0;     // particle slots; 0: setting or automatic
 int openmc_gb300_sort = 1;              // sort the XS queue by (material, energy)
@@ -386,7 +387,9 @@ int openmc_next_batch(int* status)
     ++current_batch;
     bool active = current_batch > m.n_inactive;
     auto t0 = std::chrono::steady_clock::now();
-    BatchStats st = gpu_run_batch(s.gpu, m, current_batch, active);
+    BatchStats st = openmc_gb300_profile_next ? gpu_run_batch_profiled(s.gpu, m, current_batch, active)
+                                              : gpu_run_batch(s.gpu, m, current_batch, active);
+    openmc_gb300_profile_next = 0;
     auto t1 = std::chrono::steady_clock::now();
     s.last = st;
     s.n_batches_run++;
@@ -666,6 +669,23 @@ int openmc_gb300_last_batch(double* out)
   out[5] = b.n_lost;
   out[6] = static_cast<double>(b.n_done);
   out[7] = b.n_secondaries;
+  return 0;
+}
+
+// [n_events, n_xs_calc, n_xs_nuclide_lookups, n_surface, n_collision,
+//  n_collision_nuclide_lookups, n_mesh_segments, kernel ms x7 (xs, advance,
+//  surface, collision, refill, sort, other)]
+int openmc_gb300_last_batch_detail(double* out)
+{
+  const BatchStats& b = S().last;
+  out[0] = static_cast<double>(b.n_events);
+  out[1] = static_cast<double>(b.n_xs_calc);
+  out[2] = static_cast<double>(b.n_xs_nuc);
+  out[3] = static_cast<double>(b.n_surf);
+  out[4] = static_cast<double>(b.n_coll);
+  out[5] = static_cast<double>(b.n_coll_nuc);
+  out[6] = static_cast<double>(b.n_segments);
+  for (int k = 0; k < 7; ++k) out[7 + k] = b.kernel_ms[k];
   return 0;
 }
 

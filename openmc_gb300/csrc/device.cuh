@@ -151,6 +151,9 @@ struct DCounters {
   double total_weight, leakage;
   unsigned long long n_events;
   long long lost_id;
+  // event statistics (for algorithmic-byte accounting)
+  unsigned long long n_xs_calc, n_xs_nuc, n_surf_tot, n_coll_tot, n_coll_nuc, n_segments, n_refill;
+  int more;  // set by the iteration epilogue when another iteration is needed
 };
 
 struct DQueues {

@@ -56,6 +56,13 @@ __device__ __forceinline__ void warp_append(int* q, int* counter, int val, bool 
   if (pred) q[base + __popc(m & ((1u << lane) - 1u))] = val;
 }
 
+// Adds v over the warp with one atomic; all 32 lanes must call it.
+__device__ __forceinline__ void warp_count(unsigned long long* ctr, unsigned v)
+{
+  unsigned sum = __reduce_add_sync(0xffffffffu, v);
+  if ((threadIdx.x & 31) == 0 && sum) atomicAdd(ctr, static_cast<unsigned long long>(sum));
+}
+
 __device__ __forceinline__ bool traced(long long id)
 {
   return dq.trace != nullptr && dq.batch == dq.trace_batch && id >= 1 && id <= dq.trace_hist;
@@ -176,10 +183,11 @@ __device__ void mesh_bins_crossed(const DMesh& m, const double* r0, const double
 
 // src/tallies/tally_scoring.cpp:2416-2541 + FilterBinIter :31-139 +
 // score_general_ce_nonanalog :578-1106 (flux, total, absorption)
-__device__ void score_tracklength(const double* r0, const double* r1, const double* u, double E_last,
+__device__ int score_tracklength(const double* r0, const double* r1, const double* u, double E_last,
   double wgt, double distance, double mt, double ma)
 {
   double flux = wgt * distance;
+  int n_seg = 0;
   for (int t = 0; t < dm.n_tally; ++t) {
     const DTally& T = dm.tally[t];
     long long base = 0;
@@ -213,14 +221,17 @@ __device__ void score_tracklength(const double* r0, const double* r1, const doub
     };
     if (mesh_slot < 0) {
       add(base, 1.0);
+      ++n_seg;
     } else {
       const DMesh& M = dm.mesh[dm.filt[T.filt[mesh_slot]].mesh];
       const long long stride = T.stride[mesh_slot];
       mesh_bins_crossed(M, r0, r1, u, [&](int bin, double frac) {
         add(base + bin * stride, 1. * frac);
+        ++n_seg;
       });
     }
   }
+  return n_seg;
 }
 
 // ------------------------------------------------------- weight windows
@@ -496,6 +507,9 @@ __global__ void k_batch_init(int batch)
     c->n_events = 0;
     c->error = 0;
     c->n_lost = 0;
+    c->n_xs_calc = c->n_xs_nuc = c->n_surf_tot = c->n_coll_tot = 0;
+    c->n_coll_nuc = c->n_segments = c->n_refill = 0;
+    c->more = 1;
   }
   (void)batch;
 }
@@ -504,52 +518,65 @@ __global__ void k_batch_init(int batch)
 __global__ void __launch_bounds__(256) k_xs()
 {
   const int n = dq.cnt->n_q;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    long long s = dq.q_in[i];
-    long long pid = db.id[s];
-    bool tr = traced(pid);
-    int lvl0 = db.n_coord[s] - 1;
-    int low_cell = db.cell[lvl0 * db.cap + s];
-    int material = db.material[s];
-    int material_last = db.material_last[s];
-    if (low_cell == C_NONE) {
-      Geo g;
-      geo_load(g, s);
-      bool lost_outer = false;
-      if (!exhaustive_find_cell(g, lost_outer)) {
-        mark_lost(s);
-        continue;
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    int i = base + threadIdx.x;
+    unsigned calc = 0, nuc = 0;
+    if (i < n) {
+      long long s = dq.q_in[i];
+      long long pid = db.id[s];
+      bool tr = traced(pid);
+      int lvl0 = db.n_coord[s] - 1;
+      int low_cell = db.cell[lvl0 * db.cap + s];
+      int material = db.material[s];
+      int material_last = db.material_last[s];
+      bool ok = true;
+      if (low_cell == C_NONE) {
+        Geo g;
+        geo_load(g, s);
+        bool lost_outer = false;
+        if (!exhaustive_find_cell(g, lost_outer)) {
+          mark_lost(s);
+          ok = false;
+        } else {
+          if (db.cell_born[s] == C_NONE) db.cell_born[s] = g.cell[g.n_coord - 1];
+          db.cell_last0[s] = g.cell[0];
+          geo_store(g, s);
+          material = g.material;
+          material_last = g.material_last;
+          low_cell = g.cell[g.n_coord - 1];
+        }
       }
-      if (db.cell_born[s] == C_NONE) db.cell_born[s] = g.cell[g.n_coord - 1];
-      db.cell_last0[s] = g.cell[0];
-      geo_store(g, s);
-      material = g.material;
-      material_last = g.material_last;
-      low_cell = g.cell[g.n_coord - 1];
-    }
-    uint32_t h = 0xffffffffu;
-    double E = db.E[s];
-    if (material != C_NONE) {
-      if (material != material_last || tr) {
-        double t, a;
-        h = material_xs(material, E, t, a);
-        db.macro_t[s] = t;
-        db.macro_a[s] = a;
-      }
-    } else {
-      db.macro_t[s] = 0.0;
-      db.macro_a[s] = 0.0;
-    }
-    if (tr) {
-      TraceRec* rec = trace_slot(pid);
-      if (rec) {
-        rec->cell = low_cell;
-        rec->material = material;
-        rec->grid_hash = static_cast<int32_t>(h);
-        rec->n_coord = db.n_coord[s];
-        rec->E = E;
+      if (ok) {
+        uint32_t h = 0xffffffffu;
+        double E = db.E[s];
+        if (material != C_NONE) {
+          if (material != material_last || tr) {
+            double t, a;
+            h = material_xs(material, E, t, a);
+            db.macro_t[s] = t;
+            db.macro_a[s] = a;
+            calc = 1;
+            nuc = dm.mat_off[material + 1] - dm.mat_off[material];
+          }
+        } else {
+          db.macro_t[s] = 0.0;
+          db.macro_a[s] = 0.0;
+        }
+        if (tr) {
+          TraceRec* rec = trace_slot(pid);
+          if (rec) {
+            rec->cell = low_cell;
+            rec->material = material;
+            rec->grid_hash = static_cast<int32_t>(h);
+            rec->n_coord = db.n_coord[s];
+            rec->E = E;
+          }
+        }
       }
     }
+    warp_count(&dq.cnt->n_xs_calc, calc);
+    warp_count(&dq.cnt->n_xs_nuc, nuc);
   }
 }
 
@@ -563,6 +590,7 @@ __global__ void __launch_bounds__(256) k_advance()
     bool valid = i < n;
     long long s = valid ? dq.q_in[i] : 0;
     bool to_surf = false, to_coll = false, to_next = false;
+    unsigned n_seg = 0;
     if (valid) {
       double wgt = db.wgt[s];
       if (wgt == 0.0) {
@@ -587,7 +615,7 @@ __global__ void __launch_bounds__(256) k_advance()
           g.r[l][1] = g.r[l][1] + distance * g.u[1];
           g.r[l][2] = g.r[l][2] + distance * g.u[2];
         }
-        if (dm.n_tally > 0) score_tracklength(r0, g.r[0], g.u, db.E[s], wgt, distance, mt, db.macro_a[s]);
+        if (dm.n_tally > 0) n_seg = score_tracklength(r0, g.r[0], g.u, db.E[s], wgt, distance, mt, db.macro_a[s]);
         wgt = db.wgt[s];
         if (distance == INFTY) {
           wgt = 0.0;
@@ -622,6 +650,7 @@ __global__ void __launch_bounds__(256) k_advance()
     warp_append(dq.q_surf, &dq.cnt->n_surf, static_cast<int>(s), to_surf);
     warp_append(dq.q_coll, &dq.cnt->n_coll, static_cast<int>(s), to_coll);
     warp_append(dq.q_tmp, &dq.cnt->n_next, static_cast<int>(s), to_next);
+    warp_count(&dq.cnt->n_segments, n_seg);
   }
 }
 
@@ -818,6 +847,7 @@ __global__ void __launch_bounds__(256) k_collision()
     bool valid = i < n;
     long long s = valid ? dq.q_coll[i] : 0;
     bool to_next = false;
+    unsigned n_nuc_looked = 0;
     if (valid) {
       double E = db.E[s];
       double wgt = db.wgt[s];
@@ -840,6 +870,7 @@ __global__ void __launch_bounds__(256) k_collision()
         double prob = 0.0;
         for (int k = a; k < b; ++k) {
           int nuc = dm.mat_nuc[k];
+          ++n_nuc_looked;
           Micro m = micro_xs64(nuc, i_log, E);
           prob += dm.mat_dens[k] * m.total;
           if (prob >= cutoff) {
@@ -855,6 +886,7 @@ __global__ void __launch_bounds__(256) k_collision()
         float prob = 0.0f;
         for (int k = a; k < b; ++k) {
           int nuc = dm.mat_nuc[k];
+          ++n_nuc_looked;
           float t, ab, f32;
           int ig;
           micro_xs32(nuc, i_log, E, t, ab, ig, f32);
@@ -909,6 +941,7 @@ __global__ void __launch_bounds__(256) k_collision()
       to_next = revive_or_free(s, wgt);
     }
     warp_append(dq.q_tmp, &dq.cnt->n_next, static_cast<int>(s), to_next);
+    warp_count(&dq.cnt->n_coll_nuc, n_nuc_looked);
   }
 }
 
@@ -923,6 +956,9 @@ __global__ void k_refill_plan()
   c->refill_src = c->next_source;
   c->n_free -= static_cast<int>(k);
   c->next_source += k;
+  c->n_surf_tot += static_cast<unsigned long long>(c->n_surf);
+  c->n_coll_tot += static_cast<unsigned long long>(c->n_coll);
+  c->n_refill += static_cast<unsigned long long>(k);
   c->n_surf = 0;
   c->n_coll = 0;
 }
@@ -1016,7 +1052,7 @@ __global__ void k_copy_queue()
     dq.q_in[i] = dq.q_tmp[i];
 }
 
-__global__ void k_finish_iter(cudaGraphConditionalHandle handle)
+__device__ bool finish_iter_common()
 {
   DCounters* c = dq.cnt;
   c->n_events += static_cast<unsigned long long>(c->n_q);
@@ -1029,8 +1065,18 @@ __global__ void k_finish_iter(cudaGraphConditionalHandle handle)
     if (more) c->error |= ERR_ITERATIONS;
     more = false;
   }
+  c->more = more ? 1 : 0;
+  return more;
+}
+
+__global__ void k_finish_iter(cudaGraphConditionalHandle handle)
+{
+  bool more = finish_iter_common();
   cudaGraphSetConditional(handle, more ? 1u : 0u);
 }
+
+// same epilogue for the profiled (graph-free) batch loop
+__global__ void k_finish_iter_host() { finish_iter_common(); }
 
 // Tally::accumulate (src/tallies/tally.cpp:821-880)
 __global__ void k_accumulate(double* value, double* sum, double* sum_sq, long long n, double norm)
@@ -1518,6 +1564,36 @@ void gpu_get_trace(GpuSim* G, void* rec, int* counts)
   CK(cudaMemcpy(counts, G->queues.trace_n, sizeof(int) * n, cudaMemcpyDeviceToHost));
 }
 
+static void fill_stats(const DCounters& c, BatchStats& st)
+{
+  st.error = c.error;
+  st.n_lost = c.n_lost;
+  st.lost_id = c.lost_id;
+  st.n_done = c.n_done;
+  st.iterations = c.iter;
+  st.total_weight = c.total_weight;
+  st.leakage = c.leakage;
+  st.n_events = c.n_events;
+  st.n_secondaries = c.n_sec;
+  st.n_xs_calc = c.n_xs_calc;
+  st.n_xs_nuc = c.n_xs_nuc;
+  st.n_surf = c.n_surf_tot;
+  st.n_coll = c.n_coll_tot;
+  st.n_coll_nuc = c.n_coll_nuc;
+  st.n_segments = c.n_segments;
+}
+
+static void accumulate_batch(GpuSim* G, HModel& m)
+{
+  double norm = m.source.strength / (static_cast<double>(m.n_particles) * 1);
+  if (G->n_values > 0) {
+    k_accumulate<<<G->blocks, 256, 0, G->stream>>>(G->d_value, G->d_sum, G->d_sumsq, G->n_values, norm);
+    CK(cudaGetLastError());
+  }
+  for (auto& t : m.tallies) t.n_realizations += 1;
+  G->tallies_dirty = true;
+}
+
 BatchStats gpu_run_batch(GpuSim* G, HModel& m, int batch, bool accumulate)
 {
   G->queues.batch = batch;
@@ -1530,25 +1606,80 @@ BatchStats gpu_run_batch(GpuSim* G, HModel& m, int batch, bool accumulate)
   CK(cudaMemcpyAsync(&c, G->cnt, sizeof(c), cudaMemcpyDeviceToHost, G->stream));
   CK(cudaStreamSynchronize(G->stream));
   CK(cudaEventElapsedTime(&st.ms, G->ev0, G->ev1));
-  st.error = c.error;
-  st.n_lost = c.n_lost;
-  st.lost_id = c.lost_id;
-  st.n_done = c.n_done;
-  st.iterations = c.iter;
-  st.total_weight = c.total_weight;
-  st.leakage = c.leakage;
-  st.n_events = c.n_events;
-  st.n_secondaries = c.n_sec;
-  if (accumulate) {
-    double norm = m.source.strength / (static_cast<double>(m.n_particles) * 1);
-    if (G->n_values > 0) {
-      k_accumulate<<<G->blocks, 256, 0, G->stream>>>(G->d_value, G->d_sum, G->d_sumsq, G->n_values, norm);
-      CK(cudaGetLastError());
-    }
-    for (auto& t : m.tallies) t.n_realizations += 1;
-    G->tallies_dirty = true;
-  }
+  fill_stats(c, st);
+  if (accumulate) accumulate_batch(G, m);
   CK(cudaStreamSynchronize(G->stream));
+  return st;
+}
+
+BatchStats gpu_run_batch_profiled(GpuSim* G, HModel& m, int batch, bool accumulate)
+{
+  G->queues.batch = batch;
+  CK(cudaMemcpyToSymbolAsync(dq, &G->queues, sizeof(DQueues), 0, cudaMemcpyHostToDevice, G->stream));
+  const int nb = G->blocks, nt = 256;
+  const int n_ev = 16;
+  cudaEvent_t ev[n_ev];
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  BatchStats st {};
+  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  auto span = [&](int a, int b) {
+    float ms;
+    CK(cudaEventElapsedTime(&ms, ev[a], ev[b]));
+    return static_cast<double>(ms);
+  };
+  cudaStream_t S = G->stream;
+  CK(cudaEventRecord(ev[0], S));
+  k_batch_init<<<nb, nt, 0, S>>>(batch);
+  CK(cudaEventRecord(ev[1], S));
+  CK(cudaStreamSynchronize(S));
+  acc[6] += span(0, 1);
+  DCounters c {};
+  for (int it = 0; it < (1 << 20); ++it) {
+    CK(cudaEventRecord(ev[2], S));
+    k_xs<<<nb, nt, 0, S>>>();
+    CK(cudaEventRecord(ev[3], S));
+    k_advance<<<nb, nt, 0, S>>>();
+    CK(cudaEventRecord(ev[4], S));
+    k_surface<<<nb, nt, 0, S>>>();
+    CK(cudaEventRecord(ev[5], S));
+    k_collision<<<nb, nt, 0, S>>>();
+    CK(cudaEventRecord(ev[6], S));
+    k_refill_plan<<<1, 1, 0, S>>>();
+    CK(cudaEventRecord(ev[7], S));
+    k_refill<<<nb, nt, 0, S>>>();
+    CK(cudaEventRecord(ev[8], S));
+    if (G->sort) {
+      k_sort_hist<<<nb, nt, 0, S>>>();
+      k_sort_scan<<<1, 1024, 0, S>>>();
+      k_sort_scatter<<<nb, nt, 0, S>>>();
+    } else {
+      k_copy_queue<<<nb, nt, 0, S>>>();
+    }
+    CK(cudaEventRecord(ev[9], S));
+    k_finish_iter_host<<<1, 1, 0, S>>>();
+    CK(cudaEventRecord(ev[10], S));
+    CK(cudaMemcpyAsync(&c, G->cnt, sizeof(c), cudaMemcpyDeviceToHost, S));
+    CK(cudaStreamSynchronize(S));
+    acc[0] += span(2, 3);
+    acc[1] += span(3, 4);
+    acc[2] += span(4, 5);
+    acc[3] += span(5, 6);
+    acc[6] += span(6, 7);
+    acc[4] += span(7, 8);
+    acc[5] += span(8, 9);
+    acc[6] += span(9, 10);
+    if (!c.more) break;
+  }
+  double total = 0;
+  for (int k = 0; k < 7; ++k) {
+    st.kernel_ms[k] = static_cast<float>(acc[k]);
+    total += acc[k];
+  }
+  st.ms = static_cast<float>(total);
+  fill_stats(c, st);
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (accumulate) accumulate_batch(G, m);
+  CK(cudaStreamSynchronize(S));
   return st;
 }
 

@@ -29,11 +29,18 @@ struct BatchStats {
   double leakage = 0;
   unsigned long long n_events = 0;
   int n_secondaries = 0;
+  unsigned long long n_xs_calc = 0, n_xs_nuc = 0, n_surf = 0, n_coll = 0, n_coll_nuc = 0, n_segments = 0;
+  // per-kernel device milliseconds from a profiled batch:
+  // xs, advance, surface, collision, refill, sort, other
+  float kernel_ms[7] = {0, 0, 0, 0, 0, 0, 0};
 };
 
 GpuSim* gpu_create(const HModel& m, const GpuOptions& opt);
 void gpu_destroy(GpuSim* g);
 BatchStats gpu_run_batch(GpuSim* g, HModel& m, int batch, bool accumulate);
+// Same batch launched kernel by kernel (no graph) with CUDA events around
+// each kernel; identical results, slower, for per-kernel timing.
+BatchStats gpu_run_batch_profiled(GpuSim* g, HModel& m, int batch, bool accumulate);
 void gpu_fetch_tallies(GpuSim* g, HModel& m);
 void gpu_reset_tallies(GpuSim* g, HModel& m);
 void gpu_set_trace(GpuSim* g, long long n_hist, int cap, int batch);

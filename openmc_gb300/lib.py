@@ -136,6 +136,7 @@ _fn("openmc_weight_windows_update_magic", [C.c_int32, C.c_int32, C.c_char_p, C.c
 _fn("openmc_weight_windows_get_mesh", [C.c_int32, _p(C.c_int32)])
 _fn("openmc_gb300_last_batch", [_p(C.c_double)])
 _fn("openmc_gb300_timing", [_p(C.c_double)])
+_fn("openmc_gb300_last_batch_detail", [_p(C.c_double)])
 _fn("openmc_gb300_set_trace", [C.c_int64, C.c_int])
 _fn("openmc_gb300_get_trace", [C.c_void_p, _p(C.c_int32)])
 _fn("openmc_gb300_set_weight_windows_on", [C.c_int])
@@ -183,6 +184,7 @@ class _Settings:
     particles_in_flight = _DLLGlobal(C.c_int64, "openmc_gb300_in_flight")
     sort_queue = _DLLGlobal(C.c_int, "openmc_gb300_sort")
     trace_batch = _DLLGlobal(C.c_int, "openmc_gb300_trace_batch")
+    profile_next = _DLLGlobal(C.c_int, "openmc_gb300_profile_next")
 
     @property
     def seed(self):
@@ -392,6 +394,17 @@ def last_batch():
     _dll.openmc_gb300_last_batch(out)
     keys = ("ms", "iterations", "events", "total_weight", "leakage", "lost", "done", "secondaries")
     return dict(zip(keys, list(out)))
+
+
+def last_batch_detail():
+    out = (C.c_double * 14)()
+    _dll.openmc_gb300_last_batch_detail(out)
+    v = list(out)
+    keys = ("events", "xs_calc", "xs_nuclide_lookups", "surface", "collision",
+            "collision_nuclide_lookups", "mesh_segments")
+    d = dict(zip(keys, v[:7]))
+    d["kernel_ms"] = dict(zip(("xs", "advance", "surface", "collision", "refill", "sort", "other"), v[7:]))
+    return d
 
 
 def timing():

@@ -152,10 +152,12 @@ def shield_ww(built, tmp_path_factory):
     from openmc_gb300 import model as om
     d = tmp_path_factory.mktemp("shieldww")
     mesh = om.RegularMesh()
-    mesh.dimension = [20, 1, 1]
+    mesh.dimension = [40, 1, 1]
     mesh.lower_left = [0.0, -25.0, -25.0]
     mesh.upper_right = [200.0, 25.0, 25.0]
-    lower = 0.5 * np.exp(-0.35 * np.arange(20))
+    # importance rising tenfold every 10 cm: particles split on entering each
+    # 5 cm window bin and are rouletted when they scatter back
+    lower = 0.5 * 10.0 ** (-0.5 * np.arange(40))
     ww = om.WeightWindows(mesh, lower, upper_bound_ratio=5.0, energy_bounds=[0.0, 2.0e7 * 1.000001])
     m, path = configs.shield(d, particles=600, batches=2, n_points=2000, mesh_dim=(40, 2, 2),
                              weight_windows=ww)

@@ -126,17 +126,25 @@ def peaks():
 
 
 def algorithmic_bytes(detail, levels, fp32):
-    """Bytes each kernel must move per batch (HBM layout)."""
+    """Bytes each kernel must move per batch: the structure-of-arrays fields
+    an event reads and writes, the table bytes of each nuclide lookup (two
+    hash-window bounds, two bracketing energies, two table rows, nuclide
+    index, atom density) and 16 B of tally read-modify-write per mesh
+    segment.  The tail kernel moves the bytes of every event it runs."""
     row = 16 if fp32 else 32
     dens = 4 if fp32 else 8
     per_nuc = 8 + 16 + 2 * row + 4 + dens
-    ev = detail["events"]
-    b = {}
-    b["xs"] = ev * 36 + detail["xs_calc"] * 16 + detail["xs_nuclide_lookups"] * per_nuc
-    b["advance"] = ev * (136 + 72 * levels) + detail["mesh_segments"] * 16
-    b["surface"] = detail["surface"] * (120 + 96 * levels)
-    b["collision"] = detail["collision"] * 128 + detail["collision_nuclide_lookups"] * (per_nuc + row)
-    return b
+
+    def parts(st):
+        return {
+            "xs": st["xs_events"] * 36 + st["xs_calc"] * 16 + st["xs_nuclide_lookups"] * per_nuc,
+            "advance": st["xs_events"] * (136 + 72 * levels) + st["mesh_segments"] * 16,
+            "surface": st["surface"] * (120 + 96 * levels),
+            "collision": st["collision"] * 128 + st["collision_nuclide_lookups"] * per_nuc,
+        }
+    q = parts(detail["queue"])
+    q["tail"] = sum(parts(detail["tail"]).values())
+    return q
 
 
 def run_gb300(args):
@@ -185,10 +193,10 @@ def run_gb300(args):
     e2e = args.steps * n / sum(wall)
     kms = prof["kernel_ms"]
     byts = algorithmic_bytes(prof, levels, True)
-    dom = max(("xs", "advance", "surface", "collision"), key=lambda k: kms[k])
+    dom = max(("xs", "advance", "surface", "collision", "tail"), key=lambda k: kms[k])
     peak, peak_kind = peaks()
     achieved = byts[dom] / (kms[dom] * 1e-3) / 1e9
-    launches = sum(2 + 10 * int(i) for i in iters)
+    launches = sum(2 + 11 * int(i) for i in iters)
     out.update(value=value, ms_per_step=total_ms / args.steps, e2e=e2e, e2e_d2h=d2h, clocks=clk,
                launches=launches, dominant=dom, achieved=achieved, peak=peak, peak_kind=peak_kind,
                kernel_ms=kms, bytes=byts, detail=detail_timed, profile=prof, iterations=iters)
@@ -290,7 +298,8 @@ def main():
         "cpu_baseline": cpu,
         "kernel_ms_profiled_batch": r["kernel_ms"],
         "fp64_xs_particles_per_s": r.get("fp64_value"),
-        "events_per_step": r["detail"]["events"],
+        "events_per_step": r["detail"]["queue"]["xs_events"] + r["detail"]["tail"]["xs_events"],
+        "iterations_per_step": r["iterations"],
     }
     print(json.dumps(line))
 

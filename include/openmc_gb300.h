@@ -106,12 +106,16 @@ extern int openmc_gb300_trace_batch;
  * each kernel; results are identical, per-kernel times land in
  * openmc_gb300_last_batch_detail */
 extern int openmc_gb300_profile_next;
+/* queue length at or below which, once every source particle has started,
+ * the remaining histories run to completion one thread each (-1: default) */
+extern int64_t openmc_gb300_tail_threshold;
 
 /* last batch: [ms, iterations, events, total_weight, leakage, lost, done, secondaries] */
 int openmc_gb300_last_batch(double* out);
-/* [events, xs recomputations, xs nuclide lookups, surface events, collisions,
- *  collision nuclide lookups, mesh segments, kernel ms: xs, advance, surface,
- *  collision, refill, sort, other] */
+/* [queue phase: xs events, xs recomputations, xs nuclide lookups, mesh
+ *  segments, collision nuclide lookups, surface events, collisions; tail
+ *  phase: the same seven; kernel ms: xs, advance, surface, collision, tail,
+ *  refill, sort, other] */
 int openmc_gb300_last_batch_detail(double* out);
 /* [time_active s, time_inactive s, wall_active s, particles/s (active), in-flight slots] */
 int openmc_gb300_timing(double* out);

@@ -47,7 +47,6 @@ def log_energy_bins(n, e_min=data.E_MIN, e_max=data.E_MAX):
 
 def point_cube(directory, particles=100_000, batches=10, n_points=2000,
                seed=1, event_based=True, mesh_dim=(10, 10, 10), n_ebins=50):
-    om.reset_auto_ids()
     directory = Path(directory)
     rng = np.random.default_rng(seed)
     specs = [("H1", 1), ("C12", 12), ("O16", 16), ("Fe56", 56)]
@@ -120,7 +119,6 @@ def _lattice_materials(directory, n_points, seed):
 def lattice17(directory, particles=10_000_000, batches=20, n_points=11303,
               seed=3, event_based=True, mesh_dim=(17, 17, 50), n_ebins=100,
               height=200.0):
-    om.reset_auto_ids()
     directory = Path(directory)
     fuel, clad, mod, xs_xml = _lattice_materials(directory, n_points, seed)
     mats = om.Materials([fuel, clad, mod], cross_sections=xs_xml.name)
@@ -174,7 +172,6 @@ def shield_materials(directory, n_points, seed):
 def shield(directory, particles=1_000_000, batches=10, n_points=11303, seed=4,
            event_based=True, length=200.0, width=50.0, layer=10.0,
            mesh_dim=(200, 10, 10), weight_windows=None, back_face=10.0):
-    om.reset_auto_ids()
     directory = Path(directory)
     light, heavy, xs_xml = shield_materials(directory, n_points, seed)
     mats = om.Materials([light, heavy], cross_sections=xs_xml.name)

@@ -67,6 +67,7 @@ bool LIBMESH_ENABLED = false;
 bool UWUW_ENABLED = false;
 // GB300 extensions (no counterpart in the reference)
 int openmc_gb300_profile_next = 0;      // 1: run the next batch kernel by kernel with event timing
+int64_t openmc_gb300_tail_threshold = -1;  // queue length that starts the history-based tail (-1: default)
 int openmc_gb300_xs_fp32 = -1;          // -1: from XML (<gb300_xs_precision>), else 0/1
 int64_t openmc_gb300_in_flight = 0;     // particle slots; 0: setting or automatic
 int openmc_gb300_sort = 1;              // sort the XS queue by (material, energy)
@@ -352,6 +353,7 @@ int openmc_simulation_init()
     opt.in_flight = openmc_gb300_in_flight > 0 ? openmc_gb300_in_flight : m.max_particles_in_flight;
     opt.xs_fp32 = openmc_gb300_xs_fp32 >= 0 ? openmc_gb300_xs_fp32 != 0 : m.xs_precision == 32;
     opt.sort = openmc_gb300_sort != 0;
+    opt.tail_threshold = openmc_gb300_tail_threshold;
     if (m.ww_on && m.weight_windows.empty()) return fail(OPENMC_E_INVALID_ARGUMENT, "weight windows are on but none are defined");
     s.gpu = gpu_create(m, opt);
     if (s.trace_hist > 0) gpu_set_trace(s.gpu, s.trace_hist, s.trace_cap, openmc_gb300_trace_batch);
@@ -672,20 +674,16 @@ int openmc_gb300_last_batch(double* out)
   return 0;
 }
 
-// [n_events, n_xs_calc, n_xs_nuclide_lookups, n_surface, n_collision,
-//  n_collision_nuclide_lookups, n_mesh_segments, kernel ms x7 (xs, advance,
-//  surface, collision, refill, sort, other)]
+// [queue phase: xs events, xs recomputations, xs nuclide lookups, mesh
+//  segments, collision nuclide lookups, surface events, collisions;
+//  tail phase: the same seven; kernel ms x8 (xs, advance, surface, collision,
+//  tail, refill, sort, other)]
 int openmc_gb300_last_batch_detail(double* out)
 {
   const BatchStats& b = S().last;
-  out[0] = static_cast<double>(b.n_events);
-  out[1] = static_cast<double>(b.n_xs_calc);
-  out[2] = static_cast<double>(b.n_xs_nuc);
-  out[3] = static_cast<double>(b.n_surf);
-  out[4] = static_cast<double>(b.n_coll);
-  out[5] = static_cast<double>(b.n_coll_nuc);
-  out[6] = static_cast<double>(b.n_segments);
-  for (int k = 0; k < 7; ++k) out[7 + k] = b.kernel_ms[k];
+  for (int a = 0; a < 2; ++a)
+    for (int k = 0; k < 7; ++k) out[7 * a + k] = static_cast<double>(b.stat[a][k]);
+  for (int k = 0; k < 8; ++k) out[14 + k] = b.kernel_ms[k];
   return 0;
 }
 

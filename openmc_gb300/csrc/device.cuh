@@ -151,9 +151,14 @@ struct DCounters {
   double total_weight, leakage;
   unsigned long long n_events;
   long long lost_id;
-  // event statistics (for algorithmic-byte accounting)
-  unsigned long long n_xs_calc, n_xs_nuc, n_surf_tot, n_coll_tot, n_coll_nuc, n_segments, n_refill;
+  // event statistics for algorithmic-byte accounting, [0] queue kernels,
+  // [1] tail kernel: xs events, xs recomputations, xs nuclide lookups, mesh
+  // segments, collision nuclide lookups, surface events, collisions
+  unsigned long long stat[2][7];
+  unsigned long long n_refill;
   int more;  // set by the iteration epilogue when another iteration is needed
+  int tail;  // 1 while the loop runs the remaining histories in k_tail
+  int tail_threshold;  // queue length at or below which the tail phase starts
 };
 
 struct DQueues {

@@ -197,7 +197,7 @@ void read_mesh(const XmlNode* el, std::vector<HMesh>& meshes)
   std::string type = el->value_or("type", "regular");
   if (type != "regular") throw std::runtime_error("only regular meshes are supported (mesh " + std::to_string(m.id) + ")");
   for (const auto& e : meshes)
-    if (e.id == m.id) return;
+    if (e.id == m.id) throw std::runtime_error("Two or more meshes use the same unique ID: " + std::to_string(m.id));
   auto dim = split_ints(el->value("dimension"));
   auto ll = split_doubles(el->value("lower_left"));
   m.ndim = static_cast<int>(dim.size());

@@ -507,151 +507,126 @@ __global__ void k_batch_init(int batch)
     c->n_events = 0;
     c->error = 0;
     c->n_lost = 0;
-    c->n_xs_calc = c->n_xs_nuc = c->n_surf_tot = c->n_coll_tot = 0;
-    c->n_coll_nuc = c->n_segments = c->n_refill = 0;
+    for (int a = 0; a < 2; ++a)
+      for (int b = 0; b < 7; ++b) c->stat[a][b] = 0;
+    c->n_refill = 0;
     c->more = 1;
+    c->tail = 0;
   }
   (void)batch;
 }
 
-// src/particle.cpp:160-230
-__global__ void __launch_bounds__(256) k_xs()
+// ------------------------------------------------- per-particle events
+// Each event function works on one slot of the bank and is shared by the
+// queue kernels (one event per launch) and the tail kernel (whole histories).
+enum Next { NEXT_DEAD = 0, NEXT_XS = 1, NEXT_SURF = 2, NEXT_COLL = 3 };
+
+struct EvStats {
+  unsigned xs_ev, calc, nuc, seg, coll_nuc, surf, coll;
+};
+
+// src/particle.cpp:160-230 event_calculate_xs
+__device__ void ev_xs(long long s, EvStats& st)
 {
-  const int n = dq.cnt->n_q;
-  const int stride = gridDim.x * blockDim.x;
-  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
-    int i = base + threadIdx.x;
-    unsigned calc = 0, nuc = 0;
-    if (i < n) {
-      long long s = dq.q_in[i];
-      long long pid = db.id[s];
-      bool tr = traced(pid);
-      int lvl0 = db.n_coord[s] - 1;
-      int low_cell = db.cell[lvl0 * db.cap + s];
-      int material = db.material[s];
-      int material_last = db.material_last[s];
-      bool ok = true;
-      if (low_cell == C_NONE) {
-        Geo g;
-        geo_load(g, s);
-        bool lost_outer = false;
-        if (!exhaustive_find_cell(g, lost_outer)) {
-          mark_lost(s);
-          ok = false;
-        } else {
-          if (db.cell_born[s] == C_NONE) db.cell_born[s] = g.cell[g.n_coord - 1];
-          db.cell_last0[s] = g.cell[0];
-          geo_store(g, s);
-          material = g.material;
-          material_last = g.material_last;
-          low_cell = g.cell[g.n_coord - 1];
-        }
-      }
-      if (ok) {
-        uint32_t h = 0xffffffffu;
-        double E = db.E[s];
-        if (material != C_NONE) {
-          if (material != material_last || tr) {
-            double t, a;
-            h = material_xs(material, E, t, a);
-            db.macro_t[s] = t;
-            db.macro_a[s] = a;
-            calc = 1;
-            nuc = dm.mat_off[material + 1] - dm.mat_off[material];
-          }
-        } else {
-          db.macro_t[s] = 0.0;
-          db.macro_a[s] = 0.0;
-        }
-        if (tr) {
-          TraceRec* rec = trace_slot(pid);
-          if (rec) {
-            rec->cell = low_cell;
-            rec->material = material;
-            rec->grid_hash = static_cast<int32_t>(h);
-            rec->n_coord = db.n_coord[s];
-            rec->E = E;
-          }
-        }
-      }
+  st.xs_ev += 1;
+  long long pid = db.id[s];
+  bool tr = traced(pid);
+  int lvl0 = db.n_coord[s] - 1;
+  int low_cell = db.cell[lvl0 * db.cap + s];
+  int material = db.material[s];
+  int material_last = db.material_last[s];
+  if (low_cell == C_NONE) {
+    Geo g;
+    geo_load(g, s);
+    bool lost_outer = false;
+    if (!exhaustive_find_cell(g, lost_outer)) {
+      mark_lost(s);
+      return;
     }
-    warp_count(&dq.cnt->n_xs_calc, calc);
-    warp_count(&dq.cnt->n_xs_nuc, nuc);
+    if (db.cell_born[s] == C_NONE) db.cell_born[s] = g.cell[g.n_coord - 1];
+    db.cell_last0[s] = g.cell[0];
+    geo_store(g, s);
+    material = g.material;
+    material_last = g.material_last;
+    low_cell = g.cell[g.n_coord - 1];
+  }
+  uint32_t h = 0xffffffffu;
+  double E = db.E[s];
+  if (material != C_NONE) {
+    if (material != material_last || tr) {
+      double t, a;
+      h = material_xs(material, E, t, a);
+      db.macro_t[s] = t;
+      db.macro_a[s] = a;
+      st.calc += 1;
+      st.nuc += dm.mat_off[material + 1] - dm.mat_off[material];
+    }
+  } else {
+    db.macro_t[s] = 0.0;
+    db.macro_a[s] = 0.0;
+  }
+  if (tr) {
+    TraceRec* rec = trace_slot(pid);
+    if (rec) {
+      rec->cell = low_cell;
+      rec->material = material;
+      rec->grid_hash = static_cast<int32_t>(h);
+      rec->n_coord = db.n_coord[s];
+      rec->E = E;
+    }
   }
 }
 
-// src/particle.cpp:232-286
-__global__ void __launch_bounds__(256) k_advance()
+// src/particle.cpp:232-286 event_advance (+ track-length tallies)
+__device__ int ev_advance(long long s, EvStats& st)
 {
-  const int n = dq.cnt->n_q;
-  const int stride = gridDim.x * blockDim.x;
-  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
-    int i = base + threadIdx.x;
-    bool valid = i < n;
-    long long s = valid ? dq.q_in[i] : 0;
-    bool to_surf = false, to_coll = false, to_next = false;
-    unsigned n_seg = 0;
-    if (valid) {
-      double wgt = db.wgt[s];
-      if (wgt == 0.0) {
-        to_next = revive_or_free(s, wgt);
-      } else {
-        Geo g;
-        geo_load(g, s);
-        double bd;
-        int bs, bl, bt;
-        bool neg_lat = false;
-        distance_to_boundary(g, bd, bs, bl, bt, neg_lat);
-        if (neg_lat) mark_lost(s);
-        unsigned long long seed = db.seed[s];
-        double mt = db.macro_t[s];
-        double dcoll = (mt == 0.0) ? __longlong_as_double(0x7ff0000000000000LL) : -log(prn(seed)) / mt;
-        double distance = bd;
-        if (dcoll < distance) distance = dcoll;
-        if (INFTY < distance) distance = INFTY;
-        double r0[3] = {g.r[0][0], g.r[0][1], g.r[0][2]};
-        for (int l = 0; l < g.n_coord; ++l) {
-          g.r[l][0] = g.r[l][0] + distance * g.u[0];
-          g.r[l][1] = g.r[l][1] + distance * g.u[1];
-          g.r[l][2] = g.r[l][2] + distance * g.u[2];
-        }
-        if (dm.n_tally > 0) n_seg = score_tracklength(r0, g.r[0], g.u, db.E[s], wgt, distance, mt, db.macro_a[s]);
-        wgt = db.wgt[s];
-        if (distance == INFTY) {
-          wgt = 0.0;
-          db.wgt[s] = 0.0;
-        }
-        const long long cap = db.cap;
-        for (int l = 0; l < g.n_coord; ++l) {
-          long long k = l * cap + s;
-          db.rx[k] = g.r[l][0];
-          db.ry[k] = g.r[l][1];
-          db.rz[k] = g.r[l][2];
-        }
-        db.seed[s] = seed;
-        db.bdist[s] = bd;
-        db.bsurf[s] = bs;
-        db.blevel[s] = bl;
-        db.btrans[s] = bt;
-        db.dcoll[s] = dcoll;
-        long long pid = db.id[s];
-        if (traced(pid)) {
-          TraceRec* rec = trace_slot(pid);
-          if (rec) rec->dist = distance;
-        }
-        if (wgt != 0.0) {
-          to_surf = dcoll > bd;
-          to_coll = !to_surf;
-        } else {
-          to_next = revive_or_free(s, wgt);
-        }
-      }
-    }
-    warp_append(dq.q_surf, &dq.cnt->n_surf, static_cast<int>(s), to_surf);
-    warp_append(dq.q_coll, &dq.cnt->n_coll, static_cast<int>(s), to_coll);
-    warp_append(dq.q_tmp, &dq.cnt->n_next, static_cast<int>(s), to_next);
-    warp_count(&dq.cnt->n_segments, n_seg);
+  double wgt = db.wgt[s];
+  if (wgt == 0.0) return revive_or_free(s, wgt) ? NEXT_XS : NEXT_DEAD;
+  Geo g;
+  geo_load(g, s);
+  double bd;
+  int bs, bl, bt;
+  bool neg_lat = false;
+  distance_to_boundary(g, bd, bs, bl, bt, neg_lat);
+  if (neg_lat) mark_lost(s);
+  unsigned long long seed = db.seed[s];
+  double mt = db.macro_t[s];
+  double dcoll = (mt == 0.0) ? __longlong_as_double(0x7ff0000000000000LL) : -log(prn(seed)) / mt;
+  double distance = bd;
+  if (dcoll < distance) distance = dcoll;
+  if (INFTY < distance) distance = INFTY;
+  double r0[3] = {g.r[0][0], g.r[0][1], g.r[0][2]};
+  for (int l = 0; l < g.n_coord; ++l) {
+    g.r[l][0] = g.r[l][0] + distance * g.u[0];
+    g.r[l][1] = g.r[l][1] + distance * g.u[1];
+    g.r[l][2] = g.r[l][2] + distance * g.u[2];
   }
+  if (dm.n_tally > 0) st.seg += score_tracklength(r0, g.r[0], g.u, db.E[s], wgt, distance, mt, db.macro_a[s]);
+  wgt = db.wgt[s];
+  if (distance == INFTY) {
+    wgt = 0.0;
+    db.wgt[s] = 0.0;
+  }
+  const long long cap = db.cap;
+  for (int l = 0; l < g.n_coord; ++l) {
+    long long k = l * cap + s;
+    db.rx[k] = g.r[l][0];
+    db.ry[k] = g.r[l][1];
+    db.rz[k] = g.r[l][2];
+  }
+  db.seed[s] = seed;
+  db.bdist[s] = bd;
+  db.bsurf[s] = bs;
+  db.blevel[s] = bl;
+  db.btrans[s] = bt;
+  db.dcoll[s] = dcoll;
+  long long pid = db.id[s];
+  if (traced(pid)) {
+    TraceRec* rec = trace_slot(pid);
+    if (rec) rec->dist = distance;
+  }
+  if (wgt != 0.0) return dcoll > bd ? NEXT_SURF : NEXT_COLL;
+  return revive_or_free(s, wgt) ? NEXT_XS : NEXT_DEAD;
 }
 
 // src/geometry.cpp:301-357
@@ -682,100 +657,90 @@ __device__ void cross_lattice(Geo& g, long long s, int trans)
   }
 }
 
-// src/particle.cpp:288-329, 549-710
-__global__ void __launch_bounds__(256) k_surface()
+// src/particle.cpp:288-329, 549-710 event_cross_surface (+ revive)
+__device__ int ev_surface(long long s, EvStats& st)
 {
-  const int n = dq.cnt->n_surf;
-  const int stride = gridDim.x * blockDim.x;
-  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
-    int i = base + threadIdx.x;
-    bool valid = i < n;
-    long long s = valid ? dq.q_surf[i] : 0;
-    bool to_next = false;
-    if (valid) {
-      Geo g;
-      geo_load(g, s);
-      double wgt = db.wgt[s];
-      int bsurf = db.bsurf[s];
-      int trans = db.btrans[s];
-      db.cell_last0[s] = g.cell[0];
-      g.surface = bsurf;
-      g.n_coord = db.blevel[s];
-      bool lost_outer = false;
-      if (trans != 13) {
-        cross_lattice(g, s, trans);
-        wgt = db.wgt[s];
-      } else if (g.surface == SURFACE_NONE || abs(g.surface) > dm.n_surf) {
+  st.surf += 1;
+  Geo g;
+  geo_load(g, s);
+  double wgt = db.wgt[s];
+  int bsurf = db.bsurf[s];
+  int trans = db.btrans[s];
+  db.cell_last0[s] = g.cell[0];
+  g.surface = bsurf;
+  g.n_coord = db.blevel[s];
+  bool lost_outer = false;
+  if (trans != 13) {
+    cross_lattice(g, s, trans);
+    wgt = db.wgt[s];
+  } else if (g.surface == SURFACE_NONE || abs(g.surface) > dm.n_surf) {
+    mark_lost(s);
+    wgt = 0.0;
+  } else {
+    const DSurface& surf = dm.surf[abs(g.surface) - 1];
+    if (surf.bc == 1) {
+      // src/particle.cpp:631-655
+      atomicAdd(&dq.cnt->leakage, wgt);
+      wgt = 0.0;
+      db.wgt[s] = 0.0;
+    } else if (surf.bc == 2) {
+      // src/boundary_condition.cpp:38-47 + src/particle.cpp:657-710
+      double nx, ny, nz;
+      surf_normal(surf, g.r[0][0], g.r[0][1], g.r[0][2], nx, ny, nz);
+      double ux = g.u[0], uy = g.u[1], uz = g.u[2];
+      const double projection = nx * ux + ny * uy + nz * uz;
+      const double magnitude = nx * nx + ny * ny + nz * nz;
+      const double fac = 2.0 * projection / magnitude;
+      ux = ux - nx * fac;
+      uy = uy - ny * fac;
+      uz = uz - nz * fac;
+      double norm = sqrt(ux * ux + uy * uy + uz * uz);
+      ux /= norm;
+      uy /= norm;
+      uz /= norm;
+      if (g.n_coord != 1) {
         mark_lost(s);
         wgt = 0.0;
       } else {
-        const DSurface& surf = dm.surf[abs(g.surface) - 1];
-        if (surf.bc == 1) {
-          // src/particle.cpp:631-655
-          atomicAdd(&dq.cnt->leakage, wgt);
+        g.u[0] = ux; g.u[1] = uy; g.u[2] = uz;
+        g.cell[0] = db.cell_last0[s];
+        g.surface = -g.surface;
+        g.n_coord = 1;
+        if (!find_cell_inner(g, lost_outer)) {
+          mark_lost(s);
           wgt = 0.0;
-          db.wgt[s] = 0.0;
-        } else if (surf.bc == 2) {
-          // src/boundary_condition.cpp:38-47 + src/particle.cpp:657-710
-          double nx, ny, nz;
-          surf_normal(surf, g.r[0][0], g.r[0][1], g.r[0][2], nx, ny, nz);
-          double ux = g.u[0], uy = g.u[1], uz = g.u[2];
-          const double projection = nx * ux + ny * uy + nz * uz;
-          const double magnitude = nx * nx + ny * ny + nz * nz;
-          const double fac = 2.0 * projection / magnitude;
-          ux = ux - nx * fac;
-          uy = uy - ny * fac;
-          uz = uz - nz * fac;
-          double norm = sqrt(ux * ux + uy * uy + uz * uz);
-          ux /= norm;
-          uy /= norm;
-          uz /= norm;
-          if (g.n_coord != 1) {
+        }
+      }
+    } else {
+      // neighbour search at the crossing level, then from the root
+      if (!find_cell_inner(g, lost_outer)) {
+        g.n_coord = 1;
+        if (!exhaustive_find_cell(g, lost_outer)) {
+          g.surface = SURFACE_NONE;
+          g.n_coord = 1;
+          g.r[0][0] = g.r[0][0] + TINY_BIT * g.u[0];
+          g.r[0][1] = g.r[0][1] + TINY_BIT * g.u[1];
+          g.r[0][2] = g.r[0][2] + TINY_BIT * g.u[2];
+          if (!exhaustive_find_cell(g, lost_outer)) {
             mark_lost(s);
             wgt = 0.0;
-          } else {
-            g.u[0] = ux; g.u[1] = uy; g.u[2] = uz;
-            g.cell[0] = db.cell_last0[s];
-            g.surface = -g.surface;
-            g.n_coord = 1;
-            if (!find_cell_inner(g, lost_outer)) {
-              mark_lost(s);
-              wgt = 0.0;
-            }
-          }
-        } else {
-          // neighbour search at the crossing level, then from the root
-          if (!find_cell_inner(g, lost_outer)) {
-            g.n_coord = 1;
-            if (!exhaustive_find_cell(g, lost_outer)) {
-              g.surface = SURFACE_NONE;
-              g.n_coord = 1;
-              g.r[0][0] = g.r[0][0] + TINY_BIT * g.u[0];
-              g.r[0][1] = g.r[0][1] + TINY_BIT * g.u[1];
-              g.r[0][2] = g.r[0][2] + TINY_BIT * g.u[2];
-              if (!exhaustive_find_cell(g, lost_outer)) {
-                mark_lost(s);
-                wgt = 0.0;
-              }
-            }
           }
         }
       }
-      geo_store(g, s);
-      long long pid = db.id[s];
-      if (traced(pid)) {
-        TraceRec* rec = trace_slot(pid);
-        if (rec) {
-          rec->kind = 1;
-          rec->surface_or_nuclide = bsurf;
-          rec->wgt = wgt;
-        }
-        dq.trace_n[pid - 1] += 1;
-      }
-      to_next = revive_or_free(s, wgt);
     }
-    warp_append(dq.q_tmp, &dq.cnt->n_next, static_cast<int>(s), to_next);
   }
+  geo_store(g, s);
+  long long pid = db.id[s];
+  if (traced(pid)) {
+    TraceRec* rec = trace_slot(pid);
+    if (rec) {
+      rec->kind = 1;
+      rec->surface_or_nuclide = bsurf;
+      rec->wgt = wgt;
+    }
+    dq.trace_n[pid - 1] += 1;
+  }
+  return revive_or_free(s, wgt) ? NEXT_XS : NEXT_DEAD;
 }
 
 // src/physics.cpp:990-1041
@@ -838,110 +803,203 @@ __device__ void elastic_scatter(int nuc, double& E, double* u, unsigned long lon
 }
 
 // src/particle.cpp:331-415 + src/physics.cpp:43-168, 494-518, 638-752
+__device__ int ev_collision(long long s, EvStats& st)
+{
+  st.coll += 1;
+  double E = db.E[s];
+  double wgt = db.wgt[s];
+  unsigned long long seed = db.seed[s];
+  int mat = db.material[s];
+  double mt = db.macro_t[s];
+  db.surface[s] = SURFACE_NONE;
+  db.n_collision[s] += 1;
+  // sample_nuclide: CDF over atom_density * micro total in material order
+  double cutoff = prn(seed) * mt;
+  int a = 0, b = 0;
+  if (mat >= 0 && mat < dm.n_mat) {
+    a = dm.mat_off[mat];
+    b = dm.mat_off[mat + 1];
+  }
+  int i_log = log_union_index(E);
+  int chosen = -1;
+  double m_tot = 0, m_abs = 0;
+  if (!dm.xs_fp32) {
+    double prob = 0.0;
+    for (int k = a; k < b; ++k) {
+      int nuc = dm.mat_nuc[k];
+      st.coll_nuc += 1;
+      Micro m = micro_xs64(nuc, i_log, E);
+      prob += dm.mat_dens[k] * m.total;
+      if (prob >= cutoff) {
+        chosen = nuc;
+        m_tot = m.total;
+        m_abs = m.absorption;
+        break;
+      }
+    }
+  } else {
+    float prob = 0.0f;
+    for (int k = a; k < b; ++k) {
+      int nuc = dm.mat_nuc[k];
+      st.coll_nuc += 1;
+      float t, ab, f32;
+      int ig;
+      micro_xs32(nuc, i_log, E, t, ab, ig, f32);
+      prob += dm.mat_dens32[k] * t;
+      if (static_cast<double>(prob) >= cutoff) {
+        chosen = nuc;
+        m_tot = t;
+        m_abs = ab;
+        break;
+      }
+    }
+  }
+  double u[3] = {db.ux[s], db.uy[s], db.uz[s]};
+  if (chosen < 0) {
+    set_error(ERR_NO_NUCLIDE);
+    wgt = 0.0;
+  } else {
+    // absorption (analog) src/physics.cpp:638-672
+    if (m_abs > 0.0) {
+      if (m_abs > prn(seed) * m_tot) wgt = 0.0;
+    }
+    if (wgt != 0.0) {
+      // scatter src/physics.cpp:674-752: the reaction cutoff is drawn; the
+      // nuclides of this path have elastic scattering as their only
+      // scattering reaction, so the elastic branch is taken
+      double c2 = prn(seed) * (m_tot - m_abs);
+      (void)c2;
+      elastic_scatter(chosen, E, u, seed);
+      if (dm.ww_on) {
+        double r[3] = {db.rx[s], db.ry[s], db.rz[s]};
+        apply_weight_windows(s, wgt, seed, r, u, E, SURFACE_NONE);
+      }
+      if (E < dm.energy_cutoff) wgt = 0.0;
+    }
+  }
+  db.E[s] = E;
+  db.wgt[s] = wgt;
+  db.seed[s] = seed;
+  db.ux[s] = u[0]; db.uy[s] = u[1]; db.uz[s] = u[2];
+  db.material_last[s] = C_NONE;
+  long long pid = db.id[s];
+  if (traced(pid)) {
+    TraceRec* rec = trace_slot(pid);
+    if (rec) {
+      rec->kind = 2;
+      rec->surface_or_nuclide = chosen;
+      rec->wgt = wgt;
+    }
+    dq.trace_n[pid - 1] += 1;
+  }
+  return revive_or_free(s, wgt) ? NEXT_XS : NEXT_DEAD;
+}
+
+__device__ __forceinline__ void flush_stats(const EvStats& st, int set)
+{
+  unsigned long long* c = dq.cnt->stat[set];
+  warp_count(c + 0, st.xs_ev);
+  warp_count(c + 1, st.calc);
+  warp_count(c + 2, st.nuc);
+  warp_count(c + 3, st.seg);
+  warp_count(c + 4, st.coll_nuc);
+  warp_count(c + 5, st.surf);
+  warp_count(c + 6, st.coll);
+}
+
+// ----------------------------------------------------------- queue kernels
+// All kernels of an iteration leave at once while the loop is in its tail
+// phase (dq.cnt->tail), where k_tail runs the remaining histories instead.
+
+__global__ void __launch_bounds__(256) k_xs()
+{
+  if (dq.cnt->tail) return;
+  const int n = dq.cnt->n_q;
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    int i = base + threadIdx.x;
+    EvStats st {};
+    if (i < n) ev_xs(dq.q_in[i], st);
+    flush_stats(st, 0);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_advance()
+{
+  if (dq.cnt->tail) return;
+  const int n = dq.cnt->n_q;
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    int i = base + threadIdx.x;
+    bool valid = i < n;
+    long long s = valid ? dq.q_in[i] : 0;
+    EvStats st {};
+    int nx = valid ? ev_advance(s, st) : NEXT_DEAD;
+    warp_append(dq.q_surf, &dq.cnt->n_surf, static_cast<int>(s), nx == NEXT_SURF);
+    warp_append(dq.q_coll, &dq.cnt->n_coll, static_cast<int>(s), nx == NEXT_COLL);
+    warp_append(dq.q_tmp, &dq.cnt->n_next, static_cast<int>(s), nx == NEXT_XS);
+    flush_stats(st, 0);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_surface()
+{
+  if (dq.cnt->tail) return;
+  const int n = dq.cnt->n_surf;
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    int i = base + threadIdx.x;
+    bool valid = i < n;
+    long long s = valid ? dq.q_surf[i] : 0;
+    EvStats st {};
+    int nx = valid ? ev_surface(s, st) : NEXT_DEAD;
+    warp_append(dq.q_tmp, &dq.cnt->n_next, static_cast<int>(s), nx == NEXT_XS);
+    flush_stats(st, 0);
+  }
+}
+
 __global__ void __launch_bounds__(256) k_collision()
 {
+  if (dq.cnt->tail) return;
   const int n = dq.cnt->n_coll;
   const int stride = gridDim.x * blockDim.x;
   for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
     int i = base + threadIdx.x;
     bool valid = i < n;
     long long s = valid ? dq.q_coll[i] : 0;
-    bool to_next = false;
-    unsigned n_nuc_looked = 0;
-    if (valid) {
-      double E = db.E[s];
-      double wgt = db.wgt[s];
-      unsigned long long seed = db.seed[s];
-      int mat = db.material[s];
-      double mt = db.macro_t[s];
-      db.surface[s] = SURFACE_NONE;
-      db.n_collision[s] += 1;
-      // sample_nuclide: CDF over atom_density * micro total in material order
-      double cutoff = prn(seed) * mt;
-      int a = 0, b = 0;
-      if (mat >= 0 && mat < dm.n_mat) {
-        a = dm.mat_off[mat];
-        b = dm.mat_off[mat + 1];
-      }
-      int i_log = log_union_index(E);
-      int chosen = -1;
-      double m_tot = 0, m_abs = 0, m_el = 0;
-      if (!dm.xs_fp32) {
-        double prob = 0.0;
-        for (int k = a; k < b; ++k) {
-          int nuc = dm.mat_nuc[k];
-          ++n_nuc_looked;
-          Micro m = micro_xs64(nuc, i_log, E);
-          prob += dm.mat_dens[k] * m.total;
-          if (prob >= cutoff) {
-            chosen = nuc;
-            m_tot = m.total;
-            m_abs = m.absorption;
-            const double4* xs = dm.xs64 + dm.nuc_off[nuc];
-            m_el = (1.0 - m.f) * xs[m.i_grid].z + m.f * xs[m.i_grid + 1].z;
-            break;
-          }
-        }
-      } else {
-        float prob = 0.0f;
-        for (int k = a; k < b; ++k) {
-          int nuc = dm.mat_nuc[k];
-          ++n_nuc_looked;
-          float t, ab, f32;
-          int ig;
-          micro_xs32(nuc, i_log, E, t, ab, ig, f32);
-          prob += dm.mat_dens32[k] * t;
-          if (static_cast<double>(prob) >= cutoff) {
-            chosen = nuc;
-            m_tot = t;
-            m_abs = ab;
-            const float4* xs = dm.xs32 + dm.nuc_off[nuc];
-            m_el = (1.0f - f32) * xs[ig].z + f32 * xs[ig + 1].z;
-            break;
-          }
-        }
-      }
-      double u[3] = {db.ux[s], db.uy[s], db.uz[s]};
-      if (chosen < 0) {
-        set_error(ERR_NO_NUCLIDE);
-        wgt = 0.0;
-      } else {
-        // absorption (analog) src/physics.cpp:638-672
-        if (m_abs > 0.0) {
-          if (m_abs > prn(seed) * m_tot) wgt = 0.0;
-        }
-        if (wgt != 0.0) {
-          // scatter src/physics.cpp:674-752: cutoff drawn, elastic for MT2
-          double c2 = prn(seed) * (m_tot - m_abs);
-          (void)c2;
-          (void)m_el;
-          elastic_scatter(chosen, E, u, seed);
-          if (dm.ww_on) {
-            double r[3] = {db.rx[s], db.ry[s], db.rz[s]};
-            apply_weight_windows(s, wgt, seed, r, u, E, SURFACE_NONE);
-          }
-          if (E < dm.energy_cutoff) wgt = 0.0;
-        }
-      }
-      db.E[s] = E;
-      db.wgt[s] = wgt;
-      db.seed[s] = seed;
-      db.ux[s] = u[0]; db.uy[s] = u[1]; db.uz[s] = u[2];
-      db.material_last[s] = C_NONE;
-      long long pid = db.id[s];
-      if (traced(pid)) {
-        TraceRec* rec = trace_slot(pid);
-        if (rec) {
-          rec->kind = 2;
-          rec->surface_or_nuclide = chosen;
-          rec->wgt = wgt;
-        }
-        dq.trace_n[pid - 1] += 1;
-      }
-      to_next = revive_or_free(s, wgt);
+    EvStats st {};
+    int nx = valid ? ev_collision(s, st) : NEXT_DEAD;
+    warp_append(dq.q_tmp, &dq.cnt->n_next, static_cast<int>(s), nx == NEXT_XS);
+    flush_stats(st, 0);
+  }
+}
+
+// Tail phase: once every source particle of the batch has started and few
+// histories remain, each thread carries one history through up to
+// max_events events (src/simulation.cpp:804-821, history-based loop) instead
+// of paying one kernel launch per event.  Histories that reach the limit go
+// back to the queue.  The per-history physics is the same event functions.
+__global__ void __launch_bounds__(128) k_tail(int max_events)
+{
+  if (!dq.cnt->tail) return;
+  const int n = dq.cnt->n_q;
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    int i = base + threadIdx.x;
+    bool valid = i < n;
+    long long s = valid ? dq.q_in[i] : 0;
+    EvStats st {};
+    int nx = valid ? NEXT_XS : NEXT_DEAD;
+    for (int e = 0; e < max_events && nx == NEXT_XS; ++e) {
+      ev_xs(s, st);
+      nx = ev_advance(s, st);
+      if (nx == NEXT_SURF) nx = ev_surface(s, st);
+      else if (nx == NEXT_COLL) nx = ev_collision(s, st);
     }
-    warp_append(dq.q_tmp, &dq.cnt->n_next, static_cast<int>(s), to_next);
-    warp_count(&dq.cnt->n_coll_nuc, n_nuc_looked);
+    __syncwarp();
+    warp_append(dq.q_tmp, &dq.cnt->n_next, static_cast<int>(s), nx == NEXT_XS);
+    flush_stats(st, 1);
+    warp_count(&dq.cnt->n_events, st.xs_ev);
   }
 }
 
@@ -956,8 +1014,6 @@ __global__ void k_refill_plan()
   c->refill_src = c->next_source;
   c->n_free -= static_cast<int>(k);
   c->next_source += k;
-  c->n_surf_tot += static_cast<unsigned long long>(c->n_surf);
-  c->n_coll_tot += static_cast<unsigned long long>(c->n_coll);
   c->n_refill += static_cast<unsigned long long>(k);
   c->n_surf = 0;
   c->n_coll = 0;
@@ -978,7 +1034,10 @@ __global__ void __launch_bounds__(256) k_refill()
   }
 }
 
-// Counting sort of the next cross-section queue by (material, energy octave)
+// Counting sort of the next cross-section queue by (material, energy octave):
+// each block histograms a contiguous chunk in shared memory, one global
+// atomic per (block, key) reserves its output range, and the block scatters
+// its chunk into that range.
 __device__ __forceinline__ int sort_key(int s)
 {
   int mat = db.material[s] + 1;
@@ -988,31 +1047,40 @@ __device__ __forceinline__ int sort_key(int s)
   return mat * 64 + ex;
 }
 
-__global__ void k_sort_hist()
+constexpr int SORT_MAX_KEYS = 2048;
+
+__global__ void __launch_bounds__(512) k_sort_hist()
 {
+  __shared__ int h[SORT_MAX_KEYS];
+  const int nk = dq.sort_keys;
   const int n = dq.cnt->n_next;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    atomicAdd(&dq.hist[sort_key(dq.q_tmp[i])], 1);
+  const int chunk = (n + gridDim.x - 1) / gridDim.x;
+  const int lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
+  for (int k = threadIdx.x; k < nk; k += blockDim.x) h[k] = 0;
+  __syncthreads();
+  for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) atomicAdd(&h[sort_key(dq.q_tmp[i])], 1);
+  __syncthreads();
+  for (int k = threadIdx.x; k < nk; k += blockDim.x)
+    if (h[k]) atomicAdd(&dq.hist[k], h[k]);
 }
 
 __global__ void k_sort_scan()
 {
   // single block: exclusive scan of hist into cursor, hist cleared
   __shared__ int carry;
+  __shared__ int wsum[32];
   if (threadIdx.x == 0) carry = 0;
   __syncthreads();
   const int nk = dq.sort_keys;
   for (int base = 0; base < nk; base += blockDim.x) {
     int i = base + threadIdx.x;
     int v = i < nk ? dq.hist[i] : 0;
-    // block inclusive scan via warp shuffles
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int x = v;
     for (int o = 1; o < 32; o <<= 1) {
       int y = __shfl_up_sync(0xffffffffu, x, o);
       if (lane >= o) x += y;
     }
-    __shared__ int wsum[32];
     if (lane == 31) wsum[w] = x;
     __syncthreads();
     if (w == 0) {
@@ -1035,12 +1103,23 @@ __global__ void k_sort_scan()
   }
 }
 
-__global__ void k_sort_scatter()
+__global__ void __launch_bounds__(512) k_sort_scatter()
 {
+  __shared__ int h[SORT_MAX_KEYS];
+  const int nk = dq.sort_keys;
   const int n = dq.cnt->n_next;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  const int chunk = (n + gridDim.x - 1) / gridDim.x;
+  const int lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
+  for (int k = threadIdx.x; k < nk; k += blockDim.x) h[k] = 0;
+  __syncthreads();
+  for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) atomicAdd(&h[sort_key(dq.q_tmp[i])], 1);
+  __syncthreads();
+  for (int k = threadIdx.x; k < nk; k += blockDim.x)
+    if (h[k]) h[k] = atomicAdd(&dq.cursor[k], h[k]);
+  __syncthreads();
+  for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
     int s = dq.q_tmp[i];
-    int pos = atomicAdd(&dq.cursor[sort_key(s)], 1);
+    int pos = atomicAdd(&h[sort_key(s)], 1);
     dq.q_in[pos] = s;
   }
 }
@@ -1055,11 +1134,14 @@ __global__ void k_copy_queue()
 __device__ bool finish_iter_common()
 {
   DCounters* c = dq.cnt;
-  c->n_events += static_cast<unsigned long long>(c->n_q);
+  if (!c->tail) c->n_events += static_cast<unsigned long long>(c->n_q);
   c->n_q = c->n_next;
   c->n_next = 0;
   c->iter += 1;
   bool more = c->n_q > 0 || c->next_source <= dm.n_particles;
+  // enter the tail phase once every source particle has started and the
+  // queue is short enough that per-event launches would dominate
+  c->tail = (c->next_source > dm.n_particles && c->n_q > 0 && c->n_q <= c->tail_threshold) ? 1 : 0;
   if (c->error != 0) more = false;
   if (c->iter >= c->max_iter) {
     if (more) c->error |= ERR_ITERATIONS;
@@ -1136,6 +1218,8 @@ struct GpuSim {
   cudaGraph_t graph = nullptr;
   int blocks = 1216;
   int sort = 1;
+  long long tail_threshold = 1 << 17;
+  int tail_max_events = 1 << 16;
   bool tallies_dirty = true;
   float last_batch_ms = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -1433,6 +1517,7 @@ static void build_bank(GpuSim& G, long long cap, long long sec_cap)
   q.q_tmp = dev_alloc<int>(cap, own);
   q.free_list = dev_alloc<int>(cap, own);
   q.sort_keys = (G.model.n_mat + 1) * 64;
+  if (q.sort_keys > SORT_MAX_KEYS) G.sort = 0;
   q.hist = dev_alloc<int>(q.sort_keys, own);
   q.cursor = dev_alloc<int>(q.sort_keys, own);
   q.sec = dev_alloc<DSecondary>(sec_cap, own);
@@ -1446,6 +1531,7 @@ static void build_bank(GpuSim& G, long long cap, long long sec_cap)
   DCounters c {};
   c.sec_cap = static_cast<int>(sec_cap);
   c.max_iter = 1 << 20;
+  c.tail_threshold = static_cast<int>(G.tail_threshold);
   CK(cudaMemcpy(G.cnt, &c, sizeof(c), cudaMemcpyHostToDevice));
 }
 
@@ -1493,6 +1579,7 @@ static void build_graph(GpuSim& G)
   k_advance<<<nb, nt, 0, G.stream>>>();
   k_surface<<<nb, nt, 0, G.stream>>>();
   k_collision<<<nb, nt, 0, G.stream>>>();
+  k_tail<<<nb * 2, 128, 0, G.stream>>>(G.tail_max_events);
   k_refill_plan<<<1, 1, 0, G.stream>>>();
   k_refill<<<nb, nt, 0, G.stream>>>();
   if (G.sort) {
@@ -1517,6 +1604,7 @@ GpuSim* gpu_create(const HModel& m, const GpuOptions& opt)
     CK(cudaEventCreate(&G->ev0));
     CK(cudaEventCreate(&G->ev1));
     G->sort = opt.sort ? 1 : 0;
+    if (opt.tail_threshold >= 0) G->tail_threshold = opt.tail_threshold;
     int sms = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
     G->blocks = sms * 8;
@@ -1575,12 +1663,8 @@ static void fill_stats(const DCounters& c, BatchStats& st)
   st.leakage = c.leakage;
   st.n_events = c.n_events;
   st.n_secondaries = c.n_sec;
-  st.n_xs_calc = c.n_xs_calc;
-  st.n_xs_nuc = c.n_xs_nuc;
-  st.n_surf = c.n_surf_tot;
-  st.n_coll = c.n_coll_tot;
-  st.n_coll_nuc = c.n_coll_nuc;
-  st.n_segments = c.n_segments;
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 7; ++b) st.stat[a][b] = c.stat[a][b];
 }
 
 static void accumulate_batch(GpuSim* G, HModel& m)
@@ -1621,7 +1705,7 @@ BatchStats gpu_run_batch_profiled(GpuSim* G, HModel& m, int batch, bool accumula
   cudaEvent_t ev[n_ev];
   for (auto& e : ev) CK(cudaEventCreate(&e));
   BatchStats st {};
-  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   auto span = [&](int a, int b) {
     float ms;
     CK(cudaEventElapsedTime(&ms, ev[a], ev[b]));
@@ -1632,7 +1716,7 @@ BatchStats gpu_run_batch_profiled(GpuSim* G, HModel& m, int batch, bool accumula
   k_batch_init<<<nb, nt, 0, S>>>(batch);
   CK(cudaEventRecord(ev[1], S));
   CK(cudaStreamSynchronize(S));
-  acc[6] += span(0, 1);
+  acc[7] += span(0, 1);
   DCounters c {};
   for (int it = 0; it < (1 << 20); ++it) {
     CK(cudaEventRecord(ev[2], S));
@@ -1644,6 +1728,8 @@ BatchStats gpu_run_batch_profiled(GpuSim* G, HModel& m, int batch, bool accumula
     CK(cudaEventRecord(ev[5], S));
     k_collision<<<nb, nt, 0, S>>>();
     CK(cudaEventRecord(ev[6], S));
+    k_tail<<<nb * 2, 128, 0, S>>>(G->tail_max_events);
+    CK(cudaEventRecord(ev[11], S));
     k_refill_plan<<<1, 1, 0, S>>>();
     CK(cudaEventRecord(ev[7], S));
     k_refill<<<nb, nt, 0, S>>>();
@@ -1664,14 +1750,15 @@ BatchStats gpu_run_batch_profiled(GpuSim* G, HModel& m, int batch, bool accumula
     acc[1] += span(3, 4);
     acc[2] += span(4, 5);
     acc[3] += span(5, 6);
-    acc[6] += span(6, 7);
-    acc[4] += span(7, 8);
-    acc[5] += span(8, 9);
-    acc[6] += span(9, 10);
+    acc[4] += span(6, 11);
+    acc[7] += span(11, 7);
+    acc[5] += span(7, 8);
+    acc[6] += span(8, 9);
+    acc[7] += span(9, 10);
     if (!c.more) break;
   }
   double total = 0;
-  for (int k = 0; k < 7; ++k) {
+  for (int k = 0; k < 8; ++k) {
     st.kernel_ms[k] = static_cast<float>(acc[k]);
     total += acc[k];
   }

@@ -16,6 +16,7 @@ struct GpuOptions {
   long long secondary_cap = 0;  // secondary-site pool entries (0: automatic)
   bool xs_fp32 = false;         // FP32 cross-section tables and interpolation
   bool sort = true;             // sort the cross-section queue by (material, energy)
+  long long tail_threshold = -1;  // queue length for the history-based tail (-1: default)
 };
 
 struct BatchStats {
@@ -29,10 +30,12 @@ struct BatchStats {
   double leakage = 0;
   unsigned long long n_events = 0;
   int n_secondaries = 0;
-  unsigned long long n_xs_calc = 0, n_xs_nuc = 0, n_surf = 0, n_coll = 0, n_coll_nuc = 0, n_segments = 0;
+  // [queue, tail] x [xs events, xs recomputations, xs nuclide lookups, mesh
+  // segments, collision nuclide lookups, surface events, collisions]
+  unsigned long long stat[2][7] = {{0, 0, 0, 0, 0, 0, 0}, {0, 0, 0, 0, 0, 0, 0}};
   // per-kernel device milliseconds from a profiled batch:
-  // xs, advance, surface, collision, refill, sort, other
-  float kernel_ms[7] = {0, 0, 0, 0, 0, 0, 0};
+  // xs, advance, surface, collision, tail, refill, sort, other
+  float kernel_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
 GpuSim* gpu_create(const HModel& m, const GpuOptions& opt);

@@ -185,6 +185,7 @@ class _Settings:
     sort_queue = _DLLGlobal(C.c_int, "openmc_gb300_sort")
     trace_batch = _DLLGlobal(C.c_int, "openmc_gb300_trace_batch")
     profile_next = _DLLGlobal(C.c_int, "openmc_gb300_profile_next")
+    tail_threshold = _DLLGlobal(C.c_int64, "openmc_gb300_tail_threshold")
 
     @property
     def seed(self):
@@ -397,13 +398,16 @@ def last_batch():
 
 
 def last_batch_detail():
-    out = (C.c_double * 14)()
+    """Event statistics of the last batch for the queue and tail phases, and
+    per-kernel milliseconds when the batch ran with settings.profile_next."""
+    out = (C.c_double * 22)()
     _dll.openmc_gb300_last_batch_detail(out)
     v = list(out)
-    keys = ("events", "xs_calc", "xs_nuclide_lookups", "surface", "collision",
-            "collision_nuclide_lookups", "mesh_segments")
-    d = dict(zip(keys, v[:7]))
-    d["kernel_ms"] = dict(zip(("xs", "advance", "surface", "collision", "refill", "sort", "other"), v[7:]))
+    keys = ("xs_events", "xs_calc", "xs_nuclide_lookups", "mesh_segments",
+            "collision_nuclide_lookups", "surface", "collision")
+    d = {"queue": dict(zip(keys, v[0:7])), "tail": dict(zip(keys, v[7:14]))}
+    d["kernel_ms"] = dict(zip(("xs", "advance", "surface", "collision", "tail", "refill", "sort", "other"),
+                              v[14:22]))
     return d
 
 

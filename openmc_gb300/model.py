@@ -584,7 +584,7 @@ class Settings:
         for k, v in kw.items():
             setattr(self, k, v)
 
-    def to_xml(self):
+    def to_xml(self, skip_mesh_ids=()):
         el = ET.Element("settings")
         ET.SubElement(el, "run_mode").text = self.run_mode
         ET.SubElement(el, "particles").text = str(int(self.particles))
@@ -614,7 +614,8 @@ class Settings:
         for g in self.weight_window_generators:
             meshes[g.mesh.id] = g.mesh
         for mid in sorted(meshes):
-            el.append(meshes[mid].to_xml())
+            if mid not in skip_mesh_ids:
+                el.append(meshes[mid].to_xml())
         for ww in wws:
             el.append(ww.to_xml())
         if self.weight_windows_on is not None:
@@ -637,7 +638,8 @@ class Model:
         root = ET.Element("model")
         root.append(self.materials.to_xml())
         root.append(self.geometry.to_xml())
-        root.append(self.settings.to_xml())
+        tally_meshes = {f.mesh.id for t in self.tallies for f in t.filters if isinstance(f, MeshFilter)}
+        root.append(self.settings.to_xml(skip_mesh_ids=tally_meshes))
         if self.tallies:
             root.append(self.tallies.to_xml())
         return root

@@ -300,6 +300,8 @@ def load_model(model_xml, cross_sections=None):
     # ---- meshes (tallies and settings)
     meshes = {}
     for el in list(set_el.findall("mesh")) + (list(tal_el.findall("mesh")) if tal_el is not None else []):
+        if int(el.get("id")) in meshes:
+            raise ValueError(f"Two or more meshes use the same unique ID: {el.get('id')}")
         dim = _ints(_get(el, "dimension"))
         ll = _floats(_get(el, "lower_left"))
         ur = _get(el, "upper_right")
@@ -411,6 +413,9 @@ def load_model(model_xml, cross_sections=None):
         ww_e = _floats(_get(w, "energy_bounds"))
         ww_lower = _floats(_get(w, "lower_ww_bounds"))
         ww_upper = _floats(_get(w, "upper_ww_bounds"))
+        n_ww = (len(ww_e) - 1) * int(np.prod(mesh_dim[3 * mi:3 * mi + 3]))
+        if len(ww_lower) != n_ww or len(ww_upper) != n_ww:
+            raise ValueError("weight-window bounds have the wrong size")
         mlb = _get(w, "max_lower_bound_ratio")
         ww_i = [mi, 1, int(_get(w, "max_split", 10))]
         ww_d = [float(_get(w, "survival_ratio", 3.0)),

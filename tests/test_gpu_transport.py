@@ -155,11 +155,11 @@ def shield_ww(built, tmp_path_factory):
     mesh.dimension = [40, 1, 1]
     mesh.lower_left = [0.0, -25.0, -25.0]
     mesh.upper_right = [200.0, 25.0, 25.0]
-    # importance rising tenfold every 10 cm: particles split on entering each
-    # 5 cm window bin and are rouletted when they scatter back
-    lower = 0.5 * 10.0 ** (-0.5 * np.arange(40))
+    # importance rising threefold every 10 cm: particles split on entering
+    # deeper window bins and are rouletted when they scatter back
+    lower = 0.5 * 3.0 ** (-0.5 * np.arange(40))
     ww = om.WeightWindows(mesh, lower, upper_bound_ratio=5.0, energy_bounds=[0.0, 2.0e7 * 1.000001])
-    m, path = configs.shield(d, particles=600, batches=2, n_points=2000, mesh_dim=(40, 2, 2),
+    m, path = configs.shield(d, particles=300, batches=2, n_points=2000, mesh_dim=(40, 2, 2),
                              weight_windows=ww)
     return m.export_to_model_xml(path), path
 
@@ -167,8 +167,8 @@ def shield_ww(built, tmp_path_factory):
 def test_shield_weight_window_parity(shield_ww):
     """Splitting, roulette and LIFO secondary revival match the oracle."""
     xml, path = shield_ww
-    g = run_gpu(path, n_trace=600, cap=2048)
-    o = run_oracle(xml, n_trace=600, cap=2048)
+    g = run_gpu(path, n_trace=300, cap=2048)
+    o = run_oracle(xml, n_trace=300, cap=2048)
     assert g["batch"]["secondaries"] > 0
     bad = trace_mismatches(g["trace"], o["trace"], 2048)
     assert not bad, f"{len(bad)} histories differ, first: {bad[:5]}"

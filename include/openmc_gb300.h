@@ -102,6 +102,7 @@ extern int openmc_gb300_xs_fp32;
 extern int64_t openmc_gb300_in_flight;
 extern int openmc_gb300_sort;
 extern int openmc_gb300_trace_batch;
+extern int64_t openmc_gb300_trace_first;
 /* 1: run the next batch kernel by kernel (no graph) with CUDA events around
  * each kernel; results are identical, per-kernel times land in
  * openmc_gb300_last_batch_detail */
@@ -110,7 +111,8 @@ extern int openmc_gb300_profile_next;
  * the remaining histories run to completion one thread each (-1: default) */
 extern int64_t openmc_gb300_tail_threshold;
 
-/* last batch: [ms, iterations, events, total_weight, leakage, lost, done, secondaries] */
+/* last batch: [ms, iterations, events, total_weight, leakage, lost, done, secondaries,
+ *  events of the longest history, its particle id] */
 int openmc_gb300_last_batch(double* out);
 /* [queue phase: xs events, xs recomputations, xs nuclide lookups, mesh
  *  segments, collision nuclide lookups, surface events, collisions; tail
@@ -119,7 +121,8 @@ int openmc_gb300_last_batch(double* out);
 int openmc_gb300_last_batch_detail(double* out);
 /* [time_active s, time_inactive s, wall_active s, particles/s (active), in-flight slots] */
 int openmc_gb300_timing(double* out);
-/* per-event traces for particle ids 1..n_hist, cap records each (48-byte records) */
+/* per-event traces for particle ids first..first+n_hist-1 of the traced batch,
+ * cap records each (48-byte records) */
 int openmc_gb300_set_trace(int64_t n_hist, int cap);
 int openmc_gb300_get_trace(void* records, int32_t* counts);
 int openmc_gb300_set_weight_windows_on(int on);

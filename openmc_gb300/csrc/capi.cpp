@@ -72,6 +72,7 @@ int openmc_gb300_xs_fp32 = -1;          // -1: from XML (<gb300_xs_precision>), 
 int64_t openmc_gb300_in_flight = 0;     // particle slots; 0: setting or automatic
 int openmc_gb300_sort = 1;              // sort the XS queue by (material, energy)
 int openmc_gb300_trace_batch = 1;       // batch whose histories openmc_gb300_set_trace records
+int64_t openmc_gb300_trace_first = 1;   // first particle id openmc_gb300_set_trace records
 }
 
 namespace {
@@ -356,7 +357,7 @@ int openmc_simulation_init()
     opt.tail_threshold = openmc_gb300_tail_threshold;
     if (m.ww_on && m.weight_windows.empty()) return fail(OPENMC_E_INVALID_ARGUMENT, "weight windows are on but none are defined");
     s.gpu = gpu_create(m, opt);
-    if (s.trace_hist > 0) gpu_set_trace(s.gpu, s.trace_hist, s.trace_cap, openmc_gb300_trace_batch);
+    if (s.trace_hist > 0) gpu_set_trace(s.gpu, s.trace_hist, s.trace_cap, openmc_gb300_trace_batch, openmc_gb300_trace_first);
     gpu_reset_tallies(s.gpu, m);
     std::fill(s.global_tallies.begin(), s.global_tallies.end(), 0.0);
     current_batch = 0;
@@ -671,6 +672,8 @@ int openmc_gb300_last_batch(double* out)
   out[5] = b.n_lost;
   out[6] = static_cast<double>(b.n_done);
   out[7] = b.n_secondaries;
+  out[8] = static_cast<double>(b.longest_events);
+  out[9] = static_cast<double>(b.longest_id);
   return 0;
 }
 
@@ -706,7 +709,7 @@ int openmc_gb300_set_trace(int64_t n_hist, int cap)
   s.trace_hist = n_hist;
   s.trace_cap = cap;
   try {
-    if (s.gpu) gpu_set_trace(s.gpu, n_hist, cap, openmc_gb300_trace_batch);
+    if (s.gpu) gpu_set_trace(s.gpu, n_hist, cap, openmc_gb300_trace_batch, openmc_gb300_trace_first);
   } catch (const std::exception& e) {
     return fail(OPENMC_E_ALLOCATE, e.what());
   }

@@ -129,6 +129,7 @@ struct DBank {
   int *bsurf, *blevel, *btrans;
   int *n_event, *n_collision, *n_split;
   int* sec_top;
+  int* n_total;  // events of the whole history (all revived secondaries)
 };
 
 struct DSecondary {
@@ -159,6 +160,7 @@ struct DCounters {
   int more;  // set by the iteration epilogue when another iteration is needed
   int tail;  // 1 while the loop runs the remaining histories in k_tail
   int tail_threshold;  // queue length at or below which the tail phase starts
+  unsigned long long longest;  // (events << 34) | particle id of the longest history
 };
 
 struct DQueues {
@@ -174,6 +176,7 @@ struct DQueues {
   TraceRec* trace;
   int* trace_n;
   long long trace_hist;
+  long long trace_first;  // first traced particle id
   int trace_cap;
   int trace_batch;  // batch whose histories are traced
   int batch;
@@ -767,7 +770,10 @@ __device__ __forceinline__ Micro micro_xs64(int nuc, int i_log, double E)
   return m;
 }
 
-// FP32 tables: interpolation in FP32 from an FP64 interpolation factor
+// FP32 tables: interpolation in FP32 from an FP64 interpolation factor,
+// written as a + f (b - a), which stays accurate when f leaves [0, 1]
+// (energies below the first or above the last grid point extrapolate);
+// (1 - f) a + f b cancels catastrophically in FP32 there.
 __device__ __forceinline__ void micro_xs32(int nuc, int i_log, double E, float& t, float& a_out, int& i_grid, float& f32)
 {
   double f;
@@ -776,8 +782,8 @@ __device__ __forceinline__ void micro_xs32(int nuc, int i_log, double E, float& 
   const float4* xs = dm.xs32 + dm.nuc_off[nuc];
   float4 a = __ldg(xs + i_grid);
   float4 b = __ldg(xs + i_grid + 1);
-  t = (1.0f - f32) * a.x + f32 * b.x;
-  a_out = (1.0f - f32) * a.y + f32 * b.y;
+  t = a.x + f32 * (b.x - a.x);
+  a_out = a.y + f32 * (b.y - a.y);
 }
 
 // Hash bin of E (src/material.cpp:833-834), clamped to [0, M-1]: the

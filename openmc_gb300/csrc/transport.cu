@@ -65,14 +65,16 @@ __device__ __forceinline__ void warp_count(unsigned long long* ctr, unsigned v)
 
 __device__ __forceinline__ bool traced(long long id)
 {
-  return dq.trace != nullptr && dq.batch == dq.trace_batch && id >= 1 && id <= dq.trace_hist;
+  return dq.trace != nullptr && dq.batch == dq.trace_batch && id >= dq.trace_first &&
+         id < dq.trace_first + dq.trace_hist;
 }
 
 __device__ __forceinline__ TraceRec* trace_slot(long long id)
 {
-  int n = dq.trace_n[id - 1];
+  long long k = id - dq.trace_first;
+  int n = dq.trace_n[k];
   if (n >= dq.trace_cap) return nullptr;
-  return dq.trace + (id - 1) * dq.trace_cap + n;
+  return dq.trace + k * dq.trace_cap + n;
 }
 
 __device__ void set_error(int flag) { atomicOr(&dq.cnt->error, flag); }
@@ -442,7 +444,8 @@ __device__ void initialize_history(long long s, long long index_source)
   db.wgt[s] = wgt;
   db.seed[s] = tseed;
   atomicAdd(&dq.cnt->total_weight, wgt);
-  if (traced(index_source)) dq.trace_n[index_source - 1] = 0;
+  db.n_total[s] = 0;
+  if (traced(index_source)) dq.trace_n[index_source - dq.trace_first] = 0;
 }
 
 // src/particle.cpp:417-473 event_revive_from_secondary; returns alive.
@@ -450,6 +453,7 @@ __device__ void initialize_history(long long s, long long index_source)
 __device__ bool revive_or_free(long long s, double wgt)
 {
   int ne = db.n_event[s] + 1;
+  db.n_total[s] += 1;
   if (ne == dm.max_events) {
     wgt = 0.0;
     db.wgt[s] = 0.0;
@@ -458,6 +462,9 @@ __device__ bool revive_or_free(long long s, double wgt)
   if (wgt != 0.0) return true;
   int top = db.sec_top[s];
   if (top < 0) {
+    unsigned long long key = (static_cast<unsigned long long>(db.n_total[s]) << 34) |
+                             static_cast<unsigned long long>(db.id[s]);
+    atomicMax(&dq.cnt->longest, key);
     int k = atomicAdd(&dq.cnt->n_free, 1);
     dq.free_list[k] = static_cast<int>(s);
     atomicAdd(reinterpret_cast<unsigned long long*>(&dq.cnt->n_done), 1ull);
@@ -512,6 +519,7 @@ __global__ void k_batch_init(int batch)
     c->n_refill = 0;
     c->more = 1;
     c->tail = 0;
+    c->longest = 0;
   }
   (void)batch;
 }
@@ -738,7 +746,7 @@ __device__ int ev_surface(long long s, EvStats& st)
       rec->surface_or_nuclide = bsurf;
       rec->wgt = wgt;
     }
-    dq.trace_n[pid - 1] += 1;
+    dq.trace_n[pid - dq.trace_first] += 1;
   }
   return revive_or_free(s, wgt) ? NEXT_XS : NEXT_DEAD;
 }
@@ -890,7 +898,7 @@ __device__ int ev_collision(long long s, EvStats& st)
       rec->surface_or_nuclide = chosen;
       rec->wgt = wgt;
     }
-    dq.trace_n[pid - 1] += 1;
+    dq.trace_n[pid - dq.trace_first] += 1;
   }
   return revive_or_free(s, wgt) ? NEXT_XS : NEXT_DEAD;
 }
@@ -1510,6 +1518,7 @@ static void build_bank(GpuSim& G, long long cap, long long sec_cap)
   b.n_collision = dev_alloc<int>(cap, own);
   b.n_split = dev_alloc<int>(cap, own);
   b.sec_top = dev_alloc<int>(cap, own);
+  b.n_total = dev_alloc<int>(cap, own);
   DQueues& q = G.queues;
   q.q_in = dev_alloc<int>(cap, own);
   q.q_surf = dev_alloc<int>(cap, own);
@@ -1628,7 +1637,7 @@ GpuSim* gpu_create(const HModel& m, const GpuOptions& opt)
 
 void gpu_destroy(GpuSim* G) { delete G; }
 
-void gpu_set_trace(GpuSim* G, long long n_hist, int cap, int batch)
+void gpu_set_trace(GpuSim* G, long long n_hist, int cap, int batch, long long first)
 {
   if (n_hist <= 0) {
     G->queues.trace = nullptr;
@@ -1640,6 +1649,7 @@ void gpu_set_trace(GpuSim* G, long long n_hist, int cap, int batch)
     G->queues.trace_hist = n_hist;
     G->queues.trace_cap = cap;
     G->queues.trace_batch = batch;
+    G->queues.trace_first = first;
   }
   CK(cudaMemcpyToSymbol(dq, &G->queues, sizeof(DQueues)));
 }
@@ -1663,6 +1673,8 @@ static void fill_stats(const DCounters& c, BatchStats& st)
   st.leakage = c.leakage;
   st.n_events = c.n_events;
   st.n_secondaries = c.n_sec;
+  st.longest_events = static_cast<long long>(c.longest >> 34);
+  st.longest_id = static_cast<long long>(c.longest & ((1ULL << 34) - 1));
   for (int a = 0; a < 2; ++a)
     for (int b = 0; b < 7; ++b) st.stat[a][b] = c.stat[a][b];
 }

@@ -30,6 +30,7 @@ struct BatchStats {
   double leakage = 0;
   unsigned long long n_events = 0;
   int n_secondaries = 0;
+  long long longest_events = 0, longest_id = 0;  // longest history of the batch
   // [queue, tail] x [xs events, xs recomputations, xs nuclide lookups, mesh
   // segments, collision nuclide lookups, surface events, collisions]
   unsigned long long stat[2][7] = {{0, 0, 0, 0, 0, 0, 0}, {0, 0, 0, 0, 0, 0, 0}};
@@ -46,7 +47,7 @@ BatchStats gpu_run_batch(GpuSim* g, HModel& m, int batch, bool accumulate);
 BatchStats gpu_run_batch_profiled(GpuSim* g, HModel& m, int batch, bool accumulate);
 void gpu_fetch_tallies(GpuSim* g, HModel& m);
 void gpu_reset_tallies(GpuSim* g, HModel& m);
-void gpu_set_trace(GpuSim* g, long long n_hist, int cap, int batch);
+void gpu_set_trace(GpuSim* g, long long n_hist, int cap, int batch, long long first);
 void gpu_get_trace(GpuSim* g, void* records, int* counts);
 void gpu_set_ww_bounds(GpuSim* g, const double* lower, const double* upper, long long n);
 void gpu_set_ww_on(GpuSim* g, bool on);

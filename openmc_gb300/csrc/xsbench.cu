@@ -171,7 +171,10 @@ __global__ void __launch_bounds__(256) k_lookup(Tables T, const int* __restrict_
         float f32 = static_cast<float>(f);
         float d = __ldg(T.mat_dens32 + q);
 #pragma unroll
-        for (int c = 0; c < 5; ++c) macro32[c] += d * ((1.0f - f32) * __ldg(x + c) + f32 * __ldg(x + 5 + c));
+        for (int c = 0; c < 5; ++c) {
+          float a = __ldg(x + c), b = __ldg(x + 5 + c);
+          macro32[c] += d * (a + f32 * (b - a));
+        }
       } else {
         const double* x = T.xs64 + row;
         double d = __ldg(T.mat_dens + q);

@@ -184,6 +184,7 @@ class _Settings:
     particles_in_flight = _DLLGlobal(C.c_int64, "openmc_gb300_in_flight")
     sort_queue = _DLLGlobal(C.c_int, "openmc_gb300_sort")
     trace_batch = _DLLGlobal(C.c_int, "openmc_gb300_trace_batch")
+    trace_first = _DLLGlobal(C.c_int64, "openmc_gb300_trace_first")
     profile_next = _DLLGlobal(C.c_int, "openmc_gb300_profile_next")
     tail_threshold = _DLLGlobal(C.c_int64, "openmc_gb300_tail_threshold")
 
@@ -391,9 +392,10 @@ def get_trace():
 
 
 def last_batch():
-    out = (C.c_double * 8)()
+    out = (C.c_double * 10)()
     _dll.openmc_gb300_last_batch(out)
-    keys = ("ms", "iterations", "events", "total_weight", "leakage", "lost", "done", "secondaries")
+    keys = ("ms", "iterations", "events", "total_weight", "leakage", "lost", "done", "secondaries",
+            "longest_events", "longest_id")
     return dict(zip(keys, list(out)))
 
 

@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-table extra measurement")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=0, help="histories in the CPU baseline sample")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="launch every batch kernel by kernel instead of as one CUDA graph "
+                         "(for kernel profilers, which cannot see inside conditional graphs)")
     return ap.parse_args()
 
 
@@ -157,6 +160,8 @@ def run_gb300(args):
     try:
         lib.settings.xs_fp32 = 1
         lib.settings.particles_in_flight = args.in_flight
+        if args.no_graph:
+            lib.settings.profile_next = 2
         lib.simulation_init()
         tid = lib.tally_ids()[0]
         flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float64, device="cuda")
@@ -181,7 +186,8 @@ def run_gb300(args):
         detail_timed = lib.last_batch_detail()
         # profiled batch (kernel by kernel, CUDA events) for the roofline
         flush_l2(flush)
-        lib.settings.profile_next = 1
+        if not args.no_graph:
+            lib.settings.profile_next = 1
         lib.next_batch()
         prof = lib.last_batch_detail()
         levels = 2
@@ -196,7 +202,7 @@ def run_gb300(args):
     dom = max(("xs", "advance", "surface", "collision", "tail"), key=lambda k: kms[k])
     peak, peak_kind = peaks()
     achieved = byts[dom] / (kms[dom] * 1e-3) / 1e9
-    launches = sum(2 + 11 * int(i) for i in iters)
+    launches = sum(2 + (13 if not args.no_graph else 14) * int(i) for i in iters)
     out.update(value=value, ms_per_step=total_ms / args.steps, e2e=e2e, e2e_d2h=d2h, clocks=clk,
                launches=launches, dominant=dom, achieved=achieved, peak=peak, peak_kind=peak_kind,
                kernel_ms=kms, bytes=byts, detail=detail_timed, profile=prof, iterations=iters)

@@ -104,8 +104,9 @@ extern int openmc_gb300_sort;
 extern int openmc_gb300_trace_batch;
 extern int64_t openmc_gb300_trace_first;
 /* 1: run the next batch kernel by kernel (no graph) with CUDA events around
- * each kernel; results are identical, per-kernel times land in
- * openmc_gb300_last_batch_detail */
+ * each kernel; 2: run every batch that way (kernel profilers cannot look
+ * inside graphs with conditional nodes); results are identical, per-kernel
+ * times land in openmc_gb300_last_batch_detail */
 extern int openmc_gb300_profile_next;
 /* queue length at or below which, once every source particle has started,
  * the remaining histories run to completion one thread each (-1: default) */

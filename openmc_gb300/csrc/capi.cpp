@@ -66,7 +66,8 @@ bool DAGMC_ENABLED = false;
 bool LIBMESH_ENABLED = false;
 bool UWUW_ENABLED = false;
 // GB300 extensions (no counterpart in the reference)
-int openmc_gb300_profile_next = 0;      // 1: run the next batch kernel by kernel with event timing
+int openmc_gb300_profile_next = 0;      // 1: run the next batch kernel by kernel with event timing,
+                                        // 2: every batch (graph-free, for kernel profilers)
 int64_t openmc_gb300_tail_threshold = -1;  // queue length that starts the history-based tail (-1: default)
 int openmc_gb300_xs_fp32 = -1;          // -1: from XML (<gb300_xs_precision>), else 0/1
 int64_t openmc_gb300_in_flight = 0;     // particle slots; 0: setting or automatic
@@ -392,7 +393,7 @@ int openmc_next_batch(int* status)
     auto t0 = std::chrono::steady_clock::now();
     BatchStats st = openmc_gb300_profile_next ? gpu_run_batch_profiled(s.gpu, m, current_batch, active)
                                               : gpu_run_batch(s.gpu, m, current_batch, active);
-    openmc_gb300_profile_next = 0;
+    if (openmc_gb300_profile_next == 1) openmc_gb300_profile_next = 0;
     auto t1 = std::chrono::steady_clock::now();
     s.last = st;
     s.n_batches_run++;

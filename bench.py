@@ -202,7 +202,7 @@ def run_gb300(args):
     dom = max(("xs", "advance", "surface", "collision", "tail"), key=lambda k: kms[k])
     peak, peak_kind = peaks()
     achieved = byts[dom] / (kms[dom] * 1e-3) / 1e9
-    launches = sum(2 + (13 if not args.no_graph else 14) * int(i) for i in iters)
+    launches = sum(2 + 11 * int(i) for i in iters)
     out.update(value=value, ms_per_step=total_ms / args.steps, e2e=e2e, e2e_d2h=d2h, clocks=clk,
                launches=launches, dominant=dom, achieved=achieved, peak=peak, peak_kind=peak_kind,
                kernel_ms=kms, bytes=byts, detail=detail_timed, profile=prof, iterations=iters)

@@ -101,6 +101,8 @@ int openmc_weight_windows_get_mesh(int32_t index, int32_t* mesh_idx);
 extern int openmc_gb300_xs_fp32;
 extern int64_t openmc_gb300_in_flight;
 extern int openmc_gb300_sort;
+/* 1: the cross-section event runs inside the advance kernel */
+extern int openmc_gb300_fuse;
 extern int openmc_gb300_trace_batch;
 extern int64_t openmc_gb300_trace_first;
 /* 1: run the next batch kernel by kernel (no graph) with CUDA events around

@@ -311,6 +311,9 @@ __device__ inline double plane_distance(double r_i, double u_i, bool coincident,
 {
   const double f = offset - r_i;
   if (coincident || fabs(f) < FP_COINCIDENT || u_i == 0.0) return INFTY;
+  // f / u_i < 0 exactly when the signs differ (|f| >= 1e-12 and |u_i| <= 1,
+  // so the quotient cannot underflow to zero): skip the division then
+  if ((f < 0.0) != (u_i < 0.0)) return INFTY;
   const double d = f / u_i;
   if (d < 0.0) return INFTY;
   return d;
@@ -443,9 +446,12 @@ __device__ inline bool cell_contains(const DCell& c, double x, double y, double 
   return sp > 0 ? (stack & 1u) : true;
 }
 
-// src/cell.cpp:910-936
+// src/cell.cpp:910-936.  `bound` lets the caller skip axis-aligned planes
+// whose perpendicular distance |f| (a lower bound of the distance along any
+// direction) already exceeds it; skipped planes count as no crossing.  With
+// bound = INFTY this is exactly the reference loop.
 __device__ inline void region_distance(const DCell& c, double x, double y, double z, double ux, double uy,
-  double uz, int on_surface, double& min_dist, int& i_surf)
+  double uz, int on_surface, double& min_dist, int& i_surf, double bound = INFTY)
 {
   min_dist = INFTY;
   i_surf = 2147483647;
@@ -453,8 +459,13 @@ __device__ inline void region_distance(const DCell& c, double x, double y, doubl
   for (int k = 0; k < c.tok_len; ++k) {
     int token = t[k];
     if (token >= 2147483643) continue;
+    const DSurface& sf = dm.surf[abs(token) - 1];
+    if (sf.type <= 2) {
+      double r_i = sf.type == 0 ? x : (sf.type == 1 ? y : z);
+      if (fabs(sf.c[0] - r_i) > bound) continue;
+    }
     bool coincident = abs(token) == abs(on_surface);
-    double d = surf_distance(dm.surf[abs(token) - 1], x, y, z, ux, uy, uz, coincident);
+    double d = surf_distance(sf, x, y, z, ux, uy, uz, coincident);
     if (d < min_dist) {
       if (min_dist - d >= FP_PRECISION * min_dist) {
         min_dist = d;
@@ -667,15 +678,39 @@ __device__ inline bool exhaustive_find_cell(Geo& g, bool& lost_outer)
   return find_cell_inner(g, lost_outer);
 }
 
-// src/geometry.cpp:361-453
+// src/geometry.cpp:361-453.  The levels below the root are evaluated first;
+// the candidate distance D of level 1 bounds the root level: the reference
+// replaces any root distance above D (1 + 1e-4) by D at level 1 (its
+// FP_REL_PRECISION test is 1e-5), so root planes whose perpendicular
+// distance exceeds that bound are skipped, and a root level whose every
+// surface was skipped enters the level loop as INFINITY.  The returned
+// boundary is the reference's.
 __device__ inline void distance_to_boundary(const Geo& g, double& dist, int& surface, int& level,
   int& trans, bool& neg_lat)
 {
-  double d_lat = __longlong_as_double(0x7ff0000000000000LL);  // INFINITY
-  double d_surf;
-  int level_surf_cross;
-  int level_lat_trans = 13;
-  const double INF = __longlong_as_double(0x7ff0000000000000LL);
+  const double INF = __longlong_as_double(0x7ff0000000000000LL);  // INFINITY
+  double ds[MAXL], dl[MAXL];
+  int ss[MAXL], tt[MAXL];
+  double bound = INF;
+  for (int i = g.n_coord - 1; i >= 0; --i) {
+    const DCell& c = dm.cell[g.cell[i]];
+    const double* r = g.r[i];
+    double b = (i == 0 && g.n_coord > 1) ? bound : INFTY;
+    region_distance(c, r[0], r[1], r[2], g.u[0], g.u[1], g.u[2], g.surface, ds[i], ss[i], b);
+    if (i == 0 && g.n_coord > 1 && ss[i] == 2147483647) ds[i] = INF;  // every root surface bounded away
+    dl[i] = INF;
+    tt[i] = 13;
+    if (g.lat[i] != C_NONE) {
+      dl[i] = lattice_distance(dm.lat[g.lat[i]], r[0], r[1], r[2], g.u[0], g.u[1], g.u[2], tt[i]);
+      if (dl[i] < 0) neg_lat = true;
+    }
+    if (i == 1) {
+      // candidate of the level directly below the root: any root distance
+      // above cand (1 + 1e-4) loses to it in the level loop below
+      double cand = (ds[i] < dl[i] - FP_COINCIDENT) ? ds[i] : dl[i];
+      bound = cand * (1.0 + 1e-4);
+    }
+  }
   dist = INF;
   surface = SURFACE_NONE;
   level = 0;
@@ -683,24 +718,21 @@ __device__ inline void distance_to_boundary(const Geo& g, double& dist, int& sur
   for (int i = 0; i < g.n_coord; i++) {
     const DCell& c = dm.cell[g.cell[i]];
     const double* r = g.r[i];
-    region_distance(c, r[0], r[1], r[2], g.u[0], g.u[1], g.u[2], g.surface, d_surf, level_surf_cross);
-    if (g.lat[i] != C_NONE) {
-      d_lat = lattice_distance(dm.lat[g.lat[i]], r[0], r[1], r[2], g.u[0], g.u[1], g.u[2], level_lat_trans);
-      if (d_lat < 0) neg_lat = true;
-    }
+    double d_surf = ds[i];
+    double d_lat = dl[i];
     double& d = dist;
     if (d_surf < d_lat - FP_COINCIDENT) {
       if (d == INF || (d - d_surf) / d >= FP_REL_PRECISION) {
         d = d_surf;
         if (c.simple || d == INFTY) {
-          surface = level_surf_cross;
+          surface = ss[i];
         } else {
           double hx = r[0] + d_surf * g.u[0];
           double hy = r[1] + d_surf * g.u[1];
           double hz = r[2] + d_surf * g.u[2];
           double nx, ny, nz;
-          surf_normal(dm.surf[abs(level_surf_cross) - 1], hx, hy, hz, nx, ny, nz);
-          surface = (g.u[0] * nx + g.u[1] * ny + g.u[2] * nz > 0) ? abs(level_surf_cross) : -abs(level_surf_cross);
+          surf_normal(dm.surf[abs(ss[i]) - 1], hx, hy, hz, nx, ny, nz);
+          surface = (g.u[0] * nx + g.u[1] * ny + g.u[2] * nz > 0) ? abs(ss[i]) : -abs(ss[i]);
         }
         trans = 13;
         level = i + 1;
@@ -709,7 +741,7 @@ __device__ inline void distance_to_boundary(const Geo& g, double& dist, int& sur
       if (d == INF || (d - d_lat) / d >= FP_REL_PRECISION) {
         d = d_lat;
         surface = SURFACE_NONE;
-        trans = level_lat_trans;
+        trans = tt[i];
         level = i + 1;
       }
     }

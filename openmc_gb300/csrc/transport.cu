@@ -88,9 +88,17 @@ __device__ void mark_lost(long long s)
 
 // ------------------------------------------------------ mesh raytrace
 // src/mesh.cpp:1328-1369 RegularMesh helpers
+// ceil((r - lower_left) / width).  The quotient is first estimated in FP32
+// (relative error below 1e-6 for |q| < 2^20); only when the estimate lies
+// within 1e-4 of an integer, where the ceiling could differ, is the FP64
+// division evaluated.  The returned index equals the FP64 ceiling.
 __device__ __forceinline__ int mesh_index_in_direction(const DMesh& m, double r, int i)
 {
-  return static_cast<int>(ceil((r - m.ll[i]) / m.width[i]));
+  const double t = r - m.ll[i];
+  const float q32 = __fdiv_rn(static_cast<float>(t), static_cast<float>(m.width[i]));
+  const float fr = q32 - rintf(q32);
+  if (fabsf(q32) < 1048576.0f && fabsf(fr) > 1e-4f + 2e-6f * fabsf(q32)) return static_cast<int>(ceilf(q32));
+  return static_cast<int>(ceil(t / m.width[i]));
 }
 
 __device__ __forceinline__ void mesh_get_indices(const DMesh& m, double x, double y, double z, int* ijk, bool& in_mesh)
@@ -916,6 +924,17 @@ __device__ __forceinline__ void flush_stats(const EvStats& st, int set)
 }
 
 // ----------------------------------------------------------- queue kernels
+// Minimum resident blocks per SM for the event kernels (register budget
+// 65536 / (256 x minB) per thread).
+#ifndef OMC_MINB_ADV
+#define OMC_MINB_ADV 2
+#endif
+#ifndef OMC_MINB_SURF
+#define OMC_MINB_SURF 2
+#endif
+#ifndef OMC_MINB_COLL
+#define OMC_MINB_COLL 2
+#endif
 // All kernels of an iteration leave at once while the loop is in its tail
 // phase (dq.cnt->tail), where k_tail runs the remaining histories instead.
 
@@ -932,7 +951,12 @@ __global__ void __launch_bounds__(256) k_xs()
   }
 }
 
-__global__ void __launch_bounds__(256) k_advance()
+// with_xs: the cross-section event runs in the same thread right before the
+// advance (every calculate_xs event is followed by an advance event,
+// src/event.cpp:95-98), sparing one pass over the queue and the macroscopic
+// XS round trip through HBM.
+template<bool with_xs>
+__global__ void __launch_bounds__(256, OMC_MINB_ADV) k_advance()
 {
   if (dq.cnt->tail) return;
   const int n = dq.cnt->n_q;
@@ -942,6 +966,7 @@ __global__ void __launch_bounds__(256) k_advance()
     bool valid = i < n;
     long long s = valid ? dq.q_in[i] : 0;
     EvStats st {};
+    if (with_xs && valid) ev_xs(s, st);
     int nx = valid ? ev_advance(s, st) : NEXT_DEAD;
     warp_append(dq.q_surf, &dq.cnt->n_surf, static_cast<int>(s), nx == NEXT_SURF);
     warp_append(dq.q_coll, &dq.cnt->n_coll, static_cast<int>(s), nx == NEXT_COLL);
@@ -950,7 +975,7 @@ __global__ void __launch_bounds__(256) k_advance()
   }
 }
 
-__global__ void __launch_bounds__(256) k_surface()
+__global__ void __launch_bounds__(256, OMC_MINB_SURF) k_surface()
 {
   if (dq.cnt->tail) return;
   const int n = dq.cnt->n_surf;
@@ -966,7 +991,7 @@ __global__ void __launch_bounds__(256) k_surface()
   }
 }
 
-__global__ void __launch_bounds__(256) k_collision()
+__global__ void __launch_bounds__(256, OMC_MINB_COLL) k_collision()
 {
   if (dq.cnt->tail) return;
   const int n = dq.cnt->n_coll;
@@ -1226,6 +1251,7 @@ struct GpuSim {
   cudaGraph_t graph = nullptr;
   int blocks = 1216;
   int sort = 1;
+  int fuse = 1;  // cross-section event fused into the advance kernel
   long long tail_threshold = 1 << 17;
   int tail_max_events = 1 << 16;
   bool tallies_dirty = true;
@@ -1584,8 +1610,12 @@ static void build_graph(GpuSim& G)
   CK(cudaGraphAddNode(&cond, graph, nodes.data(), nullptr, n_nodes, &cp));
   cudaGraph_t body = cp.conditional.phGraph_out[0];
   CK(cudaStreamBeginCaptureToGraph(G.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-  k_xs<<<nb, nt, 0, G.stream>>>();
-  k_advance<<<nb, nt, 0, G.stream>>>();
+  if (G.fuse) {
+    k_advance<true><<<nb, nt, 0, G.stream>>>();
+  } else {
+    k_xs<<<nb, nt, 0, G.stream>>>();
+    k_advance<false><<<nb, nt, 0, G.stream>>>();
+  }
   k_surface<<<nb, nt, 0, G.stream>>>();
   k_collision<<<nb, nt, 0, G.stream>>>();
   k_tail<<<nb * 2, 128, 0, G.stream>>>(G.tail_max_events);
@@ -1613,6 +1643,7 @@ GpuSim* gpu_create(const HModel& m, const GpuOptions& opt)
     CK(cudaEventCreate(&G->ev0));
     CK(cudaEventCreate(&G->ev1));
     G->sort = opt.sort ? 1 : 0;
+    G->fuse = opt.fuse ? 1 : 0;
     if (opt.tail_threshold >= 0) G->tail_threshold = opt.tail_threshold;
     int sms = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
@@ -1732,9 +1763,10 @@ BatchStats gpu_run_batch_profiled(GpuSim* G, HModel& m, int batch, bool accumula
   DCounters c {};
   for (int it = 0; it < (1 << 20); ++it) {
     CK(cudaEventRecord(ev[2], S));
-    k_xs<<<nb, nt, 0, S>>>();
+    if (!G->fuse) k_xs<<<nb, nt, 0, S>>>();
     CK(cudaEventRecord(ev[3], S));
-    k_advance<<<nb, nt, 0, S>>>();
+    if (G->fuse) k_advance<true><<<nb, nt, 0, S>>>();
+    else k_advance<false><<<nb, nt, 0, S>>>();
     CK(cudaEventRecord(ev[4], S));
     k_surface<<<nb, nt, 0, S>>>();
     CK(cudaEventRecord(ev[5], S));

@@ -183,6 +183,7 @@ class _Settings:
     xs_fp32 = _DLLGlobal(C.c_int, "openmc_gb300_xs_fp32")
     particles_in_flight = _DLLGlobal(C.c_int64, "openmc_gb300_in_flight")
     sort_queue = _DLLGlobal(C.c_int, "openmc_gb300_sort")
+    fuse_xs = _DLLGlobal(C.c_int, "openmc_gb300_fuse")
     trace_batch = _DLLGlobal(C.c_int, "openmc_gb300_trace_batch")
     trace_first = _DLLGlobal(C.c_int64, "openmc_gb300_trace_first")
     profile_next = _DLLGlobal(C.c_int, "openmc_gb300_profile_next")

@@ -144,6 +144,17 @@ int openmc_gb300_xs_lookup_device(void* handle, int64_t n, const int32_t* d_mat,
   const double* d_E, double* d_out, int32_t* d_grid_hash, int sort);
 int openmc_gb300_xs_last_times(void* handle, float* ms);
 int openmc_gb300_xs_stream(void* handle, void** stream);
+/* No counterpart in the reference: the sorted lookups of
+ * openmc_gb300_xs_lookup_device for callers that cannot allocate device
+ * memory during the call (a memory budget or a pool they do not own).  It
+ * allocates nothing; its sort scratch is a static device array of the
+ * library (about 16 MiB held by every GPU that loads it).  At most 4,194,304
+ * lookups per call and 64 materials, else OPENMC_E_INVALID_ARGUMENT.  The
+ * first call on a device looks up the array's address and should come before
+ * any stream capture; calls that overlap on the GPU share the array and race.
+ * Work is queued on `stream` (cudaStream_t, NULL = default) without waiting. */
+int openmc_gb300_xs_lookup_noalloc(void* handle, int64_t n, const int32_t* d_mat,
+  const double* d_E, double* d_out, int32_t* d_grid_hash, void* stream);
 
 #ifdef __cplusplus
 }

@@ -16,6 +16,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -198,6 +199,21 @@ __global__ void __launch_bounds__(256) k_lookup(Tables T, const int* __restrict_
   } while (0)
 
 }  // namespace xsb
+
+// ---------------------------------------------------------------------------
+// Scratch for openmc_gb300_xs_lookup_noalloc: a fixed-size array in device
+// global memory that the library owns for its whole lifetime (every GPU that
+// loads the library holds these ~16 MiB until the process exits).  Layout:
+// [NOALLOC_MAX_KEYS histogram | NOALLOC_MAX_KEYS cursors | NOALLOC_MAX_LOOKUPS
+// permutation], all int32.
+constexpr long long NOALLOC_MAX_LOOKUPS = 1LL << 22;  // 4,194,304 lookups per call
+constexpr int NOALLOC_MAX_KEYS = 4096;                // materials x 64 energy octaves
+static __device__ __align__(256) int g_noalloc_scratch[2 * NOALLOC_MAX_KEYS + NOALLOC_MAX_LOOKUPS];
+
+__global__ void k_zero_ints(int* p, int n)
+{
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = 0;
+}
 
 extern "C" char openmc_err_msg[256];
 extern "C" int OPENMC_E_ALLOCATE;
@@ -398,6 +414,76 @@ int openmc_gb300_xs_last_times(void* handle, float* ms)
   cudaEventElapsedTime(&ms[0], T->ev[0], T->ev[1]);
   cudaEventElapsedTime(&ms[1], T->ev[1], T->ev[2]);
   return 0;
+}
+
+// No counterpart in the reference.  The same sorted macroscopic-XS lookups as
+// openmc_gb300_xs_lookup_device, for callers that cannot allocate device
+// memory at the time of the call: code running under a memory budget or a
+// pool it does not own, or an embedding host whose allocator must not be
+// re-entered from a solver callback.  The call allocates nothing: the sort
+// scratch is the library's static device array g_noalloc_scratch.
+//
+// - n must not exceed 4,194,304 lookups and the tables at most 64 materials
+//   (4,096 sort keys); larger requests return OPENMC_E_INVALID_ARGUMENT.
+// - The first call on a device looks up the array's device address with
+//   cudaGetSymbolAddress (with that device current) and caches it; make that
+//   first call before any stream capture on the device.
+// - All calls share the one array: calls whose work overlaps on the GPU
+//   (different streams, or other host threads) race and give wrong results.
+//   The histogram part is cleared at the start of every call; the rest is
+//   fully rewritten by each call.
+// - Inputs and outputs are device pointers; the work is queued on `stream`
+//   (a cudaStream_t, null for the legacy default stream) and the call returns
+//   without waiting for it.
+int openmc_gb300_xs_lookup_noalloc(void* handle, int64_t n, const int32_t* d_mat, const double* d_E, double* d_out,
+  int32_t* d_grid_hash, void* stream)
+{
+  static std::mutex lock;
+  static int* scratch_of_device[128] = {nullptr};
+  auto* T = static_cast<Tables*>(handle);
+  try {
+    if (!T || n < 0) throw std::invalid_argument("invalid lookup arguments");
+    if (n > NOALLOC_MAX_LOOKUPS)
+      throw std::invalid_argument("openmc_gb300_xs_lookup_noalloc: " + std::to_string(n) +
+                                  " lookups exceed the static scratch limit of 4194304 per call");
+    if (T->n_keys > NOALLOC_MAX_KEYS)
+      throw std::invalid_argument("openmc_gb300_xs_lookup_noalloc: tables with more than 64 materials "
+                                  "exceed the static sort scratch");
+    if (n == 0) return 0;
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 128) throw std::invalid_argument("device index out of range");
+    int* base;
+    {
+      std::lock_guard<std::mutex> g(lock);
+      if (!scratch_of_device[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess)
+          throw std::runtime_error(std::string("cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
+        scratch_of_device[dev] = static_cast<int*>(p);
+      }
+      base = scratch_of_device[dev];
+    }
+    int* hist = base;
+    int* cursor = base + NOALLOC_MAX_KEYS;
+    int* perm = base + 2 * NOALLOC_MAX_KEYS;
+    cudaStream_t S = static_cast<cudaStream_t>(stream);
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    int blocks = sms * 8;
+    k_zero_ints<<<(T->n_keys + 255) / 256, 256, 0, S>>>(hist, T->n_keys);
+    k_hist<<<blocks, 256, 0, S>>>(d_mat, d_E, n, hist);
+    k_scan<<<1, 1024, 0, S>>>(hist, cursor, T->n_keys);
+    k_scatter<<<blocks, 256, 0, S>>>(d_mat, d_E, n, cursor, perm);
+    if (T->fp32) k_lookup<true><<<blocks, 256, 0, S>>>(*T, d_mat, d_E, perm, n, d_out, d_grid_hash);
+    else k_lookup<false><<<blocks, 256, 0, S>>>(*T, d_mat, d_E, perm, n, d_out, d_grid_hash);
+    CK(cudaGetLastError());
+    return 0;
+  } catch (const std::exception& e) {
+    std::snprintf(openmc_err_msg, sizeof(openmc_err_msg), "%s", e.what());
+    return OPENMC_E_INVALID_ARGUMENT;
+  }
 }
 
 }  // extern "C"

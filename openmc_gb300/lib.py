@@ -151,6 +151,8 @@ _fn("openmc_gb300_xs_lookup_device", [C.c_void_p, C.c_int64, C.c_void_p, C.c_voi
                                       C.c_void_p, C.c_int])
 _fn("openmc_gb300_xs_last_times", [C.c_void_p, _p(C.c_float)])
 _fn("openmc_gb300_xs_stream", [C.c_void_p, _p(C.c_void_p)])
+_fn("openmc_gb300_xs_lookup_noalloc", [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_void_p])
 
 
 # ------------------------------------------------------------- globals
@@ -468,6 +470,14 @@ class XSTables:
     def lookup_device(self, n, d_mat, d_E, d_out, d_hash=None, sort=True):
         """Device pointers (ints) in, asynchronous on the library stream."""
         _dll.openmc_gb300_xs_lookup_device(self.h, int(n), d_mat, d_E, d_out, d_hash, 1 if sort else 0)
+
+    def lookup_noalloc(self, n, d_mat, d_E, d_out, d_hash=None, stream=None):
+        """Sorted lookups without any device allocation in the call: the sort
+        scratch is a static array of the library (at most 4,194,304 lookups
+        per call; calls that overlap on the GPU race).  Device pointers (ints)
+        in; queued on `stream` (a cudaStream_t handle, None for the default
+        stream) without waiting."""
+        _dll.openmc_gb300_xs_lookup_noalloc(self.h, int(n), d_mat, d_E, d_out, d_hash, stream)
 
     def last_times(self):
         ms = (C.c_float * 2)()

@@ -46,10 +46,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--particles", type=int, default=10_000_000)
-    ap.add_argument("--in-flight", type=int, default=0)
+    ap.add_argument("--in-flight", type=int, default=1 << 20, help="particle slots held on the device")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-table extra measurement")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-sample", type=int, default=0, help="histories in the CPU baseline sample")
+    ap.add_argument("--cpu-sample", type=int, default=0,
+                    help="histories in the CPU baseline sample (default 3,000,000: about 10 s on 16 cores)")
     ap.add_argument("--no-graph", action="store_true",
                     help="launch every batch kernel by kernel instead of as one CUDA graph "
                          "(for kernel profilers, which cannot see inside conditional graphs)")
@@ -128,6 +129,14 @@ def peaks():
     return 6800.0, "fallback"
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic
+# byte of each kernel, from an ncu capture of the same kernel on the 2x10^6
+# history lattice with 262,144 slots, matched launch by launch with the
+# OPENMC_GB300_LAUNCH_LOG counts (profiles/advance_lattice17.md).  Traffic
+# per launch scales with the events a launch processes.
+TRAFFIC_PER_ALGORITHMIC_BYTE = {"xs+advance": 1.376, "surface": 1.406, "collision": 1.273}
+
+
 def algorithmic_bytes(detail, levels, fp32):
     """Bytes each kernel must move per batch: the structure-of-arrays fields
     an event reads and writes, the table bytes of each nuclide lookup (two
@@ -161,6 +170,7 @@ def run_gb300(args):
     try:
         lib.settings.xs_fp32 = 1
         lib.settings.particles_in_flight = args.in_flight
+        fused = bool(lib.settings.fuse_xs)
         if args.no_graph:
             lib.settings.profile_next = 2
         lib.simulation_init()
@@ -201,7 +211,7 @@ def run_gb300(args):
     kms = prof["kernel_ms"]
     byts = algorithmic_bytes(prof, levels, True)
     kms = dict(kms)
-    if kms["xs"] == 0.0:  # cross-section event fused into the advance kernel
+    if fused:  # cross-section event inside the advance kernel (its own span only times event records)
         kms["xs+advance"] = kms.pop("advance")
         kms.pop("xs")
     dom = max((k for k in ("xs", "advance", "xs+advance", "surface", "collision", "tail") if k in kms),
@@ -209,8 +219,20 @@ def run_gb300(args):
     peak, peak_kind = peaks()
     achieved = byts[dom] / (kms[dom] * 1e-3) / 1e9
     launches = sum(2 + 11 * int(i) for i in iters)
+    dom_launches = int(prof["iterations"]) if "iterations" in prof else int(iters[-1])
+    alg_per_launch = byts[dom] / max(dom_launches, 1)
+    ratio = TRAFFIC_PER_ALGORITHMIC_BYTE.get(dom)
+    traffic = ratio * alg_per_launch if ratio else None
+    table = {}
+    for k, ms in kms.items():
+        if k in byts and ms > 0:
+            gbs = byts[k] / (ms * 1e-3) / 1e9
+            table[k] = {"ms": ms, "alg_bytes": byts[k], "GB/s": gbs, "frac": gbs / peak}
+        else:
+            table[k] = {"ms": ms}
     out.update(value=value, ms_per_step=total_ms / args.steps, e2e=e2e, e2e_d2h=d2h, clocks=clk,
                launches=launches, dominant=dom, achieved=achieved, peak=peak, peak_kind=peak_kind,
+               traffic=traffic, alg_per_launch=alg_per_launch, dom_launches=dom_launches, kernel_table=table,
                kernel_ms=kms, bytes=byts, detail=detail_timed, profile=prof, iterations=iters)
     if not args.no_fp64:
         lib.init(directory=path)
@@ -228,12 +250,15 @@ def run_gb300(args):
     return out
 
 
-def cpu_baseline(path, sample, threads=None):
+def cpu_baseline(path, sample, threads=None, mode=1):
+    """Oracle transport of `sample` histories of batch 1 on the host cores:
+    mode 1 = event-based loop (100,000 particles in flight, the reference's
+    default max_particles_in_flight), mode 0 = history-based loop."""
     import oracle
     o = oracle.Oracle(path / "model.xml")
     threads = threads or os.cpu_count()
     t0 = time.perf_counter()
-    o.transport(1, 1, sample, mode=1, threads=threads, in_flight=100000)
+    o.transport(1, 1, sample, mode=mode, threads=threads, in_flight=100000 if mode == 1 else 0)
     dt = time.perf_counter() - t0
     return sample / dt, threads, dt
 
@@ -253,7 +278,7 @@ def main():
         if rank != 0:
             return
         path = model_dir(args.particles)
-        sample = args.cpu_sample or 20000
+        sample = args.cpu_sample or 2_000_000
         vals = []
         cores = os.cpu_count()
         for _ in range(args.warmup):
@@ -288,10 +313,12 @@ def main():
     cpu = None
     if not args.no_cpu_baseline:
         path = model_dir(args.particles)
-        sample = args.cpu_sample or 20000
+        sample = args.cpu_sample or 3_000_000
         v, cores, dt = cpu_baseline(path, sample)
+        vh, _, dth = cpu_baseline(path, max(sample // 3, 1000), mode=0)
         cpu = {"value": v, "unit": "particles/s", "cores": cores, "kind": "port",
-               "sample": f"{sample} histories of the same model, event-based loop, OpenMP ({dt:.1f} s)"}
+               "sample": f"{sample} histories of the same model, event-based loop, OpenMP ({dt:.1f} s)",
+               "history_based": {"value": vh, "sample": f"{max(sample // 3, 1000)} histories ({dth:.1f} s)"}}
     line = {
         "metric": METRIC, "value": r["value"], "unit": "particles/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
@@ -306,7 +333,9 @@ def main():
         "clocks": r["clocks"],
         "roofline": {"bound": "hbm", "kernel": r["dominant"], "achieved": r["achieved"], "peak": r["peak"],
                      "unit": "GB/s", "frac": r["achieved"] / r["peak"], "peak_source": r["peak_kind"],
-                     "traffic": None},
+                     "traffic": r["traffic"], "alg_bytes_per_launch": r["alg_per_launch"],
+                     "launches": r["dom_launches"]},
+        "kernels": r["kernel_table"],
         "cpu_baseline": cpu,
         "kernel_ms_profiled_batch": r["kernel_ms"],
         "fp64_xs_particles_per_s": r.get("fp64_value"),

@@ -32,6 +32,7 @@
 // and time does not feed any other quantity of this path.
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <stdexcept>
 #include <string>
@@ -1755,12 +1756,30 @@ BatchStats gpu_run_batch_profiled(GpuSim* G, HModel& m, int batch, bool accumula
     return static_cast<double>(ms);
   };
   cudaStream_t S = G->stream;
+  // OPENMC_GB300_LAUNCH_LOG=<file> appends one CSV line per iteration with
+  // the events each queue kernel processed and its duration, so that a
+  // kernel profiler's n-th advance launch (counted over the process) can be
+  // matched with the work it did.
+  static long long advance_launches = 0;
+  static FILE* launch_log = nullptr;
+  static bool launch_log_checked = false;
+  if (!launch_log_checked) {
+    launch_log_checked = true;
+    if (const char* f = std::getenv("OPENMC_GB300_LAUNCH_LOG")) {
+      launch_log = std::fopen(f, "a");
+      if (launch_log)
+        std::fprintf(launch_log,
+          "advance_launch,batch,iteration,xs_events,xs_calc,xs_nuclide_lookups,mesh_segments,"
+          "collision_nuclide_lookups,surface,collision,advance_ms,surface_ms,collision_ms\n");
+    }
+  }
   CK(cudaEventRecord(ev[0], S));
   k_batch_init<<<nb, nt, 0, S>>>(batch);
   CK(cudaEventRecord(ev[1], S));
   CK(cudaStreamSynchronize(S));
   acc[7] += span(0, 1);
   DCounters c {};
+  unsigned long long prev[7] = {0, 0, 0, 0, 0, 0, 0};
   for (int it = 0; it < (1 << 20); ++it) {
     CK(cudaEventRecord(ev[2], S));
     if (!G->fuse) k_xs<<<nb, nt, 0, S>>>();
@@ -1799,8 +1818,18 @@ BatchStats gpu_run_batch_profiled(GpuSim* G, HModel& m, int batch, bool accumula
     acc[5] += span(7, 8);
     acc[6] += span(8, 9);
     acc[7] += span(9, 10);
+    if (launch_log) {
+      std::fprintf(launch_log, "%lld,%d,%d", advance_launches, batch, it);
+      for (int b = 0; b < 7; ++b) {
+        std::fprintf(launch_log, ",%llu", c.stat[0][b] - prev[b]);
+        prev[b] = c.stat[0][b];
+      }
+      std::fprintf(launch_log, ",%.6f,%.6f,%.6f\n", span(3, 4), span(4, 5), span(5, 6));
+    }
+    ++advance_launches;
     if (!c.more) break;
   }
+  if (launch_log) std::fflush(launch_log);
   double total = 0;
   for (int k = 0; k < 8; ++k) {
     st.kernel_ms[k] = static_cast<float>(acc[k]);

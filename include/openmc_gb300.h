@@ -156,6 +156,26 @@ int openmc_gb300_xs_stream(void* handle, void** stream);
 int openmc_gb300_xs_lookup_noalloc(void* handle, int64_t n, const int32_t* d_mat,
   const double* d_E, double* d_out, int32_t* d_grid_hash, void* stream);
 
+/* Learned weight windows (no reference counterpart; its output replaces the
+ * MAGIC bounds of WeightWindows::update_weights, src/weight_windows.cpp:502-755,
+ * and is consumed unchanged by apply_weight_windows, :56-146).
+ * Importance network (x, y, z, log E) -> log flux: 4 -> 128 -> 128 -> 128 -> 1,
+ * SiLU, BF16 tcgen05 products accumulating in FP32, FP32 master weights,
+ * full-batch Adam (beta 0.9 / 0.999, eps 1e-8).  Parameters are one flat FP32
+ * vector: W1[128][4], b1[128], W2[128][128], b2, W3[128][128], b3, w4[128], b4.
+ * Host pointers throughout; x4 is n rows of 4 features. */
+int openmc_gb300_mlp_n_params(void);
+int openmc_gb300_mlp_create(int64_t max_rows, uint64_t seed, void** handle);
+int openmc_gb300_mlp_free(void* handle);
+int openmc_gb300_mlp_set_data(void* handle, int64_t n, const float* x4, const float* target,
+  const float* weight);
+int openmc_gb300_mlp_train(void* handle, int steps, double lr, float* loss_history);
+int openmc_gb300_mlp_gradients(void* handle, float* grad, float* loss);
+int openmc_gb300_mlp_predict(void* handle, int64_t n, const float* x4, float* y);
+int openmc_gb300_mlp_get_params(void* handle, float* params, int64_t n);
+int openmc_gb300_mlp_set_params(void* handle, const float* params, int64_t n);
+int openmc_gb300_mlp_last_ms(void* handle, float* ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -171,7 +171,12 @@ def shield_materials(directory, n_points, seed):
 
 def shield(directory, particles=1_000_000, batches=10, n_points=11303, seed=4,
            event_based=True, length=200.0, width=50.0, layer=10.0,
-           mesh_dim=(200, 10, 10), weight_windows=None, back_face=10.0):
+           mesh_dim=(200, 10, 10), weight_windows=None, back_face=10.0,
+           energy_groups=None, tally_mesh_windows=False):
+    """Deep-penetration slab shield.  energy_groups: bounds [eV] of an
+    energy filter on the mesh flux tally; tally_mesh_windows: add weight
+    windows on the flux tally's mesh and energy groups with every bound at
+    -1 (no window until a generator or the caller sets them)."""
     directory = Path(directory)
     light, heavy, xs_xml = shield_materials(directory, n_points, seed)
     mats = om.Materials([light, heavy], cross_sections=xs_xml.name)
@@ -197,12 +202,20 @@ def shield(directory, particles=1_000_000, batches=10, n_points=11303, seed=4,
     mesh.upper_right = [length, hw, hw]
     t = om.Tally(name="shield flux")
     t.filters = [om.MeshFilter(mesh)]
+    ebounds = [0.0, 2.0e7 * 1.000001]
+    if energy_groups is not None:
+        ebounds = [float(e) for e in energy_groups]
+        t.filters.append(om.EnergyFilter(ebounds))
     back = om.RegularMesh()
     back.dimension = [1, 1, 1]
     back.lower_left = [length - back_face, -hw, -hw]
     back.upper_right = [length, hw, hw]
     tb = om.Tally(name="back face flux")
     tb.filters = [om.MeshFilter(back)]
+    if tally_mesh_windows:
+        n = int(np.prod(mesh_dim)) * (len(ebounds) - 1)
+        weight_windows = om.WeightWindows(mesh, -np.ones(n), upper_ww_bounds=-np.ones(n),
+                                          energy_bounds=ebounds)
     if weight_windows is not None:
         settings.weight_windows = [weight_windows]
         settings.weight_windows_on = True

@@ -1,0 +1,975 @@
+// Importance MLP for learned weight windows: (x, y, z, log E) -> log flux,
+// 4 -> 128 -> 128 -> 128 -> 1 with SiLU, BF16 weights and activations in the
+// matrix products, FP32 accumulation, FP32 master weights and Adam.
+// No counterpart in the reference; its output feeds the weight-window bounds
+// consumed by apply_weight_windows (src/weight_windows.cpp:56-146).
+//
+// The three hidden-layer products of every training step -- forward
+// (Z = H W^T), input gradient (dH = dZ W) and weight gradient (dW = dZ^T H) --
+// run on the 5th-generation tensor cores: one CTA of 128 threads owns a
+// 128-row tile of D = A B^T (A: rows x K, B: N x K, both K-major BF16), stages
+// 64-wide K chunks of A and B into shared memory in the canonical no-swizzle
+// core-matrix layout (8 rows x 16 bytes per core matrix), and one elected
+// thread issues tcgen05.mma.cta_group::1.kind::f16 (M = 128, N = 16..128,
+// K = 16 per instruction) into an FP32 accumulator in tensor memory.
+// tcgen05.commit signals an mbarrier when the products are done; the four
+// warps read their 32 accumulator rows back with tcgen05.ld and apply the
+// epilogue (bias + SiLU, SiLU derivative, or split-K accumulation).
+// Every mbarrier wait is bounded: on timeout the kernel records an error,
+// releases its tensor memory and returns.
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+namespace mlp {
+
+constexpr int TILE_M = 128;  // rows of D per CTA (tcgen05 M)
+constexpr int KC = 64;       // K elements staged per chunk
+constexpr int HID = 128;     // hidden width
+constexpr int IN_PAD = 16;   // input features padded to one K step
+
+// ------------------------------------------------------------------ PTX
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor (tcgen05): start address >> 4 in bits
+// 0-13, leading-dimension byte offset >> 4 in bits 16-29 (distance between
+// core matrices along K for K-major operands), stride-dimension byte offset
+// >> 4 in bits 32-45 (distance between 8-row groups), the fixed value 0b001
+// in bits 46-48, base offset 0, no swizzle (bits 61-63 = 0).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo)
+{
+  uint64_t d = 0;
+  d |= static_cast<uint64_t>((addr >> 4) & 0x3FFF);
+  d |= static_cast<uint64_t>((lbo >> 4) & 0x3FFF) << 16;
+  d |= static_cast<uint64_t>((sbo >> 4) & 0x3FFF) << 32;
+  d |= 1ull << 46;
+  return d;
+}
+
+// Instruction descriptor for kind::f16: FP32 accumulator (bits 4-5 = 1),
+// BF16 A and B (bits 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0),
+// N >> 3 in bits 17-22, M >> 4 in bits 24-28.
+__host__ __device__ constexpr uint32_t instr_desc(int M, int N)
+{
+  return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(N >> 3) << 17) |
+         (static_cast<uint32_t>(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* smem_dst, uint32_t ncols)
+{
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(smem_dst)),
+               "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
+{
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+  uint32_t accumulate)
+{
+  asm volatile(
+    "{\n\t.reg .pred p;\n\t"
+    "setp.ne.b32 p, %4, 0;\n\t"
+    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+    "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+    : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* mbar)
+{
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                 smem_u32(mbar))
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(count) : "memory");
+}
+
+// Waits for the mbarrier phase with the given parity; gives up after
+// max_tries polls and returns false.
+__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint32_t max_tries)
+{
+  uint32_t addr = smem_u32(mbar);
+  for (uint32_t i = 0; i < max_tries; ++i) {
+    uint32_t done;
+    asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(addr), "r"(parity)
+      : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void fence_async_shared()
+{
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+
+// 32 consecutive FP32 accumulator columns of this thread's row
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
+{
+  uint32_t r[32];
+  asm volatile(
+    "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+    "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+      "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+      "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+    : "r"(taddr)
+    : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
+__device__ __forceinline__ float silu_grad(float z)
+{
+  float s = 1.0f / (1.0f + __expf(-z));
+  return s * (1.0f + z * (1.0f - s));
+}
+
+enum Epi { EPI_FORWARD = 0, EPI_DINPUT = 1, EPI_DWEIGHT = 2 };
+
+struct GemmArgs {
+  const __nv_bfloat16* A;  // rows x K (row stride lda)
+  const __nv_bfloat16* B;  // N x K (row stride ldb)
+  int lda, ldb;
+  int rows;      // valid rows of D (multiple of 128 after padding)
+  int N;         // 16 or 128
+  int K;         // reduction length handled by each CTA (multiple of 16)
+  int k_split;   // EPI_DWEIGHT: K range per CTA; CTA c reduces [c k_split, (c+1) k_split)
+  // epilogue operands
+  const float* bias;      // EPI_FORWARD: [N]
+  float* Z;               // EPI_FORWARD: pre-activation out [rows][N]
+  __nv_bfloat16* H;       // EPI_FORWARD: silu(Z) out [rows][N]
+  const float* Zprev;     // EPI_DINPUT: pre-activation of the layer below [rows][N]
+  __nv_bfloat16* dZprev;  // EPI_DINPUT: dH * silu'(Zprev) out [rows][N]
+  __nv_bfloat16* HT;      // EPI_FORWARD / EPI_DINPUT: optional transposed copy [N][ldT]
+  int ldT;
+  float* dW;              // EPI_DWEIGHT: partial blockIdx.x of [128][N]
+  int* error;
+};
+
+// Copies a tile of `nrows` rows x KC elements (row r of the source at
+// src + r * ld + k0) into shared memory in core-matrix order
+// [row/8][k/8][row%8][k%8]; elements past k_end are zero.
+__device__ __forceinline__ void stage_tile(__nv_bfloat16* dst, const __nv_bfloat16* src, int ld, int nrows, int k0,
+  int k_end, int kc)
+{
+  const int groups = kc / 8;  // 8-element (16-byte) groups per row
+  for (int idx = threadIdx.x; idx < nrows * groups; idx += blockDim.x) {
+    int r = idx / groups, g = idx % groups;
+    int k = k0 + g * 8;
+    uint4 v = make_uint4(0, 0, 0, 0);
+    if (k + 8 <= k_end) v = *reinterpret_cast<const uint4*>(src + static_cast<long long>(r) * ld + k);
+    __nv_bfloat16* out = dst + ((r / 8) * groups + g) * 64 + (r % 8) * 8;
+    *reinterpret_cast<uint4*>(out) = v;
+  }
+}
+
+// ------------------------------------------------------------------ GEMM
+constexpr int MAX_N = 144;                    // 128 outputs + ones row (bias gradient) + padding
+constexpr int A_TILE_BYTES = TILE_M * KC * 2;  // 16 KB
+constexpr int B_TILE_BYTES = MAX_N * KC * 2;   // 18 KB
+constexpr int GEMM_SMEM = 2 * (A_TILE_BYTES + B_TILE_BYTES) + 1024;
+constexpr uint32_t WAIT_TRIES = 1u << 22;
+constexpr int ERR_TIMEOUT = 1;
+
+// D = A B^T for one 128-row tile (EPI_FORWARD, EPI_DINPUT: tile blockIdx.x
+// of the rows; K = the whole reduction) or for one K range of the weight
+// gradient (EPI_DWEIGHT: the 128 output neurons x N inputs, reduced over
+// rows [blockIdx.x k_split, ...), written to partial blockIdx.x).
+// Two shared-memory stages: the 128 threads stage chunk c while the tensor
+// core multiplies chunk c-1; an mbarrier per stage, signalled by
+// tcgen05.commit, says when a stage may be overwritten.
+template <int EPI>
+__global__ void __launch_bounds__(128, 1) k_gemm(GemmArgs g)
+{
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  __nv_bfloat16* sA[2] = {reinterpret_cast<__nv_bfloat16*>(base),
+                          reinterpret_cast<__nv_bfloat16*>(base + A_TILE_BYTES)};
+  __nv_bfloat16* sB[2] = {reinterpret_cast<__nv_bfloat16*>(base + 2 * A_TILE_BYTES),
+                          reinterpret_cast<__nv_bfloat16*>(base + 2 * A_TILE_BYTES + B_TILE_BYTES)};
+  __shared__ __align__(8) uint64_t mbar[2];
+  __shared__ uint32_t tmem_s;
+
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const uint32_t ncols = g.N <= 128 ? 128u : 256u;
+  if (warp == 0) tmem_alloc(&tmem_s, ncols);
+  if (threadIdx.x == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_s;
+
+  long long row0 = 0;
+  int k_begin = 0, k_end = g.K;
+  const __nv_bfloat16* A = g.A;
+  if (EPI == EPI_DWEIGHT) {
+    k_begin = blockIdx.x * g.k_split;
+    k_end = min(g.K, k_begin + g.k_split);
+  } else {
+    row0 = static_cast<long long>(blockIdx.x) * TILE_M;
+    A = g.A + row0 * g.lda;
+  }
+  const int n_chunks = k_end > k_begin ? (k_end - k_begin + KC - 1) / KC : 0;
+  const uint32_t idesc = instr_desc(TILE_M, g.N);
+  bool ok = true;
+  for (int c = 0; c < n_chunks && ok; ++c) {
+    const int s = c & 1;
+    if (c >= 2) ok = mbar_wait(&mbar[s], ((c - 2) >> 1) & 1, WAIT_TRIES);
+    ok = __syncthreads_and(ok);
+    if (!ok) break;
+    const int k0 = k_begin + c * KC;
+    stage_tile(sA[s], A, g.lda, TILE_M, k0, k_end, KC);
+    stage_tile(sB[s], g.B, g.ldb, g.N, k0, k_end, KC);
+    fence_async_shared();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tc_fence_after();
+      const int nk = min(KC, k_end - k0);
+      const uint32_t a0 = smem_u32(sA[s]), b0 = smem_u32(sB[s]);
+      for (int j = 0; j * 16 < nk; ++j) {
+        // K step j: two core matrices (2 x 128 B) further along K
+        uint64_t ad = smem_desc(a0 + j * 256, 128, 1024);
+        uint64_t bd = smem_desc(b0 + j * 256, 128, 1024);
+        mma_bf16(tmem, ad, bd, idesc, (c > 0 || j > 0) ? 1u : 0u);
+      }
+      mma_commit(&mbar[s]);
+    }
+  }
+  if (n_chunks > 0) {
+    const int last = n_chunks - 1;
+    bool done = mbar_wait(&mbar[last & 1], (last >> 1) & 1, WAIT_TRIES);
+    ok = __syncthreads_and(ok && done);
+  }
+  if (!ok) {
+    if (threadIdx.x == 0) atomicOr(g.error, ERR_TIMEOUT);
+  } else {
+    tc_fence_after();
+    const uint32_t t_row = tmem + (static_cast<uint32_t>(32 * warp) << 16);
+    float v[32];
+    if (EPI == EPI_DWEIGHT) {
+      const int m = 32 * warp + lane;
+      float* out = g.dW + static_cast<long long>(blockIdx.x) * TILE_M * g.N + static_cast<long long>(m) * g.N;
+      for (int cb = 0; cb < g.N; cb += 32) {
+        if (n_chunks > 0) tmem_ld32(t_row + cb, v);
+        else for (int k = 0; k < 32; ++k) v[k] = 0.0f;
+        for (int k = 0; k < 32 && cb + k < g.N; ++k) out[cb + k] = v[k];
+      }
+    } else {
+      const long long r = row0 + 32 * warp + lane;
+      for (int cb = 0; cb < g.N; cb += 32) {
+        tmem_ld32(t_row + cb, v);
+        __align__(16) __nv_bfloat16 hb[32];
+        if (EPI == EPI_FORWARD) {
+          float* zr = g.Z + r * g.N + cb;
+#pragma unroll
+          for (int k = 0; k < 32; ++k) {
+            float z = v[k] + g.bias[cb + k];
+            zr[k] = z;
+            hb[k] = __float2bfloat16_rn(silu(z));
+          }
+        } else {
+          const float* zp = g.Zprev + r * g.N + cb;
+#pragma unroll
+          for (int k = 0; k < 32; ++k) hb[k] = __float2bfloat16_rn(v[k] * silu_grad(zp[k]));
+        }
+        __nv_bfloat16* dst = (EPI == EPI_FORWARD ? g.H : g.dZprev) + r * g.N + cb;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          reinterpret_cast<uint4*>(dst)[q] = reinterpret_cast<const uint4*>(hb)[q];
+        if (g.HT) {
+#pragma unroll
+          for (int k = 0; k < 32; ++k) g.HT[static_cast<long long>(cb + k) * g.ldT + r] = hb[k];
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, ncols);
+  }
+}
+
+// ------------------------------------------------------------------ output layer
+// y = H3 . w4 + b4 in FP32 (one thread per row), the weighted squared-error
+// loss against the target, and the start of the backward pass:
+// dZ3 = (dL/dy) w4 * silu'(Z3).  Per-block partial sums of dL/dw4 (128),
+// dL/db4 and the loss go to partial[block][130] in a fixed order.
+// Block 0 advances the optimizer step counter.
+__global__ void __launch_bounds__(128) k_head(const __nv_bfloat16* __restrict__ H3, const float* __restrict__ Z3,
+  const float* __restrict__ w4, const float* __restrict__ b4, const float* __restrict__ target,
+  const float* __restrict__ weight, int n_real, int R_pad, float inv_n, __nv_bfloat16* dZ3, __nv_bfloat16* dZ3T,
+  float* partial, float* y_out, int* step)
+{
+  __shared__ float sw[HID], sdy[TILE_M], sl[TILE_M];
+  const int t = threadIdx.x;
+  const long long row0 = static_cast<long long>(blockIdx.x) * TILE_M;
+  const long long r = row0 + t;
+  sw[t] = w4[t];
+  __syncthreads();
+  const __nv_bfloat16* h = H3 + r * HID;
+  float y = b4[0];
+  for (int k = 0; k < HID; k += 8) {
+    uint4 q = *reinterpret_cast<const uint4*>(h + k);
+    const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&q);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) y = fmaf(__bfloat162float(e[j]), sw[k + j], y);
+  }
+  if (y_out && r < n_real) y_out[r] = y;
+  if (!dZ3) return;
+  float dy = 0.0f, loss = 0.0f;
+  if (r < n_real) {
+    const float wt = weight ? weight[r] : 1.0f;
+    const float e = y - target[r];
+    loss = wt * e * e * inv_n;
+    dy = 2.0f * wt * e * inv_n;
+  }
+  const float* z = Z3 + r * HID;
+  for (int k = 0; k < HID; k += 8) {
+    __align__(16) __nv_bfloat16 d[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) d[j] = __float2bfloat16_rn(dy * sw[k + j] * silu_grad(z[k + j]));
+    *reinterpret_cast<uint4*>(dZ3 + r * HID + k) = *reinterpret_cast<const uint4*>(d);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) dZ3T[static_cast<long long>(k + j) * R_pad + r] = d[j];
+  }
+  sdy[t] = dy;
+  sl[t] = loss;
+  __syncthreads();
+  float acc = 0.0f;
+  for (int rr = 0; rr < TILE_M; ++rr) acc = fmaf(sdy[rr], __bfloat162float(H3[(row0 + rr) * HID + t]), acc);
+  float* out = partial + static_cast<long long>(blockIdx.x) * 130;
+  out[t] = acc;
+  if (t == 0) {
+    float sd = 0.0f, ss = 0.0f;
+    for (int rr = 0; rr < TILE_M; ++rr) {
+      sd += sdy[rr];
+      ss += sl[rr];
+    }
+    out[128] = sd;
+    out[129] = ss;
+    if (blockIdx.x == 0) step[0] += 1;
+  }
+}
+
+// ------------------------------------------------------------------ parameters
+// Flat FP32 parameter vector: W1[128][4], b1[128], W2[128][128], b2[128],
+// W3[128][128], b3[128], w4[128], b4.
+constexpr int P_W1 = 0, P_B1 = 512, P_W2 = 640, P_B2 = P_W2 + 16384, P_W3 = P_B2 + 128, P_B3 = P_W3 + 16384,
+              P_W4 = P_B3 + 128, P_B4 = P_W4 + 128, N_PARAMS = P_B4 + 1;
+constexpr int G1_N = 16, G_N = 144;  // row widths of the weight-gradient partials
+
+struct AdamArgs {
+  float* P;
+  float* m;
+  float* v;
+  const float* G1;  // [splits][128][16]: cols 0-3 dW1, col 4 db1
+  const float* G2;  // [splits][128][144]: cols 0-127 dW2, col 128 db2
+  const float* G3;
+  const float* GH;  // [head_blocks][130]: dw4, db4, loss
+  int splits, head_blocks;
+  float lr, beta1, beta2, eps;
+  const int* step;
+  int update;       // 0: gradients only
+  float* grad_out;  // optional flat gradient [N_PARAMS]
+  float* loss_out;  // optional loss of this step (indexed by step - 1)
+  __nv_bfloat16 *W1, *W2, *W2T, *W3, *W3T;  // BF16 operand copies
+};
+
+__device__ __forceinline__ float sum_partials(const float* G, int splits, long long stride, long long off)
+{
+  float s = 0.0f;
+  for (int k = 0; k < splits; ++k) s += G[k * stride + off];
+  return s;
+}
+
+// One thread per parameter: sums the gradient partials in a fixed order,
+// applies Adam (bias-corrected first and second moments) and rewrites the
+// BF16 operand copies (W and its transpose for the input-gradient product).
+__global__ void k_adam(AdamArgs a)
+{
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= N_PARAMS) return;
+  const long long s1 = 128LL * G1_N, s2 = 128LL * G_N;
+  float g;
+  if (p < P_B1) g = sum_partials(a.G1, a.splits, s1, (p / 4) * G1_N + p % 4);
+  else if (p < P_W2) g = sum_partials(a.G1, a.splits, s1, (p - P_B1) * G1_N + 4);
+  else if (p < P_B2) g = sum_partials(a.G2, a.splits, s2, ((p - P_W2) / 128) * G_N + (p - P_W2) % 128);
+  else if (p < P_W3) g = sum_partials(a.G2, a.splits, s2, (p - P_B2) * G_N + 128);
+  else if (p < P_B3) g = sum_partials(a.G3, a.splits, s2, ((p - P_W3) / 128) * G_N + (p - P_W3) % 128);
+  else if (p < P_W4) g = sum_partials(a.G3, a.splits, s2, (p - P_B3) * G_N + 128);
+  else if (p < P_B4) g = sum_partials(a.GH, a.head_blocks, 130, p - P_W4);
+  else g = sum_partials(a.GH, a.head_blocks, 130, 128);
+  if (a.grad_out) a.grad_out[p] = g;
+  const int t = a.step[0];
+  if (p == 0 && a.loss_out && t > 0) a.loss_out[t - 1] = sum_partials(a.GH, a.head_blocks, 130, 129);
+  float w = a.P[p];
+  if (a.update) {
+    float m = a.beta1 * a.m[p] + (1.0f - a.beta1) * g;
+    float v = a.beta2 * a.v[p] + (1.0f - a.beta2) * g * g;
+    a.m[p] = m;
+    a.v[p] = v;
+    const float mh = m / (1.0f - powf(a.beta1, static_cast<float>(t)));
+    const float vh = v / (1.0f - powf(a.beta2, static_cast<float>(t)));
+    w -= a.lr * mh / (sqrtf(vh) + a.eps);
+    a.P[p] = w;
+  }
+  const __nv_bfloat16 wb = __float2bfloat16_rn(w);
+  if (p < P_B1) {
+    a.W1[(p / 4) * IN_PAD + p % 4] = wb;
+  } else if (p >= P_W2 && p < P_B2) {
+    const int o = (p - P_W2) / 128, i = (p - P_W2) % 128;
+    a.W2[o * HID + i] = wb;
+    a.W2T[i * HID + o] = wb;
+  } else if (p >= P_W3 && p < P_B3) {
+    const int o = (p - P_W3) / 128, i = (p - P_W3) % 128;
+    a.W3[o * HID + i] = wb;
+    a.W3T[i * HID + o] = wb;
+  }
+}
+
+// ------------------------------------------------------------------ input staging
+// Writes the BF16 input tile X0[R][16] (features 0-3, zero padding), its
+// transpose X0T[16][R] (row 4 = 1 so that column 4 of the first weight
+// gradient is the bias gradient), and the constant rows 128-143 of the
+// transposed hidden activations (row 128 = 1 for the same reason).
+__global__ void k_prepare(const float* __restrict__ x4, long long n, long long R, __nv_bfloat16* X0,
+  __nv_bfloat16* X0T, __nv_bfloat16* H1T, __nv_bfloat16* H2T)
+{
+  const __nv_bfloat16 one = __float2bfloat16_rn(1.0f), zero = __float2bfloat16_rn(0.0f);
+  for (long long r = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; r < R;
+       r += static_cast<long long>(gridDim.x) * blockDim.x) {
+    for (int i = 0; i < IN_PAD; ++i) {
+      __nv_bfloat16 v = (i < 4 && r < n) ? __float2bfloat16_rn(x4[r * 4 + i]) : zero;
+      X0[r * IN_PAD + i] = v;
+      X0T[i * R + r] = (i == 4) ? one : v;
+    }
+    if (H1T) {
+      for (int i = HID; i < MAX_N; ++i) {
+        H1T[i * R + r] = (i == HID) ? one : zero;
+        H2T[i * R + r] = (i == HID) ? one : zero;
+      }
+    }
+  }
+}
+
+__global__ void k_fill_f32(float* p, long long n, float v)
+{
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x)
+    p[i] = v;
+}
+
+// ------------------------------------------------------------------ host
+#define MLP_CK(x)                                                                                    \
+  do {                                                                                               \
+    cudaError_t e_ = (x);                                                                            \
+    if (e_ != cudaSuccess) throw std::runtime_error(std::string("CUDA: ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+struct Net {
+  int device = 0;
+  long long cap = 0;  // rows (multiple of 128)
+  long long n = 0, R = 0;
+  int splits = 0, k_split = 0;
+  int max_splits = 0;
+  cudaStream_t stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  float graph_lr = -1.0f;
+  float last_ms = 0.0f;
+  // parameters, optimizer state, gradients
+  float *P = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr, *loss_hist = nullptr;
+  int *step = nullptr, *err = nullptr;
+  long long loss_cap = 0;
+  __nv_bfloat16 *W1 = nullptr, *W2 = nullptr, *W2T = nullptr, *W3 = nullptr, *W3T = nullptr;
+  float *G1 = nullptr, *G2 = nullptr, *G3 = nullptr, *GH = nullptr;
+  // data and activations
+  float *x4 = nullptr, *target = nullptr, *weight = nullptr, *y = nullptr;
+  __nv_bfloat16 *X0 = nullptr, *X0T = nullptr;
+  float *Z1 = nullptr, *Z2 = nullptr, *Z3 = nullptr;
+  __nv_bfloat16 *H1 = nullptr, *H2 = nullptr, *H3 = nullptr, *H1T = nullptr, *H2T = nullptr;
+  __nv_bfloat16 *dZ1 = nullptr, *dZ2 = nullptr, *dZ3 = nullptr, *dZ1T = nullptr, *dZ2T = nullptr, *dZ3T = nullptr;
+  std::vector<void*> allocs;
+
+  template <class T>
+  T* alloc(size_t count)
+  {
+    void* p = nullptr;
+    MLP_CK(cudaMalloc(&p, count * sizeof(T) + 16));
+    MLP_CK(cudaMemset(p, 0, count * sizeof(T) + 16));
+    allocs.push_back(p);
+    return static_cast<T*>(p);
+  }
+
+  ~Net()
+  {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (void* p : allocs) cudaFree(p);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+static bool g_attr_set[64] = {false};
+
+static void set_gemm_attributes(int dev)
+{
+  if (dev >= 0 && dev < 64 && g_attr_set[dev]) return;
+  MLP_CK(cudaFuncSetAttribute(k_gemm<EPI_FORWARD>, cudaFuncAttributeMaxDynamicSharedMemorySize, GEMM_SMEM));
+  MLP_CK(cudaFuncSetAttribute(k_gemm<EPI_DINPUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, GEMM_SMEM));
+  MLP_CK(cudaFuncSetAttribute(k_gemm<EPI_DWEIGHT>, cudaFuncAttributeMaxDynamicSharedMemorySize, GEMM_SMEM));
+  if (dev >= 0 && dev < 64) g_attr_set[dev] = true;
+}
+
+static GemmArgs gemm_args(Net& N)
+{
+  GemmArgs g;
+  std::memset(&g, 0, sizeof(g));
+  g.error = N.err;
+  return g;
+}
+
+template <int EPI>
+static void launch_gemm(Net& N, const GemmArgs& g, int grid)
+{
+  k_gemm<EPI><<<grid, 128, GEMM_SMEM, N.stream>>>(g);
+  MLP_CK(cudaGetLastError());
+}
+
+// Forward pass over the N.R staged rows; `train` also writes the transposed
+// activations and runs the output layer's backward part.
+static void enqueue_forward(Net& N, bool train, float* y_out)
+{
+  const int tiles = static_cast<int>(N.R / TILE_M);
+  const int ldT = static_cast<int>(N.R);
+  GemmArgs g = gemm_args(N);
+  g.A = N.X0; g.lda = IN_PAD; g.B = N.W1; g.ldb = IN_PAD; g.K = IN_PAD; g.N = HID;
+  g.bias = N.P + P_B1; g.Z = N.Z1; g.H = N.H1; g.HT = train ? N.H1T : nullptr; g.ldT = ldT;
+  launch_gemm<EPI_FORWARD>(N, g, tiles);
+  g.A = N.H1; g.lda = HID; g.B = N.W2; g.ldb = HID; g.K = HID;
+  g.bias = N.P + P_B2; g.Z = N.Z2; g.H = N.H2; g.HT = train ? N.H2T : nullptr;
+  launch_gemm<EPI_FORWARD>(N, g, tiles);
+  g.A = N.H2; g.B = N.W3; g.bias = N.P + P_B3; g.Z = N.Z3; g.H = N.H3; g.HT = nullptr;
+  launch_gemm<EPI_FORWARD>(N, g, tiles);
+  const float inv_n = N.n > 0 ? 1.0f / static_cast<float>(N.n) : 0.0f;
+  k_head<<<tiles, TILE_M, 0, N.stream>>>(N.H3, N.Z3, N.P + P_W4, N.P + P_B4, N.target, N.weight,
+    static_cast<int>(N.n), static_cast<int>(N.R), inv_n, train ? N.dZ3 : nullptr, N.dZ3T, N.GH, y_out, N.step);
+  MLP_CK(cudaGetLastError());
+}
+
+static void enqueue_backward(Net& N)
+{
+  const int tiles = static_cast<int>(N.R / TILE_M);
+  const int K = static_cast<int>(N.R);
+  GemmArgs g = gemm_args(N);
+  // dW3 = dZ3^T [H2 | 1]
+  g.A = N.dZ3T; g.lda = K; g.B = N.H2T; g.ldb = K; g.K = K; g.N = G_N; g.k_split = N.k_split; g.dW = N.G3;
+  launch_gemm<EPI_DWEIGHT>(N, g, N.splits);
+  // dZ2 = (dZ3 W3) * silu'(Z2)
+  g = gemm_args(N);
+  g.A = N.dZ3; g.lda = HID; g.B = N.W3T; g.ldb = HID; g.K = HID; g.N = HID;
+  g.Zprev = N.Z2; g.dZprev = N.dZ2; g.HT = N.dZ2T; g.ldT = K;
+  launch_gemm<EPI_DINPUT>(N, g, tiles);
+  // dW2 = dZ2^T [H1 | 1]
+  g = gemm_args(N);
+  g.A = N.dZ2T; g.lda = K; g.B = N.H1T; g.ldb = K; g.K = K; g.N = G_N; g.k_split = N.k_split; g.dW = N.G2;
+  launch_gemm<EPI_DWEIGHT>(N, g, N.splits);
+  // dZ1 = (dZ2 W2) * silu'(Z1)
+  g = gemm_args(N);
+  g.A = N.dZ2; g.lda = HID; g.B = N.W2T; g.ldb = HID; g.K = HID; g.N = HID;
+  g.Zprev = N.Z1; g.dZprev = N.dZ1; g.HT = N.dZ1T; g.ldT = K;
+  launch_gemm<EPI_DINPUT>(N, g, tiles);
+  // dW1 = dZ1^T [X0 | 1]
+  g = gemm_args(N);
+  g.A = N.dZ1T; g.lda = K; g.B = N.X0T; g.ldb = K; g.K = K; g.N = G1_N; g.k_split = N.k_split; g.dW = N.G1;
+  launch_gemm<EPI_DWEIGHT>(N, g, N.splits);
+}
+
+static AdamArgs adam_args(Net& N, int update, float lr)
+{
+  AdamArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.P = N.P; a.m = N.m; a.v = N.v;
+  a.G1 = N.G1; a.G2 = N.G2; a.G3 = N.G3; a.GH = N.GH;
+  a.splits = N.splits; a.head_blocks = static_cast<int>(N.R / TILE_M);
+  a.lr = lr; a.beta1 = 0.9f; a.beta2 = 0.999f; a.eps = 1e-8f;
+  a.step = N.step; a.update = update;
+  a.W1 = N.W1; a.W2 = N.W2; a.W2T = N.W2T; a.W3 = N.W3; a.W3T = N.W3T;
+  return a;
+}
+
+static void enqueue_adam(Net& N, const AdamArgs& a)
+{
+  k_adam<<<(N_PARAMS + 255) / 256, 256, 0, N.stream>>>(a);
+  MLP_CK(cudaGetLastError());
+}
+
+static void check_error(Net& N)
+{
+  int e = 0;
+  MLP_CK(cudaMemcpyAsync(&e, N.err, sizeof(int), cudaMemcpyDeviceToHost, N.stream));
+  MLP_CK(cudaStreamSynchronize(N.stream));
+  if (e) {
+    MLP_CK(cudaMemsetAsync(N.err, 0, sizeof(int), N.stream));
+    throw std::runtime_error("tensor-core product did not complete within its wait limit");
+  }
+}
+
+static void drop_graph(Net& N)
+{
+  if (N.exec) cudaGraphExecDestroy(N.exec);
+  if (N.graph) cudaGraphDestroy(N.graph);
+  N.exec = nullptr;
+  N.graph = nullptr;
+}
+
+static uint64_t splitmix(uint64_t& s)
+{
+  uint64_t z = (s += 0x9E3779B97F4A7C15ULL);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+// LeCun-uniform weights (variance 1/fan_in), zero biases.
+static std::vector<float> init_params(uint64_t seed)
+{
+  std::vector<float> p(N_PARAMS, 0.0f);
+  uint64_t s = seed;
+  auto fill = [&](int off, int count, int fan_in) {
+    const double a = std::sqrt(3.0 / fan_in);
+    for (int i = 0; i < count; ++i) {
+      double u = static_cast<double>(splitmix(s) >> 11) * (1.0 / 9007199254740992.0);
+      p[off + i] = static_cast<float>((2.0 * u - 1.0) * a);
+    }
+  };
+  fill(P_W1, 512, 4);
+  fill(P_W2, 16384, HID);
+  fill(P_W3, 16384, HID);
+  fill(P_W4, HID, HID);
+  return p;
+}
+
+static void upload_params(Net& N, const float* p)
+{
+  MLP_CK(cudaMemcpyAsync(N.P, p, sizeof(float) * N_PARAMS, cudaMemcpyHostToDevice, N.stream));
+  MLP_CK(cudaMemsetAsync(N.m, 0, sizeof(float) * N_PARAMS, N.stream));
+  MLP_CK(cudaMemsetAsync(N.v, 0, sizeof(float) * N_PARAMS, N.stream));
+  MLP_CK(cudaMemsetAsync(N.step, 0, sizeof(int), N.stream));
+  // refresh the BF16 copies without an update (no gradient partials yet: splits = 0)
+  AdamArgs a = adam_args(N, 0, 0.0f);
+  a.splits = 0;
+  a.head_blocks = 0;
+  enqueue_adam(N, a);
+  MLP_CK(cudaStreamSynchronize(N.stream));
+}
+
+}  // namespace mlp
+
+// ------------------------------------------------------------------ C API
+extern "C" char openmc_err_msg[256];
+extern "C" int OPENMC_E_ALLOCATE;
+extern "C" int OPENMC_E_INVALID_ARGUMENT;
+extern "C" int OPENMC_E_UNASSIGNED;
+
+namespace {
+
+int fail(int code, const char* what)
+{
+  std::snprintf(openmc_err_msg, sizeof(openmc_err_msg), "%s", what);
+  return code;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Number of FP32 parameters of the importance network (33,793).
+int openmc_gb300_mlp_n_params(void) { return mlp::N_PARAMS; }
+
+// Creates a network with seeded LeCun-uniform weights on the current device,
+// with room for max_rows training or query rows.
+int openmc_gb300_mlp_create(int64_t max_rows, uint64_t seed, void** handle)
+{
+  using namespace mlp;
+  if (!handle || max_rows <= 0) return fail(OPENMC_E_INVALID_ARGUMENT, "invalid network capacity");
+  Net* N = nullptr;
+  try {
+    N = new Net();
+    MLP_CK(cudaGetDevice(&N->device));
+    set_gemm_attributes(N->device);
+    MLP_CK(cudaStreamCreateWithFlags(&N->stream, cudaStreamNonBlocking));
+    N->cap = (max_rows + TILE_M - 1) / TILE_M * TILE_M;
+    const long long R = N->cap;
+    N->max_splits = 160;
+    N->P = N->alloc<float>(N_PARAMS);
+    N->m = N->alloc<float>(N_PARAMS);
+    N->v = N->alloc<float>(N_PARAMS);
+    N->grad = N->alloc<float>(N_PARAMS);
+    N->loss_cap = 1 << 16;
+    N->loss_hist = N->alloc<float>(N->loss_cap);
+    N->step = N->alloc<int>(1);
+    N->err = N->alloc<int>(1);
+    N->W1 = N->alloc<__nv_bfloat16>(HID * IN_PAD);
+    N->W2 = N->alloc<__nv_bfloat16>(HID * HID);
+    N->W2T = N->alloc<__nv_bfloat16>(HID * HID);
+    N->W3 = N->alloc<__nv_bfloat16>(HID * HID);
+    N->W3T = N->alloc<__nv_bfloat16>(HID * HID);
+    N->G1 = N->alloc<float>(static_cast<size_t>(N->max_splits) * HID * G1_N);
+    N->G2 = N->alloc<float>(static_cast<size_t>(N->max_splits) * HID * G_N);
+    N->G3 = N->alloc<float>(static_cast<size_t>(N->max_splits) * HID * G_N);
+    N->GH = N->alloc<float>(static_cast<size_t>(R / TILE_M) * 130);
+    N->x4 = N->alloc<float>(R * 4);
+    N->target = N->alloc<float>(R);
+    N->weight = N->alloc<float>(R);
+    N->y = N->alloc<float>(R);
+    N->X0 = N->alloc<__nv_bfloat16>(R * IN_PAD);
+    N->X0T = N->alloc<__nv_bfloat16>(R * IN_PAD);
+    N->Z1 = N->alloc<float>(R * HID);
+    N->Z2 = N->alloc<float>(R * HID);
+    N->Z3 = N->alloc<float>(R * HID);
+    N->H1 = N->alloc<__nv_bfloat16>(R * HID);
+    N->H2 = N->alloc<__nv_bfloat16>(R * HID);
+    N->H3 = N->alloc<__nv_bfloat16>(R * HID);
+    N->H1T = N->alloc<__nv_bfloat16>(R * MAX_N);
+    N->H2T = N->alloc<__nv_bfloat16>(R * MAX_N);
+    N->dZ1 = N->alloc<__nv_bfloat16>(R * HID);
+    N->dZ2 = N->alloc<__nv_bfloat16>(R * HID);
+    N->dZ3 = N->alloc<__nv_bfloat16>(R * HID);
+    N->dZ1T = N->alloc<__nv_bfloat16>(R * HID);
+    N->dZ2T = N->alloc<__nv_bfloat16>(R * HID);
+    N->dZ3T = N->alloc<__nv_bfloat16>(R * HID);
+    std::vector<float> p = init_params(seed);
+    upload_params(*N, p.data());
+    *handle = N;
+    return 0;
+  } catch (const std::exception& e) {
+    delete N;
+    return fail(OPENMC_E_ALLOCATE, e.what());
+  }
+}
+
+int openmc_gb300_mlp_free(void* handle)
+{
+  delete static_cast<mlp::Net*>(handle);
+  return 0;
+}
+
+// Stages n training rows: x4 = n x (x, y, z, log E) features (host, FP32,
+// already scaled to about [-1, 1]), target = n values of the regression
+// target, weight = n per-row loss weights (NULL: all 1).
+int openmc_gb300_mlp_set_data(void* handle, int64_t n, const float* x4, const float* target, const float* weight)
+{
+  using namespace mlp;
+  Net* N = static_cast<Net*>(handle);
+  if (!N || n <= 0 || !x4 || !target) return fail(OPENMC_E_INVALID_ARGUMENT, "invalid training data");
+  try {
+    const long long R = (n + TILE_M - 1) / TILE_M * TILE_M;
+    if (R > N->cap) return fail(OPENMC_E_INVALID_ARGUMENT, "more rows than the network was created for");
+    N->n = n;
+    N->R = R;
+    long long per = (R + 147) / 148;
+    N->k_split = static_cast<int>(std::max<long long>(256, (per + KC - 1) / KC * KC));
+    N->splits = static_cast<int>((R + N->k_split - 1) / N->k_split);
+    if (N->splits > N->max_splits) return fail(OPENMC_E_INVALID_ARGUMENT, "too many gradient partials");
+    MLP_CK(cudaMemsetAsync(N->target, 0, sizeof(float) * R, N->stream));
+    MLP_CK(cudaMemcpyAsync(N->x4, x4, sizeof(float) * 4 * n, cudaMemcpyHostToDevice, N->stream));
+    MLP_CK(cudaMemcpyAsync(N->target, target, sizeof(float) * n, cudaMemcpyHostToDevice, N->stream));
+    if (weight) {
+      MLP_CK(cudaMemsetAsync(N->weight, 0, sizeof(float) * R, N->stream));
+      MLP_CK(cudaMemcpyAsync(N->weight, weight, sizeof(float) * n, cudaMemcpyHostToDevice, N->stream));
+    } else {
+      k_fill_f32<<<64, 256, 0, N->stream>>>(N->weight, R, 1.0f);
+      MLP_CK(cudaGetLastError());
+    }
+    k_prepare<<<152, 256, 0, N->stream>>>(N->x4, n, R, N->X0, N->X0T, N->H1T, N->H2T);
+    MLP_CK(cudaGetLastError());
+    MLP_CK(cudaStreamSynchronize(N->stream));
+    drop_graph(*N);
+    return 0;
+  } catch (const std::exception& e) {
+    return fail(OPENMC_E_ALLOCATE, e.what());
+  }
+}
+
+// Runs `steps` full-batch Adam steps (learning rate lr) on the staged rows,
+// as one CUDA graph per step.  loss_history (host, may be NULL) receives the
+// loss before each step's update.
+int openmc_gb300_mlp_train(void* handle, int steps, double lr, float* loss_history)
+{
+  using namespace mlp;
+  Net* N = static_cast<Net*>(handle);
+  if (!N || steps < 0 || N->R == 0) return fail(OPENMC_E_INVALID_ARGUMENT, "no training data staged");
+  try {
+    int t0 = 0;
+    MLP_CK(cudaMemcpyAsync(&t0, N->step, sizeof(int), cudaMemcpyDeviceToHost, N->stream));
+    MLP_CK(cudaStreamSynchronize(N->stream));
+    if (t0 + steps > N->loss_cap) return fail(OPENMC_E_INVALID_ARGUMENT, "too many optimizer steps");
+    if (!N->exec || N->graph_lr != static_cast<float>(lr)) {
+      drop_graph(*N);
+      MLP_CK(cudaStreamBeginCapture(N->stream, cudaStreamCaptureModeThreadLocal));
+      enqueue_forward(*N, true, nullptr);
+      enqueue_backward(*N);
+      AdamArgs a = adam_args(*N, 1, static_cast<float>(lr));
+      a.loss_out = N->loss_hist;
+      enqueue_adam(*N, a);
+      MLP_CK(cudaStreamEndCapture(N->stream, &N->graph));
+      MLP_CK(cudaGraphInstantiate(&N->exec, N->graph, 0));
+      N->graph_lr = static_cast<float>(lr);
+    }
+    cudaEvent_t e0, e1;
+    MLP_CK(cudaEventCreate(&e0));
+    MLP_CK(cudaEventCreate(&e1));
+    MLP_CK(cudaEventRecord(e0, N->stream));
+    for (int s = 0; s < steps; ++s) MLP_CK(cudaGraphLaunch(N->exec, N->stream));
+    MLP_CK(cudaEventRecord(e1, N->stream));
+    MLP_CK(cudaEventSynchronize(e1));
+    MLP_CK(cudaEventElapsedTime(&N->last_ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    check_error(*N);
+    if (loss_history && steps > 0)
+      MLP_CK(cudaMemcpy(loss_history, N->loss_hist + t0, sizeof(float) * steps, cudaMemcpyDeviceToHost));
+    return 0;
+  } catch (const std::exception& e) {
+    return fail(OPENMC_E_UNASSIGNED, e.what());
+  }
+}
+
+// One forward and backward pass over the staged rows without an update:
+// grad (host, n_params floats) receives dLoss/dparams, loss the loss.
+int openmc_gb300_mlp_gradients(void* handle, float* grad, float* loss)
+{
+  using namespace mlp;
+  Net* N = static_cast<Net*>(handle);
+  if (!N || N->R == 0 || !grad) return fail(OPENMC_E_INVALID_ARGUMENT, "no training data staged");
+  try {
+    int t0 = 0;
+    MLP_CK(cudaMemcpyAsync(&t0, N->step, sizeof(int), cudaMemcpyDeviceToHost, N->stream));
+    MLP_CK(cudaStreamSynchronize(N->stream));
+    enqueue_forward(*N, true, nullptr);
+    enqueue_backward(*N);
+    AdamArgs a = adam_args(*N, 0, 0.0f);
+    a.grad_out = N->grad;
+    enqueue_adam(*N, a);
+    check_error(*N);
+    MLP_CK(cudaMemcpy(grad, N->grad, sizeof(float) * N_PARAMS, cudaMemcpyDeviceToHost));
+    if (loss) {
+      std::vector<float> gh(static_cast<size_t>(N->R / TILE_M) * 130);
+      MLP_CK(cudaMemcpy(gh.data(), N->GH, sizeof(float) * gh.size(), cudaMemcpyDeviceToHost));
+      float s = 0.0f;
+      for (size_t b = 0; b < gh.size() / 130; ++b) s += gh[b * 130 + 129];
+      *loss = s;
+    }
+    // a gradient evaluation is not an optimizer step
+    MLP_CK(cudaMemcpyAsync(N->step, &t0, sizeof(int), cudaMemcpyHostToDevice, N->stream));
+    MLP_CK(cudaStreamSynchronize(N->stream));
+    return 0;
+  } catch (const std::exception& e) {
+    return fail(OPENMC_E_UNASSIGNED, e.what());
+  }
+}
+
+// Network output for n query rows (host x4 [n][4] -> host y [n]), in
+// chunks of the network's row capacity.  Replaces the staged training rows.
+int openmc_gb300_mlp_predict(void* handle, int64_t n, const float* x4, float* y)
+{
+  using namespace mlp;
+  Net* N = static_cast<Net*>(handle);
+  if (!N || n < 0 || (n > 0 && (!x4 || !y))) return fail(OPENMC_E_INVALID_ARGUMENT, "invalid query");
+  try {
+    drop_graph(*N);
+    for (long long off = 0; off < n; off += N->cap) {
+      const long long c = std::min<long long>(N->cap, n - off);
+      const long long R = (c + TILE_M - 1) / TILE_M * TILE_M;
+      N->n = c;
+      N->R = R;
+      MLP_CK(cudaMemcpyAsync(N->x4, x4 + off * 4, sizeof(float) * 4 * c, cudaMemcpyHostToDevice, N->stream));
+      k_prepare<<<152, 256, 0, N->stream>>>(N->x4, c, R, N->X0, N->X0T, nullptr, nullptr);
+      MLP_CK(cudaGetLastError());
+      enqueue_forward(*N, false, N->y);
+      check_error(*N);
+      MLP_CK(cudaMemcpy(y + off, N->y, sizeof(float) * c, cudaMemcpyDeviceToHost));
+    }
+    N->n = 0;
+    N->R = 0;
+    return 0;
+  } catch (const std::exception& e) {
+    return fail(OPENMC_E_UNASSIGNED, e.what());
+  }
+}
+
+int openmc_gb300_mlp_get_params(void* handle, float* params, int64_t n)
+{
+  using namespace mlp;
+  Net* N = static_cast<Net*>(handle);
+  if (!N || !params || n != N_PARAMS) return fail(OPENMC_E_INVALID_ARGUMENT, "parameter count mismatch");
+  try {
+    MLP_CK(cudaStreamSynchronize(N->stream));
+    MLP_CK(cudaMemcpy(params, N->P, sizeof(float) * N_PARAMS, cudaMemcpyDeviceToHost));
+    return 0;
+  } catch (const std::exception& e) {
+    return fail(OPENMC_E_UNASSIGNED, e.what());
+  }
+}
+
+// Replaces the parameters and resets the optimizer state.
+int openmc_gb300_mlp_set_params(void* handle, const float* params, int64_t n)
+{
+  using namespace mlp;
+  Net* N = static_cast<Net*>(handle);
+  if (!N || !params || n != N_PARAMS) return fail(OPENMC_E_INVALID_ARGUMENT, "parameter count mismatch");
+  try {
+    upload_params(*N, params);
+    return 0;
+  } catch (const std::exception& e) {
+    return fail(OPENMC_E_UNASSIGNED, e.what());
+  }
+}
+
+// Device milliseconds of the last openmc_gb300_mlp_train call.
+int openmc_gb300_mlp_last_ms(void* handle, float* ms)
+{
+  mlp::Net* N = static_cast<mlp::Net*>(handle);
+  if (!N || !ms) return fail(OPENMC_E_INVALID_ARGUMENT, "invalid handle");
+  *ms = N->last_ms;
+  return 0;
+}
+
+}  // extern "C"

@@ -153,6 +153,16 @@ _fn("openmc_gb300_xs_last_times", [C.c_void_p, _p(C.c_float)])
 _fn("openmc_gb300_xs_stream", [C.c_void_p, _p(C.c_void_p)])
 _fn("openmc_gb300_xs_lookup_noalloc", [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_void_p])
+_fn("openmc_gb300_mlp_n_params", [], C.c_int, check=False)
+_fn("openmc_gb300_mlp_create", [C.c_int64, C.c_uint64, _p(C.c_void_p)])
+_fn("openmc_gb300_mlp_free", [C.c_void_p])
+_fn("openmc_gb300_mlp_set_data", [C.c_void_p, C.c_int64, _p(C.c_float), _p(C.c_float), _p(C.c_float)])
+_fn("openmc_gb300_mlp_train", [C.c_void_p, C.c_int, C.c_double, _p(C.c_float)])
+_fn("openmc_gb300_mlp_gradients", [C.c_void_p, _p(C.c_float), _p(C.c_float)])
+_fn("openmc_gb300_mlp_predict", [C.c_void_p, C.c_int64, _p(C.c_float), _p(C.c_float)])
+_fn("openmc_gb300_mlp_get_params", [C.c_void_p, _p(C.c_float), C.c_int64])
+_fn("openmc_gb300_mlp_set_params", [C.c_void_p, _p(C.c_float), C.c_int64])
+_fn("openmc_gb300_mlp_last_ms", [C.c_void_p, _p(C.c_float)])
 
 
 # ------------------------------------------------------------- globals
@@ -488,3 +498,83 @@ class XSTables:
         s = C.c_void_p()
         _dll.openmc_gb300_xs_stream(self.h, C.byref(s))
         return s.value
+
+
+def _f32(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+class ImportanceNetwork:
+    """The learned-weight-window network on the GPU: (x, y, z, log E) -> a
+    regression target (log flux), 4 -> 128 -> 128 -> 128 -> 1 with SiLU,
+    BF16 tensor-core products accumulating in FP32, full-batch Adam."""
+
+    n_params = int(_dll.openmc_gb300_mlp_n_params())
+
+    def __init__(self, max_rows=1 << 16, seed=1):
+        h = C.c_void_p()
+        _dll.openmc_gb300_mlp_create(int(max_rows), int(seed), C.byref(h))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            _dll.openmc_gb300_mlp_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_data(self, x4, target, weight=None):
+        x4 = _f32(x4)
+        n = x4.shape[0]
+        x4 = x4.reshape(n, 4)
+        t = _f32(target, (n,))
+        w = _f32(weight, (n,)) if weight is not None else None
+        self._keep = (x4, t, w)
+        _dll.openmc_gb300_mlp_set_data(self.h, n, x4.ctypes.data_as(_p(C.c_float)),
+                                       t.ctypes.data_as(_p(C.c_float)),
+                                       w.ctypes.data_as(_p(C.c_float)) if w is not None else None)
+
+    def train(self, steps, lr=1e-3):
+        """Runs `steps` Adam steps; returns the loss before each update."""
+        loss = np.zeros(max(int(steps), 1), np.float32)
+        _dll.openmc_gb300_mlp_train(self.h, int(steps), float(lr), loss.ctypes.data_as(_p(C.c_float)))
+        return loss[:int(steps)]
+
+    def gradients(self):
+        """(loss, dLoss/dparams) over the staged rows, without an update."""
+        g = np.zeros(self.n_params, np.float32)
+        loss = C.c_float()
+        _dll.openmc_gb300_mlp_gradients(self.h, g.ctypes.data_as(_p(C.c_float)), C.byref(loss))
+        return float(loss.value), g
+
+    def predict(self, x4):
+        x4 = _f32(x4)
+        n = x4.shape[0]
+        x4 = x4.reshape(n, 4)
+        y = np.zeros(n, np.float32)
+        _dll.openmc_gb300_mlp_predict(self.h, n, x4.ctypes.data_as(_p(C.c_float)),
+                                      y.ctypes.data_as(_p(C.c_float)))
+        return y
+
+    @property
+    def params(self):
+        p = np.zeros(self.n_params, np.float32)
+        _dll.openmc_gb300_mlp_get_params(self.h, p.ctypes.data_as(_p(C.c_float)), self.n_params)
+        return p
+
+    @params.setter
+    def params(self, p):
+        p = _f32(p, (self.n_params,))
+        _dll.openmc_gb300_mlp_set_params(self.h, p.ctypes.data_as(_p(C.c_float)), self.n_params)
+
+    def last_train_ms(self):
+        ms = C.c_float()
+        _dll.openmc_gb300_mlp_last_ms(self.h, C.byref(ms))
+        return float(ms.value)

@@ -473,7 +473,7 @@ class Tally:
 
 
 class Tallies(list):
-    def to_xml(self):
+    def to_xml(self, skip_mesh_ids=()):
         el = ET.Element("tallies")
         meshes, filters = {}, {}
         for t in self:
@@ -482,7 +482,8 @@ class Tallies(list):
                 if isinstance(f, MeshFilter):
                     meshes[f.mesh.id] = f.mesh
         for mid in sorted(meshes):
-            el.append(meshes[mid].to_xml())
+            if mid not in skip_mesh_ids:
+                el.append(meshes[mid].to_xml())
         for fid in sorted(filters):
             el.append(filters[fid].to_xml())
         for t in self:
@@ -584,6 +585,12 @@ class Settings:
         for k, v in kw.items():
             setattr(self, k, v)
 
+    def mesh_ids(self):
+        """Ids of the meshes the weight windows and generators refer to."""
+        wws = self.weight_windows if isinstance(self.weight_windows, (list, tuple)) else [self.weight_windows]
+        ids = {ww.mesh.id for ww in wws if ww is not None}
+        return ids | {g.mesh.id for g in self.weight_window_generators}
+
     def to_xml(self, skip_mesh_ids=()):
         el = ET.Element("settings")
         ET.SubElement(el, "run_mode").text = self.run_mode
@@ -610,14 +617,16 @@ class Settings:
         meshes = {}
         wws = self.weight_windows if isinstance(self.weight_windows, (list, tuple)) else [self.weight_windows]
         for ww in wws:
-            meshes[ww.mesh.id] = ww.mesh
+            if ww is not None:
+                meshes[ww.mesh.id] = ww.mesh
         for g in self.weight_window_generators:
             meshes[g.mesh.id] = g.mesh
         for mid in sorted(meshes):
             if mid not in skip_mesh_ids:
                 el.append(meshes[mid].to_xml())
         for ww in wws:
-            el.append(ww.to_xml())
+            if ww is not None:
+                el.append(ww.to_xml())
         if self.weight_windows_on is not None:
             ET.SubElement(el, "weight_windows_on").text = str(bool(self.weight_windows_on)).lower()
         if self.weight_window_generators:
@@ -638,10 +647,12 @@ class Model:
         root = ET.Element("model")
         root.append(self.materials.to_xml())
         root.append(self.geometry.to_xml())
-        tally_meshes = {f.mesh.id for t in self.tallies for f in t.filters if isinstance(f, MeshFilter)}
-        root.append(self.settings.to_xml(skip_mesh_ids=tally_meshes))
+        # each mesh is written once, in settings when weight windows use it
+        # (settings are read first), else with the tallies
+        # (openmc/model/model.py export_to_model_xml, mesh_memo)
+        root.append(self.settings.to_xml())
         if self.tallies:
-            root.append(self.tallies.to_xml())
+            root.append(self.tallies.to_xml(skip_mesh_ids=self.settings.mesh_ids()))
         return root
 
     def export_to_model_xml(self, path="model.xml"):

@@ -157,6 +157,7 @@ def algorithmic_bytes(detail, levels, fp32):
     q = parts(detail["queue"])
     q["tail"] = sum(parts(detail["tail"]).values())
     q["xs+advance"] = q["xs"] + q["advance"]
+    q["xs+advance+surface"] = q["xs"] + q["advance"] + q["surface"]
     return q
 
 
@@ -170,7 +171,8 @@ def run_gb300(args):
     try:
         lib.settings.xs_fp32 = 1
         lib.settings.particles_in_flight = args.in_flight
-        fused = bool(lib.settings.fuse_xs)
+        fused = int(lib.settings.fuse_xs)
+        sort = int(lib.settings.sort_queue)
         if args.no_graph:
             lib.settings.profile_next = 2
         lib.simulation_init()
@@ -211,14 +213,24 @@ def run_gb300(args):
     kms = prof["kernel_ms"]
     byts = algorithmic_bytes(prof, levels, True)
     kms = dict(kms)
-    if fused:  # cross-section event inside the advance kernel (its own span only times event records)
+    # fused events run inside the advance kernel; their own spans only time event records
+    if fused & 2:
+        kms["xs+advance+surface"] = kms.pop("advance")
+        kms.pop("xs")
+        kms.pop("surface")
+    elif fused & 1:
         kms["xs+advance"] = kms.pop("advance")
         kms.pop("xs")
-    dom = max((k for k in ("xs", "advance", "xs+advance", "surface", "collision", "tail") if k in kms),
+    dom = max((k for k in ("xs", "advance", "xs+advance", "xs+advance+surface", "surface", "collision", "tail")
+               if k in kms),
               key=lambda k: kms[k])
     peak, peak_kind = peaks()
     achieved = byts[dom] / (kms[dom] * 1e-3) / 1e9
-    launches = sum(2 + 11 * int(i) for i in iters)
+    # kernels per event iteration: advance, [xs], [surface], collision, tail,
+    # refill plan, refill, sort (3) or queue copy (1), finish; plus batch init
+    # and accumulate
+    per_iter = 1 + (0 if fused & 1 else 1) + (0 if fused & 2 else 1) + 1 + 1 + 2 + (3 if sort else 1) + 1
+    launches = sum(2 + per_iter * int(i) for i in iters)
     dom_launches = int(prof["iterations"]) if "iterations" in prof else int(iters[-1])
     alg_per_launch = byts[dom] / max(dom_launches, 1)
     ratio = TRAFFIC_PER_ALGORITHMIC_BYTE.get(dom)

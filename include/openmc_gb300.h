@@ -101,7 +101,8 @@ int openmc_weight_windows_get_mesh(int32_t index, int32_t* mesh_idx);
 extern int openmc_gb300_xs_fp32;
 extern int64_t openmc_gb300_in_flight;
 extern int openmc_gb300_sort;
-/* 1: the cross-section event runs inside the advance kernel */
+/* bit 0: the cross-section event runs inside the advance kernel; bit 1 (with
+ * bit 0): so does the surface crossing (default 3; 0: one kernel per event) */
 extern int openmc_gb300_fuse;
 extern int openmc_gb300_trace_batch;
 extern int64_t openmc_gb300_trace_first;
@@ -113,8 +114,11 @@ extern int openmc_gb300_profile_next;
 /* queue length at or below which, once every source particle has started,
  * the remaining histories run to completion one thread each (-1: default) */
 extern int64_t openmc_gb300_tail_threshold;
+/* entries of the device pool of banked secondaries (split particles); 0: automatic
+ * (with weight windows max(32 x slots, 2^22), else 1024); each entry is 72 bytes */
+extern int64_t openmc_gb300_secondary_capacity;
 
-/* last batch: [ms, iterations, events, total_weight, leakage, lost, done, secondaries,
+/* last batch: [ms, iterations, events, total_weight, leakage, lost, done, secondary-pool entries used,
  *  events of the longest history, its particle id] */
 int openmc_gb300_last_batch(double* out);
 /* [queue phase: xs events, xs recomputations, xs nuclide lookups, mesh

@@ -154,31 +154,31 @@ def lattice17(directory, particles=10_000_000, batches=20, n_points=11303,
     return om.Model(geom, mats, settings, om.Tallies([t])), directory
 
 
-def shield_materials(directory, n_points, seed):
+def shield_materials(directory, n_points, seed, density_scale=1.0):
     specs = [("Lt1", 1), ("Lt16", 16), ("Lt10", 10), ("Lt2", 2),
              ("Cl56", 56), ("Cl58", 58), ("Cl54", 54), ("Cl52", 52)]
     _, xs_xml = _library(directory, specs, n_points, seed)
     light = om.Material(name="light scatterer")
     for n, f in zip(["Lt1", "Lt16", "Lt10", "Lt2"], [0.66, 0.32, 0.019, 0.001]):
         light.add_nuclide(n, f)
-    light.set_density("atom/b-cm", 0.1)
+    light.set_density("atom/b-cm", 0.1 * density_scale)
     heavy = om.Material(name="heavy absorber")
     for n, f in zip(["Cl56", "Cl58", "Cl54", "Cl52"], [0.72, 0.18, 0.06, 0.04]):
         heavy.add_nuclide(n, f)
-    heavy.set_density("atom/b-cm", 0.085)
+    heavy.set_density("atom/b-cm", 0.085 * density_scale)
     return light, heavy, xs_xml
 
 
 def shield(directory, particles=1_000_000, batches=10, n_points=11303, seed=4,
            event_based=True, length=200.0, width=50.0, layer=10.0,
            mesh_dim=(200, 10, 10), weight_windows=None, back_face=10.0,
-           energy_groups=None, tally_mesh_windows=False):
+           energy_groups=None, tally_mesh_windows=False, density_scale=1.0):
     """Deep-penetration slab shield.  energy_groups: bounds [eV] of an
     energy filter on the mesh flux tally; tally_mesh_windows: add weight
     windows on the flux tally's mesh and energy groups with every bound at
     -1 (no window until a generator or the caller sets them)."""
     directory = Path(directory)
-    light, heavy, xs_xml = shield_materials(directory, n_points, seed)
+    light, heavy, xs_xml = shield_materials(directory, n_points, seed, density_scale)
     mats = om.Materials([light, heavy], cross_sections=xs_xml.name)
     n_layers = int(round(length / layer))
     xp = [om.XPlane(k * layer) for k in range(n_layers + 1)]
@@ -212,6 +212,12 @@ def shield(directory, particles=1_000_000, batches=10, n_points=11303, seed=4,
     back.upper_right = [length, hw, hw]
     tb = om.Tally(name="back face flux")
     tb.filters = [om.MeshFilter(back)]
+    depth = om.RegularMesh()
+    depth.dimension = [n_layers, 1, 1]
+    depth.lower_left = [0.0, -hw, -hw]
+    depth.upper_right = [length, hw, hw]
+    tp = om.Tally(name="flux per layer")
+    tp.filters = [om.MeshFilter(depth)]
     if tally_mesh_windows:
         n = int(np.prod(mesh_dim)) * (len(ebounds) - 1)
         weight_windows = om.WeightWindows(mesh, -np.ones(n), upper_ww_bounds=-np.ones(n),
@@ -219,4 +225,4 @@ def shield(directory, particles=1_000_000, batches=10, n_points=11303, seed=4,
     if weight_windows is not None:
         settings.weight_windows = [weight_windows]
         settings.weight_windows_on = True
-    return om.Model(geom, mats, settings, om.Tallies([t, tb])), directory
+    return om.Model(geom, mats, settings, om.Tallies([t, tb, tp])), directory

@@ -68,8 +68,9 @@ bool UWUW_ENABLED = false;
 // GB300 extensions (no counterpart in the reference)
 int openmc_gb300_profile_next = 0;      // 1: run the next batch kernel by kernel with event timing,
                                         // 2: every batch (graph-free, for kernel profilers)
-int openmc_gb300_fuse = 1;              // cross-section event inside the advance kernel
+int openmc_gb300_fuse = 3;              // bit 0: cross-section event, bit 1: surface crossing, inside the advance kernel
 int64_t openmc_gb300_tail_threshold = -1;  // queue length that starts the history-based tail (-1: default)
+int64_t openmc_gb300_secondary_capacity = 0;  // secondary-site pool entries (0: automatic)
 int openmc_gb300_xs_fp32 = -1;          // -1: from XML (<gb300_xs_precision>), else 0/1
 int64_t openmc_gb300_in_flight = 0;     // particle slots; 0: setting or automatic
 int openmc_gb300_sort = 1;              // sort the XS queue by (material, energy)
@@ -277,7 +278,7 @@ int check_device_errors(const BatchStats& st)
   HModel& m = S().model;
   n_lost_particles += st.n_lost;
   if (st.error & ERR_SECONDARY_OVERFLOW)
-    return fail(OPENMC_E_ALLOCATE, "The secondary particle pool on the GPU is full; raise openmc_gb300_set_secondary_capacity.");
+    return fail(OPENMC_E_ALLOCATE, "The secondary particle pool on the GPU is full; raise openmc_gb300_secondary_capacity.");
   if (st.error & ERR_NO_NUCLIDE) return fail(OPENMC_E_PHYSICS, "Did not sample any nuclide during collision.");
   if (st.error & ERR_REJECTION)
     return fail(OPENMC_E_INVALID_ARGUMENT, "Too few source sites satisfied the constraints.");
@@ -357,7 +358,8 @@ int openmc_simulation_init()
     opt.xs_fp32 = openmc_gb300_xs_fp32 >= 0 ? openmc_gb300_xs_fp32 != 0 : m.xs_precision == 32;
     opt.sort = openmc_gb300_sort != 0;
     opt.tail_threshold = openmc_gb300_tail_threshold;
-    opt.fuse = openmc_gb300_fuse != 0;
+    opt.secondary_cap = openmc_gb300_secondary_capacity;
+    opt.fuse = openmc_gb300_fuse;
     if (m.ww_on && m.weight_windows.empty()) return fail(OPENMC_E_INVALID_ARGUMENT, "weight windows are on but none are defined");
     s.gpu = gpu_create(m, opt);
     if (s.trace_hist > 0) gpu_set_trace(s.gpu, s.trace_hist, s.trace_cap, openmc_gb300_trace_batch, openmc_gb300_trace_first);

@@ -83,6 +83,7 @@ struct DModel {
   const float* mat_dens32;
   int n_nuc, n_mat, M, xs_fp32;
   double e_min, e_max, log_spacing;
+  float log_emin32, inv_spacing32;  // FP32 log(e_min) and 1 / log_spacing for the hash-bin pre-test
   // source
   int sp_type, an_type, en_type, dom_type, n_en, n_dom;
   double sp[6], uref[3];
@@ -128,7 +129,8 @@ struct DBank {
   double *bdist, *dcoll;
   int *bsurf, *blevel, *btrans;
   int *n_event, *n_collision, *n_split;
-  int* sec_top;
+  int* sec_top;   // top of the slot's LIFO chain of banked secondaries
+  int* sec_free;  // the slot's chain of pool entries already revived (reused first)
   int* n_total;  // events of the whole history (all revived secondaries)
 };
 
@@ -163,7 +165,18 @@ struct DCounters {
   unsigned long long longest;  // (events << 34) | particle id of the longest history
 };
 
+// Source site of one history, sampled for the whole batch up front:
+// position, direction, energy and the history's tracking-stream seed.
+struct SourceSite {
+  double r[3];
+  double u[3];
+  double E;
+  unsigned long long tseed;
+};
+
 struct DQueues {
+  SourceSite* src_bank;  // [n_particles] or null (sites sampled at refill)
+  long long src_n;
   int* q_in;
   int* q_surf;
   int* q_coll;
@@ -756,7 +769,9 @@ struct Micro {
   double f;
 };
 
-__device__ __forceinline__ int nuclide_grid(int nuc, int i_log, double E, double& f)
+// Locates the grid interval of E and returns its index and bracketing
+// energies e0 < e1 (duplicate points skipped as the reference does).
+__device__ __forceinline__ int nuclide_grid(int nuc, int i_log, double E, double& e0_out, double& e1_out)
 {
   const long long off = dm.nuc_off[nuc];
   const int G = static_cast<int>(dm.nuc_off[nuc + 1] - off);
@@ -778,7 +793,8 @@ __device__ __forceinline__ int nuclide_grid(int nuc, int i_log, double E, double
     e0 = e1;
     e1 = __ldg(e + i_grid + 1);
   }
-  f = (E - e0) / (e1 - e0);
+  e0_out = e0;
+  e1_out = e1;
   return i_grid;
 }
 
@@ -793,7 +809,9 @@ __device__ __forceinline__ double4 ldg4(const double4* p)
 __device__ __forceinline__ Micro micro_xs64(int nuc, int i_log, double E)
 {
   Micro m;
-  m.i_grid = nuclide_grid(nuc, i_log, E, m.f);
+  double e0, e1;
+  m.i_grid = nuclide_grid(nuc, i_log, E, e0, e1);
+  m.f = (E - e0) / (e1 - e0);
   const double4* xs = dm.xs64 + dm.nuc_off[nuc];
   double4 a = ldg4(xs + m.i_grid);
   double4 b = ldg4(xs + m.i_grid + 1);
@@ -802,15 +820,17 @@ __device__ __forceinline__ Micro micro_xs64(int nuc, int i_log, double E)
   return m;
 }
 
-// FP32 tables: interpolation in FP32 from an FP64 interpolation factor,
-// written as a + f (b - a), which stays accurate when f leaves [0, 1]
-// (energies below the first or above the last grid point extrapolate);
-// (1 - f) a + f b cancels catastrophically in FP32 there.
+// FP32 tables: the grid search stays FP64 (E against FP64 grid energies);
+// the interpolation factor is formed in FP32 from the two FP64 differences
+// E - e0 and e1 - e0 (each rounded once to FP32), and the interpolation is
+// written a + f (b - a), which stays accurate when f leaves [0, 1] (energies
+// below the first or above the last grid point extrapolate); (1 - f) a + f b
+// cancels catastrophically in FP32 there.
 __device__ __forceinline__ void micro_xs32(int nuc, int i_log, double E, float& t, float& a_out, int& i_grid, float& f32)
 {
-  double f;
-  i_grid = nuclide_grid(nuc, i_log, E, f);
-  f32 = static_cast<float>(f);
+  double e0, e1;
+  i_grid = nuclide_grid(nuc, i_log, E, e0, e1);
+  f32 = static_cast<float>(E - e0) / static_cast<float>(e1 - e0);
   const float4* xs = dm.xs32 + dm.nuc_off[nuc];
   float4 a = __ldg(xs + i_grid);
   float4 b = __ldg(xs + i_grid + 1);
@@ -822,9 +842,20 @@ __device__ __forceinline__ void micro_xs32(int nuc, int i_log, double E, float& 
 // reference reads grid_index[M+1] past the end of the table for E equal to
 // the grid maximum (and a negative bin below the minimum); the clamp keeps
 // the search window inside the table and the located grid index unchanged.
+// The bin is first formed in FP32, (logf(E) - log e_min) / spacing: E
+// rounded to FP32 (6e-8 relative), logf within 1 ulp and the two rounded
+// constants put it within 2e-3 bins of the exact quotient, so when it lies
+// more than 1/64 bin from an integer its floor is the reference's FP64
+// result; otherwise (and for non-finite values) the FP64 expression decides.
+// The returned bin is always the FP64 expression's.
 __device__ __forceinline__ int log_union_index(double E)
 {
-  int i = static_cast<int>(log(E / dm.e_min) / dm.log_spacing);
+  const float q = (logf(static_cast<float>(E)) - dm.log_emin32) * dm.inv_spacing32;
+  const float fl = floorf(q);
+  const float fr = q - fl;
+  int i;
+  if (fr > 0.015625f && fr < 0.984375f && fabsf(q) < 1.0e7f) i = static_cast<int>(fl);
+  else i = static_cast<int>(log(E / dm.e_min) / dm.log_spacing);
   return i < 0 ? 0 : (i > dm.M - 1 ? dm.M - 1 : i);
 }
 

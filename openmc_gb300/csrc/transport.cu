@@ -31,6 +31,7 @@
 // Particle time is not tracked: no time cutoff or time filter is supported,
 // and time does not feed any other quantity of this path.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -263,26 +264,45 @@ __device__ bool get_weight_window(double x, double y, double z, double E, double
   return lower >= 0.0;
 }
 
+// Banks n copies of a site on the slot's LIFO chain (Particle::split,
+// src/particle.cpp:95-112).  Pool entries the slot has already revived are
+// reused first (only this slot's thread touches its chains), so the pool
+// bounds the secondaries banked at one time per slot, not those of a batch;
+// the rest come from the pool's bump pointer.
 __device__ void push_secondaries(long long s, int n, double wgt, const double* r, const double* u, double E, int surf)
 {
   if (n <= 0) return;
-  int base = atomicAdd(&dq.cnt->n_sec, n);
-  if (base + n > dq.cnt->sec_cap) {
-    set_error(ERR_SECONDARY_OVERFLOW);
-    return;
+  int reuse = 0;
+  for (int e = db.sec_free[s]; e >= 0 && reuse < n; e = dq.sec[e].prev) ++reuse;
+  int base = 0;
+  if (n > reuse) {
+    base = atomicAdd(&dq.cnt->n_sec, n - reuse);
+    if (base + (n - reuse) > dq.cnt->sec_cap) {
+      set_error(ERR_SECONDARY_OVERFLOW);
+      return;
+    }
   }
   int top = db.sec_top[s];
+  int fr = db.sec_free[s];
   for (int l = 0; l < n; ++l) {
-    DSecondary& d = dq.sec[base + l];
+    int e;
+    if (fr >= 0) {
+      e = fr;
+      fr = dq.sec[e].prev;
+    } else {
+      e = base++;
+    }
+    DSecondary& d = dq.sec[e];
     d.r[0] = r[0]; d.r[1] = r[1]; d.r[2] = r[2];
     d.u[0] = u[0]; d.u[1] = u[1]; d.u[2] = u[2];
     d.E = E;
     d.wgt = wgt;
     d.surf = surf;
     d.prev = top;
-    top = base + l;
+    top = e;
   }
   db.sec_top[s] = top;
+  db.sec_free[s] = fr;
 }
 
 // src/weight_windows.cpp:56-146 (wgt/seed passed in registers)
@@ -375,13 +395,17 @@ __device__ double sample_energy(unsigned long long& seed)
   return dm.en_x[dm.en_alias[u]];
 }
 
-// src/simulation.cpp:573-649 initialize_history (fixed source) into slot s
-__device__ void initialize_history(long long s, long long index_source)
+// The source site of history index_source of the current batch
+// (src/simulation.cpp:573-616 up to the particle seeds, src/source.cpp:
+// 355-415): position, direction, energy, and the tracking-stream seed.
+__device__ void sample_source_site(long long index_source, SourceSite& site)
 {
   long long id = static_cast<long long>(dq.batch - 1) * dm.n_particles + index_source;
   unsigned long long seed = future_seed(static_cast<unsigned long long>(id) * dm.stride,
     static_cast<unsigned long long>(dm.master_seed + 1));
-  double r[3], u[3], E;
+  double* r = site.r;
+  double* u = site.u;
+  double E;
   // src/source.cpp:355-415
   int tries = 0;
   for (;;) {
@@ -420,6 +444,21 @@ __device__ void initialize_history(long long s, long long index_source)
       break;
     }
   }
+  site.E = E;
+  site.tseed = future_seed(static_cast<unsigned long long>(id) * dm.stride,
+    static_cast<unsigned long long>(dm.master_seed + 0));
+}
+
+// src/simulation.cpp:573-649 initialize_history (fixed source) into slot s.
+// The site comes from the batch's source bank when one was sampled.
+__device__ void initialize_history(long long s, long long index_source)
+{
+  SourceSite site;
+  if (dq.src_n >= index_source) site = dq.src_bank[index_source - 1];
+  else sample_source_site(index_source, site);
+  const double* r = site.r;
+  const double* u = site.u;
+  const double E = site.E;
   // from_source (src/particle.cpp:114-158)
   const long long cap = db.cap;
   db.n_coord[s] = 1;
@@ -446,8 +485,7 @@ __device__ void initialize_history(long long s, long long index_source)
   db.ww_factor[s] = 0.0;
   db.wgt_born[s] = wgt;
   db.sec_top[s] = -1;
-  unsigned long long tseed = future_seed(static_cast<unsigned long long>(id) * dm.stride,
-    static_cast<unsigned long long>(dm.master_seed + 0));
+  unsigned long long tseed = site.tseed;
   db.wgt_ww_born[s] = -1.0;
   apply_weight_windows(s, wgt, tseed, r, u, E, SURFACE_NONE);
   db.wgt[s] = wgt;
@@ -500,16 +538,36 @@ __device__ bool revive_or_free(long long s, double wgt)
   db.ux[s] = site.u[0]; db.uy[s] = site.u[1]; db.uz[s] = site.u[2];
   db.E[s] = site.E;
   db.n_event[s] = 0;
+  // the revived entry joins the slot's free chain
+  dq.sec[top].prev = db.sec_free[s];
+  db.sec_free[s] = top;
   return true;
 }
 
 // ================================================================ kernels
+// Samples every source site of the batch at full occupancy.  Sampling a site
+// is a long dependent chain (two seed skip-aheads, rejection sampling against
+// the domain constraint, energy sampling); done at refill time it ran as
+// small, latency-bound launches every iteration.
+__global__ void __launch_bounds__(256) k_source_bank()
+{
+  const long long n = dq.src_n;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    SourceSite site;
+    sample_source_site(i + 1, site);
+    dq.src_bank[i] = site;
+  }
+}
+
 __global__ void k_batch_init(int batch)
 {
   long long cap = db.cap;
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < cap;
-       i += static_cast<long long>(gridDim.x) * blockDim.x)
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
     dq.free_list[i] = static_cast<int>(i);
+    db.sec_free[i] = -1;
+  }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     DCounters* c = dq.cnt;
     c->n_q = c->n_surf = c->n_coll = c->n_next = 0;
@@ -595,6 +653,22 @@ __device__ void ev_xs(long long s, EvStats& st)
 }
 
 // src/particle.cpp:232-286 event_advance (+ track-length tallies)
+// -log(xi) / Sigma_t (src/particle.cpp:243).  With FP32 tables Sigma_t
+// carries FP32 precision, and the logarithm is taken in FP32 too: of 1 - xi
+// through log1pf for xi > 1/2 (no cancellation near xi = 1), of xi itself
+// down to 2^-20, and in FP64 below (so that small xi keep finite, exact
+// tails); the distance is then FP32-accurate like Sigma_t.  FP64 tables
+// keep the reference's FP64 expression.
+__device__ __forceinline__ double collision_distance(double xi, double mt)
+{
+  if (!dm.xs_fp32) return -log(xi) / mt;
+  float lg;
+  if (xi > 0.5) lg = log1pf(-static_cast<float>(1.0 - xi));
+  else if (xi >= 0x1p-20) lg = logf(static_cast<float>(xi));
+  else lg = static_cast<float>(log(xi));
+  return static_cast<double>(-lg / static_cast<float>(mt));
+}
+
 __device__ int ev_advance(long long s, EvStats& st)
 {
   double wgt = db.wgt[s];
@@ -608,7 +682,7 @@ __device__ int ev_advance(long long s, EvStats& st)
   if (neg_lat) mark_lost(s);
   unsigned long long seed = db.seed[s];
   double mt = db.macro_t[s];
-  double dcoll = (mt == 0.0) ? __longlong_as_double(0x7ff0000000000000LL) : -log(prn(seed)) / mt;
+  double dcoll = (mt == 0.0) ? __longlong_as_double(0x7ff0000000000000LL) : collision_distance(prn(seed), mt);
   double distance = bd;
   if (dcoll < distance) distance = dcoll;
   if (INFTY < distance) distance = INFTY;
@@ -955,8 +1029,12 @@ __global__ void __launch_bounds__(256) k_xs()
 // with_xs: the cross-section event runs in the same thread right before the
 // advance (every calculate_xs event is followed by an advance event,
 // src/event.cpp:95-98), sparing one pass over the queue and the macroscopic
-// XS round trip through HBM.
-template<bool with_xs>
+// XS round trip through HBM.  with_surf: a particle that reaches a boundary
+// crosses it in the same thread (the surface event always follows such an
+// advance, src/event.cpp:119-124); its latency-bound lookups then overlap
+// the FP64 work of the other warps instead of running as a separate pass.
+// Per-history results do not depend on either fusion.
+template<bool with_xs, bool with_surf>
 __global__ void __launch_bounds__(256, OMC_MINB_ADV) k_advance()
 {
   if (dq.cnt->tail) return;
@@ -969,7 +1047,8 @@ __global__ void __launch_bounds__(256, OMC_MINB_ADV) k_advance()
     EvStats st {};
     if (with_xs && valid) ev_xs(s, st);
     int nx = valid ? ev_advance(s, st) : NEXT_DEAD;
-    warp_append(dq.q_surf, &dq.cnt->n_surf, static_cast<int>(s), nx == NEXT_SURF);
+    if (with_surf && nx == NEXT_SURF) nx = ev_surface(s, st);
+    if (!with_surf) warp_append(dq.q_surf, &dq.cnt->n_surf, static_cast<int>(s), nx == NEXT_SURF);
     warp_append(dq.q_coll, &dq.cnt->n_coll, static_cast<int>(s), nx == NEXT_COLL);
     warp_append(dq.q_tmp, &dq.cnt->n_next, static_cast<int>(s), nx == NEXT_XS);
     flush_stats(st, 0);
@@ -1252,7 +1331,7 @@ struct GpuSim {
   cudaGraph_t graph = nullptr;
   int blocks = 1216;
   int sort = 1;
-  int fuse = 1;  // cross-section event fused into the advance kernel
+  int fuse = 3;  // bit 0: cross-section event, bit 1: surface crossing, inside the advance kernel
   long long tail_threshold = 1 << 17;
   int tail_max_events = 1 << 16;
   bool tallies_dirty = true;
@@ -1381,6 +1460,8 @@ static void build_model(GpuSim& G, const HModel& m, const GpuOptions& opt)
   d.e_min = m.energy_min;
   d.e_max = m.energy_max;
   d.log_spacing = m.log_spacing;
+  d.log_emin32 = static_cast<float>(std::log(m.energy_min));
+  d.inv_spacing32 = static_cast<float>(1.0 / m.log_spacing);
 
   // source
   const HSource& src = m.source;
@@ -1545,6 +1626,7 @@ static void build_bank(GpuSim& G, long long cap, long long sec_cap)
   b.n_collision = dev_alloc<int>(cap, own);
   b.n_split = dev_alloc<int>(cap, own);
   b.sec_top = dev_alloc<int>(cap, own);
+  b.sec_free = dev_alloc<int>(cap, own);
   b.n_total = dev_alloc<int>(cap, own);
   DQueues& q = G.queues;
   q.q_in = dev_alloc<int>(cap, own);
@@ -1557,6 +1639,14 @@ static void build_bank(GpuSim& G, long long cap, long long sec_cap)
   q.hist = dev_alloc<int>(q.sort_keys, own);
   q.cursor = dev_alloc<int>(q.sort_keys, own);
   q.sec = dev_alloc<DSecondary>(sec_cap, own);
+  // batch source bank (64 B per history) up to 2^27 histories per batch;
+  // larger batches sample their sites at refill time
+  q.src_bank = nullptr;
+  q.src_n = 0;
+  if (G.model.n_particles > 0 && G.model.n_particles <= (1LL << 27)) {
+    q.src_bank = dev_alloc<SourceSite>(G.model.n_particles, own);
+    q.src_n = G.model.n_particles;
+  }
   G.cnt = dev_alloc<DCounters>(1, own);
   q.cnt = G.cnt;
   q.trace = nullptr;
@@ -1596,6 +1686,7 @@ static void build_graph(GpuSim& G)
   // prologue
   CK(cudaStreamBeginCaptureToGraph(G.stream, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
   k_batch_init<<<nb, nt, 0, G.stream>>>(0);
+  if (G.queues.src_n > 0) k_source_bank<<<nb, nt, 0, G.stream>>>();
   CK(cudaStreamEndCapture(G.stream, &graph));
   size_t n_nodes = 0;
   CK(cudaGraphGetNodes(graph, nullptr, &n_nodes));
@@ -1611,13 +1702,14 @@ static void build_graph(GpuSim& G)
   CK(cudaGraphAddNode(&cond, graph, nodes.data(), nullptr, n_nodes, &cp));
   cudaGraph_t body = cp.conditional.phGraph_out[0];
   CK(cudaStreamBeginCaptureToGraph(G.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-  if (G.fuse) {
-    k_advance<true><<<nb, nt, 0, G.stream>>>();
+  if (G.fuse & 1) {
+    if (G.fuse & 2) k_advance<true, true><<<nb, nt, 0, G.stream>>>();
+    else k_advance<true, false><<<nb, nt, 0, G.stream>>>();
   } else {
     k_xs<<<nb, nt, 0, G.stream>>>();
-    k_advance<false><<<nb, nt, 0, G.stream>>>();
+    k_advance<false, false><<<nb, nt, 0, G.stream>>>();
   }
-  k_surface<<<nb, nt, 0, G.stream>>>();
+  if (!(G.fuse & 2)) k_surface<<<nb, nt, 0, G.stream>>>();
   k_collision<<<nb, nt, 0, G.stream>>>();
   k_tail<<<nb * 2, 128, 0, G.stream>>>(G.tail_max_events);
   k_refill_plan<<<1, 1, 0, G.stream>>>();
@@ -1644,7 +1736,8 @@ GpuSim* gpu_create(const HModel& m, const GpuOptions& opt)
     CK(cudaEventCreate(&G->ev0));
     CK(cudaEventCreate(&G->ev1));
     G->sort = opt.sort ? 1 : 0;
-    G->fuse = opt.fuse ? 1 : 0;
+    G->fuse = opt.fuse & 3;
+    if (G->fuse == 2) G->fuse = 3;  // the surface fusion builds on the cross-section fusion
     if (opt.tail_threshold >= 0) G->tail_threshold = opt.tail_threshold;
     int sms = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
@@ -1654,7 +1747,7 @@ GpuSim* gpu_create(const HModel& m, const GpuOptions& opt)
     if (cap > m.n_particles) cap = m.n_particles;
     if (cap < 1) cap = 1;
     long long sec_cap = opt.secondary_cap;
-    if (sec_cap <= 0) sec_cap = m.ww_on || !m.weight_windows.empty() ? cap * 16 : 1024;
+    if (sec_cap <= 0) sec_cap = m.ww_on || !m.weight_windows.empty() ? std::max(cap * 32, 1LL << 22) : 1024;
     if (sec_cap > (1LL << 31) - 1) sec_cap = (1LL << 31) - 1;
     build_bank(*G, cap, sec_cap);
     upload_constants(*G);
@@ -1775,6 +1868,7 @@ BatchStats gpu_run_batch_profiled(GpuSim* G, HModel& m, int batch, bool accumula
   }
   CK(cudaEventRecord(ev[0], S));
   k_batch_init<<<nb, nt, 0, S>>>(batch);
+  if (G->queues.src_n > 0) k_source_bank<<<nb, nt, 0, S>>>();
   CK(cudaEventRecord(ev[1], S));
   CK(cudaStreamSynchronize(S));
   acc[7] += span(0, 1);
@@ -1782,12 +1876,13 @@ BatchStats gpu_run_batch_profiled(GpuSim* G, HModel& m, int batch, bool accumula
   unsigned long long prev[7] = {0, 0, 0, 0, 0, 0, 0};
   for (int it = 0; it < (1 << 20); ++it) {
     CK(cudaEventRecord(ev[2], S));
-    if (!G->fuse) k_xs<<<nb, nt, 0, S>>>();
+    if (!(G->fuse & 1)) k_xs<<<nb, nt, 0, S>>>();
     CK(cudaEventRecord(ev[3], S));
-    if (G->fuse) k_advance<true><<<nb, nt, 0, S>>>();
-    else k_advance<false><<<nb, nt, 0, S>>>();
+    if (G->fuse == 3) k_advance<true, true><<<nb, nt, 0, S>>>();
+    else if (G->fuse == 1) k_advance<true, false><<<nb, nt, 0, S>>>();
+    else k_advance<false, false><<<nb, nt, 0, S>>>();
     CK(cudaEventRecord(ev[4], S));
-    k_surface<<<nb, nt, 0, S>>>();
+    if (!(G->fuse & 2)) k_surface<<<nb, nt, 0, S>>>();
     CK(cudaEventRecord(ev[5], S));
     k_collision<<<nb, nt, 0, S>>>();
     CK(cudaEventRecord(ev[6], S));

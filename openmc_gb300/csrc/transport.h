@@ -17,7 +17,7 @@ struct GpuOptions {
   bool xs_fp32 = false;         // FP32 cross-section tables and interpolation
   bool sort = true;             // sort the cross-section queue by (material, energy)
   long long tail_threshold = -1;  // queue length for the history-based tail (-1: default)
-  bool fuse = true;             // run the cross-section event inside the advance kernel
+  int fuse = 3;                 // bit 0: cross-section event, bit 1: surface crossing, inside the advance kernel
 };
 
 struct BatchStats {

@@ -28,6 +28,7 @@ namespace xsb {
 struct Tables {
   int n_nuc, G, M, n_mat, fp32;
   double e_min, e_max, log_spacing;
+  float log_emin32, inv_spacing32;
   double* energy;
   double* xs64;
   float* xs32;
@@ -138,7 +139,15 @@ __global__ void __launch_bounds__(256) k_lookup(Tables T, const int* __restrict_
     int k = perm ? __ldg(perm + j) : static_cast<int>(j);
     int m = __ldg(mat + k);
     double E = __ldg(Ein + k);
-    int i_log = static_cast<int>(log(E / T.e_min) / T.log_spacing);
+    // hash bin: FP32 pre-test, FP64 expression within 1/64 bin of a bin
+    // edge (the same exact scheme as the transport kernels)
+    int i_log;
+    {
+      const float q = (logf(static_cast<float>(E)) - T.log_emin32) * T.inv_spacing32;
+      const float fl = floorf(q), fr = q - fl;
+      if (fr > 0.015625f && fr < 0.984375f && fabsf(q) < 1.0e7f) i_log = static_cast<int>(fl);
+      else i_log = static_cast<int>(log(E / T.e_min) / T.log_spacing);
+    }
     i_log = i_log < 0 ? 0 : (i_log > T.M - 1 ? T.M - 1 : i_log);
     double macro[5] = {0, 0, 0, 0, 0};
     float macro32[5] = {0, 0, 0, 0, 0};
@@ -164,12 +173,11 @@ __global__ void __launch_bounds__(256) k_lookup(Tables T, const int* __restrict_
         e0 = e1;
         e1 = __ldg(e + i_grid + 1);
       }
-      double f = (E - e0) / (e1 - e0);
       h = h * 31u + static_cast<uint32_t>(i_grid);
       long long row = (static_cast<long long>(nuc) * T.G + i_grid) * 5;
       if (FP32) {
         const float* x = T.xs32 + row;
-        float f32 = static_cast<float>(f);
+        const float f32 = static_cast<float>(E - e0) / static_cast<float>(e1 - e0);
         float d = __ldg(T.mat_dens32 + q);
 #pragma unroll
         for (int c = 0; c < 5; ++c) {
@@ -177,6 +185,7 @@ __global__ void __launch_bounds__(256) k_lookup(Tables T, const int* __restrict_
           macro32[c] += d * (a + f32 * (b - a));
         }
       } else {
+        const double f = (E - e0) / (e1 - e0);
         const double* x = T.xs64 + row;
         double d = __ldg(T.mat_dens + q);
 #pragma unroll
@@ -267,6 +276,8 @@ int openmc_gb300_xs_tables_create(int n_nuc, int G, const double* energy, const 
       }
     }
     T->log_spacing = std::log(emax / emin) / M;
+    T->log_emin32 = static_cast<float>(std::log(emin));
+    T->inv_spacing32 = static_cast<float>(1.0 / T->log_spacing);
     size_t ne = static_cast<size_t>(n_nuc) * G;
     CK(cudaMalloc(&T->energy, ne * 8));
     CK(cudaMemcpy(T->energy, energy, ne * 8, cudaMemcpyHostToDevice));

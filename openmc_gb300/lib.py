@@ -200,6 +200,7 @@ class _Settings:
     trace_first = _DLLGlobal(C.c_int64, "openmc_gb300_trace_first")
     profile_next = _DLLGlobal(C.c_int, "openmc_gb300_profile_next")
     tail_threshold = _DLLGlobal(C.c_int64, "openmc_gb300_tail_threshold")
+    secondary_capacity = _DLLGlobal(C.c_int64, "openmc_gb300_secondary_capacity")
 
     @property
     def seed(self):

@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=0,
                     help="histories in the CPU baseline sample (default 3,000,000: about 10 s on 16 cores)")
+    ap.add_argument("--no-xs-bench", action="store_true", help="skip the XS-lookup microbenchmark extra")
     ap.add_argument("--no-graph", action="store_true",
                     help="launch every batch kernel by kernel instead of as one CUDA graph "
                          "(for kernel profilers, which cannot see inside conditional graphs)")
@@ -262,6 +263,45 @@ def run_gb300(args):
     return out
 
 
+def xs_lookup_bench(fp32, n=17_000_000, reps=5):
+    """Macroscopic-XS lookup microbenchmark: 68 nuclides x 11,303 points x 5
+    channels, 12 materials, 1.7e7 (material, energy) lookups resident on the
+    device, sorted by (material, energy) before the lookup kernel.  Returns
+    lookups/s of the lookup kernel and of sort + lookup, and the kernel's
+    algorithmic bytes per second: 12 B in + 40 B out per lookup and, per
+    nuclide of the material, two hash-window bounds (8 B), two bracketing
+    grid energies (16 B), two table rows (2 x 5 x 8 B, or x 4 B in FP32),
+    the nuclide index (4 B) and its atom density (8 B, or 4 B)."""
+    import torch
+    from openmc_gb300 import data, lib
+    d = data.make_xsbench()
+    mats, e = data.xsbench_lookups(d, n, seed=11)
+    counts = np.diff(np.asarray(d.mat_off))
+    nuc_per_lookup = float(np.mean(counts[mats]))
+    per_nuc = 8 + 16 + 2 * 5 * (4 if fp32 else 8) + 4 + (4 if fp32 else 8)
+    alg = 52 + nuc_per_lookup * per_nuc
+    t = lib.XSTables(d, fp32=fp32, max_lookups=n)
+    dm = torch.from_numpy(mats).cuda()
+    de = torch.from_numpy(e).cuda()
+    do = torch.empty(n * 5, dtype=torch.float64, device="cuda")
+    k_ms, tot_ms = [], []
+    for r in range(reps + 2):
+        t.lookup_device(n, dm.data_ptr(), de.data_ptr(), do.data_ptr(), None, sort=True)
+        torch.cuda.synchronize()
+        sort_ms, look_ms = t.last_times()
+        if r >= 2:
+            k_ms.append(look_ms)
+            tot_ms.append(sort_ms + look_ms)
+    t.close()
+    km, tm = statistics.median(k_ms), statistics.median(tot_ms)
+    peak, kind = peaks()
+    gbs = alg * n / (km * 1e-3) / 1e9
+    return {"lookups_per_s": n / (km * 1e-3), "with_sort_lookups_per_s": n / (tm * 1e-3),
+            "kernel_ms": km, "nuclides_per_lookup": nuc_per_lookup, "alg_bytes_per_lookup": alg,
+            "GB/s": gbs, "frac_of_hbm_peak": gbs / peak,
+            "note": "tables (37 MB FP64) stay in the 129 MB L2; inputs/outputs stream from HBM"}
+
+
 def cpu_baseline(path, sample, threads=None, mode=1):
     """Oracle transport of `sample` histories of batch 1 on the host cores:
     mode 1 = event-based loop (100,000 particles in flight, the reference's
@@ -314,6 +354,8 @@ def main():
     import torch
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     r = run_gb300(args)
+    if not args.no_xs_bench and rank == 0:
+        r["xs_lookup"] = {"fp64": xs_lookup_bench(False), "fp32": xs_lookup_bench(True)}
     if world > 1:
         import torch.distributed as dist
         t = torch.tensor([r["ms_per_step"]], dtype=torch.float64)
@@ -353,6 +395,7 @@ def main():
         "fp64_xs_particles_per_s": r.get("fp64_value"),
         "events_per_step": r["detail"]["queue"]["xs_events"] + r["detail"]["tail"]["xs_events"],
         "iterations_per_step": r["iterations"],
+        "xs_lookup_microbench": r.get("xs_lookup"),
     }
     print(json.dumps(line))
 

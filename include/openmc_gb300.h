@@ -117,6 +117,12 @@ extern int64_t openmc_gb300_tail_threshold;
 /* entries of the device pool of banked secondaries (split particles); 0: automatic
  * (with weight windows max(32 x slots, 2^22), else 1024); each entry is 72 bytes */
 extern int64_t openmc_gb300_secondary_capacity;
+/* 1: particles split by weight windows wait in a device ring and start in free
+ * slots with their own tracking seeds (a hash of the parent's seed), so that a
+ * split tree is tracked in parallel; 0 (default): the reference's behaviour,
+ * each copy banked on the parent's LIFO stack and continued on the parent's
+ * random stream after it (src/particle.cpp:417-473) */
+extern int openmc_gb300_split_to_slots;
 
 /* last batch: [ms, iterations, events, total_weight, leakage, lost, done, secondary-pool entries used,
  *  events of the longest history, its particle id] */

@@ -139,6 +139,16 @@ struct DSecondary {
   int surf, prev;
 };
 
+// A split particle waiting for a free slot of its own (split-to-slots mode):
+// the parent's state at the split plus an independent tracking seed.
+struct DSplitSite {
+  double r[3], u[3];
+  double E, wgt, wgt_born, wgt_ww_born, ww_factor;
+  unsigned long long seed;
+  long long id;
+  int surf, n_split;
+};
+
 struct TraceRec {
   int32_t kind, cell, material, surface_or_nuclide, grid_hash, n_coord;
   double E, dist, wgt;
@@ -163,6 +173,11 @@ struct DCounters {
   int tail;  // 1 while the loop runs the remaining histories in k_tail
   int tail_threshold;  // queue length at or below which the tail phase starts
   unsigned long long longest;  // (events << 34) | particle id of the longest history
+  // split-to-slots mode: ring of split particles waiting for a slot;
+  // producers append at split_tail, the refill step consumes from split_head
+  unsigned long long split_head, split_tail, refill_split_base;
+  int refill_split;  // of this iteration's refill: how many come from the ring
+  int split_cap;
 };
 
 // Source site of one history, sampled for the whole batch up front:
@@ -185,6 +200,7 @@ struct DQueues {
   int* hist;
   int* cursor;
   DSecondary* sec;
+  DSplitSite* split;  // split-to-slots ring, or null
   DCounters* cnt;
   TraceRec* trace;
   int* trace_n;

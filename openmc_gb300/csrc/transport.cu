@@ -269,6 +269,50 @@ __device__ bool get_weight_window(double x, double y, double z, double E, double
 // reused first (only this slot's thread touches its chains), so the pool
 // bounds the secondaries banked at one time per slot, not those of a batch;
 // the rest come from the pool's bump pointer.
+// Split-to-slots mode: the n copies go to a global ring from which the
+// refill step starts them in free slots, so that the particles of one split
+// tree are tracked in parallel.  Copy k gets its own tracking seed, a
+// splitmix64 hash of the parent's current seed and k (the reference instead
+// continues each banked copy on the parent's stream after the parent dies,
+// src/particle.cpp:417-473, which serialises the whole tree in one slot).
+// Every copy still carries weight / n, so the estimator stays unbiased.
+__device__ __forceinline__ unsigned long long split_seed(unsigned long long seed, int k)
+{
+  unsigned long long z = seed + static_cast<unsigned long long>(k + 1) * 0x9E3779B97F4A7C15ULL;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+__device__ void push_split_sites(long long s, int n, double wgt, const double* r, const double* u, double E,
+  int surf, unsigned long long seed)
+{
+  const unsigned long long cap = static_cast<unsigned long long>(dq.cnt->split_cap);
+  unsigned long long base = atomicAdd(&dq.cnt->split_tail, static_cast<unsigned long long>(n));
+  atomicAdd(&dq.cnt->n_sec, n);
+  // entries from refill_split_base on may still be read by the running
+  // refill (the head only moves in the refill plan, which never runs
+  // concurrently with a producer)
+  if (base + n - dq.cnt->refill_split_base > cap) {
+    set_error(ERR_SECONDARY_OVERFLOW);
+    return;
+  }
+  for (int k = 0; k < n; ++k) {
+    DSplitSite& d = dq.split[(base + k) % cap];
+    d.r[0] = r[0]; d.r[1] = r[1]; d.r[2] = r[2];
+    d.u[0] = u[0]; d.u[1] = u[1]; d.u[2] = u[2];
+    d.E = E;
+    d.wgt = wgt;
+    d.wgt_born = db.wgt_born[s];
+    d.wgt_ww_born = db.wgt_ww_born[s];
+    d.ww_factor = db.ww_factor[s];
+    d.seed = split_seed(seed, k);
+    d.id = db.id[s];
+    d.surf = surf;
+    d.n_split = db.n_split[s];
+  }
+}
+
 __device__ void push_secondaries(long long s, int n, double wgt, const double* r, const double* u, double E, int surf)
 {
   if (n <= 0) return;
@@ -347,7 +391,8 @@ __device__ void apply_weight_windows(long long s, double& wgt, unsigned long lon
     n_split = fmin(n_split, max_split);
     db.n_split[s] = static_cast<int>(n_split_hist + n_split);
     int i_split = static_cast<int>(llround(n_split));
-    push_secondaries(s, i_split - 1, weight / n_split, r, u, E, surface);
+    if (dq.split) push_split_sites(s, i_split - 1, weight / n_split, r, u, E, surface, seed);
+    else push_secondaries(s, i_split - 1, weight / n_split, r, u, E, surface);
     wgt = weight / n_split;
   } else if (weight <= lower) {
     double weight_survive = fmin(weight * dm.ww_max_split, survival);
@@ -495,6 +540,41 @@ __device__ void initialize_history(long long s, long long index_source)
   if (traced(index_source)) dq.trace_n[index_source - dq.trace_first] = 0;
 }
 
+// Starts a split particle in slot s (split-to-slots mode): the slot takes
+// the parent's state at the split (from_source, src/particle.cpp:114-158,
+// with the split copy's weights and window state) and the copy's own seed.
+__device__ void start_split_site(long long s, const DSplitSite& d)
+{
+  const long long cap = db.cap;
+  db.n_coord[s] = 1;
+  for (int l = 0; l < MAXL; ++l) {
+    long long k = l * cap + s;
+    db.cell[k] = C_NONE;
+    db.univ[k] = C_NONE;
+    db.latt[k] = C_NONE;
+    db.lix[k] = 0; db.liy[k] = 0; db.liz[k] = 0;
+  }
+  db.cell_last0[s] = C_NONE;
+  db.cell_born[s] = C_NONE;
+  db.surface[s] = d.surf;
+  db.material[s] = C_NONE;
+  db.material_last[s] = C_NONE;
+  db.n_collision[s] = 0;
+  db.rx[s] = d.r[0]; db.ry[s] = d.r[1]; db.rz[s] = d.r[2];
+  db.ux[s] = d.u[0]; db.uy[s] = d.u[1]; db.uz[s] = d.u[2];
+  db.E[s] = d.E;
+  db.wgt[s] = d.wgt;
+  db.id[s] = d.id;
+  db.n_event[s] = 0;
+  db.n_split[s] = d.n_split;
+  db.ww_factor[s] = d.ww_factor;
+  db.wgt_born[s] = d.wgt_born;
+  db.wgt_ww_born[s] = d.wgt_ww_born;
+  db.sec_top[s] = -1;
+  db.seed[s] = d.seed;
+  db.n_total[s] = 0;
+}
+
 // src/particle.cpp:417-473 event_revive_from_secondary; returns alive.
 // Dead slots without secondaries go back to the free list.
 __device__ bool revive_or_free(long long s, double wgt)
@@ -575,6 +655,10 @@ __global__ void k_batch_init(int batch)
     c->next_source = 1;
     c->n_done = 0;
     c->n_sec = 0;
+    c->split_head = 0;
+    c->split_tail = 0;
+    c->refill_split_base = 0;
+    c->refill_split = 0;
     c->iter = 0;
     c->total_weight = 0.0;
     c->leakage = 0.0;
@@ -1116,16 +1200,27 @@ __global__ void __launch_bounds__(128) k_tail(int max_events)
   }
 }
 
+// Free slots take waiting split particles first (split-to-slots mode), then
+// new source particles.
 __global__ void k_refill_plan()
 {
   DCounters* c = dq.cnt;
+  int ks = 0;
+  c->refill_split_base = c->split_head;
+  if (dq.split && c->split_tail > c->split_head && c->error == 0) {
+    const unsigned long long avail = c->split_tail - c->split_head;
+    ks = avail < static_cast<unsigned long long>(c->n_free) ? static_cast<int>(avail) : c->n_free;
+    c->split_head += static_cast<unsigned long long>(ks);
+  }
+  c->refill_split = ks;
   long long remaining = dm.n_particles - c->next_source + 1;
   if (remaining < 0) remaining = 0;
-  long long k = c->n_free < remaining ? c->n_free : remaining;
-  c->refill_k = static_cast<int>(k);
-  c->refill_free_base = c->n_free - static_cast<int>(k);
+  long long room = c->n_free - ks;
+  long long k = room < remaining ? room : remaining;
+  c->refill_k = ks + static_cast<int>(k);
+  c->refill_free_base = c->n_free - c->refill_k;
   c->refill_src = c->next_source;
-  c->n_free -= static_cast<int>(k);
+  c->n_free -= c->refill_k;
   c->next_source += k;
   c->n_refill += static_cast<unsigned long long>(k);
   c->n_surf = 0;
@@ -1137,12 +1232,18 @@ __global__ void __launch_bounds__(256) k_refill()
   const int k = dq.cnt->refill_k;
   const int fb = dq.cnt->refill_free_base;
   const long long src = dq.cnt->refill_src;
+  const int ks = dq.cnt->refill_split;
+  const unsigned long long sb = dq.cnt->refill_split_base;
+  const unsigned long long scap = static_cast<unsigned long long>(dq.cnt->split_cap);
   const int stride = gridDim.x * blockDim.x;
   for (int base = blockIdx.x * blockDim.x; base < k; base += stride) {
     int j = base + threadIdx.x;
     bool valid = j < k;
     int s = valid ? dq.free_list[fb + j] : 0;
-    if (valid) initialize_history(s, src + j);
+    if (valid) {
+      if (j < ks) start_split_site(s, dq.split[(sb + j) % scap]);
+      else initialize_history(s, src + (j - ks));
+    }
     warp_append(dq.q_tmp, &dq.cnt->n_next, s, valid);
   }
 }
@@ -1251,10 +1352,13 @@ __device__ bool finish_iter_common()
   c->n_q = c->n_next;
   c->n_next = 0;
   c->iter += 1;
-  bool more = c->n_q > 0 || c->next_source <= dm.n_particles;
-  // enter the tail phase once every source particle has started and the
-  // queue is short enough that per-event launches would dominate
-  c->tail = (c->next_source > dm.n_particles && c->n_q > 0 && c->n_q <= c->tail_threshold) ? 1 : 0;
+  const bool split_waiting = c->split_tail > c->split_head;
+  bool more = c->n_q > 0 || c->next_source <= dm.n_particles || split_waiting;
+  // enter the tail phase once every source particle (and split particle)
+  // has started and the queue is short enough that per-event launches would
+  // dominate
+  c->tail = (c->next_source > dm.n_particles && !split_waiting && c->n_q > 0 &&
+             c->n_q <= c->tail_threshold) ? 1 : 0;
   if (c->error != 0) more = false;
   if (c->iter >= c->max_iter) {
     if (more) c->error |= ERR_ITERATIONS;
@@ -1332,6 +1436,7 @@ struct GpuSim {
   int blocks = 1216;
   int sort = 1;
   int fuse = 3;  // bit 0: cross-section event, bit 1: surface crossing, inside the advance kernel
+  int split_slots = 0;  // split particles start in free slots with their own seeds
   long long tail_threshold = 1 << 17;
   int tail_max_events = 1 << 16;
   bool tallies_dirty = true;
@@ -1638,7 +1743,8 @@ static void build_bank(GpuSim& G, long long cap, long long sec_cap)
   if (q.sort_keys > SORT_MAX_KEYS) G.sort = 0;
   q.hist = dev_alloc<int>(q.sort_keys, own);
   q.cursor = dev_alloc<int>(q.sort_keys, own);
-  q.sec = dev_alloc<DSecondary>(sec_cap, own);
+  q.sec = dev_alloc<DSecondary>(G.split_slots ? 1 : sec_cap, own);
+  q.split = G.split_slots ? dev_alloc<DSplitSite>(sec_cap, own) : nullptr;
   // batch source bank (64 B per history) up to 2^27 histories per batch;
   // larger batches sample their sites at refill time
   q.src_bank = nullptr;
@@ -1655,7 +1761,8 @@ static void build_bank(GpuSim& G, long long cap, long long sec_cap)
   q.trace_cap = 0;
   q.batch = 1;
   DCounters c {};
-  c.sec_cap = static_cast<int>(sec_cap);
+  c.sec_cap = G.split_slots ? 1 : static_cast<int>(sec_cap);
+  c.split_cap = G.split_slots ? static_cast<int>(sec_cap) : 0;
   c.max_iter = 1 << 20;
   c.tail_threshold = static_cast<int>(G.tail_threshold);
   CK(cudaMemcpy(G.cnt, &c, sizeof(c), cudaMemcpyHostToDevice));
@@ -1739,6 +1846,7 @@ GpuSim* gpu_create(const HModel& m, const GpuOptions& opt)
     G->fuse = opt.fuse & 3;
     if (G->fuse == 2) G->fuse = 3;  // the surface fusion builds on the cross-section fusion
     if (opt.tail_threshold >= 0) G->tail_threshold = opt.tail_threshold;
+    G->split_slots = (opt.split_slots && (m.ww_on || !m.weight_windows.empty())) ? 1 : 0;
     int sms = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
     G->blocks = sms * 8;

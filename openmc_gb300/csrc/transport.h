@@ -18,6 +18,7 @@ struct GpuOptions {
   bool sort = true;             // sort the cross-section queue by (material, energy)
   long long tail_threshold = -1;  // queue length for the history-based tail (-1: default)
   int fuse = 3;                 // bit 0: cross-section event, bit 1: surface crossing, inside the advance kernel
+  int split_slots = 0;          // split particles start in free slots with their own seeds
 };
 
 struct BatchStats {

@@ -201,6 +201,7 @@ class _Settings:
     profile_next = _DLLGlobal(C.c_int, "openmc_gb300_profile_next")
     tail_threshold = _DLLGlobal(C.c_int64, "openmc_gb300_tail_threshold")
     secondary_capacity = _DLLGlobal(C.c_int64, "openmc_gb300_secondary_capacity")
+    split_to_slots = _DLLGlobal(C.c_int, "openmc_gb300_split_to_slots")
 
     @property
     def seed(self):

@@ -12,6 +12,8 @@ learned windows from ``learned_ww.fit`` on the same tally (2,000 Adam
 steps).  Each method then runs the same number of batches; its figure of
 merit is 1 / (R^2 T) with R the back-face tally's relative error and T the
 device time of the measured batches (docs variance_reduction.rst:132-134).
+Split particles run in free slots of their own (split-to-slots mode) unless
+--serial-splits keeps the reference's per-history stack.
 
 ``python -m openmc_gb300.shield_study`` prints one JSON object.
 """
@@ -91,14 +93,17 @@ def _summary(r):
 
 def run(directory, length=200.0, mesh_dim=(200, 10, 10), n_points=11303, pilot_particles=1_000_000,
         pilot_batches=5, particles=1_000_000, batches=10, steps=2000, lr=2e-3, ratio=5.0, fp32=True,
-        methods=("plain", "magic", "learned"), density_scale=DENSITY_SCALE, verbose=False):
+        methods=("plain", "magic", "learned"), density_scale=DENSITY_SCALE, verbose=False,
+        split_to_slots=True):
     path, geom = build(directory, length, mesh_dim, n_points, density_scale=density_scale)
     out = {"workload": f"shield {length:g} cm, mesh {mesh_dim}, {geom.n_groups} energy groups, "
                        f"densities x {density_scale:g}",
+           "split_to_slots": bool(split_to_slots),
            "pilot": f"{pilot_batches} x {pilot_particles}", "measure": f"{batches} x {particles}"}
     lib.init(directory=path)
     try:
         lib.settings.xs_fp32 = 1 if fp32 else 0
+        lib.settings.split_to_slots = 1 if split_to_slots else 0
         ww = lib.WeightWindows(0)
         off = -np.ones(geom.n_mesh * geom.n_groups)
         pilot = _run(pilot_particles, pilot_batches, windows_on=False, log="pilot" if verbose else None)
@@ -153,11 +158,13 @@ def main():
     ap.add_argument("--density-scale", type=float, default=DENSITY_SCALE)
     ap.add_argument("--methods", default="plain,magic,learned")
     ap.add_argument("-v", "--verbose", action="store_true")
+    ap.add_argument("--serial-splits", action="store_true",
+                    help="bank split particles on the parent's stack (the reference's order)")
     a = ap.parse_args()
     out = run(Path(a.dir), length=a.length, mesh_dim=(int(a.length), 10, 10),
               pilot_particles=a.pilot_particles, pilot_batches=a.pilot_batches, particles=a.particles,
               batches=a.batches, steps=a.steps, fp32=not a.fp64, density_scale=a.density_scale,
-              methods=tuple(a.methods.split(",")), verbose=a.verbose)
+              methods=tuple(a.methods.split(",")), verbose=a.verbose, split_to_slots=not a.serial_splits)
     print(json.dumps(out))
 
 

@@ -123,6 +123,10 @@ extern int64_t openmc_gb300_secondary_capacity;
  * each copy banked on the parent's LIFO stack and continued on the parent's
  * random stream after it (src/particle.cpp:417-473) */
 extern int openmc_gb300_split_to_slots;
+/* coordinate depth the transport kernels are built for: 0 (default) picks the
+ * 2-level build for models nested at most 2 deep (per-level state in
+ * registers) and the 4-level build otherwise; 4 forces the 4-level build */
+extern int openmc_gb300_max_levels;
 
 /* last batch: [ms, iterations, events, total_weight, leakage, lost, done, secondary-pool entries used,
  *  events of the longest history, its particle id] */

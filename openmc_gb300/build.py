@@ -19,7 +19,10 @@ OUT = PKG / "_lib"
 LIB = OUT / "libopenmc_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-fmad=false"]
-SOURCES = ["host_model.cpp", "capi.cpp", "transport.cu", "xsbench.cu", "mlp.cu"]
+SOURCES = ["host_model.cpp", "capi.cpp", "transport_dispatch.cpp", "xsbench.cu", "mlp.cu"]
+# transport.cu is built once per maximum coordinate depth (namespaces l2, l4)
+VARIANTS = [("transport.cu", "transport_l2", ["-DOMC_MAXL=2", "-DOMC_NS=l2"]),
+            ("transport.cu", "transport_l4", ["-DOMC_MAXL=4", "-DOMC_NS=l4"])]
 
 
 def nvcc():
@@ -38,15 +41,18 @@ def _compile(src: Path, obj: Path, extra):
 
 
 def build(force: bool = False, verbose: bool = False, extra=()) -> Path:
-    srcs = [CSRC / s for s in SOURCES if (CSRC / s).exists()]
+    units = [(CSRC / s, Path(s).stem, []) for s in SOURCES if (CSRC / s).exists()]
+    units += [(CSRC / s, stem, flags) for s, stem, flags in VARIANTS]
+    srcs = [u[0] for u in units]
     headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh"))
     newest = max(p.stat().st_mtime for p in srcs + headers)
     if LIB.exists() and not force and LIB.stat().st_mtime >= newest:
         return LIB
     OUT.mkdir(parents=True, exist_ok=True)
-    objs = [OUT / (s.stem + ".o") for s in srcs]
-    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
-        futs = [ex.submit(_compile, s, o, list(extra)) for s, o in zip(srcs, objs)]
+    objs = [OUT / (stem + ".o") for _, stem, _ in units]
+    with cf.ThreadPoolExecutor(max_workers=min(8, len(units))) as ex:
+        futs = [ex.submit(_compile, src, o, list(flags) + list(extra))
+                for (src, _, flags), o in zip(units, objs)]
         for f in futs:
             msg = f.result()
             if verbose and msg:

@@ -10,9 +10,18 @@
 
 #include "transport.h"
 
+// Each build of the transport kernels for a maximum coordinate depth lives
+// in its own namespace (omc::l2, omc::l4) so that both link into one library.
+#ifndef OMC_NS
+#define OMC_NS l4
+#endif
 namespace omc {
+namespace OMC_NS {
 
-constexpr int MAXL = 4;  // coordinate levels held per particle
+#ifndef OMC_MAXL
+#define OMC_MAXL 4
+#endif
+constexpr int MAXL = OMC_MAXL;  // coordinate levels held per particle
 constexpr double INFTY = 1.7976931348623157e308;  // numeric_limits<double>::max()
 constexpr double PI = 3.141592653589793238462643383279502884;
 constexpr double TINY_BIT = 1e-8;
@@ -506,19 +515,21 @@ __device__ inline void region_distance(const DCell& c, double x, double y, doubl
 
 // ------------------------------------------------------------- lattices
 // src/lattice.cpp:252-306
+// inv_u: 1/u per axis (FP32-table mode: the quotients become products,
+// still FP64 but rounded twice), or null for the reference's divisions.
 __device__ inline double lattice_distance(const DLattice& lat, double x, double y, double z, double ux,
-  double uy, double uz, int& trans)
+  double uy, double uz, int& trans, const double* inv_u = nullptr)
 {
   double x0 = copysign(0.5 * lat.pitch[0], ux);
   double y0 = copysign(0.5 * lat.pitch[1], uy);
   double d = INFTY;
   trans = 13;  // encoded (tx+1) + 3(ty+1) + 9(tz+1); 13 == no translation
   if ((fabs(x - x0) > FP_PRECISION) && ux != 0) {
-    d = (x0 - x) / ux;
+    d = inv_u ? (x0 - x) * inv_u[0] : (x0 - x) / ux;
     trans = (ux > 0) ? 14 : 12;
   }
   if ((fabs(y - y0) > FP_PRECISION) && uy != 0) {
-    double this_d = (y0 - y) / uy;
+    double this_d = inv_u ? (y0 - y) * inv_u[1] : (y0 - y) / uy;
     if (this_d < d) {
       d = this_d;
       trans = (uy > 0) ? 16 : 10;
@@ -527,7 +538,7 @@ __device__ inline double lattice_distance(const DLattice& lat, double x, double 
   if (lat.is3d) {
     double z0 = copysign(0.5 * lat.pitch[2], uz);
     if ((fabs(z - z0) > FP_PRECISION) && uz != 0) {
-      double this_d = (z0 - z) / uz;
+      double this_d = inv_u ? (z0 - z) * inv_u[2] : (z0 - z) / uz;
       if (this_d < d) {
         d = this_d;
         trans = (uz > 0) ? 22 : 4;
@@ -582,6 +593,20 @@ struct Geo {
   int material, material_last;
 };
 
+// Per-level arrays of a Geo are only ever indexed by compile-time levels
+// (loops over levels are unrolled up to MAXL with a run-time guard, and a
+// level known only at run time is read through lvl_get), so that the
+// compiler can keep them in registers instead of thread-local memory.
+template<class T>
+__device__ __forceinline__ T lvl_get(const T (&a)[MAXL], int l)
+{
+  T v = a[0];
+#pragma unroll
+  for (int k = 1; k < MAXL; ++k)
+    if (l == k) v = a[k];
+  return v;
+}
+
 __device__ inline void geo_load(Geo& g, long long s)
 {
   const long long cap = db.cap;
@@ -589,6 +614,7 @@ __device__ inline void geo_load(Geo& g, long long s)
   g.u[0] = db.ux[s];
   g.u[1] = db.uy[s];
   g.u[2] = db.uz[s];
+#pragma unroll
   for (int l = 0; l < MAXL; ++l) {
     if (l >= g.n_coord) break;
     long long k = l * cap + s;
@@ -614,6 +640,7 @@ __device__ inline void geo_store(const Geo& g, long long s)
   db.ux[s] = g.u[0];
   db.uy[s] = g.u[1];
   db.uz[s] = g.u[2];
+#pragma unroll
   for (int l = 0; l < MAXL; ++l) {
     if (l >= g.n_coord) break;
     long long k = l * cap + s;
@@ -640,10 +667,10 @@ __device__ __forceinline__ void coord_reset(Geo& g, int l)
   g.li[l][0] = g.li[l][1] = g.li[l][2] = 0;
 }
 
-// src/universe.cpp:40-59
-__device__ inline bool universe_find_cell(Geo& g)
+// src/universe.cpp:40-59 at coordinate level lvl (a compile-time level
+// wherever this is inlined)
+__device__ __forceinline__ bool universe_find_cell(Geo& g, const int lvl)
 {
-  int lvl = g.n_coord - 1;
   int u = g.univ[lvl];
   int a = dm.univ_off[u], b = dm.univ_off[u + 1];
   for (int k = a; k < b; ++k) {
@@ -662,17 +689,20 @@ __device__ inline bool universe_find_cell(Geo& g)
 // ordering optimisation with the same result for non-overlapping cells)
 __device__ inline bool find_cell_inner(Geo& g, bool& lost_outer)
 {
-  for (;; ++g.n_coord) {
-    if (!universe_find_cell(g)) return false;
-    int lvl = g.n_coord - 1;
+  const int start = g.n_coord - 1;
+#pragma unroll
+  for (int lvl = 0; lvl < MAXL; ++lvl) {
+    if (lvl < start) continue;
+    g.n_coord = lvl + 1;
+    if (!universe_find_cell(g, lvl)) return false;
     const DCell& c = dm.cell[g.cell[lvl]];
     if (c.fill_type == 0) {
       g.material_last = g.material;
       g.material = c.fill;
       return true;
     }
-    if (g.n_coord >= dm.n_coord_levels) return false;
-    int nl = lvl + 1;
+    if (g.n_coord >= dm.n_coord_levels || lvl + 1 >= MAXL) return false;
+    const int nl = lvl + 1 < MAXL ? lvl + 1 : lvl;  // == lvl + 1 on every path that reaches it
     g.r[nl][0] = g.r[lvl][0] - c.tr[0];
     g.r[nl][1] = g.r[lvl][1] - c.tr[1];
     g.r[nl][2] = g.r[lvl][2] - c.tr[2];
@@ -695,12 +725,13 @@ __device__ inline bool find_cell_inner(Geo& g, bool& lost_outer)
     }
     g.cell[nl] = C_NONE;
   }
+  return false;
 }
 
 // src/geometry.cpp:284-298
 __device__ inline bool exhaustive_find_cell(Geo& g, bool& lost_outer)
 {
-  if (g.univ[g.n_coord - 1] == C_NONE) {
+  if (lvl_get(g.univ, g.n_coord - 1) == C_NONE) {
     g.univ[0] = dm.root_univ;
     g.n_coord = 1;
   }
@@ -715,13 +746,15 @@ __device__ inline bool exhaustive_find_cell(Geo& g, bool& lost_outer)
 // surface was skipped enters the level loop as INFINITY.  The returned
 // boundary is the reference's.
 __device__ inline void distance_to_boundary(const Geo& g, double& dist, int& surface, int& level,
-  int& trans, bool& neg_lat)
+  int& trans, bool& neg_lat, const double* inv_u = nullptr)
 {
   const double INF = __longlong_as_double(0x7ff0000000000000LL);  // INFINITY
   double ds[MAXL], dl[MAXL];
   int ss[MAXL], tt[MAXL];
   double bound = INF;
-  for (int i = g.n_coord - 1; i >= 0; --i) {
+#pragma unroll
+  for (int i = MAXL - 1; i >= 0; --i) {
+    if (i >= g.n_coord) continue;
     const DCell& c = dm.cell[g.cell[i]];
     const double* r = g.r[i];
     double b = (i == 0 && g.n_coord > 1) ? bound : INFTY;
@@ -730,7 +763,7 @@ __device__ inline void distance_to_boundary(const Geo& g, double& dist, int& sur
     dl[i] = INF;
     tt[i] = 13;
     if (g.lat[i] != C_NONE) {
-      dl[i] = lattice_distance(dm.lat[g.lat[i]], r[0], r[1], r[2], g.u[0], g.u[1], g.u[2], tt[i]);
+      dl[i] = lattice_distance(dm.lat[g.lat[i]], r[0], r[1], r[2], g.u[0], g.u[1], g.u[2], tt[i], inv_u);
       if (dl[i] < 0) neg_lat = true;
     }
     if (i == 1) {
@@ -744,7 +777,9 @@ __device__ inline void distance_to_boundary(const Geo& g, double& dist, int& sur
   surface = SURFACE_NONE;
   level = 0;
   trans = 13;
-  for (int i = 0; i < g.n_coord; i++) {
+#pragma unroll
+  for (int i = 0; i < MAXL; i++) {
+    if (i >= g.n_coord) break;
     const DCell& c = dm.cell[g.cell[i]];
     const double* r = g.r[i];
     double d_surf = ds[i];
@@ -912,4 +947,5 @@ __device__ inline uint32_t material_xs(int mat, double E, double& tot, double& a
   return h;
 }
 
+}  // namespace OMC_NS
 }  // namespace omc

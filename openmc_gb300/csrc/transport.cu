@@ -44,6 +44,7 @@
 #include "transport.h"
 
 namespace omc {
+namespace OMC_NS {
 
 // --------------------------------------------------------------- helpers
 __device__ __forceinline__ void warp_append(int* q, int* counter, int val, bool pred)
@@ -105,9 +106,11 @@ __device__ __forceinline__ int mesh_index_in_direction(const DMesh& m, double r,
 
 __device__ __forceinline__ void mesh_get_indices(const DMesh& m, double x, double y, double z, int* ijk, bool& in_mesh)
 {
-  double r[3] = {x, y, z};
+  const double r[3] = {x, y, z};
   in_mesh = true;
-  for (int i = 0; i < m.ndim; ++i) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    if (i >= m.ndim) break;
     ijk[i] = mesh_index_in_direction(m, r[i], i);
     if (ijk[i] < 1 || ijk[i] > m.shape[i]) in_mesh = false;
   }
@@ -128,7 +131,10 @@ struct MeshDist {
   double distance;
 };
 
-__device__ __forceinline__ MeshDist mesh_dist(const DMesh& m, const int* ijk, int i, const double* r0, const double* u)
+// inv_u: 1/u per axis in FP32-table mode (products instead of quotients),
+// or null for the reference's divisions.
+__device__ __forceinline__ MeshDist mesh_dist(const DMesh& m, const int* ijk, int i, const double* r0, const double* u,
+  const double* inv_u)
 {
   MeshDist d;
   d.next_index = ijk[i];
@@ -138,21 +144,32 @@ __device__ __forceinline__ MeshDist mesh_dist(const DMesh& m, const int* ijk, in
   d.max_surface = (u[i] > 0);
   if (d.max_surface && (ijk[i] <= m.shape[i])) {
     d.next_index++;
-    d.distance = ((m.ll[i] + ijk[i] * m.width[i]) - r0[i]) / u[i];
+    const double f = (m.ll[i] + ijk[i] * m.width[i]) - r0[i];
+    d.distance = inv_u ? f * inv_u[i] : f / u[i];
   } else if (!d.max_surface && (ijk[i] >= 1)) {
     d.next_index--;
-    d.distance = ((m.ll[i] + (ijk[i] - 1) * m.width[i]) - r0[i]) / u[i];
+    const double f = (m.ll[i] + (ijk[i] - 1) * m.width[i]) - r0[i];
+    d.distance = inv_u ? f * inv_u[i] : f / u[i];
   }
   return d;
 }
 
 // src/mesh.cpp:999-1146 raytrace_mesh/bins_crossed; calls f(bin, fraction)
 template<class F>
-__device__ void mesh_bins_crossed(const DMesh& m, const double* r0, const double* r1, const double* u, F f)
+// inv_u (FP32-table mode): reciprocal direction; the track length is then
+// taken as the advance distance itself and fractions use its reciprocal.
+__device__ void mesh_bins_crossed(const DMesh& m, const double* r0, const double* r1, const double* u, F f,
+  const double* inv_u = nullptr, double track = 0.0)
 {
-  double dx = r1[0] - r0[0], dy = r1[1] - r0[1], dz = r1[2] - r0[2];
-  double total_distance = sqrt(dx * dx + dy * dy + dz * dz);
+  double total_distance;
+  if (inv_u) {
+    total_distance = track;
+  } else {
+    double dx = r1[0] - r0[0], dy = r1[1] - r0[1], dz = r1[2] - r0[2];
+    total_distance = sqrt(dx * dx + dy * dy + dz * dz);
+  }
   if (total_distance == 0.0) return;
+  const double inv_total = inv_u ? 1.0 / total_distance : 0.0;
   const int n = m.ndim;
   bool in_mesh;
   double traveled = 0.0;
@@ -162,23 +179,37 @@ __device__ void mesh_bins_crossed(const DMesh& m, const double* r0, const double
     if (in_mesh) f(mesh_bin(m, ijk), 1.0);
     return;
   }
+  // the per-axis arrays are indexed by unrolled compile-time axes only, so
+  // that they stay in registers
   MeshDist dist[3];
   dist[0].distance = dist[1].distance = dist[2].distance = INFTY;
-  for (int k = 0; k < n; ++k) dist[k] = mesh_dist(m, ijk, k, r0, u);
+  dist[0].next_index = dist[1].next_index = dist[2].next_index = 0;
+  dist[0].max_surface = dist[1].max_surface = dist[2].max_surface = true;
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    if (k < n) dist[k] = mesh_dist(m, ijk, k, r0, u, inv_u);
   for (int guard = 0; guard < 1 << 24; ++guard) {
     if (in_mesh) {
       int k = 0;
-      if (dist[1].distance < dist[k].distance) k = 1;
-      if (dist[2].distance < dist[k].distance) k = 2;
-      f(mesh_bin(m, ijk), (fmin(dist[k].distance, total_distance) - traveled) / total_distance);
-      traveled = dist[k].distance;
+      double dk = dist[0].distance;
+      if (dist[1].distance < dk) { k = 1; dk = dist[1].distance; }
+      if (dist[2].distance < dk) { k = 2; dk = dist[2].distance; }
+      const double seg = fmin(dk, total_distance) - traveled;
+      f(mesh_bin(m, ijk), inv_u ? seg * inv_total : seg / total_distance);
+      traveled = dk;
       if (traveled >= total_distance) return;
-      ijk[k] = dist[k].next_index;
-      dist[k] = mesh_dist(m, ijk, k, r0, u);
-      in_mesh = ((ijk[k] >= 1) && (ijk[k] <= m.shape[k]));
+#pragma unroll
+      for (int kk = 0; kk < 3; ++kk) {
+        if (kk != k) continue;
+        ijk[kk] = dist[kk].next_index;
+        dist[kk] = mesh_dist(m, ijk, kk, r0, u, inv_u);
+        in_mesh = ((ijk[kk] >= 1) && (ijk[kk] <= m.shape[kk]));
+      }
     } else {
       int k_max = -1;
-      for (int k = 0; k < n; ++k) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        if (k >= n) break;
         if ((ijk[k] < 1 || ijk[k] > m.shape[k]) && (dist[k].distance > traveled)) {
           traveled = dist[k].distance;
           k_max = k;
@@ -188,7 +219,9 @@ __device__ void mesh_bins_crossed(const DMesh& m, const double* r0, const double
       if (traveled >= total_distance) return;
       double t = traveled + TINY_BIT;
       mesh_get_indices(m, r0[0] + t * u[0], r0[1] + t * u[1], r0[2] + t * u[2], ijk, in_mesh);
-      for (int k = 0; k < n; ++k) dist[k] = mesh_dist(m, ijk, k, r0, u);
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        if (k < n) dist[k] = mesh_dist(m, ijk, k, r0, u, inv_u);
     }
   }
 }
@@ -196,7 +229,7 @@ __device__ void mesh_bins_crossed(const DMesh& m, const double* r0, const double
 // src/tallies/tally_scoring.cpp:2416-2541 + FilterBinIter :31-139 +
 // score_general_ce_nonanalog :578-1106 (flux, total, absorption)
 __device__ int score_tracklength(const double* r0, const double* r1, const double* u, double E_last,
-  double wgt, double distance, double mt, double ma)
+  double wgt, double distance, double mt, double ma, const double* inv_u = nullptr)
 {
   double flux = wgt * distance;
   int n_seg = 0;
@@ -240,7 +273,7 @@ __device__ int score_tracklength(const double* r0, const double* r1, const doubl
       mesh_bins_crossed(M, r0, r1, u, [&](int bin, double frac) {
         add(base + bin * stride, 1. * frac);
         ++n_seg;
-      });
+      }, inv_u, distance);
     }
   }
   return n_seg;
@@ -422,7 +455,9 @@ __device__ bool satisfies_spatial_constraints(double x, double y, double z)
     for (int k = 0; k < dm.n_dom; ++k) if (dm.dom_ids[k] == id) return true;
     return false;
   }
-  for (int i = 0; i < g.n_coord; ++i) {
+#pragma unroll
+  for (int i = 0; i < MAXL; ++i) {
+    if (i >= g.n_coord) break;
     int id = dm.dom_type == 0 ? dm.cell_id[g.cell[i]] : g.univ[i];
     for (int k = 0; k < dm.n_dom; ++k) if (dm.dom_ids[k] == id) return true;
   }
@@ -702,12 +737,12 @@ __device__ void ev_xs(long long s, EvStats& st)
       mark_lost(s);
       return;
     }
-    if (db.cell_born[s] == C_NONE) db.cell_born[s] = g.cell[g.n_coord - 1];
+    if (db.cell_born[s] == C_NONE) db.cell_born[s] = lvl_get(g.cell, g.n_coord - 1);
     db.cell_last0[s] = g.cell[0];
     geo_store(g, s);
     material = g.material;
     material_last = g.material_last;
-    low_cell = g.cell[g.n_coord - 1];
+    low_cell = lvl_get(g.cell, g.n_coord - 1);
   }
   uint32_t h = 0xffffffffu;
   double E = db.E[s];
@@ -762,7 +797,16 @@ __device__ int ev_advance(long long s, EvStats& st)
   double bd;
   int bs, bl, bt;
   bool neg_lat = false;
-  distance_to_boundary(g, bd, bs, bl, bt, neg_lat);
+  // FP32-table mode: reciprocal direction shared by the lattice and mesh
+  // distances (FP64 products in place of FP64 quotients)
+  double inv_u[3];
+  const bool recip = dm.xs_fp32 != 0;
+  if (recip) {
+    inv_u[0] = 1.0 / g.u[0];
+    inv_u[1] = 1.0 / g.u[1];
+    inv_u[2] = 1.0 / g.u[2];
+  }
+  distance_to_boundary(g, bd, bs, bl, bt, neg_lat, recip ? inv_u : nullptr);
   if (neg_lat) mark_lost(s);
   unsigned long long seed = db.seed[s];
   double mt = db.macro_t[s];
@@ -771,19 +815,24 @@ __device__ int ev_advance(long long s, EvStats& st)
   if (dcoll < distance) distance = dcoll;
   if (INFTY < distance) distance = INFTY;
   double r0[3] = {g.r[0][0], g.r[0][1], g.r[0][2]};
-  for (int l = 0; l < g.n_coord; ++l) {
+#pragma unroll
+  for (int l = 0; l < MAXL; ++l) {
+    if (l >= g.n_coord) break;
     g.r[l][0] = g.r[l][0] + distance * g.u[0];
     g.r[l][1] = g.r[l][1] + distance * g.u[1];
     g.r[l][2] = g.r[l][2] + distance * g.u[2];
   }
-  if (dm.n_tally > 0) st.seg += score_tracklength(r0, g.r[0], g.u, db.E[s], wgt, distance, mt, db.macro_a[s]);
+  if (dm.n_tally > 0)
+    st.seg += score_tracklength(r0, g.r[0], g.u, db.E[s], wgt, distance, mt, db.macro_a[s], recip ? inv_u : nullptr);
   wgt = db.wgt[s];
   if (distance == INFTY) {
     wgt = 0.0;
     db.wgt[s] = 0.0;
   }
   const long long cap = db.cap;
-  for (int l = 0; l < g.n_coord; ++l) {
+#pragma unroll
+  for (int l = 0; l < MAXL; ++l) {
+    if (l >= g.n_coord) break;
     long long k = l * cap + s;
     db.rx[k] = g.r[l][0];
     db.ry[k] = g.r[l][1];
@@ -807,28 +856,34 @@ __device__ int ev_advance(long long s, EvStats& st)
 // src/geometry.cpp:301-357
 __device__ void cross_lattice(Geo& g, long long s, int trans)
 {
-  int lvl = g.n_coord - 1;
-  const DLattice& lat = dm.lat[g.lat[lvl]];
-  g.li[lvl][0] += trans % 3 - 1;
-  g.li[lvl][1] += (trans / 3) % 3 - 1;
-  g.li[lvl][2] += trans / 9 - 1;
-  const int up = lvl - 1;
-  const DCell& cell = dm.cell[g.cell[up]];
-  g.r[lvl][0] = g.r[up][0] - cell.tr[0];
-  g.r[lvl][1] = g.r[up][1] - cell.tr[1];
-  g.r[lvl][2] = g.r[up][2] - cell.tr[2];
-  lattice_local_position(lat, g.r[lvl][0], g.r[lvl][1], g.r[lvl][2], g.li[lvl]);
+  const int lvl_rt = g.n_coord - 1;  // a lattice level is never the root
+  bool valid = false;
+#pragma unroll
+  for (int lvl = 1; lvl < MAXL; ++lvl) {
+    if (lvl != lvl_rt) continue;
+    const DLattice& lat = dm.lat[g.lat[lvl]];
+    g.li[lvl][0] += trans % 3 - 1;
+    g.li[lvl][1] += (trans / 3) % 3 - 1;
+    g.li[lvl][2] += trans / 9 - 1;
+    const int up = lvl - 1;
+    const DCell& cell = dm.cell[g.cell[up]];
+    g.r[lvl][0] = g.r[up][0] - cell.tr[0];
+    g.r[lvl][1] = g.r[up][1] - cell.tr[1];
+    g.r[lvl][2] = g.r[up][2] - cell.tr[2];
+    lattice_local_position(lat, g.r[lvl][0], g.r[lvl][1], g.r[lvl][2], g.li[lvl]);
+    valid = lattice_valid(lat, g.li[lvl]);
+    if (valid) {
+      g.univ[lvl] = dm.lat_univ[lat.univ_off + lat.n[0] * lat.n[1] * g.li[lvl][2] + lat.n[0] * g.li[lvl][1] + g.li[lvl][0]];
+      g.cell[lvl] = C_NONE;
+    }
+  }
   bool lost_outer = false;
-  if (!lattice_valid(lat, g.li[lvl])) {
+  if (!valid) {
     g.n_coord = 1;
     if (!exhaustive_find_cell(g, lost_outer)) mark_lost(s);
-  } else {
-    g.univ[lvl] = dm.lat_univ[lat.univ_off + lat.n[0] * lat.n[1] * g.li[lvl][2] + lat.n[0] * g.li[lvl][1] + g.li[lvl][0]];
-    g.cell[lvl] = C_NONE;
-    if (!exhaustive_find_cell(g, lost_outer)) {
-      g.n_coord = 1;
-      if (!exhaustive_find_cell(g, lost_outer)) mark_lost(s);
-    }
+  } else if (!exhaustive_find_cell(g, lost_outer)) {
+    g.n_coord = 1;
+    if (!exhaustive_find_cell(g, lost_outer)) mark_lost(s);
   }
 }
 
@@ -2098,4 +2153,5 @@ void gpu_set_ww_on(GpuSim* G, bool on)
 
 long long gpu_capacity(GpuSim* G) { return G->bank.cap; }
 
+}  // namespace OMC_NS
 }  // namespace omc

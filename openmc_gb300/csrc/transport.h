@@ -19,6 +19,7 @@ struct GpuOptions {
   long long tail_threshold = -1;  // queue length for the history-based tail (-1: default)
   int fuse = 3;                 // bit 0: cross-section event, bit 1: surface crossing, inside the advance kernel
   int split_slots = 0;          // split particles start in free slots with their own seeds
+  int max_levels = 0;           // coordinate depth of the kernels (0: the model's, rounded up to 2 or 4)
 };
 
 struct BatchStats {
@@ -41,6 +42,28 @@ struct BatchStats {
   float kernel_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
+// The interface below is implemented twice (transport.cu built for at most
+// 2 and at most 4 coordinate levels, namespaces l2 and l4); the functions in
+// omc itself pick the build from the model's depth (transport_dispatch.cpp).
+#define OMC_GPU_API(NS)                                                                     \
+  namespace NS {                                                                            \
+  struct GpuSim;                                                                            \
+  GpuSim* gpu_create(const HModel& m, const GpuOptions& opt);                               \
+  void gpu_destroy(GpuSim* g);                                                              \
+  BatchStats gpu_run_batch(GpuSim* g, HModel& m, int batch, bool accumulate);               \
+  BatchStats gpu_run_batch_profiled(GpuSim* g, HModel& m, int batch, bool accumulate);      \
+  void gpu_fetch_tallies(GpuSim* g, HModel& m);                                             \
+  void gpu_reset_tallies(GpuSim* g, HModel& m);                                             \
+  void gpu_set_trace(GpuSim* g, long long n_hist, int cap, int batch, long long first);     \
+  void gpu_get_trace(GpuSim* g, void* records, int* counts);                                \
+  void gpu_set_ww_bounds(GpuSim* g, const double* lower, const double* upper, long long n); \
+  void gpu_set_ww_on(GpuSim* g, bool on);                                                   \
+  long long gpu_capacity(GpuSim* g);                                                        \
+  }
+
+OMC_GPU_API(l2)
+OMC_GPU_API(l4)
+
 GpuSim* gpu_create(const HModel& m, const GpuOptions& opt);
 void gpu_destroy(GpuSim* g);
 BatchStats gpu_run_batch(GpuSim* g, HModel& m, int batch, bool accumulate);
@@ -54,5 +77,7 @@ void gpu_get_trace(GpuSim* g, void* records, int* counts);
 void gpu_set_ww_bounds(GpuSim* g, const double* lower, const double* upper, long long n);
 void gpu_set_ww_on(GpuSim* g, bool on);
 long long gpu_capacity(GpuSim* g);
+// coordinate depth of the kernels a simulation runs (2 or 4)
+int gpu_levels(GpuSim* g);
 
 }  // namespace omc

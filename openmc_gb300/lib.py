@@ -202,6 +202,7 @@ class _Settings:
     tail_threshold = _DLLGlobal(C.c_int64, "openmc_gb300_tail_threshold")
     secondary_capacity = _DLLGlobal(C.c_int64, "openmc_gb300_secondary_capacity")
     split_to_slots = _DLLGlobal(C.c_int, "openmc_gb300_split_to_slots")
+    max_levels = _DLLGlobal(C.c_int, "openmc_gb300_max_levels")
 
     @property
     def seed(self):

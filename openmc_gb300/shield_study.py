@@ -101,6 +101,7 @@ def run(directory, length=200.0, mesh_dim=(200, 10, 10), n_points=11303, pilot_p
            "split_to_slots": bool(split_to_slots),
            "pilot": f"{pilot_batches} x {pilot_particles}", "measure": f"{batches} x {particles}"}
     lib.init(directory=path)
+    saved = (lib.settings.xs_fp32, lib.settings.split_to_slots)
     try:
         lib.settings.xs_fp32 = 1 if fp32 else 0
         lib.settings.split_to_slots = 1 if split_to_slots else 0
@@ -127,6 +128,7 @@ def run(directory, length=200.0, mesh_dim=(200, 10, 10), n_points=11303, pilot_p
             res[name] = r
             out[name] = {**out.get(name, {}), **_summary(r)}
     finally:
+        lib.settings.xs_fp32, lib.settings.split_to_slots = saved
         lib.finalize()
     base = out["plain"]["fom"] if "plain" in out else 0.0
     for name in methods:

@@ -26,6 +26,7 @@ def _layers(path, split, batches=6):
         m, s = lib.tally_mean_std(lib.tally_ids()[2])
         lib.simulation_finalize()
     finally:
+        lib.settings.split_to_slots = 0
         lib.finalize()
     return m.ravel(), s.ravel(), sec
 

@@ -22,13 +22,17 @@ DISCRETE = ("kind", "cell", "material", "surface_or_nuclide", "grid_hash", "n_co
 CONT = ("E", "dist", "wgt")
 
 
-def run_gpu(path, n_trace=0, cap=256, fp32=False, in_flight=0, sort=True, batches=None, ww_on=None):
+def run_gpu(path, n_trace=0, cap=256, fp32=False, in_flight=0, sort=True, batches=None, ww_on=None,
+            max_levels=0, fuse=3):
     from openmc_gb300 import lib
     lib.init(directory=path)
     try:
         lib.settings.xs_fp32 = 1 if fp32 else 0
         lib.settings.particles_in_flight = in_flight
         lib.settings.sort_queue = 1 if sort else 0
+        lib.settings.max_levels = max_levels
+        lib.settings.fuse_xs = fuse
+        lib.settings.split_to_slots = 0  # the reference's per-history secondary order
         if n_trace:
             lib.set_trace(n_trace, cap)
         lib.simulation_init()
@@ -146,6 +150,20 @@ def test_lattice_history_parity(lattice):
     assert_tallies_close(g["tallies"], o["tallies"])
     lk = g["batch"]["leakage"] / g["batch"]["total_weight"]
     assert 0.0 <= lk <= 1.0
+
+
+def test_lattice_builds_agree(lattice):
+    """The 2-level build (per-level state in registers) and the 4-level
+    build, and the unfused event kernels, give the same histories."""
+    xml, path = lattice
+    a = run_gpu(path, n_trace=600, cap=1024)
+    b = run_gpu(path, n_trace=600, cap=1024, max_levels=4)
+    c = run_gpu(path, n_trace=600, cap=1024, fuse=0)
+    for other in (b, c):
+        assert not trace_mismatches(a["trace"], other["trace"], 1024)
+        for (ra, na), (rb, nb) in zip(a["tallies"], other["tallies"]):
+            assert na == nb
+            np.testing.assert_allclose(ra[..., 1], rb[..., 1], rtol=1e-9, atol=1e-300)
 
 
 @pytest.fixture(scope="module")

@@ -262,6 +262,21 @@ def run_gb300(args):
             lib.simulation_finalize()
         finally:
             lib.finalize()
+        # the same batch through the history-based kernel (settings.event_based = False)
+        lib.init(directory=path)
+        try:
+            lib.settings.xs_fp32 = 1
+            lib.settings.event_based = False
+            lib.settings.particles_in_flight = args.in_flight
+            lib.simulation_init()
+            lib.next_batch()
+            flush_l2(flush)
+            lib.next_batch()
+            out["history_value"] = n / (lib.last_batch()["ms"] / 1000.0)
+            lib.simulation_finalize()
+        finally:
+            lib.settings.event_based = True
+            lib.finalize()
     return out
 
 
@@ -395,6 +410,7 @@ def main():
         "cpu_baseline": cpu,
         "kernel_ms_profiled_batch": r["kernel_ms"],
         "fp64_xs_particles_per_s": r.get("fp64_value"),
+        "history_based_gpu_particles_per_s": r.get("history_value"),
         "events_per_step": r["detail"]["queue"]["xs_events"] + r["detail"]["tail"]["xs_events"],
         "iterations_per_step": r["iterations"],
         "xs_lookup_microbench": r.get("xs_lookup"),

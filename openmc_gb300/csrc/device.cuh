@@ -210,6 +210,7 @@ struct DQueues {
   int* cursor;
   DSecondary* sec;
   DSplitSite* split;  // split-to-slots ring, or null
+  int history;        // 1: history-based loop (slots are not recycled through the free list)
   DCounters* cnt;
   TraceRec* trace;
   int* trace_n;

@@ -627,8 +627,10 @@ __device__ bool revive_or_free(long long s, double wgt)
     unsigned long long key = (static_cast<unsigned long long>(db.n_total[s]) << 34) |
                              static_cast<unsigned long long>(db.id[s]);
     atomicMax(&dq.cnt->longest, key);
-    int k = atomicAdd(&dq.cnt->n_free, 1);
-    dq.free_list[k] = static_cast<int>(s);
+    if (!dq.history) {
+      int k = atomicAdd(&dq.cnt->n_free, 1);
+      dq.free_list[k] = static_cast<int>(s);
+    }
     atomicAdd(reinterpret_cast<unsigned long long*>(&dq.cnt->n_done), 1ull);
     return false;
   }
@@ -1231,7 +1233,7 @@ __global__ void __launch_bounds__(256, OMC_MINB_COLL) k_collision()
 // max_events events (src/simulation.cpp:804-821, history-based loop) instead
 // of paying one kernel launch per event.  Histories that reach the limit go
 // back to the queue.  The per-history physics is the same event functions.
-__global__ void __launch_bounds__(128) k_tail(int max_events)
+__global__ void __launch_bounds__(128, 2) k_tail(int max_events)
 {
   if (!dq.cnt->tail) return;
   const int n = dq.cnt->n_q;
@@ -1257,6 +1259,35 @@ __global__ void __launch_bounds__(128) k_tail(int max_events)
 
 // Free slots take waiting split particles first (split-to-slots mode), then
 // new source particles.
+// History-based loop (src/simulation.cpp:804-831, the reference's default
+// when settings.event_based is false): each thread owns one slot and
+// carries a history from birth through every banked secondary to its end
+// with the same event functions, then claims the next source index.
+__global__ void __launch_bounds__(128, 2) k_history()
+{
+  const long long s = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  EvStats st {};
+  if (s < db.cap) {
+    for (;;) {
+      const long long idx = static_cast<long long>(
+        atomicAdd(reinterpret_cast<unsigned long long*>(&dq.cnt->next_source), 1ull));
+      if (idx > dm.n_particles || dq.cnt->error != 0) break;
+      initialize_history(s, idx);
+      int nx = NEXT_XS;
+      // every particle dies within max_events events (revive_or_free)
+      for (long long e = 0; nx == NEXT_XS && e < (1LL << 40); ++e) {
+        ev_xs(s, st);
+        nx = ev_advance(s, st);
+        if (nx == NEXT_SURF) nx = ev_surface(s, st);
+        else if (nx == NEXT_COLL) nx = ev_collision(s, st);
+      }
+    }
+  }
+  __syncwarp();
+  flush_stats(st, 1);
+  warp_count(&dq.cnt->n_events, st.xs_ev);
+}
+
 __global__ void k_refill_plan()
 {
   DCounters* c = dq.cnt;
@@ -1492,6 +1523,7 @@ struct GpuSim {
   int sort = 1;
   int fuse = 3;  // bit 0: cross-section event, bit 1: surface crossing, inside the advance kernel
   int split_slots = 0;  // split particles start in free slots with their own seeds
+  int history = 0;      // history-based loop (settings.event_based false)
   long long tail_threshold = 1 << 17;
   int tail_max_events = 1 << 16;
   bool tallies_dirty = true;
@@ -1815,6 +1847,7 @@ static void build_bank(GpuSim& G, long long cap, long long sec_cap)
   q.trace_hist = 0;
   q.trace_cap = 0;
   q.batch = 1;
+  q.history = G.history;
   DCounters c {};
   c.sec_cap = G.split_slots ? 1 : static_cast<int>(sec_cap);
   c.split_cap = G.split_slots ? static_cast<int>(sec_cap) : 0;
@@ -1901,7 +1934,8 @@ GpuSim* gpu_create(const HModel& m, const GpuOptions& opt)
     G->fuse = opt.fuse & 3;
     if (G->fuse == 2) G->fuse = 3;  // the surface fusion builds on the cross-section fusion
     if (opt.tail_threshold >= 0) G->tail_threshold = opt.tail_threshold;
-    G->split_slots = (opt.split_slots && (m.ww_on || !m.weight_windows.empty())) ? 1 : 0;
+    G->history = m.event_based ? 0 : 1;
+    G->split_slots = (!G->history && opt.split_slots && (m.ww_on || !m.weight_windows.empty())) ? 1 : 0;
     int sms = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
     G->blocks = sms * 8;
@@ -1978,12 +2012,23 @@ static void accumulate_batch(GpuSim* G, HModel& m)
   G->tallies_dirty = true;
 }
 
+static void launch_history_batch(GpuSim* G, int batch)
+{
+  const int nb = G->blocks, nt = 256;
+  k_batch_init<<<nb, nt, 0, G->stream>>>(batch);
+  if (G->queues.src_n > 0) k_source_bank<<<nb, nt, 0, G->stream>>>();
+  const long long threads = G->bank.cap;
+  k_history<<<static_cast<unsigned>((threads + 127) / 128), 128, 0, G->stream>>>();
+  CK(cudaGetLastError());
+}
+
 BatchStats gpu_run_batch(GpuSim* G, HModel& m, int batch, bool accumulate)
 {
   G->queues.batch = batch;
   CK(cudaMemcpyToSymbolAsync(dq, &G->queues, sizeof(DQueues), 0, cudaMemcpyHostToDevice, G->stream));
   CK(cudaEventRecord(G->ev0, G->stream));
-  CK(cudaGraphLaunch(G->exec, G->stream));
+  if (G->queues.history) launch_history_batch(G, batch);
+  else CK(cudaGraphLaunch(G->exec, G->stream));
   CK(cudaEventRecord(G->ev1, G->stream));
   BatchStats st {};
   DCounters c {};
@@ -1998,6 +2043,11 @@ BatchStats gpu_run_batch(GpuSim* G, HModel& m, int batch, bool accumulate)
 
 BatchStats gpu_run_batch_profiled(GpuSim* G, HModel& m, int batch, bool accumulate)
 {
+  if (G->queues.history) {
+    BatchStats st = gpu_run_batch(G, m, batch, accumulate);
+    st.kernel_ms[4] = st.ms;  // the whole batch is one history-based kernel
+    return st;
+  }
   G->queues.batch = batch;
   CK(cudaMemcpyToSymbolAsync(dq, &G->queues, sizeof(DQueues), 0, cudaMemcpyHostToDevice, G->stream));
   const int nb = G->blocks, nt = 256;

@@ -23,10 +23,11 @@ CONT = ("E", "dist", "wgt")
 
 
 def run_gpu(path, n_trace=0, cap=256, fp32=False, in_flight=0, sort=True, batches=None, ww_on=None,
-            max_levels=0, fuse=3):
+            max_levels=0, fuse=3, event_based=True):
     from openmc_gb300 import lib
     lib.init(directory=path)
     try:
+        lib.settings.event_based = event_based
         lib.settings.xs_fp32 = 1 if fp32 else 0
         lib.settings.particles_in_flight = in_flight
         lib.settings.sort_queue = 1 if sort else 0
@@ -150,6 +151,19 @@ def test_lattice_history_parity(lattice):
     assert_tallies_close(g["tallies"], o["tallies"])
     lk = g["batch"]["leakage"] / g["batch"]["total_weight"]
     assert 0.0 <= lk <= 1.0
+
+
+def test_lattice_history_based_parity(lattice):
+    """settings.event_based = False runs the history-based kernel (one thread
+    per history, src/simulation.cpp:804-831); histories and tallies match the
+    oracle as the event-based loop does."""
+    xml, path = lattice
+    g = run_gpu(path, n_trace=800, cap=1024, event_based=False)
+    o = run_oracle(xml, n_trace=800, cap=1024)
+    bad = trace_mismatches(g["trace"], o["trace"], 1024)
+    assert not bad, f"{len(bad)} histories differ, first: {bad[:5]}"
+    assert_tallies_close(g["tallies"], o["tallies"])
+    assert g["batch"]["done"] > 0
 
 
 def test_lattice_builds_agree(lattice):

@@ -226,3 +226,107 @@ def shield(directory, particles=1_000_000, batches=10, n_points=11303, seed=4,
         settings.weight_windows = [weight_windows]
         settings.weight_windows_on = True
     return om.Model(geom, mats, settings, om.Tallies([t, tb, tp])), directory
+
+
+def full_scale(directory, particles=100_000_000, batches=50, n_points=11303, seed=3,
+               event_based=True, shield_layers=10, layer=10.0, height=200.0,
+               mesh_dim=(100, 100, 60), n_ebins=50, ww_mesh_dim=None, ww_groups=None):
+    """The 17x17 lattice wrapped in a layered shield: alternating 10 cm
+    shells of the lattice's light scatterer and A=56-like clad material
+    around the lattice box (vacuum outside and at the axial ends), 68
+    synthetic nuclides (the lattice's 12 plus 56 trace nuclides spread over
+    the materials), source in the fuel, flux on a 100 x 100 x 60 mesh x 50
+    energy bins over the whole assembly (3e7 bins), and a flux tally on the
+    outermost shell.  ww_mesh_dim / ww_groups add weight windows (all -1) on
+    a mesh of that shape over the assembly with those energy bounds, plus a
+    flux tally on the same mesh and groups (for pilot runs)."""
+    directory = Path(directory)
+    specs = [("Hv235", 235), ("Hv238", 238), ("Ox16", 16), ("Hv240", 240),
+             ("Cl56", 56), ("Cl58", 58), ("Cl90", 90), ("Cl91", 91),
+             ("Lt1", 1), ("Lt2", 2), ("Lt16", 16), ("Lt10", 10)]
+    rng = np.random.default_rng(seed + 101)
+    extra = [(f"Tr{k:02d}", int(a)) for k, a in enumerate(rng.integers(20, 245, 56))]
+    _, xs_xml = _library(directory, specs + extra, n_points, seed)
+
+    def mixture(name, names, weights, density):
+        m = om.Material(name=name)
+        w = np.asarray(weights, float)
+        for n, f in zip(names, w / w.sum()):
+            m.add_nuclide(n, float(f))
+        m.set_density("atom/b-cm", density)
+        return m
+
+    tr = [n for n, _ in extra]
+    fuel = mixture("heavy absorber", ["Hv235", "Hv238", "Ox16", "Hv240"] + tr[:32],
+                   [0.03, 0.30, 0.66, 0.01] + [2e-4] * 32, 0.069)
+    clad = mixture("clad", ["Cl56", "Cl58", "Cl90", "Cl91"] + tr[32:48],
+                   [0.6, 0.2, 0.15, 0.05] + [1e-3] * 16, 0.043)
+    mod = mixture("light scatterer", ["Lt1", "Lt2", "Lt16", "Lt10"] + tr[48:],
+                  [0.66, 0.001, 0.33, 0.009] + [1e-4] * 8, 0.1)
+    mats = om.Materials([fuel, clad, mod], cross_sections=xs_xml.name)
+    pin = _pin_universe(fuel, clad, mod)
+    gt = _pin_universe(fuel, clad, mod, r_pin=0.56, r_clad=0.60, guide=True)
+    pitch, n = 1.26, 17
+    half = pitch * n / 2.0
+    lat = om.RectLattice()
+    lat.pitch = [pitch, pitch]
+    lat.lower_left = [-half, -half]
+    rows = [[pin] * n for _ in range(n)]
+    for (i, j) in GUIDE_TUBES:
+        rows[i][j] = gt
+    lat.universes = rows
+    zlo = om.ZPlane(-height / 2, boundary_type="vacuum")
+    zhi = om.ZPlane(height / 2, boundary_type="vacuum")
+    hws = [half + k * layer for k in range(shield_layers + 1)]
+    xm = [om.XPlane(-h) for h in hws]
+    xp = [om.XPlane(h) for h in hws]
+    ym = [om.YPlane(-h) for h in hws]
+    yp = [om.YPlane(h) for h in hws]
+    for s in (xm[-1], xp[-1], ym[-1], yp[-1]):
+        s.boundary_type = "vacuum"
+
+    def box(k):
+        return +xm[k] & -xp[k] & +ym[k] & -yp[k]
+
+    cells = [om.Cell(fill=lat, region=box(0) & +zlo & -zhi)]
+    for k in range(shield_layers):
+        cells.append(om.Cell(fill=(mod if k % 2 == 0 else clad),
+                             region=box(k + 1) & ~box(k) & +zlo & -zhi))
+    geom = om.Geometry(om.Universe(cells=cells))
+    settings = om.Settings(particles=particles, batches=batches, event_based=event_based, seed=1)
+    settings.source = [om.IndependentSource(
+        space=om.Box((-half, -half, -height / 2), (half, half, height / 2)),
+        angle=om.Isotropic(), energy=om.Maxwell(1.3e6),
+        constraints={"domains": [fuel]})]
+    outer = hws[-1]
+    mesh = om.RegularMesh()
+    mesh.dimension = list(mesh_dim)
+    mesh.lower_left = [-outer, -outer, -height / 2]
+    mesh.upper_right = [outer, outer, height / 2]
+    t = om.Tally(name="assembly flux")
+    t.filters = [om.MeshFilter(mesh), om.EnergyFilter(log_energy_bins(n_ebins))]
+    # flux in the outermost shell: a 2x2x1 mesh bins the whole assembly; the
+    # outer shell is recovered by the caller from the layer tally below
+    shell = om.RegularMesh()
+    shell.dimension = [2 * shield_layers + 1, 1, 1]
+    shell.lower_left = [-outer, -half, -height / 2]
+    shell.upper_right = [outer, half, height / 2]
+    ts = om.Tally(name="flux across the shells (x slab through the lattice)")
+    ts.filters = [om.MeshFilter(shell)]
+    tallies = [t, ts]
+    if ww_mesh_dim is not None:
+        groups = [float(e) for e in (ww_groups if ww_groups is not None else [0.0, 2.0e7 * 1.000001])]
+        wm = om.RegularMesh()
+        wm.dimension = list(ww_mesh_dim)
+        wm.lower_left = [-outer, -outer, -height / 2]
+        wm.upper_right = [outer, outer, height / 2]
+        tw = om.Tally(name="window mesh flux")
+        tw.filters = [om.MeshFilter(wm)]
+        if len(groups) > 2:
+            tw.filters.append(om.EnergyFilter(groups))
+        tallies.append(tw)
+        nb = int(np.prod(ww_mesh_dim)) * (len(groups) - 1)
+        settings.weight_windows = [om.WeightWindows(wm, -np.ones(nb), upper_ww_bounds=-np.ones(nb),
+                                                    energy_bounds=groups)]
+        settings.weight_windows_on = True
+    return om.Model(geom, mats, settings, om.Tallies(tallies)), directory

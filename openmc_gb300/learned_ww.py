@@ -82,6 +82,14 @@ class Result:
     info: dict = field(default_factory=dict)
 
 
+def scored_bins(mean, std, geom, rel_max=1.0):
+    """Bins [n_groups * n_mesh, group-major] that enter the training set."""
+    m = np.asarray(mean, float).reshape(geom.n_mesh, geom.n_groups).T
+    s = np.asarray(std, float).reshape(geom.n_mesh, geom.n_groups).T
+    rel = np.where(m > 0, s / np.where(m > 0, m, 1.0), np.inf)
+    return ((m > 0) & (rel < rel_max)).ravel()
+
+
 def training_pairs(mean, std, geom, rel_max=1.0, rel_floor=0.05):
     """(features, target, weight) from a pilot flux tally.
 
@@ -109,12 +117,25 @@ def training_pairs(mean, std, geom, rel_max=1.0, rel_floor=0.05):
     return x_all[ok], target, w, f
 
 
-def bounds_from_log_flux(log_flux, geom, ratio=5.0):
+def bounds_from_log_flux(log_flux, geom, ratio=5.0, scored=None, max_extrapolation=1.0e3):
     """MAGIC's normalisation applied to a predicted flux [n_groups * n_mesh]:
-    per group lower = flux / (2 max), upper = ratio * lower."""
+    per group lower = flux / (2 max), upper = ratio * lower.
+
+    scored (bool [n_groups * n_mesh], optional): bins the pilot scored.  In
+    the other bins the prediction is an extrapolation; there the lower bound
+    is kept at or above the group's lowest scored bound / max_extrapolation,
+    so that an extrapolation far below the true flux cannot split a particle
+    into an unbounded number of copies (a bound above the true flux only
+    rouletted particles, which costs efficiency, not correctness)."""
     lf = np.asarray(log_flux, float).reshape(geom.n_groups, geom.n_mesh)
     lf = lf - lf.max(axis=1, keepdims=True)
     lower = 0.5 * np.exp(lf)
+    if scored is not None:
+        sc = np.asarray(scored, bool).reshape(geom.n_groups, geom.n_mesh)
+        for g in range(geom.n_groups):
+            if sc[g].any():
+                floor = lower[g][sc[g]].min() / max_extrapolation
+                lower[g] = np.where(sc[g], lower[g], np.maximum(lower[g], floor))
     return lower.ravel(), ratio * lower.ravel()
 
 
@@ -131,7 +152,7 @@ def fit(mean, std, geom, steps=2000, lr=2e-3, seed=1, ratio=5.0, rel_max=1.0):
         pred = net.predict(feats.inputs()).astype(np.float64) * feats.sigma + feats.mu
     finally:
         net.close()
-    lower, upper = bounds_from_log_flux(pred, geom, ratio)
+    lower, upper = bounds_from_log_flux(pred, geom, ratio, scored=scored_bins(mean, std, geom, rel_max))
     return Result(lower, upper, loss, ms, len(target),
                   {"train_wall_s": wall, "mu": feats.mu, "sigma": feats.sigma, "log_flux": pred})
 

@@ -54,3 +54,18 @@ def test_bounds_follow_magic_normalisation():
     np.testing.assert_allclose(up, 5.0 * lo)
     flux = np.exp(lf).reshape(g.n_groups, g.n_mesh)
     np.testing.assert_allclose(per, flux / (2 * flux.max(axis=1, keepdims=True)))
+
+
+def test_extrapolated_bounds_are_floored():
+    from openmc_gb300.learned_ww import bounds_from_log_flux
+    g = _geom()
+    lf = -np.arange(g.n_mesh * g.n_groups, dtype=float) * 2.0
+    scored = np.zeros(g.n_mesh * g.n_groups, bool)
+    scored[:4] = True  # group 0, first four bins
+    lo, _ = bounds_from_log_flux(lf, g, scored=scored, max_extrapolation=100.0)
+    per = lo.reshape(g.n_groups, g.n_mesh)
+    floor = per[0, :4].min() / 100.0
+    assert np.all(per[0, 4:] >= floor * (1 - 1e-12))
+    np.testing.assert_allclose(per[0, :4], 0.5 * np.exp(lf[:4] - lf[:16].max()))
+    # groups without scored bins keep the plain prediction
+    np.testing.assert_allclose(per[1], 0.5 * np.exp(lf[16:32] - lf[16:32].max()))

@@ -1,0 +1,69 @@
+"""Edge cases on the GPU: a single history, a single particle slot, a model
+without tallies, empty lookups, a one-row network."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_single_history_and_single_slot(built, tmp_path):
+    from openmc_gb300 import configs, lib
+    import oracle
+    m, path = configs.point_cube(tmp_path, particles=1, batches=3, n_points=400, mesh_dim=(3, 3, 3), n_ebins=4)
+    xml = m.export_to_model_xml(path)
+    lib.init(directory=path)
+    try:
+        lib.settings.particles_in_flight = 1
+        lib.set_trace(1, 4096)
+        lib.simulation_init()
+        for _ in range(3):
+            lib.next_batch()
+            assert lib.last_batch()["done"] == 1
+        mean, _ = lib.tally_mean_std(lib.tally_ids()[0])
+        lib.simulation_finalize()
+    finally:
+        lib.settings.particles_in_flight = 0
+        lib.finalize()
+    o = oracle.Oracle(xml)
+    o.run(threads=1)
+    assert np.allclose(mean.ravel(), o.tally(0)[:, 1] / 3, rtol=1e-5, atol=1e-12)
+
+
+def test_model_without_tallies(built, tmp_path):
+    from openmc_gb300 import configs, lib
+    from openmc_gb300 import model as om
+    m, path = configs.point_cube(tmp_path, particles=2000, batches=2, n_points=400)
+    m.tallies = om.Tallies([])
+    m.export_to_model_xml(path)
+    lib.init(directory=path)
+    try:
+        lib.run()
+        assert lib.tally_ids() == []
+        assert lib.last_batch()["done"] == 2000
+    finally:
+        lib.finalize()
+
+
+def test_empty_and_single_lookups(built):
+    from openmc_gb300 import data, lib
+    d = data.make_xsbench(n_nuc=6, n_points=300, seed=2, mat_counts=(4, 2))
+    t = lib.XSTables(d, n_log_bins=200, max_lookups=16)
+    out, h = t.lookup(np.zeros(0, np.int32), np.zeros(0))
+    assert out.shape == (0, 5) and h.shape == (0,)
+    out, h = t.lookup(np.array([1], np.int32), np.array([data.E_MAX]))
+    assert np.isfinite(out).all()
+    t.close()
+
+
+def test_one_row_network(built):
+    from openmc_gb300 import lib
+    from oracle import mlp as om
+    net = lib.ImportanceNetwork(max_rows=1, seed=9)
+    x = np.array([[0.1, -0.2, 0.3, 0.9]], np.float32)
+    net.set_data(x, np.array([0.5], np.float32))
+    loss, g = net.gradients()
+    loss_ref, g_ref = om.loss_and_grad(net.params.astype(np.float64), x.astype(np.float64), np.array([0.5]))
+    assert abs(loss - loss_ref) <= 1e-3 * abs(loss_ref) + 1e-7
+    assert np.linalg.norm(g - g_ref) <= 2e-2 * np.linalg.norm(g_ref)
+    assert np.isfinite(net.predict(x)).all()
+    net.close()

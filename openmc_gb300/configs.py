@@ -46,7 +46,8 @@ def log_energy_bins(n, e_min=data.E_MIN, e_max=data.E_MAX):
 
 
 def point_cube(directory, particles=100_000, batches=10, n_points=2000,
-               seed=1, event_based=True, mesh_dim=(10, 10, 10), n_ebins=50):
+               seed=1, event_based=True, mesh_dim=(10, 10, 10), n_ebins=50,
+               estimator_tallies=False):
     directory = Path(directory)
     rng = np.random.default_rng(seed)
     specs = [("H1", 1), ("C12", 12), ("O16", 16), ("Fe56", 56)]
@@ -81,7 +82,26 @@ def point_cube(directory, particles=100_000, batches=10, n_points=2000,
     t = om.Tally(name="mesh flux")
     t.filters = [om.MeshFilter(mesh), om.EnergyFilter(log_energy_bins(n_ebins))]
     t.scores = ["flux"]
-    return om.Model(geom, mats, settings, om.Tallies([t])), directory
+    tallies = [t]
+    if estimator_tallies:
+        # the same quantities with both estimators, binned by cell and by
+        # material (src/tallies/filter_cell.cpp, filter_material.cpp)
+        groups = om.EnergyFilter([data.E_MIN, 1.0, 1.0e3, 1.0e5, data.E_MAX])
+        for est in ("tracklength", "collision"):
+            tc = om.Tally(name=f"cell {est}")
+            tc.filters = [om.CellFilter(cells), groups]
+            tc.scores = ["flux", "total", "absorption"]
+            tc.estimator = est
+            tm = om.Tally(name=f"material {est}")
+            tm.filters = [om.MaterialFilter([mat])]
+            tm.scores = ["flux", "absorption"]
+            tm.estimator = est
+            te = om.Tally(name=f"mesh {est}")
+            te.filters = [om.MeshFilter(mesh)]
+            te.scores = ["flux"]
+            te.estimator = est
+            tallies += [tc, tm, te]
+    return om.Model(geom, mats, settings, om.Tallies(tallies)), directory
 
 
 def _pin_universe(fuel, clad, mod, r_pin=0.41, r_clad=0.475, guide=False):

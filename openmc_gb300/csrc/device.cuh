@@ -59,10 +59,12 @@ struct DMesh {
 
 struct DFilter {
   int type, mesh, nbins, e_off;
+  int i_off;  // cell / material filters: offset of the bins' indices in DModel::fids
 };
 
 struct DTally {
   long long value_off;
+  int estimator;  // 0 track length, 1 collision
   int nfilt, nscore;
   int filt[3], stride[3];
   int score[4];
@@ -103,10 +105,12 @@ struct DModel {
   const int* cell_id;
   // tallies
   int n_tally;
+  int n_tally_tracklength, n_tally_collision;
   const DTally* tally;
   const DFilter* filt;
   const DMesh* mesh;
   const double* ebins;
+  const int* fids;  // cell / material indices of cell and material filter bins
   double* value;
   // weight windows
   int ww_on, ww_mesh, ww_ne, ww_max_split;

@@ -581,6 +581,24 @@ void load_model(const std::string& path_in, HModel& m)
         f.type = FILTER_PARTICLE;
         f.mesh = -1;
         f.nbins = 1;
+      } else if (t == "cell" || t == "material") {
+        // src/tallies/filter_cell.cpp:48-58, filter_material.cpp:47-55
+        f.type = t == "cell" ? FILTER_CELL : FILTER_MATERIAL;
+        f.mesh = -1;
+        for (auto id : split_ints(bins)) {
+          int found = -1;
+          if (f.type == FILTER_CELL) {
+            for (size_t k = 0; k < m.cells.size(); ++k)
+              if (m.cells[k].id == static_cast<int>(id)) found = static_cast<int>(k);
+          } else {
+            for (size_t k = 0; k < m.materials.size(); ++k)
+              if (m.materials[k].id == static_cast<int>(id)) found = static_cast<int>(k);
+          }
+          if (found < 0) throw std::runtime_error(t + " filter " + std::to_string(f.id) + ": unknown id " + std::to_string(id));
+          f.ids.push_back(found);
+        }
+        f.nbins = static_cast<int>(f.ids.size());
+        if (f.nbins == 0) throw std::runtime_error(t + " filter " + std::to_string(f.id) + " has no bins");
       } else {
         throw std::runtime_error("filter type '" + t + "' is not supported by the GPU transport path");
       }
@@ -595,8 +613,10 @@ void load_model(const std::string& path_in, HModel& m)
           if (!filt_index.count(static_cast<int>(fid))) throw std::runtime_error("tally " + std::to_string(t.id) + ": unknown filter");
           t.filters.push_back(filt_index[static_cast<int>(fid)]);
         }
-      std::string est = te->value_or("estimator", "tracklength");
-      if (est != "tracklength") throw std::runtime_error("only track-length estimators are supported");
+      std::string est = XmlNode::trim(te->value_or("estimator", "tracklength"));
+      if (est == "tracklength") t.estimator = EST_TRACKLENGTH;
+      else if (est == "collision") t.estimator = EST_COLLISION;
+      else throw std::runtime_error("only track-length and collision estimators are supported");
       if (te->has("nuclides") && XmlNode::trim(te->value("nuclides")) != "total")
         throw std::runtime_error("nuclide bins other than 'total' are not supported");
       for (const auto& s : split_words(te->value("scores"))) {
@@ -608,6 +628,9 @@ void load_model(const std::string& path_in, HModel& m)
       int n_mesh = 0;
       for (int f : t.filters) n_mesh += m.filters[f].type == FILTER_MESH;
       if (n_mesh > 1) throw std::runtime_error("a tally may hold at most one mesh filter");
+      int n_cell = 0;
+      for (int f : t.filters) n_cell += m.filters[f].type == FILTER_CELL;
+      if (n_cell > 1) throw std::runtime_error("a tally may hold at most one cell filter");
       if (t.filters.size() > 3) throw std::runtime_error("a tally may hold at most three filters");
       m.tallies.push_back(std::move(t));
     }

@@ -13,7 +13,8 @@ constexpr int SURF_XPLANE = 0, SURF_YPLANE = 1, SURF_ZPLANE = 2, SURF_XCYL = 3,
               SURF_YCYL = 4, SURF_ZCYL = 5, SURF_SPHERE = 6;
 constexpr int BC_TRANSMIT = 0, BC_VACUUM = 1, BC_REFLECT = 2;
 constexpr int FILL_MATERIAL = 0, FILL_UNIVERSE = 1, FILL_LATTICE = 2;
-constexpr int FILTER_MESH = 0, FILTER_ENERGY = 1, FILTER_PARTICLE = 2;
+constexpr int FILTER_MESH = 0, FILTER_ENERGY = 1, FILTER_PARTICLE = 2, FILTER_CELL = 3, FILTER_MATERIAL = 4;
+constexpr int EST_TRACKLENGTH = 0, EST_COLLISION = 1;
 constexpr int SCORE_FLUX = 0, SCORE_TOTAL = 1, SCORE_ABSORPTION = 2;
 // Region operator tokens, include/openmc/cell.h:31-35
 constexpr int32_t OP_LEFT_PAREN = 2147483647;
@@ -53,10 +54,12 @@ struct HMesh {
 struct HFilter {
   int id, type, mesh, nbins;
   std::vector<double> bins;
+  std::vector<int> ids;  // cell / material indices of the bins
 };
 
 struct HTally {
   int id;
+  int estimator = EST_TRACKLENGTH;
   std::vector<int> filters, strides, scores;
   int64_t n_filter_bins = 1;
   std::vector<double> results;  // [bins][scores][3] host mirror (VALUE, SUM, SUM_SQ)

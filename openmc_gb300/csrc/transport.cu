@@ -154,10 +154,10 @@ __device__ __forceinline__ MeshDist mesh_dist(const DMesh& m, const int* ijk, in
   return d;
 }
 
-// src/mesh.cpp:999-1146 raytrace_mesh/bins_crossed; calls f(bin, fraction)
-template<class F>
+// src/mesh.cpp:999-1146 raytrace_mesh/bins_crossed; calls f(bin, fraction).
 // inv_u (FP32-table mode): reciprocal direction; the track length is then
 // taken as the advance distance itself and fractions use its reciprocal.
+template<class F>
 __device__ void mesh_bins_crossed(const DMesh& m, const double* r0, const double* r1, const double* u, F f,
   const double* inv_u = nullptr, double track = 0.0)
 {
@@ -226,32 +226,76 @@ __device__ void mesh_bins_crossed(const DMesh& m, const double* r0, const double
   }
 }
 
-// src/tallies/tally_scoring.cpp:2416-2541 + FilterBinIter :31-139 +
-// score_general_ce_nonanalog :578-1106 (flux, total, absorption)
+// Cells of the particle's coordinate levels (cell filters match any level).
+struct LevelCells {
+  int c[MAXL];
+  int n;
+};
+
+// Offsets of the non-mesh filter bins of tally T for the particle's state
+// (src/tallies/tally_scoring.cpp:31-139 FilterBinIter; the energy filter
+// bins the pre-event energy E_last, src/tallies/filter_energy.cpp:59-80; a
+// cell filter matches every level whose cell is a bin, filter_cell.cpp:
+// 48-58; a material filter the particle's material, filter_material.cpp:
+// 47-55).  Returns how many combinations there are (0: no bin matches);
+// mesh_slot receives the position of the mesh filter or -1.
+__device__ __forceinline__ int tally_offsets(const DTally& T, double E_last, const LevelCells& lc, int material,
+  long long (&offs)[MAXL], int& mesh_slot)
+{
+  int n = 1;
+  offs[0] = 0;
+  mesh_slot = -1;
+  for (int i = 0; i < T.nfilt; ++i) {
+    const DFilter& F = dm.filt[T.filt[i]];
+    const long long st = T.stride[i];
+    if (F.type == 0) {
+      mesh_slot = i;
+    } else if (F.type == 1) {
+      const double* b = dm.ebins + F.e_off;
+      if (!(E_last >= b[0] && E_last <= b[F.nbins])) return 0;
+      const long long add = static_cast<long long>(lower_bound_index_pos(b, 0, F.nbins + 1, E_last)) * st;
+      for (int k = 0; k < n; ++k) offs[k] += add;
+    } else if (F.type == 4) {
+      int hit = -1;
+      for (int b = 0; b < F.nbins; ++b)
+        if (dm.fids[F.i_off + b] == material) { hit = b; break; }
+      if (hit < 0) return 0;
+      for (int k = 0; k < n; ++k) offs[k] += hit * st;
+    } else if (F.type == 3) {
+      // at most one cell filter per tally, so n == 1 here
+      const long long base = offs[0];
+      int m = 0;
+#pragma unroll
+      for (int l = 0; l < MAXL; ++l) {
+        if (l >= lc.n) break;
+        for (int b = 0; b < F.nbins; ++b)
+          if (dm.fids[F.i_off + b] == lc.c[l]) {
+            if (m < MAXL) offs[m++] = base + b * st;
+            break;
+          }
+      }
+      if (m == 0) return 0;
+      n = m;
+    }
+  }
+  return n;
+}
+
+// src/tallies/tally_scoring.cpp:2416-2541 score_tracklength_tally with the
+// flux, total and absorption scores of score_general_ce_nonanalog
+// (:578-1106): flux = wgt x distance, mesh filters through the raytrace.
 __device__ int score_tracklength(const double* r0, const double* r1, const double* u, double E_last,
-  double wgt, double distance, double mt, double ma, const double* inv_u = nullptr)
+  double wgt, double distance, double mt, double ma, const LevelCells& lc, int material,
+  const double* inv_u = nullptr)
 {
   double flux = wgt * distance;
   int n_seg = 0;
   for (int t = 0; t < dm.n_tally; ++t) {
     const DTally& T = dm.tally[t];
-    long long base = 0;
-    int mesh_slot = -1;
-    bool empty = false;
-    for (int i = 0; i < T.nfilt; ++i) {
-      const DFilter& F = dm.filt[T.filt[i]];
-      if (F.type == 0) {
-        mesh_slot = i;
-      } else if (F.type == 1) {
-        const double* b = dm.ebins + F.e_off;
-        if (E_last >= b[0] && E_last <= b[F.nbins]) {
-          base += static_cast<long long>(lower_bound_index_pos(b, 0, F.nbins + 1, E_last)) * T.stride[i];
-        } else {
-          empty = true;
-        }
-      }
-    }
-    if (empty) continue;
+    if (T.estimator != 0) continue;
+    long long offs[MAXL];
+    int mesh_slot;
+    const int n_off = tally_offsets(T, E_last, lc, material, offs, mesh_slot);
     double* val = dm.value + T.value_off;
     const int ns = T.nscore;
     auto add = [&](long long index, double weight) {
@@ -264,19 +308,60 @@ __device__ int score_tracklength(const double* r0, const double* r1, const doubl
         atomicAdd(val + index * ns + s, score * weight);
       }
     };
-    if (mesh_slot < 0) {
-      add(base, 1.0);
-      ++n_seg;
-    } else {
-      const DMesh& M = dm.mesh[dm.filt[T.filt[mesh_slot]].mesh];
-      const long long stride = T.stride[mesh_slot];
-      mesh_bins_crossed(M, r0, r1, u, [&](int bin, double frac) {
-        add(base + bin * stride, 1. * frac);
+    for (int o = 0; o < n_off; ++o) {
+      const long long base = offs[o];
+      if (mesh_slot < 0) {
+        add(base, 1.0);
         ++n_seg;
-      }, inv_u, distance);
+      } else {
+        const DMesh& M = dm.mesh[dm.filt[T.filt[mesh_slot]].mesh];
+        const long long stride = T.stride[mesh_slot];
+        mesh_bins_crossed(M, r0, r1, u, [&](int bin, double frac) {
+          add(base + bin * stride, 1. * frac);
+          ++n_seg;
+        }, inv_u, distance);
+      }
     }
   }
   return n_seg;
+}
+
+// src/tallies/tally_scoring.cpp:2543-2600 score_collision_tally, called
+// after the collision (src/particle.cpp:361-364): flux = wgt_last /
+// Sigma_t with the pre-collision cross sections, mesh filters bin the
+// collision site (src/tallies/filter_mesh.cpp:40-70), energy filters the
+// pre-collision energy.
+__device__ void score_collision(const double* r, double E_last, double wgt_last, double mt, double ma,
+  const LevelCells& lc, int material)
+{
+  if (mt <= 0.0) return;
+  const double flux = wgt_last / mt;
+  for (int t = 0; t < dm.n_tally; ++t) {
+    const DTally& T = dm.tally[t];
+    if (T.estimator != 1) continue;
+    long long offs[MAXL];
+    int mesh_slot;
+    const int n_off = tally_offsets(T, E_last, lc, material, offs, mesh_slot);
+    long long mesh_add = 0;
+    if (mesh_slot >= 0 && n_off > 0) {
+      const DMesh& M = dm.mesh[dm.filt[T.filt[mesh_slot]].mesh];
+      int ijk[3] = {0, 0, 0};
+      bool in_mesh;
+      mesh_get_indices(M, r[0], r[1], r[2], ijk, in_mesh);
+      if (!in_mesh) continue;
+      mesh_add = static_cast<long long>(mesh_bin(M, ijk)) * T.stride[mesh_slot];
+    }
+    double* val = dm.value + T.value_off;
+    const int ns = T.nscore;
+    for (int o = 0; o < n_off; ++o) {
+      const long long index = offs[o] + mesh_add;
+      for (int s = 0; s < ns; ++s) {
+        const int sc = T.score[s];
+        const double score = sc == 0 ? flux : (sc == 1 ? mt * flux : ma * flux);
+        atomicAdd(val + index * ns + s, score);
+      }
+    }
+  }
 }
 
 // ------------------------------------------------------- weight windows
@@ -824,8 +909,14 @@ __device__ int ev_advance(long long s, EvStats& st)
     g.r[l][1] = g.r[l][1] + distance * g.u[1];
     g.r[l][2] = g.r[l][2] + distance * g.u[2];
   }
-  if (dm.n_tally > 0)
-    st.seg += score_tracklength(r0, g.r[0], g.u, db.E[s], wgt, distance, mt, db.macro_a[s], recip ? inv_u : nullptr);
+  if (dm.n_tally_tracklength > 0) {
+    LevelCells lc;
+#pragma unroll
+    for (int l = 0; l < MAXL; ++l) lc.c[l] = g.cell[l];
+    lc.n = g.n_coord;
+    st.seg += score_tracklength(r0, g.r[0], g.u, db.E[s], wgt, distance, mt, db.macro_a[s], lc, db.material[s],
+      recip ? inv_u : nullptr);
+  }
   wgt = db.wgt[s];
   if (distance == INFTY) {
     wgt = 0.0;
@@ -1040,6 +1131,7 @@ __device__ int ev_collision(long long s, EvStats& st)
   st.coll += 1;
   double E = db.E[s];
   double wgt = db.wgt[s];
+  const double E_in = E, wgt_in = wgt;
   unsigned long long seed = db.seed[s];
   int mat = db.material[s];
   double mt = db.macro_t[s];
@@ -1108,6 +1200,15 @@ __device__ int ev_collision(long long s, EvStats& st)
       }
       if (E < dm.energy_cutoff) wgt = 0.0;
     }
+  }
+  if (dm.n_tally_collision > 0 && chosen >= 0) {
+    const long long cap = db.cap;
+    LevelCells lc;
+    lc.n = db.n_coord[s];
+#pragma unroll
+    for (int l = 0; l < MAXL; ++l) lc.c[l] = l < lc.n ? db.cell[l * cap + s] : C_NONE;
+    const double r[3] = {db.rx[s], db.ry[s], db.rz[s]};
+    score_collision(r, E_in, wgt_in, mt, db.macro_a[s], lc, mat);
   }
   db.E[s] = E;
   db.wgt[s] = wgt;
@@ -1714,12 +1815,15 @@ static void build_model(GpuSim& G, const HModel& m, const GpuOptions& opt)
   }
   std::vector<DFilter> filts(m.filters.size());
   std::vector<double> ebins;
+  std::vector<int> fids;
   for (size_t k = 0; k < filts.size(); ++k) {
     filts[k].type = m.filters[k].type;
     filts[k].mesh = m.filters[k].mesh;
     filts[k].nbins = m.filters[k].nbins;
     filts[k].e_off = static_cast<int>(ebins.size());
     ebins.insert(ebins.end(), m.filters[k].bins.begin(), m.filters[k].bins.end());
+    filts[k].i_off = static_cast<int>(fids.size());
+    fids.insert(fids.end(), m.filters[k].ids.begin(), m.filters[k].ids.end());
   }
   std::vector<DTally> tallies(m.tallies.size());
   long long off = 0;
@@ -1727,6 +1831,7 @@ static void build_model(GpuSim& G, const HModel& m, const GpuOptions& opt)
   for (size_t k = 0; k < tallies.size(); ++k) {
     const HTally& t = m.tallies[k];
     tallies[k].value_off = off;
+    tallies[k].estimator = t.estimator;
     tallies[k].nfilt = static_cast<int>(t.filters.size());
     tallies[k].nscore = static_cast<int>(t.scores.size());
     if (tallies[k].nscore > 4) throw std::runtime_error("at most four scores per tally are supported");
@@ -1743,8 +1848,11 @@ static void build_model(GpuSim& G, const HModel& m, const GpuOptions& opt)
   d.mesh = dev_upload(meshes, own);
   d.filt = dev_upload(filts, own);
   d.ebins = dev_upload(ebins, own);
+  d.fids = dev_upload(fids, own);
   d.tally = dev_upload(tallies, own);
   d.n_tally = static_cast<int>(tallies.size());
+  d.n_tally_tracklength = d.n_tally_collision = 0;
+  for (const auto& t : tallies) (t.estimator == 1 ? d.n_tally_collision : d.n_tally_tracklength) += 1;
   G.d_value = dev_alloc<double>(off, own);
   G.d_sum = dev_alloc<double>(off, own);
   G.d_sumsq = dev_alloc<double>(off, own);

@@ -18,8 +18,9 @@ names and XML output:
 * independent sources: point or box space with optional domain constraints,
   isotropic or monodirectional angle, discrete or Maxwell energy
   (``openmc/source.py``, ``openmc/stats``);
-* regular meshes, mesh/energy/particle filters and flux/total/absorption
-  track-length tallies (``openmc/tallies.py``, ``openmc/filter.py``);
+* regular meshes, mesh/energy/particle/cell/material filters and
+  flux/total/absorption scores with track-length or collision estimators
+  (``openmc/tallies.py``, ``openmc/filter.py``);
 * weight windows and MAGIC weight-window generators
   (``openmc/weight_windows.py``).
 """
@@ -450,6 +451,32 @@ class ParticleFilter:
     def to_xml(self):
         el = ET.Element("filter", id=str(self.id), type="particle")
         ET.SubElement(el, "bins").text = " ".join(self.bins)
+        return el
+
+
+class CellFilter:
+    """Bins by cell at any coordinate level (openmc/filter.py CellFilter)."""
+
+    def __init__(self, bins, filter_id=None):
+        self.id = _next_id("filter", filter_id)
+        self.bins = list(bins)
+
+    def to_xml(self):
+        el = ET.Element("filter", id=str(self.id), type="cell")
+        ET.SubElement(el, "bins").text = " ".join(str(c.id if hasattr(c, "id") else int(c)) for c in self.bins)
+        return el
+
+
+class MaterialFilter:
+    """Bins by the particle's material (openmc/filter.py MaterialFilter)."""
+
+    def __init__(self, bins, filter_id=None):
+        self.id = _next_id("filter", filter_id)
+        self.bins = list(bins)
+
+    def to_xml(self):
+        el = ET.Element("filter", id=str(self.id), type="material")
+        ET.SubElement(el, "bins").text = " ".join(str(m.id if hasattr(m, "id") else int(m)) for m in self.bins)
         return el
 
 

@@ -327,7 +327,9 @@ def load_model(model_xml, cross_sections=None):
 
     # ---- tallies
     filt_type, filt_mesh, filt_nbins, filt_eoff, filt_e = [], [], [], [0], []
-    tal_id, tal_filt_off, tal_filt, tal_score_off, tal_score = [], [0], [], [0], []
+    filt_ioff, filt_ids = [0], []
+    tal_id, tal_filt_off, tal_filt, tal_score_off, tal_score, tal_est = [], [0], [], [0], [], []
+    cell_index = {int(c.get("id")): k for k, c in enumerate(cells)}
     if tal_el is not None:
         filters = tal_el.findall("filter")
         filt_index = {int(f.get("id")): k for k, f in enumerate(filters)}
@@ -348,9 +350,17 @@ def load_model(model_xml, cross_sections=None):
                 if bins.split() != ["neutron"]:
                     raise ValueError("only neutron particle filters are supported")
                 filt_type.append(2); filt_mesh.append(-1); filt_nbins.append(1)
+            elif t in ("cell", "material"):
+                # src/tallies/filter_cell.cpp, filter_material.cpp: bins are ids
+                index = cell_index if t == "cell" else mat_index
+                ids = [index[i] for i in _ints(bins)]
+                filt_type.append(3 if t == "cell" else 4); filt_mesh.append(-1)
+                filt_nbins.append(len(ids))
+                filt_ids.extend(ids)
             else:
                 raise ValueError(f"unsupported filter type {t}")
             filt_eoff.append(len(filt_e))
+            filt_ioff.append(len(filt_ids))
         for t in tal_el.findall("tally"):
             tal_id.append(int(t.get("id")))
             fl = _get(t, "filters")
@@ -358,8 +368,9 @@ def load_model(model_xml, cross_sections=None):
                 tal_filt.append(filt_index[fid])
             tal_filt_off.append(len(tal_filt))
             est = _get(t, "estimator", "tracklength")
-            if est != "tracklength":
-                raise ValueError("only track-length tallies are supported")
+            if est not in ("tracklength", "collision"):
+                raise ValueError("only track-length and collision estimators are supported")
+            tal_est.append(0 if est == "tracklength" else 1)
             for s in _get(t, "scores").split():
                 tal_score.append(SCORES[s])
             tal_score_off.append(len(tal_score))
@@ -449,8 +460,9 @@ def load_model(model_xml, cross_sections=None):
         "mesh_ur": D(mesh_ur), "mesh_width": D(mesh_width),
         "filt_type": I(filt_type), "filt_mesh": I(filt_mesh),
         "filt_nbins": I(filt_nbins), "filt_eoff": I(filt_eoff), "filt_e": D(filt_e),
+        "filt_ioff": I(filt_ioff), "filt_ids": I(filt_ids),
         "tal_id": I(tal_id), "tal_filt_off": I(tal_filt_off), "tal_filt": I(tal_filt),
-        "tal_score_off": I(tal_score_off), "tal_score": I(tal_score),
+        "tal_score_off": I(tal_score_off), "tal_score": I(tal_score), "tal_est": I(tal_est),
         "src_i": I([sp_type, an_type, en_type, dom_type]),
         "src_space": D(sp_par), "src_uref": D(an_ref), "src_energy": D(en_par),
         "src_strength": D([strength]), "src_dom_ids": I(dom_ids),

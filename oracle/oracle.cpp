@@ -309,14 +309,16 @@ struct Mesh {
 };
 
 struct Filter {
-  int type;  // 0 mesh 1 energy 2 particle
+  int type;  // 0 mesh 1 energy 2 particle 3 cell 4 material
   int mesh;
   int nbins;
   std::vector<double> bins;
+  std::vector<int> ids;  // cell / material indices of the bins (types 3, 4)
 };
 
 struct Tally {
   int id;
+  int estimator = 0;  // 0 track length, 1 collision
   std::vector<int> filters;
   std::vector<int> strides;
   std::vector<int> scores;  // 0 flux 1 total 2 absorption
@@ -453,6 +455,7 @@ struct Sim {
   std::vector<Mesh> meshes;
   std::vector<Filter> filters;
   std::vector<Tally> tallies;
+  int n_collision_tallies = 0;
   WeightWindows ww;
   // source
   int sp_type, an_type, en_type, dom_type;
@@ -1110,6 +1113,110 @@ void mesh_bins_crossed(const Mesh& m, const Pos& r0, const Pos& r1, const Pos& u
 
 // src/tallies/tally_scoring.cpp:2416-2541 with FilterBinIter :31-139 and
 // score_general_ce_nonanalog :578-1106 (flux, total, absorption scores)
+// Bins of a cell filter (src/tallies/filter_cell.cpp:48-58: every coordinate
+// level whose cell is in the filter) and of a material filter
+// (src/tallies/filter_material.cpp:47-55).
+void cell_material_bins(const Filter& F, const Particle& p, std::vector<int>& bins, std::vector<double>& w)
+{
+  if (F.type == 3) {
+    for (int i = 0; i < p.n_coord; ++i)
+      for (size_t b = 0; b < F.ids.size(); ++b)
+        if (F.ids[b] == p.coord[i].cell) {
+          bins.push_back(static_cast<int>(b));
+          w.push_back(1.0);
+        }
+  } else {
+    for (size_t b = 0; b < F.ids.size(); ++b)
+      if (F.ids[b] == p.material) {
+        bins.push_back(static_cast<int>(b));
+        w.push_back(1.0);
+      }
+  }
+}
+
+// Adds score x weight for every combination of the tally's filter bins
+// (src/tallies/tally_scoring.cpp:31-139 FilterBinIter, last filter fastest).
+void score_bins(Tally& tally, const std::vector<std::vector<int>>& fbins,
+  const std::vector<std::vector<double>>& fw, double flux, const Particle& p)
+{
+  int nf = static_cast<int>(tally.filters.size());
+  std::vector<int> ib(nf, 0);
+  int ns = static_cast<int>(tally.scores.size());
+  while (true) {
+    int64_t index = 0;
+    double weight = 1.;
+    for (int i = 0; i < nf; ++i) {
+      int f = tally.filters[i];
+      index += static_cast<int64_t>(fbins[f][ib[i]]) * tally.strides[i];
+      weight *= fw[f][ib[i]];
+    }
+    for (int s = 0; s < ns; ++s) {
+      double score;
+      switch (tally.scores[s]) {
+      case 0: score = flux; break;
+      case 1: score = p.macro_total * flux; break;
+      default: score = p.macro_absorption * flux; break;
+      }
+      double* slot = &tally.results[(index * ns + s) * 3];
+#pragma omp atomic
+      *slot += score * weight;
+    }
+    int i = nf - 1;
+    for (; i >= 0; --i) {
+      int f = tally.filters[i];
+      if (ib[i] < static_cast<int>(fbins[f].size()) - 1) {
+        ++ib[i];
+        break;
+      } else {
+        ib[i] = 0;
+      }
+    }
+    if (i < 0) break;
+  }
+}
+
+// src/tallies/tally_scoring.cpp:2543-2600 score_collision_tally: after the
+// collision, flux = wgt_last / Sigma_t with the pre-collision macroscopic
+// cross sections; mesh filters bin the collision site, energy filters the
+// pre-collision energy.
+void score_collision_tally(Sim& S, Particle& p)
+{
+  const double flux = p.wgt_last / p.macro_total;
+  std::vector<std::vector<int>> fbins(S.filters.size());
+  std::vector<std::vector<double>> fw(S.filters.size());
+  for (auto& tally : S.tallies) {
+    if (tally.estimator != 1) continue;
+    bool empty = false;
+    for (int f : tally.filters) {
+      fbins[f].clear();
+      fw[f].clear();
+      const Filter& F = S.filters[f];
+      if (F.type == 0) {
+        int ijk[3];
+        bool in_mesh;
+        mesh_get_indices(S.meshes[F.mesh], p.r(), ijk, in_mesh);
+        if (in_mesh) {
+          fbins[f].push_back(mesh_bin_from_indices(S.meshes[F.mesh], ijk));
+          fw[f].push_back(1.0);
+        }
+      } else if (F.type == 1) {
+        double E = p.E_last;
+        if (E >= F.bins.front() && E <= F.bins.back()) {
+          fbins[f].push_back(static_cast<int>(lower_bound_index(F.bins.data(), F.bins.data() + F.bins.size(), E)));
+          fw[f].push_back(1.0);
+        }
+      } else if (F.type == 2) {
+        fbins[f].push_back(0);
+        fw[f].push_back(1.0);
+      } else {
+        cell_material_bins(F, p, fbins[f], fw[f]);
+      }
+      if (fbins[f].empty()) empty = true;
+    }
+    if (!empty) score_bins(tally, fbins, fw, flux, p);
+  }
+}
+
 void score_tracklength_tally(Sim& S, Particle& p, double distance)
 {
   double flux = p.wgt * distance;
@@ -1117,12 +1224,15 @@ void score_tracklength_tally(Sim& S, Particle& p, double distance)
   std::vector<std::vector<double>> fw(S.filters.size());
   std::vector<bool> present(S.filters.size(), false);
   for (auto& tally : S.tallies) {
+    if (tally.estimator != 0) continue;
     bool empty = false;
     for (int f : tally.filters) {
       if (!present[f]) {
         const Filter& F = S.filters[f];
         if (F.type == 0) {
           mesh_bins_crossed(S.meshes[F.mesh], p.r_last, p.r(), p.u(), fbins[f], fw[f]);
+        } else if (F.type == 3 || F.type == 4) {
+          cell_material_bins(F, p, fbins[f], fw[f]);
         } else if (F.type == 1) {
           double E = p.E_last;
           if (E >= F.bins.front() && E <= F.bins.back()) {
@@ -1139,41 +1249,7 @@ void score_tracklength_tally(Sim& S, Particle& p, double distance)
     }
     if (empty)
       continue;
-    int nf = static_cast<int>(tally.filters.size());
-    std::vector<int> ib(nf, 0);
-    int ns = static_cast<int>(tally.scores.size());
-    while (true) {
-      int64_t index = 0;
-      double weight = 1.;
-      for (int i = 0; i < nf; ++i) {
-        int f = tally.filters[i];
-        index += static_cast<int64_t>(fbins[f][ib[i]]) * tally.strides[i];
-        weight *= fw[f][ib[i]];
-      }
-      for (int s = 0; s < ns; ++s) {
-        double score;
-        switch (tally.scores[s]) {
-        case 0: score = flux; break;
-        case 1: score = p.macro_total * flux; break;
-        default: score = p.macro_absorption * flux; break;
-        }
-        double* slot = &tally.results[(index * ns + s) * 3];
-#pragma omp atomic
-        *slot += score * weight;
-      }
-      // advance the last filter fastest
-      int i = nf - 1;
-      for (; i >= 0; --i) {
-        int f = tally.filters[i];
-        if (ib[i] < static_cast<int>(fbins[f].size()) - 1) {
-          ++ib[i];
-          break;
-        } else {
-          ib[i] = 0;
-        }
-      }
-      if (i < 0) break;
-    }
+    score_bins(tally, fbins, fw, flux, p);
   }
 }
 
@@ -1558,6 +1634,8 @@ void event_collide(Sim& S, Particle& p)
 {
   p.surface = SURFACE_NONE;
   collision(S, p);
+  // src/particle.cpp:361-364
+  if (S.n_collision_tallies > 0) score_collision_tally(S, p);
   p.material_last = C_NONE;
   for (int j = 0; j < p.n_coord - 1; ++j)
     p.coord[j + 1].u = p.coord[j].u;
@@ -1890,6 +1968,8 @@ void build(Sim& S, const Blob& B)
     f.nbins = static_cast<int>(B.I("filt_nbins")[k]);
     for (int64_t j = B.I("filt_eoff")[k]; j < B.I("filt_eoff")[k + 1]; ++j)
       f.bins.push_back(B.D("filt_e")[j]);
+    for (int64_t j = B.I("filt_ioff")[k]; j < B.I("filt_ioff")[k + 1]; ++j)
+      f.ids.push_back(static_cast<int>(B.I("filt_ids")[j]));
   }
   const auto& tid = B.I("tal_id");
   S.tallies.resize(tid.size());
@@ -1900,6 +1980,8 @@ void build(Sim& S, const Blob& B)
       t.filters.push_back(static_cast<int>(B.I("tal_filt")[j]));
     for (int64_t j = B.I("tal_score_off")[k]; j < B.I("tal_score_off")[k + 1]; ++j)
       t.scores.push_back(static_cast<int>(B.I("tal_score")[j]));
+    t.estimator = static_cast<int>(B.I("tal_est")[k]);
+    if (t.estimator == 1) ++S.n_collision_tallies;
     t.strides.assign(t.filters.size(), 1);
     int64_t stride = 1;
     for (int i = static_cast<int>(t.filters.size()) - 1; i >= 0; --i) {

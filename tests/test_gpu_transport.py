@@ -153,6 +153,23 @@ def test_lattice_history_parity(lattice):
     assert 0.0 <= lk <= 1.0
 
 
+def test_cell_material_filters_and_collision_estimator(built, tmp_path):
+    """Cell and material filters with track-length and collision estimators
+    (tally_scoring.cpp:2416-2600, filter_cell.cpp, filter_material.cpp)
+    match the oracle bin by bin."""
+    from openmc_gb300 import configs
+    m, path = configs.point_cube(tmp_path, particles=3000, batches=2, n_points=600,
+                                 mesh_dim=(4, 4, 4), n_ebins=5, estimator_tallies=True)
+    xml = m.export_to_model_xml(path)
+    g = run_gpu(path)
+    o = run_oracle(xml)
+    assert len(g["tallies"]) == 7
+    assert_tallies_close(g["tallies"], o["tallies"])
+    for k in range(1, 7):
+        r, n = g["tallies"][k]
+        assert n == 2 and r[..., 1].sum() > 0
+
+
 def test_lattice_history_based_parity(lattice):
     """settings.event_based = False runs the history-based kernel (one thread
     per history, src/simulation.cpp:804-831); histories and tallies match the

@@ -98,3 +98,38 @@ def test_xsbench_oracle_matches_numpy():
             f = (E - g[i]) / (g[i + 1] - g[i])
             tot += d.mat_dens[j] * ((1 - f) * d.xs[n, i] + f * d.xs[n, i + 1])
         assert np.allclose(out[k], tot, rtol=1e-12)
+
+
+def test_oracle_estimators_agree(tmp_path):
+    """Track-length and collision estimates of the same cell, material and
+    mesh fluxes agree within statistics (the reference's estimator-agreement
+    check, tests/unit_tests/test_filter_mesh.py:10-61)."""
+    import numpy as np
+    import oracle
+    from openmc_gb300 import configs
+    m, path = configs.point_cube(tmp_path, particles=4000, batches=8, n_points=600,
+                                 mesh_dim=(4, 4, 4), n_ebins=5, estimator_tallies=True)
+    xml = m.export_to_model_xml(path)
+    o = oracle.Oracle(xml)
+    o.run(threads=4)
+    n = 8
+
+    def mean_std(k):
+        r = o.tally(k)
+        mu = r[:, 1] / n
+        sd = np.sqrt(np.maximum(r[:, 2] / n - mu * mu, 0) / (n - 1))
+        return mu, sd
+
+    for k_tl, k_col in ((1, 4), (2, 5), (3, 6)):
+        a, sa = mean_std(k_tl)
+        b, sb = mean_std(k_col)
+        ok = (sa > 0) & (sb > 0)
+        assert ok.sum() > 0
+        z = np.abs(a - b)[ok] / np.hypot(sa, sb)[ok]
+        assert (z > 4).sum() == 0, (k_tl, z.max())
+    # one material: its flux is the sum over the cells
+    a, _ = mean_std(2)
+    c, _ = mean_std(1)
+    tot_cells = c.reshape(3, 4, 3)[:, :, 0].sum()
+    # (up to tracks below the lowest energy group bound)
+    assert abs(a.reshape(-1, 2)[0, 0] - tot_cells) <= 1e-5 * tot_cells

@@ -263,17 +263,28 @@ __device__ __forceinline__ double uniform_distribution(double a, double b, unsig
 }
 
 // src/math_functions.cpp:763-792 (phi sampled)
-__device__ inline void rotate_angle(double& ux, double& uy, double& uz, double mu, unsigned long long& s)
+// recip: divide by multiplying with the reciprocal (FP32-table mode; FP64
+// products rounded twice instead of FP64 quotients).  sin and cos of the
+// sampled angle come from one sincos call (the device's own functions in
+// either form).
+__device__ inline void rotate_angle(double& ux, double& uy, double& uz, double mu, unsigned long long& s,
+  bool recip = false)
 {
   double phi_ = 2.0 * PI * prn(s);
-  double sinphi = sin(phi_);
-  double cosphi = cos(phi_);
+  double sinphi, cosphi;
+  sincos(phi_, &sinphi, &cosphi);
   double a = sqrt(fmax(0., 1. - mu * mu));
   double b = sqrt(fmax(0., 1. - uz * uz));
   double x = ux, y = uy, z = uz;
   if (b > 1e-10) {
-    ux = mu * x + a * (x * z * cosphi - y * sinphi) / b;
-    uy = mu * y + a * (y * z * cosphi + x * sinphi) / b;
+    if (recip) {
+      const double ib = 1.0 / b;
+      ux = mu * x + a * (x * z * cosphi - y * sinphi) * ib;
+      uy = mu * y + a * (y * z * cosphi + x * sinphi) * ib;
+    } else {
+      ux = mu * x + a * (x * z * cosphi - y * sinphi) / b;
+      uy = mu * y + a * (y * z * cosphi + x * sinphi) / b;
+    }
     uz = mu * z - a * b * cosphi;
   } else {
     b = sqrt(1. - y * y);

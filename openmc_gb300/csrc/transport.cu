@@ -1094,7 +1094,7 @@ __device__ void sample_cxs_target_velocity(double awr, double E, const double* u
   }
   double vt = sqrt(beta_vt_sq * kT / awr);
   double x = u[0], y = u[1], z = u[2];
-  rotate_angle(x, y, z, mu, seed);
+  rotate_angle(x, y, z, mu, seed, dm.xs_fp32 != 0);
   vt_out[0] = vt * x;
   vt_out[1] = vt * y;
   vt_out[2] = vt * z;
@@ -1109,20 +1109,39 @@ __device__ void elastic_scatter(int nuc, double& E, double* u, unsigned long lon
   double vn[3] = {vel * u[0], vel * u[1], vel * u[2]};
   double vt[3] = {0.0, 0.0, 0.0};
   if (!(E >= 400.0 * kT && awr > 1.0)) sample_cxs_target_velocity(awr, E, u, kT, seed, vt);
+  // FP32-table mode: the quotients by (awr + 1) and by the speeds become
+  // products with FP64 reciprocals (double rounding instead of one)
+  const bool recip = dm.xs_fp32 != 0;
   double vcm[3];
-  for (int k = 0; k < 3; ++k) vcm[k] = (vn[k] + awr * vt[k]) / (awr + 1.0);
+  if (recip) {
+    const double iw = 1.0 / (awr + 1.0);
+    for (int k = 0; k < 3; ++k) vcm[k] = (vn[k] + awr * vt[k]) * iw;
+  } else {
+    for (int k = 0; k < 3; ++k) vcm[k] = (vn[k] + awr * vt[k]) / (awr + 1.0);
+  }
   for (int k = 0; k < 3; ++k) vn[k] = vn[k] - vcm[k];
   vel = sqrt(vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2]);
   double mu_cm = uniform_distribution(-1., 1., seed);
-  double ucm[3] = {vn[0] / vel, vn[1] / vel, vn[2] / vel};
-  rotate_angle(ucm[0], ucm[1], ucm[2], mu_cm, seed);
+  double ucm[3];
+  if (recip) {
+    const double iv = 1.0 / vel;
+    ucm[0] = vn[0] * iv; ucm[1] = vn[1] * iv; ucm[2] = vn[2] * iv;
+  } else {
+    ucm[0] = vn[0] / vel; ucm[1] = vn[1] / vel; ucm[2] = vn[2] / vel;
+  }
+  rotate_angle(ucm[0], ucm[1], ucm[2], mu_cm, seed, recip);
   for (int k = 0; k < 3; ++k) vn[k] = vel * ucm[k];
   for (int k = 0; k < 3; ++k) vn[k] = vn[k] + vcm[k];
   E = vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2];
   vel = sqrt(E);
-  u[0] = vn[0] / vel;
-  u[1] = vn[1] / vel;
-  u[2] = vn[2] / vel;
+  if (recip) {
+    const double iv = 1.0 / vel;
+    u[0] = vn[0] * iv; u[1] = vn[1] * iv; u[2] = vn[2] * iv;
+  } else {
+    u[0] = vn[0] / vel;
+    u[1] = vn[1] / vel;
+    u[2] = vn[2] / vel;
+  }
 }
 
 // src/particle.cpp:331-415 + src/physics.cpp:43-168, 494-518, 638-752

@@ -3,12 +3,14 @@
 // same names, argument meanings, return codes and exported globals, so that
 // openmc.lib-style ctypes bindings work unchanged.
 #include <algorithm>
+#include <charconv>
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
 #include <limits>
 #include <memory>
 #include <stdexcept>
@@ -436,6 +438,101 @@ int openmc_next_batch(int* status)
   }
 }
 
+namespace {
+
+// Shortest round-trip decimal form of a double, as the reference's fmt "{}".
+std::string shortest(double v)
+{
+  char buf[64];
+  auto r = std::to_chars(buf, buf + sizeof(buf), v);
+  return std::string(buf, r.ptr);
+}
+
+// " ====...>     TEXT     <====...", src/output.cpp:103-125
+std::string header_line(const std::string& msg)
+{
+  const int len = static_cast<int>(msg.size());
+  const int n_prefix = (63 - len) / 2;
+  const int n_suffix = n_prefix + ((len % 2) == 0 ? 1 : 0);
+  std::string upper(msg);
+  std::transform(upper.begin(), upper.end(), upper.begin(), [](unsigned char c) { return std::toupper(c); });
+  return " " + std::string(std::max(n_prefix, 0), '=') + ">     " + upper + "     <" +
+         std::string(std::max(n_suffix, 0), '=');
+}
+
+std::string filter_label(const HModel& m, const HFilter& f, int bin)
+{
+  switch (f.type) {
+  case FILTER_MESH: {
+    // src/mesh.cpp:604-615 bin_label, x index fastest, 1-based
+    const HMesh& mesh = m.meshes[f.mesh];
+    int ijk[3] = {0, 0, 0};
+    int rem = bin;
+    for (int i = 0; i < mesh.ndim; ++i) {
+      ijk[i] = rem % mesh.shape[i] + 1;
+      rem /= mesh.shape[i];
+    }
+    if (mesh.ndim > 2) return "Mesh Index (" + std::to_string(ijk[0]) + ", " + std::to_string(ijk[1]) + ", " +
+                              std::to_string(ijk[2]) + ")";
+    if (mesh.ndim > 1) return "Mesh Index (" + std::to_string(ijk[0]) + ", " + std::to_string(ijk[1]) + ")";
+    return "Mesh Index (" + std::to_string(ijk[0]) + ")";
+  }
+  case FILTER_ENERGY:  // src/tallies/filter_energy.cpp:89-92
+    return "Incoming Energy [" + shortest(f.bins[bin]) + ", " + shortest(f.bins[bin + 1]) + ")";
+  case FILTER_PARTICLE:  // src/tallies/filter_particle.cpp:55-59
+    return "Particle: neutron";
+  case FILTER_CELL:  // src/tallies/filter_cell.cpp:69-72
+    return "Cell " + std::to_string(m.cells[f.ids[bin]].id);
+  default:  // src/tallies/filter_material.cpp
+    return "Material " + std::to_string(m.materials[f.ids[bin]].id);
+  }
+}
+
+// src/output.cpp:605-720 write_tallies: every filter-bin combination (last
+// filter fastest), a filter's label where its bin starts, "Total Material",
+// then "score  mean +/- standard deviation of the mean" (t-value 1).
+void write_tallies(const HModel& m)
+{
+  if (m.tallies.empty() || !m.output_tallies) return;
+  std::string dir = m.path_output.empty() ? std::string(".") : m.path_output;
+  std::ofstream out(dir + "/tallies.out", std::ios::out | std::ios::trunc);
+  if (!out) return;
+  static const char* score_name[] = {"Flux", "Total Reaction Rate", "Absorption Rate"};
+  char line[256];
+  for (const auto& t : m.tallies) {
+    std::string title = "TALLY " + std::to_string(t.id);
+    if (!t.name.empty()) title += ": " + t.name;
+    out << header_line(title) << "\n\n";
+    const int nf = static_cast<int>(t.filters.size());
+    const int ns = static_cast<int>(t.scores.size());
+    const int n = t.n_realizations;
+    for (int64_t index = 0; index < t.n_filter_bins; ++index) {
+      int indent = 0;
+      for (int i = 0; i < nf; ++i) {
+        if (index % t.strides[i] == 0) {
+          const HFilter& f = m.filters[t.filters[i]];
+          const int bin = static_cast<int>((index / t.strides[i]) % f.nbins);
+          out << std::string(indent + 1, ' ') << filter_label(m, f, bin) << "\n";
+        }
+        indent += 2;
+      }
+      out << std::string(indent + 1, ' ') << "Total Material\n";
+      indent += 2;
+      for (int s = 0; s < ns; ++s) {
+        const double* r = &t.results[(index * ns + s) * 3];
+        double mean = n > 0 ? r[1] / n : 0.0;
+        double sd = 0.0;
+        if (n > 1) sd = std::sqrt(std::max((r[2] / n - mean * mean) / (n - 1), 0.0));
+        std::snprintf(line, sizeof(line), "%*s%-36s %.6g +/- %.6g\n", indent + 1, "", score_name[t.scores[s]],
+          mean, sd);
+        out << line;
+      }
+    }
+  }
+}
+
+}  // namespace
+
 int openmc_simulation_finalize()
 {
   State& s = S();
@@ -445,6 +542,7 @@ int openmc_simulation_finalize()
     gpu_destroy(s.gpu);
     s.gpu = nullptr;
     initialized = false;
+    write_tallies(s.model);  // src/simulation.cpp:183-185
     return 0;
   } catch (const std::exception& e) {
     return fail(OPENMC_E_UNASSIGNED, e.what());

@@ -457,6 +457,11 @@ void load_model(const std::string& path_in, HModel& m)
   m.n_log_bins = std::stoi(set->value_or("log_grid_bins", "8000"));
   if (m.n_log_bins < 1) throw std::runtime_error("Number of bins for logarithmic grid must be greater than zero.");
   m.event_based = XmlNode::trim(set->value_or("event_based", "false")) == "true";
+  if (const XmlNode* out = set->child("output")) {
+    if (out->has("tallies")) m.output_tallies = XmlNode::trim(out->value("tallies")) == "true";
+    if (out->has("path")) m.path_output = XmlNode::trim(out->value("path"));
+  }
+  if (m.path_output.empty()) m.path_output = dir;
   if (set->has("max_particles_in_flight")) m.max_particles_in_flight = std::stoll(set->value("max_particles_in_flight"));
   if (set->has("max_history_splits")) m.max_history_splits = std::stoll(set->value("max_history_splits"));
   if (set->has("max_particle_events")) m.max_particle_events = std::stoi(set->value("max_particle_events"));
@@ -608,6 +613,7 @@ void load_model(const std::string& path_in, HModel& m)
     for (const XmlNode* te : tal->all("tally")) {
       HTally t;
       t.id = std::stoi(te->value("id"));
+      t.name = te->value_or("name", "");
       if (te->has("filters"))
         for (auto fid : split_ints(te->value("filters"))) {
           if (!filt_index.count(static_cast<int>(fid))) throw std::runtime_error("tally " + std::to_string(t.id) + ": unknown filter");

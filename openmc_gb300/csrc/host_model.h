@@ -59,6 +59,7 @@ struct HFilter {
 
 struct HTally {
   int id;
+  std::string name;
   int estimator = EST_TRACKLENGTH;
   std::vector<int> filters, strides, scores;
   int64_t n_filter_bins = 1;
@@ -111,6 +112,9 @@ struct HWWGenerator {
 };
 
 struct HModel {
+  // output (src/settings.cpp: <output><tallies>, <output><path>)
+  bool output_tallies = true;
+  std::string path_output;  // directory for tallies.out (default: the input's directory)
   // settings (src/settings.cpp)
   int64_t n_particles = 0;
   int n_batches = 0, n_inactive = 0;

@@ -67,3 +67,27 @@ def test_one_row_network(built):
     assert np.linalg.norm(g - g_ref) <= 2e-2 * np.linalg.norm(g_ref)
     assert np.isfinite(net.predict(x)).all()
     net.close()
+
+
+def test_tallies_out_written(built, tmp_path):
+    """simulation_finalize writes tallies.out next to the input in the
+    reference's layout (src/output.cpp:605-720)."""
+    from openmc_gb300 import configs, lib
+    m, path = configs.point_cube(tmp_path, particles=2000, batches=3, n_points=400, mesh_dim=(2, 2, 2), n_ebins=3)
+    m.export_to_model_xml(path)
+    lib.init(directory=path)
+    try:
+        lib.run()
+        mean, std = lib.tally_mean_std(lib.tally_ids()[0])
+    finally:
+        lib.finalize()
+    text = (path / "tallies.out").read_text().splitlines()
+    title = f"TALLY {m.tallies[0].id}: MESH FLUX"
+    assert text[0].strip().startswith("=") and f">     {title}     <" in text[0]
+    assert text[2] == " Mesh Index (1, 1, 1)"
+    assert text[3].startswith("   Incoming Energy [")
+    assert text[4] == "     Total Material"
+    fields = text[5].split()
+    assert fields[0] == "Flux" and fields[2] == "+/-"
+    assert abs(float(fields[1]) - mean.ravel()[0]) <= 1e-5 * abs(mean.ravel()[0]) + 1e-300
+    assert abs(float(fields[3]) - std.ravel()[0]) <= 1e-5 * abs(std.ravel()[0]) + 1e-300

@@ -214,6 +214,7 @@ def run_gb300(args, barrier=lambda: None, rank=0):
         prof = lib.last_batch_detail()
         levels = 2
         lib.simulation_finalize()
+        fp32_tally = lib.tally_mean_std(tid)
     finally:
         lib.finalize()
     total_ms = sum(dev_ms)
@@ -261,11 +262,14 @@ def run_gb300(args, barrier=lambda: None, rank=0):
             lib.settings.xs_fp32 = 0
             lib.settings.particles_in_flight = args.in_flight
             lib.simulation_init()
-            lib.next_batch()
+            # five batches, so that the tally comparison has usable error bars
+            for _ in range(4):
+                lib.next_batch()
             flush_l2(flush)
             lib.next_batch()
             out["fp64_value"] = n / (lib.last_batch()["ms"] / 1000.0)
             lib.simulation_finalize()
+            out["fp32_vs_fp64"] = compare_tallies(fp32_tally, lib.tally_mean_std(lib.tally_ids()[0]))
         finally:
             lib.finalize()
         # the same batch through the history-based kernel (settings.event_based = False)
@@ -284,6 +288,22 @@ def run_gb300(args, barrier=lambda: None, rank=0):
             lib.settings.event_based = True
             lib.finalize()
     return out
+
+
+def compare_tallies(a, b):
+    """FP32-table tally (a) against the FP64-table tally (b), both
+    (mean, std of the mean): share of bins scored by both within 3 combined
+    sigma, the largest |z|, and the relative difference of the summed flux
+    with its combined sigma."""
+    ma, sa = (np.asarray(x, float).ravel() for x in a)
+    mb, sb = (np.asarray(x, float).ravel() for x in b)
+    both = (sa > 0) & (sb > 0)
+    z = np.abs(ma - mb)[both] / np.hypot(sa, sb)[both]
+    ta, tb = ma.sum(), mb.sum()
+    st = np.sqrt((sa ** 2).sum() + (sb ** 2).sum())
+    return {"bins_scored_by_both": int(both.sum()), "share_within_3_sigma": float((z <= 3).mean()),
+            "max_abs_z": float(z.max()), "total_rel_diff": float((ta - tb) / tb),
+            "total_z": float(abs(ta - tb) / st) if st > 0 else None}
 
 
 def xs_lookup_bench(fp32, n=17_000_000, reps=5):
@@ -316,13 +336,15 @@ def xs_lookup_bench(fp32, n=17_000_000, reps=5):
             k_ms.append(look_ms)
             tot_ms.append(sort_ms + look_ms)
     t.close()
+    head = do[:5 * 1_000_000].view(-1, 5).cpu().numpy()
     km, tm = statistics.median(k_ms), statistics.median(tot_ms)
     peak, kind = peaks()
     gbs = alg * n / (km * 1e-3) / 1e9
     return {"lookups_per_s": n / (km * 1e-3), "with_sort_lookups_per_s": n / (tm * 1e-3),
             "kernel_ms": km, "nuclides_per_lookup": nuc_per_lookup, "alg_bytes_per_lookup": alg,
             "GB/s": gbs, "frac_of_hbm_peak": gbs / peak,
-            "note": "tables (37 MB FP64) stay in the 129 MB L2; inputs/outputs stream from HBM"}
+            "note": "tables (37 MB FP64) stay in the 129 MB L2; inputs/outputs stream from HBM",
+            "_head": head}
 
 
 def cpu_baseline(path, sample, threads=None, mode=1):
@@ -383,7 +405,12 @@ def main():
         barrier = dist.barrier
     r = run_gb300(args, barrier=barrier, rank=rank)
     if not args.no_xs_bench and rank == 0:
-        r["xs_lookup"] = {"fp64": xs_lookup_bench(False), "fp32": xs_lookup_bench(True)}
+        x64, x32 = xs_lookup_bench(False), xs_lookup_bench(True)
+        h64, h32 = x64.pop("_head"), x32.pop("_head")
+        rel = np.abs(h32 - h64) / np.maximum(np.abs(h64), 1e-300)
+        x32["max_rel_err_vs_fp64"] = {c: float(rel[:, k].max()) for k, c in
+                                      enumerate(("total", "elastic", "absorption", "aux1", "aux2"))}
+        r["xs_lookup"] = {"fp64": x64, "fp32": x32}
     if world > 1:
         import torch.distributed as dist
         # whole-job throughput over the slowest rank (device time and e2e wall time)
@@ -423,6 +450,7 @@ def main():
         "cpu_baseline": cpu,
         "kernel_ms_profiled_batch": r["kernel_ms"],
         "fp64_xs_particles_per_s": r.get("fp64_value"),
+        "fp32_vs_fp64_tally": r.get("fp32_vs_fp64"),
         "history_based_gpu_particles_per_s": r.get("history_value"),
         "events_per_step": r["detail"]["queue"]["xs_events"] + r["detail"]["tail"]["xs_events"],
         "iterations_per_step": r["iterations"],

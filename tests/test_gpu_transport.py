@@ -153,6 +153,21 @@ def test_lattice_history_parity(lattice):
     assert 0.0 <= lk <= 1.0
 
 
+def test_lattice_first_10k_histories(built, tmp_path):
+    """FP64 tables: the first 10^4 histories of a lattice batch have the
+    oracle's event kinds, cells, materials, surfaces / nuclides, grid-index
+    hashes, coordinate depths and event counts."""
+    from openmc_gb300 import configs
+    m, path = configs.lattice17(tmp_path, particles=10_000, batches=1, n_points=2000,
+                                mesh_dim=(17, 17, 5), n_ebins=10)
+    xml = m.export_to_model_xml(path)
+    g = run_gpu(path, n_trace=10_000, cap=256)
+    o = run_oracle(xml, n_trace=10_000, cap=256)
+    bad = trace_mismatches(g["trace"], o["trace"], 256)
+    assert not bad, f"{len(bad)} of 10000 histories differ, first: {bad[:5]}"
+    assert_tallies_close(g["tallies"], o["tallies"])
+
+
 def test_cell_material_filters_and_collision_estimator(built, tmp_path):
     """Cell and material filters with track-length and collision estimators
     (tally_scoring.cpp:2416-2600, filter_cell.cpp, filter_material.cpp)

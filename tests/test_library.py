@@ -114,3 +114,25 @@ def test_no_cpu_fallback(built, tmp_path):
             lib.simulation_init()
     finally:
         lib.finalize()
+
+
+@pytest.mark.parametrize("case", ["analog", "unknown_cell", "two_cell_filters"])
+def test_unsupported_tallies_rejected(built, tmp_path, case):
+    """Tally options outside the GPU path fail at openmc_init with an
+    OPENMC_E_INVALID_ARGUMENT message, as the reference's input checks do."""
+    from openmc_gb300 import configs, lib
+    from openmc_gb300 import model as om
+    m, d = configs.point_cube(tmp_path, particles=100, batches=2, n_points=300, mesh_dim=(2, 2, 2), n_ebins=2)
+    t = om.Tally(name="bad")
+    cells = m.geometry.root_universe.cells
+    if case == "analog":
+        t.estimator = "analog"
+    elif case == "unknown_cell":
+        t.filters = [om.CellFilter([987654])]
+    else:
+        t.filters = [om.CellFilter(cells[:1]), om.CellFilter(cells[1:])]
+    m.tallies.append(t)
+    m.export_to_model_xml(d)
+    with pytest.raises(lib.InvalidArgumentError):
+        lib.init(directory=d)
+    lib.finalize()

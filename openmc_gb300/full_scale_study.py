@@ -65,9 +65,12 @@ def run(directory, particles=100_000_000, batches=3, pilot_particles=10_000_000,
                        "flux 100x100x60 mesh x 50 E bins (3e7 bins)",
            "batches": batches, "particles_per_batch": particles}
     lib.init(directory=path)
-    saved = (lib.settings.xs_fp32, lib.settings.split_to_slots)
+    saved = (lib.settings.xs_fp32, lib.settings.split_to_slots, lib.settings.secondary_capacity)
     try:
         lib.settings.split_to_slots = 1
+        if learned_particles:
+            # uniform particle density over the shells: give the split ring room
+            lib.settings.secondary_capacity = 1 << 26
         if learned_particles:
             pilot = _run(pilot_particles, pilot_batches, False, True, "pilot")
             mean, std = pilot["tallies"][2][0][:, 0], pilot["tallies"][2][1][:, 0]
@@ -84,7 +87,7 @@ def run(directory, particles=100_000_000, batches=3, pilot_particles=10_000_000,
             first_name = "plain_fp32"
         plain = _run(particles, batches, False, False, "plain fp64")
     finally:
-        lib.settings.xs_fp32, lib.settings.split_to_slots = saved
+        lib.settings.xs_fp32, lib.settings.split_to_slots, lib.settings.secondary_capacity = saved
         lib.finalize()
     learned = first
     out["compared"] = f"{first_name} against plain_fp64"

@@ -68,3 +68,55 @@ def test_learned_windows_raise_figure_of_merit(built, tmp_path):
     # unbiased: back-face means agree within 3.5 combined sigma
     assert out["z_learned_plain"] < 3.5, out
     assert out["z_magic_plain"] < 3.5, out
+
+
+@pytest.mark.parametrize("value", ["mean", "rel_err"])
+def test_magic_update_matches_restatement(built, tmp_path, value):
+    """openmc_weight_windows_update_magic against a numpy restatement of
+    WeightWindows::update_weights (src/weight_windows.cpp:502-755) applied to
+    the same tally results: per-group normalisation by twice the maximum of
+    flux / volume, -1 where unscored or noisier than the threshold, upper =
+    ratio x lower."""
+    from openmc_gb300 import configs, lib
+    groups = [0.0, 1.0, 1.0e4, 2.0e7 * 1.000001]
+    m, path = configs.shield(tmp_path, particles=20_000, batches=3, n_points=1500, length=60.0,
+                             mesh_dim=(12, 2, 2), energy_groups=groups, tally_mesh_windows=True,
+                             density_scale=0.1)
+    m.export_to_model_xml(path)
+    threshold, ratio = 0.02, 5.0  # low enough that the deeper bins are dropped
+    lib.init(directory=path)
+    try:
+        lib.settings.split_to_slots = 0
+        lib.settings.weight_windows_on = False
+        lib.simulation_init()
+        for _ in range(3):
+            lib.next_batch()
+        lib.simulation_finalize()
+        tid = lib.tally_ids()[0]
+        res = lib.tally_results(tid).copy()       # [mesh * group][score][3]
+        n = lib.tally_n_realizations(tid)
+        ww = lib.WeightWindows(0)
+        ww.update_magic(lib.tally_index(tid), value, threshold, ratio)
+        lower, upper = ww.bounds
+    finally:
+        lib.finalize()
+    n_mesh, n_e = 12 * 2 * 2, len(groups) - 1
+    s = res[:, 0, 1].reshape(n_mesh, n_e).T         # [e][m]
+    s2 = res[:, 0, 2].reshape(n_mesh, n_e).T
+    mean = s / n
+    with np.errstate(divide="ignore", invalid="ignore"):
+        rel = np.where(s > 0, np.sqrt((s2 / n - mean * mean) / (n - 1)) / mean, np.inf)
+        b = 1.0 / rel if value == "rel_err" else mean.copy()
+    vol = (60.0 / 12) * (50.0 / 2) * (50.0 / 2)
+    b = b / vol
+    for e in range(n_e):
+        mx = b[e].max()
+        if mx > 0:
+            b[e] = b[e] * (1.0 / (2.0 * mx))
+    b = np.where(s <= 0, -1.0, np.where(rel > threshold, -1.0, b))
+    assert (b > 0).sum() > 0 and (b < 0).sum() > 0
+    # 1 / rel_err goes through sum_sq / n - mean^2, whose cancellation turns
+    # the host compiler's freedom to fuse multiply-adds into ~1e-11 relative
+    tol = 1e-14 if value == "mean" else 1e-10
+    np.testing.assert_allclose(lower, b.ravel(), rtol=tol, atol=0)
+    np.testing.assert_allclose(upper, ratio * b.ravel(), rtol=tol, atol=0)

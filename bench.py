@@ -136,8 +136,8 @@ def peaks():
 # OPENMC_GB300_LAUNCH_LOG counts (profiles/advance_surface_collision_lattice17_2M.md;
 # the unfused kernels' ratios come from the same capture of the earlier build).
 # Traffic per launch scales with the events a launch processes.
-TRAFFIC_PER_ALGORITHMIC_BYTE = {"xs+advance+surface": 0.749, "xs+advance": 1.376, "surface": 1.406,
-                                "collision": 1.275}
+TRAFFIC_PER_ALGORITHMIC_BYTE = {"xs+advance+surface": 0.802, "xs+advance": 1.376, "surface": 1.406,
+                                "collision": 1.276}
 
 
 def algorithmic_bytes(detail, levels, fp32):

@@ -46,7 +46,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--particles", type=int, default=10_000_000)
-    ap.add_argument("--in-flight", type=int, default=1 << 20, help="particle slots held on the device")
+    ap.add_argument("--in-flight", type=int, default=0,
+                    help="particle slots held on the device (0: the library's default, 2^19)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-table extra measurement")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=0,

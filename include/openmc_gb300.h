@@ -115,7 +115,8 @@ extern int openmc_gb300_profile_next;
  * the remaining histories run to completion one thread each (-1: default) */
 extern int64_t openmc_gb300_tail_threshold;
 /* entries of the device pool of banked secondaries (split particles); 0: automatic
- * (with weight windows max(32 x slots, 2^22), else 1024); each entry is 72 bytes */
+ * (with weight windows max(64 x slots, 2^22), else 1024); 72 bytes per entry, 112 in
+ * split-to-slots mode */
 extern int64_t openmc_gb300_secondary_capacity;
 /* 1: particles split by weight windows wait in a device ring and start in free
  * slots with their own tracking seeds (a hash of the parent's seed), so that a

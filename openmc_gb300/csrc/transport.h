@@ -12,7 +12,7 @@ constexpr int ERR_LOST = 1, ERR_SECONDARY_OVERFLOW = 2, ERR_NO_NUCLIDE = 4,
 struct GpuSim;
 
 struct GpuOptions {
-  long long in_flight = 0;      // particle slots in HBM (0: min(n_particles, 2^21))
+  long long in_flight = 0;      // particle slots in HBM (0: min(n_particles, 2^19))
   long long secondary_cap = 0;  // secondary-site pool entries (0: automatic)
   bool xs_fp32 = false;         // FP32 cross-section tables and interpolation
   bool sort = true;             // sort the cross-section queue by (material, energy)

@@ -139,7 +139,6 @@ struct DBank {
   int *n_coord, *cell_last0, *cell_born;
   int *surface, *material, *material_last;
   double *macro_t, *macro_a;
-  double *bdist, *dcoll;
   int *bsurf, *blevel, *btrans;
   int *n_event, *n_collision, *n_split;
   int* sec_top;   // top of the slot's LIFO chain of banked secondaries

@@ -875,6 +875,12 @@ __device__ __forceinline__ double collision_distance(double xi, double mt)
   return static_cast<double>(-lg / static_cast<float>(mt));
 }
 
+__device__ int ev_surface_g(long long s, EvStats& st, Geo& g, double wgt, int bsurf, int trans, int blevel);
+
+// with_surf: a particle that reaches the boundary crosses it right away from
+// the registers (the surface event always follows such an advance), instead
+// of storing its state for a surface pass to reload.
+template<bool with_surf>
 __device__ int ev_advance(long long s, EvStats& st)
 {
   double wgt = db.wgt[s];
@@ -922,6 +928,14 @@ __device__ int ev_advance(long long s, EvStats& st)
     wgt = 0.0;
     db.wgt[s] = 0.0;
   }
+  db.seed[s] = seed;
+  long long pid = db.id[s];
+  if (traced(pid)) {
+    TraceRec* rec = trace_slot(pid);
+    if (rec) rec->dist = distance;
+  }
+  const bool cross = wgt != 0.0 && dcoll > bd;
+  if (with_surf && cross) return ev_surface_g(s, st, g, wgt, bs, bt, bl);
   const long long cap = db.cap;
 #pragma unroll
   for (int l = 0; l < MAXL; ++l) {
@@ -931,18 +945,13 @@ __device__ int ev_advance(long long s, EvStats& st)
     db.ry[k] = g.r[l][1];
     db.rz[k] = g.r[l][2];
   }
-  db.seed[s] = seed;
-  db.bdist[s] = bd;
-  db.bsurf[s] = bs;
-  db.blevel[s] = bl;
-  db.btrans[s] = bt;
-  db.dcoll[s] = dcoll;
-  long long pid = db.id[s];
-  if (traced(pid)) {
-    TraceRec* rec = trace_slot(pid);
-    if (rec) rec->dist = distance;
+  if (cross) {
+    db.bsurf[s] = bs;
+    db.blevel[s] = bl;
+    db.btrans[s] = bt;
+    return NEXT_SURF;
   }
-  if (wgt != 0.0) return dcoll > bd ? NEXT_SURF : NEXT_COLL;
+  if (wgt != 0.0) return NEXT_COLL;
   return revive_or_free(s, wgt) ? NEXT_XS : NEXT_DEAD;
 }
 
@@ -981,17 +990,15 @@ __device__ void cross_lattice(Geo& g, long long s, int trans)
 }
 
 // src/particle.cpp:288-329, 549-710 event_cross_surface (+ revive)
-__device__ int ev_surface(long long s, EvStats& st)
+// The crossing itself on a particle state already held in registers (g, at
+// the boundary), with the boundary the advance found: signed surface bsurf,
+// lattice translation trans and coordinate level blevel.
+__device__ int ev_surface_g(long long s, EvStats& st, Geo& g, double wgt, int bsurf, int trans, int blevel)
 {
   st.surf += 1;
-  Geo g;
-  geo_load(g, s);
-  double wgt = db.wgt[s];
-  int bsurf = db.bsurf[s];
-  int trans = db.btrans[s];
   db.cell_last0[s] = g.cell[0];
   g.surface = bsurf;
-  g.n_coord = db.blevel[s];
+  g.n_coord = blevel;
   bool lost_outer = false;
   if (trans != 13) {
     cross_lattice(g, s, trans);
@@ -1064,6 +1071,13 @@ __device__ int ev_surface(long long s, EvStats& st)
     dq.trace_n[pid - dq.trace_first] += 1;
   }
   return revive_or_free(s, wgt) ? NEXT_XS : NEXT_DEAD;
+}
+
+__device__ int ev_surface(long long s, EvStats& st)
+{
+  Geo g;
+  geo_load(g, s);
+  return ev_surface_g(s, st, g, db.wgt[s], db.bsurf[s], db.btrans[s], db.blevel[s]);
 }
 
 // src/physics.cpp:990-1041
@@ -1307,8 +1321,7 @@ __global__ void __launch_bounds__(256, OMC_MINB_ADV) k_advance()
     long long s = valid ? dq.q_in[i] : 0;
     EvStats st {};
     if (with_xs && valid) ev_xs(s, st);
-    int nx = valid ? ev_advance(s, st) : NEXT_DEAD;
-    if (with_surf && nx == NEXT_SURF) nx = ev_surface(s, st);
+    int nx = valid ? ev_advance<with_surf>(s, st) : NEXT_DEAD;
     if (!with_surf) warp_append(dq.q_surf, &dq.cnt->n_surf, static_cast<int>(s), nx == NEXT_SURF);
     warp_append(dq.q_coll, &dq.cnt->n_coll, static_cast<int>(s), nx == NEXT_COLL);
     warp_append(dq.q_tmp, &dq.cnt->n_next, static_cast<int>(s), nx == NEXT_XS);
@@ -1366,9 +1379,8 @@ __global__ void __launch_bounds__(128, 2) k_tail(int max_events)
     int nx = valid ? NEXT_XS : NEXT_DEAD;
     for (int e = 0; e < max_events && nx == NEXT_XS; ++e) {
       ev_xs(s, st);
-      nx = ev_advance(s, st);
-      if (nx == NEXT_SURF) nx = ev_surface(s, st);
-      else if (nx == NEXT_COLL) nx = ev_collision(s, st);
+      nx = ev_advance<true>(s, st);
+      if (nx == NEXT_COLL) nx = ev_collision(s, st);
     }
     __syncwarp();
     warp_append(dq.q_tmp, &dq.cnt->n_next, static_cast<int>(s), nx == NEXT_XS);
@@ -1397,9 +1409,8 @@ __global__ void __launch_bounds__(128, 2) k_history()
       // every particle dies within max_events events (revive_or_free)
       for (long long e = 0; nx == NEXT_XS && e < (1LL << 40); ++e) {
         ev_xs(s, st);
-        nx = ev_advance(s, st);
-        if (nx == NEXT_SURF) nx = ev_surface(s, st);
-        else if (nx == NEXT_COLL) nx = ev_collision(s, st);
+        nx = ev_advance<true>(s, st);
+        if (nx == NEXT_COLL) nx = ev_collision(s, st);
       }
     }
   }
@@ -1936,8 +1947,6 @@ static void build_bank(GpuSim& G, long long cap, long long sec_cap)
   b.material_last = dev_alloc<int>(cap, own);
   b.macro_t = dev_alloc<double>(cap, own);
   b.macro_a = dev_alloc<double>(cap, own);
-  b.bdist = dev_alloc<double>(cap, own);
-  b.dcoll = dev_alloc<double>(cap, own);
   b.bsurf = dev_alloc<int>(cap, own);
   b.blevel = dev_alloc<int>(cap, own);
   b.btrans = dev_alloc<int>(cap, own);

@@ -5,18 +5,25 @@
 // until every history of the batch has ended.
 //
 // Kernel <-> reference mapping
+//   k_source_bank sample_external_source src/source.cpp:355-415, 627-660 and
+//                 the particle seeds of initialize_history
+//                 src/simulation.cpp:573-616, for every history of the batch
 //   k_refill      process_init_events  src/event.cpp:62-71 + initialize_history
-//                 src/simulation.cpp:573-649 + sample_external_source
-//                 src/source.cpp:355-415, 627-660
+//                 src/simulation.cpp:573-649 (or a waiting split particle)
 //   k_xs          process_calculate_xs_events src/event.cpp:73-105 ->
 //                 Particle::event_calculate_xs src/particle.cpp:160-230
+//                 (by default inside k_advance)
 //   k_advance     process_advance_particle_events src/event.cpp:107-128 ->
 //                 Particle::event_advance src/particle.cpp:232-286 + track-length
-//                 tallies src/tallies/tally_scoring.cpp:2416-2541
+//                 tallies src/tallies/tally_scoring.cpp:2416-2541 (+ by default
+//                 the surface crossing, below)
 //   k_surface     process_surface_crossing_events src/event.cpp:130-147 ->
 //                 event_cross_surface src/particle.cpp:288-329 + revive
 //   k_collision   process_collision_events src/event.cpp:149-166 ->
-//                 event_collide src/particle.cpp:331-415 + revive
+//                 event_collide src/particle.cpp:331-415 + collision-estimator
+//                 tallies src/tallies/tally_scoring.cpp:2543-2600 + revive
+//   k_tail        the history-based loop for the last histories of a batch
+//   k_history     transport_history_based src/simulation.cpp:804-831
 //   k_accumulate  Tally::accumulate src/tallies/tally.cpp:821-880
 //
 // Queues replace SharedArray::thread_safe_append (include/openmc/

@@ -176,6 +176,30 @@ struct GemmArgs {
   int* error;
 };
 
+// Issues asynchronous 16-byte copies (cp.async, zero-filled past k_end) of
+// a tile of `nrows` rows x KC elements (row r of the source at
+// src + r * ld + k0) into shared memory in core-matrix order
+// [row/8][k/8][row%8][k%8]; the caller commits and waits for the group.
+__device__ __forceinline__ void stage_tile_async(__nv_bfloat16* dst, const __nv_bfloat16* src, int ld, int nrows,
+  int k0, int k_end)
+{
+  constexpr int groups = KC / 8;  // 8-element (16-byte) groups per row
+  for (int idx = threadIdx.x; idx < nrows * groups; idx += blockDim.x) {
+    const int r = idx / groups, g = idx % groups;
+    const int k = k0 + g * 8;
+    const bool in = k + 8 <= k_end;
+    const __nv_bfloat16* from = in ? src + static_cast<long long>(r) * ld + k : src;
+    __nv_bfloat16* out = dst + ((r / 8) * groups + g) * 64 + (r % 8) * 8;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(out)), "l"(from),
+                 "r"(in ? 16 : 0)
+                 : "memory");
+  }
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 // Copies a tile of `nrows` rows x KC elements (row r of the source at
 // src + r * ld + k0) into shared memory in core-matrix order
 // [row/8][k/8][row%8][k%8]; elements past k_end are zero.
@@ -246,18 +270,35 @@ __global__ void __launch_bounds__(128, 1) k_gemm(GemmArgs g)
   const int n_chunks = k_end > k_begin ? (k_end - k_begin + KC - 1) / KC : 0;
   const uint32_t idesc = instr_desc(TILE_M, g.N);
   bool ok = true;
+  // Two-stage pipeline: the copies of chunk c + 1 are in flight while the
+  // tensor core multiplies chunk c; a stage is refilled once the MMAs that
+  // read it have committed to its mbarrier.
+  if (n_chunks > 0) {
+    stage_tile_async(sA[0], A, g.lda, TILE_M, k_begin, k_end);
+    stage_tile_async(sB[0], g.B, g.ldb, g.N, k_begin, k_end);
+    cp_async_commit();
+  }
   for (int c = 0; c < n_chunks && ok; ++c) {
     const int s = c & 1;
-    if (c >= 2) ok = mbar_wait(&mbar[s], ((c - 2) >> 1) & 1, WAIT_TRIES);
-    ok = __syncthreads_and(ok);
-    if (!ok) break;
-    const int k0 = k_begin + c * KC;
-    stage_tile(sA[s], A, g.lda, TILE_M, k0, k_end, KC);
-    stage_tile(sB[s], g.B, g.ldb, g.N, k0, k_end, KC);
+    if (c + 1 < n_chunks) {
+      const int s1 = (c + 1) & 1;
+      // stage s1 was last read by the MMAs of chunk c - 1
+      if (c >= 1) ok = mbar_wait(&mbar[s1], ((c - 1) >> 1) & 1, WAIT_TRIES);
+      ok = __syncthreads_and(ok);
+      if (!ok) break;
+      const int k1 = k_begin + (c + 1) * KC;
+      stage_tile_async(sA[s1], A, g.lda, TILE_M, k1, k_end);
+      stage_tile_async(sB[s1], g.B, g.ldb, g.N, k1, k_end);
+      cp_async_commit();
+      cp_async_wait<1>();  // this thread's copies of chunk c have landed
+    } else {
+      cp_async_wait<0>();
+    }
     fence_async_shared();
     __syncthreads();
     if (threadIdx.x == 0) {
       tc_fence_after();
+      const int k0 = k_begin + c * KC;
       const int nk = min(KC, k_end - k0);
       const uint32_t a0 = smem_u32(sA[s]), b0 = smem_u32(sB[s]);
       for (int j = 0; j * 16 < nk; ++j) {
@@ -269,6 +310,7 @@ __global__ void __launch_bounds__(128, 1) k_gemm(GemmArgs g)
       mma_commit(&mbar[s]);
     }
   }
+  cp_async_wait<0>();
   if (n_chunks > 0) {
     const int last = n_chunks - 1;
     bool done = mbar_wait(&mbar[last & 1], (last >> 1) & 1, WAIT_TRIES);
@@ -278,43 +320,59 @@ __global__ void __launch_bounds__(128, 1) k_gemm(GemmArgs g)
     if (threadIdx.x == 0) atomicOr(g.error, ERR_TIMEOUT);
   } else {
     tc_fence_after();
+    // Epilogue.  tcgen05.ld gives each thread one row (32 columns at a
+    // time); rows are written through a per-warp 32 x 33 shared-memory
+    // transpose so that each global store covers consecutive columns of one
+    // row, while the transposed copies (HT) are written from the row layout,
+    // where consecutive lanes hold consecutive rows.  The stage buffers are
+    // free: every MMA has completed.
+    float* st = reinterpret_cast<float*>(base) + warp * (32 * 33);
     const uint32_t t_row = tmem + (static_cast<uint32_t>(32 * warp) << 16);
+    const long long r0w = row0 + 32 * warp;  // first row of this warp
     float v[32];
-    if (EPI == EPI_DWEIGHT) {
-      const int m = 32 * warp + lane;
-      float* out = g.dW + static_cast<long long>(blockIdx.x) * TILE_M * g.N + static_cast<long long>(m) * g.N;
-      for (int cb = 0; cb < g.N; cb += 32) {
-        if (n_chunks > 0) tmem_ld32(t_row + cb, v);
-        else for (int k = 0; k < 32; ++k) v[k] = 0.0f;
-        for (int k = 0; k < 32 && cb + k < g.N; ++k) out[cb + k] = v[k];
-      }
-    } else {
-      const long long r = row0 + 32 * warp + lane;
-      for (int cb = 0; cb < g.N; cb += 32) {
-        tmem_ld32(t_row + cb, v);
-        __align__(16) __nv_bfloat16 hb[32];
-        if (EPI == EPI_FORWARD) {
-          float* zr = g.Z + r * g.N + cb;
-#pragma unroll
-          for (int k = 0; k < 32; ++k) {
-            float z = v[k] + g.bias[cb + k];
-            zr[k] = z;
-            hb[k] = __float2bfloat16_rn(silu(z));
-          }
-        } else {
-          const float* zp = g.Zprev + r * g.N + cb;
-#pragma unroll
-          for (int k = 0; k < 32; ++k) hb[k] = __float2bfloat16_rn(v[k] * silu_grad(zp[k]));
-        }
-        __nv_bfloat16* dst = (EPI == EPI_FORWARD ? g.H : g.dZprev) + r * g.N + cb;
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-          reinterpret_cast<uint4*>(dst)[q] = reinterpret_cast<const uint4*>(hb)[q];
+    for (int cb = 0; cb < g.N; cb += 32) {
+      if (n_chunks > 0) tmem_ld32(t_row + cb, v);
+      else for (int k = 0; k < 32; ++k) v[k] = 0.0f;
+      if (EPI == EPI_FORWARD) {
         if (g.HT) {
 #pragma unroll
-          for (int k = 0; k < 32; ++k) g.HT[static_cast<long long>(cb + k) * g.ldT + r] = hb[k];
+          for (int k = 0; k < 32; ++k)
+            g.HT[static_cast<long long>(cb + k) * g.ldT + r0w + lane] =
+              __float2bfloat16_rn(silu(v[k] + g.bias[cb + k]));
         }
       }
+#pragma unroll
+      for (int k = 0; k < 32; ++k) st[lane * 33 + k] = v[k];
+      __syncwarp();
+      const int col = cb + lane;
+      if (EPI == EPI_FORWARD) {
+        const float b = g.bias[col];
+        for (int rr = 0; rr < 32; ++rr) {
+          const long long r = r0w + rr;
+          const float z = st[rr * 33 + lane] + b;
+          g.Z[r * g.N + col] = z;
+          g.H[r * g.N + col] = __float2bfloat16_rn(silu(z));
+        }
+      } else if (EPI == EPI_DINPUT) {
+        for (int rr = 0; rr < 32; ++rr) {
+          const long long r = r0w + rr;
+          const float d = st[rr * 33 + lane] * silu_grad(g.Zprev[r * g.N + col]);
+          const __nv_bfloat16 db16 = __float2bfloat16_rn(d);
+          g.dZprev[r * g.N + col] = db16;
+          st[rr * 33 + lane] = __bfloat162float(db16);
+        }
+        __syncwarp();
+        if (g.HT) {
+#pragma unroll
+          for (int k = 0; k < 32; ++k)
+            g.HT[static_cast<long long>(cb + k) * g.ldT + r0w + lane] = __float2bfloat16_rn(st[lane * 33 + k]);
+        }
+      } else {
+        float* out = g.dW + static_cast<long long>(blockIdx.x) * TILE_M * g.N;
+        if (col < g.N)
+          for (int rr = 0; rr < 32; ++rr) out[(32 * warp + rr) * static_cast<long long>(g.N) + col] = st[rr * 33 + lane];
+      }
+      __syncwarp();
     }
   }
   tc_fence_before();
@@ -737,7 +795,7 @@ int openmc_gb300_mlp_create(int64_t max_rows, uint64_t seed, void** handle)
     MLP_CK(cudaStreamCreateWithFlags(&N->stream, cudaStreamNonBlocking));
     N->cap = (max_rows + TILE_M - 1) / TILE_M * TILE_M;
     const long long R = N->cap;
-    N->max_splits = 160;
+    N->max_splits = 320;
     N->P = N->alloc<float>(N_PARAMS);
     N->m = N->alloc<float>(N_PARAMS);
     N->v = N->alloc<float>(N_PARAMS);
@@ -804,7 +862,8 @@ int openmc_gb300_mlp_set_data(void* handle, int64_t n, const float* x4, const fl
     if (R > N->cap) return fail(OPENMC_E_INVALID_ARGUMENT, "more rows than the network was created for");
     N->n = n;
     N->R = R;
-    long long per = (R + 147) / 148;
+    // about two weight-gradient tiles per SM, each at least 256 rows deep
+    long long per = (R + 295) / 296;
     N->k_split = static_cast<int>(std::max<long long>(256, (per + KC - 1) / KC * KC));
     N->splits = static_cast<int>((R + N->k_split - 1) / N->k_split);
     if (N->splits > N->max_splits) return fail(OPENMC_E_INVALID_ARGUMENT, "too many gradient partials");

@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=0,
                     help="histories in the CPU baseline sample (default 3,000,000: about 10 s on 16 cores)")
     ap.add_argument("--no-xs-bench", action="store_true", help="skip the XS-lookup microbenchmark extra")
+    ap.add_argument("--no-network-bench", action="store_true", help="skip the importance-network extra")
+    ap.add_argument("--network-only", action="store_true",
+                    help="only time the importance network's training kernels (for kernel profilers)")
     ap.add_argument("--no-graph", action="store_true",
                     help="launch every batch kernel by kernel instead of as one CUDA graph "
                          "(for kernel profilers, which cannot see inside conditional graphs)")
@@ -291,6 +294,35 @@ def run_gb300(args, barrier=lambda: None, rank=0):
     return out
 
 
+def network_bench(rows=1 << 20, steps=20):
+    """Training throughput of the importance network's tensor-core kernels:
+    full-batch Adam steps over `rows` random rows.  FLOPs per step count the
+    matrix products only: forward 2R(16x128 + 2x128x128), input gradients
+    2R(2x128x128), weight gradients 2R(2x128x144 + 128x16)."""
+    from openmc_gb300 import lib
+    rng = np.random.default_rng(3)
+    x = rng.uniform(-1, 1, size=(rows, 4)).astype(np.float32)
+    t = (x[:, 0] - 0.5 * x[:, 3]).astype(np.float32)
+    net = lib.ImportanceNetwork(max_rows=rows, seed=1)
+    try:
+        net.set_data(x, t)
+        net.train(2, lr=1e-3)
+        net.train(steps, lr=1e-3)
+        ms = net.last_train_ms()
+    finally:
+        net.close()
+    flops = 2.0 * rows * (16 * 128 + 2 * 128 * 128 + 2 * 128 * 128 + 2 * 128 * 144 + 128 * 16)
+    tflops = flops * steps / (ms * 1e-3) / 1e12
+    peak = 0.0
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peak = float(json.loads(pk.read_text()).get("bf16_tflops", 0.0))
+    return {"rows": rows, "steps": steps, "ms_per_step": ms / steps, "tflops": tflops,
+            "bf16_peak_tflops": peak or None, "frac_of_bf16_peak": tflops / peak if peak else None,
+            "note": "hidden width 128: each 128-row tile moves ~200 KB for 4 MFLOP, so the products are "
+                    "bound by memory traffic, not by the tensor cores"}
+
+
 def compare_tallies(a, b):
     """FP32-table tally (a) against the FP64-table tally (b), both
     (mean, std of the mean): share of bins scored by both within 3 combined
@@ -400,11 +432,16 @@ def main():
         return
     import torch
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    if args.network_only:
+        print(json.dumps({"importance_network": network_bench(rows=args.particles, steps=args.steps)}))
+        return
     barrier = (lambda: None)
     if world > 1:
         import torch.distributed as dist
         barrier = dist.barrier
     r = run_gb300(args, barrier=barrier, rank=rank)
+    if not args.no_network_bench and rank == 0:
+        r["network"] = network_bench()
     if not args.no_xs_bench and rank == 0:
         x64, x32 = xs_lookup_bench(False), xs_lookup_bench(True)
         h64, h32 = x64.pop("_head"), x32.pop("_head")
@@ -456,6 +493,7 @@ def main():
         "events_per_step": r["detail"]["queue"]["xs_events"] + r["detail"]["tail"]["xs_events"],
         "iterations_per_step": r["iterations"],
         "xs_lookup_microbench": r.get("xs_lookup"),
+        "importance_network_training": r.get("network"),
     }
     print(json.dumps(line))
 

@@ -354,9 +354,15 @@ __global__ void __launch_bounds__(128, 1) k_gemm(GemmArgs g)
           g.H[r * g.N + col] = __float2bfloat16_rn(silu(z));
         }
       } else if (EPI == EPI_DINPUT) {
+        // all 32 pre-activations of this column first, so that the loads
+        // are in flight together
+        float zp[32];
+#pragma unroll
+        for (int rr = 0; rr < 32; ++rr) zp[rr] = __ldg(g.Zprev + (r0w + rr) * g.N + col);
+#pragma unroll
         for (int rr = 0; rr < 32; ++rr) {
           const long long r = r0w + rr;
-          const float d = st[rr * 33 + lane] * silu_grad(g.Zprev[r * g.N + col]);
+          const float d = st[rr * 33 + lane] * silu_grad(zp[rr]);
           const __nv_bfloat16 db16 = __float2bfloat16_rn(d);
           g.dZprev[r * g.N + col] = db16;
           st[rr * 33 + lane] = __bfloat162float(db16);

@@ -231,13 +231,25 @@ __constant__ DBank db;
 __constant__ DQueues dq;
 
 // ------------------------------------------------------------------- RNG
-// src/random_lcg.cpp:32-44
-__device__ __forceinline__ double prn(unsigned long long& s)
+// src/random_lcg.cpp:32-44: one step of the generator and its output word
+__device__ __forceinline__ unsigned long long prn_word(unsigned long long& s)
 {
   s = PRN_MULT * s + PRN_ADD;
   unsigned long long word = ((s >> ((s >> 59u) + 5u)) ^ s) * 12605985483714917081ull;
-  unsigned long long result = (word >> 43u) ^ word;
-  return __ull2double_rn(result) * 5.421010862427522170037264e-20;  // 2^-64
+  return (word >> 43u) ^ word;
+}
+
+__device__ __forceinline__ double prn(unsigned long long& s)
+{
+  return __ull2double_rn(prn_word(s)) * 5.421010862427522170037264e-20;  // 2^-64
+}
+
+// The same generator step as prn, as an FP32 number in (0, 1): the top 23
+// bits of the word, centred in their interval ((2k + 1) 2^-24 is exact in
+// FP32), so that it is never 0 or 1 and its logarithm stays finite.
+__device__ __forceinline__ float prn_f(unsigned long long& s)
+{
+  return __uint2float_rn(2u * static_cast<unsigned>(prn_word(s) >> 41) + 1u) * 0x1p-24f;
 }
 
 // src/random_lcg.cpp:91-120
@@ -261,13 +273,9 @@ __device__ __forceinline__ double uniform_distribution(double a, double b, unsig
   return a + (b - a) * prn(s);
 }
 
-// src/math_functions.cpp:763-792 (phi sampled)
-// recip: divide by multiplying with the reciprocal (FP32-table mode; FP64
-// products rounded twice instead of FP64 quotients).  sin and cos of the
-// sampled angle come from one sincos call (the device's own functions in
-// either form).
-__device__ inline void rotate_angle(double& ux, double& uy, double& uz, double mu, unsigned long long& s,
-  bool recip = false)
+// src/math_functions.cpp:763-792 (phi sampled; sin and cos of the sampled
+// angle from one sincos call)
+__device__ inline void rotate_angle(double& ux, double& uy, double& uz, double mu, unsigned long long& s)
 {
   double phi_ = 2.0 * PI * prn(s);
   double sinphi, cosphi;
@@ -276,20 +284,39 @@ __device__ inline void rotate_angle(double& ux, double& uy, double& uz, double m
   double b = sqrt(fmax(0., 1. - uz * uz));
   double x = ux, y = uy, z = uz;
   if (b > 1e-10) {
-    if (recip) {
-      const double ib = 1.0 / b;
-      ux = mu * x + a * (x * z * cosphi - y * sinphi) * ib;
-      uy = mu * y + a * (y * z * cosphi + x * sinphi) * ib;
-    } else {
-      ux = mu * x + a * (x * z * cosphi - y * sinphi) / b;
-      uy = mu * y + a * (y * z * cosphi + x * sinphi) / b;
-    }
+    ux = mu * x + a * (x * z * cosphi - y * sinphi) / b;
+    uy = mu * y + a * (y * z * cosphi + x * sinphi) / b;
     uz = mu * z - a * b * cosphi;
   } else {
     b = sqrt(1. - y * y);
     ux = mu * x + a * (-x * y * sinphi + z * cosphi) / b;
     uy = mu * y + a * b * sinphi;
     uz = mu * z - a * (y * z * sinphi + x * cosphi) / b;
+  }
+}
+
+// rotate_angle in FP32 (FP32-table mode's collision kinematics).  The
+// perpendicular norm b is sqrt(ux^2 + uy^2) (sqrt(ux^2 + uz^2) in the second
+// branch), which equals the reference's sqrt(1 - uz^2) for a unit vector
+// and keeps FP32 accuracy when uz is near +-1, where 1 - uz^2 cancels.
+__device__ inline void rotate_angle_f(float& ux, float& uy, float& uz, float mu, unsigned long long& s)
+{
+  float sinphi, cosphi;
+  sincospif(2.0f * prn_f(s), &sinphi, &cosphi);
+  const float a = sqrtf(fmaxf(0.f, 1.f - mu * mu));
+  const float x = ux, y = uy, z = uz;
+  float b = sqrtf(x * x + y * y);
+  if (b > 1e-10f) {
+    const float ib = 1.0f / b;
+    ux = mu * x + a * (x * z * cosphi - y * sinphi) * ib;
+    uy = mu * y + a * (y * z * cosphi + x * sinphi) * ib;
+    uz = mu * z - a * b * cosphi;
+  } else {
+    b = sqrtf(x * x + z * z);
+    const float ib = 1.0f / b;
+    ux = mu * x + a * (-x * y * sinphi + z * cosphi) * ib;
+    uy = mu * y + a * b * sinphi;
+    uz = mu * z - a * (y * z * sinphi + x * cosphi) * ib;
   }
 }
 
@@ -309,7 +336,7 @@ __device__ inline double maxwell_spectrum(double T, unsigned long long& s)
 __device__ __forceinline__ int lower_bound_index_pos(const double* a, int lo, int hi, double v)
 {
   // returns lower_bound(a+lo, a+hi, v) - (a+lo) - 1, or 0 when a[lo] == v
-  if (a[lo] == v) return 0;
+  if (__double_as_longlong(__ldg(a + lo)) == __double_as_longlong(v)) return 0;
   long long key = __double_as_longlong(v);
   int first = lo, count = hi - lo;
   while (count > 0) {
@@ -837,15 +864,18 @@ struct Micro {
 
 // Locates the grid interval of E and returns its index and bracketing
 // energies e0 < e1 (duplicate points skipped as the reference does).
+// Energies are non-negative doubles, which order (and compare equal) like
+// their bit patterns: the comparisons run on the integer pipe.
 __device__ __forceinline__ int nuclide_grid(int nuc, int i_log, double E, double& e0_out, double& e1_out)
 {
   const long long off = dm.nuc_off[nuc];
   const int G = static_cast<int>(dm.nuc_off[nuc + 1] - off);
   const double* e = dm.energy + off;
+  const long long kE = __double_as_longlong(E);
   int i_grid;
-  if (E < __ldg(e)) {
+  if (kE < __double_as_longlong(__ldg(e))) {
     i_grid = 0;
-  } else if (E > __ldg(e + G - 1)) {
+  } else if (kE > __double_as_longlong(__ldg(e + G - 1))) {
     i_grid = G - 2;
   } else {
     const int* gi = dm.grid_index + static_cast<long long>(nuc) * (dm.M + 1);
@@ -854,7 +884,7 @@ __device__ __forceinline__ int nuclide_grid(int nuc, int i_log, double E, double
     i_grid = i_low + lower_bound_index_pos(e, i_low, i_high, E);
   }
   double e0 = __ldg(e + i_grid), e1 = __ldg(e + i_grid + 1);
-  if (e0 == e1) {
+  if (__double_as_longlong(e0) == __double_as_longlong(e1)) {
     ++i_grid;
     e0 = e1;
     e1 = __ldg(e + i_grid + 1);

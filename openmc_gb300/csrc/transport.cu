@@ -259,7 +259,9 @@ __device__ __forceinline__ int tally_offsets(const DTally& T, double E_last, con
       mesh_slot = i;
     } else if (F.type == 1) {
       const double* b = dm.ebins + F.e_off;
-      if (!(E_last >= b[0] && E_last <= b[F.nbins])) return 0;
+      // non-negative doubles compare like their bit patterns (integer pipe)
+      const long long kE = __double_as_longlong(E_last);
+      if (!(kE >= __double_as_longlong(__ldg(b)) && kE <= __double_as_longlong(__ldg(b + F.nbins)))) return 0;
       const long long add = static_cast<long long>(lower_bound_index_pos(b, 0, F.nbins + 1, E_last)) * st;
       for (int k = 0; k < n; ++k) offs[k] += add;
     } else if (F.type == 4) {
@@ -1115,54 +1117,108 @@ __device__ void sample_cxs_target_velocity(double awr, double E, const double* u
   }
   double vt = sqrt(beta_vt_sq * kT / awr);
   double x = u[0], y = u[1], z = u[2];
-  rotate_angle(x, y, z, mu, seed, dm.xs_fp32 != 0);
+  rotate_angle(x, y, z, mu, seed);
   vt_out[0] = vt * x;
   vt_out[1] = vt * y;
   vt_out[2] = vt * z;
 }
 
-// src/physics.cpp:754-818 elastic scattering with free-gas target
+// src/physics.cpp:990-1041 in FP32 (FP32-table mode): the same draws in
+// the same order as sample_cxs_target_velocity, each an FP32 uniform from
+// prn_f; cos(pi/2 r) through cospif.
+__device__ void sample_cxs_target_velocity_f(float awr, float E, const float* u, float kT,
+  unsigned long long& seed, float* vt_out)
+{
+  const float beta_vn = sqrtf(awr * E / kT);
+  const float alpha = 1.0f / (1.0f + 0.886226925f * beta_vn);  // sqrt(pi) / 2
+  float beta_vt_sq = 0.0f;
+  float mu = 0.0f;
+  for (int it = 0;; ++it) {
+    const float r1 = prn_f(seed);
+    const float r2 = prn_f(seed);
+    if (prn_f(seed) < alpha) {
+      beta_vt_sq = -logf(r1 * r2);
+    } else {
+      const float c = cospif(0.5f * prn_f(seed));
+      beta_vt_sq = -logf(r1) - logf(r2) * c * c;
+    }
+    const float beta_vt = sqrtf(beta_vt_sq);
+    mu = 2.0f * prn_f(seed) - 1.0f;
+    const float accept_prob =
+      sqrtf(fmaxf(0.0f, beta_vn * beta_vn + beta_vt_sq - 2.0f * beta_vn * beta_vt * mu)) / (beta_vn + beta_vt);
+    if (prn_f(seed) < accept_prob) break;
+    if (it > 1000000) {
+      set_error(ERR_REJECTION);
+      break;
+    }
+  }
+  const float vt = sqrtf(beta_vt_sq * kT / awr);
+  float x = u[0], y = u[1], z = u[2];
+  rotate_angle_f(x, y, z, mu, seed);
+  vt_out[0] = vt * x;
+  vt_out[1] = vt * y;
+  vt_out[2] = vt * z;
+}
+
+// src/physics.cpp:754-818 elastic scattering with free-gas target.
+// FP32-table mode runs the kinematics in FP32 (the outgoing energy and
+// direction then carry FP32 precision, like the cross sections that chose
+// the reaction); the free-gas test stays FP64, and the direction returns to
+// unit length in FP64 through one Newton step on 1 / |u| (|u|^2 - 1 is
+// O(1e-7) in FP32 and O(1e-14) after the step), so that the FP64 tracking
+// sees a unit vector.  FP64 tables keep the reference's FP64 expression.
 __device__ void elastic_scatter(int nuc, double& E, double* u, unsigned long long& seed)
 {
+  const double awr = dm.awr[nuc];
+  const double kT = dm.kT[nuc];
+  const bool free_gas = !(E >= 400.0 * kT && awr > 1.0);
+  if (dm.xs_fp32) {
+    const float awf = static_cast<float>(awr);
+    const float Ef = static_cast<float>(E);
+    const float uf[3] = {static_cast<float>(u[0]), static_cast<float>(u[1]), static_cast<float>(u[2])};
+    float vel = sqrtf(Ef);
+    float vn[3] = {vel * uf[0], vel * uf[1], vel * uf[2]};
+    float vt[3] = {0.0f, 0.0f, 0.0f};
+    if (free_gas) sample_cxs_target_velocity_f(awf, Ef, uf, static_cast<float>(kT), seed, vt);
+    const float iw = 1.0f / (awf + 1.0f);
+    float vcm[3];
+    for (int k = 0; k < 3; ++k) vcm[k] = (vn[k] + awf * vt[k]) * iw;
+    for (int k = 0; k < 3; ++k) vn[k] = vn[k] - vcm[k];
+    vel = sqrtf(vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2]);
+    const float mu_cm = 2.0f * prn_f(seed) - 1.0f;
+    const float iv = 1.0f / vel;
+    float ucm[3] = {vn[0] * iv, vn[1] * iv, vn[2] * iv};
+    rotate_angle_f(ucm[0], ucm[1], ucm[2], mu_cm, seed);
+    for (int k = 0; k < 3; ++k) vn[k] = vel * ucm[k] + vcm[k];
+    const float Eo = vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2];
+    const float io = rsqrtf(Eo);
+    const double x = vn[0] * io, y = vn[1] * io, z = vn[2] * io;
+    const double c = 1.5 - 0.5 * (x * x + y * y + z * z);
+    E = Eo;
+    u[0] = x * c;
+    u[1] = y * c;
+    u[2] = z * c;
+    return;
+  }
   double vel = sqrt(E);
-  double awr = dm.awr[nuc];
-  double kT = dm.kT[nuc];
   double vn[3] = {vel * u[0], vel * u[1], vel * u[2]};
   double vt[3] = {0.0, 0.0, 0.0};
-  if (!(E >= 400.0 * kT && awr > 1.0)) sample_cxs_target_velocity(awr, E, u, kT, seed, vt);
-  // FP32-table mode: the quotients by (awr + 1) and by the speeds become
-  // products with FP64 reciprocals (double rounding instead of one)
-  const bool recip = dm.xs_fp32 != 0;
+  if (free_gas) sample_cxs_target_velocity(awr, E, u, kT, seed, vt);
   double vcm[3];
-  if (recip) {
-    const double iw = 1.0 / (awr + 1.0);
-    for (int k = 0; k < 3; ++k) vcm[k] = (vn[k] + awr * vt[k]) * iw;
-  } else {
-    for (int k = 0; k < 3; ++k) vcm[k] = (vn[k] + awr * vt[k]) / (awr + 1.0);
-  }
+  for (int k = 0; k < 3; ++k) vcm[k] = (vn[k] + awr * vt[k]) / (awr + 1.0);
   for (int k = 0; k < 3; ++k) vn[k] = vn[k] - vcm[k];
   vel = sqrt(vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2]);
   double mu_cm = uniform_distribution(-1., 1., seed);
   double ucm[3];
-  if (recip) {
-    const double iv = 1.0 / vel;
-    ucm[0] = vn[0] * iv; ucm[1] = vn[1] * iv; ucm[2] = vn[2] * iv;
-  } else {
-    ucm[0] = vn[0] / vel; ucm[1] = vn[1] / vel; ucm[2] = vn[2] / vel;
-  }
-  rotate_angle(ucm[0], ucm[1], ucm[2], mu_cm, seed, recip);
+  ucm[0] = vn[0] / vel; ucm[1] = vn[1] / vel; ucm[2] = vn[2] / vel;
+  rotate_angle(ucm[0], ucm[1], ucm[2], mu_cm, seed);
   for (int k = 0; k < 3; ++k) vn[k] = vel * ucm[k];
   for (int k = 0; k < 3; ++k) vn[k] = vn[k] + vcm[k];
   E = vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2];
   vel = sqrt(E);
-  if (recip) {
-    const double iv = 1.0 / vel;
-    u[0] = vn[0] * iv; u[1] = vn[1] * iv; u[2] = vn[2] * iv;
-  } else {
-    u[0] = vn[0] / vel;
-    u[1] = vn[1] / vel;
-    u[2] = vn[2] / vel;
-  }
+  u[0] = vn[0] / vel;
+  u[1] = vn[1] / vel;
+  u[2] = vn[2] / vel;
 }
 
 // src/particle.cpp:331-415 + src/physics.cpp:43-168, 494-518, 638-752

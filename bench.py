@@ -136,12 +136,12 @@ def peaks():
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic
 # byte of each kernel, from an ncu capture of the same kernel on the 2x10^6
-# history lattice with 262,144 slots, matched launch by launch with the
+# history lattice with 524,288 slots, matched launch by launch with the
 # OPENMC_GB300_LAUNCH_LOG counts (profiles/advance_surface_collision_lattice17_2M.md;
 # the unfused kernels' ratios come from the same capture of the earlier build).
 # Traffic per launch scales with the events a launch processes.
-TRAFFIC_PER_ALGORITHMIC_BYTE = {"xs+advance+surface": 0.802, "xs+advance": 1.376, "surface": 1.406,
-                                "collision": 1.276}
+TRAFFIC_PER_ALGORITHMIC_BYTE = {"xs+advance+surface": 2.338, "xs+advance": 1.376, "surface": 1.406,
+                                "collision": 1.254}
 
 
 def algorithmic_bytes(detail, levels, fp32):

@@ -98,17 +98,29 @@ __device__ void mark_lost(long long s)
 
 // ------------------------------------------------------ mesh raytrace
 // src/mesh.cpp:1328-1369 RegularMesh helpers
-// ceil((r - lower_left) / width).  The quotient is first estimated in FP32
-// (relative error below 1e-6 for |q| < 2^20); only when the estimate lies
-// within 1e-4 of an integer, where the ceiling could differ, is the FP64
-// division evaluated.  The returned index equals the FP64 ceiling.
-__device__ __forceinline__ int mesh_index_in_direction(const DMesh& m, double r, int i)
+// ceil((r - lower_left) / width) decided in FP32: the quotient estimated in
+// FP32 (relative error below 1e-6 for |q| < 2^20) settles the ceiling when it
+// lies at least 1e-4 + 2e-6 |q| from an integer, i.e. when r is at least
+// 1e-4 widths from a cell face.  Returns false otherwise.
+__device__ __forceinline__ bool mesh_index_fp32(const DMesh& m, double r, int i, int& idx)
 {
   const double t = r - m.ll[i];
   const float q32 = __fdiv_rn(static_cast<float>(t), static_cast<float>(m.width[i]));
   const float fr = q32 - rintf(q32);
-  if (fabsf(q32) < 1048576.0f && fabsf(fr) > 1e-4f + 2e-6f * fabsf(q32)) return static_cast<int>(ceilf(q32));
-  return static_cast<int>(ceil(t / m.width[i]));
+  if (fabsf(q32) < 1048576.0f && fabsf(fr) > 1e-4f + 2e-6f * fabsf(q32)) {
+    idx = static_cast<int>(ceilf(q32));
+    return true;
+  }
+  return false;
+}
+
+// ceil((r - lower_left) / width): FP32 where that is decided, else the FP64
+// division.  The returned index equals the FP64 ceiling.
+__device__ __forceinline__ int mesh_index_in_direction(const DMesh& m, double r, int i)
+{
+  int idx;
+  if (mesh_index_fp32(m, r, i, idx)) return idx;
+  return static_cast<int>(ceil((r - m.ll[i]) / m.width[i]));
 }
 
 __device__ __forceinline__ void mesh_get_indices(const DMesh& m, double x, double y, double z, int* ijk, bool& in_mesh)
@@ -176,7 +188,6 @@ __device__ void mesh_bins_crossed(const DMesh& m, const double* r0, const double
     total_distance = sqrt(dx * dx + dy * dy + dz * dz);
   }
   if (total_distance == 0.0) return;
-  const double inv_total = inv_u ? 1.0 / total_distance : 0.0;
   const int n = m.ndim;
   bool in_mesh;
   double traveled = 0.0;
@@ -186,6 +197,27 @@ __device__ void mesh_bins_crossed(const DMesh& m, const double* r0, const double
     if (in_mesh) f(mesh_bin(m, ijk), 1.0);
     return;
   }
+  // A track that ends in the in-mesh cell it starts in (most tracks of a mesh
+  // as fine as the lattice): when the end point lies in that cell on every
+  // axis at least 1e-4 widths from its faces (decided in FP32), the distance
+  // from the start to each face ahead exceeds the track length by that
+  // margin, so the walk below would score this cell once with fraction
+  // total / total = 1 and stop.  Scored directly.  Tracks that end on a face
+  // (a lattice boundary on the mesh) take the walk.
+  if (in_mesh) {
+    bool same = true;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      if (k >= n) break;
+      int e = -1;
+      same = same && mesh_index_fp32(m, r1[k], k, e) && e == ijk[k];
+    }
+    if (same) {
+      f(mesh_bin(m, ijk), 1.0);
+      return;
+    }
+  }
+  const double inv_total = inv_u ? 1.0 / total_distance : 0.0;
   // the per-axis arrays are indexed by unrolled compile-time axes only, so
   // that they stay in registers
   MeshDist dist[3];
@@ -1123,9 +1155,11 @@ __device__ void sample_cxs_target_velocity(double awr, double E, const double* u
   vt_out[2] = vt * z;
 }
 
-// src/physics.cpp:990-1041 in FP32 (FP32-table mode): the same draws in
-// the same order as sample_cxs_target_velocity, each an FP32 uniform from
-// prn_f; cos(pi/2 r) through cospif.
+// src/physics.cpp:990-1041 in FP32 (FP32-table mode): the target nucleus's
+// velocity, a random variate that only enters the neutron's FP64 kinematics.
+// The same draws in the same order as sample_cxs_target_velocity, each an
+// FP32 uniform from prn_f; cos(pi/2 r) through cospif; the target direction
+// rotated by rotate_angle_f.
 __device__ void sample_cxs_target_velocity_f(float awr, float E, const float* u, float kT,
   unsigned long long& seed, float* vt_out)
 {
@@ -1160,65 +1194,64 @@ __device__ void sample_cxs_target_velocity_f(float awr, float E, const float* u,
   vt_out[2] = vt * z;
 }
 
-// src/physics.cpp:754-818 elastic scattering with free-gas target.
-// FP32-table mode runs the kinematics in FP32 (the outgoing energy and
-// direction then carry FP32 precision, like the cross sections that chose
-// the reaction); the free-gas test stays FP64, and the direction returns to
-// unit length in FP64 through one Newton step on 1 / |u| (|u|^2 - 1 is
-// O(1e-7) in FP32 and O(1e-14) after the step), so that the FP64 tracking
-// sees a unit vector.  FP64 tables keep the reference's FP64 expression.
+// src/physics.cpp:754-818 elastic scattering with free-gas target.  In
+// FP32-table mode the target velocity (a random variate of the target
+// nucleus, sampled in FP32 by sample_cxs_target_velocity_f) enters the FP64
+// centre-of-mass transformation; the neutron's own energy and direction are
+// computed in FP64 throughout, with the quotients by (awr + 1) and by the
+// speeds written as products with FP64 reciprocals (rounded twice instead of
+// once).  FP64 tables keep the reference's expression.
 __device__ void elastic_scatter(int nuc, double& E, double* u, unsigned long long& seed)
 {
-  const double awr = dm.awr[nuc];
-  const double kT = dm.kT[nuc];
-  const bool free_gas = !(E >= 400.0 * kT && awr > 1.0);
-  if (dm.xs_fp32) {
-    const float awf = static_cast<float>(awr);
-    const float Ef = static_cast<float>(E);
-    const float uf[3] = {static_cast<float>(u[0]), static_cast<float>(u[1]), static_cast<float>(u[2])};
-    float vel = sqrtf(Ef);
-    float vn[3] = {vel * uf[0], vel * uf[1], vel * uf[2]};
-    float vt[3] = {0.0f, 0.0f, 0.0f};
-    if (free_gas) sample_cxs_target_velocity_f(awf, Ef, uf, static_cast<float>(kT), seed, vt);
-    const float iw = 1.0f / (awf + 1.0f);
-    float vcm[3];
-    for (int k = 0; k < 3; ++k) vcm[k] = (vn[k] + awf * vt[k]) * iw;
-    for (int k = 0; k < 3; ++k) vn[k] = vn[k] - vcm[k];
-    vel = sqrtf(vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2]);
-    const float mu_cm = 2.0f * prn_f(seed) - 1.0f;
-    const float iv = 1.0f / vel;
-    float ucm[3] = {vn[0] * iv, vn[1] * iv, vn[2] * iv};
-    rotate_angle_f(ucm[0], ucm[1], ucm[2], mu_cm, seed);
-    for (int k = 0; k < 3; ++k) vn[k] = vel * ucm[k] + vcm[k];
-    const float Eo = vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2];
-    const float io = rsqrtf(Eo);
-    const double x = vn[0] * io, y = vn[1] * io, z = vn[2] * io;
-    const double c = 1.5 - 0.5 * (x * x + y * y + z * z);
-    E = Eo;
-    u[0] = x * c;
-    u[1] = y * c;
-    u[2] = z * c;
-    return;
-  }
   double vel = sqrt(E);
+  double awr = dm.awr[nuc];
+  double kT = dm.kT[nuc];
   double vn[3] = {vel * u[0], vel * u[1], vel * u[2]};
   double vt[3] = {0.0, 0.0, 0.0};
-  if (free_gas) sample_cxs_target_velocity(awr, E, u, kT, seed, vt);
+  const bool recip = dm.xs_fp32 != 0;
+  if (!(E >= 400.0 * kT && awr > 1.0)) {
+    if (recip) {
+      const float uf[3] = {static_cast<float>(u[0]), static_cast<float>(u[1]), static_cast<float>(u[2])};
+      float vtf[3];
+      sample_cxs_target_velocity_f(static_cast<float>(awr), static_cast<float>(E), uf, static_cast<float>(kT), seed,
+                                   vtf);
+      vt[0] = vtf[0];
+      vt[1] = vtf[1];
+      vt[2] = vtf[2];
+    } else {
+      sample_cxs_target_velocity(awr, E, u, kT, seed, vt);
+    }
+  }
   double vcm[3];
-  for (int k = 0; k < 3; ++k) vcm[k] = (vn[k] + awr * vt[k]) / (awr + 1.0);
+  if (recip) {
+    const double iw = 1.0 / (awr + 1.0);
+    for (int k = 0; k < 3; ++k) vcm[k] = (vn[k] + awr * vt[k]) * iw;
+  } else {
+    for (int k = 0; k < 3; ++k) vcm[k] = (vn[k] + awr * vt[k]) / (awr + 1.0);
+  }
   for (int k = 0; k < 3; ++k) vn[k] = vn[k] - vcm[k];
   vel = sqrt(vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2]);
   double mu_cm = uniform_distribution(-1., 1., seed);
   double ucm[3];
-  ucm[0] = vn[0] / vel; ucm[1] = vn[1] / vel; ucm[2] = vn[2] / vel;
-  rotate_angle(ucm[0], ucm[1], ucm[2], mu_cm, seed);
+  if (recip) {
+    const double iv = 1.0 / vel;
+    ucm[0] = vn[0] * iv; ucm[1] = vn[1] * iv; ucm[2] = vn[2] * iv;
+  } else {
+    ucm[0] = vn[0] / vel; ucm[1] = vn[1] / vel; ucm[2] = vn[2] / vel;
+  }
+  rotate_angle(ucm[0], ucm[1], ucm[2], mu_cm, seed, recip);
   for (int k = 0; k < 3; ++k) vn[k] = vel * ucm[k];
   for (int k = 0; k < 3; ++k) vn[k] = vn[k] + vcm[k];
   E = vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2];
   vel = sqrt(E);
-  u[0] = vn[0] / vel;
-  u[1] = vn[1] / vel;
-  u[2] = vn[2] / vel;
+  if (recip) {
+    const double iv = 1.0 / vel;
+    u[0] = vn[0] * iv; u[1] = vn[1] * iv; u[2] = vn[2] * iv;
+  } else {
+    u[0] = vn[0] / vel;
+    u[1] = vn[1] / vel;
+    u[2] = vn[2] / vel;
+  }
 }
 
 // src/particle.cpp:331-415 + src/physics.cpp:43-168, 494-518, 638-752

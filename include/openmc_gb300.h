@@ -128,6 +128,11 @@ extern int openmc_gb300_split_to_slots;
  * 2-level build for models nested at most 2 deep (per-level state in
  * registers) and the 4-level build otherwise; 4 forces the 4-level build */
 extern int openmc_gb300_max_levels;
+/* 1: each block of the event kernels copies the cell, surface, region-token,
+ * universe and per-material nuclide tables into shared memory at entry (when
+ * they fit in 32 KB) and reads them there; 0 (default): read through L1 from
+ * global memory, where tables of a few KB stay resident */
+extern int openmc_gb300_stage_tables;
 
 /* last batch: [ms, iterations, events, total_weight, leakage, lost, done, secondary-pool entries used,
  *  events of the longest history, its particle id] */

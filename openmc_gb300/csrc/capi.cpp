@@ -74,6 +74,7 @@ int openmc_gb300_fuse = 3;              // bit 0: cross-section event, bit 1: su
 int64_t openmc_gb300_tail_threshold = -1;  // queue length that starts the history-based tail (-1: default)
 int64_t openmc_gb300_secondary_capacity = 0;  // secondary-site pool entries (0: automatic)
 int openmc_gb300_split_to_slots = 0;  // split particles start in free slots with their own seeds
+int openmc_gb300_stage_tables = 0;    // event kernels copy the geometry/material tables into shared memory
 int openmc_gb300_max_levels = 0;      // coordinate depth of the transport kernels (0: from the model)
 int openmc_gb300_xs_fp32 = -1;          // -1: from XML (<gb300_xs_precision>), else 0/1
 int64_t openmc_gb300_in_flight = 0;     // particle slots; 0: setting or automatic
@@ -365,6 +366,7 @@ int openmc_simulation_init()
     opt.secondary_cap = openmc_gb300_secondary_capacity;
     opt.split_slots = openmc_gb300_split_to_slots;
     opt.max_levels = openmc_gb300_max_levels;
+    opt.stage_tables = openmc_gb300_stage_tables;
     opt.fuse = openmc_gb300_fuse;
     if (m.ww_on && m.weight_windows.empty()) return fail(OPENMC_E_INVALID_ARGUMENT, "weight windows are on but none are defined");
     s.gpu = gpu_create(m, opt);

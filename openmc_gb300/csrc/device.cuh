@@ -125,6 +125,10 @@ struct DModel {
   long long n_particles;
   long long master_seed;
   unsigned long long stride;
+  // shared-memory copy of the per-event tables (tables_enter): byte offset
+  // and 4-byte word count of each table, total bytes (0: not staged)
+  int stage_off[9], stage_words[9];
+  int stage_bytes;
 };
 
 // Structure-of-arrays particle bank; level-major arrays are [MAXL][cap].
@@ -229,6 +233,98 @@ struct DQueues {
 __constant__ DModel dm;
 __constant__ DBank db;
 __constant__ DQueues dq;
+
+// ------------------------------------------------------ per-event tables
+// The cell, surface, region-token, universe and per-material nuclide tables
+// are read by every event.  Device code reaches them through the block's
+// pointer table s_tabs, which each kernel sets at entry (tables_enter): to
+// copies in dynamic shared memory when the stage_tables option is on and the
+// launch provides room for all of them (dm.stage_bytes, at most
+// OMC_STAGE_MAX_BYTES), else to the tables in global memory.
+enum {
+  STG_SURF, STG_CELL, STG_TOK, STG_UNIV_OFF, STG_UNIV_CELLS, STG_MAT_OFF, STG_MAT_NUC, STG_MAT_DENS,
+  STG_MAT_DENS32, STG_N
+};
+
+#ifndef OMC_STAGE_MAX_BYTES
+#define OMC_STAGE_MAX_BYTES 32768
+#endif
+
+struct Tabs {
+  const DSurface* surf;
+  const DCell* cell;
+  const int* tok;
+  const int* univ_off;
+  const int* univ_cells;
+  const int* mat_off;
+  const int* mat_nuc;
+  const double* mat_dens;
+  const float* mat_dens32;
+};
+
+__shared__ Tabs s_tabs;
+extern __shared__ __align__(16) unsigned char s_stage[];
+
+__device__ __forceinline__ unsigned dynamic_smem_bytes()
+{
+  unsigned r;
+  asm volatile("mov.u32 %0, %%dynamic_smem_size;" : "=r"(r));
+  return r;
+}
+
+__device__ __forceinline__ const void* stage_source(int k)
+{
+  switch (k) {
+  case STG_SURF: return dm.surf;
+  case STG_CELL: return dm.cell;
+  case STG_TOK: return dm.tok;
+  case STG_UNIV_OFF: return dm.univ_off;
+  case STG_UNIV_CELLS: return dm.univ_cells;
+  case STG_MAT_OFF: return dm.mat_off;
+  case STG_MAT_NUC: return dm.mat_nuc;
+  case STG_MAT_DENS: return dm.mat_dens;
+  default: return dm.mat_dens32;
+  }
+}
+
+// Sets s_tabs (copying the tables first when the launch's dynamic shared
+// memory holds them).  Every thread of the block calls it, at kernel entry,
+// before any thread can leave: it ends in a block barrier.
+__device__ __forceinline__ void tables_enter()
+{
+  const bool stage = dm.stage_bytes > 0 && dynamic_smem_bytes() >= static_cast<unsigned>(dm.stage_bytes);
+  if (stage) {
+    for (int k = 0; k < STG_N; ++k) {
+      const unsigned* src = static_cast<const unsigned*>(stage_source(k));
+      unsigned* dst = reinterpret_cast<unsigned*>(s_stage + dm.stage_off[k]);
+      for (int w = threadIdx.x; w < dm.stage_words[k]; w += blockDim.x) dst[w] = __ldg(src + w);
+    }
+  }
+  if (threadIdx.x == 0) {
+    if (stage) {
+      s_tabs.surf = reinterpret_cast<const DSurface*>(s_stage + dm.stage_off[STG_SURF]);
+      s_tabs.cell = reinterpret_cast<const DCell*>(s_stage + dm.stage_off[STG_CELL]);
+      s_tabs.tok = reinterpret_cast<const int*>(s_stage + dm.stage_off[STG_TOK]);
+      s_tabs.univ_off = reinterpret_cast<const int*>(s_stage + dm.stage_off[STG_UNIV_OFF]);
+      s_tabs.univ_cells = reinterpret_cast<const int*>(s_stage + dm.stage_off[STG_UNIV_CELLS]);
+      s_tabs.mat_off = reinterpret_cast<const int*>(s_stage + dm.stage_off[STG_MAT_OFF]);
+      s_tabs.mat_nuc = reinterpret_cast<const int*>(s_stage + dm.stage_off[STG_MAT_NUC]);
+      s_tabs.mat_dens = reinterpret_cast<const double*>(s_stage + dm.stage_off[STG_MAT_DENS]);
+      s_tabs.mat_dens32 = reinterpret_cast<const float*>(s_stage + dm.stage_off[STG_MAT_DENS32]);
+    } else {
+      s_tabs.surf = dm.surf;
+      s_tabs.cell = dm.cell;
+      s_tabs.tok = dm.tok;
+      s_tabs.univ_off = dm.univ_off;
+      s_tabs.univ_cells = dm.univ_cells;
+      s_tabs.mat_off = dm.mat_off;
+      s_tabs.mat_nuc = dm.mat_nuc;
+      s_tabs.mat_dens = dm.mat_dens;
+      s_tabs.mat_dens32 = dm.mat_dens32;
+    }
+  }
+  __syncthreads();
+}
 
 // ------------------------------------------------------------------- RNG
 // src/random_lcg.cpp:32-44: one step of the generator and its output word
@@ -498,7 +594,7 @@ __device__ inline bool surf_sense(const DSurface& s, double x, double y, double 
 __device__ inline bool cell_contains(const DCell& c, double x, double y, double z, double ux, double uy,
   double uz, int on_surface)
 {
-  const int* t = dm.tok + c.tok_off;
+  const int* t = s_tabs.tok + c.tok_off;
   if (c.simple) {
     for (int k = 0; k < c.tok_len; ++k) {
       int token = t[k];
@@ -506,7 +602,7 @@ __device__ inline bool cell_contains(const DCell& c, double x, double y, double 
       } else if (-token == on_surface) {
         return false;
       } else {
-        bool sense = surf_sense(dm.surf[abs(token) - 1], x, y, z, ux, uy, uz);
+        bool sense = surf_sense(s_tabs.surf[abs(token) - 1], x, y, z, ux, uy, uz);
         if (sense != (token > 0)) return false;
       }
     }
@@ -520,7 +616,7 @@ __device__ inline bool cell_contains(const DCell& c, double x, double y, double 
       bool v;
       if (token == on_surface) v = true;
       else if (-token == on_surface) v = false;
-      else v = (surf_sense(dm.surf[abs(token) - 1], x, y, z, ux, uy, uz) == (token > 0));
+      else v = (surf_sense(s_tabs.surf[abs(token) - 1], x, y, z, ux, uy, uz) == (token > 0));
       stack = (stack & ~(1u << sp)) | (unsigned(v) << sp);
       ++sp;
     } else if (token == 2147483645) {  // OP_COMPLEMENT
@@ -545,11 +641,11 @@ __device__ inline void region_distance(const DCell& c, double x, double y, doubl
 {
   min_dist = INFTY;
   i_surf = 2147483647;
-  const int* t = dm.tok + c.tok_off;
+  const int* t = s_tabs.tok + c.tok_off;
   for (int k = 0; k < c.tok_len; ++k) {
     int token = t[k];
     if (token >= 2147483643) continue;
-    const DSurface& sf = dm.surf[abs(token) - 1];
+    const DSurface& sf = s_tabs.surf[abs(token) - 1];
     if (sf.type <= 2) {
       double r_i = sf.type == 0 ? x : (sf.type == 1 ? y : z);
       if (fabs(sf.c[0] - r_i) > bound) continue;
@@ -724,10 +820,10 @@ __device__ __forceinline__ void coord_reset(Geo& g, int l)
 __device__ __forceinline__ bool universe_find_cell(Geo& g, const int lvl)
 {
   int u = g.univ[lvl];
-  int a = dm.univ_off[u], b = dm.univ_off[u + 1];
+  int a = s_tabs.univ_off[u], b = s_tabs.univ_off[u + 1];
   for (int k = a; k < b; ++k) {
-    int ic = dm.univ_cells[k];
-    const DCell& c = dm.cell[ic];
+    int ic = s_tabs.univ_cells[k];
+    const DCell& c = s_tabs.cell[ic];
     if (c.universe != u) continue;
     if (cell_contains(c, g.r[lvl][0], g.r[lvl][1], g.r[lvl][2], g.u[0], g.u[1], g.u[2], g.surface)) {
       g.cell[lvl] = ic;
@@ -747,7 +843,7 @@ __device__ inline bool find_cell_inner(Geo& g, bool& lost_outer)
     if (lvl < start) continue;
     g.n_coord = lvl + 1;
     if (!universe_find_cell(g, lvl)) return false;
-    const DCell& c = dm.cell[g.cell[lvl]];
+    const DCell& c = s_tabs.cell[g.cell[lvl]];
     if (c.fill_type == 0) {
       g.material_last = g.material;
       g.material = c.fill;
@@ -807,7 +903,7 @@ __device__ inline void distance_to_boundary(const Geo& g, double& dist, int& sur
 #pragma unroll
   for (int i = MAXL - 1; i >= 0; --i) {
     if (i >= g.n_coord) continue;
-    const DCell& c = dm.cell[g.cell[i]];
+    const DCell& c = s_tabs.cell[g.cell[i]];
     const double* r = g.r[i];
     double b = (i == 0 && g.n_coord > 1) ? bound : INFTY;
     region_distance(c, r[0], r[1], r[2], g.u[0], g.u[1], g.u[2], g.surface, ds[i], ss[i], b);
@@ -832,7 +928,7 @@ __device__ inline void distance_to_boundary(const Geo& g, double& dist, int& sur
 #pragma unroll
   for (int i = 0; i < MAXL; i++) {
     if (i >= g.n_coord) break;
-    const DCell& c = dm.cell[g.cell[i]];
+    const DCell& c = s_tabs.cell[g.cell[i]];
     const double* r = g.r[i];
     double d_surf = ds[i];
     double d_lat = dl[i];
@@ -847,7 +943,7 @@ __device__ inline void distance_to_boundary(const Geo& g, double& dist, int& sur
           double hy = r[1] + d_surf * g.u[1];
           double hz = r[2] + d_surf * g.u[2];
           double nx, ny, nz;
-          surf_normal(dm.surf[abs(ss[i]) - 1], hx, hy, hz, nx, ny, nz);
+          surf_normal(s_tabs.surf[abs(ss[i]) - 1], hx, hy, hz, nx, ny, nz);
           surface = (g.u[0] * nx + g.u[1] * ny + g.u[2] * nz > 0) ? abs(ss[i]) : -abs(ss[i]);
         }
         trans = 13;
@@ -970,15 +1066,15 @@ __device__ __forceinline__ int log_union_index(double E)
 __device__ inline uint32_t material_xs(int mat, double E, double& tot, double& abs_)
 {
   int i_log = log_union_index(E);
-  int a = dm.mat_off[mat], b = dm.mat_off[mat + 1];
+  int a = s_tabs.mat_off[mat], b = s_tabs.mat_off[mat + 1];
   uint32_t h = 0;
   if (!dm.xs_fp32) {
     double t = 0.0, ab = 0.0;
     for (int k = a; k < b; ++k) {
-      int nuc = dm.mat_nuc[k];
+      int nuc = s_tabs.mat_nuc[k];
       Micro m = micro_xs64(nuc, i_log, E);
       h = h * 31u + static_cast<uint32_t>(m.i_grid);
-      double dens = dm.mat_dens[k];
+      double dens = s_tabs.mat_dens[k];
       t += dens * m.total;
       ab += dens * m.absorption;
     }
@@ -987,12 +1083,12 @@ __device__ inline uint32_t material_xs(int mat, double E, double& tot, double& a
   } else {
     float t = 0.0f, ab = 0.0f;
     for (int k = a; k < b; ++k) {
-      int nuc = dm.mat_nuc[k];
+      int nuc = s_tabs.mat_nuc[k];
       float mt, ma, f32;
       int ig;
       micro_xs32(nuc, i_log, E, mt, ma, ig, f32);
       h = h * 31u + static_cast<uint32_t>(ig);
-      float dens = dm.mat_dens32[k];
+      float dens = s_tabs.mat_dens32[k];
       t += dens * mt;
       ab += dens * ma;
     }

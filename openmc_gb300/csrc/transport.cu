@@ -46,6 +46,9 @@
 #include <string>
 #include <vector>
 
+#include <cooperative_groups.h>
+#include <cooperative_groups/reduce.h>
+
 #include "device.cuh"
 #include "host_model.h"
 #include "transport.h"
@@ -265,6 +268,28 @@ __device__ void mesh_bins_crossed(const DMesh& m, const double* r0, const double
   }
 }
 
+// Warp-aggregated FP64 atomic add (src/tallies/tally_scoring.cpp:1103-1106
+// adds each score with its own atomic): the lanes that execute this call
+// together and add to the same bin first combine their values, and one lane
+// per distinct bin issues the atomic.  The sum of a bin is the same up to
+// the order of FP64 additions, which atomics leave open anyway.
+__device__ __forceinline__ void atomic_add_agg(double* p, double v)
+{
+  namespace cg = cooperative_groups;
+  cg::coalesced_group active = cg::coalesced_threads();
+  if (active.size() == 1) {
+    atomicAdd(p, v);
+    return;
+  }
+  cg::coalesced_group peers = cg::labeled_partition(active, reinterpret_cast<unsigned long long>(p));
+  if (peers.size() == 1) {
+    atomicAdd(p, v);
+    return;
+  }
+  const double sum = cg::reduce(peers, v, cg::plus<double>());
+  if (peers.thread_rank() == 0) atomicAdd(p, sum);
+}
+
 // Cells of the particle's coordinate levels (cell filters match any level).
 struct LevelCells {
   int c[MAXL];
@@ -346,7 +371,7 @@ __device__ int score_tracklength(const double* r0, const double* r1, const doubl
         if (sc == 0) score = flux;
         else if (sc == 1) score = mt * flux;
         else score = ma * flux;
-        atomicAdd(val + index * ns + s, score * weight);
+        atomic_add_agg(val + index * ns + s, score * weight);
       }
     };
     for (int o = 0; o < n_off; ++o) {
@@ -399,7 +424,7 @@ __device__ void score_collision(const double* r, double E_last, double wgt_last,
       for (int s = 0; s < ns; ++s) {
         const int sc = T.score[s];
         const double score = sc == 0 ? flux : (sc == 1 ? mt * flux : ma * flux);
-        atomicAdd(val + index * ns + s, score);
+        atomic_add_agg(val + index * ns + s, score);
       }
     }
   }
@@ -794,6 +819,7 @@ __device__ bool revive_or_free(long long s, double wgt)
 // small, latency-bound launches every iteration.
 __global__ void __launch_bounds__(256) k_source_bank()
 {
+  tables_enter();
   const long long n = dq.src_n;
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<long long>(gridDim.x) * blockDim.x) {
@@ -881,7 +907,7 @@ __device__ void ev_xs(long long s, EvStats& st)
       db.macro_t[s] = t;
       db.macro_a[s] = a;
       st.calc += 1;
-      st.nuc += dm.mat_off[material + 1] - dm.mat_off[material];
+      st.nuc += s_tabs.mat_off[material + 1] - s_tabs.mat_off[material];
     }
   } else {
     db.macro_t[s] = 0.0;
@@ -1009,7 +1035,7 @@ __device__ void cross_lattice(Geo& g, long long s, int trans)
     g.li[lvl][1] += (trans / 3) % 3 - 1;
     g.li[lvl][2] += trans / 9 - 1;
     const int up = lvl - 1;
-    const DCell& cell = dm.cell[g.cell[up]];
+    const DCell& cell = s_tabs.cell[g.cell[up]];
     g.r[lvl][0] = g.r[up][0] - cell.tr[0];
     g.r[lvl][1] = g.r[up][1] - cell.tr[1];
     g.r[lvl][2] = g.r[up][2] - cell.tr[2];
@@ -1048,7 +1074,7 @@ __device__ int ev_surface_g(long long s, EvStats& st, Geo& g, double wgt, int bs
     mark_lost(s);
     wgt = 0.0;
   } else {
-    const DSurface& surf = dm.surf[abs(g.surface) - 1];
+    const DSurface& surf = s_tabs.surf[abs(g.surface) - 1];
     if (surf.bc == 1) {
       // src/particle.cpp:631-655
       atomicAdd(&dq.cnt->leakage, wgt);
@@ -1270,8 +1296,8 @@ __device__ int ev_collision(long long s, EvStats& st)
   double cutoff = prn(seed) * mt;
   int a = 0, b = 0;
   if (mat >= 0 && mat < dm.n_mat) {
-    a = dm.mat_off[mat];
-    b = dm.mat_off[mat + 1];
+    a = s_tabs.mat_off[mat];
+    b = s_tabs.mat_off[mat + 1];
   }
   int i_log = log_union_index(E);
   int chosen = -1;
@@ -1279,10 +1305,10 @@ __device__ int ev_collision(long long s, EvStats& st)
   if (!dm.xs_fp32) {
     double prob = 0.0;
     for (int k = a; k < b; ++k) {
-      int nuc = dm.mat_nuc[k];
+      int nuc = s_tabs.mat_nuc[k];
       st.coll_nuc += 1;
       Micro m = micro_xs64(nuc, i_log, E);
-      prob += dm.mat_dens[k] * m.total;
+      prob += s_tabs.mat_dens[k] * m.total;
       if (prob >= cutoff) {
         chosen = nuc;
         m_tot = m.total;
@@ -1293,12 +1319,12 @@ __device__ int ev_collision(long long s, EvStats& st)
   } else {
     float prob = 0.0f;
     for (int k = a; k < b; ++k) {
-      int nuc = dm.mat_nuc[k];
+      int nuc = s_tabs.mat_nuc[k];
       st.coll_nuc += 1;
       float t, ab, f32;
       int ig;
       micro_xs32(nuc, i_log, E, t, ab, ig, f32);
-      prob += dm.mat_dens32[k] * t;
+      prob += s_tabs.mat_dens32[k] * t;
       if (static_cast<double>(prob) >= cutoff) {
         chosen = nuc;
         m_tot = t;
@@ -1386,7 +1412,8 @@ __device__ __forceinline__ void flush_stats(const EvStats& st, int set)
 
 __global__ void __launch_bounds__(256) k_xs()
 {
-  if (dq.cnt->tail) return;
+  if (dq.cnt->tail) return;  // the same for every thread of the grid
+  tables_enter();
   const int n = dq.cnt->n_q;
   const int stride = gridDim.x * blockDim.x;
   for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
@@ -1409,6 +1436,7 @@ template<bool with_xs, bool with_surf>
 __global__ void __launch_bounds__(256, OMC_MINB_ADV) k_advance()
 {
   if (dq.cnt->tail) return;
+  tables_enter();
   const int n = dq.cnt->n_q;
   const int stride = gridDim.x * blockDim.x;
   for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
@@ -1428,6 +1456,7 @@ __global__ void __launch_bounds__(256, OMC_MINB_ADV) k_advance()
 __global__ void __launch_bounds__(256, OMC_MINB_SURF) k_surface()
 {
   if (dq.cnt->tail) return;
+  tables_enter();
   const int n = dq.cnt->n_surf;
   const int stride = gridDim.x * blockDim.x;
   for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
@@ -1444,6 +1473,7 @@ __global__ void __launch_bounds__(256, OMC_MINB_SURF) k_surface()
 __global__ void __launch_bounds__(256, OMC_MINB_COLL) k_collision()
 {
   if (dq.cnt->tail) return;
+  tables_enter();
   const int n = dq.cnt->n_coll;
   const int stride = gridDim.x * blockDim.x;
   for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
@@ -1465,6 +1495,7 @@ __global__ void __launch_bounds__(256, OMC_MINB_COLL) k_collision()
 __global__ void __launch_bounds__(128, 2) k_tail(int max_events)
 {
   if (!dq.cnt->tail) return;
+  tables_enter();
   const int n = dq.cnt->n_q;
   const int stride = gridDim.x * blockDim.x;
   for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
@@ -1493,6 +1524,7 @@ __global__ void __launch_bounds__(128, 2) k_tail(int max_events)
 // with the same event functions, then claims the next source index.
 __global__ void __launch_bounds__(128, 2) k_history()
 {
+  tables_enter();
   const long long s = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
   EvStats st {};
   if (s < db.cap) {
@@ -1542,6 +1574,7 @@ __global__ void k_refill_plan()
 
 __global__ void __launch_bounds__(256) k_refill()
 {
+  tables_enter();
   const int k = dq.cnt->refill_k;
   const int fb = dq.cnt->refill_free_base;
   const long long src = dq.cnt->refill_src;
@@ -1753,6 +1786,10 @@ struct GpuSim {
   int history = 0;      // history-based loop (settings.event_based false)
   long long tail_threshold = 1 << 15;  // measured best on the 17x17 lattice (2^17: +1 %, 2^19: +10 %)
   int tail_max_events = 1 << 16;
+  // dynamic shared memory of the event kernels: the staged tables (option
+  // stage_tables), or 0.  Off by default: the tables are a few KB and stay
+  // in L1, and the per-block copy cost 1.4 % of the lattice batch.
+  unsigned smem = 0;
   bool tallies_dirty = true;
   float last_batch_ms = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -1870,6 +1907,23 @@ static void build_model(GpuSim& G, const HModel& m, const GpuOptions& opt)
   d.mat_dens = dev_upload(mat_dens, own);
   d.mat_dens32 = dev_upload(mat_dens32, own);
   d.mat_id = dev_upload(mat_id, own);
+  // shared-memory layout of the per-event tables (tables_enter): each table
+  // starts on a 16-byte boundary; staged only when all of them fit
+  {
+    const size_t bytes[STG_N] = {surf.size() * sizeof(DSurface), cells.size() * sizeof(DCell),
+                                 tok.size() * sizeof(int), univ_off.size() * sizeof(int),
+                                 univ_cells.size() * sizeof(int), mat_off.size() * sizeof(int),
+                                 mat_nuc.size() * sizeof(int), mat_dens.size() * sizeof(double),
+                                 mat_dens32.size() * sizeof(float)};
+    size_t off = 0;
+    for (int k = 0; k < STG_N; ++k) {
+      d.stage_off[k] = static_cast<int>(off);
+      d.stage_words[k] = static_cast<int>(bytes[k] / 4);
+      off += (bytes[k] + 15) / 16 * 16;
+    }
+    d.stage_bytes = (opt.stage_tables && off <= OMC_STAGE_MAX_BYTES) ? static_cast<int>(off) : 0;
+    G.smem = static_cast<unsigned>(d.stage_bytes);
+  }
   std::vector<int> cell_id;
   for (const auto& c : m.cells) cell_id.push_back(c.id);
   d.cell_id = dev_upload(cell_id, own);
@@ -2113,7 +2167,7 @@ static void build_graph(GpuSim& G)
   // prologue
   CK(cudaStreamBeginCaptureToGraph(G.stream, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
   k_batch_init<<<nb, nt, 0, G.stream>>>(0);
-  if (G.queues.src_n > 0) k_source_bank<<<nb, nt, 0, G.stream>>>();
+  if (G.queues.src_n > 0) k_source_bank<<<nb, nt, G.smem, G.stream>>>();
   CK(cudaStreamEndCapture(G.stream, &graph));
   size_t n_nodes = 0;
   CK(cudaGraphGetNodes(graph, nullptr, &n_nodes));
@@ -2130,15 +2184,15 @@ static void build_graph(GpuSim& G)
   cudaGraph_t body = cp.conditional.phGraph_out[0];
   CK(cudaStreamBeginCaptureToGraph(G.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
   if (G.fuse & 1) {
-    if (G.fuse & 2) k_advance<true, true><<<nb, nt, 0, G.stream>>>();
-    else k_advance<true, false><<<nb, nt, 0, G.stream>>>();
+    if (G.fuse & 2) k_advance<true, true><<<nb, nt, G.smem, G.stream>>>();
+    else k_advance<true, false><<<nb, nt, G.smem, G.stream>>>();
   } else {
-    k_xs<<<nb, nt, 0, G.stream>>>();
-    k_advance<false, false><<<nb, nt, 0, G.stream>>>();
+    k_xs<<<nb, nt, G.smem, G.stream>>>();
+    k_advance<false, false><<<nb, nt, G.smem, G.stream>>>();
   }
-  if (!(G.fuse & 2)) k_surface<<<nb, nt, 0, G.stream>>>();
-  k_collision<<<nb, nt, 0, G.stream>>>();
-  k_tail<<<nb * 2, 128, 0, G.stream>>>(G.tail_max_events);
+  if (!(G.fuse & 2)) k_surface<<<nb, nt, G.smem, G.stream>>>();
+  k_collision<<<nb, nt, G.smem, G.stream>>>();
+  k_tail<<<nb * 2, 128, G.smem, G.stream>>>(G.tail_max_events);
   k_refill_plan<<<1, 1, 0, G.stream>>>();
   k_refill<<<nb, nt, 0, G.stream>>>();
   if (G.sort) {
@@ -2251,9 +2305,9 @@ static void launch_history_batch(GpuSim* G, int batch)
 {
   const int nb = G->blocks, nt = 256;
   k_batch_init<<<nb, nt, 0, G->stream>>>(batch);
-  if (G->queues.src_n > 0) k_source_bank<<<nb, nt, 0, G->stream>>>();
+  if (G->queues.src_n > 0) k_source_bank<<<nb, nt, G->smem, G->stream>>>();
   const long long threads = G->bank.cap;
-  k_history<<<static_cast<unsigned>((threads + 127) / 128), 128, 0, G->stream>>>();
+  k_history<<<static_cast<unsigned>((threads + 127) / 128), 128, G->smem, G->stream>>>();
   CK(cudaGetLastError());
 }
 
@@ -2316,7 +2370,7 @@ BatchStats gpu_run_batch_profiled(GpuSim* G, HModel& m, int batch, bool accumula
   }
   CK(cudaEventRecord(ev[0], S));
   k_batch_init<<<nb, nt, 0, S>>>(batch);
-  if (G->queues.src_n > 0) k_source_bank<<<nb, nt, 0, S>>>();
+  if (G->queues.src_n > 0) k_source_bank<<<nb, nt, G->smem, S>>>();
   CK(cudaEventRecord(ev[1], S));
   CK(cudaStreamSynchronize(S));
   acc[7] += span(0, 1);
@@ -2324,17 +2378,17 @@ BatchStats gpu_run_batch_profiled(GpuSim* G, HModel& m, int batch, bool accumula
   unsigned long long prev[7] = {0, 0, 0, 0, 0, 0, 0};
   for (int it = 0; it < (1 << 20); ++it) {
     CK(cudaEventRecord(ev[2], S));
-    if (!(G->fuse & 1)) k_xs<<<nb, nt, 0, S>>>();
+    if (!(G->fuse & 1)) k_xs<<<nb, nt, G->smem, S>>>();
     CK(cudaEventRecord(ev[3], S));
-    if (G->fuse == 3) k_advance<true, true><<<nb, nt, 0, S>>>();
-    else if (G->fuse == 1) k_advance<true, false><<<nb, nt, 0, S>>>();
-    else k_advance<false, false><<<nb, nt, 0, S>>>();
+    if (G->fuse == 3) k_advance<true, true><<<nb, nt, G->smem, S>>>();
+    else if (G->fuse == 1) k_advance<true, false><<<nb, nt, G->smem, S>>>();
+    else k_advance<false, false><<<nb, nt, G->smem, S>>>();
     CK(cudaEventRecord(ev[4], S));
-    if (!(G->fuse & 2)) k_surface<<<nb, nt, 0, S>>>();
+    if (!(G->fuse & 2)) k_surface<<<nb, nt, G->smem, S>>>();
     CK(cudaEventRecord(ev[5], S));
-    k_collision<<<nb, nt, 0, S>>>();
+    k_collision<<<nb, nt, G->smem, S>>>();
     CK(cudaEventRecord(ev[6], S));
-    k_tail<<<nb * 2, 128, 0, S>>>(G->tail_max_events);
+    k_tail<<<nb * 2, 128, G->smem, S>>>(G->tail_max_events);
     CK(cudaEventRecord(ev[11], S));
     k_refill_plan<<<1, 1, 0, S>>>();
     CK(cudaEventRecord(ev[7], S));

@@ -20,6 +20,7 @@ struct GpuOptions {
   int fuse = 3;                 // bit 0: cross-section event, bit 1: surface crossing, inside the advance kernel
   int split_slots = 0;          // split particles start in free slots with their own seeds
   int max_levels = 0;           // coordinate depth of the kernels (0: the model's, rounded up to 2 or 4)
+  int stage_tables = 0;         // copy the cell/surface/material tables into shared memory per block
 };
 
 struct BatchStats {

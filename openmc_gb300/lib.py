@@ -203,6 +203,7 @@ class _Settings:
     secondary_capacity = _DLLGlobal(C.c_int64, "openmc_gb300_secondary_capacity")
     split_to_slots = _DLLGlobal(C.c_int, "openmc_gb300_split_to_slots")
     max_levels = _DLLGlobal(C.c_int, "openmc_gb300_max_levels")
+    stage_tables = _DLLGlobal(C.c_int, "openmc_gb300_stage_tables")
 
     @property
     def seed(self):

@@ -23,9 +23,10 @@ CONT = ("E", "dist", "wgt")
 
 
 def run_gpu(path, n_trace=0, cap=256, fp32=False, in_flight=0, sort=True, batches=None, ww_on=None,
-            max_levels=0, fuse=3, event_based=True):
+            max_levels=0, fuse=3, event_based=True, stage_tables=0):
     from openmc_gb300 import lib
     lib.init(directory=path)
+    lib.settings.stage_tables = stage_tables
     try:
         lib.settings.event_based = event_based
         lib.settings.xs_fp32 = 1 if fp32 else 0
@@ -54,6 +55,7 @@ def run_gpu(path, n_trace=0, cap=256, fp32=False, in_flight=0, sort=True, batche
                           for t in lib.tally_ids()]
         return out
     finally:
+        lib.settings.stage_tables = 0
         lib.finalize()
 
 
@@ -200,12 +202,16 @@ def test_lattice_history_based_parity(lattice):
 
 def test_lattice_builds_agree(lattice):
     """The 2-level build (per-level state in registers) and the 4-level
-    build, and the unfused event kernels, give the same histories."""
+    build, the unfused event kernels, and the kernels reading their
+    geometry and material tables from shared-memory copies (event- and
+    history-based) give the same histories."""
     xml, path = lattice
     a = run_gpu(path, n_trace=600, cap=1024)
     b = run_gpu(path, n_trace=600, cap=1024, max_levels=4)
     c = run_gpu(path, n_trace=600, cap=1024, fuse=0)
-    for other in (b, c):
+    d = run_gpu(path, n_trace=600, cap=1024, stage_tables=1)
+    e = run_gpu(path, n_trace=600, cap=1024, stage_tables=1, event_based=False)
+    for other in (b, c, d, e):
         assert not trace_mismatches(a["trace"], other["trace"], 1024)
         for (ra, na), (rb, nb) in zip(a["tallies"], other["tallies"]):
             assert na == nb

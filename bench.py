@@ -140,8 +140,8 @@ def peaks():
 # OPENMC_GB300_LAUNCH_LOG counts (profiles/advance_surface_collision_lattice17_2M.md;
 # the unfused kernels' ratios come from the same capture of the earlier build).
 # Traffic per launch scales with the events a launch processes.
-TRAFFIC_PER_ALGORITHMIC_BYTE = {"xs+advance+surface": 2.338, "xs+advance": 1.376, "surface": 1.406,
-                                "collision": 1.254}
+TRAFFIC_PER_ALGORITHMIC_BYTE = {"xs+advance+surface": 2.333, "xs+advance": 1.376, "surface": 1.406,
+                                "collision": 1.258}
 
 
 def algorithmic_bytes(detail, levels, fp32):
@@ -326,16 +326,24 @@ def network_bench(rows=1 << 20, steps=20):
 def compare_tallies(a, b):
     """FP32-table tally (a) against the FP64-table tally (b), both
     (mean, std of the mean): share of bins scored by both within 3 combined
-    sigma, the largest |z|, and the relative difference of the summed flux
-    with its combined sigma."""
+    sigma, the largest |z|, the largest relative difference among the bins
+    both runs converged to 1 % relative error (with the largest combined
+    relative error of those bins beside it), and the relative difference of
+    the summed flux with its combined sigma."""
     ma, sa = (np.asarray(x, float).ravel() for x in a)
     mb, sb = (np.asarray(x, float).ravel() for x in b)
     both = (sa > 0) & (sb > 0)
     z = np.abs(ma - mb)[both] / np.hypot(sa, sb)[both]
     ta, tb = ma.sum(), mb.sum()
     st = np.sqrt((sa ** 2).sum() + (sb ** 2).sum())
+    conv = both & (sa < 0.01 * np.abs(ma)) & (sb < 0.01 * np.abs(mb))
+    rel = np.abs(ma - mb)[conv] / np.abs(mb)[conv]
+    crel = np.hypot(sa, sb)[conv] / np.abs(mb)[conv]
     return {"bins_scored_by_both": int(both.sum()), "share_within_3_sigma": float((z <= 3).mean()),
-            "max_abs_z": float(z.max()), "total_rel_diff": float((ta - tb) / tb),
+            "max_abs_z": float(z.max()), "converged_bins": int(conv.sum()),
+            "max_rel_diff_converged": float(rel.max()) if rel.size else None,
+            "max_combined_rel_err_converged": float(crel.max()) if crel.size else None,
+            "total_rel_diff": float((ta - tb) / tb),
             "total_z": float(abs(ta - tb) / st) if st > 0 else None}
 
 

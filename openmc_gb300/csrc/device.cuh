@@ -45,6 +45,11 @@ struct DCell {
   int universe, fill_type, fill, tok_off, tok_len, simple;
 };
 
+// FP64 cross-section row of one grid point (32 B, two 16-byte loads)
+struct alignas(16) XsRow64 {
+  double total, absorption, elastic, unused;
+};
+
 struct DLattice {
   double ll[3], pitch[3];
   int n[3];
@@ -83,7 +88,7 @@ struct DModel {
   // nuclear data
   const long long* nuc_off;  // grid offsets
   const double* energy;
-  const double4* xs64;  // (total, absorption, elastic, 0) per grid point
+  const XsRow64* xs64;  // (total, absorption, elastic, 0) per grid point
   const float4* xs32;
   const int* grid_index;  // [n_nuc][M+1]
   const double* awr;
@@ -1000,12 +1005,13 @@ __device__ __forceinline__ int nuclide_grid(int nuc, int i_log, double E, double
   return i_grid;
 }
 
-__device__ __forceinline__ double4 ldg4(const double4* p)
+// one FP64 row as two 16-byte read-only loads
+__device__ __forceinline__ XsRow64 ldg_row(const XsRow64* p)
 {
   const double2* q = reinterpret_cast<const double2*>(p);
-  double2 a = __ldg(q);
-  double2 b = __ldg(q + 1);
-  return make_double4(a.x, a.y, b.x, b.y);
+  const double2 a = __ldg(q);
+  const double2 b = __ldg(q + 1);
+  return XsRow64 {a.x, a.y, b.x, b.y};
 }
 
 __device__ __forceinline__ Micro micro_xs64(int nuc, int i_log, double E)
@@ -1014,11 +1020,11 @@ __device__ __forceinline__ Micro micro_xs64(int nuc, int i_log, double E)
   double e0, e1;
   m.i_grid = nuclide_grid(nuc, i_log, E, e0, e1);
   m.f = (E - e0) / (e1 - e0);
-  const double4* xs = dm.xs64 + dm.nuc_off[nuc];
-  double4 a = ldg4(xs + m.i_grid);
-  double4 b = ldg4(xs + m.i_grid + 1);
-  m.total = (1.0 - m.f) * a.x + m.f * b.x;
-  m.absorption = (1.0 - m.f) * a.y + m.f * b.y;
+  const XsRow64* xs = dm.xs64 + dm.nuc_off[nuc];
+  const XsRow64 a = ldg_row(xs + m.i_grid);
+  const XsRow64 b = ldg_row(xs + m.i_grid + 1);
+  m.total = (1.0 - m.f) * a.total + m.f * b.total;
+  m.absorption = (1.0 - m.f) * a.absorption + m.f * b.absorption;
   return m;
 }
 

@@ -1869,13 +1869,13 @@ static void build_model(GpuSim& G, const HModel& m, const GpuOptions& opt)
   // nuclear data: energies FP64, rows (total, absorption, elastic, 0)
   std::vector<long long> nuc_off {0};
   std::vector<double> energy, awr, kT;
-  std::vector<double4> xs64;
+  std::vector<XsRow64> xs64;
   std::vector<float4> xs32;
   std::vector<int> grid_index;
   for (const auto& n : m.nuclides) {
     energy.insert(energy.end(), n.energy.begin(), n.energy.end());
     for (size_t k = 0; k < n.energy.size(); ++k) {
-      xs64.push_back(make_double4(n.total[k], n.absorption[k], n.elastic[k], 0.0));
+      xs64.push_back(XsRow64 {n.total[k], n.absorption[k], n.elastic[k], 0.0});
       xs32.push_back(make_float4(static_cast<float>(n.total[k]), static_cast<float>(n.absorption[k]),
         static_cast<float>(n.elastic[k]), 0.0f));
     }

@@ -609,6 +609,8 @@ class Settings:
         self.max_history_splits = None
         self.energy_cutoff = None
         self.survival_biasing = False
+        self.max_lost_particles = None
+        self.rel_max_lost_particles = None
         for k, v in kw.items():
             setattr(self, k, v)
 
@@ -638,6 +640,10 @@ class Settings:
             ET.SubElement(el, "log_grid_bins").text = str(int(self.log_grid_bins))
         if self.max_history_splits is not None:
             ET.SubElement(el, "max_history_splits").text = str(int(self.max_history_splits))
+        if self.max_lost_particles is not None:
+            ET.SubElement(el, "max_lost_particles").text = str(int(self.max_lost_particles))
+        if self.rel_max_lost_particles is not None:
+            ET.SubElement(el, "rel_max_lost_particles").text = repr(float(self.rel_max_lost_particles))
         if self.energy_cutoff is not None:
             co = ET.SubElement(el, "cutoff")
             ET.SubElement(co, "energy_neutron").text = repr(float(self.energy_cutoff))

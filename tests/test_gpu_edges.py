@@ -1,5 +1,7 @@
 """Edge cases on the GPU: a single history, a single particle slot, a model
-without tallies, empty lookups, a one-row network."""
+without tallies, empty lookups, a one-row network, lost particles (a
+geometry with a hole) and a full split ring, the last two ending as error
+codes of openmc_next_batch."""
 import numpy as np
 import pytest
 
@@ -91,3 +93,79 @@ def test_tallies_out_written(built, tmp_path):
     assert fields[0] == "Flux" and fields[2] == "+/-"
     assert abs(float(fields[1]) - mean.ravel()[0]) <= 1e-5 * abs(mean.ravel()[0]) + 1e-300
     assert abs(float(fields[3]) - std.ravel()[0]) <= 1e-5 * abs(std.ravel()[0]) + 1e-300
+
+
+def _holed_cube(tmp_path, **settings):
+    """The point cube without its annulus cell (1 < r < 3 cm): particles that
+    leave the inner cylinder find no cell there and are lost."""
+    from openmc_gb300 import configs
+    m, path = configs.point_cube(tmp_path, particles=400, batches=1, n_points=400, mesh_dim=(3, 3, 3), n_ebins=4)
+    del m.geometry.root_universe.cells[1]
+    for k, v in settings.items():
+        setattr(m.settings, k, v)
+    return m.export_to_model_xml(path), path
+
+
+def test_lost_particles_counted_like_the_oracle(built, tmp_path):
+    """A particle that finds no cell is killed and counted
+    (src/particle.cpp mark_as_lost); with the limits raised the batch ends
+    normally and the count is the oracle's."""
+    from openmc_gb300 import lib
+    import oracle
+    xml, path = _holed_cube(tmp_path, max_lost_particles=10 ** 9, rel_max_lost_particles=1.0)
+    lib.init(directory=path)
+    saved = lib.settings.xs_fp32
+    try:
+        lib.settings.xs_fp32 = 0
+        lib.simulation_init()
+        lib.next_batch()
+        b = lib.last_batch()
+        lib.simulation_finalize()
+    finally:
+        lib.settings.xs_fp32 = saved
+        lib.finalize()
+    o = oracle.Oracle(xml)
+    o.run(threads=1)
+    assert b["lost"] > 0 and b["done"] == 400
+    assert b["lost"] == o.globals()[2]
+
+
+def test_lost_particles_beyond_the_limit_are_a_geometry_error(built, tmp_path):
+    """More lost particles than max_lost_particles (default 10) and
+    rel_max_lost_particles x histories: OPENMC_E_GEOMETRY."""
+    from openmc_gb300 import lib
+    _, path = _holed_cube(tmp_path)
+    lib.init(directory=path)
+    try:
+        lib.simulation_init()
+        with pytest.raises(lib.GeometryError):
+            lib.next_batch()
+    finally:
+        lib.finalize()
+
+
+def test_full_split_ring_is_an_allocation_error(built, tmp_path):
+    """Windows falling 10x per 1 cm mesh bin split every particle that moves
+    deeper (windows are scaled by the particle's birth window,
+    src/weight_windows.cpp:56-146, so only their variation matters); a
+    16-entry split ring fills and the batch ends with OPENMC_E_ALLOCATE
+    (nothing is written past the ring, and the split copies waiting in it
+    are not started)."""
+    from openmc_gb300 import configs, lib
+    m, path = configs.shield(tmp_path, particles=2000, batches=1, n_points=400, tally_mesh_windows=True)
+    m.export_to_model_xml(path)
+    lib.init(directory=path)
+    saved = (lib.settings.split_to_slots, lib.settings.secondary_capacity)
+    try:
+        lib.settings.split_to_slots = 1
+        lib.settings.secondary_capacity = 16
+        lo, _ = lib.WeightWindows(0).bounds
+        ix = np.arange(lo.size) % 200  # x index of the 200 x 10 x 10 mesh bin (x fastest)
+        lower = 0.1 ** ix
+        lib.WeightWindows(0).bounds = (lower, 5.0 * lower)
+        lib.simulation_init()
+        with pytest.raises(lib.AllocationError):
+            lib.next_batch()
+    finally:
+        lib.settings.split_to_slots, lib.settings.secondary_capacity = saved
+        lib.finalize()

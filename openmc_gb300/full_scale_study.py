@@ -6,8 +6,9 @@ transport with FP64 tables on the same GPU.
 By default plain transport with FP32 tables runs against plain transport
 with FP64 tables.  With --learned-particles, a plain FP32 pilot fills a
 coarse window-mesh flux tally, the importance network is fitted to it
-(``learned_ww.fit``), and a run with those windows (FP32 tables,
-split-to-slots) replaces the plain FP32 run; the windowed run may use fewer
+(``learned_ww.fit``; with --magic, OpenMC's MAGIC generator runs on it
+instead), and a run with those windows (FP32 tables, split-to-slots)
+replaces the plain FP32 run; the windowed run may use fewer
 histories per batch, the figures of merit being per unit device time.
 Windows normalised like MAGIC's ask for the same particle density in every
 bin, which around a 100 cm shield (100x the core's volume, flux falling
@@ -56,7 +57,7 @@ def _run(particles, batches, windows_on, fp32, log):
 
 
 def run(directory, particles=100_000_000, batches=3, pilot_particles=10_000_000, pilot_batches=2,
-        steps=2000, n_points=11303, ww_mesh_dim=(44, 44, 10), learned_particles=0):
+        steps=2000, n_points=11303, ww_mesh_dim=(44, 44, 10), learned_particles=0, magic=False):
     m, path = configs.full_scale(directory, particles=particles, batches=100_000, n_points=n_points,
                                  ww_mesh_dim=ww_mesh_dim, ww_groups=GROUPS)
     m.export_to_model_xml(path)
@@ -74,14 +75,20 @@ def run(directory, particles=100_000_000, batches=3, pilot_particles=10_000_000,
             lib.settings.secondary_capacity = 1 << 26
         if learned_particles:
             pilot = _run(pilot_particles, pilot_batches, False, True, "pilot")
-            mean, std = pilot["tallies"][2][0][:, 0], pilot["tallies"][2][1][:, 0]
-            fit = learned_ww.fit(mean, std, geom, steps=steps)
-            out["learned_fit"] = {"pairs": fit.n_pairs, "loss_first": float(fit.loss[0]),
-                                  "loss_last": float(fit.loss[-1]), "train_ms": fit.train_ms}
-            lib.WeightWindows(0).bounds = (fit.lower, fit.upper)
+            if magic:
+                # OpenMC's own generator on the same pilot tally
+                lib.WeightWindows(0).update_magic(lib.tally_index(lib.tally_ids()[2]), "mean", 1.0, 5.0)
+                out["magic_window_bins"] = int((lib.WeightWindows(0).bounds[0] > 0).sum())
+                first_name = "magic_fp32"
+            else:
+                mean, std = pilot["tallies"][2][0][:, 0], pilot["tallies"][2][1][:, 0]
+                fit = learned_ww.fit(mean, std, geom, steps=steps)
+                out["learned_fit"] = {"pairs": fit.n_pairs, "loss_first": float(fit.loss[0]),
+                                      "loss_last": float(fit.loss[-1]), "train_ms": fit.train_ms}
+                lib.WeightWindows(0).bounds = (fit.lower, fit.upper)
+                first_name = "learned_fp32"
             lp = learned_particles
-            first = _run(lp, batches, True, True, "learned fp32")
-            first_name = "learned_fp32"
+            first = _run(lp, batches, True, True, first_name.replace("_", " "))
         else:
             lp = particles
             first = _run(lp, batches, False, True, "plain fp32")
@@ -103,13 +110,17 @@ def run(directory, particles=100_000_000, batches=3, pilot_particles=10_000_000,
     # bins both runs converged to 10 % relative error, where the batch
     # estimates of sigma are themselves reliable
     conv = both & (sa < 0.1 * np.abs(ma)) & (sb < 0.1 * np.abs(mb))
-    zc = np.abs(ma - mb)[conv] / np.hypot(sa, sb)[conv]
+    zs = (ma - mb)[conv] / np.hypot(sa, sb)[conv]  # signed: a bias shows as a shifted mean
+    zc = np.abs(zs)
     out["assembly_tally"] = {"bins": int(ma.size), "scored_by_both": int(both.sum()),
                              "share_within_3_sigma": float((z <= 3).mean()) if z.size else None,
                              "max_z": float(z.max()) if z.size else None,
                              "converged_by_both": int(conv.sum()),
                              "converged_share_within_3_sigma": float((zc <= 3).mean()) if zc.size else None,
-                             "converged_max_z": float(zc.max()) if zc.size else None}
+                             "converged_max_z": float(zc.max()) if zc.size else None,
+                             "converged_mean_signed_z": float(zs.mean()) if zs.size else None,
+                             "converged_share_above_3_sigma": float((zs > 3).mean()) if zs.size else None,
+                             "converged_share_below_3_sigma": float((zs < -3).mean()) if zs.size else None}
     # flux and FOM per shell along the x slab
     (la, lsa), (lb_, lsb) = learned["tallies"][1], plain["tallies"][1]
     la, lsa, lb_, lsb = la.ravel(), lsa.ravel(), lb_.ravel(), lsb.ravel()
@@ -137,9 +148,12 @@ def main():
     ap.add_argument("--learned-particles", type=int, default=0,
                     help="run learned windows (FP32) with this many histories per batch against plain FP64; "
                          "default: plain FP32 against plain FP64")
+    ap.add_argument("--magic", action="store_true",
+                    help="with --learned-particles: MAGIC windows from the same pilot instead of learned ones")
     a = ap.parse_args()
     out = run(Path(a.dir), particles=a.particles, batches=a.batches, pilot_particles=a.pilot_particles,
-              pilot_batches=a.pilot_batches, steps=a.steps, learned_particles=a.learned_particles or None)
+              pilot_batches=a.pilot_batches, steps=a.steps, learned_particles=a.learned_particles or None,
+              magic=a.magic)
     print(json.dumps(out))
 
 

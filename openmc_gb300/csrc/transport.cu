@@ -37,6 +37,10 @@
 // cutoff, lost particle): their secondaries are still revived.
 // Particle time is not tracked: no time cutoff or time filter is supported,
 // and time does not feed any other quantity of this path.
+//
+// Every kernel that reads the cell, surface, universe or material tables
+// sets the block's table pointers first (tables_enter, device.cuh); tally
+// bins are incremented with warp-aggregated FP64 atomics (atomic_add_agg).
 #include <algorithm>
 #include <cmath>
 #include <cstdio>

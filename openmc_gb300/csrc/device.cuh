@@ -1029,19 +1029,20 @@ __device__ __forceinline__ Micro micro_xs64(int nuc, int i_log, double E)
 }
 
 // FP32 tables: the grid search stays FP64 (E against FP64 grid energies);
-// the interpolation factor is formed in FP32 from the two FP64 differences
-// E - e0 and e1 - e0 (each rounded once to FP32), and the interpolation is
-// written a + f (b - a), which stays accurate when f leaves [0, 1] (energies
-// below the first or above the last grid point extrapolate); (1 - f) a + f b
-// cancels catastrophically in FP32 there.
+// the interpolation factor is the FP64 difference E - e0 rounded to FP32
+// times the interval's reciprocal width stored (rounded to FP32) in the
+// row's last slot, and the interpolation is written a + f (b - a), which
+// stays accurate when f leaves [0, 1] (energies below the first or above the
+// last grid point extrapolate); (1 - f) a + f b cancels catastrophically in
+// FP32 there.
 __device__ __forceinline__ void micro_xs32(int nuc, int i_log, double E, float& t, float& a_out, int& i_grid, float& f32)
 {
   double e0, e1;
   i_grid = nuclide_grid(nuc, i_log, E, e0, e1);
-  f32 = static_cast<float>(E - e0) / static_cast<float>(e1 - e0);
   const float4* xs = dm.xs32 + dm.nuc_off[nuc];
   float4 a = __ldg(xs + i_grid);
   float4 b = __ldg(xs + i_grid + 1);
+  f32 = static_cast<float>(E - e0) * a.w;
   t = a.x + f32 * (b.x - a.x);
   a_out = a.y + f32 * (b.y - a.y);
 }

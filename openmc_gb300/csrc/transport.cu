@@ -1870,7 +1870,9 @@ static void build_model(GpuSim& G, const HModel& m, const GpuOptions& opt)
   d.n_coord_levels = m.n_coord_levels;
   if (m.n_coord_levels > MAXL) throw std::runtime_error("geometry nests deeper than the supported coordinate levels");
 
-  // nuclear data: energies FP64, rows (total, absorption, elastic, 0)
+  // nuclear data: energies FP64, rows (total, absorption, elastic, 0); the
+  // FP32 rows carry 1 / (e[k+1] - e[k]) in their last slot (0 at the last
+  // point and at duplicate points, whose interval is never interpolated)
   std::vector<long long> nuc_off {0};
   std::vector<double> energy, awr, kT;
   std::vector<XsRow64> xs64;
@@ -1880,8 +1882,9 @@ static void build_model(GpuSim& G, const HModel& m, const GpuOptions& opt)
     energy.insert(energy.end(), n.energy.begin(), n.energy.end());
     for (size_t k = 0; k < n.energy.size(); ++k) {
       xs64.push_back(XsRow64 {n.total[k], n.absorption[k], n.elastic[k], 0.0});
+      const double de = k + 1 < n.energy.size() ? n.energy[k + 1] - n.energy[k] : 0.0;
       xs32.push_back(make_float4(static_cast<float>(n.total[k]), static_cast<float>(n.absorption[k]),
-        static_cast<float>(n.elastic[k]), 0.0f));
+        static_cast<float>(n.elastic[k]), de > 0.0 ? static_cast<float>(1.0 / de) : 0.0f));
     }
     nuc_off.push_back(static_cast<long long>(energy.size()));
     grid_index.insert(grid_index.end(), n.grid_index.begin(), n.grid_index.end());

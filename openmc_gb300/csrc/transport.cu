@@ -105,14 +105,15 @@ __device__ void mark_lost(long long s)
 
 // ------------------------------------------------------ mesh raytrace
 // src/mesh.cpp:1328-1369 RegularMesh helpers
-// ceil((r - lower_left) / width) decided in FP32: the quotient estimated in
-// FP32 (relative error below 1e-6 for |q| < 2^20) settles the ceiling when it
-// lies at least 1e-4 + 2e-6 |q| from an integer, i.e. when r is at least
-// 1e-4 widths from a cell face.  Returns false otherwise.
+// ceil((r - lower_left) / width) decided in FP32: the quotient estimated as
+// FP32(r - lower_left) x FP32(1 / width) (three roundings, relative error
+// below 2e-7) settles the ceiling when it lies at least 1e-4 + 2e-6 |q| from
+// an integer (and |q| < 2^20), i.e. when r is at least 1e-4 widths from a
+// cell face.  Returns false otherwise.
 __device__ __forceinline__ bool mesh_index_fp32(const DMesh& m, double r, int i, int& idx)
 {
   const double t = r - m.ll[i];
-  const float q32 = __fdiv_rn(static_cast<float>(t), static_cast<float>(m.width[i]));
+  const float q32 = __fmul_rn(static_cast<float>(t), m.inv_width32[i]);
   const float fr = q32 - rintf(q32);
   if (fabsf(q32) < 1048576.0f && fabsf(fr) > 1e-4f + 2e-6f * fabsf(q32)) {
     idx = static_cast<int>(ceilf(q32));
@@ -1996,6 +1997,7 @@ static void build_model(GpuSim& G, const HModel& m, const GpuOptions& opt)
     for (int j = 0; j < 3; ++j) {
       meshes[k].ll[j] = m.meshes[k].ll[j];
       meshes[k].width[j] = m.meshes[k].width[j];
+      meshes[k].inv_width32[j] = m.meshes[k].width[j] > 0.0 ? static_cast<float>(1.0 / m.meshes[k].width[j]) : 0.0f;
       meshes[k].shape[j] = m.meshes[k].shape[j];
     }
     meshes[k].ndim = m.meshes[k].ndim;

@@ -56,6 +56,31 @@ def _run(particles, batches, windows_on, fp32, log):
     return {"device_s": dev_ms * 1e-3, "events": events, "tallies": res}
 
 
+def agreement(a, b, converged_rel=0.1):
+    """Bin-by-bin agreement of tally a with tally b, each (mean, std of the
+    mean): share of the bins scored by both within 3 combined sigma and the
+    largest |z|; the same over the bins both converged to converged_rel
+    relative error (where the batch estimates of sigma are themselves
+    reliable), with the mean signed z and the shares beyond +3 and -3 sigma
+    (a bias of a shows as a shifted mean and a one-sided excess)."""
+    ma, sa = (np.asarray(x, float).ravel() for x in a)
+    mb, sb = (np.asarray(x, float).ravel() for x in b)
+    both = (sa > 0) & (sb > 0)
+    z = np.abs(ma - mb)[both] / np.hypot(sa, sb)[both]
+    conv = both & (sa < converged_rel * np.abs(ma)) & (sb < converged_rel * np.abs(mb))
+    zs = (ma - mb)[conv] / np.hypot(sa, sb)[conv]
+    zc = np.abs(zs)
+    return {"bins": int(ma.size), "scored_by_both": int(both.sum()),
+            "share_within_3_sigma": float((z <= 3).mean()) if z.size else None,
+            "max_z": float(z.max()) if z.size else None,
+            "converged_by_both": int(conv.sum()),
+            "converged_share_within_3_sigma": float((zc <= 3).mean()) if zc.size else None,
+            "converged_max_z": float(zc.max()) if zc.size else None,
+            "converged_mean_signed_z": float(zs.mean()) if zs.size else None,
+            "converged_share_above_3_sigma": float((zs > 3).mean()) if zs.size else None,
+            "converged_share_below_3_sigma": float((zs < -3).mean()) if zs.size else None}
+
+
 def run(directory, particles=100_000_000, batches=3, pilot_particles=10_000_000, pilot_batches=2,
         steps=2000, n_points=11303, ww_mesh_dim=(44, 44, 10), learned_particles=0, magic=False):
     m, path = configs.full_scale(directory, particles=particles, batches=100_000, n_points=n_points,
@@ -103,24 +128,7 @@ def run(directory, particles=100_000_000, batches=3, pilot_particles=10_000_000,
         out[name] = {"particles_per_batch": n, "device_s": r["device_s"], "events": r["events"],
                      "particles_per_s": n * batches / r["device_s"]}
     # agreement of the 3e7-bin assembly tally
-    (ma, sa), (mb, sb) = learned["tallies"][0], plain["tallies"][0]
-    ma, sa, mb, sb = ma.ravel(), sa.ravel(), mb.ravel(), sb.ravel()
-    both = (sa > 0) & (sb > 0)
-    z = np.abs(ma - mb)[both] / np.hypot(sa, sb)[both]
-    # bins both runs converged to 10 % relative error, where the batch
-    # estimates of sigma are themselves reliable
-    conv = both & (sa < 0.1 * np.abs(ma)) & (sb < 0.1 * np.abs(mb))
-    zs = (ma - mb)[conv] / np.hypot(sa, sb)[conv]  # signed: a bias shows as a shifted mean
-    zc = np.abs(zs)
-    out["assembly_tally"] = {"bins": int(ma.size), "scored_by_both": int(both.sum()),
-                             "share_within_3_sigma": float((z <= 3).mean()) if z.size else None,
-                             "max_z": float(z.max()) if z.size else None,
-                             "converged_by_both": int(conv.sum()),
-                             "converged_share_within_3_sigma": float((zc <= 3).mean()) if zc.size else None,
-                             "converged_max_z": float(zc.max()) if zc.size else None,
-                             "converged_mean_signed_z": float(zs.mean()) if zs.size else None,
-                             "converged_share_above_3_sigma": float((zs > 3).mean()) if zs.size else None,
-                             "converged_share_below_3_sigma": float((zs < -3).mean()) if zs.size else None}
+    out["assembly_tally"] = agreement(learned["tallies"][0], plain["tallies"][0])
     # flux and FOM per shell along the x slab
     (la, lsa), (lb_, lsb) = learned["tallies"][1], plain["tallies"][1]
     la, lsa, lb_, lsb = la.ravel(), lsa.ravel(), lb_.ravel(), lsb.ravel()

@@ -151,6 +151,14 @@ int openmc_gb300_get_trace(void* records, int32_t* counts);
 int openmc_gb300_set_weight_windows_on(int on);
 /* [n_nuclides, n_materials, n_cells, n_surfaces, n_tallies, log_grid_bins, batches, coord_levels] */
 int openmc_gb300_model_info(int64_t* out);
+/* macroscopic total and absorption cross sections of the initialised
+ * simulation's materials (0-based material indices) at energies E [eV],
+ * evaluated on the device by the transport kernels' own lookup and tables
+ * (FP32 or FP64 as openmc_gb300_xs_fp32 chose), with the hash of the
+ * nuclides' grid indices; Material::calculate_neutron_xs
+ * (src/material.cpp:829-901) per pair.  Host arrays of length n. */
+int openmc_gb300_material_xs(int64_t n, const int32_t* material, const double* E, double* total,
+                             double* absorption, uint32_t* grid_hash);
 
 /* macroscopic-XS lookup on flat 5-channel tables; counterpart of
  * Material::calculate_neutron_xs (src/material.cpp:829-901) per lookup */

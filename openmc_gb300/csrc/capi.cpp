@@ -850,6 +850,23 @@ int openmc_gb300_set_weight_windows_on(int on)
   return 0;
 }
 
+int openmc_gb300_material_xs(int64_t n, const int32_t* material, const double* E, double* total,
+                             double* absorption, uint32_t* grid_hash)
+{
+  State& s = S();
+  if (!s.gpu) return fail(OPENMC_E_ALLOCATE, "Simulation has not been initialized.");
+  if (n < 0) return fail(OPENMC_E_INVALID_SIZE, "Negative number of lookups.");
+  const int n_mat = static_cast<int>(s.model.materials.size());
+  for (int64_t i = 0; i < n; ++i)
+    if (material[i] < 0 || material[i] >= n_mat) return fail(OPENMC_E_OUT_OF_BOUNDS, "Material index out of range.");
+  try {
+    gpu_material_xs(s.gpu, n, material, E, total, absorption, grid_hash);
+  } catch (const std::exception& e) {
+    return fail(OPENMC_E_UNASSIGNED, e.what());
+  }
+  return 0;
+}
+
 int openmc_gb300_model_info(int64_t* out)
 {
   const HModel& m = S().model;

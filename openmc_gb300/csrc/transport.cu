@@ -1728,6 +1728,25 @@ __global__ void k_finish_iter(cudaGraphConditionalHandle handle)
 // same epilogue for the profiled (graph-free) batch loop
 __global__ void k_finish_iter_host() { finish_iter_common(); }
 
+// Macroscopic cross sections at (material index, E) pairs through the same
+// lookup the event kernels run (Material::calculate_neutron_xs,
+// src/material.cpp:829-901), for checking the tables against the oracle.
+__global__ void __launch_bounds__(256) k_material_xs(long long n, const int* mat, const double* E, double* tot,
+  double* abs_, unsigned* hash)
+{
+  tables_enter();
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int m = mat[i];
+    double t = 0.0, a = 0.0;
+    uint32_t h = 0xffffffffu;
+    if (m >= 0 && m < dm.n_mat) h = material_xs(m, E[i], t, a);
+    tot[i] = t;
+    abs_[i] = a;
+    hash[i] = h;
+  }
+}
+
 // Tally::accumulate (src/tallies/tally.cpp:821-880)
 __global__ void k_accumulate(double* value, double* sum, double* sum_sq, long long n, double norm)
 {
@@ -2500,6 +2519,39 @@ void gpu_set_ww_on(GpuSim* G, bool on)
 }
 
 long long gpu_capacity(GpuSim* G) { return G->bank.cap; }
+
+void gpu_material_xs(GpuSim* G, long long n, const int* mat, const double* E, double* total, double* absorption,
+                     unsigned* grid_hash)
+{
+  if (n <= 0) return;
+  struct Scratch {
+    int* mat = nullptr;
+    double *E = nullptr, *t = nullptr, *a = nullptr;
+    unsigned* h = nullptr;
+    ~Scratch()
+    {
+      cudaFree(mat);
+      cudaFree(E);
+      cudaFree(t);
+      cudaFree(a);
+      cudaFree(h);
+    }
+  } d;
+  CK(cudaMalloc(&d.mat, n * sizeof(int)));
+  CK(cudaMalloc(&d.E, n * sizeof(double)));
+  CK(cudaMalloc(&d.t, n * sizeof(double)));
+  CK(cudaMalloc(&d.a, n * sizeof(double)));
+  CK(cudaMalloc(&d.h, n * sizeof(unsigned)));
+  CK(cudaMemcpyAsync(d.mat, mat, n * sizeof(int), cudaMemcpyHostToDevice, G->stream));
+  CK(cudaMemcpyAsync(d.E, E, n * sizeof(double), cudaMemcpyHostToDevice, G->stream));
+  const long long blocks = std::min<long long>((n + 255) / 256, G->blocks);
+  k_material_xs<<<static_cast<unsigned>(blocks), 256, G->smem, G->stream>>>(n, d.mat, d.E, d.t, d.a, d.h);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(total, d.t, n * sizeof(double), cudaMemcpyDeviceToHost, G->stream));
+  CK(cudaMemcpyAsync(absorption, d.a, n * sizeof(double), cudaMemcpyDeviceToHost, G->stream));
+  CK(cudaMemcpyAsync(grid_hash, d.h, n * sizeof(unsigned), cudaMemcpyDeviceToHost, G->stream));
+  CK(cudaStreamSynchronize(G->stream));
+}
 
 }  // namespace OMC_NS
 }  // namespace omc

@@ -60,6 +60,8 @@ struct BatchStats {
   void gpu_set_ww_bounds(GpuSim* g, const double* lower, const double* upper, long long n); \
   void gpu_set_ww_on(GpuSim* g, bool on);                                                   \
   long long gpu_capacity(GpuSim* g);                                                        \
+  void gpu_material_xs(GpuSim* g, long long n, const int* mat, const double* E, double* total, \
+                       double* absorption, unsigned* grid_hash);                               \
   }
 
 OMC_GPU_API(l2)
@@ -78,6 +80,11 @@ void gpu_get_trace(GpuSim* g, void* records, int* counts);
 void gpu_set_ww_bounds(GpuSim* g, const double* lower, const double* upper, long long n);
 void gpu_set_ww_on(GpuSim* g, bool on);
 long long gpu_capacity(GpuSim* g);
+// Macroscopic total and absorption cross sections (and the nuclide grid-index
+// hash) of the model's materials at (material index, E) pairs, evaluated on
+// the device by the transport kernels' own lookup (host arrays of length n).
+void gpu_material_xs(GpuSim* g, long long n, const int* mat, const double* E, double* total, double* absorption,
+                     unsigned* grid_hash);
 // coordinate depth of the kernels a simulation runs (2 or 4)
 int gpu_levels(GpuSim* g);
 

@@ -75,4 +75,10 @@ void gpu_set_ww_on(GpuSim* g, bool on) { OMC_FORWARD(gpu_set_ww_on, on); }
 long long gpu_capacity(GpuSim* g) { OMC_FORWARD(gpu_capacity); }
 int gpu_levels(GpuSim* g) { return g ? g->levels : 0; }
 
+void gpu_material_xs(GpuSim* g, long long n, const int* mat, const double* E, double* total, double* absorption,
+                     unsigned* grid_hash)
+{
+  OMC_FORWARD(gpu_material_xs, n, mat, E, total, absorption, grid_hash);
+}
+
 }  // namespace omc

@@ -141,6 +141,8 @@ _fn("openmc_gb300_set_trace", [C.c_int64, C.c_int])
 _fn("openmc_gb300_get_trace", [C.c_void_p, _p(C.c_int32)])
 _fn("openmc_gb300_set_weight_windows_on", [C.c_int])
 _fn("openmc_gb300_model_info", [_p(C.c_int64)])
+_fn("openmc_gb300_material_xs", [C.c_int64, _p(C.c_int32), _p(C.c_double), _p(C.c_double), _p(C.c_double),
+                                 _p(C.c_uint32)])
 _fn("openmc_gb300_xs_tables_create", [C.c_int, C.c_int, _p(C.c_double), _p(C.c_double), C.c_int,
                                       _p(C.c_int32), _p(C.c_int32), _p(C.c_double), C.c_int, C.c_int,
                                       C.c_int64, _p(C.c_void_p)])
@@ -435,6 +437,21 @@ def timing():
     _dll.openmc_gb300_timing(out)
     keys = ("time_active", "time_inactive", "time_wall_active", "calculation_rate", "in_flight")
     return dict(zip(keys, list(out)))
+
+
+def material_xs(materials, energies):
+    """Macroscopic (total, absorption) cross sections and the nuclide
+    grid-index hash at (material index, E) pairs, from the transport kernels'
+    own device lookup of the initialised simulation."""
+    mats = np.ascontiguousarray(materials, np.int32)
+    e = np.ascontiguousarray(energies, np.float64)
+    n = len(e)
+    tot, ab = np.empty(n), np.empty(n)
+    gh = np.empty(n, np.uint32)
+    _dll.openmc_gb300_material_xs(n, mats.ctypes.data_as(_p(C.c_int32)), e.ctypes.data_as(_p(C.c_double)),
+                                  tot.ctypes.data_as(_p(C.c_double)), ab.ctypes.data_as(_p(C.c_double)),
+                                  gh.ctypes.data_as(_p(C.c_uint32)))
+    return tot, ab, gh
 
 
 def loaded_library():

@@ -267,6 +267,43 @@ def test_fp32_tables_within_3_sigma(built, tmp_path):
     assert abs(tot_a - tot_b) <= 3 * np.sqrt((sa ** 2).sum() + (sb ** 2).sum()) + 1e-12 * tot_a
 
 
+def test_transport_macro_xs_against_oracle(lattice):
+    """The transport kernels' own macroscopic XS lookup (material_xs on the
+    device, the tables the batch uses) at seeded (material, E) pairs against
+    the oracle: FP64 tables give the oracle's nuclide grid-index hashes and
+    macroscopic XS within 1e-12; FP32 tables keep the hashes, and their
+    largest relative error is below 1e-5 (FP32 rows and interpolation
+    factor, FP32 accumulation over the material's nuclides)."""
+    import oracle
+    from openmc_gb300 import data, lib
+    xml, path = lattice
+    rng = np.random.default_rng(12)
+    n = 20000
+    e = np.exp(rng.uniform(np.log(data.E_MIN), np.log(data.E_MAX), n))
+    e[:2] = [data.E_MIN, data.E_MAX]
+    mats = rng.integers(0, 3, n).astype(np.int32)
+    ot, oa, oh = oracle.Oracle(xml).macro_xs(mats, e)
+    ref = np.stack([ot, oa])
+    saved = lib.settings.xs_fp32
+    out = {}
+    for fp32 in (0, 1):
+        lib.init(directory=path)
+        try:
+            lib.settings.xs_fp32 = fp32
+            lib.simulation_init()
+            t, a, h = lib.material_xs(mats, e)
+            lib.simulation_finalize()
+        finally:
+            lib.settings.xs_fp32 = saved
+            lib.finalize()
+        out[fp32] = (np.stack([t, a]), h.view(np.int32))
+    for fp32, tol in ((0, 1e-12), (1, 1e-5)):
+        got, h = out[fp32]
+        assert np.array_equal(h, oh)
+        rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)
+        assert rel.max() <= tol, f"fp32={fp32}: max relative error {rel.max():.3g}"
+
+
 def test_xs_lookup_parity(built):
     """Lookup microbenchmark tables (68 x 11,303 x 5): bit-exact grid indices
     (hash over each material's nuclides) and <=1e-12 relative macro XS in

@@ -588,7 +588,11 @@ int openmc_reset()
     t.n_realizations = 0;
     std::fill(t.results.begin(), t.results.end(), 0.0);
   }
-  if (s.gpu) gpu_reset_tallies(s.gpu, s.model);
+  try {
+    if (s.gpu) gpu_reset_tallies(s.gpu, s.model);
+  } catch (const std::exception& e) {
+    return fail(OPENMC_E_UNASSIGNED, e.what());
+  }
   std::fill(s.global_tallies.begin(), s.global_tallies.end(), 0.0);
   s.time_active = s.time_inactive = s.time_wall_active = 0.0;
   return 0;

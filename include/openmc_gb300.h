@@ -45,6 +45,7 @@ extern int verbosity;
 extern bool weight_windows_on;
 extern bool restart_run;
 extern int current_batch;
+extern int32_t n_realizations;  /* active batches realised (include/openmc/simulation.h) */
 extern bool initialized;
 extern int n_lost_particles;
 extern int n_coord_levels;
@@ -203,6 +204,50 @@ int openmc_gb300_mlp_predict(void* handle, int64_t n, const float* x4, float* y)
 int openmc_gb300_mlp_get_params(void* handle, float* params, int64_t n);
 int openmc_gb300_mlp_set_params(void* handle, const float* params, int64_t n);
 int openmc_gb300_mlp_last_ms(void* handle, float* ms);
+
+/* ---- model queries the reference's Python bindings use (openmc/lib/cell.py,
+ *      material.py, mesh.py, filter.py, tally.py, nuclide.py, core.py),
+ *      answered from the loaded model; prototypes of include/openmc/capi.h */
+bool openmc_master(void);                                              /* src/initialize.cpp */
+bool openmc_is_statepoint_batch(void);                                 /* src/state_point.cpp */
+int openmc_get_n_batches(int* n_batches, bool get_max_batches);        /* src/settings.cpp:1319-1324 */
+int openmc_set_n_batches(int32_t n_batches, bool set_max_batches, bool add_statepoint_batch);  /* :1285-1317 */
+int openmc_get_keff(double k_combined[]);                              /* src/eigenvalue.cpp:420-440 */
+int openmc_get_cell_index(int32_t id, int32_t* index);                 /* src/cell.cpp */
+int openmc_cell_get_id(int32_t index, int32_t* id);
+int openmc_cell_get_translation(int32_t index, double xyz[]);
+int openmc_cell_get_name(int32_t index, const char** name);
+int openmc_get_material_index(int32_t id, int32_t* index);             /* src/material.cpp */
+int openmc_material_get_id(int32_t index, int32_t* id);
+int openmc_material_get_name(int32_t index, const char** name);
+int openmc_get_nuclide_index(const char name[], int* index);           /* src/nuclide.cpp */
+int openmc_nuclide_name(int index, const char** name);
+int openmc_get_mesh_index(int32_t id, int32_t* index);                 /* src/mesh.cpp */
+int openmc_mesh_get_id(int32_t index, int32_t* id);
+int openmc_mesh_get_type(int32_t index, char* type);                   /* :2285-2293 */
+int openmc_mesh_get_n_elements(int32_t index, size_t* n);
+int openmc_mesh_bounding_box(int32_t index, double* ll, double* ur);
+int openmc_regular_mesh_get_dimension(int32_t index, int** dims, int* n);  /* :2508-2517 */
+int openmc_regular_mesh_get_params(int32_t index, double** ll, double** ur, double** width, int* n);  /* :2534-2555 */
+int openmc_get_filter_index(int32_t id, int32_t* index);               /* src/tallies/filter.cpp */
+int openmc_filter_get_id(int32_t index, int32_t* id);
+int openmc_filter_get_type(int32_t index, char* type);                 /* :234-241 */
+int openmc_filter_get_num_bins(int32_t index, int* n_bins);            /* :243-250 */
+int openmc_energy_filter_get_bins(int32_t index, const double** energies, size_t* n);  /* filter_energy.cpp */
+int openmc_mesh_filter_get_mesh(int32_t index, int32_t* index_mesh);   /* filter_mesh.cpp */
+int openmc_cell_filter_get_bins(int32_t index, const int32_t** cells, int32_t* n);  /* filter_cell.cpp */
+int openmc_material_filter_get_bins(int32_t index, const int32_t** bins, size_t* n);  /* filter_material.cpp */
+int openmc_tally_get_type(int32_t index, int32_t* type);               /* src/tallies/tally.cpp */
+int openmc_tally_get_estimator(int32_t index, int* estimator);
+int openmc_tally_get_active(int32_t index, bool* active);
+int openmc_tally_get_writable(int32_t index, bool* writable);
+int openmc_tally_get_multiply_density(int32_t index, bool* value);
+int openmc_tally_get_filters(int32_t index, const int32_t** indices, size_t* n);
+int openmc_tally_get_scores(int32_t index, int** scores, int* n);
+int openmc_tally_get_nuclides(int32_t index, int** nuclides, int* n);
+
+/* ---- every other entry point the reference's Python bindings name:
+ *      include/openmc_gb300_offpath.h (each returns OPENMC_E_UNASSIGNED) */
 
 #ifdef __cplusplus
 }

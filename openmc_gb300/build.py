@@ -19,7 +19,8 @@ OUT = PKG / "_lib"
 LIB = OUT / "libopenmc_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-fmad=false"]
-SOURCES = ["host_model.cpp", "capi.cpp", "transport_dispatch.cpp", "xsbench.cu", "mlp.cu"]
+SOURCES = ["host_model.cpp", "capi.cpp", "capi_model.cpp", "capi_offpath.cpp", "transport_dispatch.cpp", "xsbench.cu",
+           "mlp.cu"]
 # transport.cu is built once per maximum coordinate depth (namespaces l2, l4)
 VARIANTS = [("transport.cu", "transport_l2", ["-DOMC_MAXL=2", "-DOMC_NS=l2"]),
             ("transport.cu", "transport_l4", ["-DOMC_MAXL=4", "-DOMC_NS=l4"])]

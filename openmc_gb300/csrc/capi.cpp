@@ -59,6 +59,7 @@ int run_mode = 1;  // fixed source
 const char* path_statepoint_c = "";
 int current_batch = 0;
 int current_gen = 0;
+int32_t n_realizations = 0;  // active batches realised (simulation::n_realizations)
 bool initialized = false;
 int n_lost_particles = 0;
 double keff = 1.0;
@@ -278,6 +279,17 @@ int update_magic(HModel& m, int ww_idx, int tally_idx, const std::string& value,
   return 0;
 }
 
+}  // namespace
+
+namespace omc {
+// The loaded model (nullptr before openmc_init) and the error setter, for
+// the model getters and off-path entry points of capi_model.cpp.
+HModel* capi_model() { return S().model_loaded ? &S().model : nullptr; }
+int capi_fail(int code, const std::string& msg) { return fail(code, msg); }
+}  // namespace omc
+
+namespace {
+
 int check_device_errors(const BatchStats& st)
 {
   HModel& m = S().model;
@@ -334,6 +346,7 @@ int openmc_init(int argc, char* argv[], const void* intracomm)
     s.global_tallies.assign(12, 0.0);
     sync_globals_from_model();
     current_batch = 0;
+    n_realizations = 0;
     n_lost_particles = 0;
     initialized = false;
     return 0;
@@ -374,6 +387,7 @@ int openmc_simulation_init()
     gpu_reset_tallies(s.gpu, m);
     std::fill(s.global_tallies.begin(), s.global_tallies.end(), 0.0);
     current_batch = 0;
+    n_realizations = 0;
     n_lost_particles = 0;
     s.time_active = s.time_inactive = s.time_wall_active = 0.0;
     s.n_batches_run = 0;
@@ -417,6 +431,7 @@ int openmc_next_batch(int* status)
     }
     if (int rc = check_device_errors(st)) return rc;
     if (active) {
+      ++n_realizations;
       // global leakage tally normalised by total source weight (tally.cpp:1059-1100)
       double val = st.leakage / st.total_weight;
       s.global_tallies[9 + 1] += val;
@@ -575,6 +590,7 @@ int openmc_finalize()
   s = State();
   initialized = false;
   current_batch = 0;
+  n_realizations = 0;
   n_particles = 0;
   n_lost_particles = 0;
   event_based = false;
@@ -595,6 +611,7 @@ int openmc_reset()
   }
   std::fill(s.global_tallies.begin(), s.global_tallies.end(), 0.0);
   s.time_active = s.time_inactive = s.time_wall_active = 0.0;
+  n_realizations = 0;
   return 0;
 }
 

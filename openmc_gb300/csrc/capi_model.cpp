@@ -1,0 +1,474 @@
+// Model queries of the openmc.lib C API that the reference's Python bindings
+// bind at import (openmc/lib/cell.py, material.py, mesh.py, filter.py,
+// tally.py, nuclide.py, core.py): index and ID lookups, regular-mesh
+// parameters, filter and tally descriptions, batch counts and k-effective,
+// answered from the loaded host model.  Names, arguments, borrowed-pointer
+// returns and error codes follow include/openmc/capi.h and the reference
+// functions cited beside each group.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "host_model.h"
+
+namespace omc {
+HModel* capi_model();
+int capi_fail(int code, const std::string& msg);
+}  // namespace omc
+
+extern "C" {
+extern int OPENMC_E_ALLOCATE;
+extern int OPENMC_E_OUT_OF_BOUNDS;
+extern int OPENMC_E_INVALID_ARGUMENT;
+extern int OPENMC_E_INVALID_TYPE;
+extern int OPENMC_E_INVALID_ID;
+extern int OPENMC_E_DATA;
+extern int32_t n_inactive;
+extern int32_t n_realizations;
+extern double keff;
+extern double keff_std;
+}
+
+namespace {
+
+using omc::capi_fail;
+using omc::HModel;
+
+// The loaded model, or an OPENMC_E_ALLOCATE error as the reference returns
+// before openmc_init.
+HModel* model_or_fail(int& rc)
+{
+  HModel* m = omc::capi_model();
+  rc = m ? 0 : capi_fail(OPENMC_E_ALLOCATE, "OpenMC has not been initialized.");
+  return m;
+}
+
+template<class V>
+bool in_range(const V& v, int32_t index)
+{
+  return index >= 0 && index < static_cast<int32_t>(v.size());
+}
+
+template<class V>
+int index_of_id(const V& v, int32_t id, int32_t* index, const char* what)
+{
+  for (size_t k = 0; k < v.size(); ++k)
+    if (v[k].id == id) {
+      *index = static_cast<int32_t>(k);
+      return 0;
+    }
+  return capi_fail(OPENMC_E_INVALID_ID, std::string("No ") + what + " exists with ID=" + std::to_string(id) + ".");
+}
+
+const char* filter_type_str(int type)
+{
+  switch (type) {
+  case omc::FILTER_MESH: return "mesh";
+  case omc::FILTER_ENERGY: return "energy";
+  case omc::FILTER_PARTICLE: return "particle";
+  case omc::FILTER_CELL: return "cell";
+  default: return "material";
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+// ---------------------------------------------------------------- run state
+// src/initialize.cpp (openmc_master), src/state_point.cpp
+// (openmc_is_statepoint_batch), src/settings.cpp:1285-1324 (batches),
+// src/eigenvalue.cpp:420-440 (k-effective)
+bool openmc_master() { return true; }
+
+bool openmc_is_statepoint_batch() { return false; }
+
+int openmc_get_n_batches(int* n_batches, bool get_max_batches)
+{
+  (void)get_max_batches;  // no triggers: n_batches == n_max_batches
+  int rc;
+  HModel* m = model_or_fail(rc);
+  if (!m) return rc;
+  *n_batches = m->n_batches;
+  return 0;
+}
+
+int openmc_set_n_batches(int32_t n_batches, bool set_max_batches, bool add_statepoint_batch)
+{
+  (void)set_max_batches;
+  (void)add_statepoint_batch;  // no statepoints are written on this path
+  int rc;
+  HModel* m = model_or_fail(rc);
+  if (!m) return rc;
+  if (m->n_inactive >= n_batches)
+    return capi_fail(OPENMC_E_INVALID_ARGUMENT, "Number of active batches must be greater than zero.");
+  m->n_batches = n_batches;
+  return 0;
+}
+
+// Fixed-source runs leave k at its initial 1 with no spread; the reference
+// reports an infinite standard deviation up to one realization.
+int openmc_get_keff(double k_combined[])
+{
+  k_combined[0] = keff;
+  k_combined[1] = n_realizations <= 1 ? std::numeric_limits<double>::infinity() : keff_std;
+  return 0;
+}
+
+// -------------------------------------------------------- cells, materials
+// src/cell.cpp (openmc_get_cell_index, openmc_cell_get_id,
+// openmc_cell_get_translation, openmc_cell_get_name), src/material.cpp
+// (openmc_get_material_index, openmc_material_get_id,
+// openmc_material_get_name)
+int openmc_get_cell_index(int32_t id, int32_t* index)
+{
+  int rc;
+  HModel* m = model_or_fail(rc);
+  return m ? index_of_id(m->cells, id, index, "cell") : rc;
+}
+
+int openmc_cell_get_id(int32_t index, int32_t* id)
+{
+  int rc;
+  HModel* m = model_or_fail(rc);
+  if (!m) return rc;
+  if (!in_range(m->cells, index)) return capi_fail(OPENMC_E_OUT_OF_BOUNDS, "Index in cells array is out of bounds.");
+  *id = m->cells[index].id;
+  return 0;
+}
+
+int openmc_cell_get_translation(int32_t index, double xyz[])
+{
+  int rc;
+  HModel* m = model_or_fail(rc);
+  if (!m) return rc;
+  if (!in_range(m->cells, index)) return capi_fail(OPENMC_E_OUT_OF_BOUNDS, "Index in cells array is out of bounds.");
+  for (int k = 0; k < 3; ++k) xyz[k] = m->cells[index].tr[k];
+  return 0;
+}
+
+int openmc_cell_get_name(int32_t index, const char** name)
+{
+  int rc;
+  HModel* m = model_or_fail(rc);
+  if (!m) return rc;
+  if (!in_range(m->cells, index)) return capi_fail(OPENMC_E_OUT_OF_BOUNDS, "Index in cells array is out of bounds.");
+  *name = "";  // names are not kept by this library's model reader
+  return 0;
+}
+
+int openmc_get_material_index(int32_t id, int32_t* index)
+{
+  int rc;
+  HModel* m = model_or_fail(rc);
+  return m ? index_of_id(m->materials, id, index, "material") : rc;
+}
+
+int openmc_material_get_id(int32_t index, int32_t* id)
+{
+  int rc;
+  HModel* m = model_or_fail(rc);
+  if (!m) return rc;
+  if (!in_range(m->materials, index))
+    return capi_fail(OPENMC_E_OUT_OF_BOUNDS, "Index in materials array is out of bounds.");
+  *id = m->materials[index].id;
+  return 0;
+}
+
+int openmc_material_get_name(int32_t index, const char** name)
+{
+  int rc;
+  HModel* m = model_or_fail(rc);
+  if (!m) return rc;
+  if (!in_range(m->materials, index))
+    return capi_fail(OPENMC_E_OUT_OF_BOUNDS, "Index in materials array is out of bounds.");
+  *name = "";
+  return 0;
+}
+
+// ----------------------------------------------------------------- nuclides
+// src/nuclide.cpp (openmc_get_nuclide_index, openmc_nuclide_name)
+int openmc_get_nuclide_index(const char name[], int* index)
+{
+  int rc;
+  HModel* m = model_or_fail(rc);
+  if (!m) return rc;
+  for (size_t k = 0; k < m->nuclides.size(); ++k)
+    if (m->nuclides[k].name == name) {
+      *index = static_cast<int>(k);
+      return 0;
+    }
+  return capi_fail(OPENMC_E_DATA, std::string("No nuclide named '") + name + "' has been loaded.");
+}
+
+int openmc_nuclide_name(int index, const char** name)
+{
+  int rc;
+  HModel* m = model_or_fail(rc);
+  if (!m) return rc;
+  if (!in_range(m->nuclides, index))
+    return capi_fail(OPENMC_E_OUT_OF_BOUNDS, "Index in nuclides array is out of bounds.");
+  *name = m->nuclides[index].name.c_str();
+  return 0;
+}
+
+// ------------------------------------------------------------------- meshes
+// src/mesh.cpp (openmc_get_mesh_index, openmc_mesh_get_id,
+// openmc_mesh_get_type :2285-2293, openmc_mesh_get_n_elements,
+// openmc_mesh_bounding_box, openmc_regular_mesh_get_dimension :2508-2517,
+// openmc_regular_mesh_get_params :2534-2555); every mesh here is regular
+int openmc_get_mesh_index(int32_t id, int32_t* index)
+{
+  int rc;
+  HModel* m = model_or_fail(rc);
+  return m ? index_of_id(m->meshes, id, index, "mesh") : rc;
+}
+
+static int check_mesh(HModel*& m, int32_t index)
+{
+  int rc;
+  m = model_or_fail(rc);
+  if (!m) return rc;
+  if (!in_range(m->meshes, index)) return capi_fail(OPENMC_E_OUT_OF_BOUNDS, "Index in meshes array is out of bounds.");
+  return 0;
+}
+
+int openmc_mesh_get_id(int32_t index, int32_t* id)
+{
+  HModel* m;
+  if (int rc = check_mesh(m, index)) return rc;
+  *id = m->meshes[index].id;
+  return 0;
+}
+
+int openmc_mesh_get_type(int32_t index, char* type)
+{
+  HModel* m;
+  if (int rc = check_mesh(m, index)) return rc;
+  std::strcpy(type, "regular");
+  return 0;
+}
+
+int openmc_mesh_get_n_elements(int32_t index, size_t* n)
+{
+  HModel* m;
+  if (int rc = check_mesh(m, index)) return rc;
+  *n = static_cast<size_t>(m->meshes[index].n_bins());
+  return 0;
+}
+
+int openmc_mesh_bounding_box(int32_t index, double* ll, double* ur)
+{
+  HModel* m;
+  if (int rc = check_mesh(m, index)) return rc;
+  const omc::HMesh& h = m->meshes[index];
+  for (int k = 0; k < 3; ++k) {
+    const bool used = k < h.ndim;
+    ll[k] = used ? h.ll[k] : -std::numeric_limits<double>::infinity();
+    ur[k] = used ? h.ur[k] : std::numeric_limits<double>::infinity();
+  }
+  return 0;
+}
+
+int openmc_regular_mesh_get_dimension(int32_t index, int** dims, int* n)
+{
+  HModel* m;
+  if (int rc = check_mesh(m, index)) return rc;
+  *dims = m->meshes[index].shape;
+  *n = m->meshes[index].ndim;
+  return 0;
+}
+
+int openmc_regular_mesh_get_params(int32_t index, double** ll, double** ur, double** width, int* n)
+{
+  HModel* m;
+  if (int rc = check_mesh(m, index)) return rc;
+  omc::HMesh& h = m->meshes[index];
+  *ll = h.ll;
+  *ur = h.ur;
+  *width = h.width;
+  *n = h.ndim;
+  return 0;
+}
+
+// ------------------------------------------------------------------ filters
+// src/tallies/filter.cpp (openmc_get_filter_index, openmc_filter_get_id,
+// openmc_filter_get_type :234-241, openmc_filter_get_num_bins :243-250),
+// filter_energy.cpp (openmc_energy_filter_get_bins), filter_mesh.cpp
+// (openmc_mesh_filter_get_mesh), filter_cell.cpp
+// (openmc_cell_filter_get_bins), filter_material.cpp
+// (openmc_material_filter_get_bins)
+int openmc_get_filter_index(int32_t id, int32_t* index)
+{
+  int rc;
+  HModel* m = model_or_fail(rc);
+  return m ? index_of_id(m->filters, id, index, "filter") : rc;
+}
+
+static int check_filter(HModel*& m, int32_t index, int type = -1)
+{
+  int rc;
+  m = model_or_fail(rc);
+  if (!m) return rc;
+  if (!in_range(m->filters, index)) return capi_fail(OPENMC_E_OUT_OF_BOUNDS, "Index in filters array is out of bounds.");
+  if (type >= 0 && m->filters[index].type != type)
+    return capi_fail(OPENMC_E_INVALID_TYPE, std::string("Tried to get bins on a non-") + filter_type_str(type) +
+                                                " filter.");
+  return 0;
+}
+
+int openmc_filter_get_id(int32_t index, int32_t* id)
+{
+  HModel* m;
+  if (int rc = check_filter(m, index)) return rc;
+  *id = m->filters[index].id;
+  return 0;
+}
+
+int openmc_filter_get_type(int32_t index, char* type)
+{
+  HModel* m;
+  if (int rc = check_filter(m, index)) return rc;
+  std::strcpy(type, filter_type_str(m->filters[index].type));
+  return 0;
+}
+
+int openmc_filter_get_num_bins(int32_t index, int* n_bins)
+{
+  HModel* m;
+  if (int rc = check_filter(m, index)) return rc;
+  *n_bins = m->filters[index].nbins;
+  return 0;
+}
+
+int openmc_energy_filter_get_bins(int32_t index, const double** energies, size_t* n)
+{
+  HModel* m;
+  if (int rc = check_filter(m, index, omc::FILTER_ENERGY)) return rc;
+  *energies = m->filters[index].bins.data();
+  *n = m->filters[index].bins.size();
+  return 0;
+}
+
+int openmc_mesh_filter_get_mesh(int32_t index, int32_t* index_mesh)
+{
+  HModel* m;
+  if (int rc = check_filter(m, index, omc::FILTER_MESH)) return rc;
+  *index_mesh = m->filters[index].mesh;
+  return 0;
+}
+
+int openmc_cell_filter_get_bins(int32_t index, const int32_t** cells, int32_t* n)
+{
+  HModel* m;
+  if (int rc = check_filter(m, index, omc::FILTER_CELL)) return rc;
+  *cells = m->filters[index].ids.data();
+  *n = static_cast<int32_t>(m->filters[index].ids.size());
+  return 0;
+}
+
+int openmc_material_filter_get_bins(int32_t index, const int32_t** bins, size_t* n)
+{
+  HModel* m;
+  if (int rc = check_filter(m, index, omc::FILTER_MATERIAL)) return rc;
+  *bins = m->filters[index].ids.data();
+  *n = m->filters[index].ids.size();
+  return 0;
+}
+
+// ------------------------------------------------------------------ tallies
+// src/tallies/tally.cpp (openmc_tally_get_type, _get_estimator, _get_active,
+// _get_writable, _get_multiply_density, _get_filters, _get_scores,
+// _get_nuclides).  Every tally here is a volume tally, active, writable and
+// multiplied by density, over the total of all nuclides; scores are
+// reported with the reference's codes (include/openmc/constants.h:310-314:
+// flux -1, total -2, absorption -5) and estimators with TallyEstimator
+// (:299; track-length 1, collision 2).
+static int check_tally(HModel*& m, int32_t index)
+{
+  int rc;
+  m = model_or_fail(rc);
+  if (!m) return rc;
+  if (!in_range(m->tallies, index)) return capi_fail(OPENMC_E_OUT_OF_BOUNDS, "Index in tallies array is out of bounds.");
+  return 0;
+}
+
+int openmc_tally_get_type(int32_t index, int32_t* type)
+{
+  HModel* m;
+  if (int rc = check_tally(m, index)) return rc;
+  *type = 0;  // TallyType::VOLUME
+  return 0;
+}
+
+int openmc_tally_get_estimator(int32_t index, int* estimator)
+{
+  HModel* m;
+  if (int rc = check_tally(m, index)) return rc;
+  *estimator = m->tallies[index].estimator == omc::EST_COLLISION ? 2 : 1;
+  return 0;
+}
+
+int openmc_tally_get_active(int32_t index, bool* active)
+{
+  HModel* m;
+  if (int rc = check_tally(m, index)) return rc;
+  *active = true;
+  return 0;
+}
+
+int openmc_tally_get_writable(int32_t index, bool* writable)
+{
+  HModel* m;
+  if (int rc = check_tally(m, index)) return rc;
+  *writable = true;
+  return 0;
+}
+
+int openmc_tally_get_multiply_density(int32_t index, bool* value)
+{
+  HModel* m;
+  if (int rc = check_tally(m, index)) return rc;
+  *value = true;
+  return 0;
+}
+
+int openmc_tally_get_filters(int32_t index, const int32_t** indices, size_t* n)
+{
+  HModel* m;
+  if (int rc = check_tally(m, index)) return rc;
+  *indices = m->tallies[index].filters.data();
+  *n = m->tallies[index].filters.size();
+  return 0;
+}
+
+int openmc_tally_get_scores(int32_t index, int** scores, int* n)
+{
+  HModel* m;
+  if (int rc = check_tally(m, index)) return rc;
+  // the reference codes live as long as the tally (a borrowed pointer)
+  static std::map<const omc::HTally*, std::vector<int>> codes;
+  const omc::HTally& t = m->tallies[index];
+  std::vector<int>& c = codes[&t];
+  c.clear();
+  for (int s : t.scores) c.push_back(s == omc::SCORE_FLUX ? -1 : (s == omc::SCORE_TOTAL ? -2 : -5));
+  *scores = c.data();
+  *n = static_cast<int>(c.size());
+  return 0;
+}
+
+int openmc_tally_get_nuclides(int32_t index, int** nuclides, int* n)
+{
+  HModel* m;
+  if (int rc = check_tally(m, index)) return rc;
+  static int total = -1;  // the "total" nuclide bin
+  *nuclides = &total;
+  *n = 1;
+  return 0;
+}
+
+}  // extern "C"

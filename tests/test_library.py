@@ -1,6 +1,7 @@
-"""The C-ABI library: loads, exports every symbol include/openmc_gb300.h
-declares, parses models and reports errors like the reference (CPU only; no
-compute calls)."""
+"""The C-ABI library: loads, exports every symbol include/*.h declares and
+every function and global the reference's Python bindings resolve, parses
+models, answers model queries and reports errors like the reference (CPU
+only; no compute calls)."""
 import ctypes as C
 import re
 from pathlib import Path
@@ -12,7 +13,7 @@ ROOT = Path(__file__).resolve().parent.parent
 
 
 def header_symbols():
-    text = (ROOT / "include" / "openmc_gb300.h").read_text()
+    text = "".join(h.read_text() for h in sorted((ROOT / "include").glob("*.h")))
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     funcs = re.findall(r"^\s*(?:[A-Za-z_][\w\s\*]*?)\b((?:openmc_|tallies_)\w+)\s*\(", text, flags=re.M)
     globs = re.findall(r"^\s*extern\s+[\w\s\*]+?\b(\w+)(?:\[\d+\])?\s*;", text, flags=re.M)
@@ -136,3 +137,79 @@ def test_unsupported_tallies_rejected(built, tmp_path, case):
     with pytest.raises(lib.InvalidArgumentError):
         lib.init(directory=d)
     lib.finalize()
+
+
+def test_reference_bindings_resolve(built):
+    """openmc/lib/*.py declares argument types for every function it uses at
+    import, so each must be exported for `import openmc.lib` to succeed on
+    this library (list generated by tests/golden/make_bindings_list.py)."""
+    import json
+    from openmc_gb300 import lib
+    names = json.loads((ROOT / "tests" / "golden" / "openmc_lib_bindings.json").read_text())
+    assert len(names["functions"]) > 150 and len(names["globals"]) > 15
+    dll = C.CDLL(lib.loaded_library())
+    missing = [f for f in names["functions"] if not hasattr(dll, f)]
+    assert not missing, f"functions the reference's bindings need: {missing}"
+    for g in names["globals"]:
+        C.c_int.in_dll(dll, g)
+
+
+def test_model_queries_and_off_path_calls(built, tmp_path):
+    from openmc_gb300 import configs, lib
+    m, d = configs.lattice17(tmp_path, particles=100, batches=3, n_points=300, mesh_dim=(17, 17, 5), n_ebins=4)
+    m.export_to_model_xml(d)
+    lib.init(directory=d)
+    try:
+        # a separate handle: return codes as the reference's bindings see them
+        dll = C.CDLL(lib.loaded_library())
+
+        def code(name):
+            return C.c_int.in_dll(dll, "OPENMC_E_" + name).value
+
+        i32, i = C.c_int32(), C.c_int()
+        tally = m.tallies[0]
+        mesh_f, energy_f = tally.filters
+        # filters: index by id, type, bins
+        assert dll.openmc_get_filter_index(mesh_f.id, C.byref(i32)) == 0
+        fi = i32.value
+        buf = C.create_string_buffer(32)
+        assert dll.openmc_filter_get_type(fi, buf) == 0 and buf.value == b"mesh"
+        assert dll.openmc_mesh_filter_get_mesh(fi, C.byref(i32)) == 0
+        mi = i32.value
+        assert dll.openmc_get_filter_index(energy_f.id, C.byref(i32)) == 0
+        ei = i32.value
+        e_ptr, n = C.POINTER(C.c_double)(), C.c_size_t()
+        assert dll.openmc_energy_filter_get_bins(ei, C.byref(e_ptr), C.byref(n)) == 0
+        assert n.value == 5 and e_ptr[0] < e_ptr[4]
+        assert dll.openmc_energy_filter_get_bins(fi, C.byref(e_ptr), C.byref(n)) == code("INVALID_TYPE")
+        # the regular mesh's dimension and parameters (borrowed pointers)
+        dims, nd = C.POINTER(C.c_int)(), C.c_int()
+        assert dll.openmc_regular_mesh_get_dimension(mi, C.byref(dims), C.byref(nd)) == 0
+        assert [dims[k] for k in range(nd.value)] == [17, 17, 5]
+        ll, ur, w = C.POINTER(C.c_double)(), C.POINTER(C.c_double)(), C.POINTER(C.c_double)()
+        assert dll.openmc_regular_mesh_get_params(mi, C.byref(ll), C.byref(ur), C.byref(w), C.byref(nd)) == 0
+        assert np.isclose(ur[0] - ll[0], 17 * w[0])
+        assert dll.openmc_mesh_get_type(mi, buf) == 0 and buf.value == b"regular"
+        # tallies: estimator (TallyEstimator::TRACKLENGTH), flux score code, filters
+        ti = lib.tally_index(tally.id)
+        assert dll.openmc_tally_get_estimator(ti, C.byref(i)) == 0 and i.value == 1
+        sc, ns = C.POINTER(C.c_int)(), C.c_int()
+        assert dll.openmc_tally_get_scores(ti, C.byref(sc), C.byref(ns)) == 0 and ns.value == 1 and sc[0] == -1
+        fl, nf = C.POINTER(C.c_int32)(), C.c_size_t()
+        assert dll.openmc_tally_get_filters(ti, C.byref(fl), C.byref(nf)) == 0
+        assert [fl[k] for k in range(nf.value)] == [fi, ei]
+        # cells and materials by id; an unknown id
+        cid = m.geometry.root_universe.cells[0].id
+        assert dll.openmc_get_cell_index(cid, C.byref(i32)) == 0
+        out = C.c_int32()
+        assert dll.openmc_cell_get_id(i32.value, C.byref(out)) == 0 and out.value == cid
+        assert dll.openmc_get_material_index(99999, C.byref(i32)) == code("INVALID_ID")
+        # batches and k (fixed source: 1 with an infinite spread before two realizations)
+        assert dll.openmc_get_n_batches(C.byref(i), False) == 0 and i.value == 3
+        k = (C.c_double * 2)()
+        assert dll.openmc_get_keff(k) == 0 and k[0] == 1.0 and np.isinf(k[1])
+        # an entry point outside the path: an error code and a message, no crash
+        assert dll.openmc_calculate_volumes() == code("UNASSIGNED")
+        assert b"openmc_calculate_volumes" in (C.c_char * 256).in_dll(dll, "openmc_err_msg").value
+    finally:
+        lib.finalize()

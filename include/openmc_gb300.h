@@ -220,6 +220,9 @@ int openmc_cell_get_name(int32_t index, const char** name);
 int openmc_get_material_index(int32_t id, int32_t* index);             /* src/material.cpp */
 int openmc_material_get_id(int32_t index, int32_t* id);
 int openmc_material_get_name(int32_t index, const char** name);
+int openmc_material_get_densities(int32_t index, const int** nuclides, const double** densities, int* n);  /* :1389-1407 */
+int openmc_material_get_density(int32_t index, double* density);      /* :1409-1419 */
+int openmc_cell_get_fill(int32_t index, int* type, int32_t** indices, int32_t* n);  /* src/cell.cpp */
 int openmc_get_nuclide_index(const char name[], int* index);           /* src/nuclide.cpp */
 int openmc_nuclide_name(int index, const char** name);
 int openmc_get_mesh_index(int32_t id, int32_t* index);                 /* src/mesh.cpp */
@@ -237,6 +240,8 @@ int openmc_energy_filter_get_bins(int32_t index, const double** energies, size_t
 int openmc_mesh_filter_get_mesh(int32_t index, int32_t* index_mesh);   /* filter_mesh.cpp */
 int openmc_cell_filter_get_bins(int32_t index, const int32_t** cells, int32_t* n);  /* filter_cell.cpp */
 int openmc_material_filter_get_bins(int32_t index, const int32_t** bins, size_t* n);  /* filter_material.cpp */
+int openmc_mesh_filter_get_translation(int32_t index, double translation[3]);  /* filter_mesh.cpp */
+int openmc_particle_filter_get_bins(int32_t idx, int bins[]);          /* filter_particle.cpp */
 int openmc_tally_get_type(int32_t index, int32_t* type);               /* src/tallies/tally.cpp */
 int openmc_tally_get_estimator(int32_t index, int* estimator);
 int openmc_tally_get_active(int32_t index, bool* active);

@@ -21,7 +21,6 @@ typedef struct { double x, y, z; } openmc_gb300_position;  /* Position */
 int openmc_calculate_volumes(void);
 int openmc_cell_bounding_box(const int32_t index, double* llc, double* urc);
 int openmc_cell_get_density(int32_t index, const int32_t* instance, double* rho);
-int openmc_cell_get_fill(int32_t index, int* type, int32_t** indices, int32_t* n);
 int openmc_cell_get_num_instances(int32_t index, int32_t* num_instances);
 int openmc_cell_get_rotation(int32_t index, double rot[], size_t* n);
 int openmc_cell_get_temperature(int32_t index, const int32_t* instance, double* T);
@@ -59,8 +58,6 @@ int openmc_legendre_filter_set_order(int32_t index, int order);
 int openmc_load_nuclide(const char* name, const double* temps, int n);
 int openmc_material_add_nuclide(int32_t index, const char name[], double density);
 int openmc_material_filter_set_bins(int32_t index, size_t n, const int32_t* bins);
-int openmc_material_get_densities(int32_t index, const int** nuclides, const double** densities, int* n);
-int openmc_material_get_density(int32_t index, double* density);
 int openmc_material_get_depletable(int32_t index, bool* depletable);
 int openmc_material_get_temperature(int32_t index, double* temperature);
 int openmc_material_get_volume(int32_t index, double* volume);
@@ -71,7 +68,6 @@ int openmc_material_set_id(int32_t index, int32_t id);
 int openmc_material_set_name(int32_t index, const char* name);
 int openmc_material_set_volume(int32_t index, double volume);
 int openmc_mesh_filter_get_rotation(int32_t index, double rot[], size_t* n);
-int openmc_mesh_filter_get_translation(int32_t index, double translation[3]);
 int openmc_mesh_filter_set_mesh(int32_t index, int32_t index_mesh);
 int openmc_mesh_filter_set_rotation(int32_t index, const double rot[], size_t rot_len);
 int openmc_mesh_filter_set_translation(int32_t index, double translation[3]);
@@ -89,7 +85,6 @@ int openmc_meshsurface_filter_set_mesh(int32_t index, int32_t index_mesh);
 int openmc_meshsurface_filter_set_translation(int32_t index, double translation[3]);
 int openmc_new_filter(const char* type, int32_t* index);
 int openmc_nuclide_collapse_rate(int index, int MT, double temperature, const double* energy, const double* flux, int n, double* xs);
-int openmc_particle_filter_get_bins(int32_t idx, int bins[]);
 int openmc_plot_geometry(void);
 int openmc_properties_export(const char* filename);
 int openmc_properties_import(const char* filename);

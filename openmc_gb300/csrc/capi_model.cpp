@@ -190,6 +190,56 @@ int openmc_material_get_name(int32_t index, const char** name)
   return 0;
 }
 
+// Atom densities [atom/b-cm] of the material's nuclides (borrowed) and the
+// mass density [g/cm^3] = sum n_i awr_i m_n / N_A (src/material.cpp:
+// 1389-1419, the sum of :456-466; neutron mass 1.00866491595 u, Avogadro
+// 0.602214076e24 /mol).
+int openmc_material_get_densities(int32_t index, const int** nuclides, const double** densities, int* n)
+{
+  int rc;
+  HModel* m = model_or_fail(rc);
+  if (!m) return rc;
+  if (!in_range(m->materials, index))
+    return capi_fail(OPENMC_E_OUT_OF_BOUNDS, "Index in materials array is out of bounds.");
+  const omc::HMaterial& mat = m->materials[index];
+  if (mat.nuclide.empty()) return capi_fail(OPENMC_E_ALLOCATE, "Material atom density array has not been allocated.");
+  *nuclides = mat.nuclide.data();
+  *densities = mat.atom_density.data();
+  *n = static_cast<int>(mat.nuclide.size());
+  return 0;
+}
+
+int openmc_material_get_density(int32_t index, double* density)
+{
+  int rc;
+  HModel* m = model_or_fail(rc);
+  if (!m) return rc;
+  if (!in_range(m->materials, index))
+    return capi_fail(OPENMC_E_OUT_OF_BOUNDS, "Index in materials array is out of bounds.");
+  const omc::HMaterial& mat = m->materials[index];
+  double rho = 0.0;
+  for (size_t k = 0; k < mat.nuclide.size(); ++k)
+    rho += mat.atom_density[k] * m->nuclides[mat.nuclide[k]].awr * 1.00866491595 / 0.602214076;
+  *density = rho;
+  return 0;
+}
+
+// Fill of a cell (src/cell.cpp openmc_cell_get_fill): type 0 material,
+// 1 universe, 2 lattice (the reference's Fill enum), with a borrowed pointer
+// to the one material, universe or lattice index.
+int openmc_cell_get_fill(int32_t index, int* type, int32_t** indices, int32_t* n)
+{
+  int rc;
+  HModel* m = model_or_fail(rc);
+  if (!m) return rc;
+  if (!in_range(m->cells, index)) return capi_fail(OPENMC_E_OUT_OF_BOUNDS, "Index in cells array is out of bounds.");
+  omc::HCell& c = m->cells[index];
+  *type = c.fill_type;
+  *indices = &c.fill;
+  *n = 1;
+  return 0;
+}
+
 // ----------------------------------------------------------------- nuclides
 // src/nuclide.cpp (openmc_get_nuclide_index, openmc_nuclide_name)
 int openmc_get_nuclide_index(const char name[], int* index)
@@ -377,6 +427,24 @@ int openmc_material_filter_get_bins(int32_t index, const int32_t** bins, size_t*
   if (int rc = check_filter(m, index, omc::FILTER_MATERIAL)) return rc;
   *bins = m->filters[index].ids.data();
   *n = m->filters[index].ids.size();
+  return 0;
+}
+
+// Mesh filters here carry no translation; particle filters bin neutrons
+// only (ParticleType::neutron = 0).
+int openmc_mesh_filter_get_translation(int32_t index, double translation[3])
+{
+  HModel* m;
+  if (int rc = check_filter(m, index, omc::FILTER_MESH)) return rc;
+  translation[0] = translation[1] = translation[2] = 0.0;
+  return 0;
+}
+
+int openmc_particle_filter_get_bins(int32_t idx, int bins[])
+{
+  HModel* m;
+  if (int rc = check_filter(m, idx, omc::FILTER_PARTICLE)) return rc;
+  for (int b = 0; b < m->filters[idx].nbins; ++b) bins[b] = 0;
   return 0;
 }
 

@@ -36,9 +36,6 @@ int openmc_cell_bounding_box(const int32_t index, double* llc, double* urc)
 int openmc_cell_get_density(int32_t index, const int32_t* instance, double* rho)
 { return off_path("openmc_cell_get_density"); }
 
-int openmc_cell_get_fill(int32_t index, int* type, int32_t** indices, int32_t* n)
-{ return off_path("openmc_cell_get_fill"); }
-
 int openmc_cell_get_num_instances(int32_t index, int32_t* num_instances)
 { return off_path("openmc_cell_get_num_instances"); }
 
@@ -156,12 +153,6 @@ int openmc_material_add_nuclide(int32_t index, const char name[], double density
 int openmc_material_filter_set_bins(int32_t index, size_t n, const int32_t* bins)
 { return off_path("openmc_material_filter_set_bins"); }
 
-int openmc_material_get_densities(int32_t index, const int** nuclides, const double** densities, int* n)
-{ return off_path("openmc_material_get_densities"); }
-
-int openmc_material_get_density(int32_t index, double* density)
-{ return off_path("openmc_material_get_density"); }
-
 int openmc_material_get_depletable(int32_t index, bool* depletable)
 { return off_path("openmc_material_get_depletable"); }
 
@@ -191,9 +182,6 @@ int openmc_material_set_volume(int32_t index, double volume)
 
 int openmc_mesh_filter_get_rotation(int32_t index, double rot[], size_t* n)
 { return off_path("openmc_mesh_filter_get_rotation"); }
-
-int openmc_mesh_filter_get_translation(int32_t index, double translation[3])
-{ return off_path("openmc_mesh_filter_get_translation"); }
 
 int openmc_mesh_filter_set_mesh(int32_t index, int32_t index_mesh)
 { return off_path("openmc_mesh_filter_set_mesh"); }
@@ -245,9 +233,6 @@ int openmc_new_filter(const char* type, int32_t* index)
 
 int openmc_nuclide_collapse_rate(int index, int MT, double temperature, const double* energy, const double* flux, int n, double* xs)
 { return off_path("openmc_nuclide_collapse_rate"); }
-
-int openmc_particle_filter_get_bins(int32_t idx, int bins[])
-{ return off_path("openmc_particle_filter_get_bins"); }
 
 int openmc_plot_geometry()
 { return off_path("openmc_plot_geometry"); }

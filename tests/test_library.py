@@ -204,6 +204,23 @@ def test_model_queries_and_off_path_calls(built, tmp_path):
         out = C.c_int32()
         assert dll.openmc_cell_get_id(i32.value, C.byref(out)) == 0 and out.value == cid
         assert dll.openmc_get_material_index(99999, C.byref(i32)) == code("INVALID_ID")
+        # the root cell is filled with the lattice (Fill::LATTICE = 2)
+        ft, fidx, fn = C.c_int(), C.POINTER(C.c_int32)(), C.c_int32()
+        assert dll.openmc_get_cell_index(cid, C.byref(i32)) == 0
+        assert dll.openmc_cell_get_fill(i32.value, C.byref(ft), C.byref(fidx), C.byref(fn)) == 0
+        assert ft.value == 2 and fn.value == 1 and fidx[0] == 0
+        # a material's nuclides and atom densities (borrowed), and its mass density
+        mat = m.materials[0]
+        assert dll.openmc_get_material_index(mat.id, C.byref(i32)) == 0
+        nuc, dens, nn = C.POINTER(C.c_int)(), C.POINTER(C.c_double)(), C.c_int()
+        assert dll.openmc_material_get_densities(i32.value, C.byref(nuc), C.byref(dens), C.byref(nn)) == 0
+        assert nn.value == 4 and all(dens[k] > 0 for k in range(4))
+        rho = C.c_double()
+        assert dll.openmc_material_get_density(i32.value, C.byref(rho)) == 0 and rho.value > 0
+        name = C.c_char_p()
+        assert dll.openmc_nuclide_name(nuc[0], C.byref(name)) == 0
+        back = C.c_int()
+        assert dll.openmc_get_nuclide_index(name.value, C.byref(back)) == 0 and back.value == nuc[0]
         # batches and k (fixed source: 1 with an infinite spread before two realizations)
         assert dll.openmc_get_n_batches(C.byref(i), False) == 0 and i.value == 3
         k = (C.c_double * 2)()

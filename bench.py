@@ -54,6 +54,8 @@ def parse():
                     help="histories in the CPU baseline sample (default 3,000,000: about 10 s on 16 cores)")
     ap.add_argument("--no-xs-bench", action="store_true", help="skip the XS-lookup microbenchmark extra")
     ap.add_argument("--no-network-bench", action="store_true", help="skip the importance-network extra")
+    ap.add_argument("--no-shield", action="store_true",
+                    help="skip the shield figure-of-merit extra (plain, MAGIC and learned windows)")
     ap.add_argument("--network-only", action="store_true",
                     help="only time the importance network's training kernels (for kernel profilers)")
     ap.add_argument("--no-graph", action="store_true",
@@ -294,6 +296,27 @@ def run_gb300(args, barrier=lambda: None, rank=0):
     return out
 
 
+def shield_fom():
+    """The metric's second half: figure of merit 1/(R^2 T) of the back-face
+    flux of the 200 cm deep-penetration shield (densities x 0.1, 200 x 10 x 10
+    mesh x 6 energy groups) for plain transport, MAGIC windows and learned
+    windows from the same 5 x 10^6-history pilot, 10 x 10^6 histories each,
+    FP32 tables; T is the device time of the measured batches.  A failure
+    here is reported in the line instead of ending the bench."""
+    from openmc_gb300 import shield_study
+    try:
+        r = shield_study.run(ROOT / "_models" / "shield_bench")
+    except Exception as e:  # the transport line above stands on its own
+        return {"error": f"{type(e).__name__}: {e}"}
+    out = {"workload": r["workload"], "pilot": r["pilot"], "measure": r["measure"]}
+    for k in ("plain", "magic", "learned"):
+        v = r[k]
+        out[k] = {"fom": v["fom"], "rel_err": v["rel_err"], "back_mean": v["back_mean"],
+                  "device_s": v["device_s"], **({"fom_gain": v["fom_gain"]} if "fom_gain" in v else {})}
+    out["z"] = {k: r[k] for k in ("z_magic_plain", "z_learned_plain", "z_learned_magic") if k in r}
+    return out
+
+
 def network_bench(rows=1 << 20, steps=20):
     """Training throughput of the importance network's tensor-core kernels:
     full-batch Adam steps over `rows` random rows.  FLOPs per step count the
@@ -450,6 +473,8 @@ def main():
     r = run_gb300(args, barrier=barrier, rank=rank)
     if not args.no_network_bench and rank == 0:
         r["network"] = network_bench()
+    if not args.no_shield and rank == 0:
+        r["shield"] = shield_fom()
     if not args.no_xs_bench and rank == 0:
         x64, x32 = xs_lookup_bench(False), xs_lookup_bench(True)
         h64, h32 = x64.pop("_head"), x32.pop("_head")
@@ -502,6 +527,7 @@ def main():
         "iterations_per_step": r["iterations"],
         "xs_lookup_microbench": r.get("xs_lookup"),
         "importance_network_training": r.get("network"),
+        "shield_fom": r.get("shield"),
     }
     print(json.dumps(line))
 

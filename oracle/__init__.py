@@ -4,8 +4,8 @@ ctypes wrapper over ``oracle/_build/liboracle.so`` (the CPU restatement of the
 reference transport path in ``oracle.cpp``) and over
 ``oracle/_ref/librandom_lcg_ref.so`` (the reference's own ``random_lcg.cpp``
 compiled from source).  Only the tests, ``__graft_entry__.smoke()`` and the
-CPU-baseline leg of ``bench.py`` may use this package, and only as a checker
-or a baseline: nothing in ``openmc_gb300`` imports it.
+CPU-baseline leg of ``bench.py`` may use this package, and only to check
+results or as a timed baseline: nothing in ``openmc_gb300`` imports it.
 """
 from __future__ import annotations
 

@@ -4,7 +4,8 @@
 // path (event-based and history-based loops), written from the reference's
 // behaviour with each function citing the reference file:line it follows.
 // Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline may load
-// the library built from this file, and only as a checker or baseline.
+// the library built from this file, and only to check results or as the
+// timed baseline.
 //
 // Parity pins: prn / future_seed / init_seed are checked bit-for-bit against
 // the reference's own src/random_lcg.cpp compiled from source (oracle/_ref),

@@ -223,6 +223,9 @@ int openmc_material_get_name(int32_t index, const char** name);
 int openmc_material_get_densities(int32_t index, const int** nuclides, const double** densities, int* n);  /* :1389-1407 */
 int openmc_material_get_density(int32_t index, double* density);      /* :1409-1419 */
 int openmc_cell_get_fill(int32_t index, int* type, int32_t** indices, int32_t* n);  /* src/cell.cpp */
+int openmc_cell_get_num_instances(int32_t index, int32_t* num_instances);  /* src/cell.cpp */
+int openmc_cell_bounding_box(const int32_t index, double* llc, double* urc);  /* src/cell.cpp */
+int openmc_global_bounding_box(double* llc, double* urc);              /* src/geometry.cpp */
 int openmc_get_nuclide_index(const char name[], int* index);           /* src/nuclide.cpp */
 int openmc_nuclide_name(int index, const char** name);
 int openmc_get_mesh_index(int32_t id, int32_t* index);                 /* src/mesh.cpp */

@@ -19,9 +19,7 @@ extern "C" {
 typedef struct { double x, y, z; } openmc_gb300_position;  /* Position */
 
 int openmc_calculate_volumes(void);
-int openmc_cell_bounding_box(const int32_t index, double* llc, double* urc);
 int openmc_cell_get_density(int32_t index, const int32_t* instance, double* rho);
-int openmc_cell_get_num_instances(int32_t index, int32_t* num_instances);
 int openmc_cell_get_rotation(int32_t index, double rot[], size_t* n);
 int openmc_cell_get_temperature(int32_t index, const int32_t* instance, double* T);
 int openmc_cell_set_density(int32_t index, double rho, const int32_t* instance, bool set_contained);
@@ -49,7 +47,6 @@ int openmc_extend_tallies(int32_t n, int32_t* index_start, int32_t* index_end);
 int openmc_extend_weight_windows(int32_t n, int32_t* index_start, int32_t* index_end);
 int openmc_filter_set_id(int32_t index, int32_t id);
 int openmc_find_cell(const double* xyz, int32_t* index, int32_t* instance);
-int openmc_global_bounding_box(double* llc, double* urc);
 int openmc_id_map(const void* slice, int32_t* data_out);
 void openmc_initialize_linsolver(const int* indptr, int len_indptr, const int* indices, int n_elements, int dim, double spectral, const int* map, bool use_all_threads);
 void openmc_initialize_mesh_egrid(const int meshtally_id, const int* cmfd_indices, const double norm);

@@ -5,8 +5,10 @@
 // answered from the loaded host model.  Names, arguments, borrowed-pointer
 // returns and error codes follow include/openmc/capi.h and the reference
 // functions cited beside each group.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <map>
@@ -237,6 +239,150 @@ int openmc_cell_get_fill(int32_t index, int* type, int32_t** indices, int32_t* n
   *type = c.fill_type;
   *indices = &c.fill;
   *n = 1;
+  return 0;
+}
+
+// Instances of a cell (src/geometry_aux.cpp count_cell_instances): one per
+// path from the root universe through universe and lattice fills (a
+// lattice's outer universe is not counted).
+static void count_instances(const HModel& m, int univ, std::vector<int32_t>& n, int depth)
+{
+  if (univ < 0 || univ >= static_cast<int>(m.universes.size()) || depth > 64) return;
+  for (int c : m.universes[univ]) {
+    n[c] += 1;
+    const omc::HCell& cell = m.cells[c];
+    if (cell.fill_type == omc::FILL_UNIVERSE) {
+      count_instances(m, cell.fill, n, depth + 1);
+    } else if (cell.fill_type == omc::FILL_LATTICE && cell.fill >= 0 &&
+               cell.fill < static_cast<int>(m.lattices.size())) {
+      for (int u : m.lattices[cell.fill].univ) count_instances(m, u, n, depth + 1);
+    }
+  }
+}
+
+int openmc_cell_get_num_instances(int32_t index, int32_t* num_instances)
+{
+  int rc;
+  HModel* m = model_or_fail(rc);
+  if (!m) return rc;
+  if (!in_range(m->cells, index)) return capi_fail(OPENMC_E_OUT_OF_BOUNDS, "Index in cells array is out of bounds.");
+  std::vector<int32_t> n(m->cells.size(), 0);
+  count_instances(*m, m->root_universe, n, 0);
+  *num_instances = n[index];
+  return 0;
+}
+
+// Bounding boxes (src/cell.cpp:1033-1076 Region::bounding_box, the surfaces'
+// bounding_box(pos_side) in src/surface.cpp, Universe::bounding_box): the
+// half-space of an axis plane bounds one axis, the inside of a cylinder its
+// two transverse axes, the inside of a sphere all three; other half-spaces
+// are unbounded.  Simple regions intersect their half-spaces; complex ones
+// evaluate the postfix with union and intersection, a complemented
+// sub-region counting as unbounded.
+struct Box {
+  double lo[3], hi[3];
+  static Box inf()
+  {
+    const double I = std::numeric_limits<double>::infinity();
+    return Box {{-I, -I, -I}, {I, I, I}};
+  }
+  static Box empty()
+  {
+    const double I = std::numeric_limits<double>::infinity();
+    return Box {{I, I, I}, {-I, -I, -I}};
+  }
+  Box operator&(const Box& o) const
+  {
+    Box b;
+    for (int k = 0; k < 3; ++k) {
+      b.lo[k] = std::max(lo[k], o.lo[k]);
+      b.hi[k] = std::min(hi[k], o.hi[k]);
+    }
+    return b;
+  }
+  Box operator|(const Box& o) const
+  {
+    Box b;
+    for (int k = 0; k < 3; ++k) {
+      b.lo[k] = std::min(lo[k], o.lo[k]);
+      b.hi[k] = std::max(hi[k], o.hi[k]);
+    }
+    return b;
+  }
+};
+
+static Box halfspace_box(const omc::HSurface& s, bool pos_side)
+{
+  Box b = Box::inf();
+  if (s.type <= 2) {  // x-, y-, z-plane at c[0]
+    (pos_side ? b.lo : b.hi)[s.type] = s.c[0];
+  } else if (s.type <= 5 && !pos_side) {  // cylinder along x, y or z
+    const int axis = s.type - 3;
+    const int a = axis == 0 ? 1 : 0, c2 = axis == 2 ? 1 : 2;
+    b.lo[a] = s.c[0] - s.c[2];
+    b.hi[a] = s.c[0] + s.c[2];
+    b.lo[c2] = s.c[1] - s.c[2];
+    b.hi[c2] = s.c[1] + s.c[2];
+  } else if (s.type == 6 && !pos_side) {  // sphere
+    for (int k = 0; k < 3; ++k) {
+      b.lo[k] = s.c[k] - s.c[3];
+      b.hi[k] = s.c[k] + s.c[3];
+    }
+  }
+  return b;
+}
+
+static Box cell_box(const HModel& m, const omc::HCell& c)
+{
+  auto surf = [&](int32_t token) { return halfspace_box(m.surfaces[std::abs(token) - 1], token > 0); };
+  if (c.simple) {
+    Box b = Box::inf();
+    for (int32_t t : c.expr) b = b & surf(t);
+    return b;
+  }
+  std::vector<Box> st;
+  for (int32_t t : c.expr) {
+    if (t == omc::OP_UNION || t == omc::OP_INTERSECTION) {
+      if (st.size() < 2) return Box::inf();
+      Box r = st.back();
+      st.pop_back();
+      st.back() = t == omc::OP_UNION ? (st.back() | r) : (st.back() & r);
+    } else if (t == omc::OP_COMPLEMENT) {
+      if (st.empty()) return Box::inf();
+      st.back() = Box::inf();
+    } else {
+      st.push_back(surf(t));
+    }
+  }
+  return st.empty() ? Box::inf() : st.back();
+}
+
+int openmc_cell_bounding_box(const int32_t index, double* llc, double* urc)
+{
+  int rc;
+  HModel* m = model_or_fail(rc);
+  if (!m) return rc;
+  if (!in_range(m->cells, index)) return capi_fail(OPENMC_E_OUT_OF_BOUNDS, "Index in cells array is out of bounds.");
+  const Box b = cell_box(*m, m->cells[index]);
+  for (int k = 0; k < 3; ++k) {
+    llc[k] = b.lo[k];
+    urc[k] = b.hi[k];
+  }
+  return 0;
+}
+
+int openmc_global_bounding_box(double* llc, double* urc)
+{
+  int rc;
+  HModel* m = model_or_fail(rc);
+  if (!m) return rc;
+  Box b = Box::empty();
+  if (m->root_universe >= 0 && m->root_universe < static_cast<int>(m->universes.size()))
+    for (int c : m->universes[m->root_universe]) b = b | cell_box(*m, m->cells[c]);
+  for (int k = 0; k < 3; ++k) {
+    llc[k] = b.lo[k];
+    urc[k] = b.hi[k];
+  }
   return 0;
 }
 

@@ -30,14 +30,8 @@ extern "C" {
 int openmc_calculate_volumes()
 { return off_path("openmc_calculate_volumes"); }
 
-int openmc_cell_bounding_box(const int32_t index, double* llc, double* urc)
-{ return off_path("openmc_cell_bounding_box"); }
-
 int openmc_cell_get_density(int32_t index, const int32_t* instance, double* rho)
 { return off_path("openmc_cell_get_density"); }
-
-int openmc_cell_get_num_instances(int32_t index, int32_t* num_instances)
-{ return off_path("openmc_cell_get_num_instances"); }
 
 int openmc_cell_get_rotation(int32_t index, double rot[], size_t* n)
 { return off_path("openmc_cell_get_rotation"); }
@@ -121,9 +115,6 @@ int openmc_filter_set_id(int32_t index, int32_t id)
 
 int openmc_find_cell(const double* xyz, int32_t* index, int32_t* instance)
 { return off_path("openmc_find_cell"); }
-
-int openmc_global_bounding_box(double* llc, double* urc)
-{ return off_path("openmc_global_bounding_box"); }
 
 int openmc_id_map(const void* slice, int32_t* data_out)
 { return off_path("openmc_id_map"); }

@@ -209,6 +209,21 @@ def test_model_queries_and_off_path_calls(built, tmp_path):
         assert dll.openmc_get_cell_index(cid, C.byref(i32)) == 0
         assert dll.openmc_cell_get_fill(i32.value, C.byref(ft), C.byref(fidx), C.byref(fn)) == 0
         assert ft.value == 2 and fn.value == 1 and fidx[0] == 0
+        # instances (one per lattice position of the pin universe) and boxes
+        lat = m.geometry.root_universe.cells[0].fill
+        fuel_cell = lat.universes[0][0].cells[0]
+        guide_water = lat.universes[2][5].cells[0]
+        ni = C.c_int32()
+        for cell, expect in ((fuel_cell, 17 * 17 - 25), (guide_water, 25), (m.geometry.root_universe.cells[0], 1)):
+            assert dll.openmc_get_cell_index(cell.id, C.byref(i32)) == 0
+            assert dll.openmc_cell_get_num_instances(i32.value, C.byref(ni)) == 0 and ni.value == expect
+        llc, urc = (C.c_double * 3)(), (C.c_double * 3)()
+        assert dll.openmc_global_bounding_box(llc, urc) == 0
+        assert np.allclose(list(llc), [-10.71, -10.71, -100.0]) and np.allclose(list(urc), [10.71, 10.71, 100.0])
+        assert dll.openmc_get_cell_index(fuel_cell.id, C.byref(i32)) == 0
+        assert dll.openmc_cell_bounding_box(i32.value, llc, urc) == 0
+        assert np.allclose(list(llc)[:2], [-0.41, -0.41]) and np.allclose(list(urc)[:2], [0.41, 0.41])
+        assert np.isinf(llc[2]) and np.isinf(urc[2])
         # a material's nuclides and atom densities (borrowed), and its mass density
         mat = m.materials[0]
         assert dll.openmc_get_material_index(mat.id, C.byref(i32)) == 0

@@ -251,6 +251,7 @@ enum {
   STG_SURF, STG_CELL, STG_TOK, STG_UNIV_OFF, STG_UNIV_CELLS, STG_MAT_OFF, STG_MAT_NUC, STG_MAT_DENS,
   STG_MAT_DENS32, STG_N
 };
+static_assert(STG_N == sizeof(DModel::stage_off) / sizeof(int), "one staging slot per table");
 
 #ifndef OMC_STAGE_MAX_BYTES
 #define OMC_STAGE_MAX_BYTES 32768

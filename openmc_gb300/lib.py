@@ -336,6 +336,212 @@ def global_tallies():
 
 
 # --------------------------------------------------------- weight windows
+# ---- read-only model views (openmc/lib/cell.py, material.py, mesh.py,
+# core.py): objects addressed by index, mappings keyed by id
+_fn("openmc_get_cell_index", [C.c_int32, _p(C.c_int32)])
+_fn("openmc_cell_get_id", [C.c_int32, _p(C.c_int32)])
+_fn("openmc_cell_get_fill", [C.c_int32, _p(C.c_int), _p(_p(C.c_int32)), _p(C.c_int32)])
+_fn("openmc_cell_get_num_instances", [C.c_int32, _p(C.c_int32)])
+_fn("openmc_cell_get_translation", [C.c_int32, _p(C.c_double)])
+_fn("openmc_cell_bounding_box", [C.c_int32, _p(C.c_double), _p(C.c_double)])
+_fn("openmc_global_bounding_box", [_p(C.c_double), _p(C.c_double)])
+_fn("openmc_get_material_index", [C.c_int32, _p(C.c_int32)])
+_fn("openmc_material_get_id", [C.c_int32, _p(C.c_int32)])
+_fn("openmc_material_get_densities", [C.c_int32, _p(_p(C.c_int)), _p(_p(C.c_double)), _p(C.c_int)])
+_fn("openmc_material_get_density", [C.c_int32, _p(C.c_double)])
+_fn("openmc_nuclide_name", [C.c_int, _p(C.c_char_p)])
+_fn("openmc_get_mesh_index", [C.c_int32, _p(C.c_int32)])
+_fn("openmc_mesh_get_id", [C.c_int32, _p(C.c_int32)])
+_fn("openmc_regular_mesh_get_dimension", [C.c_int32, _p(_p(C.c_int)), _p(C.c_int)])
+_fn("openmc_regular_mesh_get_params", [C.c_int32, _p(_p(C.c_double)), _p(_p(C.c_double)),
+                                       _p(_p(C.c_double)), _p(C.c_int)])
+_fn("openmc_get_keff", [_p(C.c_double)])
+
+FILL_TYPES = {0: "material", 1: "universe", 2: "lattice"}
+
+
+class Cell:
+    """A cell of the loaded model (openmc/lib/cell.py Cell, read-only)."""
+
+    def __init__(self, index):
+        self._index = int(index)
+
+    @property
+    def id(self):
+        v = C.c_int32()
+        _dll.openmc_cell_get_id(self._index, v)
+        return v.value
+
+    @property
+    def fill(self):
+        """(type name, index of the material, universe or lattice)."""
+        t, idx, n = C.c_int(), _p(C.c_int32)(), C.c_int32()
+        _dll.openmc_cell_get_fill(self._index, t, idx, n)
+        return FILL_TYPES[t.value], idx[0]
+
+    @property
+    def num_instances(self):
+        v = C.c_int32()
+        _dll.openmc_cell_get_num_instances(self._index, v)
+        return v.value
+
+    @property
+    def translation(self):
+        xyz = (C.c_double * 3)()
+        _dll.openmc_cell_get_translation(self._index, xyz)
+        return np.array(xyz)
+
+    @property
+    def bounding_box(self):
+        lo, hi = (C.c_double * 3)(), (C.c_double * 3)()
+        _dll.openmc_cell_bounding_box(self._index, lo, hi)
+        return np.array(lo), np.array(hi)
+
+
+class Material:
+    """A material of the loaded model (openmc/lib/material.py, read-only)."""
+
+    def __init__(self, index):
+        self._index = int(index)
+
+    @property
+    def id(self):
+        v = C.c_int32()
+        _dll.openmc_material_get_id(self._index, v)
+        return v.value
+
+    def _densities(self):
+        nuc, dens, n = _p(C.c_int)(), _p(C.c_double)(), C.c_int()
+        _dll.openmc_material_get_densities(self._index, nuc, dens, n)
+        return [nuc[k] for k in range(n.value)], np.array([dens[k] for k in range(n.value)])
+
+    @property
+    def nuclides(self):
+        names = []
+        for i in self._densities()[0]:
+            name = C.c_char_p()
+            _dll.openmc_nuclide_name(i, name)
+            names.append(name.value.decode())
+        return names
+
+    @property
+    def densities(self):
+        """Atom densities [atom/b-cm] in the order of ``nuclides``."""
+        return self._densities()[1]
+
+    def get_density(self, units="g/cm3"):
+        if units != "g/cm3":
+            raise ValueError("only g/cm3 is available")
+        v = C.c_double()
+        _dll.openmc_material_get_density(self._index, v)
+        return v.value
+
+
+class RegularMesh:
+    """A regular mesh of the loaded model (openmc/lib/mesh.py, read-only)."""
+
+    def __init__(self, index):
+        self._index = int(index)
+
+    @property
+    def id(self):
+        v = C.c_int32()
+        _dll.openmc_mesh_get_id(self._index, v)
+        return v.value
+
+    @property
+    def dimension(self):
+        dims, n = _p(C.c_int)(), C.c_int()
+        _dll.openmc_regular_mesh_get_dimension(self._index, dims, n)
+        return tuple(dims[k] for k in range(n.value))
+
+    def _params(self):
+        ll, ur, w, n = _p(C.c_double)(), _p(C.c_double)(), _p(C.c_double)(), C.c_int()
+        _dll.openmc_regular_mesh_get_params(self._index, ll, ur, w, n)
+        return [np.array([p[k] for k in range(n.value)]) for p in (ll, ur, w)]
+
+    @property
+    def lower_left(self):
+        return self._params()[0]
+
+    @property
+    def upper_right(self):
+        return self._params()[1]
+
+    @property
+    def width(self):
+        return self._params()[2]
+
+
+class _IdMap:
+    """id -> object mapping over the loaded model (openmc.lib.cells, ...)."""
+
+    def __init__(self, cls, index_fn, id_fn, count):
+        self._cls, self._index_fn, self._id_fn, self._count = cls, index_fn, id_fn, count
+
+    def __getitem__(self, key):
+        idx = C.c_int32()
+        try:
+            self._index_fn(key, idx)
+        except InvalidIDError:
+            raise KeyError(key)
+        return self._cls(idx.value)
+
+    def __len__(self):
+        return self._count()
+
+    def __iter__(self):
+        v = C.c_int32()
+        for i in range(len(self)):
+            self._id_fn(i, v)
+            yield v.value
+
+    def keys(self):
+        return list(iter(self))
+
+    def values(self):
+        return [self[k] for k in self]
+
+    def items(self):
+        return [(k, self[k]) for k in self]
+
+
+def _model_count(k):
+    info = (C.c_int64 * 8)()
+    _dll.openmc_gb300_model_info(info)
+    return int(info[k])
+
+
+def _mesh_count():
+    n, v = 0, C.c_int32()
+    while True:
+        try:
+            _dll.openmc_mesh_get_id(n, v)
+        except OutOfBoundsError:
+            return n
+        n += 1
+
+
+cells = _IdMap(Cell, _dll.openmc_get_cell_index, _dll.openmc_cell_get_id, lambda: _model_count(2))
+materials = _IdMap(Material, _dll.openmc_get_material_index, _dll.openmc_material_get_id, lambda: _model_count(1))
+meshes = _IdMap(RegularMesh, _dll.openmc_get_mesh_index, _dll.openmc_mesh_get_id, _mesh_count)
+
+
+def global_bounding_box():
+    """(lower-left, upper-right) of the root universe (openmc/lib/core.py)."""
+    lo, hi = (C.c_double * 3)(), (C.c_double * 3)()
+    _dll.openmc_global_bounding_box(lo, hi)
+    return np.array(lo), np.array(hi)
+
+
+def keff():
+    """(k, standard deviation): 1 and an infinite (one realization or
+    fewer) or zero spread on this fixed-source path (openmc/lib/core.py)."""
+    k = (C.c_double * 2)()
+    _dll.openmc_get_keff(k)
+    return k[0], k[1]
+
+
 class WeightWindows:
     """openmc.lib.WeightWindows subset (openmc/lib/weight_windows.py)."""
 

@@ -245,3 +245,34 @@ def test_model_queries_and_off_path_calls(built, tmp_path):
         assert b"openmc_calculate_volumes" in (C.c_char * 256).in_dll(dll, "openmc_err_msg").value
     finally:
         lib.finalize()
+
+
+def test_python_model_views(built, tmp_path):
+    """openmc.lib-style views of the loaded model: cells, materials and
+    meshes keyed by id, global bounding box, k-effective."""
+    from openmc_gb300 import configs, lib
+    m, d = configs.lattice17(tmp_path, particles=100, batches=3, n_points=300, mesh_dim=(17, 17, 5), n_ebins=4)
+    m.export_to_model_xml(d)
+    lib.init(directory=d)
+    try:
+        root = m.geometry.root_universe.cells[0]
+        lat = root.fill
+        assert len(lib.cells) == 1 + 3 + 3 and root.id in lib.cells.keys()
+        assert lib.cells[root.id].fill == ("lattice", 0)
+        assert lib.cells[lat.universes[0][0].cells[0].id].num_instances == 17 * 17 - 25
+        lo, hi = lib.global_bounding_box()
+        assert np.allclose(lo, [-10.71, -10.71, -100.0]) and np.allclose(hi, [10.71, 10.71, 100.0])
+        with pytest.raises(KeyError):
+            lib.cells[987654]
+        fuel = lib.materials[m.materials[0].id]
+        assert fuel.nuclides == ["Hv235", "Hv238", "Ox16", "Hv240"]
+        assert np.isclose(fuel.densities.sum(), 0.069) and fuel.get_density() > 0
+        mesh = lib.meshes[m.tallies[0].filters[0].mesh.id]
+        assert mesh.dimension == (17, 17, 5)
+        assert np.allclose(mesh.upper_right - mesh.lower_left, [17 * 1.26, 17 * 1.26, 200.0])
+        assert np.allclose(mesh.width * np.array(mesh.dimension), mesh.upper_right - mesh.lower_left)
+        assert len(lib.meshes) == 1
+        k, s = lib.keff()
+        assert k == 1.0 and np.isinf(s)
+    finally:
+        lib.finalize()

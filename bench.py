@@ -146,6 +146,16 @@ TRAFFIC_PER_ALGORITHMIC_BYTE = {"xs+advance+surface": 2.333, "xs+advance": 1.376
                                 "collision": 1.258}
 
 
+# What bounds the transport kernels instead of HBM: the FP64 pipe busy
+# fraction of the same ncu captures (not measured by this run).
+FP64_PIPE_NOTE = {
+    "xs+advance+surface": {"fp64_pipe_busy": 0.615, "dram_busy": 0.185,
+                           "source": "ncu capture, profiles/advance_surface_collision_lattice17_2M.md"},
+    "collision": {"fp64_pipe_busy": 0.623, "dram_busy": 0.046,
+                  "source": "ncu capture, profiles/advance_surface_collision_lattice17_2M.md"},
+}
+
+
 def algorithmic_bytes(detail, levels, fp32):
     """Bytes each kernel must move per batch: the structure-of-arrays fields
     an event reads and writes, the table bytes of each nuclide lookup (two
@@ -516,7 +526,8 @@ def main():
         "roofline": {"bound": "hbm", "kernel": r["dominant"], "achieved": r["achieved"], "peak": r["peak"],
                      "unit": "GB/s", "frac": r["achieved"] / r["peak"], "peak_source": r["peak_kind"],
                      "traffic": r["traffic"], "alg_bytes_per_launch": r["alg_per_launch"],
-                     "launches": r["dom_launches"]},
+                     "launches": r["dom_launches"],
+                     "limiter": FP64_PIPE_NOTE.get(r["dominant"])},
         "kernels": r["kernel_table"],
         "cpu_baseline": cpu,
         "kernel_ms_profiled_batch": r["kernel_ms"],

@@ -137,22 +137,20 @@ def peaks():
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic
-# byte of each kernel, from an ncu capture of the same kernel on the 2x10^6
-# history lattice with 524,288 slots, matched launch by launch with the
-# OPENMC_GB300_LAUNCH_LOG counts (profiles/advance_surface_collision_lattice17_2M.md;
-# the unfused kernels' ratios come from the same capture of the earlier build).
-# Traffic per launch scales with the events a launch processes.
+# byte of each kernel, from an ncu capture of one launch of the same kernel
+# (iteration 100 of a 2x10^6-history lattice batch, 524,288 slots), matched
+# with that launch's OPENMC_GB300_LAUNCH_LOG counts; the unfused kernels'
+# ratios come from a capture of the unfused kernels.  Traffic per launch
+# scales with the events a launch processes.
 TRAFFIC_PER_ALGORITHMIC_BYTE = {"xs+advance+surface": 2.333, "xs+advance": 1.376, "surface": 1.406,
                                 "collision": 1.258}
 
-
-# What bounds the transport kernels instead of HBM: the FP64 pipe busy
-# fraction of the same ncu captures (not measured by this run).
+# What bounds the transport kernels instead of HBM: the FP64 pipe's busy
+# fraction in the same captures (a committed profile, not measured by this run).
+_CAPTURE = "ncu --set full, iteration 100 of a 2e6-history lattice batch, 524,288 slots"
 FP64_PIPE_NOTE = {
-    "xs+advance+surface": {"fp64_pipe_busy": 0.615, "dram_busy": 0.185,
-                           "source": "ncu capture, profiles/advance_surface_collision_lattice17_2M.md"},
-    "collision": {"fp64_pipe_busy": 0.623, "dram_busy": 0.046,
-                  "source": "ncu capture, profiles/advance_surface_collision_lattice17_2M.md"},
+    "xs+advance+surface": {"fp64_pipe_busy": 0.615, "dram_busy": 0.185, "source": _CAPTURE},
+    "collision": {"fp64_pipe_busy": 0.623, "dram_busy": 0.046, "source": _CAPTURE},
 }
 
 

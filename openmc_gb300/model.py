@@ -640,6 +640,9 @@ class Settings:
             ET.SubElement(el, "log_grid_bins").text = str(int(self.log_grid_bins))
         if self.max_history_splits is not None:
             ET.SubElement(el, "max_history_splits").text = str(int(self.max_history_splits))
+        if self.survival_biasing:
+            # written so that the library rejects it instead of running without it
+            ET.SubElement(el, "survival_biasing").text = "true"
         if self.max_lost_particles is not None:
             ET.SubElement(el, "max_lost_particles").text = str(int(self.max_lost_particles))
         if self.rel_max_lost_particles is not None:

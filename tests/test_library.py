@@ -276,3 +276,19 @@ def test_python_model_views(built, tmp_path):
         assert k == 1.0 and np.isinf(s)
     finally:
         lib.finalize()
+
+
+@pytest.mark.parametrize("case", ["survival_biasing", "eigenvalue"])
+def test_unsupported_settings_rejected(built, tmp_path, case):
+    """Settings the GPU path does not implement fail at openmc_init instead
+    of running without them."""
+    from openmc_gb300 import configs, lib
+    m, d = configs.point_cube(tmp_path, particles=100, batches=2, n_points=300, mesh_dim=(2, 2, 2), n_ebins=2)
+    if case == "survival_biasing":
+        m.settings.survival_biasing = True
+    else:
+        m.settings.run_mode = "eigenvalue"
+    m.export_to_model_xml(d)
+    with pytest.raises(lib.InvalidArgumentError):
+        lib.init(directory=d)
+    lib.finalize()

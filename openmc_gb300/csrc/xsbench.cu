@@ -66,22 +66,24 @@ __device__ __forceinline__ int lb_index(const double* a, int lo, int hi, double 
   return first - lo - 1;
 }
 
-__device__ __forceinline__ int key_of(int mat, double E)
+// Sort key of a lookup: material x 64 + binary exponent of E (clamped to
+// 64 octaves).  A material index outside [0, n_mat) gets key 0, so that the
+// histogram and cursor arrays (n_mat x 64 entries) are never indexed out of
+// range; k_lookup then writes NaN for that lookup.
+__device__ __forceinline__ int key_of(int mat, double E, int n_mat)
 {
+  if (mat < 0 || mat >= n_mat) return 0;
   long long bits = __double_as_longlong(E);
   int ex = static_cast<int>((bits >> 52) & 0x7ff) - 1023 + 32;
   ex = ex < 0 ? 0 : (ex > 63 ? 63 : ex);
   return mat * 64 + ex;
 }
 
-__global__ void k_hist(const int* mat, const double* E, long long n, int* hist)
+__global__ void k_hist(const int* mat, const double* E, long long n, int n_mat, int* hist)
 {
-  extern __shared__ int sh[];
-  const int nk = gridDim.y;  // unused
-  (void)nk;
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<long long>(gridDim.x) * blockDim.x)
-    atomicAdd(&hist[key_of(mat[i], E[i])], 1);
+    atomicAdd(&hist[key_of(mat[i], E[i], n_mat)], 1);
 }
 
 __global__ void k_scan(int* hist, int* cursor, int nk)
@@ -121,11 +123,11 @@ __global__ void k_scan(int* hist, int* cursor, int nk)
   }
 }
 
-__global__ void k_scatter(const int* mat, const double* E, long long n, int* cursor, int* perm)
+__global__ void k_scatter(const int* mat, const double* E, long long n, int n_mat, int* cursor, int* perm)
 {
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<long long>(gridDim.x) * blockDim.x) {
-    int pos = atomicAdd(&cursor[key_of(mat[i], E[i])], 1);
+    int pos = atomicAdd(&cursor[key_of(mat[i], E[i], n_mat)], 1);
     perm[pos] = static_cast<int>(i);
   }
 }
@@ -139,6 +141,14 @@ __global__ void __launch_bounds__(256) k_lookup(Tables T, const int* __restrict_
     int k = perm ? __ldg(perm + j) : static_cast<int>(j);
     int m = __ldg(mat + k);
     double E = __ldg(Ein + k);
+    if (m < 0 || m >= T.n_mat) {
+      // material index out of range: no table is read; NaN results and hash 0
+      double* o = out + static_cast<long long>(k) * 5;
+#pragma unroll
+      for (int c = 0; c < 5; ++c) o[c] = __longlong_as_double(0x7ff8000000000000LL);
+      if (grid_hash) grid_hash[k] = 0;
+      continue;
+    }
     // hash bin: FP32 pre-test, FP64 expression within 1/64 bin of a bin
     // edge (the same exact scheme as the transport kernels)
     int i_log;
@@ -227,6 +237,7 @@ __global__ void k_zero_ints(int* p, int n)
 extern "C" char openmc_err_msg[256];
 extern "C" int OPENMC_E_ALLOCATE;
 extern "C" int OPENMC_E_INVALID_ARGUMENT;
+extern "C" int OPENMC_E_OUT_OF_BOUNDS;
 
 using namespace xsb;
 
@@ -361,9 +372,9 @@ int openmc_gb300_xs_lookup_device(void* handle, int64_t n, const int32_t* d_mat,
     CK(cudaEventRecord(T->ev[0], T->stream));
     if (sort) {
       if (n > T->max_n) throw std::invalid_argument("more lookups than the sort scratch holds");
-      k_hist<<<blocks, 256, 0, T->stream>>>(d_mat, d_E, n, T->keys_hist);
+      k_hist<<<blocks, 256, 0, T->stream>>>(d_mat, d_E, n, T->n_mat, T->keys_hist);
       k_scan<<<1, 1024, 0, T->stream>>>(T->keys_hist, T->keys_cursor, T->n_keys);
-      k_scatter<<<blocks, 256, 0, T->stream>>>(d_mat, d_E, n, T->keys_cursor, T->perm);
+      k_scatter<<<blocks, 256, 0, T->stream>>>(d_mat, d_E, n, T->n_mat, T->keys_cursor, T->perm);
       perm = T->perm;
     }
     CK(cudaEventRecord(T->ev[1], T->stream));
@@ -389,6 +400,12 @@ int openmc_gb300_xs_lookup(void* handle, int64_t n, const int32_t* mat, const do
   try {
     if (!T || n < 0) throw std::invalid_argument("invalid lookup arguments");
     if (n == 0) return 0;
+    for (int64_t i = 0; i < n; ++i)
+      if (mat[i] < 0 || mat[i] >= T->n_mat) {
+        std::snprintf(openmc_err_msg, sizeof(openmc_err_msg),
+                      "lookup %lld: material index %d outside [0, %d)", static_cast<long long>(i), mat[i], T->n_mat);
+        return OPENMC_E_OUT_OF_BOUNDS;
+      }
     CK(cudaMallocAsync(&dm, n * 4, T->stream));
     CK(cudaMallocAsync(&dE, n * 8, T->stream));
     CK(cudaMallocAsync(&dout, n * 40, T->stream));
@@ -484,9 +501,9 @@ int openmc_gb300_xs_lookup_noalloc(void* handle, int64_t n, const int32_t* d_mat
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     int blocks = sms * 8;
     k_zero_ints<<<(T->n_keys + 255) / 256, 256, 0, S>>>(hist, T->n_keys);
-    k_hist<<<blocks, 256, 0, S>>>(d_mat, d_E, n, hist);
+    k_hist<<<blocks, 256, 0, S>>>(d_mat, d_E, n, T->n_mat, hist);
     k_scan<<<1, 1024, 0, S>>>(hist, cursor, T->n_keys);
-    k_scatter<<<blocks, 256, 0, S>>>(d_mat, d_E, n, cursor, perm);
+    k_scatter<<<blocks, 256, 0, S>>>(d_mat, d_E, n, T->n_mat, cursor, perm);
     if (T->fp32) k_lookup<true><<<blocks, 256, 0, S>>>(*T, d_mat, d_E, perm, n, d_out, d_grid_hash);
     else k_lookup<false><<<blocks, 256, 0, S>>>(*T, d_mat, d_E, perm, n, d_out, d_grid_hash);
     CK(cudaGetLastError());

@@ -20,6 +20,10 @@ from . import flatten
 
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "_build" / "liboracle.so"
+# the same source built with the reference's default release flags
+# (RelWithDebInfo: -O2 -g -DNDEBUG, the compiler's default FP contraction) for
+# timing; the parity build keeps every multiply and add separately rounded
+TIMING_LIB_PATH = HERE / "_build" / "liboracle_timing.so"
 REF_PATH = HERE / "_ref" / "librandom_lcg_ref.so"
 
 TRACE_DTYPE = np.dtype([("kind", "<i4"), ("cell", "<i4"), ("material", "<i4"),
@@ -27,22 +31,23 @@ TRACE_DTYPE = np.dtype([("kind", "<i4"), ("cell", "<i4"), ("material", "<i4"),
                         ("n_coord", "<i4"), ("E", "<f8"), ("dist", "<f8"),
                         ("wgt", "<f8")])
 
-_lib = None
+_libs = {}
 
 
 def build(force=False):
-    """Compile the oracle library (make) if missing."""
-    if force or not LIB_PATH.exists():
+    """Compile the oracle libraries (make) if missing."""
+    if force or not LIB_PATH.exists() or not TIMING_LIB_PATH.exists():
         subprocess.run(["make", "-C", str(HERE)], check=True,
                        stdout=subprocess.DEVNULL)
     return LIB_PATH
 
 
-def lib():
-    global _lib
-    if _lib is None:
+def lib(timing=False):
+    """The parity build of the oracle library, or with timing=True the
+    timing build of the same source."""
+    if timing not in _libs:
         build()
-        L = C.CDLL(str(LIB_PATH))
+        L = C.CDLL(str(TIMING_LIB_PATH if timing else LIB_PATH))
         vp, i64, i32, dbl = C.c_void_p, C.c_int64, C.c_int32, C.c_double
         pd = C.POINTER(C.c_double)
         pi32 = C.POINTER(C.c_int32)
@@ -86,8 +91,8 @@ def lib():
         L.oracle_xsb_destroy.argtypes = [vp]
         L.oracle_xsb_grid_index.argtypes = [vp, pi32]
         L.oracle_xsb_lookup.argtypes = [vp, i64, pi32, pd, pd, pi32, C.c_int]
-        _lib = L
-    return _lib
+        _libs[timing] = L
+    return _libs[timing]
 
 
 def ref_lib():
@@ -111,8 +116,10 @@ def _p(a, t):
 class Oracle:
     """One oracle simulation built from a model.xml."""
 
-    def __init__(self, model_xml, cross_sections=None):
-        L = lib()
+    def __init__(self, model_xml, cross_sections=None, timing=False):
+        """timing=True runs the timing build (the reference's release
+        flags) instead of the parity build."""
+        self.L = L = lib(timing)
         self.arrays = flatten.load_model(model_xml, cross_sections)
         blob = flatten.to_blob(self.arrays)
         err = C.create_string_buffer(512)
@@ -125,21 +132,21 @@ class Oracle:
 
     def __del__(self):
         if getattr(self, "h", None):
-            lib().oracle_destroy(self.h)
+            self.L.oracle_destroy(self.h)
             self.h = None
 
     def set_trace(self, n_hist, cap=256, batch=1):
-        lib().oracle_set_trace(self.h, n_hist, cap, batch)
+        self.L.oracle_set_trace(self.h, n_hist, cap, batch)
         self._trace = (n_hist, cap)
 
     def transport(self, batch, first=1, count=None, mode=0, threads=1, in_flight=0):
         count = self.n_particles if count is None else count
-        rc = lib().oracle_transport(self.h, batch, first, count, mode, threads, in_flight)
+        rc = self.L.oracle_transport(self.h, batch, first, count, mode, threads, in_flight)
         if rc != 0:
-            raise RuntimeError(lib().oracle_error(self.h).decode())
+            raise RuntimeError(self.L.oracle_error(self.h).decode())
 
     def accumulate(self):
-        lib().oracle_accumulate(self.h)
+        self.L.oracle_accumulate(self.h)
 
     def run(self, batches=None, threads=1, mode=0, count=None):
         for b in range(1, (batches or self.n_batches) + 1):
@@ -147,23 +154,23 @@ class Oracle:
             self.accumulate()
 
     def tally(self, t):
-        L = lib()
+        L = self.L
         n = L.oracle_tally_size(self.h, t)
         ptr = L.oracle_tally_results(self.h, t)
         return np.ctypeslib.as_array(ptr, shape=(n,)).reshape(-1, 3).copy()
 
     @property
     def n_tallies(self):
-        return lib().oracle_n_tallies(self.h)
+        return self.L.oracle_n_tallies(self.h)
 
     def globals(self):
         out = np.zeros(8)
-        lib().oracle_globals(self.h, _p(out, C.c_double))
+        self.L.oracle_globals(self.h, _p(out, C.c_double))
         return out
 
     def traces(self):
         n_hist, cap = self._trace
-        L = lib()
+        L = self.L
         raw = L.oracle_trace_data(self.h)
         buf = (C.c_char * (n_hist * cap * TRACE_DTYPE.itemsize)).from_address(raw)
         rec = np.frombuffer(buf, TRACE_DTYPE).reshape(n_hist, cap).copy()
@@ -176,14 +183,14 @@ class Oracle:
         n = len(e)
         tot, ab = np.empty(n), np.empty(n)
         gh = np.empty(n, np.int32)
-        lib().oracle_macro_xs(self.h, n, _p(mats, C.c_int32), _p(e, C.c_double),
+        self.L.oracle_macro_xs(self.h, n, _p(mats, C.c_int32), _p(e, C.c_double),
                               _p(tot, C.c_double), _p(ab, C.c_double), _p(gh, C.c_int32))
         return tot, ab, gh
 
     def grid_index(self, nuc):
-        n = lib().oracle_grid_index(self.h, nuc, None, 0)
+        n = self.L.oracle_grid_index(self.h, nuc, None, 0)
         out = np.empty(n, np.int32)
-        lib().oracle_grid_index(self.h, nuc, _p(out, C.c_int32), n)
+        self.L.oracle_grid_index(self.h, nuc, _p(out, C.c_int32), n)
         return out
 
 

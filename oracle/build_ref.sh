@@ -2,9 +2,11 @@
 # Oracle test infrastructure: compile the reference's src/random_lcg.cpp (the
 # one hot-path source of the reference that builds without cmake, HDF5,
 # pugixml, fmt or xtensor) into oracle/_ref/librandom_lcg_ref.so.
-# Usage: oracle/build_ref.sh [reference_root]   (default /root/reference)
+# Usage: oracle/build_ref.sh [reference_root]
+# The reference tree comes from the argument, else OPENMC_REF_ROOT, else the
+# read-only mount /root/reference of the build container.
 set -e
-REF=${1:-/root/reference}
+REF=${1:-${OPENMC_REF_ROOT:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 if [ ! -f "$REF/src/random_lcg.cpp" ]; then
   echo "reference source not found at $REF; skipping" >&2

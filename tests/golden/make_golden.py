@@ -1,7 +1,7 @@
 """Generate the golden fixtures that pin the oracle to the reference.
 
-Run in a container where the reference tree is mounted (default
-/root/reference) after ``oracle/build_ref.sh`` has compiled the reference's
+Run in a container where the reference tree is mounted (the argument, else
+OPENMC_REF_ROOT, else /root/reference) after ``oracle/build_ref.sh`` has compiled the reference's
 src/random_lcg.cpp into oracle/_ref/:
 
     python tests/golden/make_golden.py [reference_root]
@@ -14,6 +14,7 @@ Writes
                          values produced by the reference's own random_lcg.cpp
 """
 import json
+import os
 import re
 import sys
 from pathlib import Path
@@ -74,7 +75,7 @@ def rng_vectors():
 
 
 if __name__ == "__main__":
-    ref_root = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref_root = Path(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("OPENMC_REF_ROOT", "/root/reference"))
     (HERE / "test_math_golden.json").write_text(json.dumps(parse_test_math(ref_root), indent=1))
     (HERE / "rng_golden.json").write_text(json.dumps(rng_vectors(), indent=1))
     print("wrote", HERE / "test_math_golden.json", HERE / "rng_golden.json")

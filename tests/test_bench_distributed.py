@@ -29,3 +29,7 @@ def test_reference_arm_two_ranks(built):
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
+    # the reference arm runs the oracle's timing build and never maps this
+    # package's CUDA library
+    assert d["libraries_mapped"] == ["oracle/_build/liboracle_timing.so"], d["libraries_mapped"]
+    assert d["cpu_baseline"]["history_based"]["value"] > 0

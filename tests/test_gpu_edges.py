@@ -1,5 +1,6 @@
 """Edge cases on the GPU: a single history, a single particle slot, a model
-without tallies, empty lookups, a one-row network, lost particles (a
+without tallies, empty lookups, out-of-range material indices, a one-row
+network, lost particles (a
 geometry with a hole) and a full split ring, the last two ending as error
 codes of openmc_next_batch."""
 import numpy as np
@@ -55,6 +56,39 @@ def test_empty_and_single_lookups(built):
     out, h = t.lookup(np.array([1], np.int32), np.array([data.E_MAX]))
     assert np.isfinite(out).all()
     t.close()
+
+
+def test_lookup_material_index_out_of_range(built):
+    """A material index outside [0, n_mat): the host-buffer lookup returns
+    OPENMC_E_OUT_OF_BOUNDS before any work; the device-buffer lookup reads no
+    table for it, writes NaN and hash 0, and leaves every other lookup as the
+    all-valid call computes it (sorted and unsorted)."""
+    import torch
+    from openmc_gb300 import data, lib
+    d = data.make_xsbench(n_nuc=6, n_points=300, seed=2, mat_counts=(4, 2, 3))
+    mats, e = data.xsbench_lookups(d, 5000, seed=3)
+    t = lib.XSTables(d, n_log_bins=200, max_lookups=len(e))
+    try:
+        good, good_h = t.lookup(mats, e)
+        bad = mats.copy()
+        bad[[7, 100, 4999]] = [-1, 3, 1 << 20]
+        with pytest.raises(lib.OutOfBoundsError):
+            t.lookup(bad, e)
+        dev = torch.device("cuda", 0)
+        dm, de = torch.from_numpy(bad).to(dev), torch.from_numpy(e).to(dev)
+        for sort in (True, False):
+            out = torch.zeros((len(e), 5), dtype=torch.float64, device=dev)
+            h = torch.full((len(e),), -7, dtype=torch.int32, device=dev)
+            torch.cuda.synchronize()  # the lookup runs on the library's own stream
+            t.lookup_device(len(e), dm.data_ptr(), de.data_ptr(), out.data_ptr(), h.data_ptr(), sort=sort)
+            torch.cuda.synchronize()
+            o, hh = out.cpu().numpy(), h.cpu().numpy()
+            ok = np.ones(len(e), bool)
+            ok[[7, 100, 4999]] = False
+            assert np.isnan(o[~ok]).all() and (hh[~ok] == 0).all()
+            assert np.array_equal(o[ok], good[ok]) and np.array_equal(hh[ok], good_h[ok])
+    finally:
+        t.close()
 
 
 def test_one_row_network(built):

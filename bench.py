@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--in-flight", type=int, default=0,
                     help="particle slots held on the device (0: the library's default, 2^19)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-table extra measurement")
+    ap.add_argument("--fp64-batches", type=int, default=20,
+                    help="batches of the FP64-table run whose tally the FP32 tally is compared with")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=0,
                     help="histories in the CPU baseline sample (default 3,000,000: about 10 s on 16 cores)")
@@ -58,10 +60,37 @@ def parse():
                     help="skip the shield figure-of-merit extra (plain, MAGIC and learned windows)")
     ap.add_argument("--network-only", action="store_true",
                     help="only time the importance network's training kernels (for kernel profilers)")
+    ap.add_argument("--no-contract", action="store_true",
+                    help="FP32-table mode on the transport build with separately rounded FP64 multiplies "
+                         "and adds (default: the build with fused multiply-adds)")
+    ap.add_argument("--no-defer", action="store_true",
+                    help="score track-length tallies inside the advance kernel instead of from track records")
     ap.add_argument("--no-graph", action="store_true",
                     help="launch every batch kernel by kernel instead of as one CUDA graph "
                          "(for kernel profilers, which cannot see inside conditional graphs)")
     return ap.parse_args()
+
+
+def mapped_libraries():
+    """Shared libraries of this repository mapped into the process (Linux
+    /proc/self/maps), relative to the repository root."""
+    out = set()
+    try:
+        with open("/proc/self/maps") as f:
+            for line in f:
+                path = line.split()[-1] if line.strip() else ""
+                if path.endswith(".so") and path.startswith(str(ROOT)):
+                    out.add(str(Path(path).relative_to(ROOT)))
+    except OSError:
+        return None
+    return sorted(out)
+
+
+def config_of(args):
+    """The workload, identical in both arms (each arm states its histories
+    per step beside it)."""
+    return {"workload": WORKLOAD, "xs_tables": "fp32 (reference arm: fp64)",
+            "parallelism": f"{args.gpus} ranks, histories sharded by seed" if args.gpus > 1 else "single GPU"}
 
 
 def model_dir(particles):
@@ -154,12 +183,15 @@ FP64_PIPE_NOTE = {
 }
 
 
-def algorithmic_bytes(detail, levels, fp32):
+def algorithmic_bytes(detail, levels, fp32, deferred=True):
     """Bytes each kernel must move per batch: the structure-of-arrays fields
     an event reads and writes, the table bytes of each nuclide lookup (two
     hash-window bounds, two bracketing energies, two table rows, nuclide
     index, atom density) and 16 B of tally read-modify-write per mesh
-    segment.  The tail kernel moves the bytes of every event it runs."""
+    segment (in the track-length tally kernel when scoring is deferred, else
+    in the advance kernel; the track records that carry a flight from one
+    kernel to the other are traffic of this design, not algorithmic bytes).
+    The tail kernel moves the bytes of every event it runs."""
     row = 16 if fp32 else 32
     dens = 4 if fp32 else 8
     per_nuc = 8 + 16 + 2 * row + 4 + dens
@@ -167,12 +199,16 @@ def algorithmic_bytes(detail, levels, fp32):
     def parts(st):
         return {
             "xs": st["xs_events"] * 36 + st["xs_calc"] * 16 + st["xs_nuclide_lookups"] * per_nuc,
-            "advance": st["xs_events"] * (136 + 72 * levels) + st["mesh_segments"] * 16,
+            "advance": st["xs_events"] * (136 + 72 * levels),
+            "tally": st["mesh_segments"] * 16,
             "surface": st["surface"] * (120 + 96 * levels),
             "collision": st["collision"] * 128 + st["collision_nuclide_lookups"] * per_nuc,
         }
     q = parts(detail["queue"])
     q["tail"] = sum(parts(detail["tail"]).values())
+    if not deferred:
+        # scored inside the advance kernel
+        q["advance"] += q.pop("tally")
     q["xs+advance"] = q["xs"] + q["advance"]
     q["xs+advance+surface"] = q["xs"] + q["advance"] + q["surface"]
     return q
@@ -189,6 +225,8 @@ def run_gb300(args, barrier=lambda: None, rank=0):
         # ranks shard the histories: each rank runs its own random streams
         lib.settings.seed = 1 + rank
         lib.settings.xs_fp32 = 1
+        lib.settings.contract = 0 if args.no_contract else 1
+        lib.settings.defer_tally = 0 if args.no_defer else 1
         lib.settings.particles_in_flight = args.in_flight
         fused = int(lib.settings.fuse_xs)
         sort = int(lib.settings.sort_queue)
@@ -229,13 +267,14 @@ def run_gb300(args, barrier=lambda: None, rank=0):
         levels = 2
         lib.simulation_finalize()
         fp32_tally = lib.tally_mean_std(tid)
+        fp32_n = lib.tally_n_realizations(tid)
     finally:
         lib.finalize()
     total_ms = sum(dev_ms)
     value = args.steps * n / (total_ms / 1000.0)
     e2e = args.steps * n / sum(wall)
     kms = prof["kernel_ms"]
-    byts = algorithmic_bytes(prof, levels, True)
+    byts = algorithmic_bytes(prof, levels, True, deferred=not args.no_defer)
     kms = dict(kms)
     # fused events run inside the advance kernel; their own spans only time event records
     if fused & 2:
@@ -276,14 +315,19 @@ def run_gb300(args, barrier=lambda: None, rank=0):
             lib.settings.xs_fp32 = 0
             lib.settings.particles_in_flight = args.in_flight
             lib.simulation_init()
-            # five batches, so that the tally comparison has usable error bars
-            for _ in range(4):
+            # as many batches as the FP32 tally holds at least (warm-up +
+            # timed + profiled), so that both sigmas have the same degrees
+            # of freedom
+            n64 = max(args.fp64_batches, 2)
+            for _ in range(n64 - 1):
                 lib.next_batch()
             flush_l2(flush)
             lib.next_batch()
             out["fp64_value"] = n / (lib.last_batch()["ms"] / 1000.0)
             lib.simulation_finalize()
-            out["fp32_vs_fp64"] = compare_tallies(fp32_tally, lib.tally_mean_std(lib.tally_ids()[0]))
+            t64 = lib.tally_ids()[0]
+            out["fp32_vs_fp64"] = compare_tallies(fp32_tally, lib.tally_mean_std(t64), fp32_n,
+                                                  lib.tally_n_realizations(t64))
         finally:
             lib.finalize()
         # the same batch through the history-based kernel (settings.event_based = False)
@@ -307,20 +351,26 @@ def run_gb300(args, barrier=lambda: None, rank=0):
 def shield_fom():
     """The metric's second half: figure of merit 1/(R^2 T) of the back-face
     flux of the 200 cm deep-penetration shield (densities x 0.1, 200 x 10 x 10
-    mesh x 6 energy groups) for plain transport, MAGIC windows and learned
-    windows from the same 5 x 10^6-history pilot, 10 x 10^6 histories each,
-    FP32 tables; T is the device time of the measured batches.  A failure
-    here is reported in the line instead of ending the bench."""
+    mesh x 6 energy groups) for plain transport (200 x 10^6 histories),
+    MAGIC windows and learned windows from the same 5 x 10^6-history pilot
+    (10 x 10^6 histories each), FP32 tables; T is the device time of the
+    measured batches (and, in fom_with_setup, also of the pilot and the
+    network's training).  Each figure of merit carries its relative
+    uncertainty.  A failure here is reported in the line instead of ending
+    the bench."""
     from openmc_gb300 import shield_study
     try:
-        r = shield_study.run(ROOT / "_models" / "shield_bench")
+        # the plain arm runs 200 batches, so that its back-face relative
+        # error (0.43 after 10 batches) comes down to ~0.1
+        r = shield_study.run(ROOT / "_models" / "shield_bench", plain_batches=200)
     except Exception as e:  # the transport line above stands on its own
         return {"error": f"{type(e).__name__}: {e}"}
-    out = {"workload": r["workload"], "pilot": r["pilot"], "measure": r["measure"]}
+    out = {"workload": r["workload"], "pilot": r["pilot"], "measure": r["measure"],
+           "measure_plain": r["measure_plain"], "pilot_device_s": r["pilot_device_s"]}
+    keys = ("fom", "fom_rel_unc", "rel_err", "back_mean", "batches", "device_s", "setup_s", "fom_with_setup",
+            "fom_gain", "fom_gain_rel_unc", "fom_gain_with_setup")
     for k in ("plain", "magic", "learned"):
-        v = r[k]
-        out[k] = {"fom": v["fom"], "rel_err": v["rel_err"], "back_mean": v["back_mean"],
-                  "device_s": v["device_s"], **({"fom_gain": v["fom_gain"]} if "fom_gain" in v else {})}
+        out[k] = {key: r[k][key] for key in keys if key in r[k]}
     out["z"] = {k: r[k] for k in ("z_magic_plain", "z_learned_plain", "z_learned_magic") if k in r}
     return out
 
@@ -354,28 +404,65 @@ def network_bench(rows=1 << 20, steps=20):
                     "bound by memory traffic, not by the tensor cores"}
 
 
-def compare_tallies(a, b):
+def compare_tallies(a, b, n_a, n_b):
     """FP32-table tally (a) against the FP64-table tally (b), both
-    (mean, std of the mean): share of bins scored by both within 3 combined
-    sigma, the largest |z|, the largest relative difference among the bins
-    both runs converged to 1 % relative error (with the largest combined
-    relative error of those bins beside it), and the relative difference of
-    the summed flux with its combined sigma."""
+    (mean, std of the mean) over n_a and n_b batches.
+
+    Per bin scored by both runs, z = (mean_a - mean_b) / hypot(s_a, s_b).
+    Each sigma is estimated from its batches, so z follows Student's t with
+    the Welch-Satterthwaite degrees of freedom of the bin, not a normal law:
+    the expected share beyond 3 (and the expected count beyond 5) is the
+    mean over bins of that t law's two-sided tail, which the observed share
+    is reported beside, with the equal-variance (pooled) t law's share as
+    the lower bound of the expectation.  A bias of the FP32 tables would show as a signed-z
+    mean away from 0 among the well-converged bins (standard error
+    1/sqrt(count)).  Per tally: the relative difference of the summed flux
+    with its z, and the largest relative difference among bins both runs
+    converged to 1 % relative error, with the largest combined relative
+    error of those bins beside it."""
     ma, sa = (np.asarray(x, float).ravel() for x in a)
     mb, sb = (np.asarray(x, float).ravel() for x in b)
     both = (sa > 0) & (sb > 0)
-    z = np.abs(ma - mb)[both] / np.hypot(sa, sb)[both]
+    va, vb = sa[both] ** 2, sb[both] ** 2
+    zs = (ma - mb)[both] / np.sqrt(va + vb)
+    z = np.abs(zs)
+    dof = (va + vb) ** 2 / (va ** 2 / max(n_a - 1, 1) + vb ** 2 / max(n_b - 1, 1))
+    try:
+        from scipy.stats import t as student_t
+        exp3 = float(np.mean(2 * student_t.sf(3.0, dof)))
+        # equal-variance bound: the pooled t law with n_a + n_b - 2 degrees of
+        # freedom (lighter tails than the per-bin Welch estimate, which
+        # over-predicts the tail when each sigma has few batches)
+        exp3_pooled = float(2 * student_t.sf(3.0, n_a + n_b - 2))
+        exp5 = float(np.sum(2 * student_t.sf(5.0, dof)))
+        pval = 2 * student_t.sf(z, dof)
+        # share of bins whose two-sided p-value is below 0.27 % (the 3-sigma
+        # level of a normal law): uniform p-values give 0.0027
+        p_share = float(np.mean(pval < 0.0027))
+    except ImportError:
+        exp3 = exp5 = p_share = exp3_pooled = None
     ta, tb = ma.sum(), mb.sum()
     st = np.sqrt((sa ** 2).sum() + (sb ** 2).sum())
     conv = both & (sa < 0.01 * np.abs(ma)) & (sb < 0.01 * np.abs(mb))
     rel = np.abs(ma - mb)[conv] / np.abs(mb)[conv]
     crel = np.hypot(sa, sb)[conv] / np.abs(mb)[conv]
-    return {"bins_scored_by_both": int(both.sum()), "share_within_3_sigma": float((z <= 3).mean()),
-            "max_abs_z": float(z.max()), "converged_bins": int(conv.sum()),
+    zc = (ma - mb)[conv] / np.hypot(sa, sb)[conv]
+    return {"batches": [int(n_a), int(n_b)], "bins_scored_by_both": int(both.sum()),
+            "share_within_3_sigma": float((z <= 3).mean()),
+            "share_beyond_3_sigma": float((z > 3).mean()),
+            "expected_share_beyond_3_sigma_t": exp3,
+            "expected_share_beyond_3_sigma_pooled_t": exp3_pooled,
+            "share_p_below_0.0027_t": p_share,
+            "beyond_5_sigma": int((z > 5).sum()), "expected_beyond_5_sigma_t": exp5,
+            "median_dof": float(np.median(dof)), "max_abs_z": float(z.max()),
+            "mean_signed_z_all": float(zs.mean()),
+            "converged_bins": int(conv.sum()),
+            "mean_signed_z_converged": float(zc.mean()) if zc.size else None,
+            "mean_signed_z_converged_stderr": float(1 / np.sqrt(zc.size)) if zc.size else None,
             "max_rel_diff_converged": float(rel.max()) if rel.size else None,
             "max_combined_rel_err_converged": float(crel.max()) if crel.size else None,
             "total_rel_diff": float((ta - tb) / tb),
-            "total_z": float(abs(ta - tb) / st) if st > 0 else None}
+            "total_z": float((ta - tb) / st) if st > 0 else None}
 
 
 def xs_lookup_bench(fp32, n=17_000_000, reps=5):
@@ -420,11 +507,13 @@ def xs_lookup_bench(fp32, n=17_000_000, reps=5):
 
 
 def cpu_baseline(path, sample, threads=None, mode=1):
-    """Oracle transport of `sample` histories of batch 1 on the host cores:
-    mode 1 = event-based loop (100,000 particles in flight, the reference's
-    default max_particles_in_flight), mode 0 = history-based loop."""
+    """Oracle transport of `sample` histories of batch 1 on the host cores,
+    timing build (the reference's release flags): mode 1 = event-based loop
+    (100,000 particles in flight, the reference's default
+    max_particles_in_flight), mode 0 = history-based loop (the reference's
+    default mode)."""
     import oracle
-    o = oracle.Oracle(path / "model.xml")
+    o = oracle.Oracle(path / "model.xml", timing=True)
     threads = threads or os.cpu_count()
     t0 = time.perf_counter()
     o.transport(1, 1, sample, mode=mode, threads=threads, in_flight=100000 if mode == 1 else 0)
@@ -436,9 +525,15 @@ def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
-    import __graft_entry__
     if rank == 0:
-        __graft_entry__.build()
+        if args.impl == "reference":
+            # the CPU implementation only: the oracle's libraries, not this
+            # package's CUDA library
+            import oracle
+            oracle.build()
+        else:
+            import __graft_entry__
+            __graft_entry__.build()
         model_dir(args.particles)  # written once, before the other ranks read it
     if world > 1:
         import torch.distributed as dist
@@ -449,24 +544,34 @@ def main():
             return
         path = model_dir(args.particles)
         sample = args.cpu_sample or 2_000_000
-        vals = []
         cores = os.cpu_count()
         for _ in range(args.warmup):
             cpu_baseline(path, max(sample // 10, 1000), cores)
         t_all = 0.0
         for _ in range(args.steps):
-            v, cores, dt = cpu_baseline(path, sample, cores)
-            vals.append(v)
+            _, cores, dt = cpu_baseline(path, sample, cores)
             t_all += dt
         value = args.steps * sample / t_all
+        # the reference's default mode, beside the event-based rate the ratio uses
+        hist_sample = max(sample // 2, 1000)
+        vh, _, dth = cpu_baseline(path, hist_sample, cores, mode=0)
         line = {"metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * t_all / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic (seeded nuclides, full-size model)", "impl": "reference",
-                "config": {"workload": WORKLOAD, "histories_per_step": sample, "threads": cores},
+                "config": config_of(args),
+                "histories_per_step": sample,
+                "sample_note": (f"each step transports {sample} of the workload's 10^7-history batch: "
+                                f"a full batch takes ~30 s on the host cores, and the run must end "
+                                f"within a few minutes; particles/s does not depend on the batch size here"),
+                "ratio_mode": "event-based (the metric's loop); history-based beside it",
                 "cpu_baseline": {"value": value, "unit": "particles/s", "cores": cores, "kind": "port",
-                                 "sample": f"{sample} histories of batch 1 per step, event-based OpenMP loop"},
+                                 "build": "timing (reference release flags: -O2 -g -DNDEBUG, default FP contraction)",
+                                 "sample": f"{sample} histories of batch 1 per step, event-based OpenMP loop",
+                                 "history_based": {"value": vh, "unit": "particles/s",
+                                                   "sample": f"{hist_sample} histories ({dth:.1f} s)"}},
                 "e2e": {"value": value, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        line["libraries_mapped"] = mapped_libraries()
         print(json.dumps(line))
         return
     import torch
@@ -514,9 +619,9 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32-xs/f64-geometry",
         "data": "synthetic (seeded nuclides, full-size model)",
-        "config": {"workload": WORKLOAD, "histories_per_step": args.particles,
-                   "l2": "flushed between steps (512 MB write)", "xs_tables": "fp32",
-                   "parallelism": f"{args.gpus} ranks, histories sharded by seed" if args.gpus > 1 else "single GPU"},
+        "config": config_of(args),
+        "histories_per_step": args.particles,
+        "l2": "flushed between steps (512 MB write)",
         "e2e": {"value": r["e2e"], "unit": "particles/s", "h2d_bytes_per_step": 256,
                 "d2h_bytes_per_step": r["e2e_d2h"]},
         "gpu_launches": r["launches"],

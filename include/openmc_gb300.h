@@ -134,6 +134,16 @@ extern int openmc_gb300_max_levels;
  * they fit in 32 KB) and reads them there; 0 (default): read through L1 from
  * global memory, where tables of a few KB stay resident */
 extern int openmc_gb300_stage_tables;
+/* 1 (default): FP32-table mode with at most 2 coordinate levels runs the
+ * transport build whose FP64 multiply-adds are fused (one rounding each, the
+ * default of most compilers); 0: the build that rounds every FP64 multiply
+ * and add separately, as FP64-table mode always does */
+extern int openmc_gb300_contract;
+/* 1 (default): in the event loop, the advance kernel writes each flight as a
+ * track record and a separate kernel scores the track-length tallies from
+ * them (score_tracklength_tally, src/tallies/tally_scoring.cpp:2416-2541);
+ * 0: the advance kernel scores them itself */
+extern int openmc_gb300_defer_tally;
 
 /* last batch: [ms, iterations, events, total_weight, leakage, lost, done, secondary-pool entries used,
  *  events of the longest history, its particle id] */
@@ -141,7 +151,7 @@ int openmc_gb300_last_batch(double* out);
 /* [queue phase: xs events, xs recomputations, xs nuclide lookups, mesh
  *  segments, collision nuclide lookups, surface events, collisions; tail
  *  phase: the same seven; kernel ms: xs, advance, surface, collision, tail,
- *  refill, sort, other] */
+ *  refill, sort, other, track-length tally] (23 doubles) */
 int openmc_gb300_last_batch_detail(double* out);
 /* [time_active s, time_inactive s, wall_active s, particles/s (active), in-flight slots] */
 int openmc_gb300_timing(double* out);
@@ -162,7 +172,11 @@ int openmc_gb300_material_xs(int64_t n, const int32_t* material, const double* E
                              double* absorption, uint32_t* grid_hash);
 
 /* macroscopic-XS lookup on flat 5-channel tables; counterpart of
- * Material::calculate_neutron_xs (src/material.cpp:829-901) per lookup */
+ * Material::calculate_neutron_xs (src/material.cpp:829-901) per lookup.
+ * Material indices outside [0, n_mat): openmc_gb300_xs_lookup (host
+ * buffers) returns OPENMC_E_OUT_OF_BOUNDS before any work; the device-buffer
+ * entry points cannot check before queuing the work, so such a lookup reads
+ * no table and gets NaN results and grid hash 0. */
 int openmc_gb300_xs_tables_create(int n_nuc, int G, const double* energy, const double* xs,
   int n_mat, const int32_t* mat_off, const int32_t* mat_nuc, const double* mat_dens,
   int n_log_bins, int fp32, int64_t max_lookups, void** handle);

@@ -3,7 +3,8 @@
 Produces ``openmc_gb300/_lib/libopenmc_gb300.so`` from the sources in
 ``openmc_gb300/csrc``.  Translation units compile in parallel; device code is
 built for ``sm_103a`` only with ``-fmad=false`` so that every floating-point
-multiply and add rounds separately, as in the reference's C++ expressions.
+multiply and add rounds separately, as in the reference's C++ expressions;
+the transport build that FP32-table mode runs (namespace l2f) fuses them.
 """
 from __future__ import annotations
 
@@ -18,12 +19,16 @@ CSRC = PKG / "csrc"
 OUT = PKG / "_lib"
 LIB = OUT / "libopenmc_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-fmad=false"]
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC"]
+EXACT = ["-fmad=false"]
 SOURCES = ["host_model.cpp", "capi.cpp", "capi_model.cpp", "capi_offpath.cpp", "transport_dispatch.cpp", "xsbench.cu",
            "mlp.cu"]
 # transport.cu is built once per maximum coordinate depth (namespaces l2, l4)
-VARIANTS = [("transport.cu", "transport_l2", ["-DOMC_MAXL=2", "-DOMC_NS=l2"]),
-            ("transport.cu", "transport_l4", ["-DOMC_MAXL=4", "-DOMC_NS=l4"])]
+# with separately rounded multiplies and adds, and once for FP32-table mode at
+# depth 2 with multiply-adds fused (l2f)
+VARIANTS = [("transport.cu", "transport_l2", ["-DOMC_MAXL=2", "-DOMC_NS=l2", *EXACT]),
+            ("transport.cu", "transport_l4", ["-DOMC_MAXL=4", "-DOMC_NS=l4", *EXACT]),
+            ("transport.cu", "transport_l2f", ["-DOMC_MAXL=2", "-DOMC_NS=l2f", "-fmad=true"])]
 
 
 def nvcc():
@@ -42,7 +47,7 @@ def _compile(src: Path, obj: Path, extra):
 
 
 def build(force: bool = False, verbose: bool = False, extra=()) -> Path:
-    units = [(CSRC / s, Path(s).stem, []) for s in SOURCES if (CSRC / s).exists()]
+    units = [(CSRC / s, Path(s).stem, list(EXACT)) for s in SOURCES if (CSRC / s).exists()]
     units += [(CSRC / s, stem, flags) for s, stem, flags in VARIANTS]
     srcs = [u[0] for u in units]
     headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh"))

@@ -78,6 +78,8 @@ int openmc_gb300_split_to_slots = 0;  // split particles start in free slots wit
 int openmc_gb300_stage_tables = 0;    // event kernels copy the geometry/material tables into shared memory
 int openmc_gb300_max_levels = 0;      // coordinate depth of the transport kernels (0: from the model)
 int openmc_gb300_xs_fp32 = -1;          // -1: from XML (<gb300_xs_precision>), else 0/1
+int openmc_gb300_contract = 1;          // FP32-table mode: transport build with fused FP64 multiply-adds
+int openmc_gb300_defer_tally = 1;       // track-length tallies scored by their own kernel from track records
 int64_t openmc_gb300_in_flight = 0;     // particle slots; 0: setting or automatic
 int openmc_gb300_sort = 1;              // sort the XS queue by (material, energy)
 int openmc_gb300_trace_batch = 1;       // batch whose histories openmc_gb300_set_trace records
@@ -381,6 +383,8 @@ int openmc_simulation_init()
     opt.max_levels = openmc_gb300_max_levels;
     opt.stage_tables = openmc_gb300_stage_tables;
     opt.fuse = openmc_gb300_fuse;
+    opt.contract = openmc_gb300_contract;
+    opt.defer_tally = openmc_gb300_defer_tally;
     if (m.ww_on && m.weight_windows.empty()) return fail(OPENMC_E_INVALID_ARGUMENT, "weight windows are on but none are defined");
     s.gpu = gpu_create(m, opt);
     if (s.trace_hist > 0) gpu_set_trace(s.gpu, s.trace_hist, s.trace_cap, openmc_gb300_trace_batch, openmc_gb300_trace_first);
@@ -809,14 +813,14 @@ int openmc_gb300_last_batch(double* out)
 
 // [queue phase: xs events, xs recomputations, xs nuclide lookups, mesh
 //  segments, collision nuclide lookups, surface events, collisions;
-//  tail phase: the same seven; kernel ms x8 (xs, advance, surface, collision,
-//  tail, refill, sort, other)]
+//  tail phase: the same seven; kernel ms x9 (xs, advance, surface, collision,
+//  tail, refill, sort, other, track-length tally)]
 int openmc_gb300_last_batch_detail(double* out)
 {
   const BatchStats& b = S().last;
   for (int a = 0; a < 2; ++a)
     for (int k = 0; k < 7; ++k) out[7 * a + k] = static_cast<double>(b.stat[a][k]);
-  for (int k = 0; k < 8; ++k) out[14 + k] = b.kernel_ms[k];
+  for (int k = 0; k < 9; ++k) out[14 + k] = b.kernel_ms[k];
   return 0;
 }
 

@@ -112,6 +112,11 @@ struct DModel {
   // tallies
   int n_tally;
   int n_tally_tracklength, n_tally_collision;
+  // what a deferred track record must carry beyond position, direction,
+  // length, weight and energy: the macroscopic XS (a track-length tally
+  // scores total or absorption), the cells of every level (a cell filter),
+  // the material (a material filter)
+  int trk_xs, trk_cells, trk_mat;
   const DTally* tally;
   const DFilter* filt;
   const DMesh* mesh;
@@ -211,7 +216,22 @@ struct SourceSite {
   unsigned long long tseed;
 };
 
+// Track records of one event iteration, written by the advance kernel at the
+// event's queue position and scored by the track-length tally kernel
+// (deferred scoring).  Structure of arrays over the bank capacity; inv_u only
+// in FP32-table mode, mt/ma, mat and cell only when a tally needs them.
+struct DTracks {
+  double *r0x, *r0y, *r0z;  // start of the flight (level 0)
+  double *ux, *uy, *uz;
+  double *iux, *iuy, *iuz;  // 1 / u (FP32-table mode)
+  double *d, *w, *E;        // flight length, weight (0: no record), pre-event energy
+  double *mt, *ma;          // macroscopic total and absorption XS
+  int* mat;                 // material
+  int* cell;                // [MAXL][cap] cells of the levels, C_NONE past n_coord
+};
+
 struct DQueues {
+  DTracks trk;           // deferred track records (trk.w null: tallies score inline)
   SourceSite* src_bank;  // [n_particles] or null (sites sampled at refill)
   long long src_n;
   int* q_in;

@@ -952,11 +952,16 @@ __device__ int ev_surface_g(long long s, EvStats& st, Geo& g, double wgt, int bs
 // with_surf: a particle that reaches the boundary crosses it right away from
 // the registers (the surface event always follows such an advance), instead
 // of storing its state for a surface pass to reload.
-template<bool with_surf>
-__device__ int ev_advance(long long s, EvStats& st)
+// defer: the track-length tallies are not scored here; the flight is written
+// as a track record at the event's queue position qi for k_score_tracks.
+template<bool with_surf, bool defer = false>
+__device__ int ev_advance(long long s, EvStats& st, int qi = 0)
 {
   double wgt = db.wgt[s];
-  if (wgt == 0.0) return revive_or_free(s, wgt) ? NEXT_XS : NEXT_DEAD;
+  if (wgt == 0.0) {
+    if (defer && dq.trk.w) dq.trk.w[qi] = 0.0;  // no record
+    return revive_or_free(s, wgt) ? NEXT_XS : NEXT_DEAD;
+  }
   Geo g;
   geo_load(g, s);
   double bd;
@@ -987,7 +992,32 @@ __device__ int ev_advance(long long s, EvStats& st)
     g.r[l][1] = g.r[l][1] + distance * g.u[1];
     g.r[l][2] = g.r[l][2] + distance * g.u[2];
   }
-  if (dm.n_tally_tracklength > 0) {
+  if (defer && dq.trk.w) {
+    const DTracks& T = dq.trk;
+    T.r0x[qi] = r0[0];
+    T.r0y[qi] = r0[1];
+    T.r0z[qi] = r0[2];
+    T.ux[qi] = g.u[0];
+    T.uy[qi] = g.u[1];
+    T.uz[qi] = g.u[2];
+    if (recip) {
+      T.iux[qi] = inv_u[0];
+      T.iuy[qi] = inv_u[1];
+      T.iuz[qi] = inv_u[2];
+    }
+    T.d[qi] = distance;
+    T.w[qi] = wgt;
+    T.E[qi] = db.E[s];
+    if (dm.trk_xs) {
+      T.mt[qi] = mt;
+      T.ma[qi] = db.macro_a[s];
+    }
+    if (dm.trk_mat) T.mat[qi] = db.material[s];
+    if (dm.trk_cells) {
+#pragma unroll
+      for (int l = 0; l < MAXL; ++l) T.cell[l * db.cap + qi] = l < g.n_coord ? g.cell[l] : C_NONE;
+    }
+  } else if (!defer && dm.n_tally_tracklength > 0) {
     LevelCells lc;
 #pragma unroll
     for (int l = 0; l < MAXL; ++l) lc.c[l] = g.cell[l];
@@ -1437,7 +1467,10 @@ __global__ void __launch_bounds__(256) k_xs()
 // advance, src/event.cpp:119-124); its latency-bound lookups then overlap
 // the FP64 work of the other warps instead of running as a separate pass.
 // Per-history results do not depend on either fusion.
-template<bool with_xs, bool with_surf>
+// defer: track-length tallies are scored afterwards by k_score_tracks from
+// the track records this kernel writes (the scoring code, the largest user
+// of registers in this kernel, then stays out of it).
+template<bool with_xs, bool with_surf, bool defer>
 __global__ void __launch_bounds__(256, OMC_MINB_ADV) k_advance()
 {
   if (dq.cnt->tail) return;
@@ -1450,10 +1483,54 @@ __global__ void __launch_bounds__(256, OMC_MINB_ADV) k_advance()
     long long s = valid ? dq.q_in[i] : 0;
     EvStats st {};
     if (with_xs && valid) ev_xs(s, st);
-    int nx = valid ? ev_advance<with_surf>(s, st) : NEXT_DEAD;
+    int nx = valid ? ev_advance<with_surf, defer>(s, st, i) : NEXT_DEAD;
     if (!with_surf) warp_append(dq.q_surf, &dq.cnt->n_surf, static_cast<int>(s), nx == NEXT_SURF);
     warp_append(dq.q_coll, &dq.cnt->n_coll, static_cast<int>(s), nx == NEXT_COLL);
     warp_append(dq.q_tmp, &dq.cnt->n_next, static_cast<int>(s), nx == NEXT_XS);
+    flush_stats(st, 0);
+  }
+}
+
+// Track-length tallies of this iteration's advance events
+// (src/tallies/tally_scoring.cpp:2416-2541, the same score_tracklength as the
+// inline path) from the records k_advance wrote at each event's queue
+// position.  The end point is recomputed with the advance's own expression
+// r0 + d u, so the mesh walk sees the same points; only the order of the
+// FP64 atomic additions differs, which atomics leave open anyway.
+__global__ void __launch_bounds__(256) k_score_tracks()
+{
+  if (dq.cnt->tail) return;
+  const DTracks& T = dq.trk;
+  const int n = dq.cnt->n_q;
+  const int stride = gridDim.x * blockDim.x;
+  const bool recip = dm.xs_fp32 != 0;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const int i = base + threadIdx.x;
+    EvStats st {};
+    const double w = i < n ? T.w[i] : 0.0;
+    if (w != 0.0) {
+      const double d = T.d[i];
+      const double r0[3] = {T.r0x[i], T.r0y[i], T.r0z[i]};
+      const double u[3] = {T.ux[i], T.uy[i], T.uz[i]};
+      double inv_u[3] = {0.0, 0.0, 0.0};
+      if (recip) {
+        inv_u[0] = T.iux[i];
+        inv_u[1] = T.iuy[i];
+        inv_u[2] = T.iuz[i];
+      }
+      const double r1[3] = {r0[0] + d * u[0], r0[1] + d * u[1], r0[2] + d * u[2]};
+      LevelCells lc;
+      lc.n = 0;
+#pragma unroll
+      for (int l = 0; l < MAXL; ++l) {
+        lc.c[l] = dm.trk_cells ? T.cell[l * db.cap + i] : C_NONE;
+        if (lc.c[l] != C_NONE) lc.n = l + 1;
+      }
+      const double mt = dm.trk_xs ? T.mt[i] : 0.0;
+      const double ma = dm.trk_xs ? T.ma[i] : 0.0;
+      const int mat = dm.trk_mat ? T.mat[i] : C_NONE;
+      st.seg += score_tracklength(r0, r1, u, T.E[i], w, d, mt, ma, lc, mat, recip ? inv_u : nullptr);
+    }
     flush_stats(st, 0);
   }
 }
@@ -1808,6 +1885,7 @@ struct GpuSim {
   int fuse = 3;  // bit 0: cross-section event, bit 1: surface crossing, inside the advance kernel
   int split_slots = 0;  // split particles start in free slots with their own seeds
   int history = 0;      // history-based loop (settings.event_based false)
+  int defer = 0;        // track-length tallies scored by k_score_tracks from track records
   long long tail_threshold = 1 << 15;  // measured best on the 17x17 lattice (2^17: +1 %, 2^19: +10 %)
   int tail_max_events = 1 << 16;
   // dynamic shared memory of the event kernels: the staged tables (option
@@ -2061,6 +2139,16 @@ static void build_model(GpuSim& G, const HModel& m, const GpuOptions& opt)
   d.n_tally = static_cast<int>(tallies.size());
   d.n_tally_tracklength = d.n_tally_collision = 0;
   for (const auto& t : tallies) (t.estimator == 1 ? d.n_tally_collision : d.n_tally_tracklength) += 1;
+  d.trk_xs = d.trk_cells = d.trk_mat = 0;
+  for (const auto& t : tallies) {
+    if (t.estimator != 0) continue;
+    for (int j = 0; j < t.nscore; ++j)
+      if (t.score[j] != 0) d.trk_xs = 1;
+    for (int j = 0; j < t.nfilt; ++j) {
+      if (filts[t.filt[j]].type == 3) d.trk_cells = 1;
+      if (filts[t.filt[j]].type == 4) d.trk_mat = 1;
+    }
+  }
   G.d_value = dev_alloc<double>(off, own);
   G.d_sum = dev_alloc<double>(off, own);
   G.d_sumsq = dev_alloc<double>(off, own);
@@ -2154,6 +2242,30 @@ static void build_bank(GpuSim& G, long long cap, long long sec_cap)
     q.src_bank = dev_alloc<SourceSite>(G.model.n_particles, own);
     q.src_n = G.model.n_particles;
   }
+  q.trk = DTracks {};
+  if (G.defer) {
+    DTracks& T = q.trk;
+    T.r0x = dev_alloc<double>(cap, own);
+    T.r0y = dev_alloc<double>(cap, own);
+    T.r0z = dev_alloc<double>(cap, own);
+    T.ux = dev_alloc<double>(cap, own);
+    T.uy = dev_alloc<double>(cap, own);
+    T.uz = dev_alloc<double>(cap, own);
+    if (G.model.xs_fp32) {
+      T.iux = dev_alloc<double>(cap, own);
+      T.iuy = dev_alloc<double>(cap, own);
+      T.iuz = dev_alloc<double>(cap, own);
+    }
+    T.d = dev_alloc<double>(cap, own);
+    T.w = dev_alloc<double>(cap, own);
+    T.E = dev_alloc<double>(cap, own);
+    if (G.model.trk_xs) {
+      T.mt = dev_alloc<double>(cap, own);
+      T.ma = dev_alloc<double>(cap, own);
+    }
+    if (G.model.trk_mat) T.mat = dev_alloc<int>(cap, own);
+    if (G.model.trk_cells) T.cell = dev_alloc<int>(cap * MAXL, own);
+  }
   G.cnt = dev_alloc<DCounters>(1, own);
   q.cnt = G.cnt;
   q.trace = nullptr;
@@ -2175,6 +2287,19 @@ static void upload_constants(GpuSim& G)
   CK(cudaMemcpyToSymbol(dm, &G.model, sizeof(DModel)));
   CK(cudaMemcpyToSymbol(db, &G.bank, sizeof(DBank)));
   CK(cudaMemcpyToSymbol(dq, &G.queues, sizeof(DQueues)));
+}
+
+// The advance kernel of the fusion and tally options.  Scoring inside the
+// advance is built only for the fully fused form (gpu_create checks); the
+// deferred forms also serve models without track-length tallies, where no
+// record is written.
+static void launch_advance(const GpuSim& G, cudaStream_t S)
+{
+  const int nb = G.blocks, nt = 256;
+  if (!G.defer && G.model.n_tally_tracklength > 0) k_advance<true, true, false><<<nb, nt, G.smem, S>>>();
+  else if (G.fuse == 3) k_advance<true, true, true><<<nb, nt, G.smem, S>>>();
+  else if (G.fuse == 1) k_advance<true, false, true><<<nb, nt, G.smem, S>>>();
+  else k_advance<false, false, true><<<nb, nt, G.smem, S>>>();
 }
 
 static void build_graph(GpuSim& G)
@@ -2211,13 +2336,9 @@ static void build_graph(GpuSim& G)
   CK(cudaGraphAddNode(&cond, graph, nodes.data(), nullptr, n_nodes, &cp));
   cudaGraph_t body = cp.conditional.phGraph_out[0];
   CK(cudaStreamBeginCaptureToGraph(G.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-  if (G.fuse & 1) {
-    if (G.fuse & 2) k_advance<true, true><<<nb, nt, G.smem, G.stream>>>();
-    else k_advance<true, false><<<nb, nt, G.smem, G.stream>>>();
-  } else {
-    k_xs<<<nb, nt, G.smem, G.stream>>>();
-    k_advance<false, false><<<nb, nt, G.smem, G.stream>>>();
-  }
+  if (!(G.fuse & 1)) k_xs<<<nb, nt, G.smem, G.stream>>>();
+  launch_advance(G, G.stream);
+  if (G.defer) k_score_tracks<<<nb, nt, 0, G.stream>>>();
   if (!(G.fuse & 2)) k_surface<<<nb, nt, G.smem, G.stream>>>();
   k_collision<<<nb, nt, G.smem, G.stream>>>();
   k_tail<<<nb * 2, 128, G.smem, G.stream>>>(G.tail_max_events);
@@ -2254,6 +2375,9 @@ GpuSim* gpu_create(const HModel& m, const GpuOptions& opt)
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
     G->blocks = sms * 8;
     build_model(*G, m, opt);
+    G->defer = (!G->history && opt.defer_tally && G->model.n_tally_tracklength > 0) ? 1 : 0;
+    if (!G->history && !opt.defer_tally && G->model.n_tally_tracklength > 0 && G->fuse != 3)
+      throw std::runtime_error("track-length tallies scored inside the advance need the fused advance (fuse 3)");
     // 2^19 slots (~200 MB of particle state for two levels) keep the bank's
     // working set close to the 129 MB L2; on the 17x17 lattice 2^19 slots
     // ran 10 % faster than 2^20 and 2^18 or 1.5 x 2^20 slower
@@ -2372,7 +2496,7 @@ BatchStats gpu_run_batch_profiled(GpuSim* G, HModel& m, int batch, bool accumula
   cudaEvent_t ev[n_ev];
   for (auto& e : ev) CK(cudaEventCreate(&e));
   BatchStats st {};
-  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   auto span = [&](int a, int b) {
     float ms;
     CK(cudaEventElapsedTime(&ms, ev[a], ev[b]));
@@ -2393,7 +2517,7 @@ BatchStats gpu_run_batch_profiled(GpuSim* G, HModel& m, int batch, bool accumula
       if (launch_log)
         std::fprintf(launch_log,
           "advance_launch,batch,iteration,xs_events,xs_calc,xs_nuclide_lookups,mesh_segments,"
-          "collision_nuclide_lookups,surface,collision,advance_ms,surface_ms,collision_ms\n");
+          "collision_nuclide_lookups,surface,collision,advance_ms,surface_ms,collision_ms,tally_ms\n");
     }
   }
   CK(cudaEventRecord(ev[0], S));
@@ -2408,9 +2532,9 @@ BatchStats gpu_run_batch_profiled(GpuSim* G, HModel& m, int batch, bool accumula
     CK(cudaEventRecord(ev[2], S));
     if (!(G->fuse & 1)) k_xs<<<nb, nt, G->smem, S>>>();
     CK(cudaEventRecord(ev[3], S));
-    if (G->fuse == 3) k_advance<true, true><<<nb, nt, G->smem, S>>>();
-    else if (G->fuse == 1) k_advance<true, false><<<nb, nt, G->smem, S>>>();
-    else k_advance<false, false><<<nb, nt, G->smem, S>>>();
+    launch_advance(*G, S);
+    CK(cudaEventRecord(ev[12], S));
+    if (G->defer) k_score_tracks<<<nb, nt, 0, S>>>();
     CK(cudaEventRecord(ev[4], S));
     if (!(G->fuse & 2)) k_surface<<<nb, nt, G->smem, S>>>();
     CK(cudaEventRecord(ev[5], S));
@@ -2435,7 +2559,8 @@ BatchStats gpu_run_batch_profiled(GpuSim* G, HModel& m, int batch, bool accumula
     CK(cudaMemcpyAsync(&c, G->cnt, sizeof(c), cudaMemcpyDeviceToHost, S));
     CK(cudaStreamSynchronize(S));
     acc[0] += span(2, 3);
-    acc[1] += span(3, 4);
+    acc[1] += span(3, 12);
+    acc[8] += span(12, 4);
     acc[2] += span(4, 5);
     acc[3] += span(5, 6);
     acc[4] += span(6, 11);
@@ -2449,14 +2574,14 @@ BatchStats gpu_run_batch_profiled(GpuSim* G, HModel& m, int batch, bool accumula
         std::fprintf(launch_log, ",%llu", c.stat[0][b] - prev[b]);
         prev[b] = c.stat[0][b];
       }
-      std::fprintf(launch_log, ",%.6f,%.6f,%.6f\n", span(3, 4), span(4, 5), span(5, 6));
+      std::fprintf(launch_log, ",%.6f,%.6f,%.6f,%.6f\n", span(3, 12), span(4, 5), span(5, 6), span(12, 4));
     }
     ++advance_launches;
     if (!c.more) break;
   }
   if (launch_log) std::fflush(launch_log);
   double total = 0;
-  for (int k = 0; k < 8; ++k) {
+  for (int k = 0; k < 9; ++k) {
     st.kernel_ms[k] = static_cast<float>(acc[k]);
     total += acc[k];
   }

@@ -21,6 +21,8 @@ struct GpuOptions {
   int split_slots = 0;          // split particles start in free slots with their own seeds
   int max_levels = 0;           // coordinate depth of the kernels (0: the model's, rounded up to 2 or 4)
   int stage_tables = 0;         // copy the cell/surface/material tables into shared memory per block
+  int contract = 1;             // FP32-table mode: run the build with FP64 multiply-adds fused
+  int defer_tally = 1;          // track-length tallies scored by their own kernel from track records
 };
 
 struct BatchStats {
@@ -39,13 +41,16 @@ struct BatchStats {
   // segments, collision nuclide lookups, surface events, collisions]
   unsigned long long stat[2][7] = {{0, 0, 0, 0, 0, 0, 0}, {0, 0, 0, 0, 0, 0, 0}};
   // per-kernel device milliseconds from a profiled batch:
-  // xs, advance, surface, collision, tail, refill, sort, other
-  float kernel_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  // xs, advance, surface, collision, tail, refill, sort, other, track-length tally
+  float kernel_ms[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 };
 
-// The interface below is implemented twice (transport.cu built for at most
-// 2 and at most 4 coordinate levels, namespaces l2 and l4); the functions in
-// omc itself pick the build from the model's depth (transport_dispatch.cpp).
+// The interface below is implemented three times: transport.cu built for at
+// most 2 and at most 4 coordinate levels with every FP64 multiply and add
+// rounded separately (namespaces l2 and l4: the reference's arithmetic), and
+// for at most 2 levels with multiply-adds fused (l2f: FP32-table mode only,
+// where results are compared statistically, not bit for bit); the functions
+// in omc itself pick the build (transport_dispatch.cpp).
 #define OMC_GPU_API(NS)                                                                     \
   namespace NS {                                                                            \
   struct GpuSim;                                                                            \
@@ -66,6 +71,7 @@ struct BatchStats {
 
 OMC_GPU_API(l2)
 OMC_GPU_API(l4)
+OMC_GPU_API(l2f)
 
 GpuSim* gpu_create(const HModel& m, const GpuOptions& opt);
 void gpu_destroy(GpuSim* g);

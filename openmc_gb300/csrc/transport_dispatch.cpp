@@ -1,8 +1,13 @@
-// Picks the transport build for a model's coordinate depth.  transport.cu is
-// compiled twice: for at most 2 levels (omc::l2), whose per-level particle
-// state then fits in registers, and for at most 4 levels (omc::l4).  Both
-// builds run the same code and give identical results; the deeper one only
-// holds more levels.
+// Picks the transport build for a model's coordinate depth and table
+// precision.  transport.cu is compiled three times: for at most 2 levels
+// (omc::l2), whose per-level particle state then fits in registers, and for at
+// most 4 levels (omc::l4), both with every FP64 multiply and add rounded
+// separately (the reference's arithmetic, identical results in both); and for
+// at most 2 levels with multiply-adds fused into FMAs (omc::l2f), which the
+// FP32-table mode runs by default: it still computes positions, directions,
+// distances and tallies in FP64, with one rounding per multiply-add instead
+// of two, and its results are checked statistically against the FP64-table
+// path rather than bit for bit.
 #include <stdexcept>
 
 #include "transport.h"
@@ -11,8 +16,10 @@ namespace omc {
 
 struct GpuSim {
   int levels = 4;
+  bool fused = false;  // the l2f build
   l2::GpuSim* g2 = nullptr;
   l4::GpuSim* g4 = nullptr;
+  l2f::GpuSim* g2f = nullptr;
 };
 
 GpuSim* gpu_create(const HModel& m, const GpuOptions& opt)
@@ -21,7 +28,11 @@ GpuSim* gpu_create(const HModel& m, const GpuOptions& opt)
   try {
     int want = opt.max_levels > 0 ? opt.max_levels : m.n_coord_levels;
     if (want < m.n_coord_levels) want = m.n_coord_levels;
-    if (want <= 2) {
+    if (want <= 2 && opt.xs_fp32 && opt.contract) {
+      g->levels = 2;
+      g->fused = true;
+      g->g2f = l2f::gpu_create(m, opt);
+    } else if (want <= 2) {
       g->levels = 2;
       g->g2 = l2::gpu_create(m, opt);
     } else {
@@ -40,11 +51,13 @@ void gpu_destroy(GpuSim* g)
   if (!g) return;
   if (g->g2) l2::gpu_destroy(g->g2);
   if (g->g4) l4::gpu_destroy(g->g4);
+  if (g->g2f) l2f::gpu_destroy(g->g2f);
   delete g;
 }
 
-#define OMC_FORWARD(name, ...) \
-  return g->levels == 2 ? l2::name(g->g2, ##__VA_ARGS__) : l4::name(g->g4, ##__VA_ARGS__)
+#define OMC_FORWARD(name, ...)                                                   \
+  return g->fused ? l2f::name(g->g2f, ##__VA_ARGS__)                             \
+                  : (g->levels == 2 ? l2::name(g->g2, ##__VA_ARGS__) : l4::name(g->g4, ##__VA_ARGS__))
 
 BatchStats gpu_run_batch(GpuSim* g, HModel& m, int batch, bool accumulate)
 {

@@ -69,32 +69,40 @@ class PhysicsError(OpenMCError):
     pass
 
 
+# Exported error-code globals of the C API and the exception each one raises
+# (the reference's openmc.lib maps the same codes to the same exception
+# names; OPENMC_E_WARNING becomes a Python warning instead).
+_ERROR_CLASSES = {
+    "OPENMC_E_ALLOCATE": AllocationError,
+    "OPENMC_E_OUT_OF_BOUNDS": OutOfBoundsError,
+    "OPENMC_E_INVALID_ARGUMENT": InvalidArgumentError,
+    "OPENMC_E_INVALID_TYPE": InvalidTypeError,
+    "OPENMC_E_INVALID_ID": InvalidIDError,
+    "OPENMC_E_GEOMETRY": GeometryError,
+    "OPENMC_E_DATA": DataError,
+    "OPENMC_E_PHYSICS": PhysicsError,
+}
+_code_to_class = None
+
+
 def _error_handler(err, func, args):
-    """Raise according to the error code (openmc/lib/error.py:8-41)."""
-    def code(name):
-        return C.c_int.in_dll(_dll, name).value
+    """ctypes errcheck: 0 passes through; OPENMC_E_WARNING (a positive code)
+    issues a warning; a negative code raises the exception its exported
+    OPENMC_E_* global names, with the library's openmc_err_msg as the
+    message."""
+    global _code_to_class
+    if err == 0:
+        return err
     msg = (C.c_char * 256).in_dll(_dll, "openmc_err_msg").value.decode()
-    if err == code("OPENMC_E_ALLOCATE"):
-        raise AllocationError(msg)
-    elif err == code("OPENMC_E_OUT_OF_BOUNDS"):
-        raise OutOfBoundsError(msg)
-    elif err == code("OPENMC_E_INVALID_ARGUMENT"):
-        raise InvalidArgumentError(msg)
-    elif err == code("OPENMC_E_INVALID_TYPE"):
-        raise InvalidTypeError(msg)
-    if err == code("OPENMC_E_INVALID_ID"):
-        raise InvalidIDError(msg)
-    elif err == code("OPENMC_E_GEOMETRY"):
-        raise GeometryError(msg)
-    elif err == code("OPENMC_E_DATA"):
-        raise DataError(msg)
-    elif err == code("OPENMC_E_PHYSICS"):
-        raise PhysicsError(msg)
-    elif err == code("OPENMC_E_WARNING"):
+    if err == C.c_int.in_dll(_dll, "OPENMC_E_WARNING").value:
         warnings.warn(msg)
-    elif err < 0:
-        raise OpenMCError(msg or f"Unknown error encountered (code {err}).")
-    return err
+        return err
+    if err > 0:
+        return err
+    if _code_to_class is None:
+        _code_to_class = {C.c_int.in_dll(_dll, name).value: cls for name, cls in _ERROR_CLASSES.items()}
+    cls = _code_to_class.get(err, OpenMCError)
+    raise cls(msg or f"error code {err} from {getattr(func, '__name__', 'the library')}")
 
 
 def _fn(name, argtypes, restype=C.c_int, check=True):
@@ -206,6 +214,8 @@ class _Settings:
     split_to_slots = _DLLGlobal(C.c_int, "openmc_gb300_split_to_slots")
     max_levels = _DLLGlobal(C.c_int, "openmc_gb300_max_levels")
     stage_tables = _DLLGlobal(C.c_int, "openmc_gb300_stage_tables")
+    contract = _DLLGlobal(C.c_int, "openmc_gb300_contract")
+    defer_tally = _DLLGlobal(C.c_int, "openmc_gb300_defer_tally")
 
     @property
     def seed(self):
@@ -627,14 +637,14 @@ def last_batch():
 def last_batch_detail():
     """Event statistics of the last batch for the queue and tail phases, and
     per-kernel milliseconds when the batch ran with settings.profile_next."""
-    out = (C.c_double * 22)()
+    out = (C.c_double * 23)()
     _dll.openmc_gb300_last_batch_detail(out)
     v = list(out)
     keys = ("xs_events", "xs_calc", "xs_nuclide_lookups", "mesh_segments",
             "collision_nuclide_lookups", "surface", "collision")
     d = {"queue": dict(zip(keys, v[0:7])), "tail": dict(zip(keys, v[7:14]))}
-    d["kernel_ms"] = dict(zip(("xs", "advance", "surface", "collision", "tail", "refill", "sort", "other"),
-                              v[14:22]))
+    d["kernel_ms"] = dict(zip(("xs", "advance", "surface", "collision", "tail", "refill", "sort", "other",
+                               "tally"), v[14:23]))
     return d
 
 

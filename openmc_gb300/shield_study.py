@@ -80,13 +80,23 @@ def _fom(m, s, t):
     return 1.0 / ((s / m) ** 2 * t) if m > 0 and s > 0 else 0.0
 
 
-def _summary(r):
+def _fom_rel_unc(batches):
+    """Relative standard uncertainty of a figure of merit 1/(R^2 T) whose R
+    comes from `batches` batch means: R^2 is a sample variance over
+    batches - 1 degrees of freedom, whose relative standard deviation is
+    sqrt(2 / (batches - 1)) for normal batch means (heavier-tailed batch
+    sums make it larger)."""
+    return float(np.sqrt(2.0 / (batches - 1))) if batches > 1 else float("inf")
+
+
+def _summary(r, batches, setup_s=0.0):
     m, s = float(r["back"][0].ravel()[0]), float(r["back"][1].ravel()[0])
     rel = s / m if m > 0 else float("inf")
     lm, ls = r["layers"][0].ravel(), r["layers"][1].ravel()
-    return {"back_mean": m, "back_std": s, "rel_err": rel, "device_s": r["device_s"],
-            "wall_s": r["wall_s"], "fom": _fom(m, s, r["device_s"]), "events": r["events"],
-            "secondaries": r["secondaries"],
+    return {"back_mean": m, "back_std": s, "rel_err": rel, "batches": batches, "device_s": r["device_s"],
+            "wall_s": r["wall_s"], "fom": _fom(m, s, r["device_s"]), "fom_rel_unc": _fom_rel_unc(batches),
+            "setup_s": setup_s, "fom_with_setup": _fom(m, s, r["device_s"] + setup_s),
+            "events": r["events"], "secondaries": r["secondaries"],
             "layer_mean": lm.tolist(), "layer_std": ls.tolist(),
             "layer_fom": [_fom(a, b, r["device_s"]) for a, b in zip(lm, ls)]}
 
@@ -94,12 +104,21 @@ def _summary(r):
 def run(directory, length=200.0, mesh_dim=(200, 10, 10), n_points=11303, pilot_particles=1_000_000,
         pilot_batches=5, particles=1_000_000, batches=10, steps=2000, lr=2e-3, ratio=5.0, fp32=True,
         methods=("plain", "magic", "learned"), density_scale=DENSITY_SCALE, verbose=False,
-        split_to_slots=True):
+        split_to_slots=True, plain_batches=None):
+    """plain_batches: batches of the plain arm (default `batches`); its back-
+    face estimate needs many more histories than the windowed arms' for a
+    comparable relative error, and the figure of merit does not depend on
+    the run length.  Each method's figure of merit is reported with its
+    relative uncertainty, and also with T including the setup the method
+    needs (the pilot run for MAGIC and learned windows, plus the network's
+    training for the learned ones)."""
+    plain_batches = plain_batches or batches
     path, geom = build(directory, length, mesh_dim, n_points, density_scale=density_scale)
     out = {"workload": f"shield {length:g} cm, mesh {mesh_dim}, {geom.n_groups} energy groups, "
                        f"densities x {density_scale:g}",
            "split_to_slots": bool(split_to_slots),
-           "pilot": f"{pilot_batches} x {pilot_particles}", "measure": f"{batches} x {particles}"}
+           "pilot": f"{pilot_batches} x {pilot_particles}", "measure": f"{batches} x {particles}",
+           "measure_plain": f"{plain_batches} x {particles}"}
     lib.init(directory=path)
     saved = (lib.settings.xs_fp32, lib.settings.split_to_slots)
     try:
@@ -121,12 +140,16 @@ def run(directory, length=200.0, mesh_dim=(200, 10, 10), n_points=11303, pilot_p
             out["learned"] = {"pairs": fit.n_pairs, "loss_first": float(fit.loss[0]),
                               "loss_last": float(fit.loss[-1]), "train_ms": fit.train_ms,
                               "steps": steps}
+        setup = {"plain": 0.0, "magic": pilot["device_s"],
+                 "learned": pilot["device_s"] + (out["learned"]["train_ms"] * 1e-3 if "learned" in out else 0.0)}
+        out["pilot_device_s"] = pilot["device_s"]
         res = {}
         for name in methods:
             ww.bounds = bounds[name]
-            r = _run(particles, batches, windows_on=(name != "plain"), log=name if verbose else None)
+            nb = plain_batches if name == "plain" else batches
+            r = _run(particles, nb, windows_on=(name != "plain"), log=name if verbose else None)
             res[name] = r
-            out[name] = {**out.get(name, {}), **_summary(r)}
+            out[name] = {**out.get(name, {}), **_summary(r, nb, setup[name])}
     finally:
         lib.settings.xs_fp32, lib.settings.split_to_slots = saved
         lib.finalize()
@@ -134,6 +157,8 @@ def run(directory, length=200.0, mesh_dim=(200, 10, 10), n_points=11303, pilot_p
     for name in methods:
         if name != "plain" and base > 0:
             out[name]["fom_gain"] = out[name]["fom"] / base
+            out[name]["fom_gain_rel_unc"] = float(np.hypot(out[name]["fom_rel_unc"], out["plain"]["fom_rel_unc"]))
+            out[name]["fom_gain_with_setup"] = out[name]["fom_with_setup"] / base
         if name != "plain" and "plain" in out:
             out[name]["layer_fom_gain"] = [a / b if b > 0 else None
                                            for a, b in zip(out[name]["layer_fom"], out["plain"]["layer_fom"])]
@@ -155,6 +180,7 @@ def main():
     ap.add_argument("--pilot-batches", type=int, default=5)
     ap.add_argument("--particles", type=int, default=1_000_000)
     ap.add_argument("--batches", type=int, default=10)
+    ap.add_argument("--plain-batches", type=int, default=0, help="batches of the plain arm (default: --batches)")
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--fp64", action="store_true")
     ap.add_argument("--density-scale", type=float, default=DENSITY_SCALE)
@@ -166,7 +192,8 @@ def main():
     out = run(Path(a.dir), length=a.length, mesh_dim=(int(a.length), 10, 10),
               pilot_particles=a.pilot_particles, pilot_batches=a.pilot_batches, particles=a.particles,
               batches=a.batches, steps=a.steps, fp32=not a.fp64, density_scale=a.density_scale,
-              methods=tuple(a.methods.split(",")), verbose=a.verbose, split_to_slots=not a.serial_splits)
+              methods=tuple(a.methods.split(",")), verbose=a.verbose, split_to_slots=not a.serial_splits,
+              plain_batches=a.plain_batches or None)
     print(json.dumps(out))
 
 

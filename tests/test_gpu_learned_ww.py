@@ -54,17 +54,72 @@ def test_split_to_slots_unbiased(built, tmp_path):
     assert (z > 3.0).sum() <= 1, z
 
 
+def _fine_tally(path, split, ww_on, batches):
+    from openmc_gb300 import lib
+    lib.init(directory=path)
+    try:
+        lib.settings.xs_fp32 = 1
+        lib.settings.split_to_slots = split
+        lib.simulation_init()
+        lib.set_weight_windows_on(ww_on)
+        for _ in range(batches):
+            lib.next_batch()
+        m, s = lib.tally_mean_std(lib.tally_ids()[0])
+        n = lib.tally_n_realizations(lib.tally_ids()[0])
+        lib.simulation_finalize()
+    finally:
+        lib.settings.split_to_slots = 0
+        lib.finalize()
+    assert n == batches
+    return m.ravel(), s.ravel()
+
+
+def test_windowed_runs_unbiased_bin_by_bin(built, tmp_path):
+    """100 batches of a 120 cm shield, flux on a 12x4x4 mesh x 3 energy
+    groups: plain transport, windows with split copies banked on the
+    parent's stack (the reference's order) and windows with split copies
+    started in free slots give the same mean in every well-scored bin.  With
+    99 degrees of freedom per sigma, z is close to normal: the signed z of
+    the bins both runs score to 20 % relative error is centred on 0 (within
+    4 standard errors), at most 1.5 % lie beyond 3 sigma and none beyond 5.5."""
+    from openmc_gb300 import configs
+    from openmc_gb300 import model as om
+    mesh = om.RegularMesh()
+    mesh.dimension = [12, 1, 1]
+    mesh.lower_left = [0.0, -25.0, -25.0]
+    mesh.upper_right = [120.0, 25.0, 25.0]
+    lower = 0.5 * 2.0 ** (-np.arange(12.0))
+    ww = om.WeightWindows(mesh, lower, upper_bound_ratio=5.0, energy_bounds=[0.0, 2.0e7 * 1.000001])
+    m, path = configs.shield(tmp_path, particles=20_000, batches=100, n_points=2000, length=120.0,
+                             mesh_dim=(12, 4, 4), weight_windows=ww, density_scale=0.1,
+                             energy_groups=[0.0, 1.0, 1.0e5, 2.0e7 * 1.000001])
+    m.export_to_model_xml(path)
+    runs = {"plain": _fine_tally(path, 0, False, 100),
+            "stack": _fine_tally(path, 0, True, 100),
+            "slots": _fine_tally(path, 1, True, 100)}
+    for a, b in (("plain", "stack"), ("plain", "slots"), ("stack", "slots")):
+        (ma, sa), (mb, sb) = runs[a], runs[b]
+        ok = (sa > 0) & (sb > 0) & (sa < 0.2 * ma) & (sb < 0.2 * mb)
+        z = (ma - mb)[ok] / np.hypot(sa, sb)[ok]
+        assert ok.sum() >= 100, (a, b, ok.sum())
+        assert abs(z.mean()) < 4.0 / np.sqrt(z.size), (a, b, z.mean(), z.size)
+        assert (np.abs(z) > 3).mean() <= 0.015, (a, b, (np.abs(z) > 3).mean())
+        assert np.abs(z).max() < 5.5, (a, b, np.abs(z).max())
+
+
 def test_learned_windows_raise_figure_of_merit(built, tmp_path):
     from openmc_gb300 import shield_study
     out = shield_study.run(tmp_path, length=120.0, mesh_dim=(120, 5, 5), n_points=2000,
                            pilot_particles=200_000, pilot_batches=3, particles=200_000, batches=8,
-                           steps=800)
+                           steps=800, plain_batches=64)
     print(out)
     lw = out["learned"]
     assert lw["loss_last"] < 0.2 * lw["loss_first"], lw
     assert lw["secondaries"] > 0
     assert out["plain"]["back_mean"] > 0
-    assert lw["fom_gain"] >= 3.0, out
+    # the north star's factor of 5 over plain transport; the plain arm's 64
+    # batches bound its figure of merit to ~18 % (one sigma)
+    assert lw["fom_gain"] >= 5.0, out
     # unbiased: back-face means agree within 3.5 combined sigma
     assert out["z_learned_plain"] < 3.5, out
     assert out["z_magic_plain"] < 3.5, out

@@ -23,10 +23,12 @@ CONT = ("E", "dist", "wgt")
 
 
 def run_gpu(path, n_trace=0, cap=256, fp32=False, in_flight=0, sort=True, batches=None, ww_on=None,
-            max_levels=0, fuse=3, event_based=True, stage_tables=0):
+            max_levels=0, fuse=3, event_based=True, stage_tables=0, contract=1, defer_tally=1):
     from openmc_gb300 import lib
     lib.init(directory=path)
     lib.settings.stage_tables = stage_tables
+    lib.settings.contract = contract
+    lib.settings.defer_tally = defer_tally
     try:
         lib.settings.event_based = event_based
         lib.settings.xs_fp32 = 1 if fp32 else 0
@@ -53,18 +55,21 @@ def run_gpu(path, n_trace=0, cap=256, fp32=False, in_flight=0, sort=True, batche
         lib.simulation_finalize()
         out["tallies"] = [(lib.tally_results(t).copy(), lib.tally_n_realizations(t))
                           for t in lib.tally_ids()]
+        out["globals"] = lib.global_tallies().copy()
         return out
     finally:
         lib.settings.stage_tables = 0
+        lib.settings.contract = 1
+        lib.settings.defer_tally = 1
         lib.finalize()
 
 
-def run_oracle(xml, n_trace=0, cap=256, batches=None):
+def run_oracle(xml, n_trace=0, cap=256, batches=None, threads=1):
     import oracle
     o = oracle.Oracle(xml)
     if n_trace:
         o.set_trace(n_trace, cap)
-    o.run(threads=1, batches=batches)
+    o.run(threads=threads, batches=batches)
     res = {"tallies": [o.tally(t) for t in range(o.n_tallies)], "globals": o.globals()}
     if n_trace:
         res["trace"] = o.traces()
@@ -170,6 +175,50 @@ def test_lattice_first_10k_histories(built, tmp_path):
     assert_tallies_close(g["tallies"], o["tallies"])
 
 
+def assert_globals_match(gpu_globals, orc_globals, rtol=1e-12):
+    """Global leakage tally (src/particle.cpp:475-512; per batch leakage /
+    source weight, accumulated as SUM and SUM_SQ like tally.cpp:1059-1100)
+    against the oracle's."""
+    g = np.asarray(gpu_globals).reshape(4, 3)[3]
+    assert np.isclose(g[1], orc_globals[0], rtol=rtol, atol=0), (g[1], orc_globals[0])
+    assert np.isclose(g[2], orc_globals[1], rtol=rtol, atol=0), (g[2], orc_globals[1])
+
+
+def test_lattice_full_size_first_10k_histories(built, tmp_path):
+    """The headline 17x17 lattice at its full size (12 nuclides of 11,303
+    grid points, flux on the 17x17x50 mesh x 100 log-energy bins), FP64
+    tables: the first 10^4 histories of the batch have the oracle's event
+    kinds, cells, materials, surfaces / nuclides, grid-index hashes,
+    coordinate depths and event counts; every one of the 1.445 M tally bins
+    agrees with the oracle's to 1e-5 relative, and so does the global
+    leakage tally."""
+    from openmc_gb300 import configs
+    import os
+    m, path = configs.lattice17(tmp_path, particles=10_000, batches=1)
+    xml = m.export_to_model_xml(path)
+    g = run_gpu(path, n_trace=10_000, cap=256)
+    o = run_oracle(xml, n_trace=10_000, cap=256, threads=min(os.cpu_count() or 1, 16))
+    bad = trace_mismatches(g["trace"], o["trace"], 256)
+    assert not bad, f"{len(bad)} of 10000 histories differ, first: {bad[:5]}"
+    (r, n), = g["tallies"]
+    assert r.shape[0] == 17 * 17 * 50 * 100 and n == 1
+    assert (r[..., 1] > 0).sum() > 10_000
+    assert_tallies_close(g["tallies"], o["tallies"])
+    assert_globals_match(g["globals"], o["globals"])
+    assert g["batch"]["done"] == 10_000 and g["batch"]["lost"] == 0
+
+
+def test_global_leakage_tally_matches_oracle(cube, shield_ww):
+    """Global leakage of the point cube (vacuum boundary) and of the shield
+    with weight windows (split and rouletted weights leak) against the
+    oracle over two batches."""
+    for xml, path in (cube, shield_ww):
+        g = run_gpu(path)
+        o = run_oracle(xml)
+        assert_globals_match(g["globals"], o["globals"])
+        assert np.asarray(g["globals"]).reshape(4, 3)[3, 1] > 0
+
+
 def test_cell_material_filters_and_collision_estimator(built, tmp_path):
     """Cell and material filters with track-length and collision estimators
     (tally_scoring.cpp:2416-2600, filter_cell.cpp, filter_material.cpp)
@@ -202,16 +251,18 @@ def test_lattice_history_based_parity(lattice):
 
 def test_lattice_builds_agree(lattice):
     """The 2-level build (per-level state in registers) and the 4-level
-    build, the unfused event kernels, and the kernels reading their
-    geometry and material tables from shared-memory copies (event- and
-    history-based) give the same histories."""
+    build, the unfused event kernels, the kernels reading their geometry and
+    material tables from shared-memory copies (event- and history-based),
+    and track-length tallies scored inside the advance kernel instead of
+    from deferred track records give the same histories and tallies."""
     xml, path = lattice
     a = run_gpu(path, n_trace=600, cap=1024)
     b = run_gpu(path, n_trace=600, cap=1024, max_levels=4)
     c = run_gpu(path, n_trace=600, cap=1024, fuse=0)
     d = run_gpu(path, n_trace=600, cap=1024, stage_tables=1)
     e = run_gpu(path, n_trace=600, cap=1024, stage_tables=1, event_based=False)
-    for other in (b, c, d, e):
+    f = run_gpu(path, n_trace=600, cap=1024, defer_tally=0)
+    for other in (b, c, d, e, f):
         assert not trace_mismatches(a["trace"], other["trace"], 1024)
         for (ra, na), (rb, nb) in zip(a["tallies"], other["tallies"]):
             assert na == nb
@@ -247,13 +298,17 @@ def test_shield_weight_window_parity(shield_ww):
     assert_tallies_close(g["tallies"], o["tallies"])
 
 
-def test_fp32_tables_within_3_sigma(built, tmp_path):
+@pytest.mark.parametrize("contract", [1, 0])
+def test_fp32_tables_within_3_sigma(built, tmp_path, contract):
+    """FP32 tables against FP64 tables, for the FP32-mode build with fused
+    FP64 multiply-adds (the default) and for the one that rounds them
+    separately."""
     from openmc_gb300 import configs
     m, path = configs.lattice17(tmp_path, particles=40000, batches=6, n_points=4000,
                                 mesh_dim=(17, 17, 4), n_ebins=10)
     m.export_to_model_xml(path)
     a = run_gpu(path, fp32=False)
-    b = run_gpu(path, fp32=True)
+    b = run_gpu(path, fp32=True, contract=contract)
     (ra, n), (rb, _) = a["tallies"][0], b["tallies"][0]
     ma, mb = ra[..., 1] / n, rb[..., 1] / n
     sa = np.sqrt(np.maximum(ra[..., 2] / n - ma ** 2, 0) / (n - 1))

@@ -200,7 +200,9 @@ void setup_generators(HModel& m)
   }
 }
 
-// WeightWindows::update_weights (MAGIC), src/weight_windows.cpp:502-755
+// WeightWindows::update_weights (MAGIC), src/weight_windows.cpp:502-755:
+// on the device while a simulation holds the tallies there (the first
+// window set, the one the transport uses), else on the host arrays.
 int update_magic(HModel& m, int ww_idx, int tally_idx, const std::string& value, double threshold, double ratio)
 {
   if (ww_idx < 0 || ww_idx >= static_cast<int>(m.weight_windows.size()))
@@ -231,6 +233,29 @@ int update_magic(HModel& m, int ww_idx, int tally_idx, const std::string& value,
   const int64_t mesh_bins = m.meshes[w.mesh].n_bins();
   const int ns = static_cast<int>(t.scores.size());
   const int n = t.n_realizations;
+  const HMesh& mesh = m.meshes[w.mesh];
+  double vol = 1.0;
+  for (int i = 0; i < mesh.ndim; ++i) vol *= mesh.width[i];
+  if (S().gpu && ww_idx == 0) {
+    // on the device, from the device's tally sums, into the transport's own
+    // window arrays (the host arrays receive a copy)
+    MagicArgs a;
+    a.tally = tally_idx;
+    a.score = score_index;
+    a.n_scores = ns;
+    a.stride_mesh = t.strides[mesh_pos];
+    a.stride_energy = energy_pos >= 0 ? t.strides[energy_pos] : -1;
+    a.e_bins = e_bins;
+    a.mesh_bins = mesh_bins;
+    a.n = n;
+    a.volume = vol;
+    a.rel_err = value == "rel_err" ? 1 : 0;
+    a.threshold = threshold;
+    a.ratio = ratio;
+    gpu_update_magic(S().gpu, a, w.lower.data(), w.upper.data());
+    return 0;
+  }
+  if (S().gpu) gpu_fetch_tallies(S().gpu, m);
   auto idx = [&](int e, int64_t mb) {
     int64_t k = mb * t.strides[mesh_pos];
     if (energy_pos >= 0) k += static_cast<int64_t>(e) * t.strides[energy_pos];
@@ -238,9 +263,6 @@ int update_magic(HModel& m, int ww_idx, int tally_idx, const std::string& value,
   };
   std::vector<double>& nb = w.lower;
   std::vector<double>& rel = w.upper;
-  const HMesh& mesh = m.meshes[w.mesh];
-  double vol = 1.0;
-  for (int i = 0; i < mesh.ndim; ++i) vol *= mesh.width[i];
   for (int e = 0; e < e_bins; e++) {
     for (int64_t mb = 0; mb < mesh_bins; mb++) {
       int64_t k = e * mesh_bins + mb;
@@ -444,7 +466,6 @@ int openmc_next_batch(int* status)
       bool need = false;
       for (const auto& g : m.ww_generators) need = need || g.tally >= 0;
       if (need) {
-        gpu_fetch_tallies(s.gpu, m);
         for (const auto& g : m.ww_generators) {
           const HTally& t = m.tallies[g.tally];
           if (g.max_realizations < t.n_realizations || t.n_realizations % g.update_interval != 0) continue;
@@ -762,7 +783,6 @@ int openmc_weight_windows_update_magic(int32_t ww_idx, int32_t tally_idx, const 
 {
   State& s = S();
   try {
-    if (s.gpu) gpu_fetch_tallies(s.gpu, s.model);
     return update_magic(s.model, ww_idx, tally_idx, value ? value : "mean", threshold, ratio);
   } catch (const std::exception& e) {
     return fail(OPENMC_E_UNASSIGNED, e.what());

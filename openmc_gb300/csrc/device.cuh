@@ -8,6 +8,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "fp64_int.cuh"
 #include "transport.h"
 
 // Each build of the transport kernels for a maximum coordinate depth lives
@@ -37,6 +38,7 @@ constexpr uint64_t PRN_ADD = 1442695040888963407ULL;
 
 struct DSurface {
   double c[4];
+  double rr;  // radius squared (cylinders, spheres), the product the distance and sense expressions form
   int type, bc;
 };
 
@@ -52,6 +54,7 @@ struct alignas(16) XsRow64 {
 
 struct DLattice {
   double ll[3], pitch[3];
+  double half[3];  // 0.5 x pitch (exact)
   int n[3];
   int is3d, outer, univ_off;
 };
@@ -362,9 +365,11 @@ __device__ __forceinline__ unsigned long long prn_word(unsigned long long& s)
   return (word >> 43u) ^ word;
 }
 
+// word x 2^-64 rounded to the nearest double (ldexp of the word converted to
+// double, as the reference), built from the word's bits on the integer pipe
 __device__ __forceinline__ double prn(unsigned long long& s)
 {
-  return __ull2double_rn(prn_word(s)) * 5.421010862427522170037264e-20;  // 2^-64
+  return fpi::u64_scaled_2m64(prn_word(s));
 }
 
 // The same generator step as prn, as an FP32 number in (0, 1): the top 23
@@ -407,10 +412,12 @@ __device__ inline void rotate_angle(double& ux, double& uy, double& uz, double m
   double phi_ = 2.0 * PI * prn(s);
   double sinphi, cosphi;
   sincos(phi_, &sinphi, &cosphi);
-  double a = sqrt(fmax(0., 1. - mu * mu));
-  double b = sqrt(fmax(0., 1. - uz * uz));
+  // fmax(0, v) as the C library returns it (+0 for v <= 0), on the integer pipe
+  const double va = 1. - mu * mu, vb = 1. - uz * uz;
+  double a = sqrt(fpi::pos(va) ? va : 0.0);
+  double b = sqrt(fpi::pos(vb) ? vb : 0.0);
   double x = ux, y = uy, z = uz;
-  if (b > 1e-10) {
+  if (fpi::lt(1e-10, b)) {
     if (recip) {
       const double ib = 1.0 / b;
       ux = mu * x + a * (x * z * cosphi - y * sinphi) * ib;
@@ -510,48 +517,49 @@ __device__ inline double surf_evaluate(const DSurface& s, double x, double y, do
   case 0: return x - s.c[0];
   case 1: return y - s.c[0];
   case 2: return z - s.c[0];
-  case 3: { double a = y - s.c[0], b = z - s.c[1]; return a * a + b * b - s.c[2] * s.c[2]; }
-  case 4: { double a = x - s.c[0], b = z - s.c[1]; return a * a + b * b - s.c[2] * s.c[2]; }
-  case 5: { double a = x - s.c[0], b = y - s.c[1]; return a * a + b * b - s.c[2] * s.c[2]; }
+  case 3: { double a = fpi::sub(y, s.c[0]), b = fpi::sub(z, s.c[1]); return a * a + b * b - s.rr; }
+  case 4: { double a = fpi::sub(x, s.c[0]), b = fpi::sub(z, s.c[1]); return a * a + b * b - s.rr; }
+  case 5: { double a = fpi::sub(x, s.c[0]), b = fpi::sub(y, s.c[1]); return a * a + b * b - s.rr; }
   default: {
-    double a = x - s.c[0], b = y - s.c[1], c = z - s.c[2];
-    return a * a + b * b + c * c - s.c[3] * s.c[3];
+    double a = fpi::sub(x, s.c[0]), b = fpi::sub(y, s.c[1]), c = fpi::sub(z, s.c[2]);
+    return a * a + b * b + c * c - s.rr;
   }
   }
 }
 
+// Comparisons run on the integer pipe (fp64_int.cuh) with the IEEE results.
 __device__ inline double plane_distance(double r_i, double u_i, bool coincident, double offset)
 {
   const double f = offset - r_i;
-  if (coincident || fabs(f) < FP_COINCIDENT || u_i == 0.0) return INFTY;
-  // f / u_i < 0 exactly when the signs differ (|f| >= 1e-12 and |u_i| <= 1,
-  // so the quotient cannot underflow to zero): skip the division then
-  if ((f < 0.0) != (u_i < 0.0)) return INFTY;
-  const double d = f / u_i;
-  if (d < 0.0) return INFTY;
-  return d;
+  if (coincident || fpi::abs_lt(f, FP_COINCIDENT) || fpi::zero(u_i)) return INFTY;
+  // f / u_i < 0 exactly when the signs differ (f and u_i are non-zero here,
+  // |f| >= 1e-12 and |u_i| <= 1, so the quotient is never a zero): skip the
+  // division then; otherwise the quotient is positive and the reference's
+  // d < 0 test never holds
+  if ((fpi::bits(f) ^ fpi::bits(u_i)) < 0) return INFTY;
+  return f / u_i;
 }
 
 __device__ inline double cylinder_distance(double u1, double r2_, double u2, double r3_, double u3,
   bool coincident, double offset1, double offset2, double radius)
 {
   const double a = 1.0 - u1 * u1;
-  if (a == 0.0) return INFTY;
-  const double r2 = r2_ - offset1;
-  const double r3 = r3_ - offset2;
+  if (fpi::zero(a)) return INFTY;
+  const double r2 = fpi::sub(r2_, offset1);
+  const double r3 = fpi::sub(r3_, offset2);
   const double k = r2 * u2 + r3 * u3;
-  const double c = r2 * r2 + r3 * r3 - radius * radius;
+  const double c = r2 * r2 + r3 * r3 - radius;  // radius: the squared radius
   const double quad = k * k - a * c;
-  if (quad < 0.0) {
+  if (fpi::neg(quad)) {
     return INFTY;
-  } else if (coincident || fabs(c) < FP_COINCIDENT) {
-    if (k >= 0.0) return INFTY;
+  } else if (coincident || fpi::abs_lt(c, FP_COINCIDENT)) {
+    if (fpi::nonneg(k)) return INFTY;
     return (-k + sqrt(quad)) / a;
-  } else if (c < 0.0) {
+  } else if (fpi::neg(c)) {
     return (-k + sqrt(quad)) / a;
   } else {
     const double d = (-k - sqrt(quad)) / a;
-    if (d < 0.0) return INFTY;
+    if (fpi::neg(d)) return INFTY;
     return d;
   }
 }
@@ -559,22 +567,22 @@ __device__ inline double cylinder_distance(double u1, double r2_, double u2, dou
 __device__ inline double sphere_distance(const DSurface& s, double x_, double y_, double z_, double ux,
   double uy, double uz, bool coincident)
 {
-  const double x = x_ - s.c[0];
-  const double y = y_ - s.c[1];
-  const double z = z_ - s.c[2];
+  const double x = fpi::sub(x_, s.c[0]);
+  const double y = fpi::sub(y_, s.c[1]);
+  const double z = fpi::sub(z_, s.c[2]);
   const double k = x * ux + y * uy + z * uz;
-  const double c = x * x + y * y + z * z - s.c[3] * s.c[3];
+  const double c = x * x + y * y + z * z - s.rr;
   const double quad = k * k - c;
-  if (quad < 0.0) {
+  if (fpi::neg(quad)) {
     return INFTY;
-  } else if (coincident || fabs(c) < FP_COINCIDENT) {
-    if (k >= 0.0) return INFTY;
+  } else if (coincident || fpi::abs_lt(c, FP_COINCIDENT)) {
+    if (fpi::nonneg(k)) return INFTY;
     return -k + sqrt(quad);
-  } else if (c < 0.0) {
+  } else if (fpi::neg(c)) {
     return -k + sqrt(quad);
   } else {
     const double d = -k - sqrt(quad);
-    if (d < 0.0) return INFTY;
+    if (fpi::neg(d)) return INFTY;
     return d;
   }
 }
@@ -586,9 +594,9 @@ __device__ inline double surf_distance(const DSurface& s, double x, double y, do
   case 0: return plane_distance(x, ux, coincident, s.c[0]);
   case 1: return plane_distance(y, uy, coincident, s.c[0]);
   case 2: return plane_distance(z, uz, coincident, s.c[0]);
-  case 3: return cylinder_distance(ux, y, uy, z, uz, coincident, s.c[0], s.c[1], s.c[2]);
-  case 4: return cylinder_distance(uy, x, ux, z, uz, coincident, s.c[0], s.c[1], s.c[2]);
-  case 5: return cylinder_distance(uz, x, ux, y, uy, coincident, s.c[0], s.c[1], s.c[2]);
+  case 3: return cylinder_distance(ux, y, uy, z, uz, coincident, s.c[0], s.c[1], s.rr);
+  case 4: return cylinder_distance(uy, x, ux, z, uz, coincident, s.c[0], s.c[1], s.rr);
+  case 5: return cylinder_distance(uz, x, ux, y, uy, coincident, s.c[0], s.c[1], s.rr);
   default: return sphere_distance(s, x, y, z, ux, uy, uz, coincident);
   }
 }
@@ -609,12 +617,12 @@ __device__ inline void surf_normal(const DSurface& s, double x, double y, double
 __device__ inline bool surf_sense(const DSurface& s, double x, double y, double z, double ux, double uy, double uz)
 {
   const double f = surf_evaluate(s, x, y, z);
-  if (fabs(f) < FP_COINCIDENT) {
+  if (fpi::abs_lt(f, FP_COINCIDENT)) {
     double nx, ny, nz;
     surf_normal(s, x, y, z, nx, ny, nz);
-    return ux * nx + uy * ny + uz * nz > 0.0;
+    return fpi::pos(ux * nx + uy * ny + uz * nz);
   }
-  return f > 0.0;
+  return fpi::pos(f);
 }
 
 // src/cell.cpp:951-969 simple regions; postfix evaluation for complex ones
@@ -675,12 +683,14 @@ __device__ inline void region_distance(const DCell& c, double x, double y, doubl
     const DSurface& sf = s_tabs.surf[abs(token) - 1];
     if (sf.type <= 2) {
       double r_i = sf.type == 0 ? x : (sf.type == 1 ? y : z);
-      if (fabs(sf.c[0] - r_i) > bound) continue;
+      if (fpi::abs_gt(sf.c[0] - r_i, bound)) continue;
     }
     bool coincident = abs(token) == abs(on_surface);
     double d = surf_distance(sf, x, y, z, ux, uy, uz, coincident);
-    if (d < min_dist) {
-      if (min_dist - d >= FP_PRECISION * min_dist) {
+    if (fpi::lt(d, min_dist)) {
+      // the first candidate against INFTY always passes: INFTY - d rounds
+      // to INFTY, which exceeds FP_PRECISION x INFTY
+      if (fpi::bits(min_dist) == fpi::bits(INFTY) || fpi::le(FP_PRECISION * min_dist, min_dist - d)) {
         min_dist = d;
         i_surf = -token;
       }
@@ -695,28 +705,32 @@ __device__ inline void region_distance(const DCell& c, double x, double y, doubl
 __device__ inline double lattice_distance(const DLattice& lat, double x, double y, double z, double ux,
   double uy, double uz, int& trans, const double* inv_u = nullptr)
 {
-  double x0 = copysign(0.5 * lat.pitch[0], ux);
-  double y0 = copysign(0.5 * lat.pitch[1], uy);
+  // x0 - x is exactly -(x - x0), so |x - x0| is read from the one difference
+  const double x0 = copysign(lat.half[0], ux);
+  const double y0 = copysign(lat.half[1], uy);
   double d = INFTY;
   trans = 13;  // encoded (tx+1) + 3(ty+1) + 9(tz+1); 13 == no translation
-  if ((fabs(x - x0) > FP_PRECISION) && ux != 0) {
-    d = inv_u ? (x0 - x) * inv_u[0] : (x0 - x) / ux;
-    trans = (ux > 0) ? 14 : 12;
+  const double fx = x0 - x;
+  if (fpi::abs_gt(fx, FP_PRECISION) && !fpi::zero(ux)) {
+    d = inv_u ? fx * inv_u[0] : fx / ux;
+    trans = fpi::pos(ux) ? 14 : 12;
   }
-  if ((fabs(y - y0) > FP_PRECISION) && uy != 0) {
-    double this_d = inv_u ? (y0 - y) * inv_u[1] : (y0 - y) / uy;
-    if (this_d < d) {
+  const double fy = y0 - y;
+  if (fpi::abs_gt(fy, FP_PRECISION) && !fpi::zero(uy)) {
+    double this_d = inv_u ? fy * inv_u[1] : fy / uy;
+    if (fpi::lt(this_d, d)) {
       d = this_d;
-      trans = (uy > 0) ? 16 : 10;
+      trans = fpi::pos(uy) ? 16 : 10;
     }
   }
   if (lat.is3d) {
-    double z0 = copysign(0.5 * lat.pitch[2], uz);
-    if ((fabs(z - z0) > FP_PRECISION) && uz != 0) {
-      double this_d = inv_u ? (z0 - z) * inv_u[2] : (z0 - z) / uz;
-      if (this_d < d) {
+    const double z0 = copysign(lat.half[2], uz);
+    const double fz = z0 - z;
+    if (fpi::abs_gt(fz, FP_PRECISION) && !fpi::zero(uz)) {
+      double this_d = inv_u ? fz * inv_u[2] : fz / uz;
+      if (fpi::lt(this_d, d)) {
         d = this_d;
-        trans = (uz > 0) ? 22 : 4;
+        trans = fpi::pos(uz) ? 22 : 4;
       }
     }
   }
@@ -745,11 +759,12 @@ __device__ inline void lattice_get_indices(const DLattice& lat, double x, double
 }
 
 // src/lattice.cpp:352-361
+// (i + 0.5 formed on the integer pipe, exactly)
 __device__ inline void lattice_local_position(const DLattice& lat, double& x, double& y, double& z, const int* i)
 {
-  x -= (lat.ll[0] + (i[0] + 0.5) * lat.pitch[0]);
-  y -= (lat.ll[1] + (i[1] + 0.5) * lat.pitch[1]);
-  if (lat.is3d) z -= (lat.ll[2] + (i[2] + 0.5) * lat.pitch[2]);
+  x -= (lat.ll[0] + fpi::half_odd(i[0]) * lat.pitch[0]);
+  y -= (lat.ll[1] + fpi::half_odd(i[1]) * lat.pitch[1]);
+  if (lat.is3d) z -= (lat.ll[2] + fpi::half_odd(i[2]) * lat.pitch[2]);
 }
 
 __device__ __forceinline__ bool lattice_valid(const DLattice& lat, const int* i)
@@ -878,9 +893,9 @@ __device__ inline bool find_cell_inner(Geo& g, bool& lost_outer)
     }
     if (g.n_coord >= dm.n_coord_levels || lvl + 1 >= MAXL) return false;
     const int nl = lvl + 1 < MAXL ? lvl + 1 : lvl;  // == lvl + 1 on every path that reaches it
-    g.r[nl][0] = g.r[lvl][0] - c.tr[0];
-    g.r[nl][1] = g.r[lvl][1] - c.tr[1];
-    g.r[nl][2] = g.r[lvl][2] - c.tr[2];
+    g.r[nl][0] = fpi::sub(g.r[lvl][0], c.tr[0]);
+    g.r[nl][1] = fpi::sub(g.r[lvl][1], c.tr[1]);
+    g.r[nl][2] = fpi::sub(g.r[lvl][2], c.tr[2]);
     if (c.fill_type == 1) {
       g.univ[nl] = c.fill;
       g.lat[nl] = C_NONE;
@@ -913,6 +928,23 @@ __device__ inline bool exhaustive_find_cell(Geo& g, bool& lost_outer)
   return find_cell_inner(g, lost_outer);
 }
 
+// (t / d >= FP_REL_PRECISION) with the quotient rounded as the reference
+// rounds it.  For a finite d >= 2^-959, t at or above d x 1e-5 (1 + 2^-40),
+// or at or below d x 1e-5 (1 - 2^-40), each product rounded once, settles
+// the rounded quotient on its side of the threshold (the margin is far
+// above the 2^-53 relative error of the product and of the quotient), so
+// the FP64 division runs only for t within that margin, or for d not
+// positive and finite.
+__device__ __forceinline__ bool rel_gap_at_least(double t, double d)
+{
+  // d in [2^-959, inf): the products stay normal doubles
+  if (fpi::bits(d) >= 0x0400000000000000LL && fpi::bits(d) < fpi::EXP_INF) {
+    if (fpi::le(d * 1.0000000000009096e-05, t)) return true;   // 1e-5 (1 + 2^-40)
+    if (fpi::le(t, d * 9.999999999990905e-06)) return false;   // 1e-5 (1 - 2^-40)
+  }
+  return t / d >= FP_REL_PRECISION;
+}
+
 // src/geometry.cpp:361-453.  The levels below the root are evaluated first;
 // the candidate distance D of level 1 bounds the root level: the reference
 // replaces any root distance above D (1 + 1e-4) by D at level 1 (its
@@ -939,12 +971,12 @@ __device__ inline void distance_to_boundary(const Geo& g, double& dist, int& sur
     tt[i] = 13;
     if (g.lat[i] != C_NONE) {
       dl[i] = lattice_distance(dm.lat[g.lat[i]], r[0], r[1], r[2], g.u[0], g.u[1], g.u[2], tt[i], inv_u);
-      if (dl[i] < 0) neg_lat = true;
+      if (fpi::neg(dl[i])) neg_lat = true;
     }
     if (i == 1) {
       // candidate of the level directly below the root: any root distance
       // above cand (1 + 1e-4) loses to it in the level loop below
-      double cand = (ds[i] < dl[i] - FP_COINCIDENT) ? ds[i] : dl[i];
+      double cand = fpi::lt(ds[i], dl[i] - FP_COINCIDENT) ? ds[i] : dl[i];
       bound = cand * (1.0 + 1e-4);
     }
   }
@@ -960,10 +992,10 @@ __device__ inline void distance_to_boundary(const Geo& g, double& dist, int& sur
     double d_surf = ds[i];
     double d_lat = dl[i];
     double& d = dist;
-    if (d_surf < d_lat - FP_COINCIDENT) {
-      if (d == INF || (d - d_surf) / d >= FP_REL_PRECISION) {
+    if (fpi::lt(d_surf, d_lat - FP_COINCIDENT)) {
+      if (fpi::bits(d) == fpi::bits(INF) || rel_gap_at_least(d - d_surf, d)) {
         d = d_surf;
-        if (c.simple || d == INFTY) {
+        if (c.simple || fpi::bits(d) == fpi::bits(INFTY)) {
           surface = ss[i];
         } else {
           double hx = r[0] + d_surf * g.u[0];
@@ -971,13 +1003,13 @@ __device__ inline void distance_to_boundary(const Geo& g, double& dist, int& sur
           double hz = r[2] + d_surf * g.u[2];
           double nx, ny, nz;
           surf_normal(s_tabs.surf[abs(ss[i]) - 1], hx, hy, hz, nx, ny, nz);
-          surface = (g.u[0] * nx + g.u[1] * ny + g.u[2] * nz > 0) ? abs(ss[i]) : -abs(ss[i]);
+          surface = fpi::pos(g.u[0] * nx + g.u[1] * ny + g.u[2] * nz) ? abs(ss[i]) : -abs(ss[i]);
         }
         trans = 13;
         level = i + 1;
       }
     } else {
-      if (d == INF || (d - d_lat) / d >= FP_REL_PRECISION) {
+      if (fpi::bits(d) == fpi::bits(INF) || rel_gap_at_least(d - d_lat, d)) {
         d = d_lat;
         surface = SURFACE_NONE;
         trans = tt[i];
@@ -1064,7 +1096,7 @@ __device__ __forceinline__ void micro_xs32(int nuc, int i_log, double E, float& 
   const float4* xs = dm.xs32 + dm.nuc_off[nuc];
   float4 a = __ldg(xs + i_grid);
   float4 b = __ldg(xs + i_grid + 1);
-  f32 = static_cast<float>(E - e0) * a.w;
+  f32 = fpi::to_float(E - e0) * a.w;
   t = a.x + f32 * (b.x - a.x);
   a_out = a.y + f32 * (b.y - a.y);
 }
@@ -1081,7 +1113,7 @@ __device__ __forceinline__ void micro_xs32(int nuc, int i_log, double E, float& 
 // The returned bin is always the FP64 expression's.
 __device__ __forceinline__ int log_union_index(double E)
 {
-  const float q = (logf(static_cast<float>(E)) - dm.log_emin32) * dm.inv_spacing32;
+  const float q = (logf(fpi::to_float(E)) - dm.log_emin32) * dm.inv_spacing32;
   const float fl = floorf(q);
   const float fr = q - fl;
   int i;
@@ -1121,8 +1153,8 @@ __device__ inline uint32_t material_xs(int mat, double E, double& tot, double& a
       t += dens * mt;
       ab += dens * ma;
     }
-    tot = t;
-    abs_ = ab;
+    tot = fpi::to_double(t);
+    abs_ = fpi::to_double(ab);
   }
   return h;
 }

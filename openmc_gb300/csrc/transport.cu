@@ -113,7 +113,7 @@ __device__ void mark_lost(long long s)
 __device__ __forceinline__ bool mesh_index_fp32(const DMesh& m, double r, int i, int& idx)
 {
   const double t = r - m.ll[i];
-  const float q32 = __fmul_rn(static_cast<float>(t), m.inv_width32[i]);
+  const float q32 = __fmul_rn(fpi::to_float(t), m.inv_width32[i]);
   const float fr = q32 - rintf(q32);
   if (fabsf(q32) < 1048576.0f && fabsf(fr) > 1e-4f + 2e-6f * fabsf(q32)) {
     idx = static_cast<int>(ceilf(q32));
@@ -167,15 +167,16 @@ __device__ __forceinline__ MeshDist mesh_dist(const DMesh& m, const int* ijk, in
   d.next_index = ijk[i];
   d.max_surface = true;
   d.distance = INFTY;
-  if (fabs(u[i]) < FP_PRECISION) return d;
-  d.max_surface = (u[i] > 0);
+  if (fpi::abs_lt(u[i], FP_PRECISION)) return d;
+  d.max_surface = fpi::pos(u[i]);
+  // grid plane ll + j width with j converted to double on the integer pipe
   if (d.max_surface && (ijk[i] <= m.shape[i])) {
     d.next_index++;
-    const double f = (m.ll[i] + ijk[i] * m.width[i]) - r0[i];
+    const double f = (m.ll[i] + fpi::to_double(ijk[i]) * m.width[i]) - r0[i];
     d.distance = inv_u ? f * inv_u[i] : f / u[i];
   } else if (!d.max_surface && (ijk[i] >= 1)) {
     d.next_index--;
-    const double f = (m.ll[i] + (ijk[i] - 1) * m.width[i]) - r0[i];
+    const double f = (m.ll[i] + fpi::to_double(ijk[i] - 1) * m.width[i]) - r0[i];
     d.distance = inv_u ? f * inv_u[i] : f / u[i];
   }
   return d;
@@ -195,13 +196,13 @@ __device__ void mesh_bins_crossed(const DMesh& m, const double* r0, const double
     double dx = r1[0] - r0[0], dy = r1[1] - r0[1], dz = r1[2] - r0[2];
     total_distance = sqrt(dx * dx + dy * dy + dz * dz);
   }
-  if (total_distance == 0.0) return;
+  if (fpi::zero(total_distance)) return;
   const int n = m.ndim;
   bool in_mesh;
   double traveled = 0.0;
   int ijk[3] = {0, 0, 0};
   mesh_get_indices(m, r0[0] + TINY_BIT * u[0], r0[1] + TINY_BIT * u[1], r0[2] + TINY_BIT * u[2], ijk, in_mesh);
-  if (total_distance < 2 * TINY_BIT) {
+  if (fpi::lt(total_distance, 2 * TINY_BIT)) {
     if (in_mesh) f(mesh_bin(m, ijk), 1.0);
     return;
   }
@@ -239,12 +240,12 @@ __device__ void mesh_bins_crossed(const DMesh& m, const double* r0, const double
     if (in_mesh) {
       int k = 0;
       double dk = dist[0].distance;
-      if (dist[1].distance < dk) { k = 1; dk = dist[1].distance; }
-      if (dist[2].distance < dk) { k = 2; dk = dist[2].distance; }
-      const double seg = fmin(dk, total_distance) - traveled;
+      if (fpi::lt(dist[1].distance, dk)) { k = 1; dk = dist[1].distance; }
+      if (fpi::lt(dist[2].distance, dk)) { k = 2; dk = dist[2].distance; }
+      const double seg = fpi::min(dk, total_distance) - traveled;
       f(mesh_bin(m, ijk), inv_u ? seg * inv_total : seg / total_distance);
       traveled = dk;
-      if (traveled >= total_distance) return;
+      if (fpi::le(total_distance, traveled)) return;
 #pragma unroll
       for (int kk = 0; kk < 3; ++kk) {
         if (kk != k) continue;
@@ -777,7 +778,7 @@ __device__ bool revive_or_free(long long s, double wgt)
     db.wgt[s] = 0.0;
   }
   db.n_event[s] = ne;
-  if (wgt != 0.0) return true;
+  if (!fpi::zero(wgt)) return true;
   int top = db.sec_top[s];
   if (top < 0) {
     unsigned long long key = (static_cast<unsigned long long>(db.n_total[s]) << 34) |
@@ -940,11 +941,12 @@ __device__ void ev_xs(long long s, EvStats& st)
 __device__ __forceinline__ double collision_distance(double xi, double mt)
 {
   if (!dm.xs_fp32) return -log(xi) / mt;
+  // xi in [0, 1): compared as bit patterns; conversions on the integer pipe
   float lg;
-  if (xi > 0.5) lg = log1pf(-static_cast<float>(1.0 - xi));
-  else if (xi >= 0x1p-20) lg = logf(static_cast<float>(xi));
+  if (fpi::bits(xi) > fpi::bits(0.5)) lg = log1pf(-fpi::to_float(1.0 - xi));
+  else if (fpi::bits(xi) >= fpi::bits(0x1p-20)) lg = logf(fpi::to_float(xi));
   else lg = static_cast<float>(log(xi));
-  return static_cast<double>(-lg / static_cast<float>(mt));
+  return fpi::to_double(-lg / fpi::to_float(mt));
 }
 
 __device__ int ev_surface_g(long long s, EvStats& st, Geo& g, double wgt, int bsurf, int trans, int blevel);
@@ -958,7 +960,7 @@ template<bool with_surf, bool defer = false>
 __device__ int ev_advance(long long s, EvStats& st, int qi = 0)
 {
   double wgt = db.wgt[s];
-  if (wgt == 0.0) {
+  if (fpi::zero(wgt)) {
     if (defer && dq.trk.w) dq.trk.w[qi] = 0.0;  // no record
     return revive_or_free(s, wgt) ? NEXT_XS : NEXT_DEAD;
   }
@@ -980,10 +982,10 @@ __device__ int ev_advance(long long s, EvStats& st, int qi = 0)
   if (neg_lat) mark_lost(s);
   unsigned long long seed = db.seed[s];
   double mt = db.macro_t[s];
-  double dcoll = (mt == 0.0) ? __longlong_as_double(0x7ff0000000000000LL) : collision_distance(prn(seed), mt);
+  double dcoll = fpi::zero(mt) ? __longlong_as_double(0x7ff0000000000000LL) : collision_distance(prn(seed), mt);
   double distance = bd;
-  if (dcoll < distance) distance = dcoll;
-  if (INFTY < distance) distance = INFTY;
+  if (fpi::lt(dcoll, distance)) distance = dcoll;
+  if (fpi::lt(INFTY, distance)) distance = INFTY;
   double r0[3] = {g.r[0][0], g.r[0][1], g.r[0][2]};
 #pragma unroll
   for (int l = 0; l < MAXL; ++l) {
@@ -1026,7 +1028,7 @@ __device__ int ev_advance(long long s, EvStats& st, int qi = 0)
       recip ? inv_u : nullptr);
   }
   wgt = db.wgt[s];
-  if (distance == INFTY) {
+  if (fpi::bits(distance) == fpi::bits(INFTY)) {
     wgt = 0.0;
     db.wgt[s] = 0.0;
   }
@@ -1036,7 +1038,7 @@ __device__ int ev_advance(long long s, EvStats& st, int qi = 0)
     TraceRec* rec = trace_slot(pid);
     if (rec) rec->dist = distance;
   }
-  const bool cross = wgt != 0.0 && dcoll > bd;
+  const bool cross = !fpi::zero(wgt) && fpi::lt(bd, dcoll);
   if (with_surf && cross) return ev_surface_g(s, st, g, wgt, bs, bt, bl);
   const long long cap = db.cap;
 #pragma unroll
@@ -1053,7 +1055,7 @@ __device__ int ev_advance(long long s, EvStats& st, int qi = 0)
     db.btrans[s] = bt;
     return NEXT_SURF;
   }
-  if (wgt != 0.0) return NEXT_COLL;
+  if (!fpi::zero(wgt)) return NEXT_COLL;
   return revive_or_free(s, wgt) ? NEXT_XS : NEXT_DEAD;
 }
 
@@ -1071,9 +1073,9 @@ __device__ void cross_lattice(Geo& g, long long s, int trans)
     g.li[lvl][2] += trans / 9 - 1;
     const int up = lvl - 1;
     const DCell& cell = s_tabs.cell[g.cell[up]];
-    g.r[lvl][0] = g.r[up][0] - cell.tr[0];
-    g.r[lvl][1] = g.r[up][1] - cell.tr[1];
-    g.r[lvl][2] = g.r[up][2] - cell.tr[2];
+    g.r[lvl][0] = fpi::sub(g.r[up][0], cell.tr[0]);
+    g.r[lvl][1] = fpi::sub(g.r[up][1], cell.tr[1]);
+    g.r[lvl][2] = fpi::sub(g.r[up][2], cell.tr[2]);
     lattice_local_position(lat, g.r[lvl][0], g.r[lvl][1], g.r[lvl][2], g.li[lvl]);
     valid = lattice_valid(lat, g.li[lvl]);
     if (valid) {
@@ -1270,15 +1272,14 @@ __device__ void elastic_scatter(int nuc, double& E, double* u, unsigned long lon
   double vn[3] = {vel * u[0], vel * u[1], vel * u[2]};
   double vt[3] = {0.0, 0.0, 0.0};
   const bool recip = dm.xs_fp32 != 0;
-  if (!(E >= 400.0 * kT && awr > 1.0)) {
+  if (!(fpi::le(400.0 * kT, E) && fpi::lt(1.0, awr))) {
     if (recip) {
-      const float uf[3] = {static_cast<float>(u[0]), static_cast<float>(u[1]), static_cast<float>(u[2])};
+      const float uf[3] = {fpi::to_float(u[0]), fpi::to_float(u[1]), fpi::to_float(u[2])};
       float vtf[3];
-      sample_cxs_target_velocity_f(static_cast<float>(awr), static_cast<float>(E), uf, static_cast<float>(kT), seed,
-                                   vtf);
-      vt[0] = vtf[0];
-      vt[1] = vtf[1];
-      vt[2] = vtf[2];
+      sample_cxs_target_velocity_f(fpi::to_float(awr), fpi::to_float(E), uf, fpi::to_float(kT), seed, vtf);
+      vt[0] = fpi::to_double(vtf[0]);
+      vt[1] = fpi::to_double(vtf[1]);
+      vt[2] = fpi::to_double(vtf[2]);
     } else {
       sample_cxs_target_velocity(awr, E, u, kT, seed, vt);
     }
@@ -1344,7 +1345,7 @@ __device__ int ev_collision(long long s, EvStats& st)
       st.coll_nuc += 1;
       Micro m = micro_xs64(nuc, i_log, E);
       prob += s_tabs.mat_dens[k] * m.total;
-      if (prob >= cutoff) {
+      if (fpi::le(cutoff, prob)) {
         chosen = nuc;
         m_tot = m.total;
         m_abs = m.absorption;
@@ -1360,10 +1361,10 @@ __device__ int ev_collision(long long s, EvStats& st)
       int ig;
       micro_xs32(nuc, i_log, E, t, ab, ig, f32);
       prob += s_tabs.mat_dens32[k] * t;
-      if (static_cast<double>(prob) >= cutoff) {
+      if (fpi::le(cutoff, fpi::to_double(prob))) {
         chosen = nuc;
-        m_tot = t;
-        m_abs = ab;
+        m_tot = fpi::to_double(t);
+        m_abs = fpi::to_double(ab);
         break;
       }
     }
@@ -1374,10 +1375,10 @@ __device__ int ev_collision(long long s, EvStats& st)
     wgt = 0.0;
   } else {
     // absorption (analog) src/physics.cpp:638-672
-    if (m_abs > 0.0) {
-      if (m_abs > prn(seed) * m_tot) wgt = 0.0;
+    if (fpi::pos(m_abs)) {
+      if (fpi::lt(prn(seed) * m_tot, m_abs)) wgt = 0.0;
     }
-    if (wgt != 0.0) {
+    if (!fpi::zero(wgt)) {
       // scatter src/physics.cpp:674-752: the reaction cutoff is drawn; the
       // nuclides of this path have elastic scattering as their only
       // scattering reaction, so the elastic branch is taken
@@ -1388,7 +1389,7 @@ __device__ int ev_collision(long long s, EvStats& st)
         double r[3] = {db.rx[s], db.ry[s], db.rz[s]};
         apply_weight_windows(s, wgt, seed, r, u, E, SURFACE_NONE);
       }
-      if (E < dm.energy_cutoff) wgt = 0.0;
+      if (fpi::lt(E, dm.energy_cutoff)) wgt = 0.0;
     }
   }
   if (dm.n_tally_collision > 0 && chosen >= 0) {
@@ -1508,7 +1509,7 @@ __global__ void __launch_bounds__(256) k_score_tracks()
     const int i = base + threadIdx.x;
     EvStats st {};
     const double w = i < n ? T.w[i] : 0.0;
-    if (w != 0.0) {
+    if (!fpi::zero(w)) {
       const double d = T.d[i];
       const double r0[3] = {T.r0x[i], T.r0y[i], T.r0z[i]};
       const double u[3] = {T.ux[i], T.uy[i], T.uz[i]};
@@ -1898,6 +1899,8 @@ struct GpuSim {
   // weight windows on device (one set)
   double *d_ww_lower = nullptr, *d_ww_upper = nullptr, *d_ww_e = nullptr;
   long long ww_size = 0;
+  unsigned long long* d_group_max = nullptr;  // MAGIC update: per-group maxima
+  int n_group_max = 0;
 
   ~GpuSim()
   {
@@ -1920,6 +1923,9 @@ static void build_model(GpuSim& G, const HModel& m, const GpuOptions& opt)
     for (int j = 0; j < 4; ++j) surf[k].c[j] = m.surfaces[k].c[j];
     surf[k].type = m.surfaces[k].type;
     surf[k].bc = m.surfaces[k].bc;
+    // squared radius, rounded once as the device expressions would round it
+    const double r = surf[k].type >= 3 && surf[k].type <= 5 ? surf[k].c[2] : surf[k].c[3];
+    surf[k].rr = surf[k].type >= 3 ? r * r : 0.0;
   }
   std::vector<DCell> cells(m.cells.size());
   std::vector<int> tok;
@@ -1946,6 +1952,7 @@ static void build_model(GpuSim& G, const HModel& m, const GpuOptions& opt)
     for (int j = 0; j < 3; ++j) {
       lats[k].ll[j] = l.ll[j];
       lats[k].pitch[j] = l.pitch[j];
+      lats[k].half[j] = 0.5 * l.pitch[j];
       lats[k].n[j] = l.n[j];
     }
     lats[k].is3d = l.is3d;
@@ -2634,6 +2641,86 @@ void gpu_set_ww_bounds(GpuSim* G, const double* lower, const double* upper, long
   if (n != G->ww_size) throw std::runtime_error("weight-window bounds have the wrong size");
   CK(cudaMemcpy(G->d_ww_lower, lower, sizeof(double) * n, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(G->d_ww_upper, upper, sizeof(double) * n, cudaMemcpyHostToDevice));
+}
+
+// src/weight_windows.cpp:640-673: mean (or 1 / relative error) per window
+// bin over the element volume, kept in lower; the relative error in upper;
+// the positive maximum of each energy group through an integer atomic max
+// on the bit pattern (positive doubles order like their bits).
+__global__ void k_magic_values(MagicArgs a, const double* sum, const double* sum_sq, double* lower, double* upper,
+                               unsigned long long* group_max)
+{
+  const long long n_bins = a.e_bins * a.mesh_bins;
+  for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < n_bins;
+       k += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int e = static_cast<int>(k / a.mesh_bins);
+    const long long mb = k - e * a.mesh_bins;
+    long long fb = mb * a.stride_mesh;
+    if (a.stride_energy >= 0) fb += e * a.stride_energy;
+    const long long i = fb * a.n_scores + a.score;
+    const double s = sum[i];
+    double nb = s / a.n;
+    double rel;
+    if (s > 0.0) {
+      const double mean_val = nb;
+      const double variance = (sum_sq[i] / a.n - mean_val * mean_val) / (a.n - 1);
+      rel = sqrt(variance) / mean_val;
+    } else {
+      rel = 1.7976931348623157e308;
+    }
+    if (a.rel_err) nb = 1.0 / rel;
+    nb /= a.volume;
+    lower[k] = nb;
+    upper[k] = rel;
+    if (nb > 0.0) atomicMax(group_max + e, static_cast<unsigned long long>(__double_as_longlong(nb)));
+  }
+}
+
+// src/weight_windows.cpp:675-700, 734-753: per-group normalisation by
+// 1 / (2 max), -1 where the bin is unscored or noisier than the threshold,
+// upper = ratio x lower.
+__global__ void k_magic_finish(MagicArgs a, const double* sum, double* lower, double* upper,
+                               const unsigned long long* group_max)
+{
+  const long long n_bins = a.e_bins * a.mesh_bins;
+  for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < n_bins;
+       k += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int e = static_cast<int>(k / a.mesh_bins);
+    const long long mb = k - e * a.mesh_bins;
+    long long fb = mb * a.stride_mesh;
+    if (a.stride_energy >= 0) fb += e * a.stride_energy;
+    const double s = sum[fb * a.n_scores + a.score];
+    double nb = lower[k];
+    const double rel = upper[k];
+    const double gm = __longlong_as_double(static_cast<long long>(group_max[e]));
+    if (gm > 0.0) nb *= 1.0 / (2.0 * gm);
+    if (s <= 0.0) nb = -1.0;
+    else if (rel > a.threshold) nb = -1.0;
+    lower[k] = nb;
+    upper[k] = a.ratio * nb;
+  }
+}
+
+void gpu_update_magic(GpuSim* G, const MagicArgs& a, double* lower, double* upper)
+{
+  const long long n = a.e_bins * a.mesh_bins;
+  if (n != G->ww_size || !G->d_ww_lower) throw std::runtime_error("weight-window bounds have the wrong size");
+  if (a.tally < 0 || a.tally + 1 >= static_cast<int>(G->tally_off.size()))
+    throw std::runtime_error("tally index out of range");
+  if (G->n_group_max < a.e_bins) {
+    G->d_group_max = dev_alloc<unsigned long long>(a.e_bins, G->owned);
+    G->n_group_max = a.e_bins;
+  }
+  const long long off = G->tally_off[a.tally];
+  CK(cudaMemsetAsync(G->d_group_max, 0, sizeof(unsigned long long) * a.e_bins, G->stream));
+  const int nb = G->blocks, nt = 256;
+  k_magic_values<<<nb, nt, 0, G->stream>>>(a, G->d_sum + off, G->d_sumsq + off, G->d_ww_lower, G->d_ww_upper,
+                                           G->d_group_max);
+  k_magic_finish<<<nb, nt, 0, G->stream>>>(a, G->d_sum + off, G->d_ww_lower, G->d_ww_upper, G->d_group_max);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(lower, G->d_ww_lower, sizeof(double) * n, cudaMemcpyDeviceToHost, G->stream));
+  CK(cudaMemcpyAsync(upper, G->d_ww_upper, sizeof(double) * n, cudaMemcpyDeviceToHost, G->stream));
+  CK(cudaStreamSynchronize(G->stream));
 }
 
 void gpu_set_ww_on(GpuSim* G, bool on)

@@ -25,6 +25,22 @@ struct GpuOptions {
   int defer_tally = 1;          // track-length tallies scored by their own kernel from track records
 };
 
+// One MAGIC weight-window update (WeightWindows::update_weights,
+// src/weight_windows.cpp:502-755) from a flux tally's accumulated sums.
+struct MagicArgs {
+  int tally = 0;              // tally index
+  int score = 0;              // position of the flux score among the tally's scores
+  int n_scores = 1;
+  long long stride_mesh = 1;  // filter-bin stride of the mesh filter
+  long long stride_energy = -1;  // of the energy filter, -1: none
+  int e_bins = 1;
+  long long mesh_bins = 1;
+  int n = 1;                  // realizations
+  double volume = 1.0;        // of one mesh element
+  int rel_err = 0;            // 1: bounds from 1 / relative error, 0: from the mean
+  double threshold = 1.0, ratio = 5.0;
+};
+
 struct BatchStats {
   float ms = 0;
   int error = 0;
@@ -64,6 +80,7 @@ struct BatchStats {
   void gpu_get_trace(GpuSim* g, void* records, int* counts);                                \
   void gpu_set_ww_bounds(GpuSim* g, const double* lower, const double* upper, long long n); \
   void gpu_set_ww_on(GpuSim* g, bool on);                                                   \
+  void gpu_update_magic(GpuSim* g, const MagicArgs& a, double* lower, double* upper);        \
   long long gpu_capacity(GpuSim* g);                                                        \
   void gpu_material_xs(GpuSim* g, long long n, const int* mat, const double* E, double* total, \
                        double* absorption, unsigned* grid_hash);                               \
@@ -85,6 +102,10 @@ void gpu_set_trace(GpuSim* g, long long n_hist, int cap, int batch, long long fi
 void gpu_get_trace(GpuSim* g, void* records, int* counts);
 void gpu_set_ww_bounds(GpuSim* g, const double* lower, const double* upper, long long n);
 void gpu_set_ww_on(GpuSim* g, bool on);
+// MAGIC update of the device's weight windows from the device's tally sums
+// (no tally copy to the host); the new bounds are also copied into the host
+// arrays lower / upper (e_bins x mesh_bins each).
+void gpu_update_magic(GpuSim* g, const MagicArgs& a, double* lower, double* upper);
 long long gpu_capacity(GpuSim* g);
 // Macroscopic total and absorption cross sections (and the nuclide grid-index
 // hash) of the model's materials at (material index, E) pairs, evaluated on

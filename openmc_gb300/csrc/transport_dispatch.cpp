@@ -85,6 +85,11 @@ void gpu_set_ww_bounds(GpuSim* g, const double* lower, const double* upper, long
 }
 
 void gpu_set_ww_on(GpuSim* g, bool on) { OMC_FORWARD(gpu_set_ww_on, on); }
+
+void gpu_update_magic(GpuSim* g, const MagicArgs& a, double* lower, double* upper)
+{
+  OMC_FORWARD(gpu_update_magic, a, lower, upper);
+}
 long long gpu_capacity(GpuSim* g) { OMC_FORWARD(gpu_capacity); }
 int gpu_levels(GpuSim* g) { return g ? g->levels : 0; }
 

@@ -126,13 +126,13 @@ def test_learned_windows_raise_figure_of_merit(built, tmp_path):
 
 
 @pytest.mark.parametrize("value", ["mean", "rel_err"])
-def test_magic_update_matches_restatement(built, tmp_path, value):
-    """openmc_weight_windows_update_magic against a numpy restatement of
-    WeightWindows::update_weights (src/weight_windows.cpp:502-755) applied to
-    the same tally results: per-group normalisation by twice the maximum of
-    flux / volume, -1 where unscored or noisier than the threshold, upper =
-    ratio x lower."""
+def test_magic_update_matches_oracle(built, tmp_path, value):
+    """openmc_weight_windows_update_magic against the oracle's restatement of
+    WeightWindows::update_weights (oracle/magic.py, src/weight_windows.cpp:
+    502-755) on the same tally sums: on the device while the simulation
+    holds the tallies there, and on the host after it has ended."""
     from openmc_gb300 import configs, lib
+    from oracle import magic
     groups = [0.0, 1.0, 1.0e4, 2.0e7 * 1.000001]
     m, path = configs.shield(tmp_path, particles=20_000, batches=3, n_points=1500, length=60.0,
                              mesh_dim=(12, 2, 2), energy_groups=groups, tally_mesh_windows=True,
@@ -146,32 +146,26 @@ def test_magic_update_matches_restatement(built, tmp_path, value):
         lib.simulation_init()
         for _ in range(3):
             lib.next_batch()
-        lib.simulation_finalize()
         tid = lib.tally_ids()[0]
+        ww = lib.WeightWindows(0)
+        ww.update_magic(lib.tally_index(tid), value, threshold, ratio)   # device
+        dev_lower, dev_upper = (b.copy() for b in ww.bounds)
+        lib.simulation_finalize()
         res = lib.tally_results(tid).copy()       # [mesh * group][score][3]
         n = lib.tally_n_realizations(tid)
-        ww = lib.WeightWindows(0)
-        ww.update_magic(lib.tally_index(tid), value, threshold, ratio)
-        lower, upper = ww.bounds
+        ww.update_magic(lib.tally_index(tid), value, threshold, ratio)   # host
+        host_lower, host_upper = (b.copy() for b in ww.bounds)
     finally:
         lib.finalize()
     n_mesh, n_e = 12 * 2 * 2, len(groups) - 1
     s = res[:, 0, 1].reshape(n_mesh, n_e).T         # [e][m]
     s2 = res[:, 0, 2].reshape(n_mesh, n_e).T
-    mean = s / n
-    with np.errstate(divide="ignore", invalid="ignore"):
-        rel = np.where(s > 0, np.sqrt((s2 / n - mean * mean) / (n - 1)) / mean, np.inf)
-        b = 1.0 / rel if value == "rel_err" else mean.copy()
     vol = (60.0 / 12) * (50.0 / 2) * (50.0 / 2)
-    b = b / vol
-    for e in range(n_e):
-        mx = b[e].max()
-        if mx > 0:
-            b[e] = b[e] * (1.0 / (2.0 * mx))
-    b = np.where(s <= 0, -1.0, np.where(rel > threshold, -1.0, b))
-    assert (b > 0).sum() > 0 and (b < 0).sum() > 0
+    lower, upper = magic.update_weights(s, s2, n, vol, value, threshold, ratio)
+    assert (lower > 0).sum() > 0 and (lower < 0).sum() > 0
     # 1 / rel_err goes through sum_sq / n - mean^2, whose cancellation turns
-    # the host compiler's freedom to fuse multiply-adds into ~1e-11 relative
+    # a compiler's freedom to fuse multiply-adds into ~1e-11 relative
     tol = 1e-14 if value == "mean" else 1e-10
-    np.testing.assert_allclose(lower, b.ravel(), rtol=tol, atol=0)
-    np.testing.assert_allclose(upper, ratio * b.ravel(), rtol=tol, atol=0)
+    for lo, up in ((dev_lower, dev_upper), (host_lower, host_upper)):
+        np.testing.assert_allclose(lo, lower.ravel(), rtol=tol, atol=0)
+        np.testing.assert_allclose(up, upper.ravel(), rtol=tol, atol=0)

@@ -65,6 +65,9 @@ def parse():
                          "and adds (default: the build with fused multiply-adds)")
     ap.add_argument("--no-defer", action="store_true",
                     help="score track-length tallies inside the advance kernel instead of from track records")
+    ap.add_argument("--fuse", type=int, default=-1,
+                    help="events run inside the advance kernel: 1 cross sections, 3 cross sections and "
+                         "surface crossings (default: the library's choice)")
     ap.add_argument("--no-graph", action="store_true",
                     help="launch every batch kernel by kernel instead of as one CUDA graph "
                          "(for kernel profilers, which cannot see inside conditional graphs)")
@@ -228,6 +231,8 @@ def run_gb300(args, barrier=lambda: None, rank=0):
         lib.settings.contract = 0 if args.no_contract else 1
         lib.settings.defer_tally = 0 if args.no_defer else 1
         lib.settings.particles_in_flight = args.in_flight
+        if args.fuse >= 0:
+            lib.settings.fuse_xs = args.fuse
         fused = int(lib.settings.fuse_xs)
         sort = int(lib.settings.sort_queue)
         if args.no_graph:
@@ -353,7 +358,7 @@ def shield_fom():
     flux of the 200 cm deep-penetration shield (densities x 0.1, 200 x 10 x 10
     mesh x 6 energy groups) for plain transport (200 x 10^6 histories),
     MAGIC windows and learned windows from the same 5 x 10^6-history pilot
-    (10 x 10^6 histories each), FP32 tables; T is the device time of the
+    (40 x 10^6 histories each), FP32 tables; T is the device time of the
     measured batches (and, in fom_with_setup, also of the pilot and the
     network's training).  Each figure of merit carries its relative
     uncertainty.  A failure here is reported in the line instead of ending
@@ -361,8 +366,9 @@ def shield_fom():
     from openmc_gb300 import shield_study
     try:
         # the plain arm runs 200 batches, so that its back-face relative
-        # error (0.43 after 10 batches) comes down to ~0.1
-        r = shield_study.run(ROOT / "_models" / "shield_bench", plain_batches=200)
+        # error (0.43 after 10 batches) comes down to ~0.1; 40 batches of
+        # each windowed arm bound its figure of merit to ~23 %
+        r = shield_study.run(ROOT / "_models" / "shield_bench", batches=40, plain_batches=200)
     except Exception as e:  # the transport line above stands on its own
         return {"error": f"{type(e).__name__}: {e}"}
     out = {"workload": r["workload"], "pilot": r["pilot"], "measure": r["measure"],

@@ -145,6 +145,10 @@ extern int openmc_gb300_contract;
  * 0: the advance kernel scores them itself */
 extern int openmc_gb300_defer_tally;
 
+/* eigenvalue run: the track-length k of every generation so far (at most n
+ * written; returns how many there are) and the last generation's
+ * fission-bank size (src/eigenvalue.cpp:50-84 k_generation) */
+int openmc_gb300_k_generation(double* k, int n, int64_t* fission_sites);
 /* last batch: [ms, iterations, events, total_weight, leakage, lost, done, secondary-pool entries used,
  *  events of the longest history, its particle id] */
 int openmc_gb300_last_batch(double* out);
@@ -226,7 +230,7 @@ bool openmc_master(void);                                              /* src/in
 bool openmc_is_statepoint_batch(void);                                 /* src/state_point.cpp */
 int openmc_get_n_batches(int* n_batches, bool get_max_batches);        /* src/settings.cpp:1319-1324 */
 int openmc_set_n_batches(int32_t n_batches, bool set_max_batches, bool add_statepoint_batch);  /* :1285-1317 */
-int openmc_get_keff(double k_combined[]);                              /* src/eigenvalue.cpp:420-440 */
+int openmc_get_keff(double k_combined[]);                              /* src/eigenvalue.cpp:420-579 */
 int openmc_get_cell_index(int32_t id, int32_t* index);                 /* src/cell.cpp */
 int openmc_cell_get_id(int32_t index, int32_t* id);
 int openmc_cell_get_translation(int32_t index, double xyz[]);

@@ -12,6 +12,9 @@
 * ``shield``         200x50x50 cm stack of alternating 10 cm light/heavy
                      layers, 1 MeV monodirectional plane source at x=0,
                      flux on a 200x10x10 mesh.
+* ``infinite_medium`` eigenvalue run in a reflective cube of one fissile
+                     mixture with energy-independent cross sections
+                     (k-infinity known exactly).
 
 Every builder writes the nuclide library it needs (seeded, deterministic) and
 returns ``(model, directory)``; ``model.export_to_model_xml`` then produces the
@@ -102,6 +105,46 @@ def point_cube(directory, particles=100_000, batches=10, n_points=2000,
             te.estimator = est
             tallies += [tc, tm, te]
     return om.Model(geom, mats, settings, om.Tallies(tallies)), directory
+
+
+def infinite_medium(directory, particles=20_000, batches=30, inactive=10, n_points=500, seed=7,
+                    event_based=True, fissile_fraction=0.045):
+    """Eigenvalue run in an infinite homogeneous medium: a reflective 20 cm
+    cube of one material made of a fissile nuclide and a light moderator
+    whose cross sections do not depend on energy, so that
+    k-infinity = nu Sigma_f / Sigma_a exactly (returned as the model's
+    ``k_inf`` attribute); flux tally on a 4x4x4 mesh."""
+    directory = Path(directory)
+    nu, sf, sc_f, se_f = 2.43, 8.0, 5.0, 10.0
+    sc_m, se_m = 0.3, 20.0
+    nucs = [data.make_flat_nuclide("Fx235", 235, n_points, seed, se_f, sc_f, fission=sf, nu=nu),
+            data.make_flat_nuclide("Mx1", 1, n_points, seed + 1, se_m, sc_m)]
+    xs_xml = data.write_library(nucs, directory)
+    mat = om.Material(name="fissile mixture")
+    mat.add_nuclide("Fx235", fissile_fraction)
+    mat.add_nuclide("Mx1", 1.0 - fissile_fraction)
+    mat.set_density("atom/b-cm", 0.1)
+    mats = om.Materials([mat], cross_sections=xs_xml.name)
+    planes = [om.XPlane(-10.0, boundary_type="reflective"), om.XPlane(10.0, boundary_type="reflective"),
+              om.YPlane(-10.0, boundary_type="reflective"), om.YPlane(10.0, boundary_type="reflective"),
+              om.ZPlane(-10.0, boundary_type="reflective"), om.ZPlane(10.0, boundary_type="reflective")]
+    box = +planes[0] & -planes[1] & +planes[2] & -planes[3] & +planes[4] & -planes[5]
+    geom = om.Geometry(om.Universe(cells=[om.Cell(fill=mat, region=box)]))
+    settings = om.Settings(run_mode="eigenvalue", particles=particles, batches=batches, inactive=inactive,
+                           event_based=event_based, seed=1)
+    settings.source = [om.IndependentSource(space=om.Box((-10.0, -10.0, -10.0), (10.0, 10.0, 10.0)),
+                                            angle=om.Isotropic(), energy=om.Maxwell(1.3e6))]
+    mesh = om.RegularMesh()
+    mesh.dimension = [4, 4, 4]
+    mesh.lower_left = [-10.0, -10.0, -10.0]
+    mesh.upper_right = [10.0, 10.0, 10.0]
+    t = om.Tally(name="mesh flux")
+    t.filters = [om.MeshFilter(mesh)]
+    t.scores = ["flux"]
+    model = om.Model(geom, mats, settings, om.Tallies([t]))
+    f = fissile_fraction
+    model.k_inf = nu * f * sf / (f * (sc_f + sf) + (1.0 - f) * sc_m)
+    return model, directory
 
 
 def _pin_universe(fuel, clad, mod, r_pin=0.41, r_clad=0.475, guide=False):

@@ -105,6 +105,13 @@ struct State {
   long long trace_hist = 0;
   int trace_cap = 0;
   bool ww_user_set = false;
+  // eigenvalue run (src/eigenvalue.cpp): every generation's track-length k,
+  // the running sums of the active ones, and the cross sums of the three
+  // estimators for the combined k
+  std::vector<double> k_generation;
+  double k_sum[2] = {0.0, 0.0};
+  double k_col_abs = 0.0, k_col_tra = 0.0, k_abs_tra = 0.0;
+  long long fission_sites = 0;
 };
 
 State& S()
@@ -314,6 +321,63 @@ int capi_fail(int code, const std::string& msg) { return fail(code, msg); }
 
 namespace {
 
+// One eigenvalue generation's end: src/simulation.cpp:522-570
+// finalize_generation (global tallies, fission-bank sort and comb on the
+// device, generation and average k), then src/tallies/tally.cpp:1059-1100
+// accumulate_tallies and src/simulation.cpp:414-418 (global tallies and
+// realizations reset after an inactive batch).
+void finish_generation(State& s, HModel& m, const BatchStats& st, bool active)
+{
+  auto& gt = s.global_tallies;  // [K_COLLISION, K_ABSORPTION, K_TRACKLENGTH, LEAKAGE][VALUE, SUM, SUM_SQ]
+  const double keff_generation_start = gt[6];
+  GenerationStats g = gpu_finish_generation(s.gpu, current_batch);
+  s.fission_sites = g.fission_sites;
+  gt[0] += g.k_col;
+  gt[3] += g.k_abs;
+  gt[6] += g.k_tra;
+  gt[9] += st.leakage;
+  // src/eigenvalue.cpp:50-84 calculate_generation_keff
+  double kg = gt[6] - keff_generation_start;
+  kg /= m.n_particles;
+  s.k_generation.push_back(kg);
+  // src/eigenvalue.cpp:367-418 calculate_average_keff (one generation per
+  // batch, no confidence-interval t-value)
+  const int i = static_cast<int>(s.k_generation.size()) - 1;
+  const int n = active ? n_realizations + 1 : 0;
+  if (n <= 0) {
+    keff = s.k_generation[i];
+  } else {
+    s.k_sum[0] += s.k_generation[i];
+    s.k_sum[1] += std::pow(s.k_generation[i], 2);
+    keff = s.k_sum[0] / n;
+    if (n > 1) {
+      const double t_value = 1.0;
+      keff_std = t_value * std::sqrt((s.k_sum[1] / n - std::pow(keff, 2)) / (n - 1));
+      if (!std::isfinite(keff_std)) keff_std = 0.0;
+    }
+  }
+  gpu_set_keff(s.gpu, keff);
+  // accumulate_tallies: global tallies per unit source weight
+  ++n_realizations;
+  const double tw = st.total_weight;
+  if (active) {
+    const double k_col = gt[0] / tw, k_abs = gt[3] / tw, k_tra = gt[6] / tw;
+    s.k_col_abs += k_col * k_abs;
+    s.k_col_tra += k_col * k_tra;
+    s.k_abs_tra += k_abs * k_tra;
+  }
+  for (int t = 0; t < 4; ++t) {
+    const double val = gt[3 * t] / tw;
+    gt[3 * t] = 0.0;
+    gt[3 * t + 1] += val;
+    gt[3 * t + 2] += val * val;
+  }
+  if (!active) {
+    std::fill(gt.begin(), gt.end(), 0.0);
+    n_realizations = 0;
+  }
+}
+
 int check_device_errors(const BatchStats& st)
 {
   HModel& m = S().model;
@@ -412,6 +476,12 @@ int openmc_simulation_init()
     if (s.trace_hist > 0) gpu_set_trace(s.gpu, s.trace_hist, s.trace_cap, openmc_gb300_trace_batch, openmc_gb300_trace_first);
     gpu_reset_tallies(s.gpu, m);
     std::fill(s.global_tallies.begin(), s.global_tallies.end(), 0.0);
+    s.k_generation.clear();
+    s.k_sum[0] = s.k_sum[1] = 0.0;
+    s.k_col_abs = s.k_col_tra = s.k_abs_tra = 0.0;
+    s.fission_sites = 0;
+    keff = 1.0;
+    keff_std = 0.0;
     current_batch = 0;
     n_realizations = 0;
     n_lost_particles = 0;
@@ -456,12 +526,16 @@ int openmc_next_batch(int* status)
       s.time_inactive += st.ms * 1e-3;
     }
     if (int rc = check_device_errors(st)) return rc;
-    if (active) {
+    if (m.eigenvalue) {
+      finish_generation(s, m, st, active);
+    } else if (active) {
       ++n_realizations;
       // global leakage tally normalised by total source weight (tally.cpp:1059-1100)
       double val = st.leakage / st.total_weight;
       s.global_tallies[9 + 1] += val;
       s.global_tallies[9 + 2] += val * val;
+    }
+    if (active) {
       // weight-window generators (src/weight_windows.cpp:967-994)
       bool need = false;
       for (const auto& g : m.ww_generators) need = need || g.tally >= 0;
@@ -718,6 +792,89 @@ int openmc_global_tallies(double** ptr)
 }
 
 // ------------------------------------------------------ weight windows
+// src/eigenvalue.cpp:420-579 openmc_get_keff: up to three realizations the
+// average k and its spread (infinite up to one realization; a fixed-source
+// run keeps k = 1); beyond, the combination of the collision, absorption and
+// track-length estimators weighted by their covariances (Urbatsch), or of
+// two of them when two estimators coincide.
+int openmc_get_keff(double* k_combined)
+{
+  const State& s = S();
+  k_combined[0] = 0.0;
+  k_combined[1] = 0.0;
+  if (n_realizations <= 3) {
+    k_combined[0] = keff;
+    k_combined[1] = keff_std;
+    if (n_realizations <= 1) k_combined[1] = std::numeric_limits<double>::infinity();
+    return 0;
+  }
+  const int64_t n = n_realizations;
+  const auto& gt = s.global_tallies;
+  double kv[3], cov[3][3];
+  for (int e = 0; e < 3; ++e) kv[e] = gt[3 * e + 1] / n;
+  for (int e = 0; e < 3; ++e) cov[e][e] = (gt[3 * e + 2] - n * kv[e] * kv[e]) / (n - 1);
+  cov[0][1] = cov[1][0] = (s.k_col_abs - n * kv[0] * kv[1]) / (n - 1);
+  cov[0][2] = cov[2][0] = (s.k_col_tra - n * kv[0] * kv[2]) / (n - 1);
+  cov[1][2] = cov[2][1] = (s.k_abs_tra - n * kv[1] * kv[2]) / (n - 1);
+  const double rel = 1e-5;  // FP_REL_PRECISION
+  auto same = [&](int a, int b) {
+    return std::abs(kv[a] - kv[b]) / kv[a] < rel && std::abs(cov[a][a] - cov[b][b]) / cov[a][a] < rel;
+  };
+  int i = 0, j = 0;
+  bool use_three = false;
+  if (same(0, 1)) {
+    i = 0;
+    j = 2;
+  } else if (same(0, 2)) {
+    i = 0;
+    j = 1;
+  } else if (same(1, 2)) {
+    i = 0;
+    j = 1;
+  } else {
+    use_three = true;
+  }
+  if (use_three) {
+    double g = 0.0;
+    double S3[3] = {0.0, 0.0, 0.0};
+    const int perm[3][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}};  // (i, j, k) for l = 0, 1, 2
+    for (int l = 0; l < 3; ++l) {
+      const int a = perm[l][0], b = perm[l][1], c = perm[l][2];
+      const double f = cov[b][b] * (cov[c][c] - cov[a][c]) - cov[c][c] * cov[a][b] +
+                       cov[b][c] * (cov[a][b] + cov[a][c] - cov[b][c]);
+      S3[0] += f * cov[0][l];
+      S3[1] += (cov[b][b] + cov[c][c] - 2.0 * cov[b][c]) * kv[l] * kv[l];
+      S3[2] += (cov[c][c] + cov[a][b] - cov[b][c] - cov[a][c]) * kv[l] * kv[b];
+      k_combined[0] += f * kv[l];
+      g += f;
+    }
+    for (double& v : S3) v *= (n - 1);
+    S3[0] *= (n - 1) * (n - 1);
+    k_combined[0] /= g;
+    g *= (n - 1) * (n - 1);
+    k_combined[1] = std::sqrt(S3[0] / (g * n * (n - 3)) * (1 + n * ((S3[1] - 2 * S3[2]) / g)));
+  } else {
+    const double f = kv[i] - kv[j];
+    const double g = cov[i][i] + cov[j][j] - 2.0 * cov[i][j];
+    k_combined[0] = kv[i] - (cov[i][i] - cov[i][j]) / g * f;
+    k_combined[1] = (cov[i][i] * cov[j][j] - cov[i][j] * cov[i][j]) * (g + n * f * f) / (n * (n - 2) * g * g);
+    k_combined[1] = std::sqrt(k_combined[1]);
+  }
+  return 0;
+}
+
+// GB300 extension (no reference counterpart): every generation's
+// track-length k (at most n of them; returns how many exist) and the last
+// generation's fission-bank size
+int openmc_gb300_k_generation(double* k, int n, int64_t* fission_sites)
+{
+  const State& s = S();
+  const int m = static_cast<int>(s.k_generation.size());
+  for (int i = 0; i < m && i < n; ++i) k[i] = s.k_generation[i];
+  if (fission_sites) *fission_sites = s.fission_sites;
+  return m;
+}
+
 // src/weight_windows.cpp:1020-1340
 size_t openmc_weight_windows_size() { return S().model.weight_windows.size(); }
 

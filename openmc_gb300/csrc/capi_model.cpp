@@ -112,15 +112,6 @@ int openmc_set_n_batches(int32_t n_batches, bool set_max_batches, bool add_state
   return 0;
 }
 
-// Fixed-source runs leave k at its initial 1 with no spread; the reference
-// reports an infinite standard deviation up to one realization.
-int openmc_get_keff(double k_combined[])
-{
-  k_combined[0] = keff;
-  k_combined[1] = n_realizations <= 1 ? std::numeric_limits<double>::infinity() : keff_std;
-  return 0;
-}
-
 // -------------------------------------------------------- cells, materials
 // src/cell.cpp (openmc_get_cell_index, openmc_cell_get_id,
 // openmc_cell_get_translation, openmc_cell_get_name), src/material.cpp

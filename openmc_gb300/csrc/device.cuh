@@ -47,9 +47,27 @@ struct DCell {
   int universe, fill_type, fill, tok_off, tok_len, simple;
 };
 
-// FP64 cross-section row of one grid point (32 B, two 16-byte loads)
+// FP64 cross-section row of one grid point (32 B, two 16-byte loads): the
+// create_derived columns the transport reads (fission and nu-fission are 0
+// for a nuclide without MT 18)
 struct alignas(16) XsRow64 {
-  double total, absorption, elastic, unused;
+  double total, absorption, fission, nu_fission;
+};
+
+// Fission neutron data of a nuclide (MT 18, prompt product): yield
+// polynomial nu0 + nu1 E, spectrum 1 Maxwell (p0 = theta) or 2 Watt (a, b),
+// restriction energy u
+struct DFission {
+  double nu0, nu1, p0, p1, u;
+  int spectrum, pad;
+};
+
+// One site of the fission bank (SourceSite of src/particle_data.h:43-57 for
+// a prompt fission neutron: weight 1, time 0, on no surface)
+struct DFissionSite {
+  double r[3], u[3], E;
+  long long parent;  // source index of the parent history (1-based)
+  int progeny, pad;
 };
 
 struct DLattice {
@@ -101,7 +119,13 @@ struct DModel {
   const int* mat_nuc;
   const double* mat_dens;
   const float* mat_dens32;
+  const DFission* fis;  // per nuclide (eigenvalue runs)
   int n_nuc, n_mat, M, xs_fp32;
+  // eigenvalue run: the running k-effective the fission sites are sampled
+  // with, and data::energy_max[neutron] (fission energies at or above it
+  // are resampled)
+  int eigen;
+  double keff, e_max_neutron;
   double e_min, e_max, log_spacing;
   float log_emin32, inv_spacing32;  // FP32 log(e_min) and 1 / log_spacing for the hash-bin pre-test
   // source
@@ -152,11 +176,15 @@ struct DBank {
   unsigned long long* seed;
   double *E, *wgt, *wgt_born, *wgt_ww_born, *ww_factor;
   double *ux, *uy, *uz;
+  double *iux, *iuy, *iuz;  // 1 / u (FP32-table mode), written wherever the direction changes
   double *rx, *ry, *rz;
   int *cell, *univ, *latt, *lix, *liy, *liz;
   int *n_coord, *cell_last0, *cell_born;
   int *surface, *material, *material_last;
   double *macro_t, *macro_a;
+  double* macro_nf;                  // macroscopic nu-fission (eigenvalue runs)
+  double *k_col, *k_abs, *k_tra;     // the history's k-effective scores (eigenvalue runs)
+  int* n_progeny;                    // fission sites the history has banked
   int *bsurf, *blevel, *btrans;
   int *n_event, *n_collision, *n_split;
   int* sec_top;   // top of the slot's LIFO chain of banked secondaries
@@ -208,6 +236,11 @@ struct DCounters {
   unsigned long long split_head, split_tail, refill_split_base;
   int refill_split;  // of this iteration's refill: how many come from the ring
   int split_cap;
+  // eigenvalue runs: fission sites banked, bank overflow, and the
+  // generation's collision, absorption and track-length k-effective sums
+  unsigned long long n_fission;
+  int fbank_full, pad1;
+  double k_col, k_abs, k_tra;
 };
 
 // Source site of one history, sampled for the whole batch up front:
@@ -246,6 +279,14 @@ struct DQueues {
   int* cursor;
   DSecondary* sec;
   DSplitSite* split;  // split-to-slots ring, or null
+  // eigenvalue runs: the generation's fission bank (append order), its
+  // capacity, the progeny count of each source index, and whether the source
+  // bank already holds this generation's sites (every generation after the
+  // first)
+  DFissionSite* fbank;
+  long long fbank_cap;
+  int* progeny;
+  int src_from_bank;
   int history;        // 1: history-based loop (slots are not recycled through the free list)
   DCounters* cnt;
   TraceRec* trace;
@@ -358,7 +399,7 @@ __device__ __forceinline__ void tables_enter()
 
 // ------------------------------------------------------------------- RNG
 // src/random_lcg.cpp:32-44: one step of the generator and its output word
-__device__ __forceinline__ unsigned long long prn_word(unsigned long long& s)
+__host__ __device__ __forceinline__ unsigned long long prn_word(unsigned long long& s)
 {
   s = PRN_MULT * s + PRN_ADD;
   unsigned long long word = ((s >> ((s >> 59u) + 5u)) ^ s) * 12605985483714917081ull;
@@ -470,6 +511,13 @@ __device__ inline double maxwell_spectrum(double T, unsigned long long& s)
   return -T * (log(r1) + log(r2) * c * c);
 }
 
+// src/random_dist.cpp:34-43
+__device__ inline double watt_spectrum(double a, double b, unsigned long long& s)
+{
+  double w = maxwell_spectrum(a, s);
+  return w + 0.25 * a * a * b + uniform_distribution(-1., 1., s) * sqrt(a * a * b * w);
+}
+
 // Lower bound index on a sorted double range (include/openmc/search.h:14-20).
 // Doubles of one sign order like their bit patterns; energies and bin edges
 // here are non-negative, so the comparisons run on the integer pipe.
@@ -550,18 +598,18 @@ __device__ inline double cylinder_distance(double u1, double r2_, double u2, dou
   const double k = r2 * u2 + r3 * u3;
   const double c = r2 * r2 + r3 * r3 - radius;  // radius: the squared radius
   const double quad = k * k - a * c;
-  if (fpi::neg(quad)) {
-    return INFTY;
-  } else if (coincident || fpi::abs_lt(c, FP_COINCIDENT)) {
-    if (fpi::nonneg(k)) return INFTY;
-    return (-k + sqrt(quad)) / a;
-  } else if (fpi::neg(c)) {
-    return (-k + sqrt(quad)) / a;
-  } else {
-    const double d = (-k - sqrt(quad)) / a;
-    if (fpi::neg(d)) return INFTY;
-    return d;
-  }
+  if (fpi::neg(quad)) return INFTY;
+  // the reference's three branches (on the surface, inside, outside) with
+  // one square root and one division shared by all lanes: far root
+  // (-k + sqrt) on the surface (moving inwards) or inside, near root
+  // (-k - sqrt, INFTY when behind) outside
+  const bool on = coincident || fpi::abs_lt(c, FP_COINCIDENT);
+  if (on && fpi::nonneg(k)) return INFTY;
+  const bool far = on || fpi::neg(c);
+  const double sq = sqrt(quad);
+  const double d = (far ? -k + sq : -k - sq) / a;
+  if (!far && fpi::neg(d)) return INFTY;
+  return d;
 }
 
 __device__ inline double sphere_distance(const DSurface& s, double x_, double y_, double z_, double ux,
@@ -573,18 +621,14 @@ __device__ inline double sphere_distance(const DSurface& s, double x_, double y_
   const double k = x * ux + y * uy + z * uz;
   const double c = x * x + y * y + z * z - s.rr;
   const double quad = k * k - c;
-  if (fpi::neg(quad)) {
-    return INFTY;
-  } else if (coincident || fpi::abs_lt(c, FP_COINCIDENT)) {
-    if (fpi::nonneg(k)) return INFTY;
-    return -k + sqrt(quad);
-  } else if (fpi::neg(c)) {
-    return -k + sqrt(quad);
-  } else {
-    const double d = -k - sqrt(quad);
-    if (fpi::neg(d)) return INFTY;
-    return d;
-  }
+  if (fpi::neg(quad)) return INFTY;
+  const bool on = coincident || fpi::abs_lt(c, FP_COINCIDENT);
+  if (on && fpi::nonneg(k)) return INFTY;
+  const bool far = on || fpi::neg(c);
+  const double sq = sqrt(quad);
+  const double d = far ? -k + sq : -k - sq;
+  if (!far && fpi::neg(d)) return INFTY;
+  return d;
 }
 
 __device__ inline double surf_distance(const DSurface& s, double x, double y, double z, double ux,
@@ -849,6 +893,22 @@ __device__ inline void geo_store(const Geo& g, long long s)
   db.material_last[s] = g.material_last;
 }
 
+// New direction of slot s; in FP32-table mode also its reciprocal, which
+// the lattice and mesh distances of every later flight multiply by (the
+// direction changes at collisions and reflections, far less often than the
+// particle flies).
+__device__ __forceinline__ void set_direction(long long s, double ux, double uy, double uz)
+{
+  db.ux[s] = ux;
+  db.uy[s] = uy;
+  db.uz[s] = uz;
+  if (dm.xs_fp32) {
+    db.iux[s] = 1.0 / ux;
+    db.iuy[s] = 1.0 / uy;
+    db.iuz[s] = 1.0 / uz;
+  }
+}
+
 __device__ __forceinline__ void coord_reset(Geo& g, int l)
 {
   g.cell[l] = C_NONE;
@@ -1025,6 +1085,7 @@ struct Micro {
   double total, absorption;
   int i_grid;
   double f;
+  double fission, nu_fission;  // interpolated only when asked for (eigenvalue runs)
 };
 
 // Locates the grid interval of E and returns its index and bracketing
@@ -1068,7 +1129,9 @@ __device__ __forceinline__ XsRow64 ldg_row(const XsRow64* p)
   return XsRow64 {a.x, a.y, b.x, b.y};
 }
 
-__device__ __forceinline__ Micro micro_xs64(int nuc, int i_log, double E)
+// fiss: also interpolate the fission and nu-fission columns (the same two
+// rows, src/nuclide.cpp:760-775)
+__device__ __forceinline__ Micro micro_xs64(int nuc, int i_log, double E, bool fiss = false)
 {
   Micro m;
   double e0, e1;
@@ -1079,6 +1142,11 @@ __device__ __forceinline__ Micro micro_xs64(int nuc, int i_log, double E)
   const XsRow64 b = ldg_row(xs + m.i_grid + 1);
   m.total = (1.0 - m.f) * a.total + m.f * b.total;
   m.absorption = (1.0 - m.f) * a.absorption + m.f * b.absorption;
+  m.fission = m.nu_fission = 0.0;
+  if (fiss) {
+    m.fission = (1.0 - m.f) * a.fission + m.f * b.fission;
+    m.nu_fission = (1.0 - m.f) * a.nu_fission + m.f * b.nu_fission;
+  }
   return m;
 }
 
@@ -1089,7 +1157,9 @@ __device__ __forceinline__ Micro micro_xs64(int nuc, int i_log, double E)
 // stays accurate when f leaves [0, 1] (energies below the first or above the
 // last grid point extrapolate); (1 - f) a + f b cancels catastrophically in
 // FP32 there.
-__device__ __forceinline__ void micro_xs32(int nuc, int i_log, double E, float& t, float& a_out, int& i_grid, float& f32)
+// (the row's z is nu-fission; nf receives it interpolated when not null)
+__device__ __forceinline__ void micro_xs32(int nuc, int i_log, double E, float& t, float& a_out, int& i_grid, float& f32,
+  float* nf = nullptr)
 {
   double e0, e1;
   i_grid = nuclide_grid(nuc, i_log, E, e0, e1);
@@ -1099,6 +1169,7 @@ __device__ __forceinline__ void micro_xs32(int nuc, int i_log, double E, float& 
   f32 = fpi::to_float(E - e0) * a.w;
   t = a.x + f32 * (b.x - a.x);
   a_out = a.y + f32 * (b.y - a.y);
+  if (nf) *nf = a.z + f32 * (b.z - a.z);
 }
 
 // Hash bin of E (src/material.cpp:833-834), clamped to [0, M-1]: the
@@ -1123,38 +1194,44 @@ __device__ __forceinline__ int log_union_index(double E)
 }
 
 // src/material.cpp:829-901.  Returns the grid-index hash of the material's
-// nuclides (h = 31 h + i_grid) for per-history trace comparison.
-__device__ inline uint32_t material_xs(int mat, double E, double& tot, double& abs_)
+// nuclides (h = 31 h + i_grid) for per-history trace comparison.  nf (an
+// eigenvalue run) receives the macroscopic nu-fission cross section.
+__device__ inline uint32_t material_xs(int mat, double E, double& tot, double& abs_, double* nf = nullptr)
 {
   int i_log = log_union_index(E);
   int a = s_tabs.mat_off[mat], b = s_tabs.mat_off[mat + 1];
   uint32_t h = 0;
+  const bool fiss = nf != nullptr;
   if (!dm.xs_fp32) {
-    double t = 0.0, ab = 0.0;
+    double t = 0.0, ab = 0.0, nuf = 0.0;
     for (int k = a; k < b; ++k) {
       int nuc = s_tabs.mat_nuc[k];
-      Micro m = micro_xs64(nuc, i_log, E);
+      Micro m = micro_xs64(nuc, i_log, E, fiss);
       h = h * 31u + static_cast<uint32_t>(m.i_grid);
       double dens = s_tabs.mat_dens[k];
       t += dens * m.total;
       ab += dens * m.absorption;
+      if (fiss) nuf += dens * m.nu_fission;
     }
     tot = t;
     abs_ = ab;
+    if (fiss) *nf = nuf;
   } else {
-    float t = 0.0f, ab = 0.0f;
+    float t = 0.0f, ab = 0.0f, nuf = 0.0f;
     for (int k = a; k < b; ++k) {
       int nuc = s_tabs.mat_nuc[k];
-      float mt, ma, f32;
+      float mt, ma, f32, mnf = 0.0f;
       int ig;
-      micro_xs32(nuc, i_log, E, mt, ma, ig, f32);
+      micro_xs32(nuc, i_log, E, mt, ma, ig, f32, fiss ? &mnf : nullptr);
       h = h * 31u + static_cast<uint32_t>(ig);
       float dens = s_tabs.mat_dens32[k];
       t += dens * mt;
       ab += dens * ma;
+      nuf += dens * mnf;
     }
     tot = fpi::to_double(t);
     abs_ = fpi::to_double(ab);
+    if (fiss) *nf = fpi::to_double(nuf);
   }
   return h;
 }

@@ -75,7 +75,7 @@ void read_nuclide_file(const std::string& path, HNuclide& nuc)
     return v;
   };
   uint32_t version = u32();
-  if (version != 1) throw std::runtime_error(path + ": unsupported nuclide file version");
+  if (version != 1 && version != 2) throw std::runtime_error(path + ": unsupported nuclide file version");
   uint32_t nl = u32();
   off += nl;
   f64();  // A
@@ -86,7 +86,7 @@ void read_nuclide_file(const std::string& path, HNuclide& nuc)
   nuc.energy.resize(G);
   std::memcpy(nuc.energy.data(), b.data() + off, 8 * G);
   off += 8 * size_t(G);
-  std::vector<double> el, cap;
+  std::vector<double> el, fis, cap;
   for (uint32_t r = 0; r < nrx; ++r) {
     uint32_t mt = u32(), thr = u32(), n = u32();
     if (thr != 0 || n != G) throw std::runtime_error(path + ": threshold reactions are not supported");
@@ -94,18 +94,49 @@ void read_nuclide_file(const std::string& path, HNuclide& nuc)
     std::memcpy(xs.data(), b.data() + off, 8 * size_t(n));
     off += 8 * size_t(n);
     if (mt == 2) el = std::move(xs);
+    else if (mt == 18) fis = std::move(xs);
     else if (mt == 102) cap = std::move(xs);
-    else throw std::runtime_error(path + ": only MT 2 and MT 102 are supported");
+    else throw std::runtime_error(path + ": only MT 2, MT 18 and MT 102 are supported");
   }
   if (el.empty() || cap.empty()) throw std::runtime_error(path + ": needs MT 2 and MT 102");
-  // src/nuclide.cpp:359-453: total and absorption start at zero; MT 2 then
-  // MT 102 are added (reaction groups are read in name order).
+  if (version >= 2 && u32() != 0) {
+    nuc.fissionable = true;
+    nuc.nu_c[0] = f64();
+    nuc.nu_c[1] = f64();
+    nuc.spectrum = static_cast<int>(u32());
+    nuc.sp[0] = f64();
+    nuc.sp[1] = f64();
+    nuc.u = f64();
+    if (nuc.spectrum != 1 && nuc.spectrum != 2) throw std::runtime_error(path + ": unknown fission spectrum");
+  }
+  if (nuc.fissionable != !fis.empty()) throw std::runtime_error(path + ": MT 18 needs its fission neutron data");
+  // src/nuclide.cpp:359-453: total and absorption start at zero; the
+  // reactions are added in name (MT) order: MT 2 to total; MT 18 to total,
+  // fission and absorption; MT 102 (disappearance) to total and absorption;
+  // then nu_fission = nu(E) x fission per grid point (Polynomial, Horner in
+  // increasing powers, src/endf.cpp:125-134)
   nuc.total.assign(G, 0.0);
   nuc.absorption.assign(G, 0.0);
+  nuc.fission.assign(G, 0.0);
+  nuc.nu_fission.assign(G, 0.0);
   for (uint32_t k = 0; k < G; ++k) nuc.total[k] += el[k];
+  if (!fis.empty()) {
+    for (uint32_t k = 0; k < G; ++k) {
+      nuc.total[k] += fis[k];
+      nuc.fission[k] += fis[k];
+      nuc.absorption[k] += fis[k];
+    }
+  }
   for (uint32_t k = 0; k < G; ++k) {
     nuc.total[k] += cap[k];
     nuc.absorption[k] += cap[k];
+  }
+  if (!fis.empty()) {
+    for (uint32_t k = 0; k < G; ++k) {
+      double y = 0.0;
+      for (int c = 1; c >= 0; --c) y = y * nuc.energy[k] + nuc.nu_c[c];
+      nuc.nu_fission[k] = y * nuc.fission[k];
+    }
   }
   nuc.elastic = std::move(el);
 }
@@ -447,8 +478,12 @@ void load_model(const std::string& path_in, HModel& m)
   m.root_universe = univ_index[roots[0]];
 
   // -------------------------------------------------------------- settings
-  std::string mode = set->value_or("run_mode", "fixed source");
-  if (mode != "fixed source") throw std::runtime_error("run mode '" + mode + "' is not supported (fixed source only)");
+  std::string mode = XmlNode::trim(set->value_or("run_mode", "fixed source"));
+  if (mode != "fixed source" && mode != "eigenvalue")
+    throw std::runtime_error("run mode '" + mode + "' is not supported (fixed source and eigenvalue)");
+  m.eigenvalue = mode == "eigenvalue";
+  if (std::stoi(set->value_or("generations_per_batch", "1")) != 1)
+    throw std::runtime_error("one generation per batch is supported");
   m.n_particles = std::stoll(set->value("particles"));
   m.n_batches = std::stoi(set->value("batches"));
   m.n_inactive = std::stoi(set->value_or("inactive", "0"));

@@ -73,7 +73,16 @@ struct HNuclide {
   double awr, kT;
   std::vector<double> energy;
   std::vector<double> total, absorption, elastic;  // create_derived columns + MT2
+  std::vector<double> fission, nu_fission;         // create_derived columns (zero without MT 18)
   std::vector<int> grid_index;                     // [M+1]
+  // MT 18 prompt neutron product: yield polynomial (increasing powers of E),
+  // spectrum 1 Maxwell (sp[0] = theta) or 2 Watt (sp = a, b), restriction
+  // energy u; isotropic emission
+  bool fissionable = false;
+  double nu_c[2] = {0.0, 0.0};
+  int spectrum = 0;
+  double sp[2] = {0.0, 0.0};
+  double u = 0.0;
 };
 
 struct HMaterial {
@@ -130,6 +139,7 @@ struct HModel {
   int max_lost_particles = 10;
   double rel_max_lost_particles = 1.0e-6;
   int xs_precision = 64;  // 64 or 32 (FP32 tables)
+  bool eigenvalue = false;  // run_mode eigenvalue (one generation per batch)
 
   std::vector<HNuclide> nuclides;
   std::vector<HMaterial> materials;

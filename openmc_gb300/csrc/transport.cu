@@ -713,7 +713,7 @@ __device__ void initialize_history(long long s, long long index_source)
   db.material_last[s] = C_NONE;
   db.n_collision[s] = 0;
   db.rx[s] = r[0]; db.ry[s] = r[1]; db.rz[s] = r[2];
-  db.ux[s] = u[0]; db.uy[s] = u[1]; db.uz[s] = u[2];
+  set_direction(s, u[0], u[1], u[2]);
   db.E[s] = E;
   double wgt = 1.0;
   db.id[s] = index_source;
@@ -729,6 +729,10 @@ __device__ void initialize_history(long long s, long long index_source)
   db.seed[s] = tseed;
   atomicAdd(&dq.cnt->total_weight, wgt);
   db.n_total[s] = 0;
+  if (dm.eigen) {
+    db.k_col[s] = db.k_abs[s] = db.k_tra[s] = 0.0;
+    db.n_progeny[s] = 0;
+  }
   if (traced(index_source)) dq.trace_n[index_source - dq.trace_first] = 0;
 }
 
@@ -753,7 +757,7 @@ __device__ void start_split_site(long long s, const DSplitSite& d)
   db.material_last[s] = C_NONE;
   db.n_collision[s] = 0;
   db.rx[s] = d.r[0]; db.ry[s] = d.r[1]; db.rz[s] = d.r[2];
-  db.ux[s] = d.u[0]; db.uy[s] = d.u[1]; db.uz[s] = d.u[2];
+  set_direction(s, d.u[0], d.u[1], d.u[2]);
   db.E[s] = d.E;
   db.wgt[s] = d.wgt;
   db.id[s] = d.id;
@@ -784,6 +788,14 @@ __device__ bool revive_or_free(long long s, double wgt)
     unsigned long long key = (static_cast<unsigned long long>(db.n_total[s]) << 34) |
                              static_cast<unsigned long long>(db.id[s]);
     atomicMax(&dq.cnt->longest, key);
+    if (dm.eigen) {
+      // event_death (src/particle.cpp:475-512): the history's k-effective
+      // scores into the generation's sums, its progeny count for the sort
+      atomicAdd(&dq.cnt->k_abs, db.k_abs[s]);
+      atomicAdd(&dq.cnt->k_col, db.k_col[s]);
+      atomicAdd(&dq.cnt->k_tra, db.k_tra[s]);
+      dq.progeny[db.id[s] - 1] = db.n_progeny[s];
+    }
     if (!dq.history) {
       int k = atomicAdd(&dq.cnt->n_free, 1);
       dq.free_list[k] = static_cast<int>(s);
@@ -809,7 +821,7 @@ __device__ bool revive_or_free(long long s, double wgt)
   db.n_collision[s] = 0;
   db.wgt[s] = site.wgt;
   db.rx[s] = site.r[0]; db.ry[s] = site.r[1]; db.rz[s] = site.r[2];
-  db.ux[s] = site.u[0]; db.uy[s] = site.u[1]; db.uz[s] = site.u[2];
+  set_direction(s, site.u[0], site.u[1], site.u[2]);
   db.E[s] = site.E;
   db.n_event[s] = 0;
   // the revived entry joins the slot's free chain
@@ -825,6 +837,8 @@ __device__ bool revive_or_free(long long s, double wgt)
 // small, latency-bound launches every iteration.
 __global__ void __launch_bounds__(256) k_source_bank()
 {
+  // an eigenvalue run's later generations start from the combed fission bank
+  if (dq.src_from_bank) return;
   tables_enter();
   const long long n = dq.src_n;
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
@@ -866,6 +880,9 @@ __global__ void k_batch_init(int batch)
     c->more = 1;
     c->tail = 0;
     c->longest = 0;
+    c->n_fission = 0;
+    c->fbank_full = 0;
+    c->k_col = c->k_abs = c->k_tra = 0.0;
   }
   (void)batch;
 }
@@ -908,16 +925,18 @@ __device__ void ev_xs(long long s, EvStats& st)
   double E = db.E[s];
   if (material != C_NONE) {
     if (material != material_last || tr) {
-      double t, a;
-      h = material_xs(material, E, t, a);
+      double t, a, nf = 0.0;
+      h = material_xs(material, E, t, a, dm.eigen ? &nf : nullptr);
       db.macro_t[s] = t;
       db.macro_a[s] = a;
+      if (dm.eigen) db.macro_nf[s] = nf;
       st.calc += 1;
       st.nuc += s_tabs.mat_off[material + 1] - s_tabs.mat_off[material];
     }
   } else {
     db.macro_t[s] = 0.0;
     db.macro_a[s] = 0.0;
+    if (dm.eigen) db.macro_nf[s] = 0.0;
   }
   if (tr) {
     TraceRec* rec = trace_slot(pid);
@@ -970,13 +989,14 @@ __device__ int ev_advance(long long s, EvStats& st, int qi = 0)
   int bs, bl, bt;
   bool neg_lat = false;
   // FP32-table mode: reciprocal direction shared by the lattice and mesh
-  // distances (FP64 products in place of FP64 quotients)
+  // distances (FP64 products in place of FP64 quotients), kept with the
+  // direction in the bank
   double inv_u[3];
   const bool recip = dm.xs_fp32 != 0;
   if (recip) {
-    inv_u[0] = 1.0 / g.u[0];
-    inv_u[1] = 1.0 / g.u[1];
-    inv_u[2] = 1.0 / g.u[2];
+    inv_u[0] = db.iux[s];
+    inv_u[1] = db.iuy[s];
+    inv_u[2] = db.iuz[s];
   }
   distance_to_boundary(g, bd, bs, bl, bt, neg_lat, recip ? inv_u : nullptr);
   if (neg_lat) mark_lost(s);
@@ -994,6 +1014,8 @@ __device__ int ev_advance(long long s, EvStats& st, int qi = 0)
     g.r[l][1] = g.r[l][1] + distance * g.u[1];
     g.r[l][2] = g.r[l][2] + distance * g.u[2];
   }
+  // track-length estimate of k-effective (src/particle.cpp:272-275)
+  if (dm.eigen) db.k_tra[s] += wgt * distance * db.macro_nf[s];
   if (defer && dq.trk.w) {
     const DTracks& T = dq.trk;
     T.r0x[qi] = r0[0];
@@ -1059,8 +1081,11 @@ __device__ int ev_advance(long long s, EvStats& st, int qi = 0)
   return revive_or_free(s, wgt) ? NEXT_XS : NEXT_DEAD;
 }
 
-// src/geometry.cpp:301-357
-__device__ void cross_lattice(Geo& g, long long s, int trans)
+// src/geometry.cpp:301-357 cross_lattice up to its cell search: the lattice
+// index moves by the translation, the local position is recomputed, and
+// the universe of the new lattice element is looked up.  Returns whether
+// the new index lies inside the lattice.
+__device__ bool lattice_step(Geo& g, int trans)
 {
   const int lvl_rt = g.n_coord - 1;  // a lattice level is never the root
   bool valid = false;
@@ -1083,20 +1108,18 @@ __device__ void cross_lattice(Geo& g, long long s, int trans)
       g.cell[lvl] = C_NONE;
     }
   }
-  bool lost_outer = false;
-  if (!valid) {
-    g.n_coord = 1;
-    if (!exhaustive_find_cell(g, lost_outer)) mark_lost(s);
-  } else if (!exhaustive_find_cell(g, lost_outer)) {
-    g.n_coord = 1;
-    if (!exhaustive_find_cell(g, lost_outer)) mark_lost(s);
-  }
+  return valid;
 }
 
 // src/particle.cpp:288-329, 549-710 event_cross_surface (+ revive)
 // The crossing itself on a particle state already held in registers (g, at
 // the boundary), with the boundary the advance found: signed surface bsurf,
-// lattice translation trans and coordinate level blevel.
+// lattice translation trans and coordinate level blevel.  A lattice
+// crossing (src/geometry.cpp:301-357), a reflection (src/particle.cpp:
+// 657-710) and a transmission through a surface (src/particle.cpp:600-629)
+// each prepare the state their own way and then run one shared cell search
+// from the crossing level (so that the lanes of a warp take it together);
+// each keeps its own fallbacks when that search fails.
 __device__ int ev_surface_g(long long s, EvStats& st, Geo& g, double wgt, int bsurf, int trans, int blevel)
 {
   st.surf += 1;
@@ -1104,9 +1127,23 @@ __device__ int ev_surface_g(long long s, EvStats& st, Geo& g, double wgt, int bs
   g.surface = bsurf;
   g.n_coord = blevel;
   bool lost_outer = false;
+  enum { NONE, LATTICE, REFLECT, TRANSMIT };
+  int path = NONE;
   if (trans != 13) {
-    cross_lattice(g, s, trans);
-    wgt = db.wgt[s];
+    if (!lattice_step(g, trans)) {
+      g.n_coord = 1;
+      if (!exhaustive_find_cell(g, lost_outer)) {
+        mark_lost(s);
+        wgt = 0.0;
+      }
+    } else {
+      path = LATTICE;
+      // exhaustive_find_cell from the new element (src/geometry.cpp:284-298)
+      if (lvl_get(g.univ, g.n_coord - 1) == C_NONE) {
+        g.univ[0] = dm.root_univ;
+        g.n_coord = 1;
+      }
+    }
   } else if (g.surface == SURFACE_NONE || abs(g.surface) > dm.n_surf) {
     mark_lost(s);
     wgt = 0.0;
@@ -1137,19 +1174,27 @@ __device__ int ev_surface_g(long long s, EvStats& st, Geo& g, double wgt, int bs
         wgt = 0.0;
       } else {
         g.u[0] = ux; g.u[1] = uy; g.u[2] = uz;
+        set_direction(s, ux, uy, uz);  // geo_store writes u again below
         g.cell[0] = db.cell_last0[s];
         g.surface = -g.surface;
         g.n_coord = 1;
-        if (!find_cell_inner(g, lost_outer)) {
-          mark_lost(s);
-          wgt = 0.0;
-        }
+        path = REFLECT;
       }
     } else {
-      // neighbour search at the crossing level, then from the root
-      if (!find_cell_inner(g, lost_outer)) {
-        g.n_coord = 1;
-        if (!exhaustive_find_cell(g, lost_outer)) {
+      path = TRANSMIT;  // neighbour search at the crossing level, then from the root
+    }
+  }
+  if (path != NONE && !find_cell_inner(g, lost_outer)) {
+    if (path == REFLECT) {
+      mark_lost(s);
+      wgt = 0.0;
+    } else {
+      g.n_coord = 1;
+      if (!exhaustive_find_cell(g, lost_outer)) {
+        if (path == LATTICE) {
+          mark_lost(s);
+          wgt = 0.0;
+        } else {
           g.surface = SURFACE_NONE;
           g.n_coord = 1;
           g.r[0][0] = g.r[0][0] + TINY_BIT * g.u[0];
@@ -1316,6 +1361,58 @@ __device__ void elastic_scatter(int nuc, double& E, double* u, unsigned long lon
   }
 }
 
+// src/physics.cpp:1043-1115 sample_fission_neutron for a prompt-only MT 18
+// (no delayed neutrons: the delayed test draws one number and never
+// passes) with isotropic emission and a Maxwell or Watt spectrum with
+// restriction energy (src/distribution_energy.cpp:282-360); energies at or
+// above the data's maximum are resampled.  Then src/physics.cpp:170-285
+// create_fission_sites: nu_t = wgt / keff x nu_fission / total of the
+// sampled nuclide, each site appended to the generation's fission bank with
+// the parent's source index and progeny number (the bank is put in (parent,
+// progeny) order after the generation).  A full bank sets an error flag and
+// banks no more sites of this particle.
+__device__ void create_fission_sites(long long s, int nuc, double wgt, double E_in, const double* u_in,
+  double m_nf, double m_tot, unsigned long long& seed)
+{
+  const double weight = 1.0;
+  const double nu_t = wgt / dm.keff * weight * m_nf / m_tot;
+  int nu = static_cast<int>(nu_t);
+  if (fpi::le(prn(seed), nu_t - fpi::to_double(nu))) ++nu;
+  if (nu == 0) return;
+  const DFission& F = dm.fis[nuc];
+  const double nu_tot = F.nu1 * E_in + F.nu0;  // Horner over (nu0, nu1); the first step 0 E + nu1 is exact
+  const double beta = 0.0 / nu_tot;
+  for (int k = 0; k < nu; ++k) {
+    if (prn(seed) < beta) break;  // never: no delayed neutron data
+    double mu = 0.0, E_out = 0.0;
+    for (int n_sample = 0; n_sample < 10000; ++n_sample) {
+      mu = uniform_distribution(-1., 1., seed);
+      for (int tries = 0; tries < 1000000; ++tries) {
+        E_out = F.spectrum == 1 ? maxwell_spectrum(F.p0, seed) : watt_spectrum(F.p0, F.p1, seed);
+        if (fpi::le(E_out, E_in - F.u)) break;
+      }
+      if (fpi::lt(E_out, dm.e_max_neutron)) break;
+    }
+    double uo[3] = {u_in[0], u_in[1], u_in[2]};
+    rotate_angle(uo[0], uo[1], uo[2], mu, seed);
+    const unsigned long long idx = atomicAdd(&dq.cnt->n_fission, 1ull);
+    if (idx >= static_cast<unsigned long long>(dq.fbank_cap)) {
+      atomicExch(&dq.cnt->fbank_full, 1);
+      return;
+    }
+    DFissionSite& site = dq.fbank[idx];
+    site.r[0] = db.rx[s];
+    site.r[1] = db.ry[s];
+    site.r[2] = db.rz[s];
+    site.u[0] = uo[0];
+    site.u[1] = uo[1];
+    site.u[2] = uo[2];
+    site.E = E_out;
+    site.parent = db.id[s];
+    site.progeny = db.n_progeny[s]++;
+  }
+}
+
 // src/particle.cpp:331-415 + src/physics.cpp:43-168, 494-518, 638-752
 __device__ int ev_collision(long long s, EvStats& st)
 {
@@ -1326,6 +1423,8 @@ __device__ int ev_collision(long long s, EvStats& st)
   unsigned long long seed = db.seed[s];
   int mat = db.material[s];
   double mt = db.macro_t[s];
+  // collision estimate of k-effective (src/particle.cpp:333-337)
+  if (dm.eigen) db.k_col[s] += wgt * db.macro_nf[s] / mt;
   db.surface[s] = SURFACE_NONE;
   db.n_collision[s] += 1;
   // sample_nuclide: CDF over atom_density * micro total in material order
@@ -1338,17 +1437,23 @@ __device__ int ev_collision(long long s, EvStats& st)
   int i_log = log_union_index(E);
   int chosen = -1;
   double m_tot = 0, m_abs = 0;
+  // the sampled nuclide's fission and nu-fission (eigenvalue runs; FP32
+  // tables carry nu-fission only, whose sign is the fission cross section's)
+  double m_fis = 0, m_nf = 0;
+  const bool eig = dm.eigen != 0;
   if (!dm.xs_fp32) {
     double prob = 0.0;
     for (int k = a; k < b; ++k) {
       int nuc = s_tabs.mat_nuc[k];
       st.coll_nuc += 1;
-      Micro m = micro_xs64(nuc, i_log, E);
+      Micro m = micro_xs64(nuc, i_log, E, eig);
       prob += s_tabs.mat_dens[k] * m.total;
       if (fpi::le(cutoff, prob)) {
         chosen = nuc;
         m_tot = m.total;
         m_abs = m.absorption;
+        m_fis = m.fission;
+        m_nf = m.nu_fission;
         break;
       }
     }
@@ -1357,14 +1462,16 @@ __device__ int ev_collision(long long s, EvStats& st)
     for (int k = a; k < b; ++k) {
       int nuc = s_tabs.mat_nuc[k];
       st.coll_nuc += 1;
-      float t, ab, f32;
+      float t, ab, f32, nf = 0.0f;
       int ig;
-      micro_xs32(nuc, i_log, E, t, ab, ig, f32);
+      micro_xs32(nuc, i_log, E, t, ab, ig, f32, eig ? &nf : nullptr);
       prob += s_tabs.mat_dens32[k] * t;
       if (fpi::le(cutoff, fpi::to_double(prob))) {
         chosen = nuc;
         m_tot = fpi::to_double(t);
         m_abs = fpi::to_double(ab);
+        m_nf = fpi::to_double(nf);
+        m_fis = m_nf;
         break;
       }
     }
@@ -1374,9 +1481,16 @@ __device__ int ev_collision(long long s, EvStats& st)
     set_error(ERR_NO_NUCLIDE);
     wgt = 0.0;
   } else {
-    // absorption (analog) src/physics.cpp:638-672
+    // fission sites (src/physics.cpp:107-127; sample_fission returns the only
+    // fission reaction without a random number)
+    if (eig && fpi::pos(m_fis)) create_fission_sites(s, chosen, wgt, E, u, m_nf, m_tot, seed);
+    // absorption (analog) src/physics.cpp:638-672, with the absorption
+    // estimate of k-effective
     if (fpi::pos(m_abs)) {
-      if (fpi::lt(prn(seed) * m_tot, m_abs)) wgt = 0.0;
+      if (fpi::lt(prn(seed) * m_tot, m_abs)) {
+        if (eig) db.k_abs[s] += wgt * m_nf / m_abs;
+        wgt = 0.0;
+      }
     }
     if (!fpi::zero(wgt)) {
       // scatter src/physics.cpp:674-752: the reaction cutoff is drawn; the
@@ -1404,7 +1518,7 @@ __device__ int ev_collision(long long s, EvStats& st)
   db.E[s] = E;
   db.wgt[s] = wgt;
   db.seed[s] = seed;
-  db.ux[s] = u[0]; db.uy[s] = u[1]; db.uz[s] = u[2];
+  set_direction(s, u[0], u[1], u[2]);
   db.material_last[s] = C_NONE;
   long long pid = db.id[s];
   if (traced(pid)) {
@@ -1901,6 +2015,9 @@ struct GpuSim {
   long long ww_size = 0;
   unsigned long long* d_group_max = nullptr;  // MAGIC update: per-group maxima
   int n_group_max = 0;
+  // eigenvalue run: fission-bank permutation (sorted position -> append
+  // position), per-history offsets, comb indices
+  int *d_perm = nullptr, *d_offset = nullptr, *d_comb = nullptr;
 
   ~GpuSim()
   {
@@ -1983,14 +2100,16 @@ static void build_model(GpuSim& G, const HModel& m, const GpuOptions& opt)
   std::vector<XsRow64> xs64;
   std::vector<float4> xs32;
   std::vector<int> grid_index;
+  std::vector<DFission> fis;
   for (const auto& n : m.nuclides) {
     energy.insert(energy.end(), n.energy.begin(), n.energy.end());
     for (size_t k = 0; k < n.energy.size(); ++k) {
-      xs64.push_back(XsRow64 {n.total[k], n.absorption[k], n.elastic[k], 0.0});
+      xs64.push_back(XsRow64 {n.total[k], n.absorption[k], n.fission[k], n.nu_fission[k]});
       const double de = k + 1 < n.energy.size() ? n.energy[k + 1] - n.energy[k] : 0.0;
       xs32.push_back(make_float4(static_cast<float>(n.total[k]), static_cast<float>(n.absorption[k]),
-        static_cast<float>(n.elastic[k]), de > 0.0 ? static_cast<float>(1.0 / de) : 0.0f));
+        static_cast<float>(n.nu_fission[k]), de > 0.0 ? static_cast<float>(1.0 / de) : 0.0f));
     }
+    fis.push_back(DFission {n.nu_c[0], n.nu_c[1], n.sp[0], n.sp[1], n.u, n.spectrum, 0});
     nuc_off.push_back(static_cast<long long>(energy.size()));
     grid_index.insert(grid_index.end(), n.grid_index.begin(), n.grid_index.end());
     awr.push_back(n.awr);
@@ -2004,6 +2123,10 @@ static void build_model(GpuSim& G, const HModel& m, const GpuOptions& opt)
   d.grid_index = dev_upload(grid_index, own);
   d.awr = dev_upload(awr, own);
   d.kT = dev_upload(kT, own);
+  d.fis = dev_upload(fis, own);
+  d.eigen = m.eigenvalue ? 1 : 0;
+  d.keff = 1.0;  // simulation::keff before the first generation
+  d.e_max_neutron = m.energy_max;
   std::vector<int> mat_off {0}, mat_nuc, mat_id;
   std::vector<double> mat_dens;
   std::vector<float> mat_dens32;
@@ -2203,6 +2326,12 @@ static void build_bank(GpuSim& G, long long cap, long long sec_cap)
   b.ux = dev_alloc<double>(cap, own);
   b.uy = dev_alloc<double>(cap, own);
   b.uz = dev_alloc<double>(cap, own);
+  b.iux = b.iuy = b.iuz = nullptr;
+  if (G.model.xs_fp32) {
+    b.iux = dev_alloc<double>(cap, own);
+    b.iuy = dev_alloc<double>(cap, own);
+    b.iuz = dev_alloc<double>(cap, own);
+  }
   b.rx = dev_alloc<double>(cap * MAXL, own);
   b.ry = dev_alloc<double>(cap * MAXL, own);
   b.rz = dev_alloc<double>(cap * MAXL, own);
@@ -2220,6 +2349,15 @@ static void build_bank(GpuSim& G, long long cap, long long sec_cap)
   b.material_last = dev_alloc<int>(cap, own);
   b.macro_t = dev_alloc<double>(cap, own);
   b.macro_a = dev_alloc<double>(cap, own);
+  b.macro_nf = b.k_col = b.k_abs = b.k_tra = nullptr;
+  b.n_progeny = nullptr;
+  if (G.model.eigen) {
+    b.macro_nf = dev_alloc<double>(cap, own);
+    b.k_col = dev_alloc<double>(cap, own);
+    b.k_abs = dev_alloc<double>(cap, own);
+    b.k_tra = dev_alloc<double>(cap, own);
+    b.n_progeny = dev_alloc<int>(cap, own);
+  }
   b.bsurf = dev_alloc<int>(cap, own);
   b.blevel = dev_alloc<int>(cap, own);
   b.btrans = dev_alloc<int>(cap, own);
@@ -2272,6 +2410,23 @@ static void build_bank(GpuSim& G, long long cap, long long sec_cap)
     }
     if (G.model.trk_mat) T.mat = dev_alloc<int>(cap, own);
     if (G.model.trk_cells) T.cell = dev_alloc<int>(cap * MAXL, own);
+  }
+  // eigenvalue run: fission bank of 3 sites per history (the reference's
+  // fission_bank capacity, src/simulation.cpp:323-330), the per-history
+  // progeny counts, and the permutation / comb index arrays of the bank's
+  // sort and resampling
+  q.fbank = nullptr;
+  q.fbank_cap = 0;
+  q.progeny = nullptr;
+  q.src_from_bank = 0;
+  if (G.model.eigen) {
+    if (q.src_n != G.model.n_particles) throw std::runtime_error("eigenvalue runs need at most 2^27 particles per batch");
+    q.fbank_cap = 3 * G.model.n_particles;
+    q.fbank = dev_alloc<DFissionSite>(q.fbank_cap, own);
+    q.progeny = dev_alloc<int>(G.model.n_particles, own);
+    G.d_perm = dev_alloc<int>(q.fbank_cap, own);
+    G.d_offset = dev_alloc<int>(G.model.n_particles, own);
+    G.d_comb = dev_alloc<int>(G.model.n_particles, own);
   }
   G.cnt = dev_alloc<DCounters>(1, own);
   q.cnt = G.cnt;
@@ -2460,6 +2615,13 @@ static void accumulate_batch(GpuSim* G, HModel& m)
   G->tallies_dirty = true;
 }
 
+// An inactive batch's tally scores are dropped (the reference does not
+// score inactive tallies, src/simulation.cpp:387-396).
+static void discard_batch(GpuSim* G)
+{
+  if (G->n_values > 0) CK(cudaMemsetAsync(G->d_value, 0, sizeof(double) * G->n_values, G->stream));
+}
+
 static void launch_history_batch(GpuSim* G, int batch)
 {
   const int nb = G->blocks, nt = 256;
@@ -2485,6 +2647,7 @@ BatchStats gpu_run_batch(GpuSim* G, HModel& m, int batch, bool accumulate)
   CK(cudaEventElapsedTime(&st.ms, G->ev0, G->ev1));
   fill_stats(c, st);
   if (accumulate) accumulate_batch(G, m);
+  else discard_batch(G);
   CK(cudaStreamSynchronize(G->stream));
   return st;
 }
@@ -2596,6 +2759,7 @@ BatchStats gpu_run_batch_profiled(GpuSim* G, HModel& m, int batch, bool accumula
   fill_stats(c, st);
   for (auto& e : ev) cudaEventDestroy(e);
   if (accumulate) accumulate_batch(G, m);
+  else discard_batch(G);
   CK(cudaStreamSynchronize(S));
   return st;
 }
@@ -2721,6 +2885,135 @@ void gpu_update_magic(GpuSim* G, const MagicArgs& a, double* lower, double* uppe
   CK(cudaMemcpyAsync(lower, G->d_ww_lower, sizeof(double) * n, cudaMemcpyDeviceToHost, G->stream));
   CK(cudaMemcpyAsync(upper, G->d_ww_upper, sizeof(double) * n, cudaMemcpyDeviceToHost, G->stream));
   CK(cudaStreamSynchronize(G->stream));
+}
+
+// ------------------------------------------------ eigenvalue generations
+// src/bank.cpp:83-88: exclusive scan of the per-history progeny counts (one
+// block; n is at most 2^27)
+__global__ void __launch_bounds__(1024) k_eig_scan(const int* progeny, int* offset, long long n)
+{
+  __shared__ int wsum[32];
+  __shared__ long long carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (long long base = 0; base < n; base += blockDim.x) {
+    const long long i = base + threadIdx.x;
+    const int v = i < n ? progeny[i] : 0;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    if (w == 0) {
+      int t = lane < static_cast<int>(blockDim.x >> 5) ? wsum[lane] : 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, t, o);
+        if (lane >= o) t += y;
+      }
+      wsum[lane] = t;
+    }
+    __syncthreads();
+    const long long incl = x + (w > 0 ? wsum[w - 1] : 0) + carry;
+    if (i < n) offset[i] = static_cast<int>(incl - v);
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = incl;
+    __syncthreads();
+  }
+}
+
+// src/bank.cpp:111-125: the sorted position of each appended site is its
+// parent's offset plus its progeny number; perm maps sorted -> appended
+__global__ void k_eig_place(const DFissionSite* bank, long long n_sites, const int* offset, int* perm)
+{
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n_sites;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const DFissionSite& site = bank[i];
+    const long long pos = static_cast<long long>(offset[site.parent - 1]) + site.progeny;
+    if (pos < 0 || pos >= n_sites) {
+      set_error(ERR_BANK);  // progeny counts and bank disagree
+      continue;
+    }
+    perm[pos] = static_cast<int>(i);
+  }
+}
+
+// The combed sites (sorted positions comb[k]) become the source sites of
+// generation `batch` (src/eigenvalue.cpp:351-356 copy into the source
+// bank), each with the tracking seed of its history id (initialize_history,
+// src/simulation.cpp:613-616)
+__global__ void k_eig_gather(const DFissionSite* bank, const int* perm, const int* comb, long long n, int batch,
+                             SourceSite* src)
+{
+  for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < n;
+       k += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const DFissionSite& site = bank[perm[comb[k]]];
+    SourceSite out;
+    for (int j = 0; j < 3; ++j) {
+      out.r[j] = site.r[j];
+      out.u[j] = site.u[j];
+    }
+    out.E = site.E;
+    const long long id = static_cast<long long>(batch - 1) * n + k + 1;
+    out.tseed = future_seed(static_cast<unsigned long long>(id) * dm.stride,
+                            static_cast<unsigned long long>(dm.master_seed + 0));
+    src[k] = out;
+  }
+}
+
+GenerationStats gpu_finish_generation(GpuSim* G, int batch)
+{
+  GenerationStats out;
+  if (!G->model.eigen) return out;
+  DCounters c {};
+  CK(cudaMemcpyAsync(&c, G->cnt, sizeof(c), cudaMemcpyDeviceToHost, G->stream));
+  CK(cudaStreamSynchronize(G->stream));
+  if (c.fbank_full) throw std::runtime_error("The shared fission bank is full.");
+  out.fission_sites = static_cast<long long>(c.n_fission);
+  out.k_col = c.k_col;
+  out.k_abs = c.k_abs;
+  out.k_tra = c.k_tra;
+  out.total_weight = c.total_weight;
+  if (out.fission_sites == 0) throw std::runtime_error("No fission sites banked on MPI rank 0");
+  const long long n = G->model.n_particles;
+  k_eig_scan<<<1, 1024, 0, G->stream>>>(G->queues.progeny, G->d_offset, n);
+  k_eig_place<<<G->blocks, 256, 0, G->stream>>>(G->queues.fbank, out.fission_sites, G->d_offset, G->d_perm);
+  // src/eigenvalue.cpp:135-174 uniform combing on one rank, the teeth
+  // positions accumulated in the reference's order
+  unsigned long long seed = future_seed(static_cast<unsigned long long>(batch) * G->model.stride,
+                                        static_cast<unsigned long long>(G->model.master_seed + 0));
+  const long long total = out.fission_sites;
+  const double teeth_distance = static_cast<double>(total) / n;
+  const double teeth_offset = std::ldexp(static_cast<double>(prn_word(seed)), -64) * teeth_distance;
+  const long long tooth_start = static_cast<long long>(std::ceil((0 - teeth_offset) / teeth_distance));
+  const long long tooth_end = static_cast<long long>(std::floor((total - teeth_offset) / teeth_distance)) + 1;
+  std::vector<int> comb;
+  comb.reserve(n);
+  double tooth = tooth_start * teeth_distance + teeth_offset;
+  for (long long i = tooth_start; i < tooth_end && static_cast<long long>(comb.size()) < n; i++) {
+    const long long idx = static_cast<long long>(std::floor(tooth));
+    if (idx < 0 || idx >= total) throw std::runtime_error("comb tooth outside the fission bank");
+    comb.push_back(static_cast<int>(idx));
+    tooth += teeth_distance;
+  }
+  if (static_cast<long long>(comb.size()) < n) throw std::runtime_error("the comb selected fewer sites than particles");
+  CK(cudaMemcpyAsync(G->d_comb, comb.data(), sizeof(int) * n, cudaMemcpyHostToDevice, G->stream));
+  k_eig_gather<<<G->blocks, 256, 0, G->stream>>>(G->queues.fbank, G->d_perm, G->d_comb, n, batch + 1,
+                                                 G->queues.src_bank);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(&c, G->cnt, sizeof(c), cudaMemcpyDeviceToHost, G->stream));
+  CK(cudaStreamSynchronize(G->stream));
+  if (c.error & ERR_BANK) throw std::runtime_error("Mismatch detected between sum of all particle progeny and shared fission bank size.");
+  G->queues.src_from_bank = 1;
+  return out;
+}
+
+void gpu_set_keff(GpuSim* G, double keff)
+{
+  G->model.keff = keff;
+  CK(cudaMemcpyToSymbol(dm, &G->model, sizeof(DModel)));
 }
 
 void gpu_set_ww_on(GpuSim* G, bool on)

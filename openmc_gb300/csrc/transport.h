@@ -7,7 +7,7 @@ namespace omc {
 
 // device error flags (bitwise OR in the batch counters)
 constexpr int ERR_LOST = 1, ERR_SECONDARY_OVERFLOW = 2, ERR_NO_NUCLIDE = 4,
-              ERR_ITERATIONS = 8, ERR_REJECTION = 16, ERR_TRACE = 32;
+              ERR_ITERATIONS = 8, ERR_REJECTION = 16, ERR_TRACE = 32, ERR_BANK = 64;
 
 struct GpuSim;
 
@@ -39,6 +39,13 @@ struct MagicArgs {
   double volume = 1.0;        // of one mesh element
   int rel_err = 0;            // 1: bounds from 1 / relative error, 0: from the mean
   double threshold = 1.0, ratio = 5.0;
+};
+
+// Bookkeeping of one eigenvalue generation, read after its transport.
+struct GenerationStats {
+  long long fission_sites = 0;
+  double k_col = 0, k_abs = 0, k_tra = 0;  // the generation's k-effective sums
+  double total_weight = 0;
 };
 
 struct BatchStats {
@@ -81,6 +88,8 @@ struct BatchStats {
   void gpu_set_ww_bounds(GpuSim* g, const double* lower, const double* upper, long long n); \
   void gpu_set_ww_on(GpuSim* g, bool on);                                                   \
   void gpu_update_magic(GpuSim* g, const MagicArgs& a, double* lower, double* upper);        \
+  GenerationStats gpu_finish_generation(GpuSim* g, int batch);                               \
+  void gpu_set_keff(GpuSim* g, double keff);                                                 \
   long long gpu_capacity(GpuSim* g);                                                        \
   void gpu_material_xs(GpuSim* g, long long n, const int* mat, const double* E, double* total, \
                        double* absorption, unsigned* grid_hash);                               \
@@ -107,6 +116,14 @@ void gpu_set_ww_on(GpuSim* g, bool on);
 // arrays lower / upper (e_bins x mesh_bins each).
 void gpu_update_magic(GpuSim* g, const MagicArgs& a, double* lower, double* upper);
 long long gpu_capacity(GpuSim* g);
+// Eigenvalue run, after generation `batch`: reads its fission-bank size and
+// k-effective sums, puts the bank in (parent, progeny) order, combs
+// n_particles sites from it (src/eigenvalue.cpp:86-365, the tooth positions
+// accumulated on the host as the reference accumulates them) and writes them
+// as the next generation's source bank.
+GenerationStats gpu_finish_generation(GpuSim* g, int batch);
+// The k-effective the next generation's fission sites are sampled with.
+void gpu_set_keff(GpuSim* g, double keff);
 // Macroscopic total and absorption cross sections (and the nuclide grid-index
 // hash) of the model's materials at (material index, E) pairs, evaluated on
 // the device by the transport kernels' own lookup (host arrays of length n).

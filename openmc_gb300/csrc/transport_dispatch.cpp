@@ -90,6 +90,9 @@ void gpu_update_magic(GpuSim* g, const MagicArgs& a, double* lower, double* uppe
 {
   OMC_FORWARD(gpu_update_magic, a, lower, upper);
 }
+
+GenerationStats gpu_finish_generation(GpuSim* g, int batch) { OMC_FORWARD(gpu_finish_generation, batch); }
+void gpu_set_keff(GpuSim* g, double keff) { OMC_FORWARD(gpu_set_keff, keff); }
 long long gpu_capacity(GpuSim* g) { OMC_FORWARD(gpu_capacity); }
 int gpu_levels(GpuSim* g) { return g ? g->levels : 0; }
 

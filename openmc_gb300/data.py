@@ -21,7 +21,16 @@ n_reactions           uint32
 energy                float64[n_points] (eV, ascending)
 per reaction          uint32 MT, uint32 threshold_idx, uint32 n,
                       float64[n] cross section (barns)
+fission (version 2)   uint32 flag; if 1: float64[2] nu polynomial
+                      coefficients (increasing powers of E, the total
+                      yield of the MT 18 neutron product), uint32
+                      spectrum type (1 Maxwell, 2 Watt), float64[2]
+                      parameters (theta, 0 or a, b; eV, 1/eV), float64
+                      restriction energy U (eV); prompt neutrons only,
+                      isotropic emission
 ====================  ==========================================
+
+Version 1 files (no fission block) are still read.
 
 The generator follows the recipe of the synthetic nuclides this project is
 benchmarked on: a log-uniform grid between 1e-5 eV and 20 MeV with a seeded
@@ -41,23 +50,40 @@ from xml.etree import ElementTree as ET
 import numpy as np
 
 MAGIC = b"OMCGBNUC"
-VERSION = 1
+VERSION = 2
 K_BOLTZMANN = 8.617333262e-5  # eV/K, include/openmc/constants.h:100
 E_MIN = 1.0e-5
 E_MAX = 2.0e7
 MT_ELASTIC = 2
+MT_FISSION = 18
 MT_CAPTURE = 102
+SPECTRUM_MAXWELL = 1
+SPECTRUM_WATT = 2
+
+
+@dataclass
+class Fission:
+    """Prompt fission neutrons of MT 18: yield nu(E) = nu[0] + nu[1] E
+    (Polynomial, src/endf.cpp:125-134), energy from a Maxwell (theta) or
+    Watt (a, b) spectrum with restriction energy U
+    (src/distribution_energy.cpp:282-360), isotropic emission."""
+    nu: tuple = (2.43, 0.0)
+    spectrum: int = SPECTRUM_WATT
+    params: tuple = (0.988e6, 2.249e-6)
+    u: float = -2.0e7
 
 
 @dataclass
 class Nuclide:
-    """One synthetic nuclide at one temperature (MT 2 and MT 102 only)."""
+    """One synthetic nuclide at one temperature (MT 2 and MT 102, and MT 18
+    with its fission neutron data for a fissile nuclide)."""
     name: str
     A: float
     awr: float
     kT: float
     energy: np.ndarray
     reactions: dict = field(default_factory=dict)  # mt -> (threshold_idx, xs)
+    fission: Fission | None = None
 
     @property
     def elastic(self) -> np.ndarray:
@@ -118,8 +144,11 @@ def nuclide_class(A: float) -> str:
 
 def make_nuclide(name: str, A: float, n_points: int, seed: int,
                  kind: str | None = None, n_peaks: int = 20,
-                 temperature: float = 294.0) -> Nuclide:
-    """Build one synthetic nuclide from a seed (deterministic)."""
+                 temperature: float = 294.0, fissile: bool = False) -> Nuclide:
+    """Build one synthetic nuclide from a seed (deterministic).  fissile adds
+    MT 18: a 1/v fission cross section (585 b at 0.0253 eV) plus the
+    resonance peaks times a seeded fission branching, with the default
+    Fission yield and Watt spectrum."""
     rng = np.random.default_rng(seed)
     kind = kind or nuclide_class(A)
     pot, cap_th, height, (b_lo, b_hi) = _CLASSES[kind]
@@ -139,6 +168,28 @@ def make_nuclide(name: str, A: float, n_points: int, seed: int,
                   kT=K_BOLTZMANN * temperature, energy=E)
     nuc.reactions[MT_ELASTIC] = (0, np.ascontiguousarray(elastic, dtype=np.float64))
     nuc.reactions[MT_CAPTURE] = (0, np.ascontiguousarray(capture, dtype=np.float64))
+    if fissile:
+        frac = rng.uniform(0.5, 2.0, n_peaks)
+        fis = 585.0 * np.sqrt(0.0253 / E) + shape @ (h * frac) + 1.0
+        nuc.reactions[MT_FISSION] = (0, np.ascontiguousarray(fis, dtype=np.float64))
+        nuc.fission = Fission()
+    return nuc
+
+
+def make_flat_nuclide(name: str, A: float, n_points: int, seed: int, elastic: float, capture: float,
+                      fission: float = 0.0, nu: float = 2.43, temperature: float = 294.0) -> Nuclide:
+    """A nuclide whose cross sections do not depend on energy (on a seeded
+    log grid): in an infinite homogeneous medium of such nuclides k-infinity
+    is nu Sigma_f / Sigma_a exactly, the known answer the reference's
+    tests/unit_tests/test_temp_interp.py builds the same way."""
+    rng = np.random.default_rng(seed)
+    E = log_grid(n_points, rng)
+    nuc = Nuclide(name=name, A=float(A), awr=awr_of(A), kT=K_BOLTZMANN * temperature, energy=E)
+    nuc.reactions[MT_ELASTIC] = (0, np.full(n_points, float(elastic)))
+    nuc.reactions[MT_CAPTURE] = (0, np.full(n_points, float(capture)))
+    if fission > 0.0:
+        nuc.reactions[MT_FISSION] = (0, np.full(n_points, float(fission)))
+        nuc.fission = Fission(nu=(float(nu), 0.0))
     return nuc
 
 
@@ -157,6 +208,12 @@ def write_nuclide(nuc: Nuclide, path: str | Path) -> None:
             thr, xs = nuc.reactions[mt]
             f.write(struct.pack("<III", mt, thr, len(xs)))
             f.write(np.ascontiguousarray(xs, dtype="<f8").tobytes())
+        fis = nuc.fission
+        f.write(struct.pack("<I", 1 if fis is not None else 0))
+        if fis is not None:
+            f.write(struct.pack("<2d", *fis.nu))
+            f.write(struct.pack("<I", fis.spectrum))
+            f.write(struct.pack("<3d", *fis.params, fis.u))
 
 
 def read_nuclide(path: str | Path) -> Nuclide:
@@ -165,7 +222,7 @@ def read_nuclide(path: str | Path) -> Nuclide:
         raise ValueError(f"{path}: not a nuclide file")
     off = 8
     (version,) = struct.unpack_from("<I", buf, off); off += 4
-    if version != VERSION:
+    if version not in (1, 2):
         raise ValueError(f"{path}: unsupported version {version}")
     (nlen,) = struct.unpack_from("<I", buf, off); off += 4
     name = buf[off:off + nlen].decode(); off += nlen
@@ -177,6 +234,13 @@ def read_nuclide(path: str | Path) -> Nuclide:
         mt, thr, m = struct.unpack_from("<III", buf, off); off += 12
         xs = np.frombuffer(buf, "<f8", m, off).copy(); off += 8 * m
         nuc.reactions[mt] = (thr, xs)
+    if version >= 2:
+        (flag,) = struct.unpack_from("<I", buf, off); off += 4
+        if flag:
+            nu = struct.unpack_from("<2d", buf, off); off += 16
+            (spec,) = struct.unpack_from("<I", buf, off); off += 4
+            a, b, u = struct.unpack_from("<3d", buf, off); off += 24
+            nuc.fission = Fission(nu=tuple(nu), spectrum=spec, params=(a, b), u=u)
     return nuc
 
 

@@ -366,6 +366,7 @@ _fn("openmc_regular_mesh_get_dimension", [C.c_int32, _p(_p(C.c_int)), _p(C.c_int
 _fn("openmc_regular_mesh_get_params", [C.c_int32, _p(_p(C.c_double)), _p(_p(C.c_double)),
                                        _p(_p(C.c_double)), _p(C.c_int)])
 _fn("openmc_get_keff", [_p(C.c_double)])
+_fn("openmc_gb300_k_generation", [_p(C.c_double), C.c_int, _p(C.c_int64)], check=False)
 
 FILL_TYPES = {0: "material", 1: "universe", 2: "lattice"}
 
@@ -545,11 +546,22 @@ def global_bounding_box():
 
 
 def keff():
-    """(k, standard deviation): 1 and an infinite (one realization or
-    fewer) or zero spread on this fixed-source path (openmc/lib/core.py)."""
+    """(k, standard deviation) of openmc_get_keff (openmc/lib/core.py): the
+    combined estimate of an eigenvalue run; 1 with an infinite (one
+    realization or fewer) or zero spread in a fixed-source run."""
     k = (C.c_double * 2)()
     _dll.openmc_get_keff(k)
     return k[0], k[1]
+
+
+def k_generation():
+    """Eigenvalue run: (track-length k of every generation so far, the last
+    generation's fission-bank size)."""
+    n = _dll.openmc_gb300_k_generation(None, 0, None)
+    k = (C.c_double * max(n, 1))()
+    sites = C.c_int64()
+    _dll.openmc_gb300_k_generation(k, n, C.byref(sites))
+    return np.array(k[:n]), sites.value
 
 
 class WeightWindows:

@@ -598,6 +598,7 @@ class Settings:
         self.particles = 1000
         self.batches = 1
         self.inactive = 0
+        self.generations_per_batch = None
         self.source = []
         self.event_based = False
         self.seed = None
@@ -627,6 +628,8 @@ class Settings:
         ET.SubElement(el, "batches").text = str(int(self.batches))
         if self.inactive:
             ET.SubElement(el, "inactive").text = str(int(self.inactive))
+        if self.generations_per_batch is not None:
+            ET.SubElement(el, "generations_per_batch").text = str(int(self.generations_per_batch))
         srcs = self.source if isinstance(self.source, (list, tuple)) else [self.source]
         for s in srcs:
             el.append(s.to_xml())

@@ -91,6 +91,15 @@ def lib(timing=False):
         L.oracle_xsb_destroy.argtypes = [vp]
         L.oracle_xsb_grid_index.argtypes = [vp, pi32]
         L.oracle_xsb_lookup.argtypes = [vp, i64, pi32, pd, pd, pi32, C.c_int]
+        L.oracle_eigen_begin.restype = C.c_int
+        L.oracle_eigen_begin.argtypes = [vp, C.c_int]
+        L.oracle_eigen_end.restype = C.c_int
+        L.oracle_eigen_end.argtypes = [vp, C.c_int]
+        L.oracle_keff.restype = C.c_int
+        L.oracle_keff.argtypes = [vp, pd, pd, C.c_int]
+        L.oracle_keff_combined.argtypes = [vp, pd]
+        L.oracle_source_bank.restype = i64
+        L.oracle_source_bank.argtypes = [vp, pd, i64]
         _libs[timing] = L
     return _libs[timing]
 
@@ -128,6 +137,7 @@ class Oracle:
             raise RuntimeError(err.value.decode())
         self.n_particles = int(self.arrays["settings_i"][0])
         self.n_batches = int(self.arrays["settings_i"][1])
+        self.eigenvalue = bool(self.arrays["eig_i"][0])
         self._trace = None
 
     def __del__(self):
@@ -149,9 +159,43 @@ class Oracle:
         self.L.oracle_accumulate(self.h)
 
     def run(self, batches=None, threads=1, mode=0, count=None):
+        """Transport and accumulate each batch; an eigenvalue run also starts
+        each generation from its source bank and ends it with the fission
+        bank's sort and comb and the k-effective bookkeeping."""
         for b in range(1, (batches or self.n_batches) + 1):
+            if self.eigenvalue:
+                if self.L.oracle_eigen_begin(self.h, b) != 0:
+                    raise RuntimeError(self.L.oracle_error(self.h).decode())
             self.transport(b, count=count, threads=threads, mode=mode)
-            self.accumulate()
+            if self.eigenvalue:
+                if self.L.oracle_eigen_end(self.h, b) != 0:
+                    raise RuntimeError(self.L.oracle_error(self.h).decode())
+            else:
+                self.accumulate()
+
+    def keff(self):
+        """Eigenvalue run: dict of keff, keff_std (of the average over active
+        generations), n_realizations, the last generation's fission sites,
+        the k estimators' SUM/SUM_SQ and cross sums, and every generation's
+        k (track-length estimate / n_particles)."""
+        out = np.zeros(13)
+        kg = np.zeros(100000)
+        n = self.L.oracle_keff(self.h, _p(out, C.c_double), _p(kg, C.c_double), len(kg))
+        names = ("keff", "keff_std", "n_realizations", "fission_sites", "k_col_sum", "k_col_sq", "k_abs_sum",
+                 "k_abs_sq", "k_tra_sum", "k_tra_sq", "k_col_abs", "k_col_tra", "k_abs_tra")
+        d = dict(zip(names, out.tolist()))
+        d["k_generation"] = kg[:n].copy()
+        kc = np.zeros(2)
+        self.L.oracle_keff_combined(self.h, _p(kc, C.c_double))
+        d["k_combined"] = (float(kc[0]), float(kc[1]))
+        return d
+
+    def source_bank(self, n=None):
+        """The coming generation's source sites: (n, 8) [r, u, E, wgt]."""
+        n = self.n_particles if n is None else n
+        out = np.zeros((n, 8))
+        m = self.L.oracle_source_bank(self.h, _p(out, C.c_double), n)
+        return out[:m]
 
     def tally(self, t):
         L = self.L

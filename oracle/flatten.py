@@ -42,10 +42,12 @@ def _read_library(xml_path):
 
 def _read_nuclide(path):
     """Read the native nuclide container (see openmc_gb300/data.py header):
-    returns (awr, kT, energy, {mt: (threshold_idx, xs)})."""
+    returns (awr, kT, energy, {mt: (threshold_idx, xs)}, fission) with
+    fission None or (nu0, nu1, spectrum, p0, p1, u)."""
     buf = Path(path).read_bytes()
     if buf[:8] != b"OMCGBNUC":
         raise ValueError(f"{path}: not a nuclide file")
+    (version,) = struct.unpack_from("<I", buf, 8)
     off = 12
     (nlen,) = struct.unpack_from("<I", buf, off); off += 4 + nlen
     _A, awr, kT = struct.unpack_from("<3d", buf, off); off += 24
@@ -55,7 +57,15 @@ def _read_nuclide(path):
     for _ in range(nrx):
         mt, thr, m = struct.unpack_from("<III", buf, off); off += 12
         rx[mt] = (thr, np.frombuffer(buf, "<f8", m, off).copy()); off += 8 * m
-    return awr, kT, energy, rx
+    fission = None
+    if version >= 2:
+        (flag,) = struct.unpack_from("<I", buf, off); off += 4
+        if flag:
+            nu0, nu1 = struct.unpack_from("<2d", buf, off); off += 16
+            (spec,) = struct.unpack_from("<I", buf, off); off += 4
+            p0, p1, u = struct.unpack_from("<3d", buf, off); off += 24
+            fission = (nu0, nu1, spec, p0, p1, u)
+    return awr, kT, energy, rx, fission
 
 
 SURF_TYPES = {"x-plane": 0, "y-plane": 1, "z-plane": 2, "x-cylinder": 3,
@@ -207,8 +217,9 @@ def load_model(model_xml, cross_sections=None):
     mat_index = {mid: k for k, mid in enumerate(mat_ids)}
 
     nuc_off, energy, elastic, capture, awr, kT = [0], [], [], [], [], []
+    fission_xs, fis_i, fis_d = [], [], []
     for name in nuc_names:
-        n_awr, n_kT, n_energy, rx = _read_nuclide(library[name])
+        n_awr, n_kT, n_energy, rx, fis = _read_nuclide(library[name])
         thr_el, el = rx[2]
         thr_c, cap = rx[102]
         if thr_el != 0 or thr_c != 0:
@@ -216,6 +227,14 @@ def load_model(model_xml, cross_sections=None):
         energy.append(n_energy); elastic.append(el); capture.append(cap)
         awr.append(n_awr); kT.append(n_kT)
         nuc_off.append(nuc_off[-1] + len(n_energy))
+        if fis is not None and 18 in rx:
+            fission_xs.append(rx[18][1])
+            fis_i.extend([1, fis[2]])
+            fis_d.extend([fis[0], fis[1], fis[3], fis[4], fis[5]])
+        else:
+            fission_xs.append(np.zeros(len(n_energy)))
+            fis_i.extend([0, 0])
+            fis_d.extend([0.0] * 5)
 
     # ---- geometry
     surfs = geom_el.findall("surface")
@@ -379,6 +398,10 @@ def load_model(model_xml, cross_sections=None):
     particles = int(_get(set_el, "particles"))
     batches = int(_get(set_el, "batches"))
     inactive = int(_get(set_el, "inactive", 0))
+    run_mode = (_get(set_el, "run_mode", "fixed source") or "fixed source").strip()
+    if run_mode not in ("fixed source", "eigenvalue"):
+        raise ValueError(f"run mode {run_mode} is not supported")
+    gen_per_batch = int(_get(set_el, "generations_per_batch", 1))
     seed = int(_get(set_el, "seed", 1))
     log_grid_bins = int(_get(set_el, "log_grid_bins", 8000))
     max_split_hist = int(_get(set_el, "max_history_splits", 10_000_000))
@@ -443,6 +466,9 @@ def load_model(model_xml, cross_sections=None):
         "nuc_energy": D(np.concatenate(energy)),
         "nuc_elastic": D(np.concatenate(elastic)),
         "nuc_capture": D(np.concatenate(capture)),
+        "nuc_fission": D(np.concatenate(fission_xs)),
+        "nuc_fis_i": I(fis_i), "nuc_fis_d": D(fis_d),
+        "eig_i": I([1 if run_mode == "eigenvalue" else 0, gen_per_batch]), "eig_d": D([1.0]),
         "mat_id": I(mat_ids), "mat_off": I(mat_off), "mat_nuc": I(mat_nuc),
         "mat_ao": D(mat_ao), "mat_density": D(mat_density),
         "surf_id": I(surf_id), "surf_type": I(surf_type),

@@ -1,8 +1,9 @@
 // ORACLE — test infrastructure only; never part of the product.
 //
-// CPU restatement of OpenMC's fixed-source continuous-energy neutron transport
-// path (event-based and history-based loops), written from the reference's
-// behaviour with each function citing the reference file:line it follows.
+// CPU restatement of OpenMC's continuous-energy neutron transport path
+// (fixed-source and eigenvalue runs, event-based and history-based loops),
+// written from the reference's behaviour with each function citing the
+// reference file:line it follows.
 // Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline may load
 // the library built from this file, and only to check results or as the
 // timed baseline.
@@ -268,6 +269,21 @@ struct Nuclide {
   std::vector<double> xs;       // [G][5] TOTAL, ABSORPTION, FISSION, NU_FISSION, PHOTON_PROD
   std::vector<double> elastic;  // reactions_[0]->xs_[0].value (MT 2)
   std::vector<int> grid_index;  // [M+1]
+  // MT 18 with one prompt neutron product: yield polynomial nu_c (increasing
+  // powers of E), energy spectrum 1 Maxwell (sp[0] = theta) or 2 Watt
+  // (sp = a, b) with restriction energy u, isotropic emission
+  bool fissionable = false;
+  double nu_c[2] = {0.0, 0.0};
+  int spectrum = 0;
+  double sp[2] = {0.0, 0.0};
+  double u = 0.0;
+  // src/endf.cpp:125-134 Polynomial::operator() (Horner, increasing powers)
+  double nu(double E) const
+  {
+    double y = 0.0;
+    for (int k = 1; k >= 0; --k) y = y * E + nu_c[k];
+    return y;
+  }
 };
 
 struct Material {
@@ -370,7 +386,7 @@ struct BoundaryInfo {
 };
 
 struct MicroXS {
-  double total, absorption, elastic;
+  double total, absorption, elastic, fission = 0.0, nu_fission = 0.0;
   int index_grid;
   double interp_factor;
   double last_E = 0.0;
@@ -380,6 +396,8 @@ struct SourceSite {
   Pos r, u;
   double E = 0, time = 0, wgt = 1.0;
   int surf_id = SURFACE_NONE;
+  int64_t parent_id = 0;  // fission sites: the parent's id and progeny number
+  int progeny_id = 0;
 };
 
 struct TraceRec {
@@ -411,6 +429,9 @@ struct Particle {
   int event_nuclide = -1;
   std::vector<SourceSite> secondary_bank;
   double keff_tally_leakage = 0;
+  double keff_tally_collision = 0, keff_tally_absorption = 0, keff_tally_tracklength = 0;
+  double macro_fission = 0, macro_nu_fission = 0;
+  int n_progeny = 0;
   double mu = 0;
   bool lost = false;
   // trace bookkeeping
@@ -471,19 +492,46 @@ struct Sim {
   int64_t n_lost = 0;
   std::vector<double> leak_sum;  // per batch normalised leakage (SUM, SUM_SQ)
   double leak_s1 = 0, leak_s2 = 0;
+  // eigenvalue run (src/eigenvalue.cpp, src/bank.cpp)
+  bool eigenvalue = false;
+  double energy_max_neutron = INFTY;  // data::energy_max[neutron]
+  double keff = 1.0, keff_std = 0.0;
+  double k_col = 0, k_abs = 0, k_tra = 0;  // this generation's global_tally_* sums
+  std::vector<SourceSite> source_bank, fission_bank;
+  int64_t fission_bank_cap = 0, n_fission_sites = 0;
+  int fission_bank_full = 0;
+  double keff_generation = 0.0;
+  std::vector<int64_t> progeny_per_particle;
+  std::vector<double> k_generation;
+  double k_sum[2] = {0.0, 0.0};
+  // global tallies K_COLLISION, K_ABSORPTION, K_TRACKLENGTH, LEAKAGE x (VALUE, SUM, SUM_SQ)
+  double gt[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  double k_col_abs = 0, k_col_tra = 0, k_abs_tra = 0;
+  int n_realizations = 0;
 };
 
 // ---------------------------------------------------------- XS data setup
-// src/nuclide.cpp:359-453 create_derived (MT2 then MT102, total += xs,
-// absorption += xs for disappearance MT 102)
-void create_derived(Nuclide& nuc, const double* el, const double* cap, int G)
+// src/nuclide.cpp:359-453 create_derived: reactions in MT order (2, 18,
+// 102); total += xs of each; MT 18 adds to fission and absorption, MT 102
+// (disappearance) to absorption; then nu_fission = nu(E) x fission per
+// grid point.  fis is null for a nuclide without MT 18.
+void create_derived(Nuclide& nuc, const double* el, const double* fis, const double* cap, int G)
 {
   nuc.xs.assign(static_cast<size_t>(G) * 5, 0.0);
   for (int k = 0; k < G; ++k) nuc.xs[5 * k + 0] += el[k];
+  if (fis) {
+    for (int k = 0; k < G; ++k) {
+      nuc.xs[5 * k + 0] += fis[k];
+      nuc.xs[5 * k + 2] += fis[k];
+      nuc.xs[5 * k + 1] += fis[k];
+    }
+  }
   for (int k = 0; k < G; ++k) {
     nuc.xs[5 * k + 0] += cap[k];
     nuc.xs[5 * k + 1] += cap[k];
   }
+  if (fis)
+    for (int k = 0; k < G; ++k) nuc.xs[5 * k + 3] = nuc.nu(nuc.energy[k]) * nuc.xs[5 * k + 2];
   nuc.elastic.assign(el, el + G);
 }
 
@@ -962,6 +1010,13 @@ void nuclide_calculate_xs(const Sim& S, int i_nuc, int i_log_union, Particle& p)
   micro.interp_factor = f;
   micro.total = (1.0 - f) * nuc.xs[5 * i_grid + 0] + f * nuc.xs[5 * (i_grid + 1) + 0];
   micro.absorption = (1.0 - f) * nuc.xs[5 * i_grid + 1] + f * nuc.xs[5 * (i_grid + 1) + 1];
+  if (nuc.fissionable) {
+    micro.fission = (1.0 - f) * nuc.xs[5 * i_grid + 2] + f * nuc.xs[5 * (i_grid + 1) + 2];
+    micro.nu_fission = (1.0 - f) * nuc.xs[5 * i_grid + 3] + f * nuc.xs[5 * (i_grid + 1) + 3];
+  } else {
+    micro.fission = 0.0;
+    micro.nu_fission = 0.0;
+  }
   micro.last_E = p.E;
 }
 
@@ -979,6 +1034,8 @@ void material_calculate_xs(Sim& S, Particle& p)
 {
   p.macro_total = 0.0;
   p.macro_absorption = 0.0;
+  p.macro_fission = 0.0;
+  p.macro_nu_fission = 0.0;
   const Material& mat = S.materials[p.material];
   int i_grid = std::log(p.E / S.energy_min) / S.log_spacing;
   i_grid = std::min(std::max(i_grid, 0), S.n_log_bins - 1);
@@ -991,6 +1048,8 @@ void material_calculate_xs(Sim& S, Particle& p)
     double atom_density = mat.atom_density_i(static_cast<int>(i), p.density_mult);
     p.macro_total += atom_density * micro.total;
     p.macro_absorption += atom_density * micro.absorption;
+    p.macro_fission += atom_density * micro.fission;
+    p.macro_nu_fission += atom_density * micro.nu_fission;
   }
   p.trace_grid = static_cast<int32_t>(h);
 }
@@ -1443,11 +1502,82 @@ int sample_nuclide(Sim& S, Particle& p)
   throw std::runtime_error("Did not sample any nuclide during collision.");
 }
 
-// src/physics.cpp:638-672 (analog)
-void absorption(Particle& p, int i_nuclide)
+// src/physics.cpp:638-672 (analog): the absorption estimate of k-effective
+// is scored when the disappearance happens
+void absorption(Sim& S, Particle& p, int i_nuclide)
 {
   if (p.micro[i_nuclide].absorption > prn(p.current_seed()) * p.micro[i_nuclide].total) {
+    if (S.eigenvalue)
+      p.keff_tally_absorption += p.wgt * p.micro[i_nuclide].nu_fission / p.micro[i_nuclide].absorption;
     p.wgt = 0.0;
+  }
+}
+
+// src/physics.cpp:1043-1115 sample_fission_neutron for a prompt-only MT 18
+// (nu_d = 0: the delayed test draws one number and never passes) whose
+// neutron product is an uncorrelated isotropic angle (mu uniform in [-1, 1],
+// src/secondary_uncorrelated.cpp) and a Maxwell or Watt spectrum with
+// restriction energy (src/distribution_energy.cpp:282-360); energies at or
+// above the data's maximum are resampled.
+void sample_fission_neutron(const Sim& S, int i_nuclide, SourceSite& site, Particle& p)
+{
+  const Nuclide& nuc = S.nuclides[i_nuclide];
+  double E_in = p.E;
+  uint64_t* seed = p.current_seed();
+  double nu_t = nuc.nu(E_in);
+  double nu_d = 0.0;
+  double beta = nu_d / nu_t;
+  if (prn(seed) < beta)
+    throw std::runtime_error("delayed neutrons are not supported");
+  double mu = 0.0;
+  for (int n_sample = 0;; ++n_sample) {
+    mu = uniform_distribution(-1., 1., seed);
+    double E_out;
+    while (true) {
+      E_out = nuc.spectrum == 1 ? maxwell_spectrum(nuc.sp[0], seed) : watt_spectrum(nuc.sp[0], nuc.sp[1], seed);
+      if (E_out <= E_in - nuc.u) break;
+    }
+    site.E = E_out;
+    if (site.E < S.energy_max_neutron) break;
+    if (n_sample + 1 == 10000) throw std::runtime_error("Resampled energy distribution maximum number of times");
+  }
+  site.u = rotate_angle(p.u(), mu, nullptr, seed);
+}
+
+// src/physics.cpp:170-285 create_fission_sites (eigenvalue run, no uniform
+// fission source): nu_t = wgt / keff x nu_fission / total of the sampled
+// nuclide; the sites go to the shared fission bank with (parent id, progeny
+// number) for the sort that makes the bank order independent of threads
+void create_fission_sites(Sim& S, Particle& p, int i_nuclide)
+{
+  double weight = 1.0;
+  const MicroXS& micro = p.micro[i_nuclide];
+  double nu_t = p.wgt / S.keff * weight * micro.nu_fission / micro.total;
+  int nu = static_cast<int>(nu_t);
+  if (prn(p.current_seed()) <= (nu_t - nu))
+    ++nu;
+  if (nu == 0)
+    return;
+  for (int n_sites = 0; n_sites < nu; n_sites++) {
+    SourceSite site;
+    site.r = p.r();
+    site.time = p.time;
+    site.wgt = 1. / weight;
+    site.surf_id = 0;
+    sample_fission_neutron(S, i_nuclide, site, p);
+    site.parent_id = p.id;
+    site.progeny_id = p.n_progeny++;
+    int64_t idx;
+#pragma omp atomic capture
+    idx = S.n_fission_sites++;
+    if (idx >= S.fission_bank_cap) {
+      // the reference warns and stops banking this particle's sites
+      p.n_progeny--;
+#pragma omp atomic write
+      S.fission_bank_full = 1;
+      break;
+    }
+    S.fission_bank[idx] = site;
   }
 }
 
@@ -1456,8 +1586,13 @@ void sample_neutron_reaction(Sim& S, Particle& p)
 {
   int i_nuclide = sample_nuclide(S, p);
   p.event_nuclide = i_nuclide;
+  // sample_fission (src/physics.cpp:552-562) returns the only fission
+  // reaction without drawing a number
+  if (S.nuclides[i_nuclide].fissionable && p.micro[i_nuclide].fission > 0.0) {
+    if (S.eigenvalue) create_fission_sites(S, p, i_nuclide);
+  }
   if (p.micro[i_nuclide].absorption > 0.0)
-    absorption(p, i_nuclide);
+    absorption(S, p, i_nuclide);
   if (!p.alive())
     return;
   scatter(S, p, i_nuclide);
@@ -1518,6 +1653,8 @@ void event_calculate_xs(Sim& S, Particle& p)
   } else {
     p.macro_total = 0.0;
     p.macro_absorption = 0.0;
+    p.macro_fission = 0.0;
+    p.macro_nu_fission = 0.0;
     p.trace_grid = -1;
   }
   if (p.trace && p.trace_n < p.trace_cap) {
@@ -1554,6 +1691,9 @@ void event_advance(Sim& S, Particle& p)
   p.time += dt;
   if (!S.tallies.empty())
     score_tracklength_tally(S, p, distance);
+  // src/particle.cpp:272-275
+  if (S.eigenvalue)
+    p.keff_tally_tracklength += p.wgt * distance * p.macro_nu_fission;
   if (distance == distance_cutoff)
     p.wgt = 0.0;
   if (p.trace && p.trace_n < p.trace_cap)
@@ -1633,6 +1773,9 @@ void event_cross_surface(Sim& S, Particle& p)
 // src/particle.cpp:331-415
 void event_collide(Sim& S, Particle& p)
 {
+  // src/particle.cpp:333-337 collision estimate of k-effective
+  if (S.eigenvalue)
+    p.keff_tally_collision += p.wgt * p.macro_nu_fission / p.macro_total;
   p.surface = SURFACE_NONE;
   collision(S, p);
   // src/particle.cpp:361-364
@@ -1687,6 +1830,17 @@ void event_death(Sim& S, Particle& p)
 #pragma omp atomic
   S.leakage += p.keff_tally_leakage;
   p.keff_tally_leakage = 0.0;
+  if (S.eigenvalue) {
+#pragma omp atomic
+    S.k_abs += p.keff_tally_absorption;
+#pragma omp atomic
+    S.k_col += p.keff_tally_collision;
+#pragma omp atomic
+    S.k_tra += p.keff_tally_tracklength;
+    p.keff_tally_absorption = p.keff_tally_collision = p.keff_tally_tracklength = 0.0;
+    // src/particle.cpp:505-510: progeny count for the fission bank sort
+    S.progeny_per_particle[p.id - 1] = p.n_progeny;
+  }
 }
 
 // ------------------------------------------------------------------ source
@@ -1782,11 +1936,19 @@ SourceSite sample_external_source(Sim& S, uint64_t* seed)
 void initialize_history(Sim& S, Particle& p, int batch, int64_t index_source)
 {
   int64_t id = static_cast<int64_t>(batch - 1) * S.n_particles + index_source;
-  uint64_t seed = init_seed(S.rng, id, STREAM_SOURCE);
-  SourceSite site = sample_external_source(S, &seed);
-  site.surf_id = SURFACE_NONE;
-  from_source(S, p, site);
+  if (S.eigenvalue) {
+    // src/simulation.cpp:576-578: from the generation's source bank
+    SourceSite site = S.source_bank[index_source - 1];
+    site.surf_id = SURFACE_NONE;
+    from_source(S, p, site);
+  } else {
+    uint64_t seed = init_seed(S.rng, id, STREAM_SOURCE);
+    SourceSite site = sample_external_source(S, &seed);
+    site.surf_id = SURFACE_NONE;
+    from_source(S, p, site);
+  }
   p.id = index_source;
+  p.n_progeny = 0;
   p.lost = false;
   p.n_event = 0;
   p.n_split = 0;
@@ -1847,6 +2009,9 @@ void build(Sim& S, const Blob& B)
   const auto& el = B.D("nuc_elastic");
   const auto& cap = B.D("nuc_capture");
   int n_nuc = static_cast<int>(off.size()) - 1;
+  const auto& fis = B.D("nuc_fission");
+  const auto& fis_i = B.I("nuc_fis_i");  // [fissionable, spectrum] per nuclide
+  const auto& fis_d = B.D("nuc_fis_d");  // [nu0, nu1, sp0, sp1, u] per nuclide
   S.nuclides.resize(n_nuc);
   for (int i = 0; i < n_nuc; ++i) {
     Nuclide& nuc = S.nuclides[i];
@@ -1854,8 +2019,19 @@ void build(Sim& S, const Blob& B)
     nuc.kT = B.D("nuc_kT")[i];
     int G = static_cast<int>(off[i + 1] - off[i]);
     nuc.energy.assign(en.begin() + off[i], en.begin() + off[i + 1]);
-    create_derived(nuc, el.data() + off[i], cap.data() + off[i], G);
+    nuc.fissionable = fis_i[2 * i] != 0;
+    nuc.spectrum = static_cast<int>(fis_i[2 * i + 1]);
+    nuc.nu_c[0] = fis_d[5 * i];
+    nuc.nu_c[1] = fis_d[5 * i + 1];
+    nuc.sp[0] = fis_d[5 * i + 2];
+    nuc.sp[1] = fis_d[5 * i + 3];
+    nuc.u = fis_d[5 * i + 4];
+    create_derived(nuc, el.data() + off[i], nuc.fissionable ? fis.data() + off[i] : nullptr, cap.data() + off[i], G);
   }
+  const auto& eig = B.I("eig_i");  // [eigenvalue run, generations per batch]
+  S.eigenvalue = eig[0] != 0;
+  if (S.eigenvalue && eig[1] != 1) throw std::runtime_error("one generation per batch is supported");
+  S.keff = B.D("eig_d")[0];
   // src/simulation.cpp:682-761 initialize_data
   S.energy_min = 0.0;
   S.energy_max = INFTY;
@@ -1865,6 +2041,7 @@ void build(Sim& S, const Blob& B)
   }
   for (auto& nuc : S.nuclides)
     init_grid(nuc, S.energy_min, S.energy_max, S.n_log_bins);
+  S.energy_max_neutron = S.energy_max;  // data::energy_max[neutron]: the smallest grid maximum
   S.log_spacing = std::log(S.energy_max / S.energy_min) / S.n_log_bins;
 
   // materials: src/material.cpp:417-467 normalize_density (atom percents)
@@ -2023,6 +2200,113 @@ void build(Sim& S, const Blob& B)
 }
 
 // src/tallies/tally.cpp:821-880 Tally::accumulate
+// ------------------------------------------------------------ eigenvalue
+// src/source.cpp:601-615 initialize_source (first generation) and
+// src/simulation.cpp:507-520 initialize_generation
+void eigen_begin_batch(Sim& S, int batch)
+{
+  if (batch == 1) {
+    S.source_bank.assign(S.n_particles, SourceSite {});
+    for (int64_t i = 0; i < S.n_particles; ++i) {
+      uint64_t seed = init_seed(S.rng, i + 1, STREAM_SOURCE);
+      S.source_bank[i] = sample_external_source(S, &seed);
+    }
+    S.fission_bank_cap = 3 * S.n_particles;
+    S.fission_bank.assign(S.fission_bank_cap, SourceSite {});
+  }
+  S.n_fission_sites = 0;
+  S.fission_bank_full = 0;
+  S.progeny_per_particle.assign(S.n_particles, 0);
+  S.keff_generation = S.gt[2][0];
+}
+
+// src/bank.cpp:76-135 sort_fission_bank: exclusive scan of the progeny
+// counts, each site to its parent's offset plus its progeny number
+void sort_fission_bank(Sim& S)
+{
+  std::vector<int64_t> off(S.progeny_per_particle.size());
+  int64_t acc = 0;
+  for (size_t i = 0; i < off.size(); ++i) {
+    off[i] = acc;
+    acc += S.progeny_per_particle[i];
+  }
+  std::vector<SourceSite> sorted(S.n_fission_sites);
+  for (int64_t i = 0; i < S.n_fission_sites; ++i) {
+    const SourceSite& site = S.fission_bank[i];
+    int64_t idx = off[site.parent_id - 1] + site.progeny_id;
+    if (idx >= S.n_fission_sites)
+      throw std::runtime_error("Mismatch detected between sum of all particle progeny and shared fission bank size.");
+    sorted[idx] = site;
+  }
+  std::copy(sorted.begin(), sorted.end(), S.fission_bank.begin());
+}
+
+// src/eigenvalue.cpp:86-365 synchronize_bank on one rank: uniform combing
+// of n_particles teeth over the sorted bank, the comb's offset drawn from
+// the tracking stream of the generation's id
+void synchronize_bank(Sim& S, int batch)
+{
+  int64_t start = 0;
+  int64_t finish = S.n_fission_sites;
+  int64_t total = finish;
+  if (S.n_fission_sites == 0) throw std::runtime_error("No fission sites banked on MPI rank 0");
+  std::vector<SourceSite> temp_sites(3 * S.n_particles);
+  int64_t index_temp = 0;
+  int64_t id = 0 + batch;  // total_gen + overall_generation() with one generation per batch
+  uint64_t seed = init_seed(S.rng, id, STREAM_TRACKING);
+  double teeth_distance = static_cast<double>(total) / S.n_particles;
+  double teeth_offset = prn(&seed) * teeth_distance;
+  int64_t end = start + S.n_fission_sites;
+  int64_t tooth_start = std::ceil((start - teeth_offset) / teeth_distance);
+  int64_t tooth_end = std::floor((end - teeth_offset) / teeth_distance) + 1;
+  double tooth = tooth_start * teeth_distance + teeth_offset;
+  for (int64_t i = tooth_start; i < tooth_end; i++) {
+    int64_t idx = std::floor(tooth) - start;
+    temp_sites[index_temp] = S.fission_bank[idx];
+    ++index_temp;
+    tooth += teeth_distance;
+  }
+  if (index_temp < S.n_particles) throw std::runtime_error("the comb selected fewer sites than particles");
+  std::copy(temp_sites.begin(), temp_sites.begin() + S.n_particles, S.source_bank.begin());
+}
+
+// src/eigenvalue.cpp:367-418 calculate_average_keff (one generation per
+// batch, no confidence-interval t-value)
+void calculate_average_keff(Sim& S, int batch)
+{
+  int i = batch - 1;
+  int n = batch > S.n_inactive ? S.n_realizations + 1 : 0;
+  if (n <= 0) {
+    S.keff = S.k_generation[i];
+  } else {
+    S.k_sum[0] += S.k_generation[i];
+    S.k_sum[1] += std::pow(S.k_generation[i], 2);
+    S.keff = S.k_sum[0] / n;
+    if (n > 1) {
+      double t_value = 1.0;
+      S.keff_std = t_value * std::sqrt((S.k_sum[1] / n - std::pow(S.keff, 2)) / (n - 1));
+      if (!std::isfinite(S.keff_std)) S.keff_std = 0.0;
+    }
+  }
+}
+
+// src/simulation.cpp:522-570 finalize_generation and
+// src/eigenvalue.cpp:50-84 calculate_generation_keff
+void eigen_end_batch(Sim& S, int batch)
+{
+  if (S.fission_bank_full) throw std::runtime_error("The shared fission bank is full.");
+  S.gt[0][0] += S.k_col;
+  S.gt[1][0] += S.k_abs;
+  S.gt[2][0] += S.k_tra;
+  S.k_col = S.k_abs = S.k_tra = 0.0;
+  sort_fission_bank(S);
+  synchronize_bank(S, batch);
+  double kg = S.gt[2][0] - S.keff_generation;
+  kg /= S.n_particles;
+  S.k_generation.push_back(kg);
+  calculate_average_keff(S, batch);
+}
+
 void accumulate(Sim& S)
 {
   double norm = S.strength / (static_cast<double>(S.n_particles) * 1);
@@ -2041,6 +2325,41 @@ void accumulate(Sim& S)
   S.leak_s2 += l * l;
   S.leakage = 0.0;
   S.total_weight = 0.0;
+}
+
+// src/tallies/tally.cpp:1059-1100 accumulate_tallies and
+// src/simulation.cpp:402-418 finalize_batch for an eigenvalue run: user
+// tallies score only in active batches; global tallies (normalised by the
+// source weight) accumulate every batch and are reset, with the realization
+// count, after each inactive one
+void accumulate_eigen(Sim& S, int batch)
+{
+  S.n_realizations += 1;
+  bool active = batch > S.n_inactive;
+  if (active) {
+    double k_col = S.gt[0][0] / S.total_weight;
+    double k_abs = S.gt[1][0] / S.total_weight;
+    double k_tra = S.gt[2][0] / S.total_weight;
+    S.k_col_abs += k_col * k_abs;
+    S.k_col_tra += k_col * k_tra;
+    S.k_abs_tra += k_abs * k_tra;
+  }
+  for (int i = 0; i < 3; ++i) {
+    double val = S.gt[i][0] / S.total_weight;
+    S.gt[i][0] = 0.0;
+    S.gt[i][1] += val;
+    S.gt[i][2] += val * val;
+  }
+  if (active) {
+    accumulate(S);
+  } else {
+    for (auto& t : S.tallies)
+      for (size_t i = 0; i < t.results.size(); i += 3) t.results[i] = 0.0;
+    S.leakage = 0.0;
+    S.total_weight = 0.0;
+    for (auto& row : S.gt) row[0] = row[1] = row[2] = 0.0;
+    S.n_realizations = 0;
+  }
 }
 
 struct Handle {
@@ -2193,6 +2512,145 @@ int oracle_accumulate(void* hv)
 {
   accumulate(static_cast<Handle*>(hv)->S);
   return 0;
+}
+
+// Eigenvalue run: before the batch's transport (first batch: initial source
+// bank from the external source), after it (fission bank sort, comb,
+// generation and average k), and the batch's accumulation.
+int oracle_eigen_begin(void* hv, int batch)
+{
+  auto* h = static_cast<Handle*>(hv);
+  try {
+    eigen_begin_batch(h->S, batch);
+  } catch (const std::exception& e) {
+    h->err = e.what();
+    return -1;
+  }
+  return 0;
+}
+
+int oracle_eigen_end(void* hv, int batch)
+{
+  auto* h = static_cast<Handle*>(hv);
+  try {
+    eigen_end_batch(h->S, batch);
+    accumulate_eigen(h->S, batch);
+  } catch (const std::exception& e) {
+    h->err = e.what();
+    return -1;
+  }
+  return 0;
+}
+
+// [keff, keff_std, n_realizations, fission sites of the last generation,
+//  K_COLLISION / K_ABSORPTION / K_TRACKLENGTH (SUM, SUM_SQ), k_col_abs,
+//  k_col_tra, k_abs_tra] and the generation k values (k_gen, up to n_gen)
+int oracle_keff(void* hv, double* out, double* k_gen, int n_gen)
+{
+  Sim& S = static_cast<Handle*>(hv)->S;
+  out[0] = S.keff;
+  out[1] = S.keff_std;
+  out[2] = S.n_realizations;
+  out[3] = static_cast<double>(S.n_fission_sites);
+  for (int i = 0; i < 3; ++i) {
+    out[4 + 2 * i] = S.gt[i][1];
+    out[5 + 2 * i] = S.gt[i][2];
+  }
+  out[10] = S.k_col_abs;
+  out[11] = S.k_col_tra;
+  out[12] = S.k_abs_tra;
+  int n = static_cast<int>(S.k_generation.size());
+  for (int i = 0; i < n && i < n_gen; ++i) k_gen[i] = S.k_generation[i];
+  return n;
+}
+
+// src/eigenvalue.cpp:420-579 openmc_get_keff: k_combined[0..1]
+void oracle_keff_combined(void* hv, double* k_combined)
+{
+  Sim& S = static_cast<Handle*>(hv)->S;
+  k_combined[0] = 0.0;
+  k_combined[1] = 0.0;
+  if (S.n_realizations <= 3) {
+    k_combined[0] = S.keff;
+    k_combined[1] = S.keff_std;
+    if (S.n_realizations <= 1) k_combined[1] = std::numeric_limits<double>::infinity();
+    return;
+  }
+  int64_t n = S.n_realizations;
+  std::array<double, 3> kv {};
+  double cov[3][3] = {};
+  kv[0] = S.gt[0][1] / n;
+  kv[1] = S.gt[1][1] / n;
+  kv[2] = S.gt[2][1] / n;
+  cov[0][0] = (S.gt[0][2] - n * kv[0] * kv[0]) / (n - 1);
+  cov[1][1] = (S.gt[1][2] - n * kv[1] * kv[1]) / (n - 1);
+  cov[2][2] = (S.gt[2][2] - n * kv[2] * kv[2]) / (n - 1);
+  cov[0][1] = (S.k_col_abs - n * kv[0] * kv[1]) / (n - 1);
+  cov[0][2] = (S.k_col_tra - n * kv[0] * kv[2]) / (n - 1);
+  cov[1][2] = (S.k_abs_tra - n * kv[1] * kv[2]) / (n - 1);
+  cov[1][0] = cov[0][1];
+  cov[2][0] = cov[0][2];
+  cov[2][1] = cov[1][2];
+  int i, j;
+  bool use_three = false;
+  if ((std::abs(kv[0] - kv[1]) / kv[0] < FP_REL_PRECISION) &&
+      (std::abs(cov[0][0] - cov[1][1]) / cov[0][0] < FP_REL_PRECISION)) {
+    i = 0; j = 2;
+  } else if ((std::abs(kv[0] - kv[2]) / kv[0] < FP_REL_PRECISION) &&
+             (std::abs(cov[0][0] - cov[2][2]) / cov[0][0] < FP_REL_PRECISION)) {
+    i = 0; j = 1;
+  } else if ((std::abs(kv[1] - kv[2]) / kv[1] < FP_REL_PRECISION) &&
+             (std::abs(cov[1][1] - cov[2][2]) / cov[1][1] < FP_REL_PRECISION)) {
+    i = 0; j = 1;
+  } else {
+    use_three = true;
+    i = j = 0;
+  }
+  if (use_three) {
+    double g = 0.0;
+    std::array<double, 3> Ssum {};
+    for (int l = 0; l < 3; ++l) {
+      int k;
+      switch (l) {
+      case 0: i = 0; j = 1; k = 2; break;
+      case 1: i = 1; j = 2; k = 0; break;
+      default: i = 2; j = 0; k = 1; break;
+      }
+      double f = cov[j][j] * (cov[k][k] - cov[i][k]) - cov[k][k] * cov[i][j] +
+                 cov[j][k] * (cov[i][j] + cov[i][k] - cov[j][k]);
+      Ssum[0] += f * cov[0][l];
+      Ssum[1] += (cov[j][j] + cov[k][k] - 2.0 * cov[j][k]) * kv[l] * kv[l];
+      Ssum[2] += (cov[k][k] + cov[i][j] - cov[j][k] - cov[i][k]) * kv[l] * kv[j];
+      k_combined[0] += f * kv[l];
+      g += f;
+    }
+    for (auto& v : Ssum) v *= (n - 1);
+    Ssum[0] *= (n - 1) * (n - 1);
+    k_combined[0] /= g;
+    g *= (n - 1) * (n - 1);
+    k_combined[1] = std::sqrt(Ssum[0] / (g * n * (n - 3)) * (1 + n * ((Ssum[1] - 2 * Ssum[2]) / g)));
+  } else {
+    double f = kv[i] - kv[j];
+    double g = cov[i][i] + cov[j][j] - 2.0 * cov[i][j];
+    k_combined[0] = kv[i] - (cov[i][i] - cov[i][j]) / g * f;
+    k_combined[1] = (cov[i][i] * cov[j][j] - cov[i][j] * cov[i][j]) * (g + n * f * f) / (n * (n - 2) * g * g);
+    k_combined[1] = std::sqrt(k_combined[1]);
+  }
+}
+
+// The source bank of the coming generation: n x [x, y, z, u, v, w, E, wgt]
+int64_t oracle_source_bank(void* hv, double* out, int64_t n)
+{
+  Sim& S = static_cast<Handle*>(hv)->S;
+  int64_t m = std::min<int64_t>(n, static_cast<int64_t>(S.source_bank.size()));
+  for (int64_t i = 0; i < m; ++i) {
+    const SourceSite& s = S.source_bank[i];
+    double* o = out + 8 * i;
+    o[0] = s.r.x; o[1] = s.r.y; o[2] = s.r.z;
+    o[3] = s.u.x; o[4] = s.u.y; o[5] = s.u.z;
+    o[6] = s.E; o[7] = s.wgt;
+  }
+  return m;
 }
 
 int oracle_n_tallies(void* hv) { return static_cast<int>(static_cast<Handle*>(hv)->S.tallies.size()); }

@@ -278,7 +278,7 @@ def test_python_model_views(built, tmp_path):
         lib.finalize()
 
 
-@pytest.mark.parametrize("case", ["survival_biasing", "eigenvalue"])
+@pytest.mark.parametrize("case", ["survival_biasing", "generations_per_batch"])
 def test_unsupported_settings_rejected(built, tmp_path, case):
     """Settings the GPU path does not implement fail at openmc_init instead
     of running without them."""
@@ -288,6 +288,7 @@ def test_unsupported_settings_rejected(built, tmp_path, case):
         m.settings.survival_biasing = True
     else:
         m.settings.run_mode = "eigenvalue"
+        m.settings.generations_per_batch = 2
     m.export_to_model_xml(d)
     with pytest.raises(lib.InvalidArgumentError):
         lib.init(directory=d)

@@ -176,7 +176,6 @@ struct DBank {
   unsigned long long* seed;
   double *E, *wgt, *wgt_born, *wgt_ww_born, *ww_factor;
   double *ux, *uy, *uz;
-  double *iux, *iuy, *iuz;  // 1 / u (FP32-table mode), written wherever the direction changes
   double *rx, *ry, *rz;
   int *cell, *univ, *latt, *lix, *liy, *liz;
   int *n_coord, *cell_last0, *cell_born;
@@ -598,18 +597,18 @@ __device__ inline double cylinder_distance(double u1, double r2_, double u2, dou
   const double k = r2 * u2 + r3 * u3;
   const double c = r2 * r2 + r3 * r3 - radius;  // radius: the squared radius
   const double quad = k * k - a * c;
-  if (fpi::neg(quad)) return INFTY;
-  // the reference's three branches (on the surface, inside, outside) with
-  // one square root and one division shared by all lanes: far root
-  // (-k + sqrt) on the surface (moving inwards) or inside, near root
-  // (-k - sqrt, INFTY when behind) outside
-  const bool on = coincident || fpi::abs_lt(c, FP_COINCIDENT);
-  if (on && fpi::nonneg(k)) return INFTY;
-  const bool far = on || fpi::neg(c);
-  const double sq = sqrt(quad);
-  const double d = (far ? -k + sq : -k - sq) / a;
-  if (!far && fpi::neg(d)) return INFTY;
-  return d;
+  if (fpi::neg(quad)) {
+    return INFTY;
+  } else if (coincident || fpi::abs_lt(c, FP_COINCIDENT)) {
+    if (fpi::nonneg(k)) return INFTY;
+    return (-k + sqrt(quad)) / a;
+  } else if (fpi::neg(c)) {
+    return (-k + sqrt(quad)) / a;
+  } else {
+    const double d = (-k - sqrt(quad)) / a;
+    if (fpi::neg(d)) return INFTY;
+    return d;
+  }
 }
 
 __device__ inline double sphere_distance(const DSurface& s, double x_, double y_, double z_, double ux,
@@ -621,14 +620,18 @@ __device__ inline double sphere_distance(const DSurface& s, double x_, double y_
   const double k = x * ux + y * uy + z * uz;
   const double c = x * x + y * y + z * z - s.rr;
   const double quad = k * k - c;
-  if (fpi::neg(quad)) return INFTY;
-  const bool on = coincident || fpi::abs_lt(c, FP_COINCIDENT);
-  if (on && fpi::nonneg(k)) return INFTY;
-  const bool far = on || fpi::neg(c);
-  const double sq = sqrt(quad);
-  const double d = far ? -k + sq : -k - sq;
-  if (!far && fpi::neg(d)) return INFTY;
-  return d;
+  if (fpi::neg(quad)) {
+    return INFTY;
+  } else if (coincident || fpi::abs_lt(c, FP_COINCIDENT)) {
+    if (fpi::nonneg(k)) return INFTY;
+    return -k + sqrt(quad);
+  } else if (fpi::neg(c)) {
+    return -k + sqrt(quad);
+  } else {
+    const double d = -k - sqrt(quad);
+    if (fpi::neg(d)) return INFTY;
+    return d;
+  }
 }
 
 __device__ inline double surf_distance(const DSurface& s, double x, double y, double z, double ux,
@@ -893,20 +896,12 @@ __device__ inline void geo_store(const Geo& g, long long s)
   db.material_last[s] = g.material_last;
 }
 
-// New direction of slot s; in FP32-table mode also its reciprocal, which
-// the lattice and mesh distances of every later flight multiply by (the
-// direction changes at collisions and reflections, far less often than the
-// particle flies).
+// New direction of slot s
 __device__ __forceinline__ void set_direction(long long s, double ux, double uy, double uz)
 {
   db.ux[s] = ux;
   db.uy[s] = uy;
   db.uz[s] = uz;
-  if (dm.xs_fp32) {
-    db.iux[s] = 1.0 / ux;
-    db.iuy[s] = 1.0 / uy;
-    db.iuz[s] = 1.0 / uz;
-  }
 }
 
 __device__ __forceinline__ void coord_reset(Geo& g, int l)

@@ -989,14 +989,15 @@ __device__ int ev_advance(long long s, EvStats& st, int qi = 0)
   int bs, bl, bt;
   bool neg_lat = false;
   // FP32-table mode: reciprocal direction shared by the lattice and mesh
-  // distances (FP64 products in place of FP64 quotients), kept with the
-  // direction in the bank
+  // distances (FP64 products in place of FP64 quotients).  Recomputed per
+  // flight: keeping it in the bank with the direction measured 5 % slower
+  // (three more scattered loads cost more than three FP64 divisions).
   double inv_u[3];
   const bool recip = dm.xs_fp32 != 0;
   if (recip) {
-    inv_u[0] = db.iux[s];
-    inv_u[1] = db.iuy[s];
-    inv_u[2] = db.iuz[s];
+    inv_u[0] = 1.0 / g.u[0];
+    inv_u[1] = 1.0 / g.u[1];
+    inv_u[2] = 1.0 / g.u[2];
   }
   distance_to_boundary(g, bd, bs, bl, bt, neg_lat, recip ? inv_u : nullptr);
   if (neg_lat) mark_lost(s);
@@ -1174,7 +1175,6 @@ __device__ int ev_surface_g(long long s, EvStats& st, Geo& g, double wgt, int bs
         wgt = 0.0;
       } else {
         g.u[0] = ux; g.u[1] = uy; g.u[2] = uz;
-        set_direction(s, ux, uy, uz);  // geo_store writes u again below
         g.cell[0] = db.cell_last0[s];
         g.surface = -g.surface;
         g.n_coord = 1;
@@ -2326,12 +2326,6 @@ static void build_bank(GpuSim& G, long long cap, long long sec_cap)
   b.ux = dev_alloc<double>(cap, own);
   b.uy = dev_alloc<double>(cap, own);
   b.uz = dev_alloc<double>(cap, own);
-  b.iux = b.iuy = b.iuz = nullptr;
-  if (G.model.xs_fp32) {
-    b.iux = dev_alloc<double>(cap, own);
-    b.iuy = dev_alloc<double>(cap, own);
-    b.iuz = dev_alloc<double>(cap, own);
-  }
   b.rx = dev_alloc<double>(cap * MAXL, own);
   b.ry = dev_alloc<double>(cap * MAXL, own);
   b.rz = dev_alloc<double>(cap * MAXL, own);

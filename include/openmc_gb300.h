@@ -231,6 +231,9 @@ bool openmc_is_statepoint_batch(void);                                 /* src/st
 int openmc_get_n_batches(int* n_batches, bool get_max_batches);        /* src/settings.cpp:1319-1324 */
 int openmc_set_n_batches(int32_t n_batches, bool set_max_batches, bool add_statepoint_batch);  /* :1285-1317 */
 int openmc_get_keff(double k_combined[]);                              /* src/eigenvalue.cpp:420-579 */
+/* statepoint file format 18.1 (tallies, k-effective, global tallies; no source
+ * bank); filename NULL: statepoint.<batch>.h5 in the output path */
+int openmc_statepoint_write(const char* filename, bool* write_source);  /* src/state_point.cpp:36-357 */
 int openmc_get_cell_index(int32_t id, int32_t* index);                 /* src/cell.cpp */
 int openmc_cell_get_id(int32_t index, int32_t* id);
 int openmc_cell_get_translation(int32_t index, double xyz[]);

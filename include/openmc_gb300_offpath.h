@@ -101,7 +101,6 @@ int openmc_spherical_mesh_set_grid(int32_t index, const double* grid_x, const in
 int openmc_sphharm_filter_get_order(int32_t index, int* order);
 int openmc_sphharm_filter_set_order(int32_t index, int order);
 int openmc_statepoint_load(const char* filename);
-int openmc_statepoint_write(const char* filename, bool* write_source);
 int openmc_tally_reset(int32_t index);
 int openmc_tally_set_active(int32_t index, bool active);
 int openmc_tally_set_estimator(int32_t index, const char* estimator);

@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # on the Arm host), as the reference's expressions and the oracle do
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
 EXACT = ["-fmad=false"]
-SOURCES = ["host_model.cpp", "capi.cpp", "capi_model.cpp", "capi_offpath.cpp", "transport_dispatch.cpp", "xsbench.cu",
+SOURCES = ["h5lite.cpp", "host_model.cpp", "capi.cpp", "capi_model.cpp", "capi_offpath.cpp", "transport_dispatch.cpp", "xsbench.cu",
            "mlp.cu"]
 # transport.cu is built once per maximum coordinate depth (namespaces l2, l4)
 # with separately rounded multiplies and adds, and once for FP32-table mode at

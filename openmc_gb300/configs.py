@@ -36,11 +36,11 @@ GUIDE_TUBES = [(2, 5), (2, 8), (2, 11), (3, 3), (3, 13), (5, 2), (5, 5),
                (13, 3), (13, 13), (14, 5), (14, 8), (14, 11)]
 
 
-def _library(directory, specs, n_points, seed):
+def _library(directory, specs, n_points, seed, fmt="native"):
     nucs = []
     for k, (name, A) in enumerate(specs):
         nucs.append(data.make_nuclide(name, A, n_points, seed * 1000 + k))
-    xml = data.write_library(nucs, directory)
+    xml = data.write_library(nucs, directory, fmt=fmt)
     return nucs, xml
 
 
@@ -108,7 +108,7 @@ def point_cube(directory, particles=100_000, batches=10, n_points=2000,
 
 
 def infinite_medium(directory, particles=20_000, batches=30, inactive=10, n_points=500, seed=7,
-                    event_based=True, fissile_fraction=0.045):
+                    event_based=True, fissile_fraction=0.045, library_format="native"):
     """Eigenvalue run in an infinite homogeneous medium: a reflective 20 cm
     cube of one material made of a fissile nuclide and a light moderator
     whose cross sections do not depend on energy, so that
@@ -119,7 +119,7 @@ def infinite_medium(directory, particles=20_000, batches=30, inactive=10, n_poin
     sc_m, se_m = 0.3, 20.0
     nucs = [data.make_flat_nuclide("Fx235", 235, n_points, seed, se_f, sc_f, fission=sf, nu=nu),
             data.make_flat_nuclide("Mx1", 1, n_points, seed + 1, se_m, sc_m)]
-    xs_xml = data.write_library(nucs, directory)
+    xs_xml = data.write_library(nucs, directory, fmt=library_format)
     mat = om.Material(name="fissile mixture")
     mat.add_nuclide("Fx235", fissile_fraction)
     mat.add_nuclide("Mx1", 1.0 - fissile_fraction)
@@ -155,11 +155,11 @@ def _pin_universe(fuel, clad, mod, r_pin=0.41, r_clad=0.475, guide=False):
                               om.Cell(fill=mod, region=+s2)])
 
 
-def _lattice_materials(directory, n_points, seed):
+def _lattice_materials(directory, n_points, seed, fmt="native"):
     specs = [("Hv235", 235), ("Hv238", 238), ("Ox16", 16), ("Hv240", 240),
              ("Cl56", 56), ("Cl58", 58), ("Cl90", 90), ("Cl91", 91),
              ("Lt1", 1), ("Lt2", 2), ("Lt16", 16), ("Lt10", 10)]
-    _, xs_xml = _library(directory, specs, n_points, seed)
+    _, xs_xml = _library(directory, specs, n_points, seed, fmt)
     rng = np.random.default_rng(seed + 17)
 
     def mixture(name, names, weights, density):
@@ -181,9 +181,9 @@ def _lattice_materials(directory, n_points, seed):
 
 def lattice17(directory, particles=10_000_000, batches=20, n_points=11303,
               seed=3, event_based=True, mesh_dim=(17, 17, 50), n_ebins=100,
-              height=200.0):
+              height=200.0, library_format="native"):
     directory = Path(directory)
-    fuel, clad, mod, xs_xml = _lattice_materials(directory, n_points, seed)
+    fuel, clad, mod, xs_xml = _lattice_materials(directory, n_points, seed, library_format)
     mats = om.Materials([fuel, clad, mod], cross_sections=xs_xml.name)
     pin = _pin_universe(fuel, clad, mod)
     gt = _pin_universe(fuel, clad, mod, r_pin=0.56, r_clad=0.60, guide=True)

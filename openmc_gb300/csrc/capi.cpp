@@ -10,6 +10,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <ctime>
 #include <fstream>
 #include <limits>
 #include <memory>
@@ -17,6 +18,7 @@
 #include <string>
 #include <vector>
 
+#include "h5lite.h"
 #include "host_model.h"
 #include "transport.h"
 
@@ -89,6 +91,8 @@ int64_t openmc_gb300_trace_first = 1;   // first particle id openmc_gb300_set_tr
 namespace {
 
 using namespace omc;
+
+extern "C" int openmc_get_keff(double k_combined[]);
 
 struct State {
   bool model_loaded = false;
@@ -399,6 +403,11 @@ int check_device_errors(const BatchStats& st)
 
 extern "C" {
 
+namespace {
+void write_statepoint(const std::string& path);
+std::string default_statepoint_name(const HModel& m);
+}  // namespace
+
 // src/initialize.cpp:45-138, 215-330 (arguments: [-e] [-n N] [-s N] [path])
 int openmc_init(int argc, char* argv[], const void* intracomm)
 {
@@ -547,6 +556,11 @@ int openmc_next_batch(int* status)
         }
       }
     }
+    if (current_batch >= m.n_batches) {
+      // src/simulation.cpp:432-441: the last batch is a statepoint batch
+      gpu_fetch_tallies(s.gpu, m);
+      write_statepoint(default_statepoint_name(m));
+    }
     if (status && current_batch >= m.n_batches) *status = 1;
     return 0;
   } catch (const std::exception& e) {
@@ -647,7 +661,182 @@ void write_tallies(const HModel& m)
   }
 }
 
+// A fixed-length string array dataset ("char[][]" of the file formats)
+h5::Value strings(const std::vector<std::string>& v)
+{
+  h5::Value out;
+  out.kind = 's';
+  out.size = 1;
+  for (const auto& x : v) out.size = std::max(out.size, x.size());
+  out.shape = {v.size()};
+  out.bytes.assign(out.size * v.size(), 0);
+  for (size_t k = 0; k < v.size(); ++k) std::copy(v[k].begin(), v[k].end(), out.bytes.begin() + k * out.size);
+  return out;
+}
+
+h5::Value int_array(const std::vector<int>& v)
+{
+  return h5::array(std::vector<long long>(v.begin(), v.end()));
+}
+
+// src/state_point.cpp:36-357 openmc_statepoint_write in the statepoint file
+// format 18.1 (docs/source/io_formats/statepoint.rst): run parameters,
+// k-effective results of an eigenvalue run, global tallies, and every
+// tally with its meshes and filters and its accumulated (SUM, SUM_SQ)
+// results.  No source bank is written (source_present 0).
+void write_statepoint(const std::string& path)
+{
+  State& s = S();
+  const HModel& m = s.model;
+  h5::WNode root;
+  root.attrs["filetype"] = h5::string("statepoint");
+  root.attrs["version"] = h5::array(std::vector<long long> {18, 1});
+  root.attrs["openmc_version"] = h5::array(std::vector<long long> {0, 15, 0});
+  root.attrs["git_sha1"] = h5::string(std::string(40, '0'));
+  {
+    std::time_t t = std::time(nullptr);
+    char buf[64];
+    std::strftime(buf, sizeof(buf), "%Y-%m-%d %H:%M:%S", std::localtime(&t));
+    root.attrs["date_and_time"] = h5::string(buf);
+  }
+  root.attrs["path"] = h5::string(m.path_output);
+  root.attrs["tallies_present"] = h5::scalar(static_cast<long long>(m.tallies.empty() ? 0 : 1));
+  root.attrs["source_present"] = h5::scalar(0LL);
+  root.dataset("seed", h5::scalar(static_cast<long long>(s.seed)));
+  {
+    h5::Value st = h5::scalar(static_cast<long long>(s.stride));
+    st.kind = 'u';
+    root.dataset("stride", st);
+  }
+  root.dataset("energy_mode", h5::string("continuous-energy"));
+  root.dataset("run_mode", h5::string(m.eigenvalue ? "eigenvalue" : "fixed source"));
+  root.dataset("n_particles", h5::scalar(static_cast<long long>(m.n_particles)));
+  root.dataset("n_batches", h5::scalar(static_cast<long long>(m.n_batches)));
+  root.dataset("current_batch", h5::scalar(static_cast<long long>(current_batch)));
+  if (m.eigenvalue) {
+    root.dataset("n_inactive", h5::scalar(static_cast<long long>(m.n_inactive)));
+    root.dataset("generations_per_batch", h5::scalar(1LL));
+    root.dataset("k_generation", h5::array(s.k_generation));
+    root.dataset("entropy", h5::array(std::vector<double> {}));
+    root.dataset("k_col_abs", h5::scalar(s.k_col_abs));
+    root.dataset("k_col_tra", h5::scalar(s.k_col_tra));
+    root.dataset("k_abs_tra", h5::scalar(s.k_abs_tra));
+    double kc[2];
+    openmc_get_keff(kc);
+    root.dataset("k_combined", h5::array(std::vector<double> {kc[0], kc[1]}));
+  }
+  root.dataset("n_realizations", h5::scalar(static_cast<long long>(n_realizations)));
+  {
+    std::vector<double> gt;
+    for (int t = 0; t < 4; ++t) {
+      gt.push_back(s.global_tallies[3 * t + 1]);
+      gt.push_back(s.global_tallies[3 * t + 2]);
+    }
+    root.dataset("global_tallies", h5::array(gt, {4, 2}));
+  }
+  h5::WNode& tg = root.group_at("tallies");
+  std::vector<int> tally_ids, mesh_ids, filter_ids;
+  for (const auto& t : m.tallies)
+    if (!t.generated) tally_ids.push_back(t.id);
+  tg.attrs["n_tallies"] = h5::scalar(static_cast<long long>(tally_ids.size()));
+  tg.attrs["ids"] = int_array(tally_ids);
+  h5::WNode& mg = tg.group_at("meshes");
+  for (const auto& mesh : m.meshes) {
+    mesh_ids.push_back(mesh.id);
+    h5::WNode& g = mg.group_at("mesh " + std::to_string(mesh.id));
+    g.attrs["id"] = h5::scalar(static_cast<long long>(mesh.id));
+    g.dataset("name", h5::string(""));
+    g.dataset("type", h5::string("regular"));
+    g.dataset("dimension", int_array(std::vector<int>(mesh.shape, mesh.shape + mesh.ndim)));
+    g.dataset("lower_left", h5::array(std::vector<double>(mesh.ll, mesh.ll + mesh.ndim)));
+    g.dataset("upper_right", h5::array(std::vector<double>(mesh.ur, mesh.ur + mesh.ndim)));
+    g.dataset("width", h5::array(std::vector<double>(mesh.width, mesh.width + mesh.ndim)));
+  }
+  mg.attrs["n_meshes"] = h5::scalar(static_cast<long long>(mesh_ids.size()));
+  mg.attrs["ids"] = int_array(mesh_ids);
+  h5::WNode& fg = tg.group_at("filters");
+  static const char* ftype[] = {"mesh", "energy", "particle", "cell", "material"};
+  for (const auto& f : m.filters) {
+    filter_ids.push_back(f.id);
+    h5::WNode& g = fg.group_at("filter " + std::to_string(f.id));
+    g.dataset("type", h5::string(ftype[f.type]));
+    g.dataset("n_bins", h5::scalar(static_cast<long long>(f.nbins)));
+    if (f.type == FILTER_MESH) {
+      g.dataset("bins", h5::scalar(static_cast<long long>(m.meshes[f.mesh].id)));
+    } else if (f.type == FILTER_ENERGY) {
+      g.dataset("bins", h5::array(f.bins));
+    } else if (f.type == FILTER_CELL || f.type == FILTER_MATERIAL) {
+      std::vector<int> ids;
+      for (int i : f.ids) ids.push_back(f.type == FILTER_CELL ? m.cells[i].id : m.materials[i].id);
+      g.dataset("bins", int_array(ids));
+    } else {
+      g.dataset("bins", strings({"neutron"}));
+    }
+  }
+  fg.attrs["n_filters"] = h5::scalar(static_cast<long long>(filter_ids.size()));
+  fg.attrs["ids"] = int_array(filter_ids);
+  static const char* sname[] = {"flux", "total", "absorption"};
+  for (const auto& t : m.tallies) {
+    if (t.generated) continue;
+    h5::WNode& g = tg.group_at("tally " + std::to_string(t.id));
+    g.attrs["internal"] = h5::scalar(0LL);
+    g.attrs["multiply_density"] = h5::scalar(1LL);
+    g.attrs["higher_moments"] = h5::scalar(0LL);
+    g.dataset("n_realizations", h5::scalar(static_cast<long long>(t.n_realizations)));
+    g.dataset("n_filters", h5::scalar(static_cast<long long>(t.filters.size())));
+    std::vector<int> fids;
+    for (int fi : t.filters) fids.push_back(m.filters[fi].id);
+    g.dataset("filters", int_array(fids));
+    g.dataset("nuclides", strings({"total"}));
+    g.dataset("estimator", h5::string(t.estimator == EST_COLLISION ? "collision" : "tracklength"));
+    g.dataset("n_score_bins", h5::scalar(static_cast<long long>(t.scores.size())));
+    std::vector<std::string> sc;
+    for (int k : t.scores) sc.push_back(sname[k]);
+    g.dataset("score_bins", strings(sc));
+    const int64_t ns = static_cast<int64_t>(t.scores.size());
+    std::vector<double> res(static_cast<size_t>(t.n_filter_bins * ns * 2));
+    for (int64_t k = 0; k < t.n_filter_bins * ns && 3 * k + 2 < static_cast<int64_t>(t.results.size()); ++k) {
+      res[2 * k] = t.results[3 * k + 1];
+      res[2 * k + 1] = t.results[3 * k + 2];
+    }
+    g.dataset("results", h5::array(res, {static_cast<uint64_t>(t.n_filter_bins), static_cast<uint64_t>(ns), 2}));
+  }
+  h5::WNode& rt = root.group_at("runtime");
+  rt.dataset("simulation", h5::scalar(s.time_active + s.time_inactive));
+  rt.dataset("transport", h5::scalar(s.time_active + s.time_inactive));
+  rt.dataset("inactive batches", h5::scalar(s.time_inactive));
+  rt.dataset("active batches", h5::scalar(s.time_active));
+  h5::write(path, root);
+}
+
+// The default statepoint name: <output path>/statepoint.<batch, zero-padded
+// to the width of n_batches>.h5 (src/state_point.cpp:46-51)
+std::string default_statepoint_name(const HModel& m)
+{
+  const std::string dir = m.path_output.empty() ? std::string(".") : m.path_output;
+  const int w = static_cast<int>(std::to_string(m.n_batches).size());
+  char buf[32];
+  std::snprintf(buf, sizeof(buf), "%0*d", w, current_batch);
+  return dir + "/statepoint." + buf + ".h5";
+}
+
 }  // namespace
+
+// src/state_point.cpp:36-357: tallies are copied from the device first;
+// filename null gives the default name
+int openmc_statepoint_write(const char* filename, bool* write_source)
+{
+  (void)write_source;  // no source bank is written
+  State& s = S();
+  if (!s.model_loaded) return fail(OPENMC_E_ALLOCATE, "OpenMC has not been initialized.");
+  try {
+    if (s.gpu) gpu_fetch_tallies(s.gpu, s.model);
+    write_statepoint(filename ? std::string(filename) : default_statepoint_name(s.model));
+    return 0;
+  } catch (const std::exception& e) {
+    return fail(OPENMC_E_UNASSIGNED, e.what());
+  }
+}
 
 int openmc_simulation_finalize()
 {

@@ -282,9 +282,6 @@ int openmc_sphharm_filter_set_order(int32_t index, int order)
 int openmc_statepoint_load(const char* filename)
 { return off_path("openmc_statepoint_load"); }
 
-int openmc_statepoint_write(const char* filename, bool* write_source)
-{ return off_path("openmc_statepoint_write"); }
-
 int openmc_tally_reset(int32_t index)
 { return off_path("openmc_tally_reset"); }
 

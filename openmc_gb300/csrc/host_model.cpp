@@ -13,6 +13,8 @@
 //               neither machine has HDF5 (field list in openmc_gb300/data.py).
 #include "host_model.h"
 
+#include "h5lite.h"
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -56,8 +58,131 @@ std::string join(const std::string& dir, const std::string& f)
   return dir + "/" + f;
 }
 
+// src/nuclide.cpp:359-453 create_derived from the MT 2, 18 (may be empty) and
+// 102 cross sections on the nuclide's grid
+void derive_columns(HNuclide& nuc, std::vector<double> el, const std::vector<double>& fis,
+                    const std::vector<double>& cap)
+{
+  const size_t G = nuc.energy.size();
+  // src/nuclide.cpp:359-453: total and absorption start at zero; the
+  // reactions are added in name (MT) order: MT 2 to total; MT 18 to total,
+  // fission and absorption; MT 102 (disappearance) to total and absorption;
+  // then nu_fission = nu(E) x fission per grid point (Polynomial, Horner in
+  // increasing powers, src/endf.cpp:125-134)
+  nuc.total.assign(G, 0.0);
+  nuc.absorption.assign(G, 0.0);
+  nuc.fission.assign(G, 0.0);
+  nuc.nu_fission.assign(G, 0.0);
+  for (size_t k = 0; k < G; ++k) nuc.total[k] += el[k];
+  if (!fis.empty()) {
+    for (size_t k = 0; k < G; ++k) {
+      nuc.total[k] += fis[k];
+      nuc.fission[k] += fis[k];
+      nuc.absorption[k] += fis[k];
+    }
+  }
+  for (size_t k = 0; k < G; ++k) {
+    nuc.total[k] += cap[k];
+    nuc.absorption[k] += cap[k];
+  }
+  if (!fis.empty()) {
+    for (size_t k = 0; k < G; ++k) {
+      double y = 0.0;
+      for (int c = 1; c >= 0; --c) y = y * nuc.energy[k] + nuc.nu_c[c];
+      nuc.nu_fission[k] = y * nuc.fission[k];
+    }
+  }
+  nuc.elastic = std::move(el);
+}
+
+// One nuclide in OpenMC's incident-neutron HDF5 layout
+// (docs/source/io_formats/nuclear_data.rst; src/nuclide.cpp:60-352 reads the
+// same fields): atomic weight ratio, the one temperature's kT and energy
+// grid, the MT 2 / 18 / 102 cross sections with threshold index 0 on that
+// grid, and for MT 18 the prompt neutron product's Polynomial yield and
+// uncorrelated Maxwell or Watt spectrum with constant parameters.
+void read_nuclide_h5(const std::string& path, HNuclide& nuc)
+{
+  h5::File f(path);
+  const h5::Node root = f.root();
+  std::string gname = nuc.name;
+  if (!root.has(gname)) {
+    const auto names = root.children();
+    if (names.size() != 1) throw std::runtime_error(path + ": no group for nuclide " + nuc.name);
+    gname = names[0];
+  }
+  const h5::Node g = root.at(gname);
+  nuc.awr = g.attr("atomic_weight_ratio").doubles().at(0);
+  const auto temps = g.at("kTs").children();
+  if (temps.size() != 1) throw std::runtime_error(path + ": one temperature per nuclide is supported");
+  const std::string T = temps[0];
+  nuc.kT = g.at("kTs/" + T).read().doubles().at(0);
+  nuc.energy = g.at("energy/" + T).read().doubles();
+  const size_t G = nuc.energy.size();
+  std::vector<double> el, fis, cap;
+  const h5::Node rxs = g.at("reactions");
+  for (const std::string& name : rxs.children()) {
+    if (name.rfind("reaction_", 0) != 0) continue;
+    const h5::Node rx = rxs.at(name);
+    const long long mt = rx.attr("mt").ints().at(0);
+    if (rx.has_attr("redundant") && rx.attr("redundant").ints().at(0) != 0) continue;
+    const h5::Node xs = rx.at(T + "/xs");
+    const long long thr = xs.has_attr("threshold_idx") ? xs.attr("threshold_idx").ints().at(0) : 0;
+    std::vector<double> v = xs.read().doubles();
+    if (thr != 0 || v.size() != G) throw std::runtime_error(path + ": threshold reactions are not supported");
+    if (mt == 2) {
+      el = std::move(v);
+    } else if (mt == 102) {
+      cap = std::move(v);
+    } else if (mt == 18) {
+      fis = std::move(v);
+      const h5::Node prod = rx.at("product_0");
+      const std::vector<double> yc = prod.at("yield").read().doubles();
+      if (yc.empty() || yc.size() > 2) throw std::runtime_error(path + ": fission yield must be a polynomial of degree <= 1");
+      nuc.nu_c[0] = yc[0];
+      nuc.nu_c[1] = yc.size() > 1 ? yc[1] : 0.0;
+      const h5::Node en = prod.at("distribution_0/energy");
+      const std::string type = en.attr("type").str();
+      nuc.u = en.attr("u").doubles().at(0);
+      // a constant Tabulated1D parameter: [[x...], [y...]] with equal y
+      auto constant = [&](const char* ds) {
+        const std::vector<double> t = en.at(ds).read().doubles();
+        const size_t n = t.size() / 2;
+        if (n == 0) throw std::runtime_error(path + ": empty spectrum parameter");
+        for (size_t k = n; k < t.size(); ++k)
+          if (t[k] != t[n]) throw std::runtime_error(path + ": energy-dependent spectrum parameters are not supported");
+        return t[n];
+      };
+      if (type == "maxwell") {
+        nuc.spectrum = 1;
+        nuc.sp[0] = constant("theta");
+      } else if (type == "watt") {
+        nuc.spectrum = 2;
+        nuc.sp[0] = constant("a");
+        nuc.sp[1] = constant("b");
+      } else {
+        throw std::runtime_error(path + ": fission spectrum '" + type + "' is not supported");
+      }
+      nuc.fissionable = true;
+    } else {
+      throw std::runtime_error(path + ": only MT 2, MT 18 and MT 102 are supported");
+    }
+  }
+  if (el.empty() || cap.empty()) throw std::runtime_error(path + ": needs MT 2 and MT 102");
+  derive_columns(nuc, std::move(el), fis, cap);
+}
+
 void read_nuclide_file(const std::string& path, HNuclide& nuc)
 {
+  {
+    std::ifstream probe(path, std::ios::binary);
+    char sig[8] = {0};
+    probe.read(sig, 8);
+    if (std::memcmp(sig, "\x89HDF\r\n\x1a\n", 8) == 0) {
+      read_nuclide_h5(path, nuc);
+      return;
+    }
+  }
   std::string b = read_file(path);
   if (b.size() < 16 || std::memcmp(b.data(), "OMCGBNUC", 8) != 0)
     throw std::runtime_error(path + ": not a nuclide file");
@@ -110,35 +235,7 @@ void read_nuclide_file(const std::string& path, HNuclide& nuc)
     if (nuc.spectrum != 1 && nuc.spectrum != 2) throw std::runtime_error(path + ": unknown fission spectrum");
   }
   if (nuc.fissionable != !fis.empty()) throw std::runtime_error(path + ": MT 18 needs its fission neutron data");
-  // src/nuclide.cpp:359-453: total and absorption start at zero; the
-  // reactions are added in name (MT) order: MT 2 to total; MT 18 to total,
-  // fission and absorption; MT 102 (disappearance) to total and absorption;
-  // then nu_fission = nu(E) x fission per grid point (Polynomial, Horner in
-  // increasing powers, src/endf.cpp:125-134)
-  nuc.total.assign(G, 0.0);
-  nuc.absorption.assign(G, 0.0);
-  nuc.fission.assign(G, 0.0);
-  nuc.nu_fission.assign(G, 0.0);
-  for (uint32_t k = 0; k < G; ++k) nuc.total[k] += el[k];
-  if (!fis.empty()) {
-    for (uint32_t k = 0; k < G; ++k) {
-      nuc.total[k] += fis[k];
-      nuc.fission[k] += fis[k];
-      nuc.absorption[k] += fis[k];
-    }
-  }
-  for (uint32_t k = 0; k < G; ++k) {
-    nuc.total[k] += cap[k];
-    nuc.absorption[k] += cap[k];
-  }
-  if (!fis.empty()) {
-    for (uint32_t k = 0; k < G; ++k) {
-      double y = 0.0;
-      for (int c = 1; c >= 0; --c) y = y * nuc.energy[k] + nuc.nu_c[c];
-      nuc.nu_fission[k] = y * nuc.fission[k];
-    }
-  }
-  nuc.elastic = std::move(el);
+  derive_columns(nuc, std::move(el), fis, cap);
 }
 
 // Region string -> tokens (src/cell.cpp:556-683).  Simple regions keep the

@@ -216,6 +216,65 @@ def write_nuclide(nuc: Nuclide, path: str | Path) -> None:
             f.write(struct.pack("<3d", *fis.params, fis.u))
 
 
+def write_nuclide_h5(nuc: Nuclide, path: str | Path) -> None:
+    """Write a nuclide in OpenMC's incident-neutron HDF5 layout
+    (docs/source/io_formats/nuclear_data.rst; what
+    openmc.data.IncidentNeutron.export_to_hdf5 writes): the energy grid and
+    kT under the temperature's name, one group per reaction with its
+    cross section and threshold index, the elastic product (isotropic in the
+    centre of mass), and for MT 18 the prompt neutron product with its
+    Polynomial yield and an uncorrelated Maxwell or Watt energy
+    distribution whose parameters are constant Tabulated1D functions."""
+    from . import h5
+    T = f"{int(round(nuc.kT / K_BOLTZMANN))}K"
+    e_lo, e_hi = float(nuc.energy[0]), float(nuc.energy[-1])
+
+    def const(v):
+        return h5.Dataset(np.array([[e_lo, e_hi], [v, v]]),
+                          {"type": np.bytes_(b"Tabulated1D"), "breakpoints": np.array([2], np.int32),
+                           "interpolation": np.array([2], np.int32)})
+
+    labels = {MT_ELASTIC: "(n,elastic)", MT_FISSION: "(n,fission)", MT_CAPTURE: "(n,gamma)"}
+    reactions = h5.Node()
+    for mt in sorted(nuc.reactions):
+        thr, xs = nuc.reactions[mt]
+        rx = h5.Node({T: h5.Node({"xs": h5.Dataset(np.asarray(xs, np.float64),
+                                                   {"threshold_idx": np.int32(thr)})})},
+                     {"mt": np.int32(mt), "label": np.bytes_(labels.get(mt, f"MT {mt}").encode()),
+                      "Q_value": 0.0, "center_of_mass": np.int32(1 if mt == MT_ELASTIC else 0),
+                      "redundant": np.int32(0)})
+        n_product = 0
+        if mt == MT_ELASTIC:
+            rx["product_0"] = h5.Node({"yield": h5.Dataset(np.array([1.0]), {"type": np.bytes_(b"Polynomial")}),
+                                       "distribution_0": h5.Node({}, {"type": np.bytes_(b"uncorrelated")})},
+                                      {"particle": np.bytes_(b"neutron"), "emission_mode": np.bytes_(b"prompt"),
+                                       "decay_rate": 0.0, "n_distribution": np.int32(1)})
+            n_product = 1
+        elif mt == MT_FISSION and nuc.fission is not None:
+            f = nuc.fission
+            if f.spectrum == SPECTRUM_MAXWELL:
+                energy = h5.Node({"theta": const(f.params[0])}, {"type": np.bytes_(b"maxwell"), "u": f.u})
+            else:
+                energy = h5.Node({"a": const(f.params[0]), "b": const(f.params[1])},
+                                 {"type": np.bytes_(b"watt"), "u": f.u})
+            rx["product_0"] = h5.Node(
+                {"yield": h5.Dataset(np.array(f.nu, np.float64), {"type": np.bytes_(b"Polynomial")}),
+                 "distribution_0": h5.Node({"energy": energy}, {"type": np.bytes_(b"uncorrelated")})},
+                {"particle": np.bytes_(b"neutron"), "emission_mode": np.bytes_(b"prompt"), "decay_rate": 0.0,
+                 "n_distribution": np.int32(1)})
+            n_product = 1
+        rx.attrs["n_product"] = np.int32(n_product)
+        reactions[f"reaction_{mt:03d}"] = rx
+    group = h5.Node({"energy": h5.Node({T: np.asarray(nuc.energy, np.float64)}),
+                     "kTs": h5.Node({T: np.float64(nuc.kT)}),
+                     "reactions": reactions},
+                    {"Z": np.int32(0), "A": np.int32(int(round(nuc.A))), "metastable": np.int32(0),
+                     "atomic_weight_ratio": float(nuc.awr), "n_reaction": np.int32(len(nuc.reactions))})
+    root = h5.Node({nuc.name: group}, {"filetype": np.bytes_(b"data_neutron"),
+                                       "version": np.array([3, 0], np.int32)})
+    h5.write(path, root)
+
+
 def read_nuclide(path: str | Path) -> Nuclide:
     buf = Path(path).read_bytes()
     if buf[:8] != MAGIC:
@@ -244,14 +303,19 @@ def read_nuclide(path: str | Path) -> Nuclide:
     return nuc
 
 
-def write_library(nuclides, directory: str | Path) -> Path:
-    """Write nuclide files plus a ``cross_sections.xml`` (OpenMC schema)."""
+def write_library(nuclides, directory: str | Path, fmt: str = "native") -> Path:
+    """Write nuclide files plus a ``cross_sections.xml`` (OpenMC schema);
+    fmt "h5" writes OpenMC's HDF5 layout (write_nuclide_h5) instead of the
+    native container."""
     directory = Path(directory)
     directory.mkdir(parents=True, exist_ok=True)
     root = ET.Element("cross_sections")
     for nuc in nuclides:
-        fname = f"{nuc.name}.nuc"
-        write_nuclide(nuc, directory / fname)
+        fname = f"{nuc.name}.h5" if fmt == "h5" else f"{nuc.name}.nuc"
+        if fmt == "h5":
+            write_nuclide_h5(nuc, directory / fname)
+        else:
+            write_nuclide(nuc, directory / fname)
         ET.SubElement(root, "library", materials=nuc.name, path=fname,
                       type="neutron")
     ET.indent(root)

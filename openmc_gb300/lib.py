@@ -124,6 +124,7 @@ _fn("openmc_finalize", [])
 _fn("openmc_reset", [])
 _fn("openmc_hard_reset", [])
 _fn("openmc_reset_timers", [])
+_fn("openmc_statepoint_write", [C.c_char_p, _p(C.c_bool)])
 _fn("openmc_get_seed", [], C.c_int64)
 _fn("openmc_set_seed", [C.c_int64], None)
 _fn("openmc_get_stride", [], C.c_uint64)
@@ -552,6 +553,14 @@ def keff():
     k = (C.c_double * 2)()
     _dll.openmc_get_keff(k)
     return k[0], k[1]
+
+
+def statepoint_write(filename=None, write_source=True):
+    """Write a statepoint file (openmc/lib/core.py: statepoint_write); no
+    source bank is written.  filename None: statepoint.<batch>.h5 in the
+    output path."""
+    flag = C.c_bool(bool(write_source))
+    _dll.openmc_statepoint_write(None if filename is None else str(filename).encode(), C.byref(flag))
 
 
 def k_generation():

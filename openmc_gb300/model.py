@@ -710,8 +710,9 @@ class Model:
 
         Mirrors ``Model.run`` (``openmc/model/model.py:755-900``): exports the
         XML, initialises the library in ``cwd``, sets ``event_based`` when
-        given, runs all batches and returns the tally means as a dict keyed by
-        tally id (the library writes no statepoint file).
+        given, runs all batches and returns the path of the statepoint file
+        written at the last batch (read it with
+        :class:`openmc_gb300.statepoint.StatePoint`).
         """
         from . import lib
         cwd = Path(cwd)
@@ -724,9 +725,7 @@ class Model:
             if event_based is not None:
                 lib.settings.event_based = bool(event_based)
             lib.run()
-            out = {}
-            for t in self.tallies:
-                out[t.id] = lib.tally_mean_std(t.id)
-            return out
+            w = len(str(int(self.settings.batches)))
+            return cwd / f"statepoint.{lib.current_batch():0{w}d}.h5"
         finally:
             lib.finalize()

@@ -81,6 +81,8 @@ def lib(timing=False):
         L.oracle_future_seed.argtypes = [C.c_uint64, C.c_uint64]
         L.oracle_init_seed.restype = C.c_uint64
         L.oracle_init_seed.argtypes = [i64, C.c_int, i64, C.c_uint64]
+        L.oracle_lower_bound_index.restype = C.c_int64
+        L.oracle_lower_bound_index.argtypes = [C.POINTER(C.c_double), C.c_int64, dbl]
         L.oracle_maxwell_spectrum.restype = dbl
         L.oracle_maxwell_spectrum.argtypes = [dbl, pu64]
         L.oracle_watt_spectrum.restype = dbl
@@ -105,7 +107,8 @@ def lib(timing=False):
 
 
 def ref_lib():
-    """The reference's random_lcg.cpp compiled from source, or None."""
+    """The reference's random_lcg.cpp and random_dist.cpp compiled from
+    source, or None."""
     if not REF_PATH.exists():
         return None
     L = C.CDLL(str(REF_PATH))
@@ -115,6 +118,16 @@ def ref_lib():
     L.ref_future_seed.argtypes = [C.c_uint64, C.c_uint64]
     L.ref_init_seed.restype = C.c_uint64
     L.ref_init_seed.argtypes = [C.c_int64, C.c_int, C.c_int64, C.c_uint64]
+    pu64 = C.POINTER(C.c_uint64)
+    if hasattr(L, "ref_lower_bound_index"):
+        L.ref_lower_bound_index.restype = C.c_int64
+        L.ref_lower_bound_index.argtypes = [C.POINTER(C.c_double), C.c_int64, C.c_double]
+    for name, args in (("ref_uniform", [C.c_double, C.c_double, pu64]), ("ref_maxwell", [C.c_double, pu64]),
+                       ("ref_watt", [C.c_double, C.c_double, pu64]),
+                       ("ref_normal", [C.c_double, C.c_double, pu64])):
+        if hasattr(L, name):  # built from random_dist.cpp as well
+            getattr(L, name).restype = C.c_double
+            getattr(L, name).argtypes = args
     return L
 
 

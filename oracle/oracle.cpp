@@ -2714,6 +2714,10 @@ uint64_t oracle_init_seed(int64_t id, int offset, int64_t master, uint64_t strid
   rc.stride = stride;
   return init_seed(rc, id, offset);
 }
+int64_t oracle_lower_bound_index(const double* first, int64_t n, double value)
+{
+  return lower_bound_index(first, first + n, value);
+}
 double oracle_maxwell_spectrum(double T, uint64_t* seed) { return maxwell_spectrum(T, seed); }
 double oracle_watt_spectrum(double a, double b, uint64_t* seed) { return watt_spectrum(a, b, seed); }
 void oracle_rotate_angle(double* uvw, double mu, const double* phi, uint64_t* seed)

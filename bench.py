@@ -318,6 +318,11 @@ def run_gb300(args, barrier=lambda: None, rank=0):
         lib.init(directory=path)
         try:
             lib.settings.xs_fp32 = 0
+            # its own random streams: the two tallies are then independent
+            # estimates, so that each bin's z follows the t law the
+            # comparison's expected shares assume (with shared seeds the
+            # runs are correlated and the z values come out smaller)
+            lib.settings.seed = 1001 + rank
             lib.settings.particles_in_flight = args.in_flight
             lib.simulation_init()
             # as many batches as the FP32 tally holds at least (warm-up +
@@ -333,6 +338,7 @@ def run_gb300(args, barrier=lambda: None, rank=0):
             t64 = lib.tally_ids()[0]
             out["fp32_vs_fp64"] = compare_tallies(fp32_tally, lib.tally_mean_std(t64), fp32_n,
                                                   lib.tally_n_realizations(t64))
+            out["fp32_vs_fp64"]["seeds"] = {"fp32": 1 + rank, "fp64": 1001 + rank}
         finally:
             lib.finalize()
         # the same batch through the history-based kernel (settings.event_based = False)

@@ -169,18 +169,66 @@ struct DModel {
   int stage_bytes;
 };
 
-// Structure-of-arrays particle bank; level-major arrays are [MAXL][cap].
+// Particle bank, one slot per particle in flight.  The fields an event
+// reads together sit together: slots are reached through a sorted queue, so
+// the 32 lanes of a warp read 32 unrelated slots, and each field that lives
+// in its own array costs a 32-byte memory sector per lane however few bytes
+// it holds.  The hot fields are therefore packed into 16- and 32-byte
+// records per slot (per level and slot for the coordinate levels: index
+// l * cap + s), and reached through strided pointers so that every access
+// reads db.f[k] as with plain arrays; the rest stay in arrays of their own.
+// Counters that an event updates after it has stored a record (event count,
+// collision count) and the particle id stay out of the records: reading a
+// record back right after storing part of it waits for the store.
+template<class T, int STRIDE>
+struct Strided {
+  T* p;  // the field in record 0
+  __host__ __device__ __forceinline__ T& operator[](long long k) const
+  {
+    return *reinterpret_cast<T*>(reinterpret_cast<char*>(p) + k * STRIDE);
+  }
+};
+
+struct alignas(32) BankDir {  // direction and energy
+  double ux, uy, uz, E;
+};
+struct alignas(32) BankHot {  // random stream, weight, macroscopic total and absorption
+  unsigned long long seed;
+  double wgt, macro_t, macro_a;
+};
+struct alignas(16) BankMisc {  // coordinate depth, surface and materials
+  int n_coord, surface, material, material_last;
+};
+struct alignas(32) BankPos {  // position at one coordinate level
+  double x, y, z, pad;
+};
+struct alignas(32) BankIdx {  // cell, universe, lattice and lattice indices at one level
+  int cell, univ, latt, lix, liy, liz, pad0, pad1;
+};
+
+template<class T>
+using BField = Strided<T, 32>;
+template<class T>
+using BField16 = Strided<T, 16>;
+
 struct DBank {
   long long cap;
+  BankPos* pos;  // the records themselves, for whole-record loads and stores
+  BankIdx* idx;
+  BankDir* dir;
+  BankHot* hot;
+  BankMisc* misc;
   long long* id;
-  unsigned long long* seed;
-  double *E, *wgt, *wgt_born, *wgt_ww_born, *ww_factor;
-  double *ux, *uy, *uz;
-  double *rx, *ry, *rz;
-  int *cell, *univ, *latt, *lix, *liy, *liz;
-  int *n_coord, *cell_last0, *cell_born;
-  int *surface, *material, *material_last;
-  double *macro_t, *macro_a;
+  BField<unsigned long long> seed;
+  BField<double> E, wgt;
+  double *wgt_born, *wgt_ww_born, *ww_factor;
+  BField<double> ux, uy, uz;
+  BField<double> rx, ry, rz;
+  BField<int> cell, univ, latt, lix, liy, liz;
+  BField16<int> n_coord;
+  int *cell_last0, *cell_born;
+  BField16<int> surface, material, material_last;
+  BField<double> macro_t, macro_a;
   double* macro_nf;                  // macroscopic nu-fission (eigenvalue runs)
   double *k_col, *k_abs, *k_tra;     // the history's k-effective scores (eigenvalue runs)
   int* n_progeny;                    // fission sites the history has banked
@@ -273,6 +321,7 @@ struct DQueues {
   int* q_surf;
   int* q_coll;
   int* q_tmp;
+  int* key_tmp;  // sort key of each q_tmp entry, written with it (null: queue not sorted)
   int* free_list;
   int* hist;
   int* cursor;
@@ -824,6 +873,7 @@ __device__ __forceinline__ bool lattice_valid(const DLattice& lat, const int* i)
 struct Geo {
   double r[MAXL][3];
   double u[3];
+  double E;  // loaded with the direction (geo_store does not write it)
   int cell[MAXL], univ[MAXL], lat[MAXL], li[MAXL][3];
   int n_coord;
   int surface;
@@ -847,27 +897,32 @@ __device__ __forceinline__ T lvl_get(const T (&a)[MAXL], int l)
 __device__ inline void geo_load(Geo& g, long long s)
 {
   const long long cap = db.cap;
-  g.n_coord = db.n_coord[s];
-  g.u[0] = db.ux[s];
-  g.u[1] = db.uy[s];
-  g.u[2] = db.uz[s];
+  const BankMisc mi = db.misc[s];
+  const BankDir d = db.dir[s];
+  g.n_coord = mi.n_coord;
+  g.u[0] = d.ux;
+  g.u[1] = d.uy;
+  g.u[2] = d.uz;
+  g.E = d.E;
 #pragma unroll
   for (int l = 0; l < MAXL; ++l) {
     if (l >= g.n_coord) break;
     long long k = l * cap + s;
-    g.r[l][0] = db.rx[k];
-    g.r[l][1] = db.ry[k];
-    g.r[l][2] = db.rz[k];
-    g.cell[l] = db.cell[k];
-    g.univ[l] = db.univ[k];
-    g.lat[l] = db.latt[k];
-    g.li[l][0] = db.lix[k];
-    g.li[l][1] = db.liy[k];
-    g.li[l][2] = db.liz[k];
+    const BankPos p = db.pos[k];
+    const BankIdx x = db.idx[k];
+    g.r[l][0] = p.x;
+    g.r[l][1] = p.y;
+    g.r[l][2] = p.z;
+    g.cell[l] = x.cell;
+    g.univ[l] = x.univ;
+    g.lat[l] = x.latt;
+    g.li[l][0] = x.lix;
+    g.li[l][1] = x.liy;
+    g.li[l][2] = x.liz;
   }
-  g.surface = db.surface[s];
-  g.material = db.material[s];
-  g.material_last = db.material_last[s];
+  g.surface = mi.surface;
+  g.material = mi.material;
+  g.material_last = mi.material_last;
 }
 
 __device__ inline void geo_store(const Geo& g, long long s)
@@ -881,15 +936,21 @@ __device__ inline void geo_store(const Geo& g, long long s)
   for (int l = 0; l < MAXL; ++l) {
     if (l >= g.n_coord) break;
     long long k = l * cap + s;
-    db.rx[k] = g.r[l][0];
-    db.ry[k] = g.r[l][1];
-    db.rz[k] = g.r[l][2];
-    db.cell[k] = g.cell[l];
-    db.univ[k] = g.univ[l];
-    db.latt[k] = g.lat[l];
-    db.lix[k] = g.li[l][0];
-    db.liy[k] = g.li[l][1];
-    db.liz[k] = g.li[l][2];
+    BankPos p;
+    p.x = g.r[l][0];
+    p.y = g.r[l][1];
+    p.z = g.r[l][2];
+    p.pad = 0.0;
+    db.pos[k] = p;
+    BankIdx x;
+    x.cell = g.cell[l];
+    x.univ = g.univ[l];
+    x.latt = g.lat[l];
+    x.lix = g.li[l][0];
+    x.liy = g.li[l][1];
+    x.liz = g.li[l][2];
+    x.pad0 = x.pad1 = 0;
+    db.idx[k] = x;
   }
   db.surface[s] = g.surface;
   db.material[s] = g.material;

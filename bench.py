@@ -170,24 +170,28 @@ def peaks():
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic
 # byte of each kernel, from an ncu capture of one launch of the same kernel
-# (iteration 100 of a 2x10^6-history lattice batch, 524,288 slots), matched
-# with that launch's OPENMC_GB300_LAUNCH_LOG counts; the unfused kernels'
-# ratios come from a capture of the unfused kernels.  Traffic per launch
-# scales with the events a launch processes.
-TRAFFIC_PER_ALGORITHMIC_BYTE = {"xs+advance+surface": 2.333, "xs+advance": 1.376, "surface": 1.406,
-                                "collision": 1.258}
+# (iteration 100 of a 2x10^6-history lattice batch, 524,288 slots; particle
+# bank packed into per-slot records), matched with that launch's
+# OPENMC_GB300_LAUNCH_LOG counts; the unfused kernels' ratios come from a
+# capture of the unfused kernels of the unpacked bank.  Traffic per launch
+# scales with the events a launch processes.  The track-length tally kernel
+# reads the 96-byte track records, traffic of this design beyond its 16
+# algorithmic bytes per mesh segment.
+TRAFFIC_PER_ALGORITHMIC_BYTE = {"xs+advance+surface": 1.028, "xs+advance": 1.376, "surface": 1.406,
+                                "collision": 1.270, "tally": 6.275}
 
 # What bounds the transport kernels instead of HBM: the FP64 pipe's busy
 # fraction in the same captures (a committed profile, not measured by this run).
 _CAPTURE = "ncu --set full, iteration 100 of a 2e6-history lattice batch, 524,288 slots"
 FP64_PIPE_NOTE = {
-    "xs+advance+surface": {"fp64_pipe_busy": 0.615, "dram_busy": 0.185, "source": _CAPTURE},
-    "collision": {"fp64_pipe_busy": 0.623, "dram_busy": 0.046, "source": _CAPTURE},
+    "xs+advance+surface": {"fp64_pipe_busy": 0.619, "dram_busy": 0.139, "source": _CAPTURE},
+    "collision": {"fp64_pipe_busy": 0.571, "dram_busy": 0.050, "source": _CAPTURE},
+    "tally": {"fp64_pipe_busy": 0.691, "dram_busy": 0.071, "source": _CAPTURE},
 }
 
 
 def algorithmic_bytes(detail, levels, fp32, deferred=True):
-    """Bytes each kernel must move per batch: the structure-of-arrays fields
+    """Bytes each kernel must move per batch: the particle-state fields
     an event reads and writes, the table bytes of each nuclide lookup (two
     hash-window bounds, two bracketing energies, two table rows, nuclide
     index, atom density) and 16 B of tally read-modify-write per mesh

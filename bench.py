@@ -60,6 +60,9 @@ def parse():
                     help="skip the shield figure-of-merit extra (plain, MAGIC and learned windows)")
     ap.add_argument("--network-only", action="store_true",
                     help="only time the importance network's training kernels (for kernel profilers)")
+    ap.add_argument("--precision-only", type=int, default=0, metavar="BATCHES",
+                    help="only compare FP32 with FP64 tables on the lattice: BATCHES batches each on "
+                         "independent seeds, beside two FP64 runs on independent seeds as the control")
     ap.add_argument("--no-contract", action="store_true",
                     help="FP32-table mode on the transport build with separately rounded FP64 multiplies "
                          "and adds (default: the build with fused multiply-adds)")
@@ -537,6 +540,38 @@ def cpu_baseline(path, sample, threads=None, mode=1):
     return sample / dt, threads, dt
 
 
+def precision_study(particles, batches):
+    """FP32 against FP64 tables on the lattice flux tally, each run with
+    `batches` batches on its own seeds, and two FP64 runs on independent
+    seeds compared the same way: the FP32 comparison's statistics (share
+    beyond 3 sigma, count beyond 5, mean signed z of converged bins, summed
+    flux) are judged against what the control shows with no FP32 involved."""
+    from openmc_gb300 import lib
+    path = model_dir(particles)
+
+    def run(fp32, seed):
+        lib.init(directory=path)
+        try:
+            lib.settings.xs_fp32 = 1 if fp32 else 0
+            lib.settings.seed = seed
+            lib.simulation_init()
+            for _ in range(batches):
+                lib.next_batch()
+            lib.simulation_finalize()
+            t = lib.tally_ids()[0]
+            return lib.tally_mean_std(t), lib.tally_n_realizations(t)
+        finally:
+            lib.finalize()
+
+    a, na = run(True, 1)
+    b, nb = run(False, 1001)
+    c, nc = run(False, 2001)
+    return {"workload": WORKLOAD, "histories_per_batch": particles, "batches": batches,
+            "seeds": {"fp32": 1, "fp64": 1001, "fp64_control": 2001},
+            "fp32_vs_fp64": compare_tallies(a, b, na, nb),
+            "fp64_vs_fp64_control": compare_tallies(c, b, nc, nb)}
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -594,6 +629,9 @@ def main():
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     if args.network_only:
         print(json.dumps({"importance_network": network_bench(rows=args.particles, steps=args.steps)}))
+        return
+    if args.precision_only:
+        print(json.dumps(precision_study(args.particles, args.precision_only)))
         return
     barrier = (lambda: None)
     if world > 1:

@@ -79,6 +79,11 @@ int openmc_tally_get_id(int32_t index, int32_t* id);
 int openmc_tally_get_n_realizations(int32_t index, int32_t* n);
 int openmc_global_tallies(double** ptr);
 size_t tallies_size(void); /* src/tallies/tally.cpp:1584 */
+int cells_size(void);           /* src/cell.cpp:1820 */
+size_t n_materials(void);       /* src/material.cpp:1599 */
+int n_meshes(void);             /* src/mesh.cpp:3900 */
+size_t nuclides_size(void);     /* src/nuclide.cpp:1105 */
+size_t tally_filters_size(void); /* src/tallies/filter.cpp:62 */
 
 /* ---- weight windows: include/openmc/capi.h:184-221, src/weight_windows.cpp:1020-1340 */
 size_t openmc_weight_windows_size(void);

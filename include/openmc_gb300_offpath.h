@@ -18,6 +18,8 @@ extern "C" {
 
 typedef struct { double x, y, z; } openmc_gb300_position;  /* Position */
 
+void calc_zn(int n, double rho, double phi, double zn[]);
+void calc_zn_rad(int n, double rho, double zn_rad[]);
 int openmc_calculate_volumes(void);
 int openmc_cell_get_density(int32_t index, const int32_t* instance, double* rho);
 int openmc_cell_get_rotation(int32_t index, double rot[], size_t* n);

@@ -33,6 +33,7 @@ extern int32_t n_inactive;
 extern int32_t n_realizations;
 extern double keff;
 extern double keff_std;
+extern int current_batch;
 }
 
 namespace {
@@ -87,7 +88,45 @@ extern "C" {
 // src/eigenvalue.cpp:420-440 (k-effective)
 bool openmc_master() { return true; }
 
-bool openmc_is_statepoint_batch() { return false; }
+// the default statepoint batches: the last one (src/settings.cpp:1008-1017)
+bool openmc_is_statepoint_batch()
+{
+  HModel* m = omc::capi_model();
+  return m && current_batch == m->n_batches;
+}
+
+// ------------------------------------------------------------ model sizes
+// src/cell.cpp:1820, src/material.cpp:1599, src/mesh.cpp:3900,
+// src/nuclide.cpp:1105, src/tallies/filter.cpp:62 (0 before openmc_init)
+int cells_size()
+{
+  HModel* m = omc::capi_model();
+  return m ? static_cast<int>(m->cells.size()) : 0;
+}
+
+size_t n_materials()
+{
+  HModel* m = omc::capi_model();
+  return m ? m->materials.size() : 0;
+}
+
+int n_meshes()
+{
+  HModel* m = omc::capi_model();
+  return m ? static_cast<int>(m->meshes.size()) : 0;
+}
+
+size_t nuclides_size()
+{
+  HModel* m = omc::capi_model();
+  return m ? m->nuclides.size() : 0;
+}
+
+size_t tally_filters_size()
+{
+  HModel* m = omc::capi_model();
+  return m ? m->filters.size() : 0;
+}
 
 int openmc_get_n_batches(int* n_batches, bool get_max_batches)
 {

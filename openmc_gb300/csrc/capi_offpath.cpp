@@ -27,6 +27,16 @@ int off_path(const char* name)
 
 extern "C" {
 
+void calc_zn(int n, double rho, double phi, double zn[])
+{
+  off_path("calc_zn");
+}
+
+void calc_zn_rad(int n, double rho, double zn_rad[])
+{
+  off_path("calc_zn_rad");
+}
+
 int openmc_calculate_volumes()
 { return off_path("openmc_calculate_volumes"); }
 

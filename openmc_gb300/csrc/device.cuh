@@ -30,6 +30,7 @@ constexpr double FP_PRECISION = 1e-14;
 constexpr double FP_REL_PRECISION = 1e-5;
 constexpr double FP_COINCIDENT = 1e-12;
 constexpr double MASS_NEUTRON_EV = 939.56542052e6;
+constexpr double C_LIGHT = 2.99792458e10;  // cm/s
 constexpr int C_NONE = -1;
 constexpr int SURFACE_NONE = 0;
 constexpr uint64_t PRN_MULT = 6364136223846793005ULL;
@@ -63,9 +64,9 @@ struct DFission {
 };
 
 // One site of the fission bank (SourceSite of src/particle_data.h:43-57 for
-// a prompt fission neutron: weight 1, time 0, on no surface)
+// a prompt fission neutron: weight 1, the parent's time, on no surface)
 struct DFissionSite {
-  double r[3], u[3], E;
+  double r[3], u[3], E, time;
   long long parent;  // source index of the parent history (1-based)
   int progeny, pad;
 };
@@ -159,6 +160,8 @@ struct DModel {
   long long max_history_splits;
   // settings
   double energy_cutoff;
+  double time_cutoff;  // neutron time cutoff in s (INFTY: none)
+  int track_time;      // particle time is advanced (a time cutoff is set)
   int max_events;
   long long n_particles;
   long long master_seed;
@@ -230,6 +233,7 @@ struct DBank {
   BField16<int> surface, material, material_last;
   BField<double> macro_t, macro_a;
   double* macro_nf;                  // macroscopic nu-fission (eigenvalue runs)
+  double* time;                      // particle time in s (runs with a time cutoff)
   double *k_col, *k_abs, *k_tra;     // the history's k-effective scores (eigenvalue runs)
   int* n_progeny;                    // fission sites the history has banked
   int *bsurf, *blevel, *btrans;
@@ -240,7 +244,7 @@ struct DBank {
 };
 
 struct DSecondary {
-  double r[3], u[3], E, wgt;
+  double r[3], u[3], E, wgt, time;
   int surf, prev;
 };
 
@@ -248,7 +252,7 @@ struct DSecondary {
 // the parent's state at the split plus an independent tracking seed.
 struct DSplitSite {
   double r[3], u[3];
-  double E, wgt, wgt_born, wgt_ww_born, ww_factor;
+  double E, wgt, wgt_born, wgt_ww_born, ww_factor, time;
   unsigned long long seed;
   long long id;
   int surf, n_split;
@@ -316,6 +320,7 @@ struct DTracks {
 struct DQueues {
   DTracks trk;           // deferred track records (trk.w null: tallies score inline)
   SourceSite* src_bank;  // [n_particles] or null (sites sampled at refill)
+  double* src_time;      // the source sites' times (eigenvalue runs with a time cutoff), or null: 0
   long long src_n;
   int* q_in;
   int* q_surf;

@@ -601,10 +601,9 @@ void load_model(const std::string& path_in, HModel& m)
   if (set->has("rel_max_lost_particles")) m.rel_max_lost_particles = std::stod(set->value("rel_max_lost_particles"));
   if (const XmlNode* co = set->child("cutoff")) {
     if (co->has("energy_neutron")) m.energy_cutoff = std::stod(co->value("energy_neutron"));
-    // particle time is not tracked on this path (src/particle.cpp:246-259
-    // advances it only to compare it with these cutoffs and time filters)
-    for (const char* t : {"time_neutron", "time_photon", "time_electron", "time_positron"})
-      if (co->has(t)) throw std::runtime_error(std::string("time cutoffs are not supported (<cutoff><") + t + ">)");
+    // src/settings.cpp:723-732; only neutrons are transported here, so the
+    // other particles' time cutoffs have nothing to act on
+    if (co->has("time_neutron")) m.time_cutoff = std::stod(co->value("time_neutron"));
     if (co->has("survival_biasing")) throw std::runtime_error("survival biasing is not supported");
   }
   if (set->has("survival_biasing") && XmlNode::trim(set->value("survival_biasing")) == "true")

@@ -135,6 +135,7 @@ struct HModel {
   int64_t max_history_splits = 10000000;
   int max_particle_events = 1000000;
   double energy_cutoff = 0.0;
+  double time_cutoff = 1.7976931348623157e308;  // neutron time cutoff in s (largest double: none)
   bool ww_on = false;
   int max_lost_particles = 10;
   double rel_max_lost_particles = 1.0e-6;

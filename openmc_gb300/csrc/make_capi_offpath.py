@@ -5,8 +5,9 @@ which declare argument types for every function they use at import
 a message naming the function (void functions only set the message; bool
 functions return false).
 
-The functions written are those the reference's bindings name and no other
-source file of this directory defines; their prototypes are read from the
+The functions written are those the reference's bindings name (openmc_*
+entry points and the few others they bind, such as the Zernike helpers of
+openmc/lib/math.py) and no other source file of this directory defines; their prototypes are read from the
 reference's include/openmc headers and, for the few declared only there,
 from the extern "C" definitions in its src/ files.
 
@@ -29,7 +30,7 @@ def _strip_comments(text):
 def bound_names(ref):
     names = set()
     for f in glob.glob(str(ref / "openmc" / "lib" / "*.py")):
-        names |= set(re.findall(r'_dll\.(openmc_\w+)', Path(f).read_text()))
+        names |= set(re.findall(r'_dll\.([A-Za-z]\w*)', Path(f).read_text()))
     return names
 
 
@@ -38,7 +39,7 @@ def defined_here():
     for f in list(HERE.glob("*.cpp")) + list(HERE.glob("*.cu")):
         if f.name == "capi_offpath.cpp":
             continue
-        names |= set(re.findall(r'^(?:extern "C" )?[\w\s\*]*?\b(openmc_\w+)\s*\([^;]*?\)\s*\{',
+        names |= set(re.findall(r'^(?:extern "C" )?[\w\s\*]*?\b([A-Za-z]\w*)\s*\([^;]*?\)\s*\{',
                                 _strip_comments(f.read_text()), flags=re.M))
     return names
 

@@ -35,8 +35,8 @@
 // Semantics kept from the history-based loop where the event-based loop of
 // the reference differs only for particles that die inside advance (time
 // cutoff, lost particle): their secondaries are still revived.
-// Particle time is not tracked: no time cutoff or time filter is supported,
-// and time does not feed any other quantity of this path.
+// Particle time is advanced only when a neutron time cutoff is set (nothing
+// else on this path reads it; time filters are not supported).
 //
 // Every kernel that reads the cell, surface, universe or material tables
 // sets the block's table pointers first (tables_enter, device.cuh); tally
@@ -105,6 +105,20 @@ __device__ __forceinline__ bool traced(long long id)
 {
   return dq.trace != nullptr && dq.batch == dq.trace_batch && id >= dq.trace_first &&
          id < dq.trace_first + dq.trace_hist;
+}
+
+// The trace record of an event after which the particle is dead without a
+// crossing or a collision (event kind 0, weight 0).
+__device__ __forceinline__ TraceRec* trace_slot(long long id);
+__device__ __forceinline__ void trace_dead(long long pid)
+{
+  TraceRec* rec = trace_slot(pid);
+  if (rec) {
+    rec->kind = 0;
+    rec->surface_or_nuclide = 0;
+    rec->wgt = 0.0;
+  }
+  dq.trace_n[pid - dq.trace_first] += 1;
 }
 
 // Whether slot s holds a traced history (its id in pid); reads the id only
@@ -526,6 +540,7 @@ __device__ void push_split_sites(long long s, int n, double wgt, const double* r
     d.wgt_born = db.wgt_born[s];
     d.wgt_ww_born = db.wgt_ww_born[s];
     d.ww_factor = db.ww_factor[s];
+    d.time = dm.track_time ? db.time[s] : 0.0;
     d.seed = split_seed(seed, k);
     d.id = db.id[s];
     d.surf = surf;
@@ -561,6 +576,7 @@ __device__ void push_secondaries(long long s, int n, double wgt, const double* r
     d.u[0] = u[0]; d.u[1] = u[1]; d.u[2] = u[2];
     d.E = E;
     d.wgt = wgt;
+    d.time = dm.track_time ? db.time[s] : 0.0;
     d.surf = surf;
     d.prev = top;
     top = e;
@@ -745,6 +761,9 @@ __device__ void initialize_history(long long s, long long index_source)
   db.rx[s] = r[0]; db.ry[s] = r[1]; db.rz[s] = r[2];
   set_direction(s, u[0], u[1], u[2]);
   db.E[s] = E;
+  // the default source time distribution is a point at 0; later
+  // generations of an eigenvalue run start at their fission sites' times
+  if (dm.track_time) db.time[s] = (dq.src_time && dq.src_n >= index_source) ? dq.src_time[index_source - 1] : 0.0;
   double wgt = 1.0;
   db.id[s] = index_source;
   db.n_event[s] = 0;
@@ -790,6 +809,7 @@ __device__ void start_split_site(long long s, const DSplitSite& d)
   set_direction(s, d.u[0], d.u[1], d.u[2]);
   db.E[s] = d.E;
   db.wgt[s] = d.wgt;
+  if (dm.track_time) db.time[s] = d.time;
   db.id[s] = d.id;
   db.n_event[s] = 0;
   db.n_split[s] = d.n_split;
@@ -853,6 +873,7 @@ __device__ bool revive_or_free(long long s, double wgt)
   db.rx[s] = site.r[0]; db.ry[s] = site.r[1]; db.rz[s] = site.r[2];
   set_direction(s, site.u[0], site.u[1], site.u[2]);
   db.E[s] = site.E;
+  if (dm.track_time) db.time[s] = site.time;
   db.n_event[s] = 0;
   // the revived entry joins the slot's free chain
   dq.sec[top].prev = db.sec_free[s];
@@ -1007,6 +1028,12 @@ __device__ __forceinline__ double collision_distance(double xi, double mt)
 
 __device__ int ev_surface_g(long long s, EvStats& st, Geo& g, double wgt, int bsurf, int trans, int blevel);
 
+// src/particle.cpp:46-73 Particle::speed for a neutron of energy E (eV), cm/s
+__device__ __forceinline__ double neutron_speed(double E)
+{
+  return C_LIGHT * sqrt(E * (E + 2 * MASS_NEUTRON_EV)) / (E + MASS_NEUTRON_EV);
+}
+
 // with_surf: a particle that reaches the boundary crosses it right away from
 // the registers (the surface event always follows such an advance), instead
 // of storing its state for a surface pass to reload.
@@ -1014,13 +1041,19 @@ __device__ int ev_surface_g(long long s, EvStats& st, Geo& g, double wgt, int bs
 // as a track record at the event's queue position qi for k_score_tracks.
 // hp: the slot's hot record as the caller holds it (after an XS event in the
 // same thread), else it is loaded here.
-template<bool with_surf, bool defer = false>
+// may_time false: built for runs without a time cutoff (the time code is
+// left out of the build rather than skipped at run time, for registers).
+template<bool with_surf, bool defer = false, bool may_time = true>
 __device__ int ev_advance(long long s, EvStats& st, int qi = 0, const BankHot* hp = nullptr)
 {
   const BankHot h = hp ? *hp : db.hot[s];
   double wgt = h.wgt;
   if (fpi::zero(wgt)) {
+    // lost in the cross-section event: no flight (its trace record has no
+    // event kind)
     if (defer && dq.trk.w) dq.trk.w[qi] = 0.0;  // no record
+    long long pid;
+    if (traced_slot(s, pid)) trace_dead(pid);
     return revive_or_free(s, wgt) ? NEXT_XS : NEXT_DEAD;
   }
   Geo g;
@@ -1044,9 +1077,19 @@ __device__ int ev_advance(long long s, EvStats& st, int qi = 0, const BankHot* h
   unsigned long long seed = h.seed;
   double mt = h.macro_t;
   double dcoll = fpi::zero(mt) ? __longlong_as_double(0x7ff0000000000000LL) : collision_distance(prn(seed), mt);
+  // src/particle.cpp:246-259: the distance the time cutoff leaves, at the
+  // speed of the particle's energy (INFTY without a cutoff); the particle
+  // moves the least of the three distances and its time advances by
+  // distance / speed
+  // (the speed is formed again for the time update rather than kept, to
+  // hold fewer registers across the flight when no cutoff is set)
+  const bool timed = may_time && dm.track_time;
+  double d_cut = INFTY;
+  if (timed) d_cut = (dm.time_cutoff - db.time[s]) * neutron_speed(g.E);
   double distance = bd;
   if (fpi::lt(dcoll, distance)) distance = dcoll;
-  if (fpi::lt(INFTY, distance)) distance = INFTY;
+  if (fpi::lt(d_cut, distance)) distance = d_cut;
+  if (timed) db.time[s] = db.time[s] + distance / neutron_speed(g.E);
   double r0[3] = {g.r[0][0], g.r[0][1], g.r[0][2]};
 #pragma unroll
   for (int l = 0; l < MAXL; ++l) {
@@ -1091,7 +1134,8 @@ __device__ int ev_advance(long long s, EvStats& st, int qi = 0, const BankHot* h
       recip ? inv_u : nullptr);
   }
   if (neg_lat) wgt = 0.0;  // mark_lost zeroed the stored weight
-  if (fpi::bits(distance) == fpi::bits(INFTY)) {
+  // killed at the time cutoff, or lost to infinity without one
+  if (fpi::eq(distance, d_cut)) {
     wgt = 0.0;
     db.wgt[s] = 0.0;
   }
@@ -1100,6 +1144,7 @@ __device__ int ev_advance(long long s, EvStats& st, int qi = 0, const BankHot* h
   if (traced_slot(s, pid)) {
     TraceRec* rec = trace_slot(pid);
     if (rec) rec->dist = distance;
+    if (fpi::zero(wgt)) trace_dead(pid);  // died in the flight (time cutoff, lost)
   }
   const bool cross = !fpi::zero(wgt) && fpi::lt(bd, dcoll);
   if (with_surf && cross) return ev_surface_g(s, st, g, wgt, bs, bt, bl);
@@ -1448,6 +1493,7 @@ __device__ void create_fission_sites(long long s, int nuc, double wgt, double E_
     site.u[1] = uo[1];
     site.u[2] = uo[2];
     site.E = E_out;
+    site.time = dm.track_time ? db.time[s] : 0.0;
     site.parent = db.id[s];
     site.progeny = db.n_progeny[s]++;
   }
@@ -1628,7 +1674,7 @@ __global__ void __launch_bounds__(256) k_xs()
 // defer: track-length tallies are scored afterwards by k_score_tracks from
 // the track records this kernel writes (the scoring code, the largest user
 // of registers in this kernel, then stays out of it).
-template<bool with_xs, bool with_surf, bool defer>
+template<bool with_xs, bool with_surf, bool defer, bool may_time = true>
 __global__ void __launch_bounds__(256, OMC_MINB_ADV) k_advance()
 {
   if (dq.cnt->tail) return;
@@ -1643,7 +1689,7 @@ __global__ void __launch_bounds__(256, OMC_MINB_ADV) k_advance()
     BankHot h {};
     if (valid) h = db.hot[s];
     if (with_xs && valid) ev_xs(s, st, &h);
-    int nx = valid ? ev_advance<with_surf, defer>(s, st, i, &h) : NEXT_DEAD;
+    int nx = valid ? ev_advance<with_surf, defer, may_time>(s, st, i, &h) : NEXT_DEAD;
     if (!with_surf) warp_append(dq.q_surf, &dq.cnt->n_surf, static_cast<int>(s), nx == NEXT_SURF);
     warp_append(dq.q_coll, &dq.cnt->n_coll, static_cast<int>(s), nx == NEXT_COLL);
     append_next(static_cast<int>(s), nx == NEXT_XS);
@@ -2353,6 +2399,8 @@ static void build_model(GpuSim& G, const HModel& m, const GpuOptions& opt)
   }
   d.max_history_splits = m.max_history_splits;
   d.energy_cutoff = m.energy_cutoff;
+  d.time_cutoff = m.time_cutoff;
+  d.track_time = m.time_cutoff < INFTY ? 1 : 0;
   d.max_events = m.max_particle_events;
   d.n_particles = m.n_particles;
   d.master_seed = m.seed;
@@ -2403,6 +2451,7 @@ static void build_bank(GpuSim& G, long long cap, long long sec_cap)
   b.ww_factor = dev_alloc<double>(cap, own);
   b.cell_last0 = dev_alloc<int>(cap, own);
   b.cell_born = dev_alloc<int>(cap, own);
+  b.time = G.model.track_time ? dev_alloc<double>(cap, own) : nullptr;
   b.macro_nf = b.k_col = b.k_abs = b.k_tra = nullptr;
   b.n_progeny = nullptr;
   if (G.model.eigen) {
@@ -2436,10 +2485,12 @@ static void build_bank(GpuSim& G, long long cap, long long sec_cap)
   // batch source bank (64 B per history) up to 2^27 histories per batch;
   // larger batches sample their sites at refill time
   q.src_bank = nullptr;
+  q.src_time = nullptr;
   q.src_n = 0;
   if (G.model.n_particles > 0 && G.model.n_particles <= (1LL << 27)) {
     q.src_bank = dev_alloc<SourceSite>(G.model.n_particles, own);
     q.src_n = G.model.n_particles;
+    if (G.model.eigen && G.model.track_time) q.src_time = dev_alloc<double>(G.model.n_particles, own);
   }
   q.trk = DTracks {};
   if (G.defer) {
@@ -2513,6 +2564,7 @@ static void launch_advance(const GpuSim& G, cudaStream_t S)
 {
   const int nb = G.blocks, nt = 256;
   if (!G.defer && G.model.n_tally_tracklength > 0) k_advance<true, true, false><<<nb, nt, G.smem, S>>>();
+  else if (G.fuse == 3 && !G.model.track_time) k_advance<true, true, true, false><<<nb, nt, G.smem, S>>>();
   else if (G.fuse == 3) k_advance<true, true, true><<<nb, nt, G.smem, S>>>();
   else if (G.fuse == 1) k_advance<true, false, true><<<nb, nt, G.smem, S>>>();
   else k_advance<false, false, true><<<nb, nt, G.smem, S>>>();
@@ -3011,6 +3063,7 @@ __global__ void k_eig_gather(const DFissionSite* bank, const int* perm, const in
       out.u[j] = site.u[j];
     }
     out.E = site.E;
+    if (dq.src_time) dq.src_time[k] = site.time;
     const long long id = static_cast<long long>(batch - 1) * n + k + 1;
     out.tseed = future_seed(static_cast<unsigned long long>(id) * dm.stride,
                             static_cast<unsigned long long>(dm.master_seed + 0));

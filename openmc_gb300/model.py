@@ -609,6 +609,7 @@ class Settings:
         self.weight_window_generators = []
         self.max_history_splits = None
         self.energy_cutoff = None
+        self.time_cutoff = None  # neutron time cutoff in s (the reference's cutoff['time_neutron'])
         self.survival_biasing = False
         self.max_lost_particles = None
         self.rel_max_lost_particles = None
@@ -650,9 +651,12 @@ class Settings:
             ET.SubElement(el, "max_lost_particles").text = str(int(self.max_lost_particles))
         if self.rel_max_lost_particles is not None:
             ET.SubElement(el, "rel_max_lost_particles").text = repr(float(self.rel_max_lost_particles))
-        if self.energy_cutoff is not None:
+        if self.energy_cutoff is not None or self.time_cutoff is not None:
             co = ET.SubElement(el, "cutoff")
-            ET.SubElement(co, "energy_neutron").text = repr(float(self.energy_cutoff))
+            if self.energy_cutoff is not None:
+                ET.SubElement(co, "energy_neutron").text = repr(float(self.energy_cutoff))
+            if self.time_cutoff is not None:
+                ET.SubElement(co, "time_neutron").text = repr(float(self.time_cutoff))
         meshes = {}
         wws = self.weight_windows if isinstance(self.weight_windows, (list, tuple)) else [self.weight_windows]
         for ww in wws:

@@ -26,6 +26,8 @@ from xml.etree import ElementTree as ET
 
 import numpy as np
 
+INFTY = float.fromhex('0x1.fffffffffffffp+1023')  # include/openmc/constants.h INFTY (largest double)
+
 
 def _read_library(xml_path):
     """name -> nuclide file path from a cross_sections.xml (OpenMC schema)."""
@@ -410,6 +412,10 @@ def load_model(model_xml, cross_sections=None):
     co = set_el.find("cutoff")
     if co is not None and _get(co, "energy_neutron") is not None:
         e_cut = float(_get(co, "energy_neutron"))
+    # src/settings.cpp:723-724 time_cutoff[neutron] (INFTY: none)
+    t_cut = INFTY
+    if co is not None and _get(co, "time_neutron") is not None:
+        t_cut = float(_get(co, "time_neutron"))
 
     # ---- source (one independent source)
     srcs = set_el.findall("source")
@@ -461,7 +467,7 @@ def load_model(model_xml, cross_sections=None):
     return {
         "settings_i": I([particles, batches, inactive, seed, log_grid_bins,
                          max_split_hist, 1 if event_based else 0, ww_on]),
-        "settings_d": D([e_cut]),
+        "settings_d": D([e_cut, t_cut]),
         "nuc_off": I(nuc_off), "nuc_awr": D(awr), "nuc_kT": D(kT),
         "nuc_energy": D(np.concatenate(energy)),
         "nuc_elastic": D(np.concatenate(elastic)),

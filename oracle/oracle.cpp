@@ -464,6 +464,7 @@ struct Sim {
   int64_t max_history_splits = 10000000;
   int max_particle_events = 1000000;
   double energy_cutoff = 0.0;
+  double time_cutoff = INFTY;  // neutron time cutoff (src/settings.cpp:112, 723-724)
   bool ww_on = false;
   double energy_min = 0, energy_max = INFTY, log_spacing = 0;
   std::vector<Nuclide> nuclides;
@@ -1683,7 +1684,7 @@ void event_advance(Sim& S, Particle& p)
     p.collision_distance = -std::log(prn(p.current_seed())) / p.macro_total;
   }
   double speed = particle_speed(p);
-  double distance_cutoff = INFTY;
+  double distance_cutoff = (S.time_cutoff < INFTY) ? (S.time_cutoff - p.time) * speed : INFTY;
   double distance = std::min({p.boundary.distance, p.collision_distance, distance_cutoff});
   for (int j = 0; j < p.n_coord; ++j)
     p.coord[j].r = p.coord[j].r + distance * p.coord[j].u;
@@ -2002,6 +2003,7 @@ void build(Sim& S, const Blob& B)
   S.max_history_splits = si[5];
   S.ww_on = si[7] != 0;
   S.energy_cutoff = B.D("settings_d")[0];
+  if (B.D("settings_d").size() > 1) S.time_cutoff = B.D("settings_d")[1];
 
   // nuclides
   const auto& off = B.I("nuc_off");

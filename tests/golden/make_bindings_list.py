@@ -15,7 +15,7 @@ def main():
     funcs, globs = set(), set()
     for f in sorted(lib.glob("*.py")):
         text = f.read_text()
-        funcs |= set(re.findall(r"_dll\.(openmc_\w+)", text))
+        funcs |= set(re.findall(r"_dll\.([A-Za-z]\w*)", text))
         globs |= set(re.findall(r"in_dll\(_dll,\s*['\"](\w+)['\"]\)", text))
         globs |= set(re.findall(r"_DLLGlobal\(\w+,\s*['\"](\w+)['\"]\)", text))
     out = Path(__file__).resolve().parent / "openmc_lib_bindings.json"

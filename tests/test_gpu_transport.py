@@ -149,6 +149,31 @@ def test_point_cube_no_sort_and_small_bank(cube):
     assert_tallies_close(g["tallies"], o["tallies"])
 
 
+def test_time_cutoff_parity(built, tmp_path):
+    """A neutron time cutoff (src/particle.cpp:246-286): a flight ends where
+    the particle's time reaches the cutoff and the particle dies there.
+    Histories and tallies equal the oracle's, and the cutoff removes the
+    slow neutrons' flux and events."""
+    from openmc_gb300 import configs
+    runs = {}
+    for cut in (None, 2e-7):
+        d = tmp_path / str(cut)
+        d.mkdir()
+        m, path = configs.point_cube(d, particles=3000, batches=2, n_points=2000)
+        m.settings.time_cutoff = cut
+        xml = m.export_to_model_xml(path)
+        runs[cut] = run_gpu(path, n_trace=3000, cap=512)
+        if cut is not None:
+            o = run_oracle(xml, n_trace=3000, cap=512)
+            bad = trace_mismatches(runs[cut]["trace"], o["trace"], 512)
+            assert not bad, f"{len(bad)} histories differ, first: {bad[:5]}"
+            assert_tallies_close(runs[cut]["tallies"], o["tallies"])
+    cut, free = runs[2e-7], runs[None]
+    assert cut["batch"]["done"] == 3000
+    assert 0 < cut["tallies"][0][0][..., 1].sum() < 0.9 * free["tallies"][0][0][..., 1].sum()
+    assert cut["batch"]["events"] < free["batch"]["events"]
+
+
 def test_lattice_history_parity(lattice):
     xml, path = lattice
     g = run_gpu(path, n_trace=1500, cap=1024)

@@ -278,7 +278,7 @@ def test_python_model_views(built, tmp_path):
         lib.finalize()
 
 
-@pytest.mark.parametrize("case", ["survival_biasing", "generations_per_batch", "time_cutoff"])
+@pytest.mark.parametrize("case", ["survival_biasing", "generations_per_batch"])
 def test_unsupported_settings_rejected(built, tmp_path, case):
     """Settings the GPU path does not implement fail at openmc_init instead
     of running without them."""
@@ -286,13 +286,10 @@ def test_unsupported_settings_rejected(built, tmp_path, case):
     m, d = configs.point_cube(tmp_path, particles=100, batches=2, n_points=300, mesh_dim=(2, 2, 2), n_ebins=2)
     if case == "survival_biasing":
         m.settings.survival_biasing = True
-    elif case == "generations_per_batch":
+    else:
         m.settings.run_mode = "eigenvalue"
         m.settings.generations_per_batch = 2
-    xml = m.export_to_model_xml(d)
-    if case == "time_cutoff":
-        text = Path(xml).read_text()
-        Path(xml).write_text(text.replace("<settings>", "<settings><cutoff><time_neutron>1e-6</time_neutron></cutoff>", 1))
+    m.export_to_model_xml(d)
     with pytest.raises(lib.InvalidArgumentError):
         lib.init(directory=d)
     lib.finalize()

@@ -1,4 +1,6 @@
 """Host-side model building and oracle self-consistency (CPU only)."""
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -133,3 +135,26 @@ def test_oracle_estimators_agree(tmp_path):
     tot_cells = c.reshape(3, 4, 3)[:, :, 0].sum()
     # (up to tracks below the lowest energy group bound)
     assert abs(a.reshape(-1, 2)[0, 0] - tot_cells) <= 1e-5 * tot_cells
+
+
+def test_time_cutoff_stops_histories(tmp_path):
+    """A neutron time cutoff (src/particle.cpp:246-286, src/settings.cpp:
+    723-724): flights end where the particle's time reaches the cutoff and
+    the particle dies there, so a short cutoff removes flux from the slow
+    neutrons of the cube, in both loops alike."""
+    from openmc_gb300 import configs
+    out = {}
+    for cut in (None, 2e-7):
+        d = tmp_path / str(cut)
+        d.mkdir()
+        m, path = configs.point_cube(d, particles=400, batches=2, n_points=300)
+        m.settings.time_cutoff = cut
+        xml = m.export_to_model_xml(path)
+        assert (cut is None) == ("time_neutron" not in Path(xml).read_text())
+        h = oracle.Oracle(xml)
+        h.run(threads=1, mode=0)
+        e = oracle.Oracle(xml)
+        e.run(threads=1, mode=1)
+        assert np.allclose(h.tally(0), e.tally(0), rtol=1e-13, atol=0)
+        out[cut] = h.tally(0)[:, 1].sum()
+    assert 0 < out[2e-7] < 0.9 * out[None]

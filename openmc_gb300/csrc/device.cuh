@@ -629,7 +629,9 @@ __device__ inline double surf_evaluate(const DSurface& s, double x, double y, do
 }
 
 // Comparisons run on the integer pipe (fp64_int.cuh) with the IEEE results.
-__device__ inline double plane_distance(double r_i, double u_i, bool coincident, double offset)
+// inv_u_i: 1 / u_i in FP32-table mode (a product replaces the quotient),
+// 0 for the reference's division.
+__device__ inline double plane_distance(double r_i, double u_i, bool coincident, double offset, double inv_u_i = 0.0)
 {
   const double f = offset - r_i;
   if (coincident || fpi::abs_lt(f, FP_COINCIDENT) || fpi::zero(u_i)) return INFTY;
@@ -638,11 +640,13 @@ __device__ inline double plane_distance(double r_i, double u_i, bool coincident,
   // division then; otherwise the quotient is positive and the reference's
   // d < 0 test never holds
   if ((fpi::bits(f) ^ fpi::bits(u_i)) < 0) return INFTY;
-  return f / u_i;
+  return fpi::zero(inv_u_i) ? f / u_i : f * inv_u_i;
 }
 
+// inv_a: 1 / (1 - u1^2) in FP32-table mode (products replace the quotients),
+// 0 for the reference's divisions.
 __device__ inline double cylinder_distance(double u1, double r2_, double u2, double r3_, double u3,
-  bool coincident, double offset1, double offset2, double radius)
+  bool coincident, double offset1, double offset2, double radius, double inv_a = 0.0)
 {
   const double a = 1.0 - u1 * u1;
   if (fpi::zero(a)) return INFTY;
@@ -651,15 +655,16 @@ __device__ inline double cylinder_distance(double u1, double r2_, double u2, dou
   const double k = r2 * u2 + r3 * u3;
   const double c = r2 * r2 + r3 * r3 - radius;  // radius: the squared radius
   const double quad = k * k - a * c;
+  const bool prod = !fpi::zero(inv_a);
   if (fpi::neg(quad)) {
     return INFTY;
   } else if (coincident || fpi::abs_lt(c, FP_COINCIDENT)) {
     if (fpi::nonneg(k)) return INFTY;
-    return (-k + sqrt(quad)) / a;
+    return prod ? (-k + sqrt(quad)) * inv_a : (-k + sqrt(quad)) / a;
   } else if (fpi::neg(c)) {
-    return (-k + sqrt(quad)) / a;
+    return prod ? (-k + sqrt(quad)) * inv_a : (-k + sqrt(quad)) / a;
   } else {
-    const double d = (-k - sqrt(quad)) / a;
+    const double d = prod ? (-k - sqrt(quad)) * inv_a : (-k - sqrt(quad)) / a;
     if (fpi::neg(d)) return INFTY;
     return d;
   }
@@ -688,16 +693,17 @@ __device__ inline double sphere_distance(const DSurface& s, double x_, double y_
   }
 }
 
+// inv_u (FP32-table mode): 1/ux, 1/uy, 1/uz and 1/(1 - uz^2) of the flight
 __device__ inline double surf_distance(const DSurface& s, double x, double y, double z, double ux,
-  double uy, double uz, bool coincident)
+  double uy, double uz, bool coincident, const double* inv_u = nullptr)
 {
   switch (s.type) {
-  case 0: return plane_distance(x, ux, coincident, s.c[0]);
-  case 1: return plane_distance(y, uy, coincident, s.c[0]);
-  case 2: return plane_distance(z, uz, coincident, s.c[0]);
+  case 0: return plane_distance(x, ux, coincident, s.c[0], inv_u ? inv_u[0] : 0.0);
+  case 1: return plane_distance(y, uy, coincident, s.c[0], inv_u ? inv_u[1] : 0.0);
+  case 2: return plane_distance(z, uz, coincident, s.c[0], inv_u ? inv_u[2] : 0.0);
   case 3: return cylinder_distance(ux, y, uy, z, uz, coincident, s.c[0], s.c[1], s.rr);
   case 4: return cylinder_distance(uy, x, ux, z, uz, coincident, s.c[0], s.c[1], s.rr);
-  case 5: return cylinder_distance(uz, x, ux, y, uy, coincident, s.c[0], s.c[1], s.rr);
+  case 5: return cylinder_distance(uz, x, ux, y, uy, coincident, s.c[0], s.c[1], s.rr, inv_u ? inv_u[3] : 0.0);
   default: return sphere_distance(s, x, y, z, ux, uy, uz, coincident);
   }
 }
@@ -773,7 +779,7 @@ __device__ inline bool cell_contains(const DCell& c, double x, double y, double 
 // direction) already exceeds it; skipped planes count as no crossing.  With
 // bound = INFTY this is exactly the reference loop.
 __device__ inline void region_distance(const DCell& c, double x, double y, double z, double ux, double uy,
-  double uz, int on_surface, double& min_dist, int& i_surf, double bound = INFTY)
+  double uz, int on_surface, double& min_dist, int& i_surf, double bound = INFTY, const double* inv_u = nullptr)
 {
   min_dist = INFTY;
   i_surf = 2147483647;
@@ -787,7 +793,7 @@ __device__ inline void region_distance(const DCell& c, double x, double y, doubl
       if (fpi::abs_gt(sf.c[0] - r_i, bound)) continue;
     }
     bool coincident = abs(token) == abs(on_surface);
-    double d = surf_distance(sf, x, y, z, ux, uy, uz, coincident);
+    double d = surf_distance(sf, x, y, z, ux, uy, uz, coincident, inv_u);
     if (fpi::lt(d, min_dist)) {
       // the first candidate against INFTY always passes: INFTY - d rounds
       // to INFTY, which exceeds FP_PRECISION x INFTY
@@ -1086,7 +1092,7 @@ __device__ inline void distance_to_boundary(const Geo& g, double& dist, int& sur
     const DCell& c = s_tabs.cell[g.cell[i]];
     const double* r = g.r[i];
     double b = (i == 0 && g.n_coord > 1) ? bound : INFTY;
-    region_distance(c, r[0], r[1], r[2], g.u[0], g.u[1], g.u[2], g.surface, ds[i], ss[i], b);
+    region_distance(c, r[0], r[1], r[2], g.u[0], g.u[1], g.u[2], g.surface, ds[i], ss[i], b, inv_u);
     if (i == 0 && g.n_coord > 1 && ss[i] == 2147483647) ds[i] = INF;  // every root surface bounded away
     dl[i] = INF;
     tt[i] = 13;

@@ -1065,12 +1065,29 @@ __device__ int ev_advance(long long s, EvStats& st, int qi = 0, const BankHot* h
   // distances (FP64 products in place of FP64 quotients).  Recomputed per
   // flight: keeping it in the bank with the direction measured 5 % slower
   // (three more scattered loads cost more than three FP64 divisions).
-  double inv_u[3];
+  // The reciprocals come from one division: with a = 1 - uz^2 (the z-
+  // cylinders' coefficient) and p = ux uy uz a, 1/ux = (uy uz a) / p and so
+  // on (a few ulps, against three or four correctly rounded quotients);
+  // separate divisions when p is zero or tiny.
+  double inv_u[4];
   const bool recip = dm.xs_fp32 != 0;
   if (recip) {
-    inv_u[0] = 1.0 / g.u[0];
-    inv_u[1] = 1.0 / g.u[1];
-    inv_u[2] = 1.0 / g.u[2];
+    const double ux = g.u[0], uy = g.u[1], uz = g.u[2];
+    const double a = 1.0 - uz * uz;
+    const double xy = ux * uy, za = uz * a;
+    const double p = xy * za;
+    if (fpi::abs_gt(p, 0x1p-900)) {
+      const double q = 1.0 / p;
+      inv_u[0] = q * (uy * za);
+      inv_u[1] = q * (ux * za);
+      inv_u[2] = q * (xy * a);
+      inv_u[3] = q * (xy * uz);
+    } else {
+      inv_u[0] = 1.0 / ux;
+      inv_u[1] = 1.0 / uy;
+      inv_u[2] = 1.0 / uz;
+      inv_u[3] = 1.0 / a;
+    }
   }
   distance_to_boundary(g, bd, bs, bl, bt, neg_lat, recip ? inv_u : nullptr);
   if (neg_lat) mark_lost(s);

@@ -50,7 +50,10 @@ std::vector<std::string> split_path(const std::string& p)
 size_t Value::count() const
 {
   size_t n = 1;
-  for (uint64_t d : shape) n *= d;
+  for (uint64_t d : shape) {
+    if (d != 0 && n > (uint64_t(1) << 40) / d) throw std::runtime_error("HDF5 dataspace too large");
+    n *= d;
+  }
   return n;
 }
 
@@ -82,6 +85,11 @@ std::vector<long long> Value::ints() const
 {
   const size_t n = count();
   std::vector<long long> out(n);
+  if (kind == 'f') {
+    const std::vector<double> d = doubles();
+    for (size_t k = 0; k < n; ++k) out[k] = static_cast<long long>(d[k]);
+    return out;
+  }
   for (size_t k = 0; k < n; ++k) {
     const uint8_t* p = bytes.data() + k * size;
     if (kind == 'i' || kind == 'u') {
@@ -89,8 +97,6 @@ std::vector<long long> Value::ints() const
       std::memcpy(&v, p, size);
       if (kind == 'i' && size < 8 && (v >> (8 * size - 1)) & 1) v |= ~0ull << (8 * size);
       out[k] = static_cast<long long>(v);
-    } else if (kind == 'f') {
-      out[k] = static_cast<long long>(doubles()[k]);
     } else {
       throw std::runtime_error("HDF5 value is not numeric");
     }
@@ -128,10 +134,32 @@ File::File(const std::string& path) : path_(path)
 
 uint64_t File::u(uint64_t off, int n) const
 {
-  if (off + n > b_.size()) fail(*this, "read past the end of the file");
+  if (off > b_.size() || static_cast<uint64_t>(n) > b_.size() - off) fail(*this, "read past the end of the file");
   uint64_t v = 0;
   for (int k = n - 1; k >= 0; --k) v = (v << 8) | b_[off + k];
   return v;
+}
+
+// Whether the 4-byte signature t stands at off (false past the end).
+bool File::tag(uint64_t off, const char* t) const
+{
+  return off <= b_.size() && b_.size() - off >= 4 && std::memcmp(&b_[off], t, 4) == 0;
+}
+
+// len bytes at off as a string (failing past the end of the file).
+std::string File::bytes_at(uint64_t off, uint64_t len) const
+{
+  if (off > b_.size() || len > b_.size() - off) fail(*this, "read past the end of the file");
+  return std::string(reinterpret_cast<const char*>(&b_[off]), len);
+}
+
+// The NUL-terminated string at off (failing when it runs past the end).
+std::string File::cstr_at(uint64_t off) const
+{
+  if (off >= b_.size()) fail(*this, "read past the end of the file");
+  const void* end = std::memchr(&b_[off], 0, b_.size() - off);
+  if (!end) fail(*this, "unterminated string");
+  return std::string(reinterpret_cast<const char*>(&b_[off]), static_cast<const uint8_t*>(end) - &b_[off]);
 }
 
 Node File::root() const { return Node(this, root_); }
@@ -139,8 +167,8 @@ Node File::root() const { return Node(this, root_); }
 std::vector<File::Msg> File::messages(uint64_t addr) const
 {
   std::vector<Msg> out;
-  if (addr + 4 <= b_.size() && std::memcmp(&b_[addr], "OHDR", 4) == 0) {
-    const int flags = b_[addr + 5];
+  if (tag(addr, "OHDR")) {
+    const int flags = static_cast<int>(u(addr + 5, 1));
     uint64_t off = addr + 6;
     if (flags & 0x20) off += 16;
     if (flags & 0x10) off += 4;
@@ -149,14 +177,15 @@ std::vector<File::Msg> File::messages(uint64_t addr) const
     off += size_len;
     std::vector<std::pair<uint64_t, uint64_t>> blocks {{off, chunk}};
     for (size_t bi = 0; bi < blocks.size(); ++bi) {
+      if (bi >= 4096) fail(*this, "too many object header continuations");
       uint64_t p = blocks[bi].first, end = blocks[bi].first + blocks[bi].second;
       while (p + 4 <= end) {
-        const int type = b_[p];
+        const int type = static_cast<int>(u(p, 1));
         const uint64_t size = u(p + 1, 2);
         p += 4 + ((flags & 0x04) ? 2 : 0);
         if (type == MSG_CONTINUATION) {
           const uint64_t ca = u(p, 8), cl = u(p + 8, 8);
-          if (std::memcmp(&b_[ca], "OCHK", 4) != 0) fail(*this, "bad object header continuation");
+          if (!tag(ca, "OCHK") || cl < 8) fail(*this, "bad object header continuation");
           blocks.push_back({ca + 4, cl - 8});
         } else {
           out.push_back({type, p, size});
@@ -166,11 +195,12 @@ std::vector<File::Msg> File::messages(uint64_t addr) const
     }
     return out;
   }
-  if (b_[addr] != 1) fail(*this, "unsupported object header version");
+  if (u(addr, 1) != 1) fail(*this, "unsupported object header version");
   const uint64_t nmsg = u(addr + 2, 2), hsize = u(addr + 8, 4);
   std::vector<std::pair<uint64_t, uint64_t>> blocks {{addr + 16, hsize}};
   uint64_t count = 0;
   for (size_t bi = 0; bi < blocks.size() && count < nmsg; ++bi) {
+    if (bi >= 4096) fail(*this, "too many object header continuations");
     uint64_t p = blocks[bi].first, end = blocks[bi].first + blocks[bi].second;
     while (p + 8 <= end && count < nmsg) {
       const int type = static_cast<int>(u(p, 2));
@@ -188,19 +218,24 @@ std::vector<File::Msg> File::messages(uint64_t addr) const
 Value File::datatype_value(uint64_t p) const
 {
   Value v;
-  const int cls = b_[p] & 0x0F;
-  const int bits0 = b_[p + 1];
+  const int cls = static_cast<int>(u(p, 1)) & 0x0F;
+  const int bits0 = static_cast<int>(u(p + 1, 1));
   v.size = u(p + 4, 4);
   if (cls == 0) {
     if (bits0 & 1) fail(*this, "big-endian integers are not supported");
+    if (v.size != 1 && v.size != 2 && v.size != 4 && v.size != 8) fail(*this, "unsupported integer size");
     v.kind = (bits0 & 0x08) ? 'i' : 'u';
   } else if (cls == 1) {
     if ((bits0 & 1) || (v.size != 4 && v.size != 8)) fail(*this, "only little-endian IEEE floats are supported");
     v.kind = 'f';
   } else if (cls == 3) {
+    if (v.size == 0) fail(*this, "empty string type");
     v.kind = 's';
   } else if (cls == 8) {
-    return datatype_value(p + 8);  // enumeration: its base type
+    // enumeration: its base type (one level; a nested enumeration is not
+    // what h5py writes)
+    if ((u(p + 8, 1) & 0x0F) == 8) fail(*this, "nested enumeration types are not supported");
+    return datatype_value(p + 8);
   } else {
     fail(*this, "unsupported datatype class " + std::to_string(cls));
   }
@@ -209,7 +244,7 @@ Value File::datatype_value(uint64_t p) const
 
 std::vector<uint64_t> File::dataspace(uint64_t p) const
 {
-  const int ver = b_[p], ndim = b_[p + 1];
+  const int ver = static_cast<int>(u(p, 1)), ndim = static_cast<int>(u(p + 1, 1));
   uint64_t q;
   if (ver == 1) q = p + 8;
   else if (ver == 2) q = p + 4;
@@ -225,14 +260,16 @@ std::vector<std::pair<std::string, uint64_t>> File::members(uint64_t addr) const
   for (const Msg& m : messages(addr)) {
     if (m.type == MSG_SYMBOL_TABLE) {
       const uint64_t btree = u(m.pos, 8), heap = u(m.pos + 8, 8);
-      if (std::memcmp(&b_[heap], "HEAP", 4) != 0) fail(*this, "bad local heap");
+      if (!tag(heap, "HEAP")) fail(*this, "bad local heap");
       const uint64_t data = u(heap + 24, 8);
       std::vector<uint64_t> stack {btree};
+      size_t visited = 0;
       while (!stack.empty()) {
+        if (++visited > (1u << 20)) fail(*this, "B-tree too large or cyclic");
         const uint64_t node = stack.back();
         stack.pop_back();
-        if (std::memcmp(&b_[node], "TREE", 4) != 0) fail(*this, "bad B-tree node");
-        const int level = b_[node + 5];
+        if (!tag(node, "TREE")) fail(*this, "bad B-tree node");
+        const int level = static_cast<int>(u(node + 5, 1));
         const uint64_t used = u(node + 6, 2);
         std::vector<uint64_t> kids;
         for (uint64_t k = 0; k < used; ++k) kids.push_back(u(node + 24 + 8 + 16 * k, 8));
@@ -241,30 +278,29 @@ std::vector<std::pair<std::string, uint64_t>> File::members(uint64_t addr) const
           continue;
         }
         for (uint64_t sn : kids) {
-          if (std::memcmp(&b_[sn], "SNOD", 4) != 0) fail(*this, "bad symbol table node");
+          if (!tag(sn, "SNOD")) fail(*this, "bad symbol table node");
           const uint64_t n = u(sn + 6, 2);
           for (uint64_t k = 0; k < n; ++k) {
             const uint64_t e = sn + 8 + 40 * k;
-            const char* name = reinterpret_cast<const char*>(&b_[data + u(e, 8)]);
-            out.push_back({std::string(name), u(e + 8, 8)});
+            out.push_back({cstr_at(data + u(e, 8)), u(e + 8, 8)});
           }
         }
       }
     } else if (m.type == MSG_LINK) {
-      const int flags = b_[m.pos + 1];
+      const int flags = static_cast<int>(u(m.pos + 1, 1));
       uint64_t q = m.pos + 2;
       int ltype = 0;
-      if (flags & 0x08) ltype = b_[q++];
+      if (flags & 0x08) ltype = static_cast<int>(u(q++, 1));
       if (flags & 0x04) q += 8;
       if (flags & 0x10) q += 1;
       const int nl = 1 << (flags & 3);
       const uint64_t len = u(q, nl);
       q += nl;
-      std::string name(reinterpret_cast<const char*>(&b_[q]), len);
+      std::string name = bytes_at(q, len);
       q += len;
       if (ltype == 0) out.push_back({name, u(q, 8)});
     } else if (m.type == MSG_LINK_INFO) {
-      const uint64_t fh = u(m.pos + 2 + ((b_[m.pos + 1] & 1) ? 8 : 0), 8);
+      const uint64_t fh = u(m.pos + 2 + ((u(m.pos + 1, 1) & 1) ? 8 : 0), 8);
       if (fh != UNDEF) fail(*this, "groups with dense link storage are not supported");
     }
   }
@@ -324,14 +360,14 @@ namespace {
 std::pair<std::string, Value> parse_attribute(const File& f, uint64_t p)
 {
   const auto& b = f.bytes();
-  const int ver = b[p];
+  const int ver = static_cast<int>(f.u(p, 1));
   const uint64_t name_size = f.u(p + 2, 2), dt_size = f.u(p + 4, 2), ds_size = f.u(p + 6, 2);
   uint64_t q;
   std::string name;
   Value v;
   if (ver == 1) {
     q = p + 8;
-    name = std::string(reinterpret_cast<const char*>(&b[q]));
+    name = f.cstr_at(q);
     q += pad8(name_size);
     v = f.datatype_value(q);
     q += pad8(dt_size);
@@ -339,7 +375,7 @@ std::pair<std::string, Value> parse_attribute(const File& f, uint64_t p)
     q += pad8(ds_size);
   } else if (ver == 2 || ver == 3) {
     q = p + 8 + (ver == 3 ? 1 : 0);
-    name = std::string(reinterpret_cast<const char*>(&b[q]));
+    name = f.cstr_at(q);
     q += name_size;
     v = f.datatype_value(q);
     q += dt_size;
@@ -349,7 +385,7 @@ std::pair<std::string, Value> parse_attribute(const File& f, uint64_t p)
     throw std::runtime_error(f.path() + ": unsupported attribute version");
   }
   const size_t n = v.count() * v.size;
-  if (q + n > b.size()) throw std::runtime_error(f.path() + ": attribute past the end of the file");
+  if (q > b.size() || n > b.size() - q) throw std::runtime_error(f.path() + ": attribute past the end of the file");
   v.bytes.assign(b.begin() + q, b.begin() + q + n);
   return {name, v};
 }
@@ -386,7 +422,7 @@ Value Node::read() const
   Value v;
   bool have_type = false, have_space = false, have_layout = false;
   uint64_t addr = UNDEF, size = 0;
-  const uint8_t* compact = nullptr;
+  uint64_t compact = UNDEF;  // file offset of a compact dataset's bytes
   for (const auto& m : f_->messages(addr_)) {
     if (m.type == MSG_DATATYPE) {
       const Value t = f_->datatype_value(m.pos);
@@ -397,12 +433,11 @@ Value Node::read() const
       v.shape = f_->dataspace(m.pos);
       have_space = true;
     } else if (m.type == MSG_LAYOUT) {
-      const auto& b = f_->bytes();
-      if (b[m.pos] != 3) throw std::runtime_error(f_->path() + ": unsupported data layout version");
-      const int cls = b[m.pos + 1];
+      if (f_->u(m.pos, 1) != 3) throw std::runtime_error(f_->path() + ": unsupported data layout version");
+      const int cls = static_cast<int>(f_->u(m.pos + 1, 1));
       if (cls == 0) {
         size = f_->u(m.pos + 2, 2);
-        compact = &b[m.pos + 4];
+        compact = m.pos + 4;
       } else if (cls == 1) {
         addr = f_->u(m.pos + 2, 8);
         size = f_->u(m.pos + 10, 8);
@@ -414,13 +449,15 @@ Value Node::read() const
   }
   if (!have_type || !have_space || !have_layout) throw std::runtime_error(f_->path() + ": not a dataset");
   const size_t n = v.count() * v.size;
-  if (compact) {
-    v.bytes.assign(compact, compact + std::min<uint64_t>(n, size));
+  if (n > (uint64_t(1) << 36)) throw std::runtime_error(f_->path() + ": dataset too large");
+  if (compact != UNDEF) {
+    const std::string c = f_->bytes_at(compact, std::min<uint64_t>(n, size));
+    v.bytes.assign(c.begin(), c.end());
   } else if (addr == UNDEF) {
     v.bytes.assign(n, 0);
   } else {
     const auto& b = f_->bytes();
-    if (addr + n > b.size()) throw std::runtime_error(f_->path() + ": dataset past the end of the file");
+    if (addr > b.size() || n > b.size() - addr) throw std::runtime_error(f_->path() + ": dataset past the end of the file");
     v.bytes.assign(b.begin() + addr, b.begin() + addr + n);
   }
   v.bytes.resize(n, 0);

@@ -66,7 +66,10 @@ class File {
   std::vector<std::pair<std::string, uint64_t>> members(uint64_t addr) const;
   Value datatype_value(uint64_t p) const;  // kind and size only
   std::vector<uint64_t> dataspace(uint64_t p) const;
-  uint64_t u(uint64_t off, int n) const;
+  uint64_t u(uint64_t off, int n) const;  // little-endian n-byte integer (bounds-checked)
+  bool tag(uint64_t off, const char* t) const;
+  std::string bytes_at(uint64_t off, uint64_t len) const;
+  std::string cstr_at(uint64_t off) const;
   const std::vector<uint8_t>& bytes() const { return b_; }
   const std::string& path() const { return path_; }
  private:

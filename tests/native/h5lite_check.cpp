@@ -10,6 +10,7 @@
 // "<path>@<name> A <value>" for an attribute.  A value is its kind, its
 // shape, and its elements (strings as text, numbers with %.17g).
 #include <cstdio>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -50,15 +51,17 @@ std::string show(const h5::Value& v)
   return out;
 }
 
-void dump(const h5::Node& n, const std::string& path)
+// depth-limited: a corrupt file can make a group its own descendant
+void dump(const h5::Node& n, const std::string& path, int depth = 0)
 {
+  if (depth > 32) throw std::runtime_error("groups nested too deeply (a cycle?)");
   for (const auto& a : n.attr_names()) std::printf("%s@%s A %s\n", path.c_str(), a.c_str(), show(n.attr(a)).c_str());
   if (n.is_dataset()) {
     std::printf("%s D %s\n", path.c_str(), show(n.read()).c_str());
     return;
   }
   std::printf("%s G\n", path.c_str());
-  for (const auto& c : n.children()) dump(n.at(c), path + "/" + c);
+  for (const auto& c : n.children()) dump(n.at(c), path + "/" + c, depth + 1);
 }
 
 }  // namespace

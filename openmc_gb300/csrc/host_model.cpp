@@ -64,6 +64,13 @@ void derive_columns(HNuclide& nuc, std::vector<double> el, const std::vector<dou
                     const std::vector<double>& cap)
 {
   const size_t G = nuc.energy.size();
+  // the grid the lookups search: at least two points, positive, finite and
+  // non-decreasing (repeated points are allowed, as in evaluated data)
+  if (G < 2) throw std::runtime_error("nuclide " + nuc.name + ": energy grid of fewer than two points");
+  for (size_t k = 0; k < G; ++k) {
+    if (!(nuc.energy[k] > 0.0) || !std::isfinite(nuc.energy[k]) || (k > 0 && nuc.energy[k] < nuc.energy[k - 1]))
+      throw std::runtime_error("nuclide " + nuc.name + ": energy grid not positive and ascending");
+  }
   // src/nuclide.cpp:359-453: total and absorption start at zero; the
   // reactions are added in name (MT) order: MT 2 to total; MT 18 to total,
   // fission and absorption; MT 102 (disappearance) to total and absorption;
@@ -187,13 +194,19 @@ void read_nuclide_file(const std::string& path, HNuclide& nuc)
   if (b.size() < 16 || std::memcmp(b.data(), "OMCGBNUC", 8) != 0)
     throw std::runtime_error(path + ": not a nuclide file");
   size_t off = 8;
+  // every read checked against the file's size (a truncated file is an error)
+  auto need = [&](size_t n) {
+    if (n > b.size() - off) throw std::runtime_error(path + ": truncated nuclide file");
+  };
   auto u32 = [&](void) {
+    need(4);
     uint32_t v;
     std::memcpy(&v, b.data() + off, 4);
     off += 4;
     return v;
   };
   auto f64 = [&](void) {
+    need(8);
     double v;
     std::memcpy(&v, b.data() + off, 8);
     off += 8;
@@ -202,19 +215,22 @@ void read_nuclide_file(const std::string& path, HNuclide& nuc)
   uint32_t version = u32();
   if (version != 1 && version != 2) throw std::runtime_error(path + ": unsupported nuclide file version");
   uint32_t nl = u32();
+  need(nl);
   off += nl;
   f64();  // A
   nuc.awr = f64();
   nuc.kT = f64();
   uint32_t G = u32();
   uint32_t nrx = u32();
+  need(8 * size_t(G));
   nuc.energy.resize(G);
-  std::memcpy(nuc.energy.data(), b.data() + off, 8 * G);
+  std::memcpy(nuc.energy.data(), b.data() + off, 8 * size_t(G));
   off += 8 * size_t(G);
   std::vector<double> el, fis, cap;
   for (uint32_t r = 0; r < nrx; ++r) {
     uint32_t mt = u32(), thr = u32(), n = u32();
     if (thr != 0 || n != G) throw std::runtime_error(path + ": threshold reactions are not supported");
+    need(8 * size_t(n));
     std::vector<double> xs(n);
     std::memcpy(xs.data(), b.data() + off, 8 * size_t(n));
     off += 8 * size_t(n);

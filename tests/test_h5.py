@@ -221,3 +221,26 @@ def test_reader_survives_corrupt_files(checker, tmp_path):
         f.write_bytes(c)
         r = subprocess.run([str(checker), "dump", str(f)], capture_output=True, timeout=60)
         assert r.returncode in (0, 1), (k, r.returncode, r.stderr[-300:].decode(errors="replace"))
+
+
+def test_truncated_native_nuclide_is_an_error(built, tmp_path):
+    """The native container's reader checks every read against the file's
+    size: truncated copies fail at openmc_init with a message, never crash."""
+    import subprocess as sp
+    import sys
+    from openmc_gb300 import configs
+    m, d = configs.infinite_medium(tmp_path, particles=100, batches=3, inactive=1, n_points=200)
+    m.export_to_model_xml(d / "model.xml")
+    victim = sorted(Path(d).rglob("*.nuc"))[0]
+    raw = victim.read_bytes()
+    script = ("import sys\n"
+              "from openmc_gb300 import lib\n"
+              "try:\n"
+              "    lib.init(directory=sys.argv[1])\n"
+              "except lib.OpenMCError as e:\n"
+              "    print('error', e)\n"
+              "lib.finalize()\n")
+    for n in (20, 60, len(raw) // 3, len(raw) - 9):
+        victim.write_bytes(raw[:n])
+        r = sp.run([sys.executable, "-c", script, str(d)], capture_output=True, text=True, cwd=str(ROOT), timeout=120)
+        assert r.returncode == 0 and "error" in r.stdout, (n, r.returncode, r.stdout[-200:], r.stderr[-300:])

@@ -141,7 +141,7 @@ int openmc_get_n_batches(int* n_batches, bool get_max_batches)
 int openmc_set_n_batches(int32_t n_batches, bool set_max_batches, bool add_statepoint_batch)
 {
   (void)set_max_batches;
-  (void)add_statepoint_batch;  // no statepoints are written on this path
+  (void)add_statepoint_batch;  // the statepoint is written at the last batch (the default statepoint batches)
   int rc;
   HModel* m = model_or_fail(rc);
   if (!m) return rc;

@@ -6,8 +6,10 @@ OpenMC reads incident-neutron data from HDF5 files listed in a
 temperature, the atomic weight ratio, ``kTs`` and one group per reaction with
 its ``threshold_idx`` and ``xs`` values (``docs/source/io_formats/
 nuclear_data.rst:16-64``).  Neither libhdf5 nor h5py exists on the machines
-this package runs on, so the same content is stored in a small native binary
-container with the same fields:
+this package runs on: ``write_nuclide_h5`` writes that HDF5 layout with the
+package's own writer (``openmc_gb300.h5``), and the same content can also be
+stored in a small native binary container with the same fields (the library
+reads either; the file's first bytes decide):
 
 ====================  ==========================================
 field                 meaning

@@ -395,32 +395,43 @@ def shield_fom():
 
 
 def network_bench(rows=1 << 20, steps=20):
-    """Training throughput of the importance network's tensor-core kernels:
-    full-batch Adam steps over `rows` random rows.  FLOPs per step count the
-    matrix products only: forward 2R(16x128 + 2x128x128), input gradients
-    2R(2x128x128), weight gradients 2R(2x128x144 + 128x16)."""
+    """Training throughput of the importance network: full-batch Adam steps
+    over `rows` random rows, with the fused per-tile kernel (the default) and
+    with the layer-by-layer kernels.  FLOPs per step count the network's
+    matrix products, independent of either kernel set's padding: forward
+    2R(4x128 + 2x128x128 + 128), backward 2R(2x128x128 + 2x128x128 + 4x128
+    + 128)."""
     from openmc_gb300 import lib
     rng = np.random.default_rng(3)
     x = rng.uniform(-1, 1, size=(rows, 4)).astype(np.float32)
     t = (x[:, 0] - 0.5 * x[:, 3]).astype(np.float32)
-    net = lib.ImportanceNetwork(max_rows=rows, seed=1)
-    try:
-        net.set_data(x, t)
-        net.train(2, lr=1e-3)
-        net.train(steps, lr=1e-3)
-        ms = net.last_train_ms()
-    finally:
-        net.close()
-    flops = 2.0 * rows * (16 * 128 + 2 * 128 * 128 + 2 * 128 * 128 + 2 * 128 * 144 + 128 * 16)
-    tflops = flops * steps / (ms * 1e-3) / 1e12
+    flops = 2.0 * rows * ((4 * 128 + 2 * 128 * 128 + 128) + (4 * 128 * 128 + 4 * 128 + 128))
     peak = 0.0
     pk = ROOT / "MEASURED_PEAKS.json"
     if pk.exists():
         peak = float(json.loads(pk.read_text()).get("bf16_tflops", 0.0))
-    return {"rows": rows, "steps": steps, "ms_per_step": ms / steps, "tflops": tflops,
+    old = lib.settings.mlp_fused
+    ms = {}
+    try:
+        for mode in (1, 0):
+            lib.settings.mlp_fused = mode
+            net = lib.ImportanceNetwork(max_rows=rows, seed=1)
+            try:
+                net.set_data(x, t)
+                net.train(3, lr=1e-3)
+                net.train(steps, lr=1e-3)
+                ms[mode] = net.last_train_ms() / steps
+            finally:
+                net.close()
+    finally:
+        lib.settings.mlp_fused = old
+    tflops = flops / (ms[1] * 1e-3) / 1e12
+    return {"rows": rows, "steps": steps, "ms_per_step": ms[1], "tflops": tflops,
             "bf16_peak_tflops": peak or None, "frac_of_bf16_peak": tflops / peak if peak else None,
-            "note": "hidden width 128: each 128-row tile moves ~200 KB for 4 MFLOP, so the products are "
-                    "bound by memory traffic, not by the tensor cores"}
+            "layer_by_layer_ms_per_step": ms[0], "layer_by_layer_tflops": flops / (ms[0] * 1e-3) / 1e12,
+            "note": "fused: one persistent kernel per step keeps each 128-row tile's activations in shared "
+                    "and tensor memory (one CTA per SM); layer-by-layer: one kernel per product, "
+                    "activations through device memory"}
 
 
 def compare_tallies(a, b, n_a, n_b):

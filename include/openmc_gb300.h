@@ -227,6 +227,10 @@ int openmc_gb300_mlp_predict(void* handle, int64_t n, const float* x4, float* y)
 int openmc_gb300_mlp_get_params(void* handle, float* params, int64_t n);
 int openmc_gb300_mlp_set_params(void* handle, const float* params, int64_t n);
 int openmc_gb300_mlp_last_ms(void* handle, float* ms);
+/* 1 (default): every training step and query is one fused kernel per
+ * 128-row tile (activations of all layers kept in shared and tensor memory);
+ * 0: one kernel per layer product, activations through device memory. */
+extern int openmc_gb300_mlp_fused;
 
 /* ---- model queries the reference's Python bindings use (openmc/lib/cell.py,
  *      material.py, mesh.py, filter.py, tally.py, nuclide.py, core.py),

@@ -552,6 +552,483 @@ __global__ void k_prepare(const float* __restrict__ x4, long long n, long long R
   }
 }
 
+// ------------------------------------------------------------------ fused training step
+// One persistent kernel for the whole forward and backward pass: each CTA
+// (one per SM, 16 warps) walks 128-row tiles and keeps every activation of a
+// tile on chip.  Shared memory holds the two hidden weight matrices for the
+// whole launch and four 128 x 128 BF16 activation tiles (H1, H2, dZ3, dZ2;
+// dZ1 reuses H2's), all in the K-major core-matrix layout by feature:
+// element (r, f) at byte ((r/8) 16 + f/8) 128 + (r%8) 16 + (f%8) 2.  The
+// products that need a transposed operand (input gradients dZ W: B = W^T;
+// weight gradients dZ^T H: A = dZ^T, B = H^T) read the same tiles through
+// MN-major descriptors, so no tile is ever written twice.  Tensor memory
+// (512 columns) holds Z2 / dH1 (columns 0-127), Z3 / dH2 and the per-tile
+// column sums (128-255), and the dW3 and dW2 accumulators (256-383,
+// 384-511), which run over all of the CTA's tiles.  Bias gradients and dW1
+// come from N = 16 products against the input tile [x0..x3, 1, 0...]
+// (column 4 = 1 gives the column sums); dw4, db4 and the loss are reduced
+// over rows with shuffles.  Each CTA writes one partial per gradient in the
+// layouts k_adam sums (G1, G2, G3, GH).  Layer 1 (K = 4) runs on the CUDA
+// cores.  BF16 rounding happens where the layer-by-layer kernels round:
+// inputs, weights, activations and pre-activation gradients.
+constexpr int F_THREADS = 512;
+constexpr int F_COLS = HID * TILE_M / F_THREADS;  // columns of a row per thread (32)
+constexpr int F_GROUPS = HID / F_COLS;           // threads per row (4)
+constexpr int TILE_BYTES = TILE_M * HID * 2;   // 32 KB
+constexpr int X0_BYTES = TILE_M * IN_PAD * 2;  // 4 KB
+constexpr int F_W2 = 0, F_W3 = F_W2 + TILE_BYTES, F_H1 = F_W3 + TILE_BYTES, F_H2 = F_H1 + TILE_BYTES,
+              F_DZ3 = F_H2 + TILE_BYTES, F_DZ2 = F_DZ3 + TILE_BYTES, F_X0 = F_DZ2 + TILE_BYTES,
+              F_PAR = F_X0 + X0_BYTES,                  // float4 W1[128]; float b1[128], b2[128]; float2 (b3, w4)[128]
+              F_RED = F_PAR + (4 * HID + 4 * HID) * 4,  // floats: red[4][128], ypart[4][128], misc[16]
+              F_END = F_RED + (4 * HID + F_GROUPS * HID + 16) * 4;
+// An MN-major descriptor read spans at most 7 x 4096 + 15 x 2048 + 255 bytes
+// past its tile's start under either assignment of the two descriptor
+// strides; the allocation covers that from the last tile, so no stride
+// reading can leave the CTA's shared memory.
+constexpr int F_SPAN = 7 * 4096 + 15 * 2048 + 256;
+constexpr int F_SMEM = (F_END > F_DZ2 + F_SPAN ? F_END : F_DZ2 + F_SPAN) + 1024;
+static_assert(F_SMEM <= 232448, "fused kernel shared memory");
+constexpr uint32_t T_R0 = 0, T_R1 = 128, T_DW3 = 256, T_DW2 = 384;
+
+struct FusedArgs {
+  const float* x4;      // [n][4]
+  const float* target;  // [n] (train)
+  const float* weight;  // [n] (train)
+  long long n;
+  int tiles;
+  int train;
+  float inv_n;
+  const __nv_bfloat16* W1;  // BF16 operand copies: [128][16], [128][128], [128][128]
+  const __nv_bfloat16* W2;
+  const __nv_bfloat16* W3;
+  const float* P;  // FP32 parameters (biases, w4, b4)
+  float* y_out;    // predictions [n] (forward only)
+  float* G1;       // per-CTA partials [grid][128][16], [grid][128][144] x 2, [grid][130]
+  float* G2;
+  float* G3;
+  float* GH;
+  int* step;
+  int* error;
+};
+
+__device__ __forceinline__ uint32_t tile_off(int r, int f)
+{
+  return static_cast<uint32_t>((((r >> 3) * 16 + (f >> 3)) << 7) + ((r & 7) << 4) + ((f & 7) << 1));
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
+{
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t*>(&v);
+}
+
+__device__ __forceinline__ float bf16_round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+
+__device__ __forceinline__ float sigm(float z) { return __fdividef(1.0f, 1.0f + __expf(-z)); }
+
+// 8 consecutive FP32 accumulator columns of this thread's row
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v)
+{
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr)
+               : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+// Sums 32 values over the 32 lanes of a warp, one column per lane: on
+// return lane l holds the sum over all lanes of v[l] (31 shuffles, fixed
+// order).  v is overwritten.
+__device__ __forceinline__ float lane_column_sums(float (&v)[32], int lane)
+{
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1) {
+    const bool hi = (lane & m) != 0;
+#pragma unroll
+    for (int i = 0; i < m; ++i) {
+      const float send = hi ? v[i] : v[i + m];
+      const float keep = hi ? v[i + m] : v[i];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, m);
+    }
+  }
+  return v[0];
+}
+
+// An operand of one product: the tile's shared-memory address, whether it is
+// read MN-major, and the shape of its layout.
+struct Operand {
+  uint32_t addr;
+  bool mn;
+  uint32_t kstep, lbo, sbo;  // bytes per K step of 16, leading / stride byte offsets
+};
+
+// 128 x 128 tile by feature, read with K = features (K-major) or K = rows
+// (MN-major: the 8 features of a core-matrix row are the M or N index)
+__device__ __forceinline__ Operand big_tile(uint32_t addr, bool mn)
+{
+  return mn ? Operand{addr, true, 4096u, 2048u, 128u} : Operand{addr, false, 256u, 128u, 2048u};
+}
+
+// 128 x 16 input tile read MN-major (N = the 16 input columns, K = rows)
+__device__ __forceinline__ Operand x0_tile(uint32_t addr) { return Operand{addr, true, 512u, 256u, 128u}; }
+
+// D (+)= A B^T over K = 128 in 8 steps of 16 (issued by one thread)
+__device__ __forceinline__ void issue_product(uint32_t d, const Operand& a, const Operand& b, int n, bool accumulate)
+{
+  const uint32_t idesc = instr_desc(TILE_M, n) | (a.mn ? 1u << 15 : 0u) | (b.mn ? 1u << 16 : 0u);
+#pragma unroll 1
+  for (int j = 0; j < HID / 16; ++j) {
+    const uint64_t ad = smem_desc(a.addr + j * a.kstep, a.lbo, a.sbo);
+    const uint64_t bd = smem_desc(b.addr + j * b.kstep, b.lbo, b.sbo);
+    mma_bf16(d, ad, bd, idesc, (accumulate || j > 0) ? 1u : 0u);
+  }
+}
+
+__global__ void __launch_bounds__(F_THREADS, 1) k_fused(FusedArgs a)
+{
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  float4* sW1 = reinterpret_cast<float4*>(base + F_PAR);  // W1 row o (BF16 values)
+  float* sb1 = reinterpret_cast<float*>(sW1 + HID);
+  float* sb2 = sb1 + HID;
+  float2* sb3w4 = reinterpret_cast<float2*>(sb2 + HID);  // (b3, w4) of neuron o
+  float* s_red = reinterpret_cast<float*>(base + F_RED);
+  float* s_ypart = s_red + 4 * HID;
+  float* s_misc = s_ypart + F_GROUPS * HID;
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_s;
+
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int q = warp & 3, h = warp >> 2;
+  const int r = 32 * q + lane;  // row of the tile (tensor-memory lane) this thread works on
+  const int c0 = F_COLS * h;    // its columns [c0, c0 + F_COLS)
+  const uint32_t sbase = smem_u32(base);
+
+  if (warp == 0) tmem_alloc(&tmem_s, 512);
+  if (t == 0) {
+    mbar_init(&mbar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // weights into the K-major layout (16-byte groups of 8 inputs), layer-1
+  // weights and the biases as FP32
+  for (int i = t; i < 2 * HID * (HID / 8); i += F_THREADS) {
+    const int w = i / (HID * (HID / 8)), k = i % (HID * (HID / 8));
+    const int o = k / (HID / 8), g = k % (HID / 8);
+    const __nv_bfloat16* src = (w ? a.W3 : a.W2) + o * HID + g * 8;
+    *reinterpret_cast<uint4*>(base + (w ? F_W3 : F_W2) + tile_off(o, g * 8)) = *reinterpret_cast<const uint4*>(src);
+  }
+  for (int o = t; o < HID; o += F_THREADS) {
+    const __nv_bfloat16* w1 = a.W1 + o * IN_PAD;
+    sW1[o] = make_float4(__bfloat162float(w1[0]), __bfloat162float(w1[1]), __bfloat162float(w1[2]),
+                         __bfloat162float(w1[3]));
+    sb1[o] = a.P[P_B1 + o];
+    sb2[o] = a.P[P_B2 + o];
+    sb3w4[o] = make_float2(a.P[P_B3 + o], a.P[P_W4 + o]);
+  }
+  const float b4 = a.P[P_B4];
+  fence_async_shared();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_s;
+  const uint32_t t_row = tmem + (static_cast<uint32_t>(32 * q) << 16);
+
+  float acc_dw4 = 0.0f, acc_db3 = 0.0f, acc_db2 = 0.0f, acc_db1 = 0.0f, acc_db4 = 0.0f, acc_loss = 0.0f;
+  float acc_dw1[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+  uint32_t phase = 0;
+  bool ok = true, first = true;
+
+  auto wait_products = [&]() {
+    const bool done = mbar_wait(&mbar, phase & 1u, WAIT_TRIES);
+    ++phase;
+    ok = ok && done;
+    tc_fence_after();
+  };
+  // all threads: shared-memory tiles written, tensor-memory reads done
+  auto tiles_ready = [&]() -> bool {
+    fence_async_shared();
+    tc_fence_before();
+    const bool all = __syncthreads_and(ok);
+    tc_fence_after();
+    return all;
+  };
+  // pre-activation of layer 1 for neuron o
+  auto z1_of = [&](const float (&x)[4], int o) {
+    const float4 w = sW1[o];
+    return fmaf(x[3], w.w, fmaf(x[2], w.z, fmaf(x[1], w.y, fmaf(x[0], w.x, sb1[o]))));
+  };
+
+  // inputs of this thread's row, loaded one tile ahead
+  auto load_x = [&](int tile) {
+    const long long row = static_cast<long long>(tile) * TILE_M + r;
+    return (tile < a.tiles && row < a.n) ? __ldg(reinterpret_cast<const float4*>(a.x4 + row * 4))
+                                         : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  };
+  float4 x_next = load_x(blockIdx.x);
+
+  for (int tile = blockIdx.x; tile < a.tiles; tile += gridDim.x) {
+    const long long rg = static_cast<long long>(tile) * TILE_M + r;
+    const bool real = rg < a.n;
+    // target and weight are used after the forward pass
+    float tgt = 0.0f, wt = 0.0f;
+    if (a.train && real) {
+      tgt = __ldg(a.target + rg);
+      wt = __ldg(a.weight + rg);
+    }
+    // ---- layer 1 on the CUDA cores: H1 = silu(X0 W1^T + b1)
+    const float x[4] = {bf16_round(x_next.x), bf16_round(x_next.y), bf16_round(x_next.z), bf16_round(x_next.w)};
+    x_next = load_x(tile + gridDim.x);
+    if (h == 0) {
+      *reinterpret_cast<uint4*>(base + F_X0 + ((r >> 3) * 2 << 7) + ((r & 7) << 4)) =
+        make_uint4(pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(1.0f, 0.0f), 0u);
+      *reinterpret_cast<uint4*>(base + F_X0 + (((r >> 3) * 2 + 1) << 7) + ((r & 7) << 4)) = make_uint4(0u, 0u, 0u, 0u);
+    }
+#pragma unroll
+    for (int g = 0; g < F_COLS / 8; ++g) {
+      uint32_t pk[4];
+#pragma unroll
+      for (int e = 0; e < 8; e += 2) {
+        const float z0 = z1_of(x, c0 + 8 * g + e), z1 = z1_of(x, c0 + 8 * g + e + 1);
+        pk[e / 2] = pack_bf16(z0 * sigm(z0), z1 * sigm(z1));
+      }
+      *reinterpret_cast<uint4*>(base + F_H1 + tile_off(r, c0 + 8 * g)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    }
+    if (!tiles_ready()) break;
+    if (t == 0) {
+      issue_product(tmem + T_R0, big_tile(sbase + F_H1, false), big_tile(sbase + F_W2, false), HID, false);
+      mma_commit(&mbar);
+    }
+    wait_products();
+    // ---- layer 2 epilogue: H2 = silu(Z2 + b2)
+    {
+      float v[32];
+      tmem_ld32(t_row + T_R0 + c0, v);
+#pragma unroll
+      for (int g = 0; g < 4; ++g) {
+        uint32_t pk[4];
+#pragma unroll
+        for (int e = 0; e < 8; e += 2) {
+          const int k = 8 * g + e, o = c0 + k;
+          const float z0 = v[k] + sb2[o], z1 = v[k + 1] + sb2[o + 1];
+          pk[e / 2] = pack_bf16(z0 * sigm(z0), z1 * sigm(z1));
+        }
+        *reinterpret_cast<uint4*>(base + F_H2 + tile_off(r, c0 + 8 * g)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      }
+    }
+    if (!tiles_ready()) break;
+    if (t == 0) {
+      issue_product(tmem + T_R1, big_tile(sbase + F_H2, false), big_tile(sbase + F_W3, false), HID, false);
+      mma_commit(&mbar);
+    }
+    wait_products();
+    // ---- layer 3 epilogue and the output layer: H3 = silu(Z3 + b3),
+    // y = H3 . w4 + b4; g3 = w4 silu'(Z3) is kept for dZ3 = dy g3
+    float g3[32];
+    uint32_t h3[16];
+    float ypart = 0.0f;
+    {
+      float v[32];
+      tmem_ld32(t_row + T_R1 + c0, v);
+#pragma unroll
+      for (int k = 0; k < 32; k += 2) {
+        float hb[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const float2 bw = sb3w4[c0 + k + u];
+          const float z = v[k + u] + bw.x;
+          const float s = sigm(z);
+          hb[u] = bf16_round(z * s);
+          ypart = fmaf(hb[u], bw.y, ypart);
+          g3[k + u] = bw.y * (s * (1.0f + z * (1.0f - s)));
+        }
+        h3[k / 2] = pack_bf16(hb[0], hb[1]);
+      }
+    }
+    s_ypart[h * HID + r] = ypart;
+    __syncthreads();
+    const float y = b4 + (((s_ypart[r] + s_ypart[HID + r]) + s_ypart[2 * HID + r]) + s_ypart[3 * HID + r]);
+    if (!a.train) {
+      if (h == 0 && real) a.y_out[rg] = y;
+      tc_fence_before();
+      __syncthreads();
+      continue;
+    }
+    float dy = 0.0f, loss = 0.0f;
+    if (real) {
+      const float e = y - tgt;
+      loss = wt * e * e * a.inv_n;
+      dy = 2.0f * wt * e * a.inv_n;
+    }
+    // dZ3 = bf16(dy g3) into its tile; dw4 = sum over rows of dy H3
+#pragma unroll
+    for (int g = 0; g < 4; ++g) {
+      uint32_t pk[4];
+#pragma unroll
+      for (int e = 0; e < 8; e += 2) pk[e / 2] = pack_bf16(dy * g3[8 * g + e], dy * g3[8 * g + e + 1]);
+      *reinterpret_cast<uint4*>(base + F_DZ3 + tile_off(r, c0 + 8 * g)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    }
+    {
+      float v[32];
+#pragma unroll
+      for (int k = 0; k < 32; k += 2) {
+        const __nv_bfloat162 p = *reinterpret_cast<const __nv_bfloat162*>(&h3[k / 2]);
+        v[k] = dy * __low2float(p);
+        v[k + 1] = dy * __high2float(p);
+      }
+      s_red[q * HID + c0 + lane] = lane_column_sums(v, lane);
+    }
+    if (h == 0) {
+      float sd = dy, sl = loss;
+#pragma unroll
+      for (int m = 16; m >= 1; m >>= 1) {
+        sd += __shfl_xor_sync(0xffffffffu, sd, m);
+        sl += __shfl_xor_sync(0xffffffffu, sl, m);
+      }
+      if (lane == 0) {
+        s_misc[q] = sd;
+        s_misc[4 + q] = sl;
+      }
+    }
+    if (!tiles_ready()) break;
+    if (t < HID) acc_dw4 += ((s_red[t] + s_red[HID + t]) + s_red[2 * HID + t]) + s_red[3 * HID + t];
+    if (t == 0) {
+      acc_db4 += ((s_misc[0] + s_misc[1]) + s_misc[2]) + s_misc[3];
+      acc_loss += ((s_misc[4] + s_misc[5]) + s_misc[6]) + s_misc[7];
+      // dH2 = dZ3 W3 (B = W3 read MN-major); dW3 += dZ3^T H2 runs on
+      // while dZ2 is formed (it reads neither tensor-memory columns 0-255
+      // nor the dZ2 tile)
+      issue_product(tmem + T_R1, big_tile(sbase + F_DZ3, false), big_tile(sbase + F_W3, true), HID, false);
+      mma_commit(&mbar);
+      issue_product(tmem + T_DW3, big_tile(sbase + F_DZ3, true), big_tile(sbase + F_H2, true), HID, !first);
+    }
+    wait_products();
+    // ---- dZ2 = bf16(dH2 silu'(Z2)), Z2 still in columns 0-127
+    {
+      float dh[32], z[32];
+      tmem_ld32(t_row + T_R1 + c0, dh);
+      tmem_ld32(t_row + T_R0 + c0, z);
+#pragma unroll
+      for (int g = 0; g < 4; ++g) {
+        uint32_t pk[4];
+#pragma unroll
+        for (int e = 0; e < 8; e += 2) {
+          float d[2];
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            const int k = 8 * g + e + u;
+            const float zz = z[k] + sb2[c0 + k];
+            const float s = sigm(zz);
+            d[u] = dh[k] * (s * (1.0f + zz * (1.0f - s)));
+          }
+          pk[e / 2] = pack_bf16(d[0], d[1]);
+        }
+        *reinterpret_cast<uint4*>(base + F_DZ2 + tile_off(r, c0 + 8 * g)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      }
+    }
+    if (!tiles_ready()) break;
+    if (t == 0) {
+      // dH1 = dZ2 W2 (its completion also covers the dW3 product issued
+      // before it); then dW2 += dZ2^T H1 and the column sums of dZ3 and dZ2
+      // (db3, db2) run on while dZ1 is formed
+      issue_product(tmem + T_R0, big_tile(sbase + F_DZ2, false), big_tile(sbase + F_W2, true), HID, false);
+      mma_commit(&mbar);
+      issue_product(tmem + T_DW2, big_tile(sbase + F_DZ2, true), big_tile(sbase + F_H1, true), HID, !first);
+      issue_product(tmem + T_R1, big_tile(sbase + F_DZ3, true), x0_tile(sbase + F_X0), IN_PAD, false);
+      issue_product(tmem + T_R1 + 32, big_tile(sbase + F_DZ2, true), x0_tile(sbase + F_X0), IN_PAD, false);
+    }
+    wait_products();
+    // ---- dZ1 = bf16(dH1 silu'(Z1)) into H2's tile (dW3, its last reader,
+    // completed before dH1)
+    {
+      float dh[32];
+      tmem_ld32(t_row + T_R0 + c0, dh);
+#pragma unroll
+      for (int g = 0; g < 4; ++g) {
+        uint32_t pk[4];
+#pragma unroll
+        for (int e = 0; e < 8; e += 2) {
+          float d[2];
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            const int k = 8 * g + e + u;
+            const float zz = z1_of(x, c0 + k);
+            const float s = sigm(zz);
+            d[u] = dh[k] * (s * (1.0f + zz * (1.0f - s)));
+          }
+          pk[e / 2] = pack_bf16(d[0], d[1]);
+        }
+        *reinterpret_cast<uint4*>(base + F_H2 + tile_off(r, c0 + 8 * g)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      }
+    }
+    if (!tiles_ready()) break;
+    if (t == 0) {
+      // dW1 (columns 0-3) and db1 (column 4); the commit covers every
+      // product of the tile
+      issue_product(tmem + T_R1 + 64, big_tile(sbase + F_H2, true), x0_tile(sbase + F_X0), IN_PAD, false);
+      mma_commit(&mbar);
+    }
+    wait_products();
+    if (h == 0) {
+      float v[8];
+      tmem_ld8(t_row + T_R1, v);
+      acc_db3 += v[4];
+      tmem_ld8(t_row + T_R1 + 32, v);
+      acc_db2 += v[4];
+      tmem_ld8(t_row + T_R1 + 64, v);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) acc_dw1[i] += v[i];
+      acc_db1 += v[4];
+    }
+    first = false;
+    // No barrier here: every product of the tile has completed, and the next
+    // tile overwrites columns 128-255 (read just above) only after two more
+    // barriers.
+    tc_fence_before();
+  }
+
+  if (!ok) {
+    if (t == 0) atomicOr(a.error, ERR_TIMEOUT);
+  } else if (a.train) {
+    // this CTA's partials: tensor-memory lane = output neuron
+    const int o = r;
+    float* g2 = a.G2 + (static_cast<long long>(blockIdx.x) * HID + o) * G_N;
+    float* g3 = a.G3 + (static_cast<long long>(blockIdx.x) * HID + o) * G_N;
+    float v[32];
+    tmem_ld32(t_row + T_DW3 + c0, v);
+#pragma unroll
+    for (int k = 0; k < 32; k += 4)
+      *reinterpret_cast<float4*>(g3 + c0 + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+    tmem_ld32(t_row + T_DW2 + c0, v);
+#pragma unroll
+    for (int k = 0; k < 32; k += 4)
+      *reinterpret_cast<float4*>(g2 + c0 + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+    if (h == 0) {
+      g3[HID] = acc_db3;
+      g2[HID] = acc_db2;
+      float* g1 = a.G1 + (static_cast<long long>(blockIdx.x) * HID + o) * G1_N;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) g1[i] = acc_dw1[i];
+      g1[4] = acc_db1;
+      float* gh = a.GH + static_cast<long long>(blockIdx.x) * 130;
+      gh[t] = acc_dw4;
+      if (t == 0) {
+        gh[128] = acc_db4;
+        gh[129] = acc_loss;
+        if (blockIdx.x == 0) a.step[0] += 1;
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 512);
+  }
+}
+
 __global__ void k_fill_f32(float* p, long long n, float v)
 {
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
@@ -568,10 +1045,14 @@ __global__ void k_fill_f32(float* p, long long n, float v)
 
 struct Net {
   int device = 0;
+  int n_sm = 0;
   long long cap = 0;  // rows (multiple of 128)
   long long n = 0, R = 0;
   int splits = 0, k_split = 0;
   int max_splits = 0;
+  int fused_grid = 0;     // CTAs of the last fused launch (= its gradient partials)
+  bool graph_fused = false;
+  bool prepared = false;  // staged rows converted for the layer-by-layer kernels
   cudaStream_t stream = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -585,6 +1066,7 @@ struct Net {
   float *G1 = nullptr, *G2 = nullptr, *G3 = nullptr, *GH = nullptr;
   // data and activations
   float *x4 = nullptr, *target = nullptr, *weight = nullptr, *y = nullptr;
+  // layer-by-layer kernels only (allocated on first use)
   __nv_bfloat16 *X0 = nullptr, *X0T = nullptr;
   float *Z1 = nullptr, *Z2 = nullptr, *Z3 = nullptr;
   __nv_bfloat16 *H1 = nullptr, *H2 = nullptr, *H3 = nullptr, *H1T = nullptr, *H2T = nullptr;
@@ -618,6 +1100,7 @@ static void set_gemm_attributes(int dev)
   MLP_CK(cudaFuncSetAttribute(k_gemm<EPI_FORWARD>, cudaFuncAttributeMaxDynamicSharedMemorySize, GEMM_SMEM));
   MLP_CK(cudaFuncSetAttribute(k_gemm<EPI_DINPUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, GEMM_SMEM));
   MLP_CK(cudaFuncSetAttribute(k_gemm<EPI_DWEIGHT>, cudaFuncAttributeMaxDynamicSharedMemorySize, GEMM_SMEM));
+  MLP_CK(cudaFuncSetAttribute(k_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM));
   if (dev >= 0 && dev < 64) g_attr_set[dev] = true;
 }
 
@@ -641,6 +1124,7 @@ static void launch_gemm(Net& N, const GemmArgs& g, int grid)
 static void enqueue_forward(Net& N, bool train, float* y_out)
 {
   const int tiles = static_cast<int>(N.R / TILE_M);
+  N.fused_grid = 0;
   const int ldT = static_cast<int>(N.R);
   GemmArgs g = gemm_args(N);
   g.A = N.X0; g.lda = IN_PAD; g.B = N.W1; g.ldb = IN_PAD; g.K = IN_PAD; g.N = HID;
@@ -685,13 +1169,80 @@ static void enqueue_backward(Net& N)
   launch_gemm<EPI_DWEIGHT>(N, g, N.splits);
 }
 
+// Activation buffers of the layer-by-layer kernels (cap rows each), and the
+// staged rows converted to their BF16 input tiles.
+static void prepare_layers(Net& N)
+{
+  if (!N.Z1) {
+    const long long R = N.cap;
+    N.X0 = N.alloc<__nv_bfloat16>(R * IN_PAD);
+    N.X0T = N.alloc<__nv_bfloat16>(R * IN_PAD);
+    N.Z1 = N.alloc<float>(R * HID);
+    N.Z2 = N.alloc<float>(R * HID);
+    N.Z3 = N.alloc<float>(R * HID);
+    N.H1 = N.alloc<__nv_bfloat16>(R * HID);
+    N.H2 = N.alloc<__nv_bfloat16>(R * HID);
+    N.H3 = N.alloc<__nv_bfloat16>(R * HID);
+    N.H1T = N.alloc<__nv_bfloat16>(R * MAX_N);
+    N.H2T = N.alloc<__nv_bfloat16>(R * MAX_N);
+    N.dZ1 = N.alloc<__nv_bfloat16>(R * HID);
+    N.dZ2 = N.alloc<__nv_bfloat16>(R * HID);
+    N.dZ3 = N.alloc<__nv_bfloat16>(R * HID);
+    N.dZ1T = N.alloc<__nv_bfloat16>(R * HID);
+    N.dZ2T = N.alloc<__nv_bfloat16>(R * HID);
+    N.dZ3T = N.alloc<__nv_bfloat16>(R * HID);
+  }
+  if (!N.prepared && N.R > 0) {
+    k_prepare<<<152, 256, 0, N.stream>>>(N.x4, N.n, N.R, N.X0, N.X0T, N.H1T, N.H2T);
+    MLP_CK(cudaGetLastError());
+    N.prepared = true;
+  }
+}
+
+// The fused kernel over the N.R staged rows: a training pass (gradient
+// partials, one per CTA) or the forward pass into y_out.
+static void enqueue_fused(Net& N, bool train, float* y_out)
+{
+  const int tiles = static_cast<int>(N.R / TILE_M);
+  FusedArgs f;
+  std::memset(&f, 0, sizeof(f));
+  f.x4 = N.x4;
+  f.target = N.target;
+  f.weight = N.weight;
+  f.n = N.n;
+  f.tiles = tiles;
+  f.train = train ? 1 : 0;
+  f.inv_n = N.n > 0 ? 1.0f / static_cast<float>(N.n) : 0.0f;
+  f.W1 = N.W1;
+  f.W2 = N.W2;
+  f.W3 = N.W3;
+  f.P = N.P;
+  f.y_out = y_out;
+  f.G1 = N.G1;
+  f.G2 = N.G2;
+  f.G3 = N.G3;
+  f.GH = N.GH;
+  f.step = N.step;
+  f.error = N.err;
+  const int grid = std::max(1, std::min(tiles, N.n_sm));
+  k_fused<<<grid, F_THREADS, F_SMEM, N.stream>>>(f);
+  MLP_CK(cudaGetLastError());
+  N.fused_grid = grid;
+}
+
 static AdamArgs adam_args(Net& N, int update, float lr)
 {
   AdamArgs a;
   std::memset(&a, 0, sizeof(a));
   a.P = N.P; a.m = N.m; a.v = N.v;
   a.G1 = N.G1; a.G2 = N.G2; a.G3 = N.G3; a.GH = N.GH;
-  a.splits = N.splits; a.head_blocks = static_cast<int>(N.R / TILE_M);
+  if (N.fused_grid > 0) {
+    a.splits = N.fused_grid;
+    a.head_blocks = N.fused_grid;
+  } else {
+    a.splits = N.splits;
+    a.head_blocks = static_cast<int>(N.R / TILE_M);
+  }
   a.lr = lr; a.beta1 = 0.9f; a.beta2 = 0.999f; a.eps = 1e-8f;
   a.step = N.step; a.update = update;
   a.W1 = N.W1; a.W2 = N.W2; a.W2T = N.W2T; a.W3 = N.W3; a.W3T = N.W3T;
@@ -772,12 +1323,30 @@ extern "C" int OPENMC_E_ALLOCATE;
 extern "C" int OPENMC_E_INVALID_ARGUMENT;
 extern "C" int OPENMC_E_UNASSIGNED;
 
+extern "C" {
+// 1 (default): each training step and query runs the fused per-tile kernel;
+// 0: the layer-by-layer kernels (activations through device memory).
+int openmc_gb300_mlp_fused = 1;
+}
+
 namespace {
 
 int fail(int code, const char* what)
 {
   std::snprintf(openmc_err_msg, sizeof(openmc_err_msg), "%s", what);
   return code;
+}
+
+// One forward (+ backward when training) pass over the staged rows.
+void enqueue_pass(mlp::Net& N, bool train, float* y_out)
+{
+  if (openmc_gb300_mlp_fused) {
+    mlp::enqueue_fused(N, train, y_out);
+  } else {
+    mlp::prepare_layers(N);
+    mlp::enqueue_forward(N, train, y_out);
+    if (train) mlp::enqueue_backward(N);
+  }
 }
 
 }  // namespace
@@ -797,6 +1366,7 @@ int openmc_gb300_mlp_create(int64_t max_rows, uint64_t seed, void** handle)
   try {
     N = new Net();
     MLP_CK(cudaGetDevice(&N->device));
+    MLP_CK(cudaDeviceGetAttribute(&N->n_sm, cudaDevAttrMultiProcessorCount, N->device));
     set_gemm_attributes(N->device);
     MLP_CK(cudaStreamCreateWithFlags(&N->stream, cudaStreamNonBlocking));
     N->cap = (max_rows + TILE_M - 1) / TILE_M * TILE_M;
@@ -823,22 +1393,6 @@ int openmc_gb300_mlp_create(int64_t max_rows, uint64_t seed, void** handle)
     N->target = N->alloc<float>(R);
     N->weight = N->alloc<float>(R);
     N->y = N->alloc<float>(R);
-    N->X0 = N->alloc<__nv_bfloat16>(R * IN_PAD);
-    N->X0T = N->alloc<__nv_bfloat16>(R * IN_PAD);
-    N->Z1 = N->alloc<float>(R * HID);
-    N->Z2 = N->alloc<float>(R * HID);
-    N->Z3 = N->alloc<float>(R * HID);
-    N->H1 = N->alloc<__nv_bfloat16>(R * HID);
-    N->H2 = N->alloc<__nv_bfloat16>(R * HID);
-    N->H3 = N->alloc<__nv_bfloat16>(R * HID);
-    N->H1T = N->alloc<__nv_bfloat16>(R * MAX_N);
-    N->H2T = N->alloc<__nv_bfloat16>(R * MAX_N);
-    N->dZ1 = N->alloc<__nv_bfloat16>(R * HID);
-    N->dZ2 = N->alloc<__nv_bfloat16>(R * HID);
-    N->dZ3 = N->alloc<__nv_bfloat16>(R * HID);
-    N->dZ1T = N->alloc<__nv_bfloat16>(R * HID);
-    N->dZ2T = N->alloc<__nv_bfloat16>(R * HID);
-    N->dZ3T = N->alloc<__nv_bfloat16>(R * HID);
     std::vector<float> p = init_params(seed);
     upload_params(*N, p.data());
     *handle = N;
@@ -883,8 +1437,8 @@ int openmc_gb300_mlp_set_data(void* handle, int64_t n, const float* x4, const fl
       k_fill_f32<<<64, 256, 0, N->stream>>>(N->weight, R, 1.0f);
       MLP_CK(cudaGetLastError());
     }
-    k_prepare<<<152, 256, 0, N->stream>>>(N->x4, n, R, N->X0, N->X0T, N->H1T, N->H2T);
-    MLP_CK(cudaGetLastError());
+    N->prepared = false;
+    if (N->Z1) prepare_layers(*N);
     MLP_CK(cudaStreamSynchronize(N->stream));
     drop_graph(*N);
     return 0;
@@ -906,17 +1460,19 @@ int openmc_gb300_mlp_train(void* handle, int steps, double lr, float* loss_histo
     MLP_CK(cudaMemcpyAsync(&t0, N->step, sizeof(int), cudaMemcpyDeviceToHost, N->stream));
     MLP_CK(cudaStreamSynchronize(N->stream));
     if (t0 + steps > N->loss_cap) return fail(OPENMC_E_INVALID_ARGUMENT, "too many optimizer steps");
-    if (!N->exec || N->graph_lr != static_cast<float>(lr)) {
+    const bool fused = openmc_gb300_mlp_fused != 0;
+    if (!N->exec || N->graph_lr != static_cast<float>(lr) || N->graph_fused != fused) {
       drop_graph(*N);
+      if (!fused) prepare_layers(*N);  // buffers and input tiles outside the capture
       MLP_CK(cudaStreamBeginCapture(N->stream, cudaStreamCaptureModeThreadLocal));
-      enqueue_forward(*N, true, nullptr);
-      enqueue_backward(*N);
+      enqueue_pass(*N, true, nullptr);
       AdamArgs a = adam_args(*N, 1, static_cast<float>(lr));
       a.loss_out = N->loss_hist;
       enqueue_adam(*N, a);
       MLP_CK(cudaStreamEndCapture(N->stream, &N->graph));
       MLP_CK(cudaGraphInstantiate(&N->exec, N->graph, 0));
       N->graph_lr = static_cast<float>(lr);
+      N->graph_fused = fused;
     }
     cudaEvent_t e0, e1;
     MLP_CK(cudaEventCreate(&e0));
@@ -948,15 +1504,15 @@ int openmc_gb300_mlp_gradients(void* handle, float* grad, float* loss)
     int t0 = 0;
     MLP_CK(cudaMemcpyAsync(&t0, N->step, sizeof(int), cudaMemcpyDeviceToHost, N->stream));
     MLP_CK(cudaStreamSynchronize(N->stream));
-    enqueue_forward(*N, true, nullptr);
-    enqueue_backward(*N);
+    enqueue_pass(*N, true, nullptr);
     AdamArgs a = adam_args(*N, 0, 0.0f);
     a.grad_out = N->grad;
     enqueue_adam(*N, a);
     check_error(*N);
     MLP_CK(cudaMemcpy(grad, N->grad, sizeof(float) * N_PARAMS, cudaMemcpyDeviceToHost));
     if (loss) {
-      std::vector<float> gh(static_cast<size_t>(N->R / TILE_M) * 130);
+      const long long blocks = N->fused_grid > 0 ? N->fused_grid : N->R / TILE_M;
+      std::vector<float> gh(static_cast<size_t>(blocks) * 130);
       MLP_CK(cudaMemcpy(gh.data(), N->GH, sizeof(float) * gh.size(), cudaMemcpyDeviceToHost));
       float s = 0.0f;
       for (size_t b = 0; b < gh.size() / 130; ++b) s += gh[b * 130 + 129];
@@ -986,14 +1542,14 @@ int openmc_gb300_mlp_predict(void* handle, int64_t n, const float* x4, float* y)
       N->n = c;
       N->R = R;
       MLP_CK(cudaMemcpyAsync(N->x4, x4 + off * 4, sizeof(float) * 4 * c, cudaMemcpyHostToDevice, N->stream));
-      k_prepare<<<152, 256, 0, N->stream>>>(N->x4, c, R, N->X0, N->X0T, nullptr, nullptr);
-      MLP_CK(cudaGetLastError());
-      enqueue_forward(*N, false, N->y);
+      N->prepared = false;
+      enqueue_pass(*N, false, N->y);
       check_error(*N);
       MLP_CK(cudaMemcpy(y + off, N->y, sizeof(float) * c, cudaMemcpyDeviceToHost));
     }
     N->n = 0;
     N->R = 0;
+    N->prepared = false;
     return 0;
   } catch (const std::exception& e) {
     return fail(OPENMC_E_UNASSIGNED, e.what());

@@ -217,6 +217,7 @@ class _Settings:
     stage_tables = _DLLGlobal(C.c_int, "openmc_gb300_stage_tables")
     contract = _DLLGlobal(C.c_int, "openmc_gb300_contract")
     defer_tally = _DLLGlobal(C.c_int, "openmc_gb300_defer_tally")
+    mlp_fused = _DLLGlobal(C.c_int, "openmc_gb300_mlp_fused")
 
     @property
     def seed(self):

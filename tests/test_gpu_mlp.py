@@ -30,11 +30,24 @@ def _blocks(v):
     return out
 
 
-@pytest.mark.parametrize("n", [1000, 777, 5000])
-def test_gradients_match_oracle(built, n):
+@pytest.fixture(params=[1, 0], ids=["fused", "layers"])
+def kernels(request, built):
+    """Runs a test with the fused per-tile kernel and with the layer-by-layer
+    kernels."""
+    from openmc_gb300 import lib
+    old = lib.settings.mlp_fused
+    lib.settings.mlp_fused = request.param
+    yield request.param
+    lib.settings.mlp_fused = old
+
+
+# 60,000 rows = 469 tiles: several tiles per CTA of the fused kernel, whose
+# weight-gradient accumulators then run across tiles
+@pytest.mark.parametrize("n", [1000, 777, 5000, 60000])
+def test_gradients_match_oracle(kernels, n):
     from openmc_gb300 import lib
     x, t, w = _data(n, n)
-    net = lib.ImportanceNetwork(max_rows=8192, seed=11)
+    net = lib.ImportanceNetwork(max_rows=max(8192, n), seed=11)
     net.set_data(x, t, w)
     p = net.params.astype(np.float64)
     loss_gpu, g_gpu = net.gradients()
@@ -50,7 +63,7 @@ def test_gradients_match_oracle(built, n):
     net.close()
 
 
-def test_forward_matches_oracle(built):
+def test_forward_matches_oracle(kernels):
     from openmc_gb300 import lib
     x, _, _ = _data(3001, 3)
     net = lib.ImportanceNetwork(max_rows=1024, seed=5)  # several capacity chunks
@@ -61,7 +74,7 @@ def test_forward_matches_oracle(built):
     net.close()
 
 
-def test_adam_step_matches_oracle(built):
+def test_adam_step_matches_oracle(kernels):
     from openmc_gb300 import lib
     x, t, w = _data(2000, 9)
     net = lib.ImportanceNetwork(max_rows=4096, seed=2)
@@ -77,7 +90,32 @@ def test_adam_step_matches_oracle(built):
     net.close()
 
 
-def test_training_fits_smooth_target(built):
+def test_fused_and_layer_kernels_agree(built):
+    """The two kernel sets round at the same places; they differ only in the
+    order of FP32 sums and in the last bits of the SiLU, so their gradients
+    agree far more closely than either does with the FP64 oracle."""
+    from openmc_gb300 import lib
+    x, t, w = _data(40000, 17)
+    old = lib.settings.mlp_fused
+    out = {}
+    try:
+        for mode in (1, 0):
+            lib.settings.mlp_fused = mode
+            net = lib.ImportanceNetwork(max_rows=40000, seed=3)
+            net.set_data(x, t, w)
+            out[mode] = net.gradients() + (net.predict(x[:3000]),)
+            net.close()
+    finally:
+        lib.settings.mlp_fused = old
+    (la, ga, ya), (lb, gb, yb) = out[1], out[0]
+    assert abs(la - lb) <= 1e-4 * abs(lb)
+    bf, bl = _blocks(ga), _blocks(gb)
+    for name in bf:
+        assert np.linalg.norm(bf[name] - bl[name]) <= 5e-3 * np.linalg.norm(bl[name]), name
+    assert np.abs(ya - yb).max() <= 1e-2 * np.std(yb) + 1e-5
+
+
+def test_training_fits_smooth_target(kernels):
     from openmc_gb300 import lib
     x, t, _ = _data(20000, 21)
     net = lib.ImportanceNetwork(max_rows=20000, seed=4)

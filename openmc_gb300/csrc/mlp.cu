@@ -561,7 +561,9 @@ __global__ void k_prepare(const float* __restrict__ x4, long long n, long long R
 // element (r, f) at byte ((r/8) 16 + f/8) 128 + (r%8) 16 + (f%8) 2.  The
 // products that need a transposed operand (input gradients dZ W: B = W^T;
 // weight gradients dZ^T H: A = dZ^T, B = H^T) read the same tiles through
-// MN-major descriptors, so no tile is ever written twice.  Tensor memory
+// MN-major descriptors, so no tile is ever written twice.  (The 128-byte
+// swizzled layout, which would also serve both readings, measured 2-3 %
+// slower in the products.)  Tensor memory
 // (512 columns) holds Z2 / dH1 (columns 0-127), Z3 / dH2 and the per-tile
 // column sums (128-255), and the dW3 and dW2 accumulators (256-383,
 // 384-511), which run over all of the CTA's tiles.  Bias gradients and dW1
@@ -611,6 +613,7 @@ struct FusedArgs {
   int* error;
 };
 
+// byte offset of element (r, f) of a 128 x 128 tile
 __device__ __forceinline__ uint32_t tile_off(int r, int f)
 {
   return static_cast<uint32_t>((((r >> 3) * 16 + (f >> 3)) << 7) + ((r & 7) << 4) + ((f & 7) << 1));
@@ -624,19 +627,108 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
 
 __device__ __forceinline__ float bf16_round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
 
-__device__ __forceinline__ float sigm(float z) { return __fdividef(1.0f, 1.0f + __expf(-z)); }
-
-// 8 consecutive FP32 accumulator columns of this thread's row
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v)
+// Logistic function 1 / (1 + e^-z) = 1 / (1 + 2^(-z log2 e)) from the
+// approximate base-2 exponential and reciprocal of the special-function
+// unit (each within a few units in the last place of FP32; the results are
+// rounded to BF16).
+// Large negative z gives 1 / inf = 0, large positive z gives 1.
+// Two columns at a time: the FP32 arithmetic of the epilogues runs as packed
+// two-wide operations (fma / add / mul .f32x2), the special-function steps
+// per column.
+__device__ __forceinline__ float ex2_approx(float x)
 {
-  uint32_t r[8];
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+__device__ __forceinline__ float rcp_approx(float x)
+{
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+__device__ __forceinline__ float2 sigm2(float2 z)
+{
+  const float2 m = __fmul2_rn(z, make_float2(-1.4426950408889634f, -1.4426950408889634f));
+  const float2 d = __fadd2_rn(make_float2(ex2_approx(m.x), ex2_approx(m.y)), make_float2(1.0f, 1.0f));
+  return make_float2(rcp_approx(d.x), rcp_approx(d.y));
+}
+
+// SiLU derivative from z and s = sigmoid(z): s (1 + z (1 - s))
+__device__ __forceinline__ float2 silu_grad2(float2 z, float2 s)
+{
+  const float2 one = make_float2(1.0f, 1.0f);
+  const float2 oms = __ffma2_rn(s, make_float2(-1.0f, -1.0f), one);
+  return __fmul2_rn(s, __ffma2_rn(z, oms, one));
+}
+
+// 16 consecutive FP32 accumulator columns of this thread's row
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
+{
+  uint32_t r[16];
+  asm volatile(
+    "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+    "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+    : "r"(taddr)
+    : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+// Issues a load of 16 consecutive FP32 accumulator columns without waiting
+// (tmem_wait16 / tmem_wait8 complete it)
+__device__ __forceinline__ void tmem_ld16_issue(uint32_t taddr, uint32_t (&r)[16])
+{
+  asm volatile(
+    "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+    "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+    : "r"(taddr)
+    : "memory");
+}
+
+// Waits for this thread's outstanding tensor-memory loads.  The destination
+// registers of the loads pass through the instruction, so no use of them
+// can be placed before it.
+__device__ __forceinline__ void tmem_wait16(uint32_t* r)
+{
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                 "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                 "+r"(r[15])
+               :
+               : "memory");
+}
+
+// 8 consecutive FP32 accumulator columns of this thread's row, not waited for
+__device__ __forceinline__ void tmem_ld8_issue(uint32_t taddr, uint32_t* r)
+{
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
                : "r"(taddr)
                : "memory");
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int k = 0; k < 8; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+__device__ __forceinline__ void tmem_wait8(uint32_t* r)
+{
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7])
+               :
+               : "memory");
+}
+
+// 8 consecutive floats of a 16-byte aligned shared-memory array
+__device__ __forceinline__ void load_f32x8(const float* p, float* v)
+{
+  const float4 a = reinterpret_cast<const float4*>(p)[0], b = reinterpret_cast<const float4*>(p)[1];
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+  v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
 }
 
 // Sums 32 values over the 32 lanes of a warp, one column per lane: on
@@ -658,11 +750,13 @@ __device__ __forceinline__ float lane_column_sums(float (&v)[32], int lane)
 }
 
 // An operand of one product: the tile's shared-memory address, whether it is
-// read MN-major, and the shape of its layout.
+// read MN-major, the bytes its descriptor advances per K step of 16, and
+// the descriptor's leading (K direction) / stride (M or N direction) byte
+// offsets between core matrices.
 struct Operand {
   uint32_t addr;
   bool mn;
-  uint32_t kstep, lbo, sbo;  // bytes per K step of 16, leading / stride byte offsets
+  uint32_t kstep, lbo, sbo;
 };
 
 // 128 x 128 tile by feature, read with K = features (K-major) or K = rows
@@ -675,26 +769,30 @@ __device__ __forceinline__ Operand big_tile(uint32_t addr, bool mn)
 // 128 x 16 input tile read MN-major (N = the 16 input columns, K = rows)
 __device__ __forceinline__ Operand x0_tile(uint32_t addr) { return Operand{addr, true, 512u, 256u, 128u}; }
 
-// D (+)= A B^T over K = 128 in 8 steps of 16 (issued by one thread)
+__device__ __forceinline__ uint64_t op_desc(const Operand& o, int j)
+{
+  return smem_desc(o.addr + j * o.kstep, o.lbo, o.sbo);
+}
+
+// D (+)= A B^T over K = 128 in 8 steps of 16 (issued by one thread; an
+// issue is accepted about as fast as the tensor core retires products)
 __device__ __forceinline__ void issue_product(uint32_t d, const Operand& a, const Operand& b, int n, bool accumulate)
 {
   const uint32_t idesc = instr_desc(TILE_M, n) | (a.mn ? 1u << 15 : 0u) | (b.mn ? 1u << 16 : 0u);
 #pragma unroll 1
-  for (int j = 0; j < HID / 16; ++j) {
-    const uint64_t ad = smem_desc(a.addr + j * a.kstep, a.lbo, a.sbo);
-    const uint64_t bd = smem_desc(b.addr + j * b.kstep, b.lbo, b.sbo);
-    mma_bf16(d, ad, bd, idesc, (accumulate || j > 0) ? 1u : 0u);
-  }
+  for (int j = 0; j < HID / 16; ++j) mma_bf16(d, op_desc(a, j), op_desc(b, j), idesc, (accumulate || j > 0) ? 1u : 0u);
 }
 
 __global__ void __launch_bounds__(F_THREADS, 1) k_fused(FusedArgs a)
 {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  float4* sW1 = reinterpret_cast<float4*>(base + F_PAR);  // W1 row o (BF16 values)
+  // layer-1 weights (BF16 values) by neuron pair p = (2p, 2p + 1):
+  // sW1[2p] = (W1[2p][0], W1[2p+1][0], W1[2p][1], W1[2p+1][1]), sW1[2p+1] the same for inputs 2, 3
+  float4* sW1 = reinterpret_cast<float4*>(base + F_PAR);
   float* sb1 = reinterpret_cast<float*>(sW1 + HID);
   float* sb2 = sb1 + HID;
-  float2* sb3w4 = reinterpret_cast<float2*>(sb2 + HID);  // (b3, w4) of neuron o
+  float4* sb3w4 = reinterpret_cast<float4*>(sb2 + HID);  // pair p: (b3[2p], b3[2p+1], w4[2p], w4[2p+1])
   float* s_red = reinterpret_cast<float*>(base + F_RED);
   float* s_ypart = s_red + 4 * HID;
   float* s_misc = s_ypart + F_GROUPS * HID;
@@ -702,9 +800,13 @@ __global__ void __launch_bounds__(F_THREADS, 1) k_fused(FusedArgs a)
   __shared__ uint32_t tmem_s;
 
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  // A warp reaches tensor-memory lanes 32 (warp mod 4) .. + 31: quarter
+  // q = warp mod 4, column group h = warp / 4.  Thread 0 also issues the
+  // products.
   const int q = warp & 3, h = warp >> 2;
   const int r = 32 * q + lane;  // row of the tile (tensor-memory lane) this thread works on
   const int c0 = F_COLS * h;    // its columns [c0, c0 + F_COLS)
+  const bool issuer = t == 0;
   const uint32_t sbase = smem_u32(base);
 
   if (warp == 0) tmem_alloc(&tmem_s, 512);
@@ -721,12 +823,14 @@ __global__ void __launch_bounds__(F_THREADS, 1) k_fused(FusedArgs a)
     *reinterpret_cast<uint4*>(base + (w ? F_W3 : F_W2) + tile_off(o, g * 8)) = *reinterpret_cast<const uint4*>(src);
   }
   for (int o = t; o < HID; o += F_THREADS) {
-    const __nv_bfloat16* w1 = a.W1 + o * IN_PAD;
-    sW1[o] = make_float4(__bfloat162float(w1[0]), __bfloat162float(w1[1]), __bfloat162float(w1[2]),
-                         __bfloat162float(w1[3]));
+    const int p = o >> 1, u = o & 1;
+    float* w = reinterpret_cast<float*>(sW1 + 2 * p);
+    for (int i = 0; i < 4; ++i) w[(i >> 1) * 4 + (i & 1) * 2 + u] = __bfloat162float(a.W1[o * IN_PAD + i]);
     sb1[o] = a.P[P_B1 + o];
     sb2[o] = a.P[P_B2 + o];
-    sb3w4[o] = make_float2(a.P[P_B3 + o], a.P[P_W4 + o]);
+    float* bw = reinterpret_cast<float*>(sb3w4 + p);
+    bw[u] = a.P[P_B3 + o];
+    bw[2 + u] = a.P[P_W4 + o];
   }
   const float b4 = a.P[P_B4];
   fence_async_shared();
@@ -755,10 +859,13 @@ __global__ void __launch_bounds__(F_THREADS, 1) k_fused(FusedArgs a)
     tc_fence_after();
     return all;
   };
-  // pre-activation of layer 1 for neuron o
-  auto z1_of = [&](const float (&x)[4], int o) {
-    const float4 w = sW1[o];
-    return fmaf(x[3], w.w, fmaf(x[2], w.z, fmaf(x[1], w.y, fmaf(x[0], w.x, sb1[o]))));
+  // pre-activations of layer 1 for neurons o, o + 1 (o even) with biases b
+  auto z1_of = [&](const float2 (&xx)[4], int o, float2 b) {
+    const float4 wa = sW1[o], wb = sW1[o + 1];
+    float2 z = __ffma2_rn(xx[0], make_float2(wa.x, wa.y), b);
+    z = __ffma2_rn(xx[1], make_float2(wa.z, wa.w), z);
+    z = __ffma2_rn(xx[2], make_float2(wb.x, wb.y), z);
+    return __ffma2_rn(xx[3], make_float2(wb.z, wb.w), z);
   };
 
   // inputs of this thread's row, loaded one tile ahead
@@ -780,24 +887,31 @@ __global__ void __launch_bounds__(F_THREADS, 1) k_fused(FusedArgs a)
     }
     // ---- layer 1 on the CUDA cores: H1 = silu(X0 W1^T + b1)
     const float x[4] = {bf16_round(x_next.x), bf16_round(x_next.y), bf16_round(x_next.z), bf16_round(x_next.w)};
+    const float2 xx[4] = {make_float2(x[0], x[0]), make_float2(x[1], x[1]), make_float2(x[2], x[2]),
+                          make_float2(x[3], x[3])};
     x_next = load_x(tile + gridDim.x);
     if (h == 0) {
       *reinterpret_cast<uint4*>(base + F_X0 + ((r >> 3) * 2 << 7) + ((r & 7) << 4)) =
         make_uint4(pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(1.0f, 0.0f), 0u);
       *reinterpret_cast<uint4*>(base + F_X0 + (((r >> 3) * 2 + 1) << 7) + ((r & 7) << 4)) = make_uint4(0u, 0u, 0u, 0u);
     }
+    {
 #pragma unroll
-    for (int g = 0; g < F_COLS / 8; ++g) {
-      uint32_t pk[4];
+      for (int g = 0; g < F_COLS / 8; ++g) {
+        uint32_t pk[4];
+        float b[8];
+        load_f32x8(sb1 + c0 + 8 * g, b);
 #pragma unroll
-      for (int e = 0; e < 8; e += 2) {
-        const float z0 = z1_of(x, c0 + 8 * g + e), z1 = z1_of(x, c0 + 8 * g + e + 1);
-        pk[e / 2] = pack_bf16(z0 * sigm(z0), z1 * sigm(z1));
+        for (int e = 0; e < 8; e += 2) {
+          const float2 z = z1_of(xx, c0 + 8 * g + e, make_float2(b[e], b[e + 1]));
+          const float2 hv = __fmul2_rn(z, sigm2(z));
+          pk[e / 2] = pack_bf16(hv.x, hv.y);
+        }
+        *reinterpret_cast<uint4*>(base + F_H1 + tile_off(r, c0 + 8 * g)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
       }
-      *reinterpret_cast<uint4*>(base + F_H1 + tile_off(r, c0 + 8 * g)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
     }
     if (!tiles_ready()) break;
-    if (t == 0) {
+    if (issuer) {
       issue_product(tmem + T_R0, big_tile(sbase + F_H1, false), big_tile(sbase + F_W2, false), HID, false);
       mma_commit(&mbar);
     }
@@ -809,43 +923,50 @@ __global__ void __launch_bounds__(F_THREADS, 1) k_fused(FusedArgs a)
 #pragma unroll
       for (int g = 0; g < 4; ++g) {
         uint32_t pk[4];
+        float b[8];
+        load_f32x8(sb2 + c0 + 8 * g, b);
 #pragma unroll
         for (int e = 0; e < 8; e += 2) {
-          const int k = 8 * g + e, o = c0 + k;
-          const float z0 = v[k] + sb2[o], z1 = v[k + 1] + sb2[o + 1];
-          pk[e / 2] = pack_bf16(z0 * sigm(z0), z1 * sigm(z1));
+          const int k = 8 * g + e;
+          const float2 z = __fadd2_rn(make_float2(v[k], v[k + 1]), make_float2(b[e], b[e + 1]));
+          const float2 hv = __fmul2_rn(z, sigm2(z));
+          pk[e / 2] = pack_bf16(hv.x, hv.y);
         }
         *reinterpret_cast<uint4*>(base + F_H2 + tile_off(r, c0 + 8 * g)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
       }
     }
     if (!tiles_ready()) break;
-    if (t == 0) {
+    if (issuer) {
       issue_product(tmem + T_R1, big_tile(sbase + F_H2, false), big_tile(sbase + F_W3, false), HID, false);
       mma_commit(&mbar);
     }
     wait_products();
     // ---- layer 3 epilogue and the output layer: H3 = silu(Z3 + b3),
     // y = H3 . w4 + b4; g3 = w4 silu'(Z3) is kept for dZ3 = dy g3
-    float g3[32];
+    float2 g3[16];
     uint32_t h3[16];
     float ypart = 0.0f;
     {
-      float v[32];
-      tmem_ld32(t_row + T_R1 + c0, v);
+      float2 yp = make_float2(0.0f, 0.0f);
 #pragma unroll
-      for (int k = 0; k < 32; k += 2) {
-        float hb[2];
+      for (int half = 0; half < 32; half += 16) {
+        float v[16];
+        tmem_ld16(t_row + T_R1 + c0 + half, v);
 #pragma unroll
-        for (int u = 0; u < 2; ++u) {
-          const float2 bw = sb3w4[c0 + k + u];
-          const float z = v[k + u] + bw.x;
-          const float s = sigm(z);
-          hb[u] = bf16_round(z * s);
-          ypart = fmaf(hb[u], bw.y, ypart);
-          g3[k + u] = bw.y * (s * (1.0f + z * (1.0f - s)));
+        for (int k = 0; k < 16; k += 2) {
+          const int kk = half + k;
+          const float4 bw = sb3w4[(c0 + kk) >> 1];  // b3, w4 of neurons c0 + kk, c0 + kk + 1
+          const float2 w4 = make_float2(bw.z, bw.w);
+          const float2 z = __fadd2_rn(make_float2(v[k], v[k + 1]), make_float2(bw.x, bw.y));
+          const float2 sg = sigm2(z);
+          const float2 hv = __fmul2_rn(z, sg);
+          h3[kk / 2] = pack_bf16(hv.x, hv.y);
+          const __nv_bfloat162 hp = *reinterpret_cast<const __nv_bfloat162*>(&h3[kk / 2]);
+          yp = __ffma2_rn(make_float2(__low2float(hp), __high2float(hp)), w4, yp);
+          g3[kk / 2] = __fmul2_rn(w4, silu_grad2(z, sg));
         }
-        h3[k / 2] = pack_bf16(hb[0], hb[1]);
       }
+      ypart = yp.x + yp.y;
     }
     s_ypart[h * HID + r] = ypart;
     __syncthreads();
@@ -863,11 +984,16 @@ __global__ void __launch_bounds__(F_THREADS, 1) k_fused(FusedArgs a)
       dy = 2.0f * wt * e * a.inv_n;
     }
     // dZ3 = bf16(dy g3) into its tile; dw4 = sum over rows of dy H3
+    const float2 dy2 = make_float2(dy, dy);
+    {
 #pragma unroll
     for (int g = 0; g < 4; ++g) {
       uint32_t pk[4];
 #pragma unroll
-      for (int e = 0; e < 8; e += 2) pk[e / 2] = pack_bf16(dy * g3[8 * g + e], dy * g3[8 * g + e + 1]);
+      for (int e = 0; e < 8; e += 2) {
+        const float2 d = __fmul2_rn(dy2, g3[(8 * g + e) / 2]);
+        pk[e / 2] = pack_bf16(d.x, d.y);
+      }
       *reinterpret_cast<uint4*>(base + F_DZ3 + tile_off(r, c0 + 8 * g)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
     }
     {
@@ -875,10 +1001,12 @@ __global__ void __launch_bounds__(F_THREADS, 1) k_fused(FusedArgs a)
 #pragma unroll
       for (int k = 0; k < 32; k += 2) {
         const __nv_bfloat162 p = *reinterpret_cast<const __nv_bfloat162*>(&h3[k / 2]);
-        v[k] = dy * __low2float(p);
-        v[k + 1] = dy * __high2float(p);
+        const float2 d = __fmul2_rn(dy2, make_float2(__low2float(p), __high2float(p)));
+        v[k] = d.x;
+        v[k + 1] = d.y;
       }
       s_red[q * HID + c0 + lane] = lane_column_sums(v, lane);
+    }
     }
     if (h == 0) {
       float sd = dy, sl = loss;
@@ -893,10 +1021,12 @@ __global__ void __launch_bounds__(F_THREADS, 1) k_fused(FusedArgs a)
       }
     }
     if (!tiles_ready()) break;
-    if (t < HID) acc_dw4 += ((s_red[t] + s_red[HID + t]) + s_red[2 * HID + t]) + s_red[3 * HID + t];
-    if (t == 0) {
+    if (h == 0) acc_dw4 += ((s_red[r] + s_red[HID + r]) + s_red[2 * HID + r]) + s_red[3 * HID + r];
+    if (issuer) {
       acc_db4 += ((s_misc[0] + s_misc[1]) + s_misc[2]) + s_misc[3];
       acc_loss += ((s_misc[4] + s_misc[5]) + s_misc[6]) + s_misc[7];
+    }
+    if (issuer) {
       // dH2 = dZ3 W3 (B = W3 read MN-major); dW3 += dZ3^T H2 runs on
       // while dZ2 is formed (it reads neither tensor-memory columns 0-255
       // nor the dZ2 tile)
@@ -907,29 +1037,34 @@ __global__ void __launch_bounds__(F_THREADS, 1) k_fused(FusedArgs a)
     wait_products();
     // ---- dZ2 = bf16(dH2 silu'(Z2)), Z2 still in columns 0-127
     {
-      float dh[32], z[32];
-      tmem_ld32(t_row + T_R1 + c0, dh);
-      tmem_ld32(t_row + T_R0 + c0, z);
 #pragma unroll
-      for (int g = 0; g < 4; ++g) {
-        uint32_t pk[4];
+      for (int half = 0; half < 32; half += 16) {
+        uint32_t dhr[16], zr[16];
+        tmem_ld16_issue(t_row + T_R1 + c0 + half, dhr);
+        tmem_ld16_issue(t_row + T_R0 + c0 + half, zr);
+        tmem_wait16(dhr);
+        tmem_wait16(zr);
 #pragma unroll
-        for (int e = 0; e < 8; e += 2) {
-          float d[2];
+        for (int g = 0; g < 2; ++g) {
+          uint32_t pk[4];
+          float b[8];
+          load_f32x8(sb2 + c0 + half + 8 * g, b);
 #pragma unroll
-          for (int u = 0; u < 2; ++u) {
-            const int k = 8 * g + e + u;
-            const float zz = z[k] + sb2[c0 + k];
-            const float s = sigm(zz);
-            d[u] = dh[k] * (s * (1.0f + zz * (1.0f - s)));
+          for (int e = 0; e < 8; e += 2) {
+            const int k = 8 * g + e;
+            const float2 zz = __fadd2_rn(make_float2(__uint_as_float(zr[k]), __uint_as_float(zr[k + 1])),
+                                         make_float2(b[e], b[e + 1]));
+            const float2 d = __fmul2_rn(make_float2(__uint_as_float(dhr[k]), __uint_as_float(dhr[k + 1])),
+                                        silu_grad2(zz, sigm2(zz)));
+            pk[e / 2] = pack_bf16(d.x, d.y);
           }
-          pk[e / 2] = pack_bf16(d[0], d[1]);
+          *reinterpret_cast<uint4*>(base + F_DZ2 + tile_off(r, c0 + half + 8 * g)) =
+            make_uint4(pk[0], pk[1], pk[2], pk[3]);
         }
-        *reinterpret_cast<uint4*>(base + F_DZ2 + tile_off(r, c0 + 8 * g)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
       }
     }
     if (!tiles_ready()) break;
-    if (t == 0) {
+    if (issuer) {
       // dH1 = dZ2 W2 (its completion also covers the dW3 product issued
       // before it); then dW2 += dZ2^T H1 and the column sums of dZ3 and dZ2
       // (db3, db2) run on while dZ1 is formed
@@ -948,23 +1083,20 @@ __global__ void __launch_bounds__(F_THREADS, 1) k_fused(FusedArgs a)
 #pragma unroll
       for (int g = 0; g < 4; ++g) {
         uint32_t pk[4];
+        float b[8];
+        load_f32x8(sb1 + c0 + 8 * g, b);
 #pragma unroll
         for (int e = 0; e < 8; e += 2) {
-          float d[2];
-#pragma unroll
-          for (int u = 0; u < 2; ++u) {
-            const int k = 8 * g + e + u;
-            const float zz = z1_of(x, c0 + k);
-            const float s = sigm(zz);
-            d[u] = dh[k] * (s * (1.0f + zz * (1.0f - s)));
-          }
-          pk[e / 2] = pack_bf16(d[0], d[1]);
+          const int k = 8 * g + e;
+          const float2 zz = z1_of(xx, c0 + k, make_float2(b[e], b[e + 1]));
+          const float2 d = __fmul2_rn(make_float2(dh[k], dh[k + 1]), silu_grad2(zz, sigm2(zz)));
+          pk[e / 2] = pack_bf16(d.x, d.y);
         }
         *reinterpret_cast<uint4*>(base + F_H2 + tile_off(r, c0 + 8 * g)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
       }
     }
     if (!tiles_ready()) break;
-    if (t == 0) {
+    if (issuer) {
       // dW1 (columns 0-3) and db1 (column 4); the commit covers every
       // product of the tile
       issue_product(tmem + T_R1 + 64, big_tile(sbase + F_H2, true), x0_tile(sbase + F_X0), IN_PAD, false);
@@ -972,15 +1104,17 @@ __global__ void __launch_bounds__(F_THREADS, 1) k_fused(FusedArgs a)
     }
     wait_products();
     if (h == 0) {
-      float v[8];
-      tmem_ld8(t_row + T_R1, v);
-      acc_db3 += v[4];
-      tmem_ld8(t_row + T_R1 + 32, v);
-      acc_db2 += v[4];
-      tmem_ld8(t_row + T_R1 + 64, v);
+      uint32_t v[24];
+      tmem_ld8_issue(t_row + T_R1, v);
+      tmem_ld8_issue(t_row + T_R1 + 32, v + 8);
+      tmem_ld8_issue(t_row + T_R1 + 64, v + 16);
+      tmem_wait16(v);
+      tmem_wait8(v + 16);
+      acc_db3 += __uint_as_float(v[4]);
+      acc_db2 += __uint_as_float(v[12]);
 #pragma unroll
-      for (int i = 0; i < 4; ++i) acc_dw1[i] += v[i];
-      acc_db1 += v[4];
+      for (int i = 0; i < 4; ++i) acc_dw1[i] += __uint_as_float(v[16 + i]);
+      acc_db1 += __uint_as_float(v[20]);
     }
     first = false;
     // No barrier here: every product of the tile has completed, and the next
@@ -1013,7 +1147,7 @@ __global__ void __launch_bounds__(F_THREADS, 1) k_fused(FusedArgs a)
       for (int i = 0; i < 4; ++i) g1[i] = acc_dw1[i];
       g1[4] = acc_db1;
       float* gh = a.GH + static_cast<long long>(blockIdx.x) * 130;
-      gh[t] = acc_dw4;
+      gh[r] = acc_dw4;
       if (t == 0) {
         gh[128] = acc_db4;
         gh[129] = acc_loss;

@@ -81,6 +81,7 @@ struct DLattice {
 struct DMesh {
   double ll[3], width[3];
   float inv_width32[3];  // 1 / width rounded to FP32, for the FP32 index pre-test
+  float width32[3];      // width rounded to FP32 (the FP32-table mode track walk)
   int shape[3];
   int ndim;
 };

@@ -202,10 +202,7 @@ struct MeshDist {
   double distance;
 };
 
-// inv_u: 1/u per axis in FP32-table mode (products instead of quotients),
-// or null for the reference's divisions.
-__device__ __forceinline__ MeshDist mesh_dist(const DMesh& m, const int* ijk, int i, const double* r0, const double* u,
-  const double* inv_u)
+__device__ __forceinline__ MeshDist mesh_dist(const DMesh& m, const int* ijk, int i, const double* r0, const double* u)
 {
   MeshDist d;
   d.next_index = ijk[i];
@@ -217,29 +214,139 @@ __device__ __forceinline__ MeshDist mesh_dist(const DMesh& m, const int* ijk, in
   if (d.max_surface && (ijk[i] <= m.shape[i])) {
     d.next_index++;
     const double f = (m.ll[i] + fpi::to_double(ijk[i]) * m.width[i]) - r0[i];
-    d.distance = inv_u ? f * inv_u[i] : f / u[i];
+    d.distance = f / u[i];
   } else if (!d.max_surface && (ijk[i] >= 1)) {
     d.next_index--;
     const double f = (m.ll[i] + fpi::to_double(ijk[i] - 1) * m.width[i]) - r0[i];
-    d.distance = inv_u ? f * inv_u[i] : f / u[i];
+    d.distance = f / u[i];
   }
   return d;
 }
 
+// Index along one axis of the mesh cell that a point q widths from the mesh
+// corner lies in, the point moving in direction uk: within 1e-6 (relative)
+// of a face it counts as on the face and takes the cell ahead, which is what
+// the reference's TINY_BIT nudge along u decides; elsewhere ceil(q).
+__device__ __forceinline__ int mesh_cell_ahead(float q, float uk)
+{
+  q = fminf(fmaxf(q, -1.0e9f), 1.0e9f);
+  const float j = rintf(q);
+  if (fabsf(q - j) <= 1.0e-6f * fmaxf(1.0f, fabsf(q))) return static_cast<int>(j) + (uk > 0.0f ? 1 : 0);
+  return static_cast<int>(ceilf(q));
+}
+
+// FP32-table mode track walk: src/mesh.cpp:999-1146 raytrace_mesh with the
+// track's start taken relative to the mesh corner (one FP64 subtraction per
+// axis) and everything after that in FP32: start cell, face distances
+// (face - start) / u from the flight's reciprocal direction, segment
+// fractions of the advance distance.  Each start is within an FP32 rounding
+// of its distance from the corner (under 2e-5 cm for a 365 cm mesh), which
+// is all the track length a face can move between two cells; a start on a
+// face (a particle that has just crossed it) takes the cell ahead.  Tallies
+// stay FP64 sums of FP64 flux x FP32 fraction.  Calls f(bin, fraction).
+template<class F>
+__device__ void mesh_bins_crossed_f32(const DMesh& m, const double* r0, const double* u, const double* inv_u,
+  double track, F f)
+{
+  if (fpi::zero(track)) return;
+  const int n = m.ndim;
+  float t[3] = {0.0f, 0.0f, 0.0f}, uf[3] = {0.0f, 0.0f, 0.0f}, iu[3] = {0.0f, 0.0f, 0.0f};
+  bool par[3] = {true, true, true};  // |u| below FP_PRECISION: no face ahead
+  int ijk[3] = {0, 0, 0};
+  bool in_mesh = true;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    if (k >= n) break;
+    t[k] = fpi::to_float(r0[k] - m.ll[k]);
+    uf[k] = fpi::to_float(u[k]);
+    iu[k] = fpi::to_float(inv_u[k]);
+    par[k] = fpi::abs_lt(u[k], FP_PRECISION);
+    ijk[k] = mesh_cell_ahead(t[k] * m.inv_width32[k], uf[k]);
+    in_mesh = in_mesh && ijk[k] >= 1 && ijk[k] <= m.shape[k];
+  }
+  if (fpi::lt(track, 2 * TINY_BIT)) {
+    if (in_mesh) f(mesh_bin(m, ijk), 1.0);
+    return;
+  }
+  const float D = fpi::to_float(track), inv_D = 1.0f / D;
+  // distance from the start to the next face on axis k (INFINITY when
+  // parallel or leaving the mesh) and the index beyond it
+  float dist[3] = {INFINITY, INFINITY, INFINITY};
+  int next[3] = {0, 0, 0};
+  auto face = [&](int k) {
+    next[k] = ijk[k];
+    dist[k] = INFINITY;
+    if (par[k]) return;
+    if (uf[k] > 0.0f) {
+      if (ijk[k] <= m.shape[k]) {
+        next[k] = ijk[k] + 1;
+        dist[k] = (static_cast<float>(ijk[k]) * m.width32[k] - t[k]) * iu[k];
+      }
+    } else if (ijk[k] >= 1) {
+      next[k] = ijk[k] - 1;
+      dist[k] = (static_cast<float>(ijk[k] - 1) * m.width32[k] - t[k]) * iu[k];
+    }
+  };
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    if (k < n) face(k);
+  float traveled = 0.0f;
+  for (int guard = 0; guard < 1 << 24; ++guard) {
+    if (in_mesh) {
+      int k = 0;
+      float dk = dist[0];
+      if (dist[1] < dk) { k = 1; dk = dist[1]; }
+      if (dist[2] < dk) { k = 2; dk = dist[2]; }
+      const float seg = fminf(dk, D) - traveled;
+      f(mesh_bin(m, ijk), fpi::to_double(seg * inv_D));
+      traveled = dk;
+      if (D <= traveled) return;
+#pragma unroll
+      for (int kk = 0; kk < 3; ++kk) {
+        if (kk != k) continue;
+        ijk[kk] = next[kk];
+        face(kk);
+        in_mesh = ijk[kk] >= 1 && ijk[kk] <= m.shape[kk];
+      }
+    } else {
+      // outside: move to the farthest face ahead on the axes that are out
+      // of range; with none the track does not enter the mesh
+      int k_max = -1;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        if (k >= n) break;
+        if ((ijk[k] < 1 || ijk[k] > m.shape[k]) && dist[k] < INFINITY && dist[k] > traveled) {
+          traveled = dist[k];
+          k_max = k;
+        }
+      }
+      if (k_max == -1 || traveled >= D) return;
+      in_mesh = true;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        if (k >= n) break;
+        ijk[k] = mesh_cell_ahead((t[k] + traveled * uf[k]) * m.inv_width32[k], uf[k]);
+        in_mesh = in_mesh && ijk[k] >= 1 && ijk[k] <= m.shape[k];
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        if (k < n) face(k);
+    }
+  }
+}
+
 // src/mesh.cpp:999-1146 raytrace_mesh/bins_crossed; calls f(bin, fraction).
-// inv_u (FP32-table mode): reciprocal direction; the track length is then
-// taken as the advance distance itself and fractions use its reciprocal.
+// inv_u (FP32-table mode): the FP32 walk above, from the advance distance.
 template<class F>
 __device__ void mesh_bins_crossed(const DMesh& m, const double* r0, const double* r1, const double* u, F f,
   const double* inv_u = nullptr, double track = 0.0)
 {
-  double total_distance;
   if (inv_u) {
-    total_distance = track;
-  } else {
-    double dx = r1[0] - r0[0], dy = r1[1] - r0[1], dz = r1[2] - r0[2];
-    total_distance = sqrt(dx * dx + dy * dy + dz * dz);
+    mesh_bins_crossed_f32(m, r0, u, inv_u, track, f);
+    return;
   }
+  double dx = r1[0] - r0[0], dy = r1[1] - r0[1], dz = r1[2] - r0[2];
+  const double total_distance = sqrt(dx * dx + dy * dy + dz * dz);
   if (fpi::zero(total_distance)) return;
   const int n = m.ndim;
   bool in_mesh;
@@ -270,7 +377,6 @@ __device__ void mesh_bins_crossed(const DMesh& m, const double* r0, const double
       return;
     }
   }
-  const double inv_total = inv_u ? 1.0 / total_distance : 0.0;
   // the per-axis arrays are indexed by unrolled compile-time axes only, so
   // that they stay in registers
   MeshDist dist[3];
@@ -279,7 +385,7 @@ __device__ void mesh_bins_crossed(const DMesh& m, const double* r0, const double
   dist[0].max_surface = dist[1].max_surface = dist[2].max_surface = true;
 #pragma unroll
   for (int k = 0; k < 3; ++k)
-    if (k < n) dist[k] = mesh_dist(m, ijk, k, r0, u, inv_u);
+    if (k < n) dist[k] = mesh_dist(m, ijk, k, r0, u);
   for (int guard = 0; guard < 1 << 24; ++guard) {
     if (in_mesh) {
       int k = 0;
@@ -287,14 +393,14 @@ __device__ void mesh_bins_crossed(const DMesh& m, const double* r0, const double
       if (fpi::lt(dist[1].distance, dk)) { k = 1; dk = dist[1].distance; }
       if (fpi::lt(dist[2].distance, dk)) { k = 2; dk = dist[2].distance; }
       const double seg = fpi::min(dk, total_distance) - traveled;
-      f(mesh_bin(m, ijk), inv_u ? seg * inv_total : seg / total_distance);
+      f(mesh_bin(m, ijk), seg / total_distance);
       traveled = dk;
       if (fpi::le(total_distance, traveled)) return;
 #pragma unroll
       for (int kk = 0; kk < 3; ++kk) {
         if (kk != k) continue;
         ijk[kk] = dist[kk].next_index;
-        dist[kk] = mesh_dist(m, ijk, kk, r0, u, inv_u);
+        dist[kk] = mesh_dist(m, ijk, kk, r0, u);
         in_mesh = ((ijk[kk] >= 1) && (ijk[kk] <= m.shape[kk]));
       }
     } else {
@@ -313,7 +419,7 @@ __device__ void mesh_bins_crossed(const DMesh& m, const double* r0, const double
       mesh_get_indices(m, r0[0] + t * u[0], r0[1] + t * u[1], r0[2] + t * u[2], ijk, in_mesh);
 #pragma unroll
       for (int k = 0; k < 3; ++k)
-        if (k < n) dist[k] = mesh_dist(m, ijk, k, r0, u, inv_u);
+        if (k < n) dist[k] = mesh_dist(m, ijk, k, r0, u);
     }
   }
 }
@@ -1741,7 +1847,13 @@ __global__ void __launch_bounds__(256) k_score_tracks()
         inv_u[1] = T.iuy[i];
         inv_u[2] = T.iuz[i];
       }
-      const double r1[3] = {r0[0] + d * u[0], r0[1] + d * u[1], r0[2] + d * u[2]};
+      // the end point for the FP64 walk (the FP32 one walks from the distance)
+      double r1[3] = {0.0, 0.0, 0.0};
+      if (!recip) {
+        r1[0] = r0[0] + d * u[0];
+        r1[1] = r0[1] + d * u[1];
+        r1[2] = r0[2] + d * u[2];
+      }
       LevelCells lc;
       lc.n = 0;
 #pragma unroll
@@ -2336,6 +2448,7 @@ static void build_model(GpuSim& G, const HModel& m, const GpuOptions& opt)
       meshes[k].ll[j] = m.meshes[k].ll[j];
       meshes[k].width[j] = m.meshes[k].width[j];
       meshes[k].inv_width32[j] = m.meshes[k].width[j] > 0.0 ? static_cast<float>(1.0 / m.meshes[k].width[j]) : 0.0f;
+      meshes[k].width32[j] = static_cast<float>(m.meshes[k].width[j]);
       meshes[k].shape[j] = m.meshes[k].shape[j];
     }
     meshes[k].ndim = m.meshes[k].ndim;

@@ -240,7 +240,7 @@ __device__ __forceinline__ int mesh_cell_ahead(float q, float uk)
 // axis) and everything after that in FP32: start cell, face distances
 // (face - start) / u from the flight's reciprocal direction, segment
 // fractions of the advance distance.  Each start is within an FP32 rounding
-// of its distance from the corner (under 2e-5 cm for a 365 cm mesh), which
+// of its distance from the corner (under 1e-5 cm at 200 cm from it), which
 // is all the track length a face can move between two cells; a start on a
 // face (a particle that has just crossed it) takes the cell ahead.  Tallies
 // stay FP64 sums of FP64 flux x FP32 fraction.  Calls f(bin, fraction).

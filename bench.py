@@ -5,8 +5,9 @@ clad r=0.475 cm, 200 cm tall, reflective radial / vacuum axial boundaries;
 3 materials from 12 synthetic nuclides of 11,303 grid points; Maxwellian
 1.3 MeV source uniform in the pins; track-length flux on a 17x17x50 mesh x
 100 log-energy bins).  One step = one batch of 10^7 histories with FP32
-cross-section tables (FP64 geometry, energies, search keys and tally sums;
-the track-length tally's mesh walk in FP32).
+cross-section tables (FP64 geometry, stored energies and directions, search
+keys and tally sums; the elastic-scatter kinematics and the track-length
+tally's mesh walk in FP32).
 Seeded synthetic nuclides stand in for evaluated data (none exists here).
 
 Metric: particles/s = histories per batch / batch time (the reference's

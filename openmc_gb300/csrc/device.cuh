@@ -496,13 +496,9 @@ __device__ __forceinline__ double uniform_distribution(double a, double b, unsig
   return a + (b - a) * prn(s);
 }
 
-// src/math_functions.cpp:763-792 (phi sampled)
-// recip: divide by multiplying with the reciprocal (FP32-table mode; FP64
-// products rounded twice instead of FP64 quotients).  sin and cos of the
-// sampled angle come from one sincos call (the device's own functions in
-// either form).
-__device__ inline void rotate_angle(double& ux, double& uy, double& uz, double mu, unsigned long long& s,
-  bool recip = false)
+// src/math_functions.cpp:763-792 (phi sampled).  sin and cos of the sampled
+// angle come from one sincos call (the device's own functions).
+__device__ inline void rotate_angle(double& ux, double& uy, double& uz, double mu, unsigned long long& s)
 {
   double phi_ = 2.0 * PI * prn(s);
   double sinphi, cosphi;
@@ -513,14 +509,8 @@ __device__ inline void rotate_angle(double& ux, double& uy, double& uz, double m
   double b = sqrt(fpi::pos(vb) ? vb : 0.0);
   double x = ux, y = uy, z = uz;
   if (fpi::lt(1e-10, b)) {
-    if (recip) {
-      const double ib = 1.0 / b;
-      ux = mu * x + a * (x * z * cosphi - y * sinphi) * ib;
-      uy = mu * y + a * (y * z * cosphi + x * sinphi) * ib;
-    } else {
-      ux = mu * x + a * (x * z * cosphi - y * sinphi) / b;
-      uy = mu * y + a * (y * z * cosphi + x * sinphi) / b;
-    }
+    ux = mu * x + a * (x * z * cosphi - y * sinphi) / b;
+    uy = mu * y + a * (y * z * cosphi + x * sinphi) / b;
     uz = mu * z - a * b * cosphi;
   } else {
     b = sqrt(1. - y * y);
@@ -530,7 +520,8 @@ __device__ inline void rotate_angle(double& ux, double& uy, double& uz, double m
   }
 }
 
-// rotate_angle in FP32 (the free-gas target direction in FP32-table mode).  The
+// rotate_angle in FP32 (FP32-table mode: the free-gas target direction and the
+// centre-of-mass direction of an elastic scatter).  The
 // perpendicular norm b is sqrt(ux^2 + uy^2) (sqrt(ux^2 + uz^2) in the second
 // branch), which equals the reference's sqrt(1 - uz^2) for a unit vector
 // and keeps FP32 accuracy when uz is near +-1, where 1 - uz^2 cancels.

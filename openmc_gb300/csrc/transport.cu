@@ -1510,63 +1510,83 @@ __device__ void sample_cxs_target_velocity_f(float awr, float E, const float* u,
   vt_out[2] = vt * z;
 }
 
-// src/physics.cpp:754-818 elastic scattering with free-gas target.  In
-// FP32-table mode the target velocity (a random variate of the target
-// nucleus, sampled in FP32 by sample_cxs_target_velocity_f) enters the FP64
-// centre-of-mass transformation; the neutron's own energy and direction are
-// computed in FP64 throughout, with the quotients by (awr + 1) and by the
-// speeds written as products with FP64 reciprocals (rounded twice instead of
-// once).  FP64 tables keep the reference's expression.
+// Elastic scattering in FP32-table mode: src/physics.cpp:754-818 with the
+// same draws in the same order, the centre-of-mass transformation and the
+// rotation in FP32 (the target velocity is the FP32 variate of
+// sample_cxs_target_velocity_f; the cosine mu_cm the same FP64 uniform,
+// rounded).  The outgoing energy is the FP32 result; the outgoing direction,
+// |u|^2 = 1 + eps with |eps| of order 1e-7 after the conversion, is scaled in
+// FP64 by 1 - eps/2 + 3 eps^2 / 8 (the series of 1/sqrt(1 + eps), error of
+// order eps^3), so that it is a unit vector to FP64 rounding: the distance to
+// a z-cylinder takes 1 - uz^2 for ux^2 + uy^2.
+__device__ void elastic_scatter_f(int nuc, double& E, double* u, unsigned long long& seed)
+{
+  const double awr_d = dm.awr[nuc], kT_d = dm.kT[nuc];
+  const float awr = fpi::to_float(awr_d);
+  const float Ef = fpi::to_float(E);
+  const float uf[3] = {fpi::to_float(u[0]), fpi::to_float(u[1]), fpi::to_float(u[2])};
+  float vel = sqrtf(Ef);
+  float vn[3] = {vel * uf[0], vel * uf[1], vel * uf[2]};
+  float vt[3] = {0.0f, 0.0f, 0.0f};
+  if (!(fpi::le(400.0 * kT_d, E) && fpi::lt(1.0, awr_d)))
+    sample_cxs_target_velocity_f(awr, Ef, uf, fpi::to_float(kT_d), seed, vt);
+  const float iw = 1.0f / (awr + 1.0f);
+  float vcm[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    vcm[k] = (vn[k] + awr * vt[k]) * iw;
+    vn[k] = vn[k] - vcm[k];
+  }
+  vel = sqrtf(vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2]);
+  const float mu_cm = fpi::to_float(uniform_distribution(-1., 1., seed));
+  const float iv = 1.0f / vel;
+  float ucm[3] = {vn[0] * iv, vn[1] * iv, vn[2] * iv};
+  rotate_angle_f(ucm[0], ucm[1], ucm[2], mu_cm, seed);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) vn[k] = vel * ucm[k] + vcm[k];
+  const float E2 = vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2];
+  E = fpi::to_double(E2);
+  const float iv2 = 1.0f / sqrtf(E2);
+  double ud[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) ud[k] = fpi::to_double(vn[k] * iv2);
+  const double eps = (ud[0] * ud[0] + ud[1] * ud[1] + ud[2] * ud[2]) - 1.0;
+  const double f = 1.0 + eps * (-0.5 + 0.375 * eps);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) u[k] = ud[k] * f;
+}
+
+// src/physics.cpp:754-818 elastic scattering with free-gas target (FP64
+// tables: the reference's expressions; FP32 tables: elastic_scatter_f).
 __device__ void elastic_scatter(int nuc, double& E, double* u, unsigned long long& seed)
 {
+  if (dm.xs_fp32) {
+    elastic_scatter_f(nuc, E, u, seed);
+    return;
+  }
   double vel = sqrt(E);
   double awr = dm.awr[nuc];
   double kT = dm.kT[nuc];
   double vn[3] = {vel * u[0], vel * u[1], vel * u[2]};
   double vt[3] = {0.0, 0.0, 0.0};
-  const bool recip = dm.xs_fp32 != 0;
-  if (!(fpi::le(400.0 * kT, E) && fpi::lt(1.0, awr))) {
-    if (recip) {
-      const float uf[3] = {fpi::to_float(u[0]), fpi::to_float(u[1]), fpi::to_float(u[2])};
-      float vtf[3];
-      sample_cxs_target_velocity_f(fpi::to_float(awr), fpi::to_float(E), uf, fpi::to_float(kT), seed, vtf);
-      vt[0] = fpi::to_double(vtf[0]);
-      vt[1] = fpi::to_double(vtf[1]);
-      vt[2] = fpi::to_double(vtf[2]);
-    } else {
-      sample_cxs_target_velocity(awr, E, u, kT, seed, vt);
-    }
-  }
+  if (!(fpi::le(400.0 * kT, E) && fpi::lt(1.0, awr))) sample_cxs_target_velocity(awr, E, u, kT, seed, vt);
   double vcm[3];
-  if (recip) {
-    const double iw = 1.0 / (awr + 1.0);
-    for (int k = 0; k < 3; ++k) vcm[k] = (vn[k] + awr * vt[k]) * iw;
-  } else {
-    for (int k = 0; k < 3; ++k) vcm[k] = (vn[k] + awr * vt[k]) / (awr + 1.0);
-  }
+  for (int k = 0; k < 3; ++k) vcm[k] = (vn[k] + awr * vt[k]) / (awr + 1.0);
   for (int k = 0; k < 3; ++k) vn[k] = vn[k] - vcm[k];
   vel = sqrt(vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2]);
   double mu_cm = uniform_distribution(-1., 1., seed);
   double ucm[3];
-  if (recip) {
-    const double iv = 1.0 / vel;
-    ucm[0] = vn[0] * iv; ucm[1] = vn[1] * iv; ucm[2] = vn[2] * iv;
-  } else {
-    ucm[0] = vn[0] / vel; ucm[1] = vn[1] / vel; ucm[2] = vn[2] / vel;
-  }
-  rotate_angle(ucm[0], ucm[1], ucm[2], mu_cm, seed, recip);
+  ucm[0] = vn[0] / vel;
+  ucm[1] = vn[1] / vel;
+  ucm[2] = vn[2] / vel;
+  rotate_angle(ucm[0], ucm[1], ucm[2], mu_cm, seed);
   for (int k = 0; k < 3; ++k) vn[k] = vel * ucm[k];
   for (int k = 0; k < 3; ++k) vn[k] = vn[k] + vcm[k];
   E = vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2];
   vel = sqrt(E);
-  if (recip) {
-    const double iv = 1.0 / vel;
-    u[0] = vn[0] * iv; u[1] = vn[1] * iv; u[2] = vn[2] * iv;
-  } else {
-    u[0] = vn[0] / vel;
-    u[1] = vn[1] / vel;
-    u[2] = vn[2] / vel;
-  }
+  u[0] = vn[0] / vel;
+  u[1] = vn[1] / vel;
+  u[2] = vn[2] / vel;
 }
 
 // src/physics.cpp:1043-1115 sample_fission_neutron for a prompt-only MT 18

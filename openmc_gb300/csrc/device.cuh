@@ -635,8 +635,23 @@ __device__ inline double plane_distance(double r_i, double u_i, bool coincident,
   return fpi::zero(inv_u_i) ? f / u_i : f * inv_u_i;
 }
 
-// inv_a: 1 / (1 - u1^2) in FP32-table mode (products replace the quotients),
-// 0 for the reference's divisions.
+// Square root for FP32-table mode geometry: the FP32 root of q refined by one
+// Newton step in FP64, y0 + (q - y0^2) / (2 y0), with 1 / (2 y0) taken in
+// FP32 (the correction is of order 1e-7 y0, so its own FP32 error is of
+// order 1e-14 of the root; the step leaves a relative error of order 1e-14
+// against 1e-16 for the FP64 root, far inside the geometry's 1e-14 and 1e-8
+// cm tolerances), two FP64 operations in place of the FP64 square root.
+// Outside [1e-30, 1e30] (never for centimetre geometry) the FP64 root.
+__device__ __forceinline__ double sqrt_refined(double q)
+{
+  if (!(fpi::bits(q) >= fpi::bits(1e-30) && fpi::bits(q) <= fpi::bits(1e30))) return sqrt(q);
+  const float y0f = sqrtf(fpi::to_float(q));
+  const double y0 = fpi::to_double(y0f);
+  return fma(fma(-y0, y0, q), fpi::to_double(0.5f / y0f), y0);
+}
+
+// inv_a: 1 / (1 - u1^2) in FP32-table mode (products replace the quotients,
+// sqrt_refined the root), 0 for the reference's divisions and root.
 __device__ inline double cylinder_distance(double u1, double r2_, double u2, double r3_, double u3,
   bool coincident, double offset1, double offset2, double radius, double inv_a = 0.0)
 {
@@ -652,11 +667,11 @@ __device__ inline double cylinder_distance(double u1, double r2_, double u2, dou
     return INFTY;
   } else if (coincident || fpi::abs_lt(c, FP_COINCIDENT)) {
     if (fpi::nonneg(k)) return INFTY;
-    return prod ? (-k + sqrt(quad)) * inv_a : (-k + sqrt(quad)) / a;
+    return prod ? (-k + sqrt_refined(quad)) * inv_a : (-k + sqrt(quad)) / a;
   } else if (fpi::neg(c)) {
-    return prod ? (-k + sqrt(quad)) * inv_a : (-k + sqrt(quad)) / a;
+    return prod ? (-k + sqrt_refined(quad)) * inv_a : (-k + sqrt(quad)) / a;
   } else {
-    const double d = prod ? (-k - sqrt(quad)) * inv_a : (-k - sqrt(quad)) / a;
+    const double d = prod ? (-k - sqrt_refined(quad)) * inv_a : (-k - sqrt(quad)) / a;
     if (fpi::neg(d)) return INFTY;
     return d;
   }

@@ -182,16 +182,16 @@ def peaks():
 # scales with the events a launch processes.  The track-length tally kernel
 # reads the 96-byte track records, traffic of this design beyond its 16
 # algorithmic bytes per mesh segment.
-TRAFFIC_PER_ALGORITHMIC_BYTE = {"xs+advance+surface": 1.055, "xs+advance": 1.376, "surface": 1.406,
-                                "collision": 1.273, "tally": 6.275}
+TRAFFIC_PER_ALGORITHMIC_BYTE = {"xs+advance+surface": 1.033, "xs+advance": 1.376, "surface": 1.406,
+                                "collision": 1.269, "tally": 6.27}
 
 # What bounds the transport kernels instead of HBM: the FP64 pipe's busy
 # fraction in the same captures (a committed profile, not measured by this run).
 _CAPTURE = "ncu --set full, iteration 100 of a 2e6-history lattice batch, 524,288 slots"
 FP64_PIPE_NOTE = {
-    "xs+advance+surface": {"fp64_pipe_busy": 0.586, "dram_busy": 0.149, "source": _CAPTURE},
-    "collision": {"fp64_pipe_busy": 0.578, "dram_busy": 0.050, "source": _CAPTURE},
-    "tally": {"fp64_pipe_busy": 0.691, "dram_busy": 0.072, "source": _CAPTURE},
+    "xs+advance+surface": {"fp64_pipe_busy": 0.579, "dram_busy": 0.146, "source": _CAPTURE},
+    "collision": {"fp64_pipe_busy": 0.334, "dram_busy": 0.078, "source": _CAPTURE},
+    "tally": {"fp64_pipe_busy": 0.470, "dram_busy": 0.094, "source": _CAPTURE},
 }
 
 

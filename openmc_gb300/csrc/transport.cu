@@ -1787,7 +1787,7 @@ __device__ __forceinline__ void flush_stats(const EvStats& st, int set)
 #define OMC_MINB_SURF 2
 #endif
 #ifndef OMC_MINB_COLL
-#define OMC_MINB_COLL 3
+#define OMC_MINB_COLL 2
 #endif
 // All kernels of an iteration leave at once while the loop is in its tail
 // phase (dq.cnt->tail), where k_tail runs the remaining histories instead.

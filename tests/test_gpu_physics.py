@@ -82,3 +82,69 @@ def test_elastic_energy_transfer_law(built, tmp_path, fp32):
     # uniform on [alpha, 1]: each tenth of the interval holds a tenth of the ratios
     hist, _ = np.histogram(q, bins=10, range=(alpha, 1.0))
     assert np.all(np.abs(hist / n - 0.1) < 5.0 * np.sqrt(0.09 / n)), hist / n
+
+
+def inner_box_model(directory):
+    """A 20 cm box around an inner 10 cm box cell, a 7x5x3 mesh over the
+    inner box only, and a point source at the centre: tracks leave the mesh,
+    re-enter it from outside and start on its faces."""
+    from openmc_gb300 import configs, data
+    from openmc_gb300 import model as om
+    _, xs_xml = configs._library(directory, [("H1", 1), ("O16", 16), ("Fe56", 56)], 600, 5)
+    mat = om.Material(name="mixture")
+    for name, f in (("H1", 0.5), ("O16", 0.3), ("Fe56", 0.2)):
+        mat.add_nuclide(name, f)
+    mat.set_density("atom/b-cm", 0.03)
+    mats = om.Materials([mat], cross_sections=xs_xml.name)
+    outer = [om.XPlane(-10.0, boundary_type="reflective"), om.XPlane(10.0, boundary_type="vacuum"),
+             om.YPlane(-10.0, boundary_type="vacuum"), om.YPlane(10.0, boundary_type="reflective"),
+             om.ZPlane(-10.0, boundary_type="vacuum"), om.ZPlane(10.0, boundary_type="vacuum")]
+    inner = [om.XPlane(-5.0), om.XPlane(5.0), om.YPlane(-5.0), om.YPlane(5.0), om.ZPlane(-5.0), om.ZPlane(5.0)]
+    big = +outer[0] & -outer[1] & +outer[2] & -outer[3] & +outer[4] & -outer[5]
+    small = +inner[0] & -inner[1] & +inner[2] & -inner[3] & +inner[4] & -inner[5]
+    c_in = om.Cell(fill=mat, region=small)
+    c_out = om.Cell(fill=mat, region=big & ~small)
+    geom = om.Geometry(om.Universe(cells=[c_in, c_out]))
+    settings = om.Settings(particles=20000, batches=2, event_based=True, seed=9)
+    settings.source = [om.IndependentSource(space=om.Point((0.0, 0.0, 0.0)), angle=om.Isotropic(),
+                                            energy=om.Discrete([2.0e6], [1.0]))]
+    mesh = om.RegularMesh()
+    mesh.dimension = [7, 5, 3]
+    mesh.lower_left = [-5.0, -5.0, -5.0]
+    mesh.upper_right = [5.0, 5.0, 5.0]
+    tm = om.Tally(name="mesh flux")
+    tm.filters = [om.MeshFilter(mesh)]
+    tm.scores = ["flux"]
+    tc = om.Tally(name="inner cell flux")
+    tc.filters = [om.CellFilter([c_in])]
+    tc.scores = ["flux"]
+    tc.estimator = "tracklength"
+    m = om.Model(geom, mats, settings, om.Tallies([tm, tc]))
+    m.export_to_model_xml(directory / "model.xml")
+    return m
+
+
+@pytest.mark.parametrize("fp32", [False, True], ids=["fp64", "fp32"])
+def test_mesh_walk_conserves_track_length(built, tmp_path, fp32):
+    """Over a mesh that covers exactly one cell, the mesh bins' track-length
+    flux sums to that cell's track-length flux in the same run (the walk of
+    src/mesh.cpp:999-1146 splits each track without losing length): to FP64
+    rounding with FP64 tables, to the FP32 walk's rounding with FP32 tables
+    (its faces are exact in FP32 here, so only the fractions round)."""
+    from openmc_gb300 import lib
+    inner_box_model(tmp_path)
+    lib.init(directory=tmp_path)
+    try:
+        lib.settings.xs_fp32 = 1 if fp32 else 0
+        lib.simulation_init()
+        status = 0
+        while status == 0:
+            status = lib.next_batch()
+        lib.simulation_finalize()
+        ids = lib.tally_ids()
+        mesh_sum = lib.tally_results(ids[0])[..., 1].sum()
+        cell = lib.tally_results(ids[1])[..., 1].sum()
+    finally:
+        lib.finalize()
+    assert cell > 0
+    assert abs(mesh_sum - cell) <= (1e-6 if fp32 else 1e-11) * cell, (mesh_sum, cell)

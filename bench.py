@@ -175,23 +175,24 @@ def peaks():
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic
 # byte of each kernel, from an ncu capture of one launch of the same kernel
-# (iteration 100 of a 2x10^6-history lattice batch, 524,288 slots; particle
-# bank packed into per-slot records), matched with that launch's
-# OPENMC_GB300_LAUNCH_LOG counts; the unfused kernels' ratios come from a
+# (iteration 20 of the 10^7-history lattice batch at the default 2,097,152
+# slots, whose bank outgrows the L2; particle bank packed into per-slot
+# records), matched with that launch's OPENMC_GB300_LAUNCH_LOG counts; the
+# unfused kernels' ratios come from a
 # capture of the unfused kernels of the unpacked bank.  Traffic per launch
 # scales with the events a launch processes.  The track-length tally kernel
 # reads the 96-byte track records, traffic of this design beyond its 16
 # algorithmic bytes per mesh segment.
-TRAFFIC_PER_ALGORITHMIC_BYTE = {"xs+advance+surface": 1.033, "xs+advance": 1.376, "surface": 1.406,
-                                "collision": 1.269, "tally": 6.27}
+TRAFFIC_PER_ALGORITHMIC_BYTE = {"xs+advance+surface": 1.846, "xs+advance": 1.376, "surface": 1.406,
+                                "collision": 2.165, "tally": 5.69}
 
 # What bounds the transport kernels instead of HBM: the FP64 pipe's busy
 # fraction in the same captures (a committed profile, not measured by this run).
-_CAPTURE = "ncu --set full, iteration 100 of a 2e6-history lattice batch, 524,288 slots"
+_CAPTURE = "ncu --metrics, iteration 20 of the 1e7-history lattice batch, 2,097,152 slots"
 FP64_PIPE_NOTE = {
-    "xs+advance+surface": {"fp64_pipe_busy": 0.579, "dram_busy": 0.146, "source": _CAPTURE},
-    "collision": {"fp64_pipe_busy": 0.334, "dram_busy": 0.078, "source": _CAPTURE},
-    "tally": {"fp64_pipe_busy": 0.470, "dram_busy": 0.094, "source": _CAPTURE},
+    "xs+advance+surface": {"fp64_pipe_busy": 0.555, "dram_busy": 0.261, "source": _CAPTURE},
+    "collision": {"fp64_pipe_busy": 0.490, "dram_busy": 0.211, "source": _CAPTURE},
+    "tally": {"fp64_pipe_busy": 0.590, "dram_busy": 0.111, "source": _CAPTURE},
 }
 
 

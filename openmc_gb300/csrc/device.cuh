@@ -351,6 +351,7 @@ struct DQueues {
   int trace_batch;  // batch whose histories are traced
   int batch;
   int sort_keys;
+  int sort_sub_bits;  // sub-octave bits of the sort key (0 or 1)
 };
 
 // Defined here: this header is included by exactly one translation unit.

@@ -2043,7 +2043,11 @@ __device__ __forceinline__ int sort_key(int s)
   long long bits = __double_as_longlong(db.E[s]);
   int ex = static_cast<int>((bits >> 52) & 0x7ff) - 1023 + 32;
   ex = ex < 0 ? 0 : (ex > 63 ? 63 : ex);
-  return mat * 64 + ex;
+  // sub-octave: the leading mantissa bits (the energy's position within its
+  // octave) when the key count allows
+  const int sb = dq.sort_sub_bits;
+  const int sub = static_cast<int>((bits >> (52 - sb)) & ((1LL << sb) - 1));
+  return (((mat * 64 + ex) << sb) | sub);
 }
 
 constexpr int SORT_MAX_KEYS = 2048;
@@ -2625,7 +2629,10 @@ static void build_bank(GpuSim& G, long long cap, long long sec_cap)
   q.q_tmp = dev_alloc<int>(cap, own);
   q.key_tmp = nullptr;
   q.free_list = dev_alloc<int>(cap, own);
-  q.sort_keys = (G.model.n_mat + 1) * 64;
+  // (material, energy octave) keys, with 1 sub-octave bit when they fit
+  // the shared-memory histogram
+  q.sort_sub_bits = (G.model.n_mat + 1) * 64 * 2 <= SORT_MAX_KEYS ? 1 : 0;
+  q.sort_keys = (G.model.n_mat + 1) * 64 << q.sort_sub_bits;
   if (q.sort_keys > SORT_MAX_KEYS) G.sort = 0;
   if (G.sort) q.key_tmp = dev_alloc<int>(cap, own);
   q.hist = dev_alloc<int>(q.sort_keys, own);

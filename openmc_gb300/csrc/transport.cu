@@ -2033,7 +2033,8 @@ __global__ void __launch_bounds__(256) k_refill()
   }
 }
 
-// Counting sort of the next cross-section queue by (material, energy octave):
+// Counting sort of the next cross-section queue by (material, energy octave,
+// and the half of the octave when the keys fit the histogram):
 // each block histograms a contiguous chunk in shared memory, one global
 // atomic per (block, key) reserves its output range, and the block scatters
 // its chunk into that range.

@@ -1786,6 +1786,9 @@ __device__ __forceinline__ void flush_stats(const EvStats& st, int set)
 #ifndef OMC_MINB_SURF
 #define OMC_MINB_SURF 2
 #endif
+#ifndef OMC_ADV_BLOCKS_PER_SM
+#define OMC_ADV_BLOCKS_PER_SM 32
+#endif
 #ifndef OMC_MINB_COLL
 #define OMC_MINB_COLL 2
 #endif
@@ -2244,6 +2247,8 @@ struct GpuSim {
   cudaGraph_t graph = nullptr;
   int blocks = 1216;
   int blocks_coll = 1216;  // grid of the collision kernel
+  int blocks_adv = 4864;   // grid of the advance kernel
+  int blocks_trk = 608;    // grid of the track-length scoring kernel
   int sort = 1;
   int fuse = 3;  // bit 0: cross-section event, bit 1: surface crossing, inside the advance kernel
   int split_slots = 0;  // split particles start in free slots with their own seeds
@@ -2720,7 +2725,7 @@ static void upload_constants(GpuSim& G)
 // record is written.
 static void launch_advance(const GpuSim& G, cudaStream_t S)
 {
-  const int nb = G.blocks, nt = 256;
+  const int nb = G.blocks_adv, nt = 256;
   if (!G.defer && G.model.n_tally_tracklength > 0) k_advance<true, true, false><<<nb, nt, G.smem, S>>>();
   else if (G.fuse == 3 && !G.model.track_time) k_advance<true, true, true, false><<<nb, nt, G.smem, S>>>();
   else if (G.fuse == 3) k_advance<true, true, true><<<nb, nt, G.smem, S>>>();
@@ -2764,7 +2769,7 @@ static void build_graph(GpuSim& G)
   CK(cudaStreamBeginCaptureToGraph(G.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
   if (!(G.fuse & 1)) k_xs<<<nb, nt, G.smem, G.stream>>>();
   launch_advance(G, G.stream);
-  if (G.defer) k_score_tracks<<<nb, nt, 0, G.stream>>>();
+  if (G.defer) k_score_tracks<<<G.blocks_trk, nt, 0, G.stream>>>();
   if (!(G.fuse & 2)) k_surface<<<nb, nt, G.smem, G.stream>>>();
   k_collision<<<G.blocks_coll, nt, G.smem, G.stream>>>();
   k_tail<<<nb * 2, 128, G.smem, G.stream>>>(G.tail_max_events);
@@ -2799,8 +2804,14 @@ GpuSim* gpu_create(const HModel& m, const GpuOptions& opt)
     G->split_slots = (!G->history && opt.split_slots && (m.ww_on || !m.weight_windows.empty())) ? 1 : 0;
     int sms = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
+    // grids (256 threads, grid-stride loops) measured on the 17x17 lattice
+    // at 2^21 slots: the advance kernel 325 ms per batch with 8 blocks per
+    // SM, 305 with 16, 298 with 32, 311 with 64 or 128; the scoring kernel
+    // 59.5 with 8, 57.1 with 4
     G->blocks = sms * 8;
     G->blocks_coll = sms * 8;
+    G->blocks_adv = sms * OMC_ADV_BLOCKS_PER_SM;
+    G->blocks_trk = sms * 4;
     build_model(*G, m, opt);
     G->defer = (!G->history && opt.defer_tally && G->model.n_tally_tracklength > 0) ? 1 : 0;
     if (!G->history && !opt.defer_tally && G->model.n_tally_tracklength > 0 && G->fuse != 3)
@@ -2971,7 +2982,7 @@ BatchStats gpu_run_batch_profiled(GpuSim* G, HModel& m, int batch, bool accumula
     CK(cudaEventRecord(ev[3], S));
     launch_advance(*G, S);
     CK(cudaEventRecord(ev[12], S));
-    if (G->defer) k_score_tracks<<<nb, nt, 0, S>>>();
+    if (G->defer) k_score_tracks<<<G->blocks_trk, nt, 0, S>>>();
     CK(cudaEventRecord(ev[4], S));
     if (!(G->fuse & 2)) k_surface<<<nb, nt, G->smem, S>>>();
     CK(cudaEventRecord(ev[5], S));

@@ -183,16 +183,16 @@ def peaks():
 # scales with the events a launch processes.  The track-length tally kernel
 # reads the 96-byte track records, traffic of this design beyond its 16
 # algorithmic bytes per mesh segment.
-TRAFFIC_PER_ALGORITHMIC_BYTE = {"xs+advance+surface": 1.846, "xs+advance": 1.376, "surface": 1.406,
-                                "collision": 2.165, "tally": 5.69}
+TRAFFIC_PER_ALGORITHMIC_BYTE = {"xs+advance+surface": 1.822, "xs+advance": 1.376, "surface": 1.406,
+                                "collision": 2.159, "tally": 5.71}
 
 # What bounds the transport kernels instead of HBM: the FP64 pipe's busy
 # fraction in the same captures (a committed profile, not measured by this run).
 _CAPTURE = "ncu --metrics, iteration 20 of the 1e7-history lattice batch, 2,097,152 slots"
 FP64_PIPE_NOTE = {
-    "xs+advance+surface": {"fp64_pipe_busy": 0.555, "dram_busy": 0.261, "source": _CAPTURE},
-    "collision": {"fp64_pipe_busy": 0.490, "dram_busy": 0.211, "source": _CAPTURE},
-    "tally": {"fp64_pipe_busy": 0.590, "dram_busy": 0.111, "source": _CAPTURE},
+    "xs+advance+surface": {"fp64_pipe_busy": 0.599, "dram_busy": 0.287, "source": _CAPTURE},
+    "collision": {"fp64_pipe_busy": 0.510, "dram_busy": 0.218, "source": _CAPTURE},
+    "tally": {"fp64_pipe_busy": 0.619, "dram_busy": 0.116, "source": _CAPTURE},
 }
 
 

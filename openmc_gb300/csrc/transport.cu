@@ -2248,7 +2248,7 @@ struct GpuSim {
   int blocks = 1216;
   int blocks_coll = 1216;  // grid of the collision kernel
   int blocks_adv = 4864;   // grid of the advance kernel
-  int blocks_trk = 608;    // grid of the track-length scoring kernel
+  int blocks_trk = 304;    // grid of the track-length scoring kernel
   int sort = 1;
   int fuse = 3;  // bit 0: cross-section event, bit 1: surface crossing, inside the advance kernel
   int split_slots = 0;  // split particles start in free slots with their own seeds
@@ -2807,11 +2807,11 @@ GpuSim* gpu_create(const HModel& m, const GpuOptions& opt)
     // grids (256 threads, grid-stride loops) measured on the 17x17 lattice
     // at 2^21 slots: the advance kernel 325 ms per batch with 8 blocks per
     // SM, 305 with 16, 298 with 32, 311 with 64 or 128; the scoring kernel
-    // 59.5 with 8, 57.1 with 4
+    // 59.5 with 8, 57.3 with 4, 55.8 with 2 (its resident count)
     G->blocks = sms * 8;
     G->blocks_coll = sms * 8;
     G->blocks_adv = sms * OMC_ADV_BLOCKS_PER_SM;
-    G->blocks_trk = sms * 4;
+    G->blocks_trk = sms * 2;
     build_model(*G, m, opt);
     G->defer = (!G->history && opt.defer_tally && G->model.n_tally_tracklength > 0) ? 1 : 0;
     if (!G->history && !opt.defer_tally && G->model.n_tally_tracklength > 0 && G->fuse != 3)

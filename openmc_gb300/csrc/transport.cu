@@ -773,9 +773,30 @@ __device__ bool satisfies_spatial_constraints(double x, double y, double z)
   return false;
 }
 
+// Unit direction from FP32 components, scaled in FP64 by the series
+// 1 - eps/2 + 3 eps^2 / 8 of 1/sqrt(|u|^2), |u|^2 = 1 + eps (|eps| of order
+// 1e-7), so that it is a unit vector to FP64 rounding.
+__device__ __forceinline__ void unit_from_f32(const float* v, double* u)
+{
+  double d[3] = {fpi::to_double(v[0]), fpi::to_double(v[1]), fpi::to_double(v[2])};
+  const double eps = (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) - 1.0;
+  const double f = 1.0 + eps * (-0.5 + 0.375 * eps);
+  u[0] = d[0] * f;
+  u[1] = d[1] * f;
+  u[2] = d[2] * f;
+}
+
 __device__ double sample_energy(unsigned long long& seed)
 {
-  if (dm.en_type == 1) return maxwell_spectrum(dm.en_x[0], seed);
+  if (dm.en_type == 1) {
+    if (dm.xs_fp32) {
+      // FP32-table mode: src/random_dist.cpp:20-32 with the same three draws
+      const float r1 = prn_f(seed), r2 = prn_f(seed), r3 = prn_f(seed);
+      const float c = cospif(0.5f * r3);
+      return fpi::to_double(-fpi::to_float(dm.en_x[0]) * (logf(r1) + logf(r2) * c * c));
+    }
+    return maxwell_spectrum(dm.en_x[0], seed);
+  }
   int n = dm.n_en;
   if (n <= 1) return dm.en_x[0];
   // src/distribution.cpp:87-101 alias sampling
@@ -814,7 +835,16 @@ __device__ void sample_source_site(long long index_source, SourceSite& site)
       break;
     }
   }
-  if (dm.an_type == 0) {
+  if (dm.an_type == 0 && dm.xs_fp32) {
+    // FP32-table mode: the same two draws, the direction in FP32
+    const float t = prn_f(seed);
+    const float mu = 2.0f * prn_f(seed) - 1.0f;
+    float sp, cp;
+    sincospif(2.0f * t, &sp, &cp);
+    const float st = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
+    const float v[3] = {mu, st * cp, st * sp};
+    unit_from_f32(v, u);
+  } else if (dm.an_type == 0) {
     // src/distribution_multi.cpp:106-112
     double phi = uniform_distribution(0., 2.0 * PI, seed);
     double mu = uniform_distribution(-1., 1., seed);

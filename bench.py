@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--particles", type=int, default=10_000_000)
     ap.add_argument("--in-flight", type=int, default=0,
-                    help="particle slots held on the device (0: the library's default, 2^21)")
+                    help="particle slots held on the device (0: the library's default, 3 x 2^20)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-table extra measurement")
     ap.add_argument("--fp64-batches", type=int, default=20,
                     help="batches of the FP64-table run whose tally the FP32 tally is compared with")

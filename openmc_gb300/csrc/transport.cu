@@ -2846,12 +2846,13 @@ GpuSim* gpu_create(const HModel& m, const GpuOptions& opt)
     G->defer = (!G->history && opt.defer_tally && G->model.n_tally_tracklength > 0) ? 1 : 0;
     if (!G->history && !opt.defer_tally && G->model.n_tally_tracklength > 0 && G->fuse != 3)
       throw std::runtime_error("track-length tallies scored inside the advance need the fused advance (fuse 3)");
-    // 2^21 slots by default: on the 17x17 lattice (10^7 histories per batch)
-    // a batch took 521 ms with 2^19 slots, 492 with 2^20, 487 with 2^21 and
-    // 483 with 3 x 2^20 (the iterations' fixed costs are shared by more
-    // events; the packed bank keeps the larger working set's traffic at its
-    // algorithmic bytes)
-    long long cap = opt.in_flight > 0 ? opt.in_flight : 1 << 21;
+    // 3 x 2^20 slots by default: on the 17x17 lattice (10^7 histories per
+    // batch) a batch took 521 ms with 2^19 slots, 492 with 2^20, 487 with
+    // 2^21 and 483 with 3 x 2^20 (8 blocks per SM for every kernel), and 449
+    // with 2^21 against 441 with 3 x 2^20 at the final grids: each
+    // iteration's fixed costs are shared by more events, while the FP64
+    // pipe, not the bank's DRAM traffic, bounds the advance kernel
+    long long cap = opt.in_flight > 0 ? opt.in_flight : 3LL << 20;
     if (cap > m.n_particles) cap = m.n_particles;
     if (cap < 1) cap = 1;
     long long sec_cap = opt.secondary_cap;

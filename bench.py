@@ -175,7 +175,7 @@ def peaks():
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic
 # byte of each kernel, from an ncu capture of one launch of the same kernel
-# (iteration 20 of the 10^7-history lattice batch at the default 2,097,152
+# (iteration 20 of the 10^7-history lattice batch at the default 3,145,728
 # slots, whose bank outgrows the L2; particle bank packed into per-slot
 # records), matched with that launch's OPENMC_GB300_LAUNCH_LOG counts; the
 # unfused kernels' ratios come from a
@@ -183,16 +183,16 @@ def peaks():
 # scales with the events a launch processes.  The track-length tally kernel
 # reads the 96-byte track records, traffic of this design beyond its 16
 # algorithmic bytes per mesh segment.
-TRAFFIC_PER_ALGORITHMIC_BYTE = {"xs+advance+surface": 1.822, "xs+advance": 1.376, "surface": 1.406,
-                                "collision": 2.159, "tally": 5.71}
+TRAFFIC_PER_ALGORITHMIC_BYTE = {"xs+advance+surface": 1.934, "xs+advance": 1.376, "surface": 1.406,
+                                "collision": 2.736, "tally": 5.66}
 
 # What bounds the transport kernels instead of HBM: the FP64 pipe's busy
 # fraction in the same captures (a committed profile, not measured by this run).
-_CAPTURE = "ncu --metrics, iteration 20 of the 1e7-history lattice batch, 2,097,152 slots"
+_CAPTURE = "ncu --metrics, iteration 20 of the 1e7-history lattice batch, 3,145,728 slots"
 FP64_PIPE_NOTE = {
-    "xs+advance+surface": {"fp64_pipe_busy": 0.599, "dram_busy": 0.287, "source": _CAPTURE},
-    "collision": {"fp64_pipe_busy": 0.510, "dram_busy": 0.218, "source": _CAPTURE},
-    "tally": {"fp64_pipe_busy": 0.619, "dram_busy": 0.116, "source": _CAPTURE},
+    "xs+advance+surface": {"fp64_pipe_busy": 0.598, "dram_busy": 0.303, "source": _CAPTURE},
+    "collision": {"fp64_pipe_busy": 0.524, "dram_busy": 0.288, "source": _CAPTURE},
+    "tally": {"fp64_pipe_busy": 0.651, "dram_busy": 0.122, "source": _CAPTURE},
 }
 
 
